@@ -1,0 +1,405 @@
+"""Benchmark of the FE operator hot path on GB300.
+
+Workload (default): P1 variable-coefficient diffusion operator div(kappa grad u)
+on a 64^3-cell Kuhn cube (1,572,864 tets, 274,625 nodes, 4,018,753 CSR
+entries), interior nodes jittered by +-0.2h, elements randomly permuted (seed 1),
+kappa lognormal (sigma 1), 4-point quadrature.  One step = FP64 assembly of the
+operator from device-resident inputs + 100 FP64 CSR SpMVs on a random vector in
+[-1, 1].  `value` = tets pushed through that step per second (tets / step time),
+summed over replicas.  L2 is flushed (a 256 MB write) before every step.
+
+Also reported (measured after the timed steps, same data): FP32 assembly and
+SpMV, each kernel's achieved GB/s against the measured HBM peak, the FP64-PCG
+vs FP32-refined-CG time to a 1e-10 relative residual on the same operator with
+Dirichlet u = 0 and f = 1, the end-to-end number through the C ABI with host
+buffers, and the oracle (a restatement of the reference algorithm) timed on one
+host core as the CPU baseline.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--n 64]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "tets assembled/s + SpMV GB/s vs HBM peak; FP32-refined vs FP64 CG time to 1e-10"
+N_SPMV = 100
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=64, help="cells per cube edge")
+    ap.add_argument("--jitter", type=float, default=0.2)
+    ap.add_argument("--sigma", type=float, default=1.0)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--no-cg", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def workload_config(a, E, N, nnz):
+    return {"workload": f"P1 kappa-diffusion operator, {a.n}^3 cells x 6 tets ({E} tets, {N} nodes, {nnz} CSR entries), "
+                        f"jitter +-{a.jitter}h, element permutation seed {a.seed}, lognormal kappa sigma {a.sigma}, "
+                        f"4-point rule; step = FP64 assembly + {N_SPMV} FP64 SpMV",
+            "n_cells": a.n, "tets": E, "nodes": N, "nnz": nnz, "quadrature": 4,
+            "l2": "flushed before every step (256 MB write)", "parallelism": f"replicas x{a.gpus}"}
+
+
+def asm_bytes(E, nv, nnz, sv, nb=4):
+    """algorithmic bytes of one assembly: E (16 conn + 8 kappa + 4 nb^2 slot map) + 24 n_v + s_v nnz"""
+    return E * (16 + 8 + 4 * nb * nb) + 24 * nv + sv * nnz
+
+
+def spmv_bytes(ndof, nnz, sv):
+    """nnz (s_v + 4) + 4 (ndof + 1) + 2 s_v ndof"""
+    return nnz * (sv + 4) + 4 * (ndof + 1) + 2 * sv * ndof
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.out = None
+
+    def __enter__(self):
+        try:
+            self.out = open(os.path.join("/tmp", f"mg_clocks_{os.getpid()}.csv"), "w+")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.out, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or self.out is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.out.flush()
+        self.out.seek(0)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.out.read().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------- reference --
+def _ref_worker(args):
+    """One host process = one 'MPI rank' of the reference algorithm: assembles
+    its slab of elements into CSR (pattern + values, insertion order sums) and
+    applies the result 100 times.  Runs the oracle (CPU restatement)."""
+    n, jitter, seed, sigma, rank, nranks, steps = args
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+    import oracle as orc
+    from morganapublic_gb300 import meshgen
+    m = meshgen.kuhn_cube(n, jitter=jitter, seed=seed, permute=True)
+    kappa = meshgen.lognormal(len(m.conn), sigma, seed)
+    E = len(m.conn)
+    lo, hi = rank * E // nranks, (rank + 1) * E // nranks
+    conn = np.ascontiguousarray(m.conn[lo:hi])
+    kap = np.ascontiguousarray(kappa[lo:hi])
+    x = np.random.default_rng(seed).uniform(-1, 1, len(m.xyz))
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        dofs = orc.elem_dofs(1, len(m.xyz), conn)
+        rp, ci = orc.pattern(1, len(m.xyz), dofs)
+        vals = orc.assemble("stiff_kappa", 1, 4, m.xyz, conn, dofs, rp, ci, kap)
+        for _ in range(N_SPMV):
+            y = orc.spmv(rp, ci, vals, x)
+        times.append(time.perf_counter() - t0)
+    return times, hi - lo
+
+
+def run_reference(a):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    import multiprocessing as mp
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+    orc.build()
+    nproc = os.cpu_count() or 1
+    steps = a.warmup + a.steps
+    # bounded sample: the full mesh split over all host cores, few steps
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(nproc) as pool:
+        res = pool.map(_ref_worker, [(a.n, a.jitter, a.seed, a.sigma, r, nproc, steps) for r in range(nproc)])
+    per_step = [max(r[0][s] for r in res) for s in range(a.warmup, steps)]
+    E = sum(r[1] for r in res)
+    t = statistics.mean(per_step)
+    val = E / t
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "tets/s", "n_gpus": a.gpus,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"P1 kappa-diffusion operator, {a.n}^3 cells x 6 tets, step = FP64 assembly "
+                                   f"(pattern + values) + {N_SPMV} SpMV, elements split over {nproc} host processes",
+                       "n_cells": a.n, "tets": E},
+            "cpu_baseline": {"value": val, "unit": "tets/s", "cores": nproc, "kind": "port",
+                             "sample": f"full {a.n}^3 mesh, {a.steps} timed steps, {nproc} processes x 1 thread, "
+                                       "CPU restatement of the reference algorithm (reference binary not buildable: "
+                                       "needs MPI, Boost, Trilinos)"},
+            "e2e": {"value": val, "unit": "tets/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def cpu_baseline_port(a, budget_s=12.0):
+    """The oracle on one host core, bounded: assembly of a 24^3 mesh repeated."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+    from morganapublic_gb300 import meshgen
+    n = min(a.n, 24)
+    m = meshgen.kuhn_cube(n, jitter=a.jitter, seed=a.seed, permute=True)
+    kappa = meshgen.lognormal(len(m.conn), a.sigma, a.seed)
+    t_asm, reps = 0.0, 0
+    t_end = time.perf_counter() + budget_s
+    while time.perf_counter() < t_end or reps == 0:
+        t0 = time.perf_counter()
+        dofs = orc.elem_dofs(1, len(m.xyz), m.conn)
+        rp, ci = orc.pattern(1, len(m.xyz), dofs)
+        orc.assemble("stiff_kappa", 1, 4, m.xyz, m.conn, dofs, rp, ci, kappa)
+        t_asm += time.perf_counter() - t0
+        reps += 1
+    return {"value": reps * len(m.conn) / t_asm, "unit": "tets/s", "cores": 1, "kind": "port",
+            "sample": f"{n}^3 mesh ({len(m.conn)} tets) assembled {reps}x (pattern + values, reference algorithm "
+                      f"restated in C, -O2), {t_asm:.1f} s"}
+
+
+# -------------------------------------------------------------------- gb300 --
+def main():
+    a = parse()
+    if a.impl == "reference":
+        return run_reference(a)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    cpu_base = None
+    if rank == 0 and not a.no_cpu_baseline:
+        cpu_base = cpu_baseline_port(a)  # before any CUDA work
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+    import morganapublic_gb300 as mg
+    from morganapublic_gb300 import meshgen
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    stream = torch.cuda.Stream()
+    peak, peak_kind = peaks()
+
+    m = meshgen.kuhn_cube(a.n, jitter=a.jitter, seed=a.seed, permute=True)
+    kappa_h = meshgen.lognormal(len(m.conn), a.sigma, a.seed)
+    E, N = len(m.conn), len(m.xyz)
+    mesh = mg.Mesh(m.xyz, m.conn, order=1)
+    b = mg.MatrixBuilder(mesh)
+    nnz, ndof = b.nnz, b.ndof
+    sched = b.schedule_info()
+    kappa = torch.from_numpy(kappa_h).cuda()
+    x = torch.from_numpy(np.random.default_rng(a.seed).uniform(-1, 1, ndof)).cuda()
+    x32 = x.float()
+    v64 = torch.empty(nnz, dtype=torch.float64, device="cuda")
+    v32 = torch.empty(nnz, dtype=torch.float32, device="cuda")
+    y = torch.empty(ndof, dtype=torch.float64, device="cuda")
+    y32 = torch.empty(ndof, dtype=torch.float32, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def step(ev=None):
+        if ev:
+            ev[0].record(stream)
+        b.assemble("stiff_kappa", coeff=kappa, quad=4, prec="f64", out=v64, stream=stream)
+        if ev:
+            ev[1].record(stream)
+        for _ in range(N_SPMV):
+            b.apply(v64, x, out=y, stream=stream)
+        if ev:
+            ev[2].record(stream)
+
+    with torch.cuda.stream(stream):
+        for _ in range(a.warmup):
+            flush.fill_(1.0)
+            step()
+        torch.cuda.synchronize()
+        evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(a.steps)]
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        with ClockSampler(local) as clk:
+            t_wall0 = time.perf_counter()
+            for s in range(a.steps):
+                flush.fill_(float(s))
+                step(evs[s])
+            torch.cuda.synchronize()
+            t_wall = time.perf_counter() - t_wall0
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+    t_asm = [e[0].elapsed_time(e[1]) for e in evs]
+    t_spmv = [e[1].elapsed_time(e[2]) / N_SPMV for e in evs]
+    t_step = [e[0].elapsed_time(e[2]) for e in evs]
+    ms_step = statistics.mean(t_step)
+    if world > 1:
+        t = torch.tensor([ms_step], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    value = world * E / (ms_step * 1e-3)
+
+    # ---------------------------------------------------------- extra metrics (untimed above)
+    extras = {}
+    if rank == 0:
+        def timed(fn, reps=10, flush_each=True):
+            ts = []
+            with torch.cuda.stream(stream):
+                for r in range(reps + 2):
+                    if flush_each:
+                        flush.fill_(float(r))
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
+                    fn()
+                    e1.record(stream)
+                    torch.cuda.synchronize()
+                    if r >= 2:
+                        ts.append(e0.elapsed_time(e1))
+            return statistics.median(ts)
+
+        B64 = asm_bytes(E, N, nnz, 8)
+        B32 = asm_bytes(E, N, nnz, 4)
+        S64, S32 = spmv_bytes(ndof, nnz, 8), spmv_bytes(ndof, nnz, 4)
+        ta64 = statistics.median(t_asm)
+        ta32 = timed(lambda: b.assemble("stiff_kappa", coeff=kappa, quad=4, prec="f32", out=v32, stream=stream))
+        ts64_cold = timed(lambda: b.apply(v64, x, out=y, stream=stream))
+        ts32_cold = timed(lambda: b.apply(v32, x32, out=y32, stream=stream))
+        ts64_warm = statistics.median(t_spmv)
+
+        def rec(bytes_, ms, units=None):
+            gbs = bytes_ / (ms * 1e-3) / 1e9
+            d = {"ms": ms, "gbs": gbs, "frac_of_hbm": gbs / peak, "algorithmic_bytes": bytes_}
+            if units:
+                d["tets_per_s"] = units / (ms * 1e-3)
+            return d
+
+        extras["assembly_f64"] = rec(B64, ta64, E)
+        extras["assembly_f32"] = rec(B32, ta32, E)
+        extras["spmv_f64_cold"] = rec(S64, ts64_cold)
+        extras["spmv_f64_in_step"] = rec(S64, ts64_warm)
+        extras["spmv_f64_in_step"]["note"] = f"{N_SPMV} back-to-back SpMVs; the {S64/1e6:.0f} MB working set stays in the 129 MB L2"
+        extras["spmv_f32_cold"] = rec(S32, ts32_cold)
+        extras["schedule"] = {"blocks": sched.nblocks, "items": sched.n_items, "recompute_factor": sched.n_items / E,
+                              "entries": sched.n_entries, "padding_factor": sched.n_entries / max(1, sched.n_contrib)}
+
+        # CG: FP64 PCG vs FP32-refined, Dirichlet u = 0, f = 1, to 1e-10
+        if not a.no_cg:
+            with torch.cuda.stream(stream):
+                rhs = b.build_vector(quad=4, stream=stream)
+                mask = torch.from_numpy(m.boundary)
+                A64 = b.assemble("stiff_kappa", coeff=kappa, quad=4, prec="f64", stream=stream)
+                A32 = b.assemble("stiff_kappa", coeff=kappa, quad=4, prec="f32", stream=stream)
+                b.apply_dirichlet(A64, mask, rhs, stream=stream)
+                b.apply_dirichlet(A32, mask, stream=stream)
+                torch.cuda.synchronize()
+                xs, i64 = b.cg(A64, rhs, rtol=1e-10, maxit=20000, stream=stream)
+                xr, imx = b.cg_refined(A64, A32, rhs, rtol=1e-10, inner_rtol=1e-4, stream=stream)
+                torch.cuda.synchronize()
+                xs, i64 = b.cg(A64, rhs, rtol=1e-10, maxit=20000, stream=stream)
+                xr, imx = b.cg_refined(A64, A32, rhs, rtol=1e-10, inner_rtol=1e-4, stream=stream)
+                torch.cuda.synchronize()
+            diff = float(torch.linalg.norm(xr - xs) / torch.linalg.norm(xs))
+            extras["cg"] = {"fp64_pcg": i64.as_dict(), "fp32_refined": imx.as_dict(),
+                            "speedup_refined_vs_fp64": i64.seconds / imx.seconds if imx.seconds > 0 else None,
+                            "refined_vs_fp64_solution_rel_diff": diff, "precond": "jacobi", "rtol": 1e-10}
+
+        # e2e through the C ABI with host buffers: kappa in, CSR values out, x in, y out
+        import ctypes
+        kap_pin = torch.from_numpy(kappa_h).pin_memory()
+        x_pin = x.cpu().pin_memory()
+        v_pin = torch.empty(nnz, dtype=torch.float64).pin_memory()
+        y_pin = torch.empty(ndof, dtype=torch.float64).pin_memory()
+        kap_d = torch.empty_like(kappa)
+        x_d = torch.empty_like(x)
+
+        def e2e_step():
+            kap_d.copy_(kap_pin, non_blocking=True)
+            x_d.copy_(x_pin, non_blocking=True)
+            b.assemble("stiff_kappa", coeff=kap_d, quad=4, prec="f64", out=v64, stream=stream)
+            v_pin.copy_(v64, non_blocking=True)
+            for _ in range(N_SPMV):
+                b.apply(v64, x_d, out=y, stream=stream)
+            y_pin.copy_(y, non_blocking=True)
+
+        te2e = timed(e2e_step, reps=max(3, min(a.steps, 10)))
+        h2d = 8 * E + 8 * ndof
+        d2h = 8 * nnz + 8 * ndof
+        del ctypes
+        e2e = {"value": world * E / (te2e * 1e-3), "unit": "tets/s", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "ms_per_step": te2e,
+               "note": "kappa and x copied in from pinned host memory, CSR values and y copied out, per step"}
+
+        dom = "assembly_f64" if statistics.median(t_asm) >= N_SPMV * ts64_warm else "spmv_f64_in_step"
+        rl = extras[dom]
+        roofline = {"bound": "hbm", "kernel": "k_assemble<1,double>" if dom == "assembly_f64" else "k_spmv<double,16>",
+                    "achieved": rl["gbs"], "peak": peak, "unit": "GB/s", "frac": rl["gbs"] / peak,
+                    "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+                    "traffic": None}
+        clocks = clk.summary()
+        line = {"metric": METRIC, "value": value, "unit": "tets/s", "n_gpus": world, "steps": a.steps,
+                "warmup": a.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Kuhn cube, lognormal kappa)",
+                "config": workload_config(a, E, N, nnz), "roofline": roofline, "cpu_baseline": cpu_base,
+                "e2e": e2e, "gpu_launches": a.steps * (1 + N_SPMV),
+                "clocks": clocks, "wall_s_timed": t_wall, "kernels": extras}
+        print(json.dumps(line))
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

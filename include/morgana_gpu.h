@@ -1,0 +1,251 @@
+/*
+ * morgana_gpu.h -- C ABI of libmorgana_gpu.so, the GB300 (sm_103a) finite-element
+ * operator path: P1/P2 tetrahedral element matrices -> CSR -> SpMV / CG.
+ *
+ * The reference (morganaPublic) exposes this path as a compile-time C++ template
+ * API with no FFI; every entry point below names the reference interface it
+ * replaces (paths relative to the morganaPublic checkout).
+ *
+ * Conventions
+ *  - Every call returns mg_status (0 = MG_OK).  Nothing aborts or exits; the text
+ *    of the last error on the calling thread is available from mg_last_error().
+ *  - Indices are 0-based (the reference's gid - 1, as exported to Epetra with
+ *    index base 0: src/morganaContainer/pMapGlobalManip.cpp:231-252).
+ *  - "d_" arguments are device pointers on the handle's device; "h_" arguments
+ *    are host pointers, copied in or out inside the call.
+ *  - stream: a cudaStream_t passed as void* (NULL = legacy default stream).
+ *  - Handles own their device memory.  One handle per host thread; a handle may
+ *    be shared between threads only under external locking.
+ *  - There is no CPU fallback: a call that cannot run on the GPU fails.
+ */
+#ifndef MORGANA_GPU_H
+#define MORGANA_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int mg_status;
+enum {
+  MG_OK = 0,
+  MG_ERR_INVALID_ARG = 1,
+  MG_ERR_CUDA = 2,
+  MG_ERR_ALLOC = 3,
+  MG_ERR_BAD_MESH = 4,       /* detJ <= 0, node id out of range, duplicate nodes in a tet */
+  MG_ERR_NOT_CONVERGED = 5,  /* solver hit its iteration cap */
+  MG_ERR_UNSUPPORTED = 6,
+  MG_ERR_IO = 7,
+  MG_ERR_SIZE = 8            /* a size above a documented limit */
+};
+
+/* P2 edge numbering rule (src/morganaGeometry/connect3d.hpp:417-491 +
+   src/morganaContainer/pVectGlobalManip.hpp). */
+enum {
+  MG_EDGES_LEX = 0,   /* pMapItem: edges sorted by (min node, max node), :414-486 */
+  MG_EDGES_FIRST = 1  /* pMapItemShare on one rank: first appearance in the element x
+                         local-edge loop, :498-578 + traitsConnectOptimization.hpp:96-119 */
+};
+
+/* Bilinear forms (src/morganaOperators). */
+enum {
+  MG_OP_STIFF_KAPPA = 0, /* opEL3dA: kappa_e grad u . grad v  (opEL3dA.hpp:129-165) */
+  MG_OP_STIFF_CONST = 1, /* opEL3dF: c grad u . grad v        (opEL3dF.hpp:102-133) */
+  MG_OP_MASS = 2,        /* opEL3dG: u v                      (opEL3dG.hpp:83-108)  */
+  MG_OP_MASS_COEFF = 3   /* opEL3dM: kappa_e u v              (opEL3dM.hpp:129-158) */
+};
+
+/* Value precision of an assembled operator / vector. */
+enum { MG_F64 = 0, MG_F32 = 1 };
+
+/* Quadrature: the reference's linearTetra STANDARD cards
+   (src/morganaIntegrator/intStaticCards.cpp:707-991) plus the published 11-point
+   degree-4 rule of Keast (1986), which the reference does not have. */
+enum { MG_QUAD_1 = 1, MG_QUAD_4 = 4, MG_QUAD_11 = 11, MG_QUAD_15 = 15, MG_QUAD_64 = 64 };
+
+/* Preconditioners for the CG solvers. */
+enum { MG_PREC_NONE = 0, MG_PREC_JACOBI = 1 };
+
+typedef struct mg_mesh mg_mesh;
+typedef struct mg_plan mg_plan;
+
+typedef struct {
+  int64_t n_nodes;
+  int64_t n_elements;
+  int64_t n_edges;
+  int64_t ndof;
+  int32_t order;      /* 1 or 2 */
+  int32_t edge_rule;  /* MG_EDGES_* */
+  double min_det;     /* smallest detJ over the reference vertices of every tet */
+} mg_mesh_info;
+
+typedef struct {
+  int32_t iterations;        /* CG iterations (inner iterations summed for refinement) */
+  int32_t outer_iterations;  /* refinement steps (0 for plain CG) */
+  int32_t converged;
+  int32_t reserved;
+  double rel_residual;       /* ||b - A x||_2 / ||b||_2 at exit, FP64 operator */
+  double seconds;            /* device time of the solve (CUDA events) */
+} mg_cg_info;
+
+/* ---------------------------------------------------------------- mesh -- */
+
+/* Builds a mesh from node coordinates (n_nodes x 3) and tetrahedra
+   (n_elements x 4, 0-based node ids), numbers edges with edge_rule, and sets up
+   the P1 (order 1) or P2 (order 2) dof map.  Node id = position in xyz, element
+   order = position in conn, as the Gmsh ingest does.
+   Replaces: meshInit3d::gmMesh_to_stdB (src/morganaGeometry/meshInit3d.hpp:485-690)
+   with connect3d::buildConnectivity (connect3d.hpp:355-694),
+   meshDoctor3d::checkJacobian (meshDoctor3d.hpp:195-227) and
+   dofMapStatic3d::startup (src/morganaFields/dofMapStatic3d.hpp:420-560).
+   Returns MG_ERR_BAD_MESH when a tet has detJ <= 0 at a reference vertex. */
+mg_status mg_mesh_create(mg_mesh** out, int64_t n_nodes, const double* h_xyz, int64_t n_elements,
+                         const int32_t* h_conn, int32_t order, int32_t edge_rule);
+
+/* Loads a Gmsh 2.x ASCII mesh: node id = line order in $Nodes (the file's own
+   node label is ignored), tetrahedra = element type 4 in file order.
+   Replaces: loadMesh::gmMeshParallel, 3d (src/morganaFile/loadMesh.hpp:2065-2330). */
+mg_status mg_mesh_load_gmsh(mg_mesh** out, const char* path, int32_t order, int32_t edge_rule);
+
+mg_status mg_mesh_destroy(mg_mesh* mesh);
+mg_status mg_mesh_get_info(const mg_mesh* mesh, mg_mesh_info* info);
+
+/* Element -> global dof table (n_elements x nb, nb = 4 or 10), local order
+   vertices 1..4 then edges 1..6.
+   Replaces: feStaticInterface3d::feIndicesLG (src/morganaFields/feStaticInterface3d.hpp:389-408)
+   via dofMapStatic3d::mapListG (dofMapStatic3d.hpp:589-662), minus 1. */
+mg_status mg_mesh_export_dofs(const mg_mesh* mesh, int32_t* h_elem_dofs);
+
+/* Edge table: h_edge_nodes (n_edges x 2) = node ids of each global edge, and
+   h_elem_edges (n_elements x 6) = global edge of each local edge.
+   Replaces: connect3d::getElementToEdge / mesh3d::getEdges (connect3d.hpp:417-491). */
+mg_status mg_mesh_export_edges(const mg_mesh* mesh, int32_t* h_edge_nodes, int32_t* h_elem_edges);
+
+/* Node coordinates and connectivity as loaded (for Gmsh ingest checks). */
+mg_status mg_mesh_export_geometry(const mg_mesh* mesh, double* h_xyz, int32_t* h_conn);
+
+/* --------------------------------------------------------------- pattern -- */
+
+/* Builds the CSR sparsity pattern (union of element couplings, explicit zeros
+   kept, sorted columns) and the GPU assembly schedule of the mesh.
+   Replaces: the pattern half of traitsMatrixBuilder::buildEpetraCrs / numEntPerRow
+   (src/morganaFiniteElements/traitsMatrixBuilder.hpp:363-544). */
+mg_status mg_pattern_build(mg_mesh* mesh, mg_plan** out);
+mg_status mg_plan_destroy(mg_plan* plan);
+mg_status mg_pattern_info(const mg_plan* plan, int64_t* ndof, int64_t* nnz);
+
+/* rowptr (ndof + 1) and colind (nnz) as int32, 0-based. */
+mg_status mg_pattern_export(const mg_plan* plan, int32_t* h_rowptr, int32_t* h_colind);
+
+/* Device copies owned by the plan (valid until mg_plan_destroy). */
+mg_status mg_pattern_device(const mg_plan* plan, const int32_t** d_rowptr, const int32_t** d_colind);
+
+/* Assembly schedule of a plan (no reference counterpart: the reference inserts
+   element blocks into Epetra one by one).  The dofs are cut into blocks of at
+   most acc_max CSR entries; one CTA of `threads` threads owns a block and
+   recomputes every element ("item") touching it.  For host-side checks the
+   schedule can be exported until the plan is first used on the GPU. */
+typedef struct {
+  int32_t nblocks;
+  int32_t threads;
+  int32_t warps;
+  int32_t acc_max;
+  int32_t chunk_items;
+  int32_t host_copy;   /* 1 while mg_plan_export_schedule is available */
+  int64_t n_items;     /* element recomputations summed over blocks */
+  int64_t n_chunks;
+  int64_t n_entries;   /* contribution-list entries, padding included */
+  int64_t n_contrib;   /* element-matrix entries scattered (= n_elements * nb^2) */
+} mg_schedule_info;
+
+mg_status mg_plan_schedule_info(const mg_plan* plan, mg_schedule_info* info);
+
+/* h_blocks: nblocks x 8 int32 {item_begin, item_count, chunk_begin, nchunks,
+   row_begin, row_count, acc_used, 0}; h_items: n_items element ids; h_chunk_ptr:
+   n_chunks x (warps + 1) offsets into h_entries; h_entries: n_entries words
+   (slot / threads) << 16 | source, the source indexing the chunk's element
+   matrices stored entry-major (k * chunk_items + item, k = field * nb + test);
+   h_rows / h_row_acc: ndof owned rows per block and their accumulator base. */
+mg_status mg_plan_export_schedule(const mg_plan* plan, int32_t* h_blocks, int32_t* h_items,
+                                  int64_t* h_chunk_ptr, uint32_t* h_entries, int32_t* h_rows,
+                                  int32_t* h_row_acc);
+
+/* ------------------------------------------------------------- assembly -- */
+
+/* Assembles the CSR values of one bilinear form into d_values (nnz entries of
+   double for MG_F64 or float for MG_F32).  coeff: per-element kappa (device,
+   n_elements doubles) for MG_OP_STIFF_KAPPA / MG_OP_MASS_COEFF, else ignored;
+   c: the constant of MG_OP_STIFF_CONST.  Deterministic: the same inputs give
+   the same bits on every call.
+   Replaces: the value half of matrixBuilder<localMatrixEL3d<...>>::buildEpetraCrs
+   (traitsMatrixBuilder.hpp:363-441) with integratorOEL3d_STD::integration
+   (src/morganaIntegrator/integratorOEL3d_STD.hpp:106-137). */
+mg_status mg_assemble(mg_plan* plan, int32_t op, const double* d_coeff, double c, int32_t quad,
+                      int32_t prec, void* d_values, void* stream);
+
+/* Host-buffer form of mg_assemble, the call an Epetra/Tpetra adapter makes:
+   copies h_coeff in, assembles, copies the nnz values out to h_values. */
+mg_status mg_assemble_host(mg_plan* plan, int32_t op, const double* h_coeff, double c, int32_t quad,
+                           int32_t prec, void* h_values, void* stream);
+
+/* Load vector b_i = sum_e s_e int_e f_h phi_i (f_h the nodal P1/P2 field d_field,
+   or 1 when d_field is NULL; s_e = d_elem_scale[e] or 1 when NULL), written to
+   d_b (ndof doubles).
+   Replaces: vectorBuilder<localVectorEL3d<fnEL3dA|fnEL3dB>>::buildEpetraVector
+   (src/morganaFiniteElements/traitsVectorBuilder.hpp:214-274). */
+mg_status mg_assemble_rhs(mg_plan* plan, const double* d_field, const double* d_elem_scale,
+                          int32_t quad, double* d_b, void* stream);
+
+/* Build addition (the reference imposes Dirichlet data with Lagrange
+   multipliers, src/morganaFiniteElements/localMatrixLA3d.hpp:292-322): symmetric
+   elimination of the dofs with d_mask[i] != 0 -- their rows and columns are
+   zeroed, the diagonal set to 1, and d_b (if not NULL) zeroed there. */
+mg_status mg_apply_dirichlet(mg_plan* plan, const uint8_t* d_mask, int32_t prec, void* d_values,
+                             double* d_b, void* stream);
+
+/* ---------------------------------------------------------------- solve -- */
+
+/* y = A x with the plan's pattern and d_values; x, y in the value precision.
+   Replaces: Epetra_CrsMatrix::Apply as consumed by Belos / ML
+   (src/morganaTrilinos/belosBlockCG.hpp:53-73, epetraOperatorSum.cpp:117-128). */
+mg_status mg_spmv(mg_plan* plan, int32_t prec, const void* d_values, const void* d_x, void* d_y,
+                  void* stream);
+
+/* FP64 preconditioned CG on the FP64 operator: stops when
+   ||b - A x||_2 <= rtol ||b||_2 (recursive residual) or after maxit iterations
+   (MG_ERR_NOT_CONVERGED).  d_x holds the initial guess on entry.
+   Replaces: belosBlockCG::solve (src/morganaTrilinos/belosBlockCG.hpp:46-82),
+   block size 1. */
+mg_status mg_cg_solve(mg_plan* plan, const double* d_values, const double* d_b, double* d_x,
+                      double rtol, int32_t maxit, int32_t precond, mg_cg_info* info, void* stream);
+
+/* Mixed-precision solve: FP64 iterative refinement around an inner CG that
+   runs on the FP32 operator with FP32 vectors and FP64 dot products.  The
+   residual r = b - A64 x, its norm and the update x += d stay in FP64.
+   Stops when ||b - A64 x||_2 <= rtol ||b||_2.  Build addition (no reference
+   counterpart); same role as mg_cg_solve. */
+mg_status mg_cg_refined(mg_plan* plan, const double* d_values64, const float* d_values32,
+                        const double* d_b, double* d_x, double rtol, int32_t max_outer,
+                        int32_t max_inner, double inner_rtol, int32_t precond, mg_cg_info* info,
+                        void* stream);
+
+/* ------------------------------------------------------------- adjoint -- */
+
+/* Build addition: per-element gradient of J(kappa) for the P0 coefficient of
+   MG_OP_STIFF_KAPPA, d_grad[e] = -lambda_e^T Khat_e u_e, with Khat_e the
+   element stiffness at kappa_e = 1, u the state and lambda the adjoint
+   solution (ndof doubles each). */
+mg_status mg_adjoint_grad(mg_plan* plan, const double* d_u, const double* d_lambda, int32_t quad,
+                          double* d_grad, void* stream);
+
+/* -------------------------------------------------------------- status -- */
+const char* mg_status_string(mg_status status);
+const char* mg_last_error(void);
+/* Library version string. */
+const char* mg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MORGANA_GPU_H */

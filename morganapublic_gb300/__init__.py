@@ -1,0 +1,371 @@
+"""GB300 (sm_103a) finite-element operator path of morganaPublic.
+
+Python mirror of the reference's builder interface over the C ABI of
+libmorgana_gpu.so (include/morgana_gpu.h):
+
+    reference (C++ templates)                       here
+    ---------------------------------------------   -----------------------------------
+    meshInit3d::gmMesh_to_stdB + dofMapStatic3d      Mesh(xyz, conn, order, edge_rule)
+                                                     Mesh.load_gmsh(path, order, edge_rule)
+    matrixBuilder<localMatrixEL3d<...>>(op)          MatrixBuilder(mesh)
+      .buildEpetraCrs(matrix)                          .build_crs(op, coeff, c, quad, prec)
+    vectorBuilder<localVectorEL3d<...>>              MatrixBuilder.build_vector(field, scale, quad)
+      .buildEpetraVector(vector)
+    Epetra_Operator::Apply                           MatrixBuilder.apply(values, x)
+    belosBlockCG::solve                              MatrixBuilder.cg(values, b, ...)
+
+Device memory is held in torch tensors (torch is used for allocation and
+streams only); every computation runs in the CUDA library.  There is no CPU
+fallback: the compute calls raise when the library or the GPU is missing.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import meshgen  # noqa: F401
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libmorgana_gpu.so")
+
+MG_OK, MG_ERR_INVALID_ARG, MG_ERR_CUDA, MG_ERR_ALLOC, MG_ERR_BAD_MESH = 0, 1, 2, 3, 4
+MG_ERR_NOT_CONVERGED, MG_ERR_UNSUPPORTED, MG_ERR_IO, MG_ERR_SIZE = 5, 6, 7, 8
+EDGES = {"lex": 0, "first": 1}
+OPS = {"stiff_kappa": 0, "stiff_const": 1, "mass": 2, "mass_coeff": 3}
+PRECS = {"f64": 0, "f32": 1}
+PRECOND = {None: 0, "none": 0, "jacobi": 1}
+
+
+class MorganaError(RuntimeError):
+    def __init__(self, status: int, where: str, message: str):
+        super().__init__(f"{where}: {message} (status {status})")
+        self.status = status
+
+
+class _MeshInfo(ctypes.Structure):
+    _fields_ = [("n_nodes", ctypes.c_int64), ("n_elements", ctypes.c_int64), ("n_edges", ctypes.c_int64),
+                ("ndof", ctypes.c_int64), ("order", ctypes.c_int32), ("edge_rule", ctypes.c_int32),
+                ("min_det", ctypes.c_double)]
+
+
+class CgInfo(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int32), ("outer_iterations", ctypes.c_int32),
+                ("converged", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("rel_residual", ctypes.c_double), ("seconds", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
+class ScheduleInfo(ctypes.Structure):
+    _fields_ = [("nblocks", ctypes.c_int32), ("threads", ctypes.c_int32), ("warps", ctypes.c_int32),
+                ("acc_max", ctypes.c_int32), ("chunk_items", ctypes.c_int32), ("host_copy", ctypes.c_int32),
+                ("n_items", ctypes.c_int64), ("n_chunks", ctypes.c_int64), ("n_entries", ctypes.c_int64),
+                ("n_contrib", ctypes.c_int64)]
+
+
+_P = ctypes.c_void_p
+_I32, _I64, _D = ctypes.c_int32, ctypes.c_int64, ctypes.c_double
+# name -> argtypes; every function returns mg_status (int) unless listed in _RESTYPES
+SIGNATURES = {
+    "mg_mesh_create": [ctypes.POINTER(_P), _I64, _P, _I64, _P, _I32, _I32],
+    "mg_mesh_load_gmsh": [ctypes.POINTER(_P), ctypes.c_char_p, _I32, _I32],
+    "mg_mesh_destroy": [_P],
+    "mg_mesh_get_info": [_P, ctypes.POINTER(_MeshInfo)],
+    "mg_mesh_export_dofs": [_P, _P],
+    "mg_mesh_export_edges": [_P, _P, _P],
+    "mg_mesh_export_geometry": [_P, _P, _P],
+    "mg_pattern_build": [_P, ctypes.POINTER(_P)],
+    "mg_plan_destroy": [_P],
+    "mg_pattern_info": [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64)],
+    "mg_pattern_export": [_P, _P, _P],
+    "mg_pattern_device": [_P, ctypes.POINTER(_P), ctypes.POINTER(_P)],
+    "mg_plan_schedule_info": [_P, ctypes.POINTER(ScheduleInfo)],
+    "mg_plan_export_schedule": [_P, _P, _P, _P, _P, _P, _P],
+    "mg_assemble": [_P, _I32, _P, _D, _I32, _I32, _P, _P],
+    "mg_assemble_host": [_P, _I32, _P, _D, _I32, _I32, _P, _P],
+    "mg_assemble_rhs": [_P, _P, _P, _I32, _P, _P],
+    "mg_apply_dirichlet": [_P, _P, _I32, _P, _P, _P],
+    "mg_spmv": [_P, _I32, _P, _P, _P, _P],
+    "mg_cg_solve": [_P, _P, _P, _P, _D, _I32, _I32, ctypes.POINTER(CgInfo), _P],
+    "mg_cg_refined": [_P, _P, _P, _P, _P, _D, _I32, _I32, _D, _I32, ctypes.POINTER(CgInfo), _P],
+    "mg_adjoint_grad": [_P, _P, _P, _I32, _P, _P],
+    "mg_status_string": [_I32],
+    "mg_last_error": [],
+    "mg_version": [],
+}
+_RESTYPES = {"mg_status_string": ctypes.c_char_p, "mg_last_error": ctypes.c_char_p, "mg_version": ctypes.c_char_p}
+
+_lib = None
+
+
+def lib():
+    """Loads libmorgana_gpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run `python -m morganapublic_gb300.build` "
+                              "(or __graft_entry__.build()) first")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, args in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = _RESTYPES.get(name, ctypes.c_int)
+        _lib = L
+    return _lib
+
+
+def _check(status: int, where: str):
+    if status != MG_OK:
+        raise MorganaError(status, where, lib().mg_last_error().decode())
+
+
+def _ptr(a) -> int | None:
+    """Raw pointer of a numpy array or a torch tensor (None passes through)."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    return a.data_ptr()
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream
+    return getattr(stream, "cuda_stream", stream)
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("morganapublic_gb300 compute calls need a CUDA device; none is visible")
+    return torch
+
+
+class Mesh:
+    """Tetrahedral mesh with its P1/P2 dof map (mg_mesh)."""
+
+    def __init__(self, xyz, conn, order: int = 1, edge_rule: str = "lex", _handle=None):
+        L = lib()
+        h = _P()
+        if _handle is None:
+            xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+            conn = np.ascontiguousarray(conn, dtype=np.int32)
+            _check(L.mg_mesh_create(ctypes.byref(h), xyz.shape[0], _ptr(xyz), conn.shape[0], _ptr(conn),
+                                    order, EDGES[edge_rule]), "mg_mesh_create")
+        else:
+            h = _handle
+        self._h = h
+        info = _MeshInfo()
+        _check(L.mg_mesh_get_info(self._h, ctypes.byref(info)), "mg_mesh_get_info")
+        self.n_nodes, self.n_elements, self.ndof = info.n_nodes, info.n_elements, info.ndof
+        self.order, self.min_det = info.order, info.min_det
+        self.nb = 4 if order == 1 else 10
+
+    @classmethod
+    def load_gmsh(cls, path: str, order: int = 1, edge_rule: str = "lex") -> "Mesh":
+        h = _P()
+        _check(lib().mg_mesh_load_gmsh(ctypes.byref(h), path.encode(), order, EDGES[edge_rule]),
+               "mg_mesh_load_gmsh")
+        return cls(None, None, order, edge_rule, _handle=h)
+
+    @property
+    def n_edges(self) -> int:
+        info = _MeshInfo()
+        _check(lib().mg_mesh_get_info(self._h, ctypes.byref(info)), "mg_mesh_get_info")
+        return info.n_edges
+
+    def elem_dofs(self) -> np.ndarray:
+        out = np.empty((self.n_elements, self.nb), dtype=np.int32)
+        _check(lib().mg_mesh_export_dofs(self._h, _ptr(out)), "mg_mesh_export_dofs")
+        return out
+
+    def edges(self):
+        """(edge_nodes (nE, 2), elem_edges (E, 6))"""
+        L = lib()
+        _check(L.mg_mesh_export_edges(self._h, None, None), "mg_mesh_export_edges")
+        ne = self.n_edges
+        en = np.empty((ne, 2), dtype=np.int32)
+        ee = np.empty((self.n_elements, 6), dtype=np.int32)
+        _check(L.mg_mesh_export_edges(self._h, _ptr(en), _ptr(ee)), "mg_mesh_export_edges")
+        return en, ee
+
+    def geometry(self):
+        xyz = np.empty((self.n_nodes, 3), dtype=np.float64)
+        conn = np.empty((self.n_elements, 4), dtype=np.int32)
+        _check(lib().mg_mesh_export_geometry(self._h, _ptr(xyz), _ptr(conn)), "mg_mesh_export_geometry")
+        return xyz, conn
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().mg_mesh_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+@dataclass
+class Csr:
+    rowptr: np.ndarray
+    colind: np.ndarray
+    values: np.ndarray
+
+
+class MatrixBuilder:
+    """CSR pattern + GPU assembly schedule of a mesh (mg_plan); the counterpart of
+    the reference's matrixBuilder / vectorBuilder and of the operator Belos uses."""
+
+    def __init__(self, mesh: Mesh):
+        self.mesh = mesh
+        h = _P()
+        _check(lib().mg_pattern_build(mesh._h, ctypes.byref(h)), "mg_pattern_build")
+        self._h = h
+        nd, nz = _I64(), _I64()
+        _check(lib().mg_pattern_info(h, ctypes.byref(nd), ctypes.byref(nz)), "mg_pattern_info")
+        self.ndof, self.nnz = nd.value, nz.value
+
+    # ----------------------------------------------------------- pattern --
+    def pattern(self):
+        rp = np.empty(self.ndof + 1, dtype=np.int32)
+        ci = np.empty(self.nnz, dtype=np.int32)
+        _check(lib().mg_pattern_export(self._h, _ptr(rp), _ptr(ci)), "mg_pattern_export")
+        return rp, ci
+
+    def schedule_info(self) -> ScheduleInfo:
+        info = ScheduleInfo()
+        _check(lib().mg_plan_schedule_info(self._h, ctypes.byref(info)), "mg_plan_schedule_info")
+        return info
+
+    def export_schedule(self) -> dict:
+        info = self.schedule_info()
+        out = {
+            "blocks": np.empty((info.nblocks, 8), dtype=np.int32),
+            "items": np.empty(info.n_items, dtype=np.int32),
+            "chunk_ptr": np.empty(info.n_chunks * (info.warps + 1), dtype=np.int64),
+            "entries": np.empty(info.n_entries, dtype=np.uint32),
+            "rows": np.empty(self.ndof, dtype=np.int32),
+            "row_acc": np.empty(self.ndof, dtype=np.int32),
+        }
+        _check(lib().mg_plan_export_schedule(self._h, *[_ptr(out[k]) for k in
+                                                        ("blocks", "items", "chunk_ptr", "entries", "rows",
+                                                         "row_acc")]), "mg_plan_export_schedule")
+        out["info"] = info
+        return out
+
+    def device_pattern(self):
+        """(rowptr, colind) as int32 torch tensors on the GPU (copies)."""
+        torch = _torch()
+        rp, ci = _P(), _P()
+        _check(lib().mg_pattern_device(self._h, ctypes.byref(rp), ctypes.byref(ci)), "mg_pattern_device")
+        rph, cih = self.pattern()
+        return torch.from_numpy(rph).cuda(), torch.from_numpy(cih).cuda()
+
+    # ---------------------------------------------------------- assembly --
+    def assemble(self, op: str = "stiff_kappa", coeff=None, c: float = 1.0, quad: int = 4, prec: str = "f64",
+                 out=None, stream=None):
+        """CSR values on the GPU (torch tensor of nnz float64/float32)."""
+        torch = _torch()
+        dt = torch.float64 if prec == "f64" else torch.float32
+        if out is None:
+            out = torch.empty(self.nnz, dtype=dt, device="cuda")
+        if coeff is not None:
+            coeff = torch.as_tensor(coeff, dtype=torch.float64, device="cuda").contiguous()
+        _check(lib().mg_assemble(self._h, OPS[op], _ptr(coeff), float(c), quad, PRECS[prec], _ptr(out),
+                                 _stream_ptr(stream)), "mg_assemble")
+        return out
+
+    def build_crs(self, op: str = "stiff_kappa", coeff=None, c: float = 1.0, quad: int = 4,
+                  prec: str = "f64") -> Csr:
+        """Host-buffer assembly (what buildEpetraCrs hands to Epetra): pattern + values."""
+        _torch()
+        vals = np.empty(self.nnz, dtype=np.float64 if prec == "f64" else np.float32)
+        cf = None if coeff is None else np.ascontiguousarray(coeff, dtype=np.float64)
+        _check(lib().mg_assemble_host(self._h, OPS[op], _ptr(cf), float(c), quad, PRECS[prec], _ptr(vals),
+                                      _stream_ptr(None)), "mg_assemble_host")
+        rp, ci = self.pattern()
+        return Csr(rp, ci, vals)
+
+    def build_vector(self, field=None, elem_scale=None, quad: int = 4, out=None, stream=None):
+        torch = _torch()
+        if out is None:
+            out = torch.empty(self.ndof, dtype=torch.float64, device="cuda")
+        f = None if field is None else torch.as_tensor(field, dtype=torch.float64, device="cuda").contiguous()
+        s = None if elem_scale is None else torch.as_tensor(elem_scale, dtype=torch.float64,
+                                                            device="cuda").contiguous()
+        _check(lib().mg_assemble_rhs(self._h, _ptr(f), _ptr(s), quad, _ptr(out), _stream_ptr(stream)),
+               "mg_assemble_rhs")
+        return out
+
+    def apply_dirichlet(self, values, mask, b=None, stream=None):
+        torch = _torch()
+        m = torch.as_tensor(mask, device="cuda").to(torch.uint8).contiguous()
+        prec = "f64" if values.dtype == torch.float64 else "f32"
+        _check(lib().mg_apply_dirichlet(self._h, _ptr(m), PRECS[prec], _ptr(values), _ptr(b),
+                                        _stream_ptr(stream)), "mg_apply_dirichlet")
+        return values
+
+    # ------------------------------------------------------------- solve --
+    def apply(self, values, x, out=None, stream=None):
+        """y = A x (Epetra_Operator::Apply)."""
+        torch = _torch()
+        prec = "f64" if values.dtype == torch.float64 else "f32"
+        if out is None:
+            out = torch.empty(self.ndof, dtype=values.dtype, device="cuda")
+        _check(lib().mg_spmv(self._h, PRECS[prec], _ptr(values), _ptr(x), _ptr(out), _stream_ptr(stream)),
+               "mg_spmv")
+        return out
+
+    def cg(self, values, b, x0=None, rtol: float = 1e-10, maxit: int = 10000, precond="jacobi", stream=None,
+           raise_on_fail: bool = True):
+        torch = _torch()
+        x = torch.zeros_like(b) if x0 is None else x0.clone()
+        info = CgInfo()
+        st = lib().mg_cg_solve(self._h, _ptr(values), _ptr(b), _ptr(x), rtol, maxit, PRECOND[precond],
+                               ctypes.byref(info), _stream_ptr(stream))
+        if raise_on_fail or st not in (MG_OK, MG_ERR_NOT_CONVERGED):
+            _check(st, "mg_cg_solve")
+        return x, info
+
+    def cg_refined(self, values64, values32, b, x0=None, rtol: float = 1e-10, max_outer: int = 50,
+                   max_inner: int = 10000, inner_rtol: float = 1e-4, precond="jacobi", stream=None,
+                   raise_on_fail: bool = True):
+        torch = _torch()
+        x = torch.zeros_like(b) if x0 is None else x0.clone()
+        info = CgInfo()
+        st = lib().mg_cg_refined(self._h, _ptr(values64), _ptr(values32), _ptr(b), _ptr(x), rtol, max_outer,
+                                 max_inner, inner_rtol, PRECOND[precond], ctypes.byref(info),
+                                 _stream_ptr(stream))
+        if raise_on_fail or st not in (MG_OK, MG_ERR_NOT_CONVERGED):
+            _check(st, "mg_cg_refined")
+        return x, info
+
+    def adjoint_grad(self, u, lam, quad: int = 4, out=None, stream=None):
+        torch = _torch()
+        if out is None:
+            out = torch.empty(self.mesh.n_elements, dtype=torch.float64, device="cuda")
+        _check(lib().mg_adjoint_grad(self._h, _ptr(u), _ptr(lam), quad, _ptr(out), _stream_ptr(stream)),
+               "mg_adjoint_grad")
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().mg_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def version() -> str:
+    return lib().mg_version().decode()

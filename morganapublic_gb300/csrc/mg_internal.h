@@ -1,0 +1,148 @@
+// Internal structures of libmorgana_gpu.so (not part of the C ABI).
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "morgana_gpu.h"
+
+namespace mg {
+
+// ------------------------------------------------------------------ errors --
+mg_status set_error(mg_status s, const std::string& msg);
+mg_status cuda_error(cudaError_t e, const char* what);
+
+#define MG_CUDA(call)                                          \
+  do {                                                         \
+    cudaError_t _e = (call);                                   \
+    if (_e != cudaSuccess) return ::mg::cuda_error(_e, #call); \
+  } while (0)
+
+#define MG_TRY(call)                  \
+  do {                                \
+    mg_status _s = (call);            \
+    if (_s != MG_OK) return _s;       \
+  } while (0)
+
+// --------------------------------------------------------- schedule sizes --
+// Threads per assembly CTA; each owns the accumulator slots s with s % kThreads
+// equal to its thread index.
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+// Accumulator slots (CSR entries of the rows a CTA owns) held in shared memory.
+constexpr int kAccMax = 8192;
+constexpr int kAccDiv = kAccMax / kThreads;  // slots per thread
+// Elements ("items") per chunk: one thread per P1 element, eight per P2 element.
+constexpr int kChunkP1 = 256;
+constexpr int kChunkP2 = 32;
+constexpr int kP2ThreadsPerItem = kThreads / kChunkP2;
+
+inline int nbasis(int order) { return order == 1 ? 4 : 10; }
+inline int chunk_items(int order) { return order == 1 ? kChunkP1 : kChunkP2; }
+
+// One CTA of the assembly kernel: a set of owned rows plus every element that
+// touches one of them.
+struct BlockDesc {
+  int32_t item_begin;   // into items[]
+  int32_t item_count;
+  int32_t chunk_begin;  // into chunk_ptr[] (in chunks)
+  int32_t nchunks;
+  int32_t row_begin;    // into rows[] / row_acc[]
+  int32_t row_count;
+  int32_t acc_used;     // accumulator slots in use
+  int32_t pad;
+};
+
+// Reference-element tables for one (order, quadrature) pair, with the quadrature
+// weights folded in.  stiff[ab][i*nb+j] = sum_q w_q dphi_i/dxi_a dphi_j/dxi_b for
+// the six symmetric pairs ab = 00,11,22,01,02,12 (off-diagonal pairs symmetrised);
+// mass[i*nb+j] = sum_q w_q phi_i phi_j.  Index i is the field (column) basis
+// function and j the test (row) one, the reference's column-major local layout.
+struct RefTables {
+  int order = 0, quad = 0, nb = 0, nq = 0;
+  std::vector<double> stiff;  // 6 * nb * nb
+  std::vector<double> mass;   // nb * nb
+  double wsum = 0.0;
+};
+mg_status build_ref_tables(int order, int quad, RefTables* t);
+int quad_rule(int quad, std::vector<double>* Y, std::vector<double>* W);
+void basis_values(int order, const double* Y, double* v);
+void basis_grads(int order, const double* Y, double* gx, double* gy, double* gz);
+
+}  // namespace mg
+
+namespace mg { struct HostSchedule; }
+
+// ---------------------------------------------------------------- handles --
+struct mg_mesh {
+  int order = 1, edge_rule = MG_EDGES_LEX, nb = 4, device = 0;
+  int64_t n_nodes = 0, n_elem = 0, n_edges = -1, ndof = 0;
+  double min_det = 0.0;
+  std::vector<double> xyz;          // n_nodes * 3
+  std::vector<int32_t> conn;        // n_elem * 4
+  std::vector<int32_t> elem_edge;   // n_elem * 6 (when built)
+  std::vector<int32_t> edge_nodes;  // n_edges * 2 (when built)
+  std::vector<int32_t> dofs;        // n_elem * nb
+  // device copies
+  double4_32a* d_xyz = nullptr;      // (x, y, z, 0)
+  float4* d_xyz_hi = nullptr;    // float pair split: x = hi + lo exactly to ~2^-48
+  float4* d_xyz_lo = nullptr;
+  int4* d_conn = nullptr;        // vertex node ids
+  int32_t* d_dofs = nullptr;     // n_elem * nb
+  bool on_device = false;
+};
+
+struct mg_plan {
+  mg_mesh* mesh = nullptr;
+  int64_t ndof = 0, nnz = 0;
+  std::vector<int32_t> rowptr, colind;
+  int32_t* d_rowptr = nullptr;
+  int32_t* d_colind = nullptr;
+  int32_t* d_diag = nullptr;  // slot of the diagonal entry of each row
+  // assembly schedule
+  int32_t nblocks = 0;
+  int64_t n_items = 0, n_chunks = 0, n_entries = 0, n_contrib = 0;
+  mg::BlockDesc* d_blocks = nullptr;
+  int32_t* d_items = nullptr;
+  int64_t* d_chunk_ptr = nullptr;  // (kWarps + 1) per chunk, offsets into entries
+  uint32_t* d_entries = nullptr;   // (slot / kThreads) << 16 | source index
+  int32_t* d_rows = nullptr;
+  int32_t* d_row_acc = nullptr;
+  // reference tables, cached per (quad) on the device
+  std::vector<mg::RefTables> tables;
+  std::vector<double*> d_tables;  // parallel to tables: stiff (6 nb^2) then mass (nb^2)
+  // solver work space (allocated on first use)
+  void* d_work = nullptr;
+  size_t work_bytes = 0;
+  double* h_pinned = nullptr;  // small pinned scalars
+  // temporary buffers of the host-buffer entry points
+  void* d_tmp_values = nullptr;
+  size_t tmp_values_bytes = 0;
+  double* d_tmp_coeff = nullptr;
+  size_t tmp_coeff_bytes = 0;
+  mg::HostSchedule* host_schedule = nullptr;  // until uploaded
+  bool on_device = false;
+};
+
+namespace mg {
+// Host copy of the assembly schedule, kept until the plan is first used on the GPU.
+struct HostSchedule {
+  std::vector<BlockDesc> blocks;
+  std::vector<int32_t> items, rows, row_acc;
+  std::vector<int64_t> chunk_ptr;
+  std::vector<uint32_t> entries;
+  int64_t n_contrib = 0;
+};
+mg_status mesh_device(mg_mesh* m);  // uploads the mesh on first GPU use
+mg_status plan_device(mg_plan* p);  // uploads mesh + plan on first GPU use
+mg_status plan_tables(mg_plan* p, int quad, const RefTables** t, const double** d_tab);
+mg_status plan_work(mg_plan* p, size_t bytes, void** ptr);
+mg_status ensure_edges(mg_mesh* m);
+mg_status launch_assemble(mg_plan* p, int op, const double* d_coeff, double c, int quad, int prec,
+                          void* d_values, cudaStream_t st);
+mg_status launch_spmv(mg_plan* p, int prec, const void* vals, const void* x, void* y, cudaStream_t st);
+mg_status launch_rowsum(mg_plan* p, const double* vals, double* y, cudaStream_t st);
+}  // namespace mg

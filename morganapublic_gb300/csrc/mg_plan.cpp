@@ -1,0 +1,446 @@
+// CSR pattern and GPU assembly schedule (host side).
+//
+// Pattern: the union of element couplings with sorted columns and explicit
+// zeros kept -- the matrix traitsMatrixBuilder::buildEpetraCrs leaves behind
+// after Epetra_FECrsMatrix::GlobalAssemble
+// (src/morganaFiniteElements/traitsMatrixBuilder.hpp:363-544 in morganaPublic).
+//
+// Schedule: the rows (dofs) are cut into blocks along a Morton curve of the dof
+// positions, each holding at most kAccMax CSR entries.  One CTA owns one block:
+// it recomputes every element touching one of its rows ("items", sorted by
+// element id) and sums each owned CSR entry in shared memory.  Accumulator slot
+// s of a block is only ever updated by thread s % kThreads, so the reduction
+// needs neither atomics nor a second pass, and every slot adds its element
+// contributions in increasing element order -- the order in which the
+// reference inserts them.  The contribution lists are stored per chunk of
+// items, per warp, interleaved by lane ([k][lane]) and padded to the warp's
+// longest list, so that phase 2 of the kernel reads them fully coalesced.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+
+#include "mg_internal.h"
+
+namespace mg {
+
+static uint64_t spread21(uint64_t v)
+{
+  v &= 0x1fffff;
+  v = (v | v << 32) & 0x1f00000000ffffULL;
+  v = (v | v << 16) & 0x1f0000ff0000ffULL;
+  v = (v | v << 8) & 0x100f00f00f00f00fULL;
+  v = (v | v << 4) & 0x10c30c30c30c30c3ULL;
+  v = (v | v << 2) & 0x1249249249249249ULL;
+  return v;
+}
+
+static mg_status build_pattern(mg_plan* p)
+{
+  mg_mesh* m = p->mesh;
+  const int nb = m->nb;
+  const int64_t E = m->n_elem, nd = m->ndof;
+  std::vector<int64_t> start(nd + 1, 0);
+  for (int64_t k = 0; k < E * nb; ++k) start[m->dofs[k] + 1]++;
+  for (int64_t r = 0; r < nd; ++r) start[r + 1] += start[r];
+  std::vector<int64_t> fill(start.begin(), start.end() - 1);
+  std::vector<int32_t> inc(E * nb);
+  for (int64_t k = 0; k < E * nb; ++k) inc[fill[m->dofs[k]]++] = (int32_t)(k / nb);
+  std::vector<int32_t> len(nd, 0);
+  int bad = 0;
+#pragma omp parallel
+  {
+    std::vector<int32_t> tmp;
+#pragma omp for schedule(dynamic, 1024)
+    for (int64_t r = 0; r < nd; ++r) {
+      tmp.clear();
+      for (int64_t t = start[r]; t < start[r + 1]; ++t)
+        for (int i = 0; i < nb; ++i) tmp.push_back(m->dofs[(int64_t)inc[t] * nb + i]);
+      std::sort(tmp.begin(), tmp.end());
+      len[r] = (int32_t)(std::unique(tmp.begin(), tmp.end()) - tmp.begin());
+      if (len[r] > kAccMax) bad = 1;
+    }
+  }
+  if (bad) return set_error(MG_ERR_SIZE, "a CSR row has more than 8192 entries");
+  p->rowptr.assign(nd + 1, 0);
+  for (int64_t r = 0; r < nd; ++r) {
+    int64_t next = (int64_t)p->rowptr[r] + len[r];
+    if (next >= INT32_MAX) return set_error(MG_ERR_SIZE, "nnz above 2^31-1");
+    p->rowptr[r + 1] = (int32_t)next;
+  }
+  p->nnz = p->rowptr[nd];
+  p->colind.resize(p->nnz);
+#pragma omp parallel
+  {
+    std::vector<int32_t> tmp;
+#pragma omp for schedule(dynamic, 1024)
+    for (int64_t r = 0; r < nd; ++r) {
+      tmp.clear();
+      for (int64_t t = start[r]; t < start[r + 1]; ++t)
+        for (int i = 0; i < nb; ++i) tmp.push_back(m->dofs[(int64_t)inc[t] * nb + i]);
+      std::sort(tmp.begin(), tmp.end());
+      tmp.erase(std::unique(tmp.begin(), tmp.end()), tmp.end());
+      std::copy(tmp.begin(), tmp.end(), p->colind.begin() + p->rowptr[r]);
+    }
+  }
+  p->ndof = nd;
+  return MG_OK;
+}
+
+static mg_status build_schedule(mg_plan* p, HostSchedule* hs)
+{
+  mg_mesh* m = p->mesh;
+  const int nb = m->nb, nb2 = nb * nb, CI = chunk_items(m->order);
+  const int64_t E = m->n_elem, nd = p->ndof, N = m->n_nodes;
+  if (CI * nb2 + 1 > 0xffff) return set_error(MG_ERR_SIZE, "chunk buffer above 16-bit index");
+  // dof positions and Morton keys
+  double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int64_t i = 0; i < N; ++i)
+    for (int k = 0; k < 3; ++k) {
+      lo[k] = std::min(lo[k], m->xyz[3 * i + k]);
+      hi[k] = std::max(hi[k], m->xyz[3 * i + k]);
+    }
+  std::vector<uint64_t> key(nd);
+#pragma omp parallel for
+  for (int64_t d = 0; d < nd; ++d) {
+    double x[3];
+    if (d < N) {
+      for (int k = 0; k < 3; ++k) x[k] = m->xyz[3 * d + k];
+    } else {
+      const int32_t a = m->edge_nodes[2 * (d - N)], b = m->edge_nodes[2 * (d - N) + 1];
+      for (int k = 0; k < 3; ++k) x[k] = 0.5 * (m->xyz[3 * (int64_t)a + k] + m->xyz[3 * (int64_t)b + k]);
+    }
+    uint64_t c = 0;
+    for (int k = 0; k < 3; ++k) {
+      double t = hi[k] > lo[k] ? (x[k] - lo[k]) / (hi[k] - lo[k]) : 0.0;
+      uint64_t q = (uint64_t)std::min(2097151.0, std::max(0.0, t * 2097151.0));
+      c |= spread21(q) << k;
+    }
+    key[d] = c;
+  }
+  std::vector<int32_t> order(nd);
+  std::iota(order.begin(), order.end(), 0);
+  std::sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
+    return key[a] != key[b] ? key[a] < key[b] : a < b;
+  });
+  // greedy blocks of at most kAccMax accumulator slots
+  std::vector<int32_t> block_of(nd);
+  std::vector<int64_t> bstart;  // into order
+  int64_t used = kAccMax + 1;
+  for (int64_t t = 0; t < nd; ++t) {
+    const int32_t r = order[t];
+    const int64_t l = p->rowptr[r + 1] - p->rowptr[r];
+    if (used + l > kAccMax) {
+      bstart.push_back(t);
+      used = 0;
+    }
+    used += l;
+    block_of[r] = (int32_t)bstart.size() - 1;
+  }
+  bstart.push_back(nd);
+  const int32_t nbk = (int32_t)bstart.size() - 1;
+  // owned rows per block, ascending row id; accumulator base of each row
+  std::vector<int32_t> row_acc_of(nd);
+  hs->rows.resize(nd);
+  hs->row_acc.resize(nd);
+  hs->blocks.assign(nbk, BlockDesc{});
+  for (int32_t b = 0; b < nbk; ++b) {
+    std::vector<int32_t> rs(order.begin() + bstart[b], order.begin() + bstart[b + 1]);
+    std::sort(rs.begin(), rs.end());
+    int32_t acc = 0;
+    for (size_t k = 0; k < rs.size(); ++k) {
+      hs->rows[bstart[b] + k] = rs[k];
+      hs->row_acc[bstart[b] + k] = acc;
+      row_acc_of[rs[k]] = acc;
+      acc += p->rowptr[rs[k] + 1] - p->rowptr[rs[k]];
+    }
+    hs->blocks[b].row_begin = (int32_t)bstart[b];
+    hs->blocks[b].row_count = (int32_t)(bstart[b + 1] - bstart[b]);
+    hs->blocks[b].acc_used = acc;
+  }
+  // items: (block, element) for every block an element touches, element order
+  std::vector<int64_t> bcount(nbk + 1, 0);
+  auto blocks_of_elem = [&](int64_t e, int32_t* out) {
+    int n = 0;
+    for (int i = 0; i < nb; ++i) {
+      int32_t b = block_of[m->dofs[e * nb + i]];
+      bool seen = false;
+      for (int u = 0; u < n; ++u) seen |= (out[u] == b);
+      if (!seen) out[n++] = b;
+    }
+    return n;
+  };
+  for (int64_t e = 0; e < E; ++e) {
+    int32_t bs[10];
+    int n = blocks_of_elem(e, bs);
+    for (int u = 0; u < n; ++u) bcount[bs[u] + 1]++;
+  }
+  for (int32_t b = 0; b < nbk; ++b) bcount[b + 1] += bcount[b];
+  if (bcount[nbk] >= INT32_MAX) return set_error(MG_ERR_SIZE, "assembly items above 2^31-1");
+  hs->items.resize(bcount[nbk]);
+  {
+    std::vector<int64_t> f(bcount.begin(), bcount.end() - 1);
+    for (int64_t e = 0; e < E; ++e) {
+      int32_t bs[10];
+      int n = blocks_of_elem(e, bs);
+      for (int u = 0; u < n; ++u) hs->items[f[bs[u]]++] = (int32_t)e;
+    }
+  }
+  int64_t nchunk_tot = 0;
+  for (int32_t b = 0; b < nbk; ++b) {
+    BlockDesc& d = hs->blocks[b];
+    d.item_begin = (int32_t)bcount[b];
+    d.item_count = (int32_t)(bcount[b + 1] - bcount[b]);
+    d.chunk_begin = (int32_t)nchunk_tot;
+    d.nchunks = (d.item_count + CI - 1) / CI;
+    nchunk_tot += d.nchunks;
+  }
+  // contribution lists, per block in parallel, then concatenated
+  std::vector<std::vector<uint32_t>> ent(nbk);
+  std::vector<std::vector<int64_t>> cptr(nbk);
+  std::vector<int64_t> contrib(nbk, 0);
+  const int32_t zero_src = CI * nb2;
+#pragma omp parallel
+  {
+    std::vector<std::vector<uint32_t>> per(kThreads);
+#pragma omp for schedule(dynamic, 1)
+    for (int32_t b = 0; b < nbk; ++b) {
+      const BlockDesc& d = hs->blocks[b];
+      for (int32_t c = 0; c < d.nchunks; ++c) {
+        for (auto& v : per) v.clear();
+        const int32_t i0 = c * CI, i1 = std::min(d.item_count, i0 + CI);
+        for (int32_t it = i0; it < i1; ++it) {
+          const int64_t e = hs->items[d.item_begin + it];
+          const int32_t t = it - i0;
+          for (int i = 0; i < nb; ++i) {      // field (column)
+            const int32_t col = m->dofs[e * nb + i];
+            for (int j = 0; j < nb; ++j) {    // test (row)
+              const int32_t row = m->dofs[e * nb + j];
+              if (block_of[row] != b) continue;
+              const int32_t* c0 = p->colind.data() + p->rowptr[row];
+              const int32_t* c1 = p->colind.data() + p->rowptr[row + 1];
+              const int32_t pos = (int32_t)(std::lower_bound(c0, c1, col) - c0);
+              const int32_t acc = row_acc_of[row] + pos;
+              const uint32_t src = (uint32_t)((i * nb + j) * CI + t);
+              per[acc % kThreads].push_back(((uint32_t)(acc / kThreads) << 16) | src);
+              contrib[b]++;
+            }
+          }
+        }
+        for (int w = 0; w < kWarps; ++w) {
+          cptr[b].push_back((int64_t)ent[b].size());
+          size_t K = 0;
+          for (int l = 0; l < 32; ++l) K = std::max(K, per[32 * w + l].size());
+          for (size_t k = 0; k < K; ++k)
+            for (int l = 0; l < 32; ++l) {
+              const auto& v = per[32 * w + l];
+              ent[b].push_back(k < v.size() ? v[k] : (uint32_t)zero_src);
+            }
+        }
+        cptr[b].push_back((int64_t)ent[b].size());
+      }
+    }
+  }
+  int64_t total = 0;
+  for (int32_t b = 0; b < nbk; ++b) total += (int64_t)ent[b].size();
+  hs->entries.resize(total);
+  hs->chunk_ptr.resize(nchunk_tot * (kWarps + 1));
+  int64_t off = 0, ck = 0;
+  for (int32_t b = 0; b < nbk; ++b) {
+    std::copy(ent[b].begin(), ent[b].end(), hs->entries.begin() + off);
+    for (size_t k = 0; k < cptr[b].size(); ++k) hs->chunk_ptr[ck * (kWarps + 1) + k] = cptr[b][k] + off;
+    ck += hs->blocks[b].nchunks;
+    off += (int64_t)ent[b].size();
+    hs->n_contrib += contrib[b];
+    std::vector<uint32_t>().swap(ent[b]);
+  }
+  p->nblocks = nbk;
+  p->n_items = (int64_t)hs->items.size();
+  p->n_chunks = nchunk_tot;
+  p->n_entries = total;
+  p->n_contrib = hs->n_contrib;
+  return MG_OK;
+}
+
+template <typename T>
+static mg_status upload(T** dst, const std::vector<T>& src)
+{
+  MG_CUDA(cudaMalloc(dst, sizeof(T) * std::max<size_t>(src.size(), 1)));
+  if (!src.empty()) MG_CUDA(cudaMemcpy(*dst, src.data(), sizeof(T) * src.size(), cudaMemcpyHostToDevice));
+  return MG_OK;
+}
+
+mg_status plan_device(mg_plan* p)
+{
+  if (p->on_device) return MG_OK;
+  MG_TRY(mesh_device(p->mesh));
+  const HostSchedule& hs = *p->host_schedule;
+  MG_TRY(upload(&p->d_rowptr, p->rowptr));
+  MG_TRY(upload(&p->d_colind, p->colind));
+  std::vector<int32_t> diag(p->ndof);
+  for (int64_t r = 0; r < p->ndof; ++r) {
+    const int32_t* c0 = p->colind.data() + p->rowptr[r];
+    const int32_t* c1 = p->colind.data() + p->rowptr[r + 1];
+    diag[r] = p->rowptr[r] + (int32_t)(std::lower_bound(c0, c1, (int32_t)r) - c0);
+  }
+  MG_TRY(upload(&p->d_diag, diag));
+  MG_TRY(upload(&p->d_blocks, hs.blocks));
+  MG_TRY(upload(&p->d_items, hs.items));
+  MG_TRY(upload(&p->d_chunk_ptr, hs.chunk_ptr));
+  MG_TRY(upload(&p->d_entries, hs.entries));
+  MG_TRY(upload(&p->d_rows, hs.rows));
+  MG_TRY(upload(&p->d_row_acc, hs.row_acc));
+  MG_CUDA(cudaMallocHost(&p->h_pinned, 64 * sizeof(double)));
+  delete p->host_schedule;
+  p->host_schedule = nullptr;
+  p->on_device = true;
+  return MG_OK;
+}
+
+static void free_plan(mg_plan* p)
+{
+  if (!p) return;
+  cudaFree(p->d_rowptr);
+  cudaFree(p->d_colind);
+  cudaFree(p->d_diag);
+  cudaFree(p->d_blocks);
+  cudaFree(p->d_items);
+  cudaFree(p->d_chunk_ptr);
+  cudaFree(p->d_entries);
+  cudaFree(p->d_rows);
+  cudaFree(p->d_row_acc);
+  for (double* t : p->d_tables) cudaFree(t);
+  cudaFree(p->d_work);
+  cudaFree(p->d_tmp_values);
+  cudaFree(p->d_tmp_coeff);
+  if (p->h_pinned) cudaFreeHost(p->h_pinned);
+  delete p->host_schedule;
+  delete p;
+}
+
+mg_status plan_tables(mg_plan* p, int quad, const RefTables** t, const double** d_tab)
+{
+  for (size_t k = 0; k < p->tables.size(); ++k)
+    if (p->tables[k].quad == quad) {
+      *t = &p->tables[k];
+      *d_tab = p->d_tables[k];
+      return MG_OK;
+    }
+  RefTables rt;
+  MG_TRY(build_ref_tables(p->mesh->order, quad, &rt));
+  std::vector<double> flat(rt.stiff);
+  flat.insert(flat.end(), rt.mass.begin(), rt.mass.end());
+  double* d = nullptr;
+  MG_CUDA(cudaMalloc(&d, sizeof(double) * flat.size()));
+  MG_CUDA(cudaMemcpy(d, flat.data(), sizeof(double) * flat.size(), cudaMemcpyHostToDevice));
+  p->tables.push_back(rt);
+  p->d_tables.push_back(d);
+  *t = &p->tables.back();
+  *d_tab = d;
+  return MG_OK;
+}
+
+mg_status plan_work(mg_plan* p, size_t bytes, void** ptr)
+{
+  if (p->work_bytes < bytes) {
+    cudaFree(p->d_work);
+    p->d_work = nullptr;
+    p->work_bytes = 0;
+    MG_CUDA(cudaMalloc(&p->d_work, bytes));
+    p->work_bytes = bytes;
+  }
+  *ptr = p->d_work;
+  return MG_OK;
+}
+
+}  // namespace mg
+
+using namespace mg;
+
+extern "C" {
+
+mg_status mg_pattern_build(mg_mesh* mesh, mg_plan** out)
+{
+  if (!mesh || !out) return set_error(MG_ERR_INVALID_ARG, "mg_pattern_build: null argument");
+  *out = nullptr;
+  mg_plan* p = new mg_plan();
+  p->mesh = mesh;
+  p->host_schedule = new HostSchedule();
+  mg_status s = build_pattern(p);
+  if (s == MG_OK) s = build_schedule(p, p->host_schedule);
+  if (s != MG_OK) {
+    free_plan(p);
+    return s;
+  }
+  *out = p;
+  return MG_OK;
+}
+
+mg_status mg_plan_destroy(mg_plan* plan)
+{
+  free_plan(plan);
+  return MG_OK;
+}
+
+mg_status mg_pattern_info(const mg_plan* p, int64_t* ndof, int64_t* nnz)
+{
+  if (!p) return set_error(MG_ERR_INVALID_ARG, "mg_pattern_info: null plan");
+  if (ndof) *ndof = p->ndof;
+  if (nnz) *nnz = p->nnz;
+  return MG_OK;
+}
+
+mg_status mg_pattern_export(const mg_plan* p, int32_t* h_rowptr, int32_t* h_colind)
+{
+  if (!p) return set_error(MG_ERR_INVALID_ARG, "mg_pattern_export: null plan");
+  if (h_rowptr) std::memcpy(h_rowptr, p->rowptr.data(), sizeof(int32_t) * p->rowptr.size());
+  if (h_colind) std::memcpy(h_colind, p->colind.data(), sizeof(int32_t) * p->colind.size());
+  return MG_OK;
+}
+
+mg_status mg_pattern_device(const mg_plan* pc, const int32_t** d_rowptr, const int32_t** d_colind)
+{
+  mg_plan* p = const_cast<mg_plan*>(pc);
+  if (!p) return set_error(MG_ERR_INVALID_ARG, "mg_pattern_device: null plan");
+  MG_TRY(plan_device(p));
+  if (d_rowptr) *d_rowptr = p->d_rowptr;
+  if (d_colind) *d_colind = p->d_colind;
+  return MG_OK;
+}
+
+mg_status mg_plan_schedule_info(const mg_plan* p, mg_schedule_info* info)
+{
+  if (!p || !info) return set_error(MG_ERR_INVALID_ARG, "mg_plan_schedule_info: null argument");
+  info->nblocks = p->nblocks;
+  info->threads = kThreads;
+  info->warps = kWarps;
+  info->acc_max = kAccMax;
+  info->chunk_items = chunk_items(p->mesh->order);
+  info->host_copy = p->host_schedule != nullptr;
+  info->n_items = p->n_items;
+  info->n_chunks = p->n_chunks;
+  info->n_entries = p->n_entries;
+  info->n_contrib = p->n_contrib;
+  return MG_OK;
+}
+
+mg_status mg_plan_export_schedule(const mg_plan* p, int32_t* h_blocks, int32_t* h_items,
+                                  int64_t* h_chunk_ptr, uint32_t* h_entries, int32_t* h_rows,
+                                  int32_t* h_row_acc)
+{
+  if (!p) return set_error(MG_ERR_INVALID_ARG, "mg_plan_export_schedule: null plan");
+  const HostSchedule* hs = p->host_schedule;
+  if (!hs)
+    return set_error(MG_ERR_UNSUPPORTED,
+                     "the host copy of the schedule is released once the plan is used on the GPU");
+  static_assert(sizeof(BlockDesc) == 8 * sizeof(int32_t), "BlockDesc layout");
+  if (h_blocks) std::memcpy(h_blocks, hs->blocks.data(), sizeof(BlockDesc) * hs->blocks.size());
+  if (h_items) std::memcpy(h_items, hs->items.data(), sizeof(int32_t) * hs->items.size());
+  if (h_chunk_ptr) std::memcpy(h_chunk_ptr, hs->chunk_ptr.data(), sizeof(int64_t) * hs->chunk_ptr.size());
+  if (h_entries) std::memcpy(h_entries, hs->entries.data(), sizeof(uint32_t) * hs->entries.size());
+  if (h_rows) std::memcpy(h_rows, hs->rows.data(), sizeof(int32_t) * hs->rows.size());
+  if (h_row_acc) std::memcpy(h_row_acc, hs->row_acc.data(), sizeof(int32_t) * hs->row_acc.size());
+  return MG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,584 @@
+// CSR SpMV and conjugate-gradient solvers for sm_103a.
+//
+// SpMV: a group of G lanes per row (G from the mean row length: 16 for P1
+// stiffness rows of ~15 entries, 32 for P2), values and column indices read
+// coalesced, x gathered through the read-only path, the row sum reduced with
+// xor shuffles in a fixed tree -- deterministic.
+//
+// CG: the reference hands the assembled Epetra operator to Belos BlockCG
+// (src/morganaTrilinos/belosBlockCG.hpp:46-82 in morganaPublic); here every
+// iteration is three kernels whose scalars (alpha, beta, r.z, r.r, a done flag)
+// live in device memory:
+//   K1  q = A p and per-CTA partials of p.q; the last CTA to finish (integer
+//       ticket) sums the partials in a fixed order and sets alpha = rz / pq;
+//   K2  x += alpha p, r -= alpha q, z = D^-1 r, partials of r.z and r.r; the last
+//       CTA forms beta, rz, rr and raises `done` when ||r|| <= tol ||b||;
+//   K3  p = z + beta p.
+// Once `done` is set the remaining kernels return at entry, so a CUDA graph of
+// several iterations can be replayed without a host round trip per iteration.
+// Dot products accumulate in FP64 in both precisions; the order of every
+// floating-point sum is fixed, so a solve is bitwise reproducible.
+#include <cmath>
+#include <vector>
+
+#include "mg_internal.h"
+
+namespace mg {
+
+constexpr int kSolveThreads = 256;
+constexpr int kMaxSolveBlocks = 1216;  // 8 CTAs of 256 threads on each of 152 SMs
+
+struct CgScalars {
+  double rz, alpha, beta, rr, bb, tol2, pq, pad;
+  int32_t done, iter, maxit, pad2;
+  uint32_t ticket[4];
+};
+
+static int row_group(const mg_plan* p)
+{
+  const double mean = p->ndof > 0 ? (double)p->nnz / (double)p->ndof : 1.0;
+  if (mean >= 24) return 32;
+  if (mean >= 12) return 16;
+  if (mean >= 6) return 8;
+  return 4;
+}
+
+template <int G>
+__device__ __forceinline__ unsigned group_mask()
+{
+  if constexpr (G == 32) {
+    return 0xffffffffu;
+  } else {
+    const unsigned lane = threadIdx.x & 31u;
+    return ((1u << G) - 1u) << (lane & ~(unsigned)(G - 1));
+  }
+}
+
+template <typename V, int G>
+__device__ __forceinline__ double row_dot(int64_t row, const int32_t* __restrict__ rp,
+                                          const int32_t* __restrict__ ci, const V* __restrict__ val,
+                                          const V* __restrict__ x)
+{
+  const int lane = threadIdx.x & (G - 1);
+  const int s0 = rp[row], s1 = rp[row + 1];
+  V sum = V(0);
+  for (int s = s0 + lane; s < s1; s += G) sum += val[s] * __ldg(x + ci[s]);
+#pragma unroll
+  for (int off = G / 2; off > 0; off >>= 1) sum += __shfl_xor_sync(group_mask<G>(), sum, off, G);
+  return (double)sum;
+}
+
+template <typename V, int G>
+__global__ void __launch_bounds__(kSolveThreads) k_spmv(int64_t n, const int32_t* __restrict__ rp,
+                                                        const int32_t* __restrict__ ci,
+                                                        const V* __restrict__ val, const V* __restrict__ x,
+                                                        V* __restrict__ y)
+{
+  const int64_t groups = (int64_t)gridDim.x * (kSolveThreads / G);
+  for (int64_t row = (blockIdx.x * (int64_t)kSolveThreads + threadIdx.x) / G; row < n; row += groups) {
+    const double s = row_dot<V, G>(row, rp, ci, val, x);
+    if ((threadIdx.x & (G - 1)) == 0) y[row] = (V)s;
+  }
+}
+
+__global__ void k_rowsum(int64_t n, const int32_t* rp, const double* val, double* y)
+{
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  double s = 0.0;
+  for (int k = rp[r]; k < rp[r + 1]; ++k) s += val[k];
+  y[r] = s;
+}
+
+// Block-wide sum of one double per thread in a fixed tree.
+__device__ __forceinline__ double block_sum(double v, double* sh)
+{
+  const int tid = threadIdx.x;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  if ((tid & 31) == 0) sh[tid >> 5] = v;
+  __syncthreads();
+  if (tid < 32) {
+    v = tid < (kSolveThreads / 32) ? sh[tid] : 0.0;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  }
+  __syncthreads();
+  return v;  // valid in thread 0
+}
+
+// Sum of partials[0..n) in a fixed order by one CTA (valid in thread 0).
+__device__ __forceinline__ double reduce_partials(const double* partials, int n, double* sh)
+{
+  double v = 0.0;
+  for (int i = threadIdx.x; i < n; i += kSolveThreads) v += partials[i];
+  return block_sum(v, sh);
+}
+
+// Last-CTA detection: returns true in the single CTA that finishes last.
+__device__ __forceinline__ bool last_block(uint32_t* ticket)
+{
+  __shared__ bool last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint32_t t = atomicAdd(ticket, 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (last) __threadfence();
+  return last;
+}
+
+// K1: q = A p, alpha = rz / (p . q)
+template <typename V, int G>
+__global__ void __launch_bounds__(kSolveThreads) k_cg_spmv(int64_t n, const int32_t* __restrict__ rp,
+                                                           const int32_t* __restrict__ ci,
+                                                           const V* __restrict__ val, const V* __restrict__ p,
+                                                           V* __restrict__ q, double* partials, CgScalars* s)
+{
+  __shared__ double sh[32];
+  if (s->done) return;
+  const int64_t groups = (int64_t)gridDim.x * (kSolveThreads / G);
+  double acc = 0.0;
+  for (int64_t row = (blockIdx.x * (int64_t)kSolveThreads + threadIdx.x) / G; row < n; row += groups) {
+    const double v = row_dot<V, G>(row, rp, ci, val, p);
+    if ((threadIdx.x & (G - 1)) == 0) {
+      q[row] = (V)v;
+      acc += (double)p[row] * (double)(V)v;
+    }
+  }
+  const double b = block_sum(acc, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = b;
+  if (last_block(&s->ticket[0])) {
+    const double pq = reduce_partials(partials, gridDim.x, sh);
+    if (threadIdx.x == 0) {
+      s->pq = pq;
+      s->alpha = s->rz / pq;
+      if (!(pq > 0.0) || !isfinite(s->alpha)) s->done = 2;  // breakdown: A not SPD on the Krylov space
+      s->ticket[0] = 0;
+    }
+  }
+}
+
+// K2: x += alpha p; r -= alpha q; z = D^-1 r; rz, rr, beta, convergence
+template <typename V>
+__global__ void __launch_bounds__(kSolveThreads) k_cg_update(int64_t n, V* __restrict__ x, V* __restrict__ r,
+                                                             V* __restrict__ z, const V* __restrict__ p,
+                                                             const V* __restrict__ q, const V* __restrict__ dinv,
+                                                             double* partials, CgScalars* s)
+{
+  __shared__ double sh[32];
+  if (s->done) return;
+  const V alpha = (V)s->alpha;
+  double prz = 0.0, prr = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)kSolveThreads + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * kSolveThreads) {
+    x[i] += alpha * p[i];
+    const V ri = r[i] - alpha * q[i];
+    r[i] = ri;
+    const V zi = dinv[i] * ri;
+    z[i] = zi;
+    prz += (double)ri * (double)zi;
+    prr += (double)ri * (double)ri;
+  }
+  const double b1 = block_sum(prz, sh);
+  const double b2 = block_sum(prr, sh);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = b1;
+    partials[gridDim.x + blockIdx.x] = b2;
+  }
+  if (last_block(&s->ticket[1])) {
+    const double rz = reduce_partials(partials, gridDim.x, sh);
+    const double rr = reduce_partials(partials + gridDim.x, gridDim.x, sh);
+    if (threadIdx.x == 0) {
+      s->beta = rz / s->rz;
+      s->rz = rz;
+      s->rr = rr;
+      s->iter += 1;
+      if (rr <= s->tol2 * s->bb) s->done = 1;
+      else if (s->iter >= s->maxit) s->done = 3;
+      s->ticket[1] = 0;
+    }
+  }
+}
+
+// K3: p = z + beta p
+template <typename V>
+__global__ void __launch_bounds__(kSolveThreads) k_cg_dir(int64_t n, const V* __restrict__ z, V* __restrict__ p,
+                                                          const CgScalars* s)
+{
+  if (s->done) return;
+  const V beta = (V)s->beta;
+  for (int64_t i = blockIdx.x * (int64_t)kSolveThreads + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * kSolveThreads)
+    p[i] = z[i] + beta * p[i];
+}
+
+// Start of a solve: r = b - A x (or r = b when x is zero), z = D^-1 r, p = z,
+// D^-1 from the diagonal, partials of r.z, r.r, b.b.
+template <typename V, int G>
+__global__ void __launch_bounds__(kSolveThreads) k_cg_start(int64_t n, const int32_t* __restrict__ rp,
+                                                            const int32_t* __restrict__ ci,
+                                                            const V* __restrict__ val, const int32_t* __restrict__ diag,
+                                                            const V* __restrict__ b, const V* __restrict__ x,
+                                                            int zero_x, int jacobi, V* __restrict__ r,
+                                                            V* __restrict__ z, V* __restrict__ p,
+                                                            V* __restrict__ dinv, double* partials, CgScalars* s)
+{
+  __shared__ double sh[32];
+  const int64_t groups = (int64_t)gridDim.x * (kSolveThreads / G);
+  double prz = 0.0, prr = 0.0, pbb = 0.0;
+  for (int64_t row = (blockIdx.x * (int64_t)kSolveThreads + threadIdx.x) / G; row < n; row += groups) {
+    double ax = 0.0;
+    if (!zero_x) ax = row_dot<V, G>(row, rp, ci, val, x);
+    if ((threadIdx.x & (G - 1)) == 0) {
+      const V dv = val[diag[row]];
+      const V di = (jacobi && dv != V(0)) ? V(1) / dv : V(1);
+      const V ri = (V)((double)b[row] - ax);
+      const V zi = di * ri;
+      dinv[row] = di;
+      r[row] = ri;
+      z[row] = zi;
+      p[row] = zi;
+      prz += (double)ri * (double)zi;
+      prr += (double)ri * (double)ri;
+      pbb += (double)b[row] * (double)b[row];
+    }
+  }
+  const double b1 = block_sum(prz, sh), b2 = block_sum(prr, sh), b3 = block_sum(pbb, sh);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = b1;
+    partials[gridDim.x + blockIdx.x] = b2;
+    partials[2 * gridDim.x + blockIdx.x] = b3;
+  }
+  if (last_block(&s->ticket[2])) {
+    const double rz = reduce_partials(partials, gridDim.x, sh);
+    const double rr = reduce_partials(partials + gridDim.x, gridDim.x, sh);
+    const double bb = reduce_partials(partials + 2 * gridDim.x, gridDim.x, sh);
+    if (threadIdx.x == 0) {
+      s->rz = rz;
+      s->rr = rr;
+      s->bb = bb > 0.0 ? bb : 1.0;
+      s->iter = 0;
+      s->done = (rr <= s->tol2 * s->bb) ? 1 : 0;
+      s->ticket[2] = 0;
+    }
+  }
+}
+
+// Refinement residual: r64 = b - A64 x, rr = r64 . r64 (last CTA), and the
+// scaled FP32 right-hand side r32 = r64 / ||r64|| is written by k_scale_cast.
+template <int G>
+__global__ void __launch_bounds__(kSolveThreads) k_residual64(int64_t n, const int32_t* __restrict__ rp,
+                                                              const int32_t* __restrict__ ci,
+                                                              const double* __restrict__ val,
+                                                              const double* __restrict__ b,
+                                                              const double* __restrict__ x,
+                                                              double* __restrict__ r, double* partials,
+                                                              CgScalars* s)
+{
+  __shared__ double sh[32];
+  const int64_t groups = (int64_t)gridDim.x * (kSolveThreads / G);
+  double prr = 0.0, pbb = 0.0;
+  for (int64_t row = (blockIdx.x * (int64_t)kSolveThreads + threadIdx.x) / G; row < n; row += groups) {
+    const double ax = row_dot<double, G>(row, rp, ci, val, x);
+    if ((threadIdx.x & (G - 1)) == 0) {
+      const double ri = b[row] - ax;
+      r[row] = ri;
+      prr += ri * ri;
+      pbb += b[row] * b[row];
+    }
+  }
+  const double b1 = block_sum(prr, sh), b2 = block_sum(pbb, sh);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = b1;
+    partials[gridDim.x + blockIdx.x] = b2;
+  }
+  if (last_block(&s->ticket[3])) {
+    const double rr = reduce_partials(partials, gridDim.x, sh);
+    const double bb = reduce_partials(partials + gridDim.x, gridDim.x, sh);
+    if (threadIdx.x == 0) {
+      s->rr = rr;
+      s->bb = bb > 0.0 ? bb : 1.0;
+      s->ticket[3] = 0;
+    }
+  }
+}
+
+__global__ void k_scale_cast(int64_t n, const double* r, double scale, float* r32, float* d32)
+{
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    r32[i] = (float)(r[i] * scale);
+    d32[i] = 0.0f;
+  }
+}
+
+__global__ void k_correct(int64_t n, double* x, const float* d32, double scale)
+{
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    x[i] += scale * (double)d32[i];
+}
+
+static int solve_blocks(const mg_plan* p, int G)
+{
+  const int64_t rows_per_block = kSolveThreads / G;
+  const int64_t need = (p->ndof + rows_per_block - 1) / rows_per_block;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(need, kMaxSolveBlocks));
+}
+
+#define MG_DISPATCH_G(G, ...)          \
+  switch (G) {                          \
+    case 32: { constexpr int g = 32; __VA_ARGS__; } break; \
+    case 16: { constexpr int g = 16; __VA_ARGS__; } break; \
+    case 8: { constexpr int g = 8; __VA_ARGS__; } break;   \
+    default: { constexpr int g = 4; __VA_ARGS__; } break;  \
+  }
+
+mg_status launch_spmv(mg_plan* p, int prec, const void* vals, const void* x, void* y, cudaStream_t st)
+{
+  if (prec != MG_F64 && prec != MG_F32) return set_error(MG_ERR_INVALID_ARG, "bad precision");
+  if (!vals || !x || !y) return set_error(MG_ERR_INVALID_ARG, "mg_spmv: null argument");
+  MG_TRY(plan_device(p));
+  const int G = row_group(p);
+  const int nb = solve_blocks(p, G);
+  if (p->ndof == 0) return MG_OK;
+  if (prec == MG_F64) {
+    MG_DISPATCH_G(G, (k_spmv<double, g><<<nb, kSolveThreads, 0, st>>>(p->ndof, p->d_rowptr, p->d_colind,
+                                                                         (const double*)vals, (const double*)x,
+                                                                         (double*)y)));
+  } else {
+    MG_DISPATCH_G(G, (k_spmv<float, g><<<nb, kSolveThreads, 0, st>>>(p->ndof, p->d_rowptr, p->d_colind,
+                                                                        (const float*)vals, (const float*)x,
+                                                                        (float*)y)));
+  }
+  MG_CUDA(cudaGetLastError());
+  return MG_OK;
+}
+
+mg_status launch_rowsum(mg_plan* p, const double* vals, double* y, cudaStream_t st)
+{
+  MG_TRY(plan_device(p));
+  const int blocks = (int)((p->ndof + 255) / 256);
+  if (blocks > 0) k_rowsum<<<blocks, 256, 0, st>>>(p->ndof, p->d_rowptr, vals, y);
+  MG_CUDA(cudaGetLastError());
+  return MG_OK;
+}
+
+// Workspace of one CG run over vectors of type V.
+template <typename V>
+struct CgWork {
+  V *r, *z, *p, *q, *dinv;
+  double* partials;  // 3 * kMaxSolveBlocks
+  CgScalars* s;
+};
+
+template <typename V>
+static size_t cg_work_bytes(int64_t n)
+{
+  const size_t vec = ((size_t)n * sizeof(V) + 255) / 256 * 256;
+  return 5 * vec + 3 * kMaxSolveBlocks * sizeof(double) + 256;
+}
+
+template <typename V>
+static CgWork<V> cg_work_carve(void* base, int64_t n)
+{
+  char* c = (char*)base;
+  const size_t vec = ((size_t)n * sizeof(V) + 255) / 256 * 256;
+  CgWork<V> w;
+  w.s = (CgScalars*)c;
+  c += 256;
+  w.partials = (double*)c;
+  c += 3 * kMaxSolveBlocks * sizeof(double);
+  w.r = (V*)c; c += vec;
+  w.z = (V*)c; c += vec;
+  w.p = (V*)c; c += vec;
+  w.q = (V*)c; c += vec;
+  w.dinv = (V*)c;
+  return w;
+}
+
+// Iterations per replay of the captured CG graph between two host checks.
+constexpr int kGraphIters = 16;
+
+// Runs CG on A (vals) from the state set up by k_cg_start until `done`.
+template <typename V>
+static mg_status cg_iterate(mg_plan* p, const V* vals, V* x, CgWork<V>& w, int G, int nb, int maxit,
+                            cudaStream_t st, CgScalars* h_s)
+{
+  const int64_t n = p->ndof;
+  const int vb = (int)std::max<int64_t>(1, std::min<int64_t>((n + kSolveThreads - 1) / kSolveThreads, kMaxSolveBlocks));
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  bool use_graph = true;
+  cudaStreamCaptureStatus cs;
+  MG_CUDA(cudaStreamIsCapturing(st, &cs));
+  if (cs != cudaStreamCaptureStatusNone || st == nullptr) use_graph = false;  // no nested capture; legacy stream cannot capture
+  auto body = [&]() {
+    MG_DISPATCH_G(G, (k_cg_spmv<V, g><<<nb, kSolveThreads, 0, st>>>(n, p->d_rowptr, p->d_colind, vals, w.p, w.q,
+                                                                      w.partials, w.s)));
+    k_cg_update<V><<<vb, kSolveThreads, 0, st>>>(n, x, w.r, w.z, w.p, w.q, w.dinv, w.partials, w.s);
+    k_cg_dir<V><<<vb, kSolveThreads, 0, st>>>(n, w.z, w.p, w.s);
+  };
+  if (use_graph) {
+    MG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    for (int k = 0; k < kGraphIters; ++k) body();
+    MG_CUDA(cudaStreamEndCapture(st, &graph));
+    MG_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+  }
+  mg_status status = MG_OK;
+  for (int launched = 0;; launched += kGraphIters) {
+    if (use_graph) {
+      cudaError_t e = cudaGraphLaunch(exec, st);
+      if (e != cudaSuccess) { status = cuda_error(e, "cudaGraphLaunch"); break; }
+    } else {
+      for (int k = 0; k < kGraphIters; ++k) body();
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) { status = cuda_error(e, "cg kernels"); break; }
+    }
+    cudaError_t e = cudaMemcpyAsync(h_s, w.s, sizeof(CgScalars), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) { status = cuda_error(e, "cg scalars"); break; }
+    if (h_s->done) break;
+    if (launched + kGraphIters > maxit + kGraphIters) break;
+  }
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
+  return status;
+}
+
+template <typename V>
+static mg_status cg_start(mg_plan* p, const V* vals, const V* b, const V* x, int zero_x, int jacobi,
+                          double tol, int maxit, CgWork<V>& w, int G, int nb, cudaStream_t st)
+{
+  CgScalars init{};
+  init.tol2 = tol * tol;
+  init.maxit = maxit;
+  MG_CUDA(cudaMemcpyAsync(w.s, &init, sizeof(CgScalars), cudaMemcpyHostToDevice, st));
+  const int64_t n = p->ndof;
+  MG_DISPATCH_G(G, (k_cg_start<V, g><<<nb, kSolveThreads, 0, st>>>(n, p->d_rowptr, p->d_colind, vals, p->d_diag, b,
+                                                                     x, zero_x, jacobi, w.r, w.z, w.p, w.dinv,
+                                                                     w.partials, w.s)));
+  MG_CUDA(cudaGetLastError());
+  return MG_OK;
+}
+
+}  // namespace mg
+
+using namespace mg;
+
+extern "C" {
+
+mg_status mg_spmv(mg_plan* plan, int32_t prec, const void* d_values, const void* d_x, void* d_y, void* stream)
+{
+  if (!plan) return set_error(MG_ERR_INVALID_ARG, "mg_spmv: null plan");
+  return launch_spmv(plan, prec, d_values, d_x, d_y, (cudaStream_t)stream);
+}
+
+mg_status mg_cg_solve(mg_plan* p, const double* d_values, const double* d_b, double* d_x, double rtol,
+                      int32_t maxit, int32_t precond, mg_cg_info* info, void* stream)
+{
+  if (!p || !d_values || !d_b || !d_x) return set_error(MG_ERR_INVALID_ARG, "mg_cg_solve: null argument");
+  if (!(rtol > 0.0) || maxit < 0) return set_error(MG_ERR_INVALID_ARG, "mg_cg_solve: rtol must be > 0, maxit >= 0");
+  MG_TRY(plan_device(p));
+  cudaStream_t st = (cudaStream_t)stream;
+  void* base = nullptr;
+  MG_TRY(plan_work(p, cg_work_bytes<double>(p->ndof), &base));
+  CgWork<double> w = cg_work_carve<double>(base, p->ndof);
+  const int G = row_group(p), nb = solve_blocks(p, G);
+  cudaEvent_t e0, e1;
+  MG_CUDA(cudaEventCreate(&e0));
+  MG_CUDA(cudaEventCreate(&e1));
+  MG_CUDA(cudaEventRecord(e0, st));
+  CgScalars* hs = reinterpret_cast<CgScalars*>(p->h_pinned);
+  mg_status s = cg_start<double>(p, d_values, d_b, d_x, 0, precond == MG_PREC_JACOBI, rtol, maxit, w, G, nb, st);
+  if (s == MG_OK) s = cg_iterate<double>(p, d_values, d_x, w, G, nb, maxit, st, hs);
+  MG_CUDA(cudaEventRecord(e1, st));
+  MG_CUDA(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (s != MG_OK) return s;
+  MG_CUDA(cudaMemcpy(hs, w.s, sizeof(CgScalars), cudaMemcpyDeviceToHost));
+  if (info) {
+    info->iterations = hs->iter;
+    info->outer_iterations = 0;
+    info->converged = hs->done == 1;
+    info->rel_residual = std::sqrt(hs->rr / hs->bb);
+    info->seconds = ms * 1e-3;
+  }
+  if (hs->done == 2) return set_error(MG_ERR_NOT_CONVERGED, "CG breakdown: p.Ap <= 0");
+  if (hs->done != 1) return set_error(MG_ERR_NOT_CONVERGED, "CG reached maxit");
+  return MG_OK;
+}
+
+mg_status mg_cg_refined(mg_plan* p, const double* d_values64, const float* d_values32, const double* d_b,
+                        double* d_x, double rtol, int32_t max_outer, int32_t max_inner, double inner_rtol,
+                        int32_t precond, mg_cg_info* info, void* stream)
+{
+  if (!p || !d_values64 || !d_values32 || !d_b || !d_x)
+    return set_error(MG_ERR_INVALID_ARG, "mg_cg_refined: null argument");
+  if (!(rtol > 0.0) || !(inner_rtol > 0.0) || max_outer < 1 || max_inner < 1)
+    return set_error(MG_ERR_INVALID_ARG, "mg_cg_refined: bad tolerance or iteration limits");
+  MG_TRY(plan_device(p));
+  cudaStream_t st = (cudaStream_t)stream;
+  const int64_t n = p->ndof;
+  // layout: [CgWork<float>][r64][d32][r32]
+  const size_t wbytes = cg_work_bytes<float>(n);
+  const size_t v64 = ((size_t)n * 8 + 255) / 256 * 256, v32 = ((size_t)n * 4 + 255) / 256 * 256;
+  void* base = nullptr;
+  MG_TRY(plan_work(p, wbytes + v64 + 2 * v32, &base));
+  CgWork<float> w = cg_work_carve<float>(base, n);
+  double* r64 = (double*)((char*)base + wbytes);
+  float* d32 = (float*)((char*)r64 + v64);
+  float* r32 = (float*)((char*)d32 + v32);
+  const int G = row_group(p), nb = solve_blocks(p, G);
+  const int eb = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 4 * kMaxSolveBlocks));
+  CgScalars* hs = reinterpret_cast<CgScalars*>(p->h_pinned);
+  MG_CUDA(cudaMemsetAsync(w.s, 0, sizeof(CgScalars), st));
+  cudaEvent_t e0, e1;
+  MG_CUDA(cudaEventCreate(&e0));
+  MG_CUDA(cudaEventCreate(&e1));
+  MG_CUDA(cudaEventRecord(e0, st));
+  int outer = 0, inner_total = 0;
+  bool converged = false;
+  double relres = INFINITY;
+  mg_status s = MG_OK;
+  for (; outer <= max_outer; ++outer) {
+    MG_DISPATCH_G(G, (k_residual64<g><<<nb, kSolveThreads, 0, st>>>(n, p->d_rowptr, p->d_colind, d_values64, d_b,
+                                                                      d_x, r64, w.partials, w.s)));
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hs, w.s, sizeof(CgScalars), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) { s = cuda_error(e, "refinement residual"); break; }
+    relres = std::sqrt(hs->rr / hs->bb);
+    if (relres <= rtol) { converged = true; break; }
+    if (outer == max_outer) break;
+    const double rn = std::sqrt(hs->rr);
+    k_scale_cast<<<eb, 256, 0, st>>>(n, r64, 1.0 / rn, r32, d32);
+    s = cg_start<float>(p, d_values32, r32, d32, 1, precond == MG_PREC_JACOBI, inner_rtol, max_inner, w, G, nb, st);
+    if (s == MG_OK) s = cg_iterate<float>(p, d_values32, d32, w, G, nb, max_inner, st, hs);
+    if (s != MG_OK) break;
+    inner_total += hs->iter;
+    k_correct<<<eb, 256, 0, st>>>(n, d_x, d32, rn);
+  }
+  MG_CUDA(cudaEventRecord(e1, st));
+  MG_CUDA(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (s != MG_OK) return s;
+  if (info) {
+    info->iterations = inner_total;
+    info->outer_iterations = outer;
+    info->converged = converged;
+    info->rel_residual = relres;
+    info->seconds = ms * 1e-3;
+  }
+  if (!converged) return set_error(MG_ERR_NOT_CONVERGED, "refinement reached max_outer");
+  return MG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,174 @@
+"""ctypes front end of the CPU oracle (morgana_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: the checker the parity tests, the smoke check and the
+cpu_baseline leg of bench.py compare the CUDA path against.  The product
+package never imports this module.
+
+Each wrapper returns numpy arrays with 0-based indices; see morgana_oracle.c for
+the reference file:line each function restates.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libmorgana_oracle.so")
+
+OPS = {"stiff_kappa": 0, "stiff_const": 1, "mass": 2, "mass_coeff": 3}
+EDGES = {"lex": 0, "first": 1}
+# quadrature names of the product (1, 4, 15, 64 points) -> reference card precision
+QUAD_PREC = {1: 1, 4: 2, 15: 3, 64: 4}
+
+_lib = None
+
+
+def build() -> str:
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        P, I64, I32, D = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_double
+        L.or_quad_rule.argtypes = [I32, P, P]
+        L.or_local_matrix.argtypes = [I32, I32, I32, P, P, D, D, P]
+        L.or_element_det.argtypes = [P, P]
+        L.or_element_det.restype = D
+        L.or_check_jacobian.argtypes = [I64, P, P, P, P]
+        L.or_build_edges.argtypes = [I64, I64, P, I32, P, P, P]
+        L.or_elem_dofs.argtypes = [I32, I64, I64, P, P, P]
+        L.or_pattern.argtypes = [I32, I64, I64, P, P, P, I64, P]
+        L.or_assemble_values.argtypes = [I32, I32, I32, P, I64, P, P, P, D, P, P, I64, P]
+        L.or_assemble_rhs.argtypes = [I32, I32, P, I64, P, P, P, P, I64, P]
+        L.or_apply_dirichlet.argtypes = [I64, P, P, P, P, P]
+        L.or_spmv.argtypes = [I64, P, P, P, P, P]
+        L.or_cg.argtypes = [I64, P, P, P, P, P, D, I32, I32, P, P]
+        L.or_adjoint_grad.argtypes = [I32, I32, P, I64, P, P, P, P, P]
+        L.or_basis_eval.argtypes = [I32, P, P]
+        L.or_basis_grad.argtypes = [I32, P, P, P, P]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def quad_rule(quad: int):
+    Y = np.empty((64, 3))
+    W = np.empty(64)
+    n = lib().or_quad_rule(QUAD_PREC[quad], _p(Y), _p(W))
+    return Y[:n].copy(), W[:n].copy()
+
+
+def local_matrix(op, order, quad, xyz, nodes4, kappa=1.0, c=1.0):
+    nb = 4 if order == 1 else 10
+    mat = np.empty(nb * nb)
+    nodes4 = np.ascontiguousarray(nodes4, dtype=np.int32)
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    rc = lib().or_local_matrix(OPS[op], order, QUAD_PREC[quad], _p(xyz), _p(nodes4), kappa, c, _p(mat))
+    assert rc == 0
+    return mat.reshape(nb, nb)  # [field i, test j]
+
+
+def check_jacobian(xyz, conn):
+    mn = ctypes.c_double()
+    bad = ctypes.c_int64()
+    rc = lib().or_check_jacobian(conn.shape[0], _p(xyz), _p(conn), ctypes.byref(mn), ctypes.byref(bad))
+    return rc, mn.value, bad.value
+
+
+def edges(n_nodes, conn, rule="lex"):
+    conn = np.ascontiguousarray(conn, dtype=np.int32)
+    E = conn.shape[0]
+    ee = np.empty((E, 6), dtype=np.int32)
+    en = np.empty((6 * E, 2), dtype=np.int32)
+    ne = ctypes.c_int64()
+    assert lib().or_build_edges(n_nodes, E, _p(conn), EDGES[rule], _p(ee), _p(en), ctypes.byref(ne)) == 0
+    return en[: ne.value].copy(), ee
+
+
+def elem_dofs(order, n_nodes, conn, elem_edge=None):
+    conn = np.ascontiguousarray(conn, dtype=np.int32)
+    nb = 4 if order == 1 else 10
+    out = np.empty((conn.shape[0], nb), dtype=np.int32)
+    ee = np.zeros((conn.shape[0], 6), dtype=np.int32) if elem_edge is None else np.ascontiguousarray(elem_edge)
+    lib().or_elem_dofs(order, n_nodes, conn.shape[0], _p(conn), _p(ee), _p(out))
+    return out
+
+
+def pattern(order, ndof, dofs):
+    nb = dofs.shape[1]
+    cap = dofs.shape[0] * nb * nb + 1
+    rp = np.empty(ndof + 1, dtype=np.int32)
+    ci = np.empty(cap, dtype=np.int32)
+    nnz = ctypes.c_int64()
+    assert lib().or_pattern(order, ndof, dofs.shape[0], _p(dofs), _p(rp), _p(ci), cap, ctypes.byref(nnz)) == 0
+    return rp, ci[: nnz.value].copy()
+
+
+def assemble(op, order, quad, xyz, conn, dofs, rowptr, colind, coeff=None, c=1.0):
+    vals = np.empty(colind.shape[0])
+    cf = None if coeff is None else np.ascontiguousarray(coeff, dtype=np.float64)
+    rc = lib().or_assemble_values(OPS[op], order, QUAD_PREC[quad], _p(xyz), conn.shape[0], _p(conn), _p(dofs),
+                                  _p(cf), c, _p(rowptr), _p(colind), rowptr.shape[0] - 1, _p(vals))
+    assert rc == 0
+    return vals
+
+
+def assemble_rhs(order, quad, xyz, conn, dofs, ndof, field=None, elem_scale=None):
+    b = np.empty(ndof)
+    f = None if field is None else np.ascontiguousarray(field, dtype=np.float64)
+    s = None if elem_scale is None else np.ascontiguousarray(elem_scale, dtype=np.float64)
+    assert lib().or_assemble_rhs(order, QUAD_PREC[quad], _p(xyz), conn.shape[0], _p(conn), _p(dofs), _p(f),
+                                 _p(s), ndof, _p(b)) == 0
+    return b
+
+
+def apply_dirichlet(rowptr, colind, mask, values, b=None):
+    m = np.ascontiguousarray(mask, dtype=np.uint8)
+    lib().or_apply_dirichlet(rowptr.shape[0] - 1, _p(rowptr), _p(colind), _p(m), _p(values), _p(b))
+
+
+def spmv(rowptr, colind, values, x):
+    y = np.empty(rowptr.shape[0] - 1)
+    lib().or_spmv(rowptr.shape[0] - 1, _p(rowptr), _p(colind), _p(values), _p(np.ascontiguousarray(x)), _p(y))
+    return y
+
+
+def cg(rowptr, colind, values, b, rtol=1e-10, maxit=10000, precond=1, x0=None):
+    x = np.zeros_like(b) if x0 is None else x0.copy()
+    it = ctypes.c_int()
+    rr = ctypes.c_double()
+    rc = lib().or_cg(rowptr.shape[0] - 1, _p(rowptr), _p(colind), _p(values), _p(b), _p(x), rtol, maxit, precond,
+                     ctypes.byref(it), ctypes.byref(rr))
+    return x, it.value, rr.value, rc
+
+
+def adjoint_grad(order, quad, xyz, conn, dofs, u, lam):
+    g = np.empty(conn.shape[0])
+    assert lib().or_adjoint_grad(order, QUAD_PREC[quad], _p(xyz), conn.shape[0], _p(conn), _p(dofs),
+                                 _p(np.ascontiguousarray(u)), _p(np.ascontiguousarray(lam)), _p(g)) == 0
+    return g
+
+
+def full_operator(op, order, quad, xyz, conn, coeff=None, c=1.0, edge_rule="lex"):
+    """Everything the reference builds for one bilinear form: dofs, pattern, values."""
+    n_nodes = xyz.shape[0]
+    ee = None
+    ndof = n_nodes
+    if order == 2:
+        en, ee = edges(n_nodes, conn, edge_rule)
+        ndof = n_nodes + en.shape[0]
+    dofs = elem_dofs(order, n_nodes, conn, ee)
+    rp, ci = pattern(order, ndof, dofs)
+    vals = assemble(op, order, quad, xyz, conn, dofs, rp, ci, coeff, c)
+    return dofs, rp, ci, vals

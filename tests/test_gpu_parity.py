@@ -1,0 +1,238 @@
+"""GPU parity tests: the CUDA path through the C ABI against the CPU oracle.
+
+Tolerances: CSR pattern and dof numbering bit-exact; FP64 values row-scaled
+|a-b| <= 1e-12 max(|a|, max_j |A_row,j|); FP32 values row-scaled 2e-6;
+solutions against the FP64 oracle solution at the stated tolerances."""
+import numpy as np
+import pytest
+
+import morganapublic_gb300 as mg
+import oracle as orc
+from morganapublic_gb300 import meshgen
+from helpers import row_scaled_err
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("no CUDA device", allow_module_level=True)
+
+F64_TOL = 1e-12
+F32_TOL = 2e-6
+
+
+def _case(n, jitter, seed, permute, sigma):
+    m = meshgen.kuhn_cube(n, jitter=jitter, seed=seed, permute=permute)
+    kappa = meshgen.lognormal(len(m.conn), sigma, seed + 100) if sigma > 0 else np.ones(len(m.conn))
+    return m, kappa
+
+
+@pytest.mark.parametrize("op", ["stiff_kappa", "stiff_const", "mass", "mass_coeff"])
+@pytest.mark.parametrize("quad", [1, 4, 15])
+def test_p1_assembly_f64(op, quad):
+    m, kappa = _case(6, 0.2, 1, True, 1.0)
+    mesh = mg.Mesh(m.xyz, m.conn, order=1)
+    b = mg.MatrixBuilder(mesh)
+    dofs, rp, ci, ref = orc.full_operator(op, 1, quad, m.xyz, m.conn, coeff=kappa, c=2.5)
+    vals = b.assemble(op, coeff=kappa, c=2.5, quad=quad, prec="f64").cpu().numpy()
+    rph, cih = b.pattern()
+    assert np.array_equal(rph, rp) and np.array_equal(cih, ci)
+    assert row_scaled_err(rp, ref, vals) <= F64_TOL
+
+
+@pytest.mark.parametrize("op", ["stiff_kappa", "mass"])
+def test_p1_assembly_f32(op):
+    m, kappa = _case(6, 0.25, 3, True, 1.5)
+    b = mg.MatrixBuilder(mg.Mesh(m.xyz, m.conn, order=1))
+    _, rp, ci, ref = orc.full_operator(op, 1, 4, m.xyz, m.conn, coeff=kappa)
+    vals = b.assemble(op, coeff=kappa, quad=4, prec="f32").cpu().numpy()
+    assert vals.dtype == np.float32
+    assert row_scaled_err(rp, ref, vals) <= F32_TOL
+
+
+@pytest.mark.parametrize("op", ["stiff_kappa", "mass", "stiff_const", "mass_coeff"])
+@pytest.mark.parametrize("rule", ["lex", "first"])
+def test_p2_assembly_f64(op, rule):
+    m, kappa = _case(3, 0.2, 2, True, 0.5)
+    mesh = mg.Mesh(m.xyz, m.conn, order=2, edge_rule=rule)
+    b = mg.MatrixBuilder(mesh)
+    dofs, rp, ci, ref = orc.full_operator(op, 2, 15, m.xyz, m.conn, coeff=kappa, c=0.75, edge_rule=rule)
+    assert np.array_equal(mesh.elem_dofs(), dofs)
+    for quad in (15, 11):  # Keast 11 is exact for these degree <= 4 integrands on affine tets
+        vals = b.assemble(op, coeff=kappa, c=0.75, quad=quad, prec="f64").cpu().numpy()
+        assert row_scaled_err(rp, ref, vals) <= F64_TOL, quad
+
+
+def test_p2_assembly_f32():
+    m, kappa = _case(3, 0.2, 2, True, 0.5)
+    b = mg.MatrixBuilder(mg.Mesh(m.xyz, m.conn, order=2))
+    _, rp, ci, ref = orc.full_operator("stiff_kappa", 2, 15, m.xyz, m.conn, coeff=kappa)
+    vals = b.assemble("stiff_kappa", coeff=kappa, quad=11, prec="f32").cpu().numpy()
+    assert row_scaled_err(rp, ref, vals) <= 2 * F32_TOL
+
+
+def test_assembly_deterministic_and_host_entry():
+    m, kappa = _case(8, 0.25, 3, True, 1.5)
+    b = mg.MatrixBuilder(mg.Mesh(m.xyz, m.conn, order=1))
+    v1 = b.assemble("stiff_kappa", coeff=kappa, prec="f64")
+    v2 = b.assemble("stiff_kappa", coeff=kappa, prec="f64")
+    assert torch.equal(v1, v2)
+    crs = b.build_crs("stiff_kappa", coeff=kappa, prec="f64")
+    assert np.array_equal(crs.values, v1.cpu().numpy())
+
+
+def test_config1_laplace_and_mass_16():
+    """The reference's CPU-runnable case: P1 16^3 Kuhn cube, kappa = 1, 4-point rule."""
+    m = meshgen.kuhn_cube(16)
+    b = mg.MatrixBuilder(mg.Mesh(m.xyz, m.conn, order=1))
+    assert (b.ndof, b.nnz) == (4913, 66961)
+    for op in ("stiff_kappa", "mass"):
+        _, rp, ci, ref = orc.full_operator(op, 1, 4, m.xyz, m.conn, coeff=np.ones(len(m.conn)))
+        vals = b.assemble(op, coeff=np.ones(len(m.conn)), quad=4, prec="f64").cpu().numpy()
+        assert row_scaled_err(rp, ref, vals) <= F64_TOL
+
+
+def test_spmv_matches_oracle():
+    m, kappa = _case(8, 0.2, 1, True, 1.0)
+    b = mg.MatrixBuilder(mg.Mesh(m.xyz, m.conn, order=1))
+    _, rp, ci, ref = orc.full_operator("stiff_kappa", 1, 4, m.xyz, m.conn, coeff=kappa)
+    x = np.random.default_rng(0).uniform(-1, 1, b.ndof)
+    y_ref = orc.spmv(rp, ci, ref, x)
+    vals = b.assemble("stiff_kappa", coeff=kappa, prec="f64")
+    y = b.apply(vals, torch.from_numpy(x).cuda()).cpu().numpy()
+    scale = np.abs(ref).max() * np.abs(x).max()
+    assert np.max(np.abs(y - y_ref)) <= 1e-13 * scale * 27
+    v32 = b.assemble("stiff_kappa", coeff=kappa, prec="f32")
+    y32 = b.apply(v32, torch.from_numpy(x.astype(np.float32)).cuda()).cpu().numpy()
+    assert np.max(np.abs(y32 - y_ref)) <= 1e-5 * scale
+
+
+def _dirichlet_system(n, order, sigma, seed):
+    m, kappa = _case(n, 0.2, seed, True, sigma)
+    mesh = mg.Mesh(m.xyz, m.conn, order=order)
+    b = mg.MatrixBuilder(mesh)
+    quad = 4 if order == 1 else 15
+    dofs, rp, ci, K = orc.full_operator("stiff_kappa", order, quad, m.xyz, m.conn, coeff=kappa)
+    mask = m.boundary if order == 1 else meshgen.p2_boundary(m.boundary, mesh.edges()[0])
+    rhs = orc.assemble_rhs(order, quad, m.xyz, m.conn, dofs, b.ndof)
+    return m, kappa, mesh, b, dofs, rp, ci, K, mask, rhs, quad
+
+
+def test_rhs_and_dirichlet_match_oracle():
+    m, kappa, mesh, b, dofs, rp, ci, K, mask, rhs, quad = _dirichlet_system(6, 1, 1.0, 4)
+    bg = b.build_vector(quad=quad).cpu().numpy()
+    assert np.max(np.abs(bg - rhs)) <= 1e-15 * 30
+    f = np.sin(np.pi * m.xyz[:, 0])
+    rhs_f = orc.assemble_rhs(1, quad, m.xyz, m.conn, dofs, b.ndof, field=f, elem_scale=kappa)
+    bf = b.build_vector(field=f, elem_scale=kappa, quad=quad).cpu().numpy()
+    assert np.max(np.abs(bf - rhs_f)) <= 1e-13 * np.abs(rhs_f).max()
+    Kd = K.copy()
+    rd = rhs.copy()
+    orc.apply_dirichlet(rp, ci, mask, Kd, rd)
+    v = b.assemble("stiff_kappa", coeff=kappa, quad=quad)
+    bt = torch.from_numpy(rhs).cuda()
+    b.apply_dirichlet(v, torch.from_numpy(mask), bt)
+    assert row_scaled_err(rp, Kd, v.cpu().numpy()) <= F64_TOL
+    assert np.array_equal(bt.cpu().numpy(), rd)
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_cg_and_refined_vs_oracle(order):
+    m, kappa, mesh, b, dofs, rp, ci, K, mask, rhs, quad = _dirichlet_system(6 if order == 1 else 4, order, 1.0, 5)
+    orc.apply_dirichlet(rp, ci, mask, K, rhs)
+    x_ref, it_ref, rr_ref, rc = orc.cg(rp, ci, K, rhs, rtol=1e-13)
+    assert rc == 0
+    v64 = b.assemble("stiff_kappa", coeff=kappa, quad=quad, prec="f64")
+    v32 = b.assemble("stiff_kappa", coeff=kappa, quad=quad, prec="f32")
+    mk = torch.from_numpy(mask)
+    bt = torch.from_numpy(rhs).cuda()
+    b.apply_dirichlet(v64, mk)
+    b.apply_dirichlet(v32, mk)
+    x, info = b.cg(v64, bt, rtol=1e-10, precond="jacobi")
+    assert info.converged and info.rel_residual <= 1e-10
+    err = np.linalg.norm(x.cpu().numpy() - x_ref) / np.linalg.norm(x_ref)
+    assert err <= 1e-8
+    xr, infor = b.cg_refined(v64, v32, bt, rtol=1e-10, inner_rtol=1e-4)
+    assert infor.converged and infor.rel_residual <= 1e-10 and infor.outer_iterations >= 1
+    err_r = np.linalg.norm(xr.cpu().numpy() - x_ref) / np.linalg.norm(x_ref)
+    assert err_r <= 1e-8
+    # the FP64 residual of the refined solution, recomputed by the oracle
+    r = rhs - orc.spmv(rp, ci, K, xr.cpu().numpy())
+    assert np.linalg.norm(r) <= 1.01e-10 * np.linalg.norm(rhs)
+
+
+def test_cg_deterministic_and_maxit_status():
+    m, kappa, mesh, b, dofs, rp, ci, K, mask, rhs, quad = _dirichlet_system(5, 1, 1.0, 6)
+    v = b.assemble("stiff_kappa", coeff=kappa, quad=quad)
+    bt = torch.from_numpy(rhs).cuda()
+    b.apply_dirichlet(v, torch.from_numpy(mask), bt)
+    x1, i1 = b.cg(v, bt, rtol=1e-10)
+    x2, i2 = b.cg(v, bt, rtol=1e-10)
+    assert torch.equal(x1, x2) and i1.iterations == i2.iterations
+    x3, i3 = b.cg(v, bt, rtol=1e-14, maxit=3, raise_on_fail=False)
+    assert not i3.converged and i3.iterations == 3
+    with pytest.raises(mg.MorganaError) as e:
+        b.cg(v, bt, rtol=1e-14, maxit=3)
+    assert e.value.status == mg.MG_ERR_NOT_CONVERGED
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_adjoint_gradient(order):
+    """dJ/dkappa_e from the adjoint kernel against the oracle gradient and
+    central finite differences of J(kappa) = 1/2 ||u(kappa) - u_t||^2."""
+    n = 4 if order == 1 else 3
+    m, kappa, mesh, b, dofs, rp, ci, K, mask, rhs, quad = _dirichlet_system(n, order, 0.5, 7)
+    ut = np.random.default_rng(1).uniform(0, 0.05, b.ndof) * (~mask)
+    mk = torch.from_numpy(mask)
+
+    def solve(kap):
+        v = b.assemble("stiff_kappa", coeff=kap, quad=quad)
+        bt = torch.from_numpy(rhs).cuda()
+        b.apply_dirichlet(v, mk, bt)
+        x, _ = b.cg(v, bt, rtol=1e-13, maxit=20000)
+        return v, x
+
+    v, u = solve(kappa)
+    res = u - torch.from_numpy(ut).cuda()
+    lam, _ = b.cg(v, res.clone(), rtol=1e-13, maxit=20000)
+    g = b.adjoint_grad(u, lam, quad=quad).cpu().numpy()
+    g_ref = orc.adjoint_grad(order, quad, m.xyz, m.conn, dofs, u.cpu().numpy(), lam.cpu().numpy())
+    assert np.max(np.abs(g - g_ref)) <= 1e-12 * np.abs(g_ref).max()
+    J = lambda uu: 0.5 * float(((uu - torch.from_numpy(ut).cuda()) ** 2).sum())
+    for e in np.random.default_rng(3).choice(len(kappa), 8, replace=False):
+        h = 1e-5 * kappa[e]
+        kp, km = kappa.copy(), kappa.copy()
+        kp[e] += h
+        km[e] -= h
+        fd = (J(solve(kp)[1]) - J(solve(km)[1])) / (2 * h)
+        assert abs(fd - g[e]) <= 1e-5 * np.abs(g).max() + 1e-6 * abs(fd)
+
+
+def test_gmsh_loaded_mesh_assembles(tmp_path):
+    m, kappa = _case(4, 0.2, 8, True, 1.0)
+    p = str(tmp_path / "c.msh")
+    meshgen.write_gmsh(p, m.xyz, m.conn)
+    b = mg.MatrixBuilder(mg.Mesh.load_gmsh(p, order=1))
+    _, rp, ci, ref = orc.full_operator("stiff_kappa", 1, 4, m.xyz, m.conn, coeff=kappa)
+    vals = b.assemble("stiff_kappa", coeff=kappa).cpu().numpy()
+    assert row_scaled_err(rp, ref, vals) <= F64_TOL
+
+
+def test_single_tet_and_empty():
+    xyz = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], dtype=np.float64)
+    b = mg.MatrixBuilder(mg.Mesh(xyz, np.array([[0, 1, 2, 3]], dtype=np.int32)))
+    K = b.assemble("stiff_kappa", coeff=np.ones(1)).cpu().numpy().reshape(4, 4)
+    assert np.allclose(K, np.array([[3, -1, -1, -1], [-1, 1, 0, 0], [-1, 0, 1, 0], [-1, 0, 0, 1]]) / 6.0,
+                       atol=1e-15)
+    e = mg.MatrixBuilder(mg.Mesh(xyz, np.zeros((0, 4), dtype=np.int32)))
+    assert e.assemble("mass").numel() == 0
+
+
+def test_invalid_arguments_fail_loudly():
+    m, kappa = _case(2, 0.0, 1, False, 0.0)
+    b = mg.MatrixBuilder(mg.Mesh(m.xyz, m.conn))
+    with pytest.raises(mg.MorganaError) as e:
+        b.assemble("stiff_kappa", coeff=None)
+    assert e.value.status == mg.MG_ERR_INVALID_ARG
+    with pytest.raises(mg.MorganaError):
+        b.assemble("mass", quad=7)
