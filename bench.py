@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-cg", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--only", default=None, choices=["asm64", "asm32", "spmv64", "spmv32"],
+                    help="run warmup + steps launches of one kernel only (for profilers) and print its timing")
     return ap.parse_args()
 
 
@@ -213,6 +215,45 @@ def cpu_baseline_port(a, budget_s=12.0):
 
 
 # -------------------------------------------------------------------- gb300 --
+def run_only(a):
+    """warmup + steps launches of a single kernel on the bench workload, L2 flushed
+    before each; prints the median launch time and its GB/s."""
+    import numpy as np
+    import torch
+    import morganapublic_gb300 as mg
+    from morganapublic_gb300 import meshgen
+    m = meshgen.kuhn_cube(a.n, jitter=a.jitter, seed=a.seed, permute=True)
+    kappa = torch.from_numpy(meshgen.lognormal(len(m.conn), a.sigma, a.seed)).cuda()
+    b = mg.MatrixBuilder(mg.Mesh(m.xyz, m.conn, order=1))
+    stream = torch.cuda.Stream()
+    x = torch.from_numpy(np.random.default_rng(a.seed).uniform(-1, 1, b.ndof)).cuda()
+    v64 = b.assemble("stiff_kappa", coeff=kappa, prec="f64")
+    v32 = b.assemble("stiff_kappa", coeff=kappa, prec="f32")
+    x32, y, y32 = x.float(), torch.empty_like(x), torch.empty_like(x, dtype=torch.float32)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    fn = {"asm64": lambda: b.assemble("stiff_kappa", coeff=kappa, prec="f64", out=v64, stream=stream),
+          "asm32": lambda: b.assemble("stiff_kappa", coeff=kappa, prec="f32", out=v32, stream=stream),
+          "spmv64": lambda: b.apply(v64, x, out=y, stream=stream),
+          "spmv32": lambda: b.apply(v32, x32, out=y32, stream=stream)}[a.only]
+    byts = {"asm64": asm_bytes(len(m.conn), len(m.xyz), b.nnz, 8), "asm32": asm_bytes(len(m.conn), len(m.xyz), b.nnz, 4),
+            "spmv64": spmv_bytes(b.ndof, b.nnz, 8), "spmv32": spmv_bytes(b.ndof, b.nnz, 4)}[a.only]
+    ts = []
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        for r in range(a.warmup + a.steps):
+            flush.fill_(float(r))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if r >= a.warmup:
+                ts.append(e0.elapsed_time(e1))
+    ms = statistics.median(ts)
+    print(json.dumps({"only": a.only, "n": a.n, "ms": ms, "gbs": byts / ms / 1e6, "algorithmic_bytes": byts}))
+    return 0
+
+
 def main():
     a = parse()
     if a.impl == "reference":
@@ -220,6 +261,8 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    if a.only:
+        return run_only(a)
     cpu_base = None
     if rank == 0 and not a.no_cpu_baseline:
         cpu_base = cpu_baseline_port(a)  # before any CUDA work

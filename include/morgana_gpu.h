@@ -157,16 +157,20 @@ typedef struct {
   int64_t n_chunks;
   int64_t n_entries;   /* contribution-list entries, padding included */
   int64_t n_contrib;   /* element-matrix entries scattered (= n_elements * nb^2) */
+  int64_t n_item_slots;      /* length of the exported item array (padding included) */
+  int64_t max_chunk_entries; /* words of the largest chunk (its shared-memory staging buffer) */
 } mg_schedule_info;
 
 mg_status mg_plan_schedule_info(const mg_plan* plan, mg_schedule_info* info);
 
 /* h_blocks: nblocks x 8 int32 {item_begin, item_count, chunk_begin, nchunks,
-   row_begin, row_count, acc_used, 0}; h_items: n_items element ids; h_chunk_ptr:
-   n_chunks x (warps + 1) offsets into h_entries; h_entries: n_entries words
-   (slot / threads) << 16 | source, the source indexing the chunk's element
-   matrices stored entry-major (k * chunk_items + item, k = field * nb + test);
-   h_rows / h_row_acc: ndof owned rows per block and their accumulator base. */
+   row_begin, row_count, acc_used, 0}; h_items: element ids (each block's list
+   padded to a multiple of 4 with -1); h_chunk_ptr: n_chunks x (warps + 1)
+   offsets into h_entries; h_entries: n_entries words source | slot << 13 |
+   end-of-segment << 31, the source indexing the chunk's symmetric element
+   matrices stored entry-major (u * chunk_items + item, u the upper-triangle
+   index of (field, test)); h_rows / h_row_acc: ndof owned rows per block and
+   their accumulator base. */
 mg_status mg_plan_export_schedule(const mg_plan* plan, int32_t* h_blocks, int32_t* h_items,
                                   int64_t* h_chunk_ptr, uint32_t* h_entries, int32_t* h_rows,
                                   int32_t* h_row_acc);
@@ -183,6 +187,12 @@ mg_status mg_plan_export_schedule(const mg_plan* plan, int32_t* h_blocks, int32_
    (src/morganaIntegrator/integratorOEL3d_STD.hpp:106-137). */
 mg_status mg_assemble(mg_plan* plan, int32_t op, const double* d_coeff, double c, int32_t quad,
                       int32_t prec, void* d_values, void* stream);
+
+/* Synchronises the device and reports a failure recorded by an earlier
+   asynchronous assembly on this plan (a bounded wait inside the kernel that
+   gave up: the values of that call are incomplete).  Clears the record.
+   No reference counterpart (the reference asserts). */
+mg_status mg_plan_status(mg_plan* plan);
 
 /* Host-buffer form of mg_assemble, the call an Epetra/Tpetra adapter makes:
    copies h_coeff in, assembles, copies the nnz values out to h_values. */

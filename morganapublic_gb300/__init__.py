@@ -64,7 +64,8 @@ class ScheduleInfo(ctypes.Structure):
     _fields_ = [("nblocks", ctypes.c_int32), ("threads", ctypes.c_int32), ("warps", ctypes.c_int32),
                 ("acc_max", ctypes.c_int32), ("chunk_items", ctypes.c_int32), ("host_copy", ctypes.c_int32),
                 ("n_items", ctypes.c_int64), ("n_chunks", ctypes.c_int64), ("n_entries", ctypes.c_int64),
-                ("n_contrib", ctypes.c_int64)]
+                ("n_contrib", ctypes.c_int64), ("n_item_slots", ctypes.c_int64),
+                ("max_chunk_entries", ctypes.c_int64)]
 
 
 _P = ctypes.c_void_p
@@ -87,6 +88,7 @@ SIGNATURES = {
     "mg_plan_export_schedule": [_P, _P, _P, _P, _P, _P, _P],
     "mg_assemble": [_P, _I32, _P, _D, _I32, _I32, _P, _P],
     "mg_assemble_host": [_P, _I32, _P, _D, _I32, _I32, _P, _P],
+    "mg_plan_status": [_P],
     "mg_assemble_rhs": [_P, _P, _P, _I32, _P, _P],
     "mg_apply_dirichlet": [_P, _P, _I32, _P, _P, _P],
     "mg_spmv": [_P, _I32, _P, _P, _P, _P],
@@ -248,7 +250,7 @@ class MatrixBuilder:
         info = self.schedule_info()
         out = {
             "blocks": np.empty((info.nblocks, 8), dtype=np.int32),
-            "items": np.empty(info.n_items, dtype=np.int32),
+            "items": np.empty(info.n_item_slots, dtype=np.int32),
             "chunk_ptr": np.empty(info.n_chunks * (info.warps + 1), dtype=np.int64),
             "entries": np.empty(info.n_entries, dtype=np.uint32),
             "rows": np.empty(self.ndof, dtype=np.int32),
@@ -303,6 +305,10 @@ class MatrixBuilder:
         _check(lib().mg_assemble_rhs(self._h, _ptr(f), _ptr(s), quad, _ptr(out), _stream_ptr(stream)),
                "mg_assemble_rhs")
         return out
+
+    def status(self):
+        """Synchronises and raises if an earlier asynchronous assembly recorded a device-side failure."""
+        _check(lib().mg_plan_status(self._h), "mg_plan_status")
 
     def apply_dirichlet(self, values, mask, b=None, stream=None):
         torch = _torch()

@@ -2,16 +2,20 @@
 // reduced straight into CSR values, plus the Dirichlet elimination, the
 // adjoint-gradient kernel and the load vector.
 //
-// One CTA owns one block of rows (see mg_plan.cpp).  Per chunk of elements:
-//   phase 1  each element's matrix is computed into shared memory, stored
-//            entry-major (buf[k * CI + item]) so that the stores are
-//            bank-conflict free;
-//   phase 2  every thread walks its own contribution list (coalesced 4-byte
-//            words) and adds buf[src] into accumulator slot (word >> 16) * 256 +
-//            threadIdx.x, a slot no other thread touches.
-// After the last chunk the accumulators of each owned row are written to the
-// row's contiguous CSR range.  No atomics; the per-slot summation order is the
-// element order, so results are bitwise reproducible.
+// k_assemble is a persistent kernel: each CTA repeatedly takes the next block of
+// rows (an integer work counter) and, for every chunk of the block's elements,
+//   stage    a bulk copy (cp.async.bulk, completion on an mbarrier) brings the
+//            chunk's element nodes and element ids into shared memory while the
+//            previous chunk is reduced, and the chunk's contribution words while
+//            its element matrices are computed;
+//   phase 1  one thread per P1 element (eight per P2 element) computes the
+//            symmetric element matrix into shared memory, entry-major;
+//   phase 2  every thread sums its own slot-sorted segments of contribution
+//            words sequentially and adds each segment's sum to its accumulator
+//            slot -- within a chunk a slot belongs to exactly one thread.
+// The owned rows are then written to their contiguous CSR ranges.  No atomics
+// touch values; the per-slot summation order is fixed by the plan, so the
+// results are bitwise reproducible.
 //
 // Element math (reference: src/morganaIntegrator/integratorOEL3d_STD.hpp:106-137,
 // src/morganaOperators/opEL3dA.hpp:129-165, opEL3dF.hpp:102-133, opEL3dG.hpp:83-108,
@@ -22,248 +26,647 @@
 //                   = (coef / det) sum_{a<=b} (C_a . C_b) T^{ab}_ij ,
 //              C_a the columns of the cofactor matrix of J (adj J = C^T),
 //              T^{ab} = sum_q w_q g^_ia g^_jb (symmetrised for a != b);
-//   P1         the reference gradients are constant, so
-//              K_ij = coef sum_q w_q / det (c_i . c_j) with c_1..3 = C_0..2,
-//              c_0 = -(c_1 + c_2 + c_3);
+//   P1         the reference gradients are constant, so for i, j >= 1
+//              K_ij = coef sum_q w_q / det (C_{i-1} . C_{j-1}), and the row of
+//              vertex 0 follows from the zero row sums of a stiffness matrix;
 //   mass       K_ij = coef det sum_q w_q phi^_i phi^_j.
 // detJ is signed, as in the reference (positive on checked meshes).
+//
+// Arithmetic modes: kF32 (FP32 values), kDW (FP64-accurate values from
+// double-word float arithmetic on the FP32 pipes, written as IEEE doubles), kF64
+// (native FP64).  GB300 runs FP64 at ~1/60 of its FP32 rate, so MG_F64 uses kDW;
+// kF64 stays available for comparison (MG_ASSEMBLY_NATIVE_F64=1).
 #include <cstdio>
+#include <cstdlib>
 
+#include "mg_ff.cuh"
 #include "mg_internal.h"
 
 namespace mg {
 
-struct AsmArgs {
-  const BlockDesc* blocks;
-  const int32_t* items;
-  const int64_t* chunk_ptr;
-  const uint32_t* entries;
-  const int32_t* rows;
-  const int32_t* row_acc;
-  const int32_t* rowptr;
-  const int4* conn;
-  const double4_32a* xyz;
-  const float4* xyz_hi;
-  const float4* xyz_lo;
-  const double* coeff;  // per element, or null
-  double cconst;        // used when coeff is null
-  const double* tables; // stiff (6 nb^2) then mass (nb^2)
-  double wsum;
-  void* values;
+enum { kF32 = 0, kDW = 1, kF64 = 2 };
+
+// ---------------------------------------------------------- double-word ops --
+__device__ __forceinline__ ff operator+(ff a, ff b) { return ff_add_s(a, b); }
+__device__ __forceinline__ ff operator-(ff a, ff b) { return ff_add_s(a, ff_neg(b)); }
+__device__ __forceinline__ ff operator-(ff a) { return ff_neg(a); }
+__device__ __forceinline__ ff operator*(ff a, ff b) { return ff_mul(a, b); }
+__device__ __forceinline__ ff operator/(ff a, ff b) { return ff_div(a, b); }
+
+template <int MODE> struct Arith;
+template <> struct Arith<kF32> {
+  using T = float;
+  using Acc = float;
+  __device__ static void acc_add(Acc& s, T x) { s += x; }
+  __device__ static T acc_value(const Acc& s) { return s; }
+  using Out = float;
+  __device__ static T from(double x) { return (float)x; }
+  __device__ static T zero() { return 0.0f; }
+  __device__ static Out out(T v) { return v; }
+};
+template <> struct Arith<kDW> {
+  using T = ff;
+  using Acc = ff_acc;
+  __device__ static void acc_add(Acc& s, T x) { ff_acc_add(s, x); }
+  __device__ static T acc_value(const Acc& s) { return ff_acc_value(s); }
+  using Out = double;
+  __device__ static T from(double x) { return ff_from_double(x); }
+  __device__ static T zero() { return ff{0.0f, 0.0f}; }
+  __device__ static Out out(T v) { return ff_to_double(v); }
+};
+template <> struct Arith<kF64> {
+  using T = double;
+  using Acc = double;
+  __device__ static void acc_add(Acc& s, T x) { s += x; }
+  __device__ static T acc_value(const Acc& s) { return s; }
+  using Out = double;
+  __device__ static T from(double x) { return x; }
+  __device__ static T zero() { return 0.0; }
+  __device__ static Out out(T v) { return v; }
 };
 
-// Flatness threshold of the FP32 path: when |det| falls below this fraction of
-// the product of the edge-vector lengths, the Jacobian is recomputed in FP64.
-constexpr float kFlatTol = 1e-3f;
+// ------------------------------------------------------------ PTX helpers --
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-template <typename V>
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
+{
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
+{
+  uint32_t ok;
+  asm volatile(
+      "{\n"
+      " .reg .pred p;\n"
+      " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n"
+      "}\n"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Orders this thread's earlier generic-proxy shared-memory accesses before
+// later async-proxy (bulk copy) writes to the same buffers.
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// Bulk copy global -> shared (16-byte aligned addresses, size a multiple of 16),
+// completion signalled on `bar` as transaction bytes.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
+{
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+
+// Bounded wait: gives up after kWaitLimit polls (each poll may suspend the
+// thread for a short, hardware-chosen time) and returns false.
+constexpr uint32_t kWaitLimit = 1u << 22;
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
+{
+  for (uint32_t i = 0; i < kWaitLimit; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+enum { kDevErrTimeout = 1 };
+
+// ---------------------------------------------------------------- geometry --
+template <typename T>
 struct Cof {
-  V c[3][3];  // cofactor matrix C[r][k] of J; column a of C = J^-T e_a * det
-  V det;
+  T c[3][3];  // cofactor matrix C[r][k] of J; column a of C = det * (J^-T e_a)
+  T det;
 };
 
-__device__ __forceinline__ void cofactors64(const double4_32a* xyz, int4 n, Cof<double>& f)
+template <typename T>
+__device__ __forceinline__ void cofactors(const T J[3][3], Cof<T>& f)
 {
-  const double4_32a a = xyz[n.x], b = xyz[n.y], c = xyz[n.z], d = xyz[n.w];
-  const double J00 = b.x - a.x, J01 = c.x - a.x, J02 = d.x - a.x;
-  const double J10 = b.y - a.y, J11 = c.y - a.y, J12 = d.y - a.y;
-  const double J20 = b.z - a.z, J21 = c.z - a.z, J22 = d.z - a.z;
-  f.c[0][0] = J11 * J22 - J12 * J21;
-  f.c[0][1] = J12 * J20 - J10 * J22;
-  f.c[0][2] = J10 * J21 - J11 * J20;
-  f.c[1][0] = J02 * J21 - J01 * J22;
-  f.c[1][1] = J00 * J22 - J02 * J20;
-  f.c[1][2] = J01 * J20 - J00 * J21;
-  f.c[2][0] = J01 * J12 - J02 * J11;
-  f.c[2][1] = J02 * J10 - J00 * J12;
-  f.c[2][2] = J00 * J11 - J01 * J10;
-  f.det = J00 * f.c[0][0] + J01 * f.c[0][1] + J02 * f.c[0][2];
+  f.c[0][0] = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+  f.c[0][1] = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+  f.c[0][2] = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+  f.c[1][0] = J[0][2] * J[2][1] - J[0][1] * J[2][2];
+  f.c[1][1] = J[0][0] * J[2][2] - J[0][2] * J[2][0];
+  f.c[1][2] = J[0][1] * J[2][0] - J[0][0] * J[2][1];
+  f.c[2][0] = J[0][1] * J[1][2] - J[0][2] * J[1][1];
+  f.c[2][1] = J[0][2] * J[1][0] - J[0][0] * J[1][2];
+  f.c[2][2] = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+  f.det = J[0][0] * f.c[0][0] + J[0][1] * f.c[0][1] + J[0][2] * f.c[0][2];
 }
 
-// FP32 geometry from the float-pair coordinates: each edge vector is
-// (hi_k - hi_0) + (lo_k - lo_0), accurate to a few float ulps of the edge itself.
-// Flat elements fall back to FP64 cofactors.
-__device__ __forceinline__ void cofactors32(const float4* hi, const float4* lo, const double4_32a* xyz,
-                                            int4 n, Cof<float>& f)
+struct GeoPtrs {
+  const double4_32a* xyz;
+  const float4* hi;
+  const float4* mid;
+  const float4* lo;
+};
+
+__device__ __forceinline__ float comp(const float4& v, int r) { return r == 0 ? v.x : (r == 1 ? v.y : v.z); }
+__device__ __forceinline__ double comp(const double4_32a& v, int r) { return r == 0 ? v.x : (r == 1 ? v.y : v.z); }
+
+// The global loads an element needs (vertex coordinates and coefficient), issued
+// one chunk ahead of their use so that their latency overlaps the previous
+// chunk's arithmetic and reduction.
+template <int MODE> struct Fetch;
+template <> struct Fetch<kF32> {
+  float h[4][3], m[4][3];
+  int4 n;
+  double coef;
+};
+template <> struct Fetch<kDW> {
+  float h[4][3], m[4][3], l[4][3];
+  double coef;
+};
+template <> struct Fetch<kF64> {
+  double x[4][3];
+  double coef;
+};
+
+__device__ __forceinline__ void load3(const float4* p, int i, float* o)
 {
-  const float4 ha = hi[n.x], hb = hi[n.y], hc = hi[n.z], hd = hi[n.w];
-  const float4 la = lo[n.x], lb = lo[n.y], lc = lo[n.z], ld = lo[n.w];
-  const float J00 = (hb.x - ha.x) + (lb.x - la.x), J01 = (hc.x - ha.x) + (lc.x - la.x),
-              J02 = (hd.x - ha.x) + (ld.x - la.x);
-  const float J10 = (hb.y - ha.y) + (lb.y - la.y), J11 = (hc.y - ha.y) + (lc.y - la.y),
-              J12 = (hd.y - ha.y) + (ld.y - la.y);
-  const float J20 = (hb.z - ha.z) + (lb.z - la.z), J21 = (hc.z - ha.z) + (lc.z - la.z),
-              J22 = (hd.z - ha.z) + (ld.z - la.z);
-  f.c[0][0] = J11 * J22 - J12 * J21;
-  f.c[0][1] = J12 * J20 - J10 * J22;
-  f.c[0][2] = J10 * J21 - J11 * J20;
-  f.c[1][0] = J02 * J21 - J01 * J22;
-  f.c[1][1] = J00 * J22 - J02 * J20;
-  f.c[1][2] = J01 * J20 - J00 * J21;
-  f.c[2][0] = J01 * J12 - J02 * J11;
-  f.c[2][1] = J02 * J10 - J00 * J12;
-  f.c[2][2] = J00 * J11 - J01 * J10;
-  f.det = J00 * f.c[0][0] + J01 * f.c[0][1] + J02 * f.c[0][2];
-  const float n0 = J00 * J00 + J10 * J10 + J20 * J20, n1 = J01 * J01 + J11 * J11 + J21 * J21,
-              n2 = J02 * J02 + J12 * J12 + J22 * J22;
-  if (fabsf(f.det) * fabsf(f.det) < kFlatTol * kFlatTol * n0 * n1 * n2) {
-    Cof<double> g;
-    cofactors64(xyz, n, g);
+  const float4 v = p[i];
+  o[0] = v.x; o[1] = v.y; o[2] = v.z;
+}
+__device__ __forceinline__ void load3(const double4_32a* p, int i, double* o)
+{
+  const double4_32a v = p[i];
+  o[0] = v.x; o[1] = v.y; o[2] = v.z;
+}
+
+__device__ __forceinline__ void fetch(const GeoPtrs& g, int4 n, Fetch<kF32>& F)
+{
+  const int id[4] = {n.x, n.y, n.z, n.w};
+#pragma unroll
+  for (int s = 0; s < 4; ++s) { load3(g.hi, id[s], F.h[s]); load3(g.mid, id[s], F.m[s]); }
+  F.n = n;
+}
+__device__ __forceinline__ void fetch(const GeoPtrs& g, int4 n, Fetch<kDW>& F)
+{
+  const int id[4] = {n.x, n.y, n.z, n.w};
+#pragma unroll
+  for (int s = 0; s < 4; ++s) { load3(g.hi, id[s], F.h[s]); load3(g.mid, id[s], F.m[s]); load3(g.lo, id[s], F.l[s]); }
+}
+__device__ __forceinline__ void fetch(const GeoPtrs& g, int4 n, Fetch<kF64>& F)
+{
+  const int id[4] = {n.x, n.y, n.z, n.w};
+#pragma unroll
+  for (int s = 0; s < 4; ++s) load3(g.xyz, id[s], F.x[s]);
+}
+
+__device__ __forceinline__ void geometry(const GeoPtrs&, const Fetch<kF64>& F, Cof<double>& f)
+{
+  double J[3][3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) J[r][k] = F.x[k + 1][r] - F.x[0][r];
+  cofactors<double>(J, f);
+}
+
+// FP32: edge vectors (hi_k - hi_0) + (mid_k - mid_0), accurate to a few float
+// ulps of the edge itself; flat elements recompute the cofactors in FP64.
+constexpr float kFlatTol = 1e-3f;
+__device__ __forceinline__ void geometry(const GeoPtrs& g, const Fetch<kF32>& F, Cof<float>& f)
+{
+  float J[3][3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) J[r][k] = (F.h[k + 1][r] - F.h[0][r]) + (F.m[k + 1][r] - F.m[0][r]);
+  cofactors<float>(J, f);
+  float nn[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) nn[k] = J[0][k] * J[0][k] + J[1][k] * J[1][k] + J[2][k] * J[2][k];
+  if (f.det * f.det < kFlatTol * kFlatTol * nn[0] * nn[1] * nn[2]) {
+    Fetch<kF64> D;
+    fetch(g, F.n, D);
+    Cof<double> d;
+    geometry(g, D, d);
     for (int r = 0; r < 3; ++r)
-      for (int k = 0; k < 3; ++k) f.c[r][k] = (float)g.c[r][k];
-    f.det = (float)g.det;
+      for (int k = 0; k < 3; ++k) f.c[r][k] = (float)d.c[r][k];
+    f.det = (float)d.det;
   }
 }
 
-template <typename V>
-__device__ __forceinline__ void geometry(const AsmArgs& a, int4 n, Cof<V>& f);
-template <>
-__device__ __forceinline__ void geometry<double>(const AsmArgs& a, int4 n, Cof<double>& f)
+// Double-word: x = hi + mid + lo exactly, so
+//   x_k - x_0 = (hi_k - hi_0) + (mid_k - mid_0) + (lo_k - lo_0)
+// with the two leading differences taken error-free (two_sum) and the result
+// renormalised -- relative error ~2^-47 of the edge vector itself.
+__device__ __forceinline__ ff dw_diff(float hb, float ha, float mb, float ma, float lb, float la)
 {
-  cofactors64(a.xyz, n, f);
-}
-template <>
-__device__ __forceinline__ void geometry<float>(const AsmArgs& a, int4 n, Cof<float>& f)
-{
-  cofactors32(a.xyz_hi, a.xyz_lo, a.xyz, n, f);
+  const ff s1 = two_sum(hb, -ha);
+  const ff s2 = two_sum(mb, -ma);
+  const ff s = two_sum(s1.hi, s2.hi);
+  const float t = __fadd_rn(__fadd_rn(__fadd_rn(s.lo, s1.lo), s2.lo), __fsub_rn(lb, la));
+  return two_sum(s.hi, t);
 }
 
-// P1 stiffness: the 16 entries (k = i*4 + j) of coef * wsum / det * (c_i . c_j).
-template <typename V>
-__device__ __forceinline__ void p1_stiff(const Cof<V>& f, V s, V* K)
+__device__ __forceinline__ void geometry(const GeoPtrs&, const Fetch<kDW>& F, Cof<ff>& f)
 {
-  V c[4][3];
-  for (int r = 0; r < 3; ++r) {
-    c[1][r] = f.c[r][0];
-    c[2][r] = f.c[r][1];
-    c[3][r] = f.c[r][2];
-    c[0][r] = -(c[1][r] + c[2][r] + c[3][r]);
-  }
+  ff J[3][3];
 #pragma unroll
-  for (int i = 0; i < 4; ++i)
+  for (int r = 0; r < 3; ++r)
 #pragma unroll
-    for (int j = i; j < 4; ++j) {
-      V v = s * (c[i][0] * c[j][0] + c[i][1] * c[j][1] + c[i][2] * c[j][2]);
-      K[i * 4 + j] = v;
-      K[j * 4 + i] = v;
+    for (int k = 0; k < 3; ++k)
+      J[r][k] = dw_diff(F.h[k + 1][r], F.h[0][r], F.m[k + 1][r], F.m[0][r], F.l[k + 1][r], F.l[0][r]);
+  f.c[0][0] = ff_cross(J[1][1], J[2][2], J[1][2], J[2][1]);
+  f.c[0][1] = ff_cross(J[1][2], J[2][0], J[1][0], J[2][2]);
+  f.c[0][2] = ff_cross(J[1][0], J[2][1], J[1][1], J[2][0]);
+  f.c[1][0] = ff_cross(J[0][2], J[2][1], J[0][1], J[2][2]);
+  f.c[1][1] = ff_cross(J[0][0], J[2][2], J[0][2], J[2][0]);
+  f.c[1][2] = ff_cross(J[0][1], J[2][0], J[0][0], J[2][1]);
+  f.c[2][0] = ff_cross(J[0][1], J[1][2], J[0][2], J[1][1]);
+  f.c[2][1] = ff_cross(J[0][2], J[1][0], J[0][0], J[1][2]);
+  f.c[2][2] = ff_cross(J[0][0], J[1][1], J[0][1], J[1][0]);
+  f.det = ff_dot3(J[0], f.c[0]);
+}
+
+// one geometry entry point for the adjoint kernel (loads and computes at once)
+template <int MODE>
+__device__ __forceinline__ void geometry_now(const GeoPtrs& g, int4 n, Cof<typename Arith<MODE>::T>& f)
+{
+  Fetch<MODE> F;
+  fetch(g, n, F);
+  geometry(g, F, f);
+}
+
+// ------------------------------------------------------- element matrices --
+// P1 stiffness, unique entries in sym_index order:
+// (0,0) (0,1) (0,2) (0,3) (1,1) (1,2) (1,3) (2,2) (2,3) (3,3)
+template <typename T>
+__device__ __forceinline__ void p1_stiff_unique(const Cof<T>& f, T s, T K[10])
+{
+  T d[3][3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = a; b < 3; ++b) {
+      d[a][b] = s * (f.c[0][a] * f.c[0][b] + f.c[1][a] * f.c[1][b] + f.c[2][a] * f.c[2][b]);
+      d[b][a] = d[a][b];
     }
+  K[4] = d[0][0];
+  K[5] = d[0][1];
+  K[6] = d[0][2];
+  K[7] = d[1][1];
+  K[8] = d[1][2];
+  K[9] = d[2][2];
+  K[1] = -(d[0][0] + d[1][0] + d[2][0]);  // rows sum to zero
+  K[2] = -(d[0][1] + d[1][1] + d[2][1]);
+  K[3] = -(d[0][2] + d[1][2] + d[2][2]);
+  K[0] = -(K[1] + K[2] + K[3]);
 }
 
-// The six scaled metric coefficients coef / det * (C_a . C_b), ab = 00,11,22,01,02,12.
-template <typename V>
-__device__ __forceinline__ void metric(const Cof<V>& f, V s, V g[6])
+template <>
+__device__ __forceinline__ void p1_stiff_unique<ff>(const Cof<ff>& f, ff s, ff K[10])
+{
+  ff col[3][3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int r = 0; r < 3; ++r) col[a][r] = f.c[r][a];
+  ff d[3][3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = a; b < 3; ++b) {
+      d[a][b] = ff_mul(s, ff_dot3(col[a], col[b]));
+      d[b][a] = d[a][b];
+    }
+  K[4] = d[0][0];
+  K[5] = d[0][1];
+  K[6] = d[0][2];
+  K[7] = d[1][1];
+  K[8] = d[1][2];
+  K[9] = d[2][2];
+  K[1] = -(d[0][0] + d[1][0] + d[2][0]);
+  K[2] = -(d[0][1] + d[1][1] + d[2][1]);
+  K[3] = -(d[0][2] + d[1][2] + d[2][2]);
+  K[0] = -(K[1] + K[2] + K[3]);
+}
+
+// The six scaled metric coefficients s (C_a . C_b), ab = 00,11,22,01,02,12.
+template <typename T>
+__device__ __forceinline__ void metric(const Cof<T>& f, T s, T g[6])
 {
   const int pa[6] = {0, 1, 2, 0, 0, 1}, pb[6] = {0, 1, 2, 1, 2, 2};
 #pragma unroll
   for (int p = 0; p < 6; ++p)
-    g[p] = s * (f.c[0][pa[p]] * f.c[0][pb[p]] + f.c[1][pa[p]] * f.c[1][pb[p]] +
-                f.c[2][pa[p]] * f.c[2][pb[p]]);
+    g[p] = s * (f.c[0][pa[p]] * f.c[0][pb[p]] + f.c[1][pa[p]] * f.c[1][pb[p]] + f.c[2][pa[p]] * f.c[2][pb[p]]);
 }
 
-template <int ORDER, typename V>
-__global__ void __launch_bounds__(kThreads, 2) k_assemble(AsmArgs a, int stiff)
+struct AsmArgs {
+  const BlockDesc* blocks;
+  const int32_t* items;
+  const int4* item_conn;
+  const ChunkDesc* chunks;
+  const uint32_t* entries;
+  const int32_t* row_csr;
+  const int32_t* row_acc;
+  GeoPtrs geo;
+  const double* coeff;   // per element, or null
+  double cconst;         // used when coeff is null
+  const double* tables;  // unique-entry tables: stiff[6][nu] then mass[nu]
+  double wsum;
+  void* values;
+  uint32_t* counters;
+  int nblocks;
+  int stiff;
+  int ent_cap;           // words of the shared-memory contribution buffer
+};
+
+template <int ORDER, int MODE>
+struct AsmLayout {
+  using T = typename Arith<MODE>::T;
+  static constexpr int NB = ORDER == 1 ? 4 : 10;
+  static constexpr int NU = ORDER == 1 ? 10 : 55;
+  static constexpr int CI = ORDER == 1 ? kChunkP1 : kChunkP2;
+  static constexpr size_t acc_bytes = sizeof(T) * kAccMax;
+  static constexpr size_t buf_bytes = (sizeof(T) * (NU * CI + 1) + 15) / 16 * 16;
+  static constexpr size_t tab_bytes = (sizeof(T) * 7 * NU + 15) / 16 * 16;
+  static constexpr size_t conn_bytes = 16 * CI;  // per stage (two stages)
+  static constexpr size_t ids_bytes = 4 * CI;    // per stage (two stages)
+  static constexpr size_t desc_bytes = sizeof(ChunkDesc);  // per stage (two stages)
+  static constexpr int kRowBatch = kThreads;       // owned rows written per batch
+  static constexpr size_t rowmeta_bytes = 8 * (kRowBatch + 1);
+  static size_t total(int ent_cap)
+  {
+    return acc_bytes + buf_bytes + tab_bytes + 2 * (conn_bytes + ids_bytes + desc_bytes) + rowmeta_bytes +
+           ((size_t)ent_cap * 4 + 15) / 16 * 16 + 32;
+  }
+};
+
+// Pipeline of one block of c = 0 .. nchunks-1 (stage = c & 1 for the element
+// nodes and ids, one buffer for the contribution words):
+//   before chunk c      nodes(c) and nodes(c+1) staged; coordinates of chunk c
+//                       already in registers (R)
+//   start of chunk c    wait nodes(c+1), load its coordinates into P
+//   phase 1 (c)         element matrices from R
+//   barrier             stage c & 1 is free: bulk copy nodes(c+2) into it
+//   phase 2 (c)         wait words(c) (copied during phase 1), segmented sums
+//   barrier             bulk copy words(c+1); R = P
+template <int ORDER, int MODE>
+__global__ void __launch_bounds__(kThreads, 2) k_assemble(AsmArgs a)
 {
-  constexpr int NB = ORDER == 1 ? 4 : 10;
-  constexpr int NB2 = NB * NB;
-  constexpr int CI = ORDER == 1 ? kChunkP1 : kChunkP2;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  V* acc = reinterpret_cast<V*>(smem_raw);
-  V* buf = acc + kAccMax;         // CI * NB2 element-matrix entries + one zero
-  V* tab = buf + CI * NB2 + 1;    // 7 * NB2 reference tables
+  using A = Arith<MODE>;
+  using T = typename A::T;
+  using L = AsmLayout<ORDER, MODE>;
+  constexpr int NU = L::NU, CI = L::CI;
+  constexpr int TPI = ORDER == 1 ? 1 : kP2ThreadsPerItem;  // threads per item
+  extern __shared__ __align__(16) unsigned char smem[];
+  unsigned char* ptr = smem;
+  T* acc = reinterpret_cast<T*>(ptr);
+  ptr += L::acc_bytes;
+  T* buf = reinterpret_cast<T*>(ptr);
+  ptr += L::buf_bytes;
+  T* tab = reinterpret_cast<T*>(ptr);
+  ptr += L::tab_bytes;
+  int4* sconn = reinterpret_cast<int4*>(ptr);  // [2][CI]
+  ptr += 2 * L::conn_bytes;
+  int32_t* sids = reinterpret_cast<int32_t*>(ptr);  // [2][CI]
+  ptr += 2 * L::ids_bytes;
+  ChunkDesc* sdesc = reinterpret_cast<ChunkDesc*>(ptr);  // [2]
+  ptr += 2 * L::desc_bytes;
+  int32_t* s_rcsr = reinterpret_cast<int32_t*>(ptr);  // [kRowBatch]
+  int32_t* s_racc = s_rcsr + L::kRowBatch;            // [kRowBatch + 1]
+  ptr += L::rowmeta_bytes;
+  uint32_t* sent = reinterpret_cast<uint32_t*>(ptr);
+  ptr += ((size_t)a.ent_cap * 4 + 15) / 16 * 16;
+  uint64_t* bar_nodes = reinterpret_cast<uint64_t*>(ptr);  // [2]
+  uint64_t* bar_ent = bar_nodes + 2;
+  __shared__ int s_block;
+
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const BlockDesc d = a.blocks[blockIdx.x];
-
-  for (int i = tid; i < 7 * NB2; i += kThreads) tab[i] = (V)a.tables[i];
-  for (int i = tid; i < kAccMax; i += kThreads) acc[i] = V(0);
-  if (tid == 0) buf[CI * NB2] = V(0);
+  const int local = tid / TPI, sub = tid % TPI;
+  for (int i = tid; i < 7 * NU; i += kThreads) tab[i] = A::from(a.tables[i]);
+  if (tid == 0) {
+    buf[NU * CI] = A::zero();
+    mbar_init(&bar_nodes[0], 1);
+    mbar_init(&bar_nodes[1], 1);
+    mbar_init(bar_ent, 1);
+    mbar_fence_init();
+  }
   __syncthreads();
+  const T wsum = A::from(a.wsum);
+  // bit st of ph_nodes: parity of the next completion of stage st's barrier;
+  // bit st of pend_nodes: a copy into stage st is in flight
+  uint32_t ph_nodes = 0, ph_ent = 0, pend_nodes = 0;
+  bool pend_ent = false, failed = false;
 
-  for (int c = 0; c < d.nchunks; ++c) {
-    // ---- phase 1: element matrices of this chunk
-    if (ORDER == 1) {
-      const int it = c * CI + tid;
-      if (it < d.item_count) {
-        const int e = a.items[d.item_begin + it];
-        const int4 n = a.conn[e];
-        const V coef = (V)(a.coeff ? a.coeff[e] : a.cconst);
-        Cof<V> f;
-        geometry<V>(a, n, f);
-        V K[16];
-        if (stiff) {
-          p1_stiff<V>(f, coef * (V)a.wsum / f.det, K);
-        } else {
-          const V s = coef * f.det;
-#pragma unroll
-          for (int k = 0; k < 16; ++k) K[k] = s * tab[6 * NB2 + k];
-        }
-#pragma unroll
-        for (int k = 0; k < 16; ++k) buf[k * CI + tid] = K[k];
-      }
-    } else {
-      const int local = tid / kP2ThreadsPerItem, sub = tid % kP2ThreadsPerItem;
+  for (;;) {
+    if (tid == 0) s_block = (int)atomicAdd(&a.counters[0], 1u);
+    __syncthreads();
+    const int b = s_block;
+    __syncthreads();
+    if (b >= a.nblocks) break;
+    const BlockDesc d = a.blocks[b];
+
+    auto issue_nodes = [&](int c) {
+      const int st = c & 1;
+      const int n = min(CI, d.item_count - c * CI), n4 = (n + 3) & ~3;
+      const int64_t first = (int64_t)d.item_begin + (int64_t)c * CI;
+      mbar_expect_tx(&bar_nodes[st], (uint32_t)(n4 * 20 + sizeof(ChunkDesc)));
+      bulk_g2s(sconn + st * CI, a.item_conn + first, (uint32_t)(n4 * 16), &bar_nodes[st]);
+      bulk_g2s(sids + st * CI, a.items + first, (uint32_t)(n4 * 4), &bar_nodes[st]);
+      bulk_g2s(sdesc + st, a.chunks + d.chunk_begin + c, (uint32_t)sizeof(ChunkDesc), &bar_nodes[st]);
+    };
+    // needs the staged descriptor of chunk c (stage c & 1)
+    auto issue_entries = [&](int c) {
+      const ChunkDesc& cd = sdesc[c & 1];
+      const uint32_t bytes = (uint32_t)cd.warp_off[kWarps] * 4u;
+      mbar_expect_tx(bar_ent, bytes);
+      if (bytes) bulk_g2s(sent, a.entries + cd.word_begin, bytes, bar_ent);
+    };
+    // waits on a stage barrier; false (uniformly) when the wait gave up
+    auto wait_nodes = [&](int c) -> bool {
+      const int st = c & 1;
+      const bool ok = mbar_wait(&bar_nodes[st], (ph_nodes >> st) & 1u);
+      if (__syncthreads_or(!ok)) return false;
+      ph_nodes ^= 1u << st;
+      pend_nodes &= ~(1u << st);
+      return true;
+    };
+    // loads the coordinates and coefficient of this thread's item of chunk c
+    auto prefetch = [&](int c, Fetch<MODE>& F) -> bool {
       const int it = c * CI + local;
-      if (it < d.item_count) {
-        const int e = a.items[d.item_begin + it];
-        const int4 n = a.conn[e];
-        const V coef = (V)(a.coeff ? a.coeff[e] : a.cconst);
-        Cof<V> f;
-        geometry<V>(a, n, f);
-        if (stiff) {
-          V g[6];
-          metric<V>(f, coef / f.det, g);
-          for (int k = sub; k < NB2; k += kP2ThreadsPerItem) {
-            V v = g[0] * tab[k];
+      if (it >= d.item_count) return false;
+      const int st = c & 1;
+      const int e = sids[st * CI + local];
+      fetch(a.geo, sconn[st * CI + local], F);
+      F.coef = a.coeff ? __ldg(a.coeff + e) : a.cconst;
+      return true;
+    };
+
+    for (int i = tid; i < kAccMax; i += kThreads) acc[i] = A::zero();
+    if (tid == 0 && d.nchunks > 0) {
+      fence_proxy_async();
+      issue_nodes(0);
+      if (d.nchunks > 1) issue_nodes(1);
+    }
+    pend_nodes = (d.nchunks > 0 ? 1u : 0u) | (d.nchunks > 1 ? 2u : 0u);
+
+    Fetch<MODE> R, P;
+    bool have_r = false, have_p = false;
+    if (d.nchunks > 0) {
+      if (!wait_nodes(0)) { failed = true; break; }
+      if (tid == 0) issue_entries(0);
+      pend_ent = true;
+      have_r = prefetch(0, R);
+    }
+    for (int c = 0; c < d.nchunks; ++c) {
+      // this warp's slice of chunk c's words, read before stage c & 1 is reused
+      const int w_beg = sdesc[c & 1].warp_off[warp], w_end = sdesc[c & 1].warp_off[warp + 1];
+      if (c + 1 < d.nchunks) {
+        if (!wait_nodes(c + 1)) { failed = true; break; }
+        have_p = prefetch(c + 1, P);
+      }
+      // ---- phase 1: element matrices of chunk c
+      if (have_r) {
+        const T coef = A::from(R.coef);
+        Cof<T> f;
+        geometry(a.geo, R, f);
+        if (ORDER == 1) {
+          T K[10];
+          if (a.stiff) {
+            p1_stiff_unique<T>(f, coef * wsum / f.det, K);
+          } else {
+            const T sc = coef * f.det;
 #pragma unroll
-            for (int p = 1; p < 6; ++p) v += g[p] * tab[p * NB2 + k];
-            buf[k * CI + local] = v;
+            for (int u = 0; u < 10; ++u) K[u] = sc * tab[6 * NU + u];
+          }
+#pragma unroll
+          for (int u = 0; u < 10; ++u) buf[u * CI + local] = K[u];
+        } else if (a.stiff) {
+          T g[6];
+          metric<T>(f, coef / f.det, g);
+          for (int u = sub; u < NU; u += TPI) {
+            T v = g[0] * tab[u];
+#pragma unroll
+            for (int q = 1; q < 6; ++q) v = v + g[q] * tab[q * NU + u];
+            buf[u * CI + local] = v;
           }
         } else {
-          const V s = coef * f.det;
-          for (int k = sub; k < NB2; k += kP2ThreadsPerItem) buf[k * CI + local] = s * tab[6 * NB2 + k];
+          const T sc = coef * f.det;
+          for (int u = sub; u < NU; u += TPI) buf[u * CI + local] = sc * tab[6 * NU + u];
         }
       }
+      __syncthreads();
+      if (tid == 0 && c + 2 < d.nchunks) {
+        fence_proxy_async();
+        issue_nodes(c + 2);
+      }
+      if (c + 2 < d.nchunks) pend_nodes |= 1u << (c & 1);
+      // ---- phase 2: segmented sums into owned slots
+      {
+        const bool ok = mbar_wait(bar_ent, ph_ent);
+        if (__syncthreads_or(!ok)) { failed = true; break; }
+        ph_ent ^= 1;
+        pend_ent = false;
+      }
+      {
+        const uint32_t* ew = sent + w_beg + lane;
+        const int K = (w_end - w_beg) >> 5;
+        typename A::Acc sum{};
+        for (int k = 0; k < K; ++k) {
+          const uint32_t w = ew[k * 32];
+          A::acc_add(sum, buf[w & kSrcMask]);
+          if (w & kEndFlag) {
+            const uint32_t slot = (w >> kSrcBits) & kSlotMask;
+            acc[slot] = acc[slot] + A::acc_value(sum);
+            sum = typename A::Acc{};
+          }
+        }
+      }
+      __syncthreads();
+      if (tid == 0 && c + 1 < d.nchunks) {
+        fence_proxy_async();
+        issue_entries(c + 1);
+      }
+      pend_ent = c + 1 < d.nchunks;
+      R = P;
+      have_r = have_p;
+      have_p = false;
     }
-    __syncthreads();
-    // ---- phase 2: owned-slot reduction
-    const int64_t* cp = a.chunk_ptr + (int64_t)(d.chunk_begin + c) * (kWarps + 1);
-    const int64_t beg = cp[warp], end = cp[warp + 1];
-    for (int64_t o = beg + lane; o < end; o += 32) {
-      const uint32_t w = __ldg(a.entries + o);
-      acc[(w >> 16) * kThreads + tid] += buf[w & 0xffffu];
+    if (failed) break;
+    // ---- write the owned rows, kRowBatch at a time: their CSR starts and
+    // accumulator bases are loaded in parallel, then one warp per row stores
+    // the row's contiguous range
+    using Out = typename A::Out;
+    Out* out = reinterpret_cast<Out*>(a.values);
+    for (int r0 = 0; r0 < d.row_count; r0 += L::kRowBatch) {
+      const int nr = min(L::kRowBatch, d.row_count - r0);
+      if (tid < nr) {
+        s_rcsr[tid] = a.row_csr[d.row_begin + r0 + tid];
+        s_racc[tid] = a.row_acc[d.row_begin + r0 + tid];
+      }
+      if (tid == 0) s_racc[nr] = (r0 + nr < d.row_count) ? a.row_acc[d.row_begin + r0 + nr] : d.acc_used;
+      __syncthreads();
+      for (int r = warp; r < nr; r += kWarps) {
+        const int s0 = s_rcsr[r], a0 = s_racc[r], len = s_racc[r + 1] - a0;
+        for (int k = lane; k < len; k += 32) out[s0 + k] = A::out(acc[a0 + k]);
+      }
+      __syncthreads();
     }
-    __syncthreads();
   }
-  // ---- write the owned rows
-  V* out = reinterpret_cast<V*>(a.values);
-  for (int r = warp; r < d.row_count; r += kWarps) {
-    const int row = a.rows[d.row_begin + r];
-    const int base = a.row_acc[d.row_begin + r];
-    const int s0 = a.rowptr[row], len = a.rowptr[row + 1] - s0;
-    for (int k = lane; k < len; k += 32) out[s0 + k] = acc[base + k];
+  if (failed) {
+    // let copies still in flight land before the CTA's shared memory goes away
+    for (int st = 0; st < 2; ++st)
+      if ((pend_nodes >> st) & 1u) mbar_wait(&bar_nodes[st], (ph_nodes >> st) & 1u);
+    if (pend_ent) mbar_wait(bar_ent, ph_ent);
+    if (tid == 0) {
+      atomicExch(&a.counters[2], (uint32_t)kDevErrTimeout);
+      atomicExch(&a.counters[3], (uint32_t)blockIdx.x);
+    }
+  }
+  __syncthreads();
+  if (tid == 0) {
+    __threadfence();
+    if (atomicAdd(&a.counters[1], 1u) == gridDim.x - 1) {
+      a.counters[0] = 0;
+      a.counters[1] = 0;
+      __threadfence();
+    }
   }
 }
 
-template <int ORDER, typename V>
-static size_t assemble_smem()
+template <int ORDER, int MODE>
+static mg_status launch_assemble_t(AsmArgs a, cudaStream_t st)
 {
-  constexpr int NB2 = ORDER == 1 ? 16 : 100;
-  constexpr int CI = ORDER == 1 ? kChunkP1 : kChunkP2;
-  return sizeof(V) * (kAccMax + CI * NB2 + 1 + 7 * NB2);
-}
-
-template <int ORDER, typename V>
-static mg_status launch_assemble_t(const AsmArgs& a, int nblocks, int stiff, cudaStream_t st)
-{
-  const size_t smem = assemble_smem<ORDER, V>();
-  static bool configured = false;
-  if (!configured) {
-    MG_CUDA(cudaFuncSetAttribute(k_assemble<ORDER, V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem));
-    configured = true;
+  const size_t smem = AsmLayout<ORDER, MODE>::total(a.ent_cap);
+  static size_t configured = 0;
+  static int per_sm = 0, sms = 0;
+  if (configured != smem) {
+    MG_CUDA(cudaFuncSetAttribute(k_assemble<ORDER, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_assemble<ORDER, MODE>, kThreads, smem));
+    int dev = 0;
+    MG_CUDA(cudaGetDevice(&dev));
+    MG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    configured = smem;
   }
-  if (nblocks > 0) k_assemble<ORDER, V><<<nblocks, kThreads, smem, st>>>(a, stiff);
+  if (per_sm < 1) return set_error(MG_ERR_SIZE, "assembly CTA does not fit on an SM (shared memory)");
+  const int grid = std::max(1, std::min(a.nblocks, per_sm * sms));
+  if (a.nblocks > 0) k_assemble<ORDER, MODE><<<grid, kThreads, smem, st>>>(a);
   MG_CUDA(cudaGetLastError());
   return MG_OK;
+}
+
+static bool native_f64()
+{
+  static int v = -1;
+  if (v < 0) {
+    const char* e = std::getenv("MG_ASSEMBLY_NATIVE_F64");
+    v = (e && e[0] == '1') ? 1 : 0;
+  }
+  return v == 1;
 }
 
 mg_status launch_assemble(mg_plan* p, int op, const double* d_coeff, double c, int quad, int prec,
@@ -272,44 +675,46 @@ mg_status launch_assemble(mg_plan* p, int op, const double* d_coeff, double c, i
   if (op < MG_OP_STIFF_KAPPA || op > MG_OP_MASS_COEFF)
     return set_error(MG_ERR_INVALID_ARG, "unknown operator " + std::to_string(op));
   if (prec != MG_F64 && prec != MG_F32) return set_error(MG_ERR_INVALID_ARG, "prec must be MG_F64 or MG_F32");
-  if (!d_values) return set_error(MG_ERR_INVALID_ARG, "mg_assemble: null values");
   const bool needs_coeff = (op == MG_OP_STIFF_KAPPA || op == MG_OP_MASS_COEFF);
   if (needs_coeff && !d_coeff && p->mesh->n_elem > 0)
     return set_error(MG_ERR_INVALID_ARG, "this operator needs the per-element coefficient array");
-  MG_TRY(plan_device(p));
   const RefTables* t = nullptr;
   const double* d_tab = nullptr;
-  MG_TRY(plan_tables(p, quad, &t, &d_tab));
+  MG_TRY(plan_tables(p, quad, &t, &d_tab));  // validates quad
+  if (p->nnz == 0) return MG_OK;  // empty mesh: nothing to write
+  if (!d_values) return set_error(MG_ERR_INVALID_ARG, "mg_assemble: null values");
+  MG_TRY(plan_device(p));
   mg_mesh* m = p->mesh;
   AsmArgs a;
   a.blocks = p->d_blocks;
   a.items = p->d_items;
-  a.chunk_ptr = p->d_chunk_ptr;
+  a.item_conn = p->d_item_conn;
+  a.chunks = p->d_chunks;
   a.entries = p->d_entries;
-  a.rows = p->d_rows;
+  a.row_csr = p->d_row_csr;
   a.row_acc = p->d_row_acc;
-  a.rowptr = p->d_rowptr;
-  a.conn = m->d_conn;
-  a.xyz = m->d_xyz;
-  a.xyz_hi = m->d_xyz_hi;
-  a.xyz_lo = m->d_xyz_lo;
+  a.geo = GeoPtrs{m->d_xyz, m->d_xyz_hi, m->d_xyz_mid, m->d_xyz_lo};
   a.coeff = needs_coeff ? d_coeff : nullptr;
   a.cconst = op == MG_OP_STIFF_CONST ? c : 1.0;
   a.tables = d_tab;
   a.wsum = t->wsum;
   a.values = d_values;
-  const int stiff = (op == MG_OP_STIFF_KAPPA || op == MG_OP_STIFF_CONST);
-  if (m->order == 1)
-    return prec == MG_F64 ? launch_assemble_t<1, double>(a, p->nblocks, stiff, st)
-                          : launch_assemble_t<1, float>(a, p->nblocks, stiff, st);
-  return prec == MG_F64 ? launch_assemble_t<2, double>(a, p->nblocks, stiff, st)
-                        : launch_assemble_t<2, float>(a, p->nblocks, stiff, st);
+  a.counters = p->d_counters;
+  a.nblocks = p->nblocks;
+  a.stiff = (op == MG_OP_STIFF_KAPPA || op == MG_OP_STIFF_CONST);
+  a.ent_cap = (int)((p->max_chunk_entries + 3) / 4 * 4);
+  if (m->order == 1) {
+    if (prec == MG_F32) return launch_assemble_t<1, kF32>(a, st);
+    return native_f64() ? launch_assemble_t<1, kF64>(a, st) : launch_assemble_t<1, kDW>(a, st);
+  }
+  if (prec == MG_F32) return launch_assemble_t<2, kF32>(a, st);
+  return native_f64() ? launch_assemble_t<2, kF64>(a, st) : launch_assemble_t<2, kDW>(a, st);
 }
 
 // --------------------------------------------------------------- Dirichlet --
 template <typename V>
-__global__ void k_dirichlet(int64_t ndof, const int32_t* rowptr, const int32_t* colind,
-                            const uint8_t* mask, V* values, double* b)
+__global__ void k_dirichlet(int64_t ndof, const int32_t* rowptr, const int32_t* colind, const uint8_t* mask,
+                            V* values, double* b)
 {
   const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (r >= ndof) return;
@@ -323,53 +728,54 @@ __global__ void k_dirichlet(int64_t ndof, const int32_t* rowptr, const int32_t* 
 }
 
 // ----------------------------------------------------------------- adjoint --
-// grad_e = -sum_{i,j} lambda[dof_j] Khat(field i, test j) u[dof_i], Khat the
-// kappa = 1 stiffness of element e.
+// grad_e = -sum_{i,j} lambda[dof_j] Khat_ij u[dof_i], Khat the kappa = 1
+// stiffness of element e (symmetric).  Double-word arithmetic on the FP32
+// pipes; u and lambda are FP64 and enter as double-word values.
 template <int ORDER>
-__global__ void k_adjoint(int64_t n_elem, const int4* conn, const int32_t* dofs,
-                          const double4_32a* xyz, const double* tables, double wsum,
-                          const double* u, const double* lam, double* grad)
+__global__ void __launch_bounds__(256) k_adjoint(int64_t n_elem, const int4* conn, const int32_t* dofs, GeoPtrs geo,
+                                                 const double* tables, double wsum, const double* u,
+                                                 const double* lam, double* grad)
 {
-  constexpr int NB = ORDER == 1 ? 4 : 10, NB2 = NB * NB;
-  __shared__ double tab[6 * NB2];
-  for (int i = threadIdx.x; i < 6 * NB2; i += blockDim.x) tab[i] = tables[i];
+  constexpr int NB = ORDER == 1 ? 4 : 10, NU = ORDER == 1 ? 10 : 55;
+  __shared__ ff tab[6 * NU];
+  for (int i = threadIdx.x; i < 6 * NU; i += blockDim.x) tab[i] = ff_from_double(tables[i]);
   __syncthreads();
   const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (e >= n_elem) return;
   const int4 n = conn[e];
-  Cof<double> f;
-  cofactors64(xyz, n, f);
-  double ue[NB], le[NB];
+  Cof<ff> f;
+  geometry_now<kDW>(geo, n, f);
+  ff ue[NB], le[NB];
 #pragma unroll
   for (int i = 0; i < NB; ++i) {
     const int dof = dofs[e * NB + i];
-    ue[i] = u[dof];
-    le[i] = lam[dof];
+    ue[i] = ff_from_double(u[dof]);
+    le[i] = ff_from_double(lam[dof]);
   }
-  double s = 0.0;
+  ff s = ff_make(0.0f);
   if (ORDER == 1) {
-    double K[16];
-    p1_stiff<double>(f, wsum / f.det, K);
+    ff K[10];
+    p1_stiff_unique<ff>(f, ff_from_double(wsum) / f.det, K);
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
-      for (int j = 0; j < 4; ++j) s += le[j] * K[i * 4 + j] * ue[i];
+      for (int j = 0; j < 4; ++j) s = s + le[j] * K[sym_index(i, j, 4)] * ue[i];
   } else {
-    double g[6];
-    metric<double>(f, 1.0 / f.det, g);
+    ff g[6];
+    metric<ff>(f, ff_make(1.0f) / f.det, g);
     for (int i = 0; i < NB; ++i) {
-      double row = 0.0;
+      ff row = ff_make(0.0f);
       for (int j = 0; j < NB; ++j) {
-        const int k = i * NB + j;
-        double v = g[0] * tab[k];
+        const int uidx = sym_index(i, j, NB);
+        ff v = g[0] * tab[uidx];
 #pragma unroll
-        for (int p = 1; p < 6; ++p) v += g[p] * tab[p * NB2 + k];
-        row += le[j] * v;
+        for (int p = 1; p < 6; ++p) v = v + g[p] * tab[p * NU + uidx];
+        row = row + le[j] * v;
       }
-      s += row * ue[i];
+      s = s + row * ue[i];
     }
   }
-  grad[e] = -s;
+  grad[e] = -ff_to_double(s);
 }
 
 }  // namespace mg
@@ -378,17 +784,33 @@ using namespace mg;
 
 extern "C" {
 
-mg_status mg_assemble(mg_plan* plan, int32_t op, const double* d_coeff, double c, int32_t quad,
-                      int32_t prec, void* d_values, void* stream)
+mg_status mg_assemble(mg_plan* plan, int32_t op, const double* d_coeff, double c, int32_t quad, int32_t prec,
+                      void* d_values, void* stream)
 {
   if (!plan) return set_error(MG_ERR_INVALID_ARG, "mg_assemble: null plan");
   return launch_assemble(plan, op, d_coeff, c, quad, prec, d_values, (cudaStream_t)stream);
 }
 
-mg_status mg_assemble_host(mg_plan* p, int32_t op, const double* h_coeff, double c, int32_t quad,
-                           int32_t prec, void* h_values, void* stream)
+mg_status mg_plan_status(mg_plan* p)
 {
-  if (!p || !h_values) return set_error(MG_ERR_INVALID_ARG, "mg_assemble_host: null argument");
+  if (!p) return set_error(MG_ERR_INVALID_ARG, "mg_plan_status: null plan");
+  if (!p->on_device) return MG_OK;
+  MG_CUDA(cudaDeviceSynchronize());
+  uint32_t c[4];
+  MG_CUDA(cudaMemcpy(c, p->d_counters, sizeof(c), cudaMemcpyDeviceToHost));
+  if (c[2]) {
+    const uint32_t zero[2] = {0u, 0u};
+    MG_CUDA(cudaMemcpy(p->d_counters + 2, zero, sizeof(zero), cudaMemcpyHostToDevice));
+    return set_error(MG_ERR_CUDA, "assembly kernel: a bulk-copy wait timed out in CTA " + std::to_string(c[3]) +
+                                      "; the values of that call are incomplete");
+  }
+  return MG_OK;
+}
+
+mg_status mg_assemble_host(mg_plan* p, int32_t op, const double* h_coeff, double c, int32_t quad, int32_t prec,
+                           void* h_values, void* stream)
+{
+  if (!p || (!h_values && p->nnz > 0)) return set_error(MG_ERR_INVALID_ARG, "mg_assemble_host: null argument");
   MG_TRY(plan_device(p));
   cudaStream_t st = (cudaStream_t)stream;
   const size_t vbytes = (size_t)p->nnz * (prec == MG_F64 ? 8 : 4);
@@ -413,13 +835,13 @@ mg_status mg_assemble_host(mg_plan* p, int32_t op, const double* h_coeff, double
     d_coeff = p->d_tmp_coeff;
   }
   MG_TRY(launch_assemble(p, op, d_coeff, c, quad, prec, p->d_tmp_values, st));
-  MG_CUDA(cudaMemcpyAsync(h_values, p->d_tmp_values, vbytes, cudaMemcpyDeviceToHost, st));
+  if (vbytes) MG_CUDA(cudaMemcpyAsync(h_values, p->d_tmp_values, vbytes, cudaMemcpyDeviceToHost, st));
   MG_CUDA(cudaStreamSynchronize(st));
-  return MG_OK;
+  return mg_plan_status(p);
 }
 
-mg_status mg_apply_dirichlet(mg_plan* p, const uint8_t* d_mask, int32_t prec, void* d_values,
-                             double* d_b, void* stream)
+mg_status mg_apply_dirichlet(mg_plan* p, const uint8_t* d_mask, int32_t prec, void* d_values, double* d_b,
+                             void* stream)
 {
   if (!p || !d_mask || !d_values) return set_error(MG_ERR_INVALID_ARG, "mg_apply_dirichlet: null argument");
   if (prec != MG_F64 && prec != MG_F32) return set_error(MG_ERR_INVALID_ARG, "bad precision");
@@ -429,42 +851,44 @@ mg_status mg_apply_dirichlet(mg_plan* p, const uint8_t* d_mask, int32_t prec, vo
   cudaStream_t st = (cudaStream_t)stream;
   if (blocks > 0) {
     if (prec == MG_F64)
-      k_dirichlet<double><<<blocks, threads, 0, st>>>(p->ndof, p->d_rowptr, p->d_colind, d_mask,
-                                                      (double*)d_values, d_b);
+      k_dirichlet<double><<<blocks, threads, 0, st>>>(p->ndof, p->d_rowptr, p->d_colind, d_mask, (double*)d_values,
+                                                      d_b);
     else
-      k_dirichlet<float><<<blocks, threads, 0, st>>>(p->ndof, p->d_rowptr, p->d_colind, d_mask,
-                                                     (float*)d_values, d_b);
+      k_dirichlet<float><<<blocks, threads, 0, st>>>(p->ndof, p->d_rowptr, p->d_colind, d_mask, (float*)d_values,
+                                                     d_b);
   }
   MG_CUDA(cudaGetLastError());
   return MG_OK;
 }
 
-mg_status mg_adjoint_grad(mg_plan* p, const double* d_u, const double* d_lambda, int32_t quad,
-                          double* d_grad, void* stream)
+mg_status mg_adjoint_grad(mg_plan* p, const double* d_u, const double* d_lambda, int32_t quad, double* d_grad,
+                          void* stream)
 {
-  if (!p || !d_u || !d_lambda || !d_grad) return set_error(MG_ERR_INVALID_ARG, "mg_adjoint_grad: null argument");
-  MG_TRY(plan_device(p));
+  if (!p || !d_u || !d_lambda || (!d_grad && p->mesh->n_elem > 0))
+    return set_error(MG_ERR_INVALID_ARG, "mg_adjoint_grad: null argument");
   const RefTables* t = nullptr;
   const double* d_tab = nullptr;
   MG_TRY(plan_tables(p, quad, &t, &d_tab));
+  MG_TRY(plan_device(p));
   mg_mesh* m = p->mesh;
   const int threads = 256;
   const int blocks = (int)((m->n_elem + threads - 1) / threads);
   cudaStream_t st = (cudaStream_t)stream;
+  const GeoPtrs geo{m->d_xyz, m->d_xyz_hi, m->d_xyz_mid, m->d_xyz_lo};
   if (blocks > 0) {
     if (m->order == 1)
-      k_adjoint<1><<<blocks, threads, 0, st>>>(m->n_elem, m->d_conn, m->d_dofs, m->d_xyz, d_tab,
-                                               t->wsum, d_u, d_lambda, d_grad);
+      k_adjoint<1><<<blocks, threads, 0, st>>>(m->n_elem, m->d_conn, m->d_dofs, geo, d_tab, t->wsum, d_u, d_lambda,
+                                               d_grad);
     else
-      k_adjoint<2><<<blocks, threads, 0, st>>>(m->n_elem, m->d_conn, m->d_dofs, m->d_xyz, d_tab,
-                                               t->wsum, d_u, d_lambda, d_grad);
+      k_adjoint<2><<<blocks, threads, 0, st>>>(m->n_elem, m->d_conn, m->d_dofs, geo, d_tab, t->wsum, d_u, d_lambda,
+                                               d_grad);
   }
   MG_CUDA(cudaGetLastError());
   return MG_OK;
 }
 
-mg_status mg_assemble_rhs(mg_plan* p, const double* d_field, const double* d_elem_scale, int32_t quad,
-                          double* d_b, void* stream)
+mg_status mg_assemble_rhs(mg_plan* p, const double* d_field, const double* d_elem_scale, int32_t quad, double* d_b,
+                          void* stream)
 {
   if (!p || !d_b) return set_error(MG_ERR_INVALID_ARG, "mg_assemble_rhs: null argument");
   MG_TRY(plan_device(p));

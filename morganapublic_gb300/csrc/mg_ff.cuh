@@ -1,0 +1,154 @@
+// Double-word ("float-float") arithmetic on the FP32 pipes.
+//
+// GB300 issues FP64 at about 1/60 of its FP32 rate (measured here: 1.20 vs 70
+// TFLOP/s of FMA), so the FP64-accurate assembly path carries each value as an
+// unevaluated sum hi + lo of two floats (|lo| <= ulp(hi)/2, ~48 significant bits,
+// relative error of one operation ~2^-47) and runs on the FP32 units.
+//
+// Building blocks (published error-free transformations):
+//   two_sum        Knuth (TAOCP vol. 2): s + e = a + b exactly, any order of |a|, |b|
+//   fast_two_sum   Dekker (1971): s + e = a + b exactly when |a| >= |b|
+//   two_prod       with a fused multiply-add: p + e = a * b exactly
+//   add / mul / div  the double-word algorithms analysed by Joldes, Muller and
+//                  Popescu, "Tight and rigorous error bounds for basic building
+//                  blocks of double-word arithmetic", ACM TOMS 44(2), 2017
+//                  (AccurateDWPlusDW, DWTimesDW with FMA, and a Newton-corrected
+//                  DW division).
+// Everything here is plain IEEE float arithmetic; the compiler must not
+// re-associate it (nvcc does not without --use_fast_math, which is not used).
+#pragma once
+
+#include <cstdint>
+
+namespace mg {
+
+struct ff {
+  float hi, lo;
+};
+
+__device__ __forceinline__ ff ff_make(float hi) { return ff{hi, 0.0f}; }
+
+__device__ __forceinline__ ff two_sum(float a, float b)
+{
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return ff{s, e};
+}
+
+__device__ __forceinline__ ff fast_two_sum(float a, float b)
+{
+  const float s = __fadd_rn(a, b);
+  const float e = __fsub_rn(b, __fsub_rn(s, a));
+  return ff{s, e};
+}
+
+__device__ __forceinline__ ff two_prod(float a, float b)
+{
+  const float p = __fmul_rn(a, b);
+  const float e = __fmaf_rn(a, b, -p);
+  return ff{p, e};
+}
+
+// AccurateDWPlusDW (relative error <= 3u^2 + 13u^3, u = 2^-24)
+__device__ __forceinline__ ff ff_add(ff a, ff b)
+{
+  ff s = two_sum(a.hi, b.hi);
+  const ff t = two_sum(a.lo, b.lo);
+  s.lo = __fadd_rn(s.lo, t.hi);
+  s = fast_two_sum(s.hi, s.lo);
+  s.lo = __fadd_rn(s.lo, t.lo);
+  return fast_two_sum(s.hi, s.lo);
+}
+
+// SloppyDWPlusDW: two_sum of the high parts, low parts added in float.  Its
+// error is bounded relative to max(|a|, |b|) (not to |a + b|), which is what a
+// sum of element contributions or a cofactor needs; 11 operations instead of 20.
+__device__ __forceinline__ ff ff_add_s(ff a, ff b)
+{
+  ff s = two_sum(a.hi, b.hi);
+  s.lo = __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo));
+  return fast_two_sum(s.hi, s.lo);
+}
+
+// a.b of two 3-vectors: error-free products of the high parts chained with
+// two_sum, every low-order term collected in one float, one renormalisation.
+__device__ __forceinline__ ff ff_dot3(const ff* a, const ff* b)
+{
+  ff p = two_prod(a[0].hi, b[0].hi);
+  float lo = __fmaf_rn(a[0].hi, b[0].lo, __fmaf_rn(a[0].lo, b[0].hi, p.lo));
+  float hi = p.hi;
+#pragma unroll
+  for (int k = 1; k < 3; ++k) {
+    const ff q = two_prod(a[k].hi, b[k].hi);
+    const ff s = two_sum(hi, q.hi);
+    hi = s.hi;
+    lo = __fadd_rn(lo, __fadd_rn(s.lo, __fmaf_rn(a[k].hi, b[k].lo, __fmaf_rn(a[k].lo, b[k].hi, q.lo))));
+  }
+  return two_sum(hi, lo);  // the dot may cancel below its low part
+}
+
+// a * b - c * d in the same style (the cofactor pattern).
+__device__ __forceinline__ ff ff_cross(ff a, ff b, ff c, ff d)
+{
+  const ff p = two_prod(a.hi, b.hi), q = two_prod(-c.hi, d.hi);
+  const ff s = two_sum(p.hi, q.hi);
+  float lo = __fadd_rn(s.lo, __fadd_rn(p.lo, q.lo));
+  lo = __fadd_rn(lo, __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, 0.0f)));
+  lo = __fsub_rn(lo, __fmaf_rn(c.hi, d.lo, __fmaf_rn(c.lo, d.hi, 0.0f)));
+  return two_sum(s.hi, lo);
+}
+
+// Running sum with deferred renormalisation: hi + lo are accumulated apart
+// (two_sum on the high parts, low parts and errors in one float) and
+// renormalised once at the end by ff_acc_value.
+struct ff_acc {
+  float hi, lo;
+};
+__device__ __forceinline__ void ff_acc_add(ff_acc& s, ff x)
+{
+  const ff t = two_sum(s.hi, x.hi);
+  s.hi = t.hi;
+  s.lo = __fadd_rn(s.lo, __fadd_rn(t.lo, x.lo));
+}
+__device__ __forceinline__ ff ff_acc_value(const ff_acc& s) { return two_sum(s.hi, s.lo); }
+
+__device__ __forceinline__ ff ff_neg(ff a) { return ff{-a.hi, -a.lo}; }
+__device__ __forceinline__ ff ff_sub(ff a, ff b) { return ff_add(a, ff_neg(b)); }
+
+// DWTimesDW with FMA (relative error <= 5u^2)
+__device__ __forceinline__ ff ff_mul(ff a, ff b)
+{
+  ff p = two_prod(a.hi, b.hi);
+  float t = __fmul_rn(a.hi, b.lo);
+  t = __fmaf_rn(a.lo, b.hi, t);
+  p.lo = __fadd_rn(p.lo, t);
+  return fast_two_sum(p.hi, p.lo);
+}
+
+// a * b + c * d with one renormalisation (the cofactor pattern)
+__device__ __forceinline__ ff ff_mul_add(ff a, ff b, ff c, ff d) { return ff_add(ff_mul(a, b), ff_mul(c, d)); }
+
+// Division: q1 = a.hi / b.hi, remainder r = a - q1 b in double-word, one
+// correction q2 = r.hi / b.hi (Newton step); relative error ~2^-46.
+__device__ __forceinline__ ff ff_div(ff a, ff b)
+{
+  const float q1 = __fdiv_rn(a.hi, b.hi);
+  const ff r = ff_sub(a, ff_mul(b, ff_make(q1)));
+  const float q2 = __fdiv_rn(r.hi, b.hi);
+  return fast_two_sum(q1, q2);
+}
+
+// Exact split of a double into hi + lo floats with |lo| <= ulp(hi)/2 (to the
+// rounding of lo, relative 2^-48), done with FP64 conversions: only used off the
+// hot loop (one coefficient per element).
+__device__ __forceinline__ ff ff_from_double(double x)
+{
+  const float hi = __double2float_rn(x);
+  const float lo = __double2float_rn(x - (double)hi);
+  return ff{hi, lo};
+}
+
+__device__ __forceinline__ double ff_to_double(ff a) { return (double)a.hi + (double)a.lo; }
+
+}  // namespace mg

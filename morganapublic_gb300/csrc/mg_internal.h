@@ -34,14 +34,26 @@ constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 // Accumulator slots (CSR entries of the rows a CTA owns) held in shared memory.
 constexpr int kAccMax = 8192;
-constexpr int kAccDiv = kAccMax / kThreads;  // slots per thread
 // Elements ("items") per chunk: one thread per P1 element, eight per P2 element.
 constexpr int kChunkP1 = 256;
 constexpr int kChunkP2 = 32;
 constexpr int kP2ThreadsPerItem = kThreads / kChunkP2;
+// Contribution-list word: source (13 bits) | accumulator slot (14 bits) << 13 |
+// end-of-segment flag << 31.  The source indexes the chunk's element matrices,
+// stored symmetric (nb (nb + 1) / 2 unique entries) and entry-major.
+constexpr uint32_t kSrcBits = 13, kSlotBits = 14;
+constexpr uint32_t kSrcMask = (1u << kSrcBits) - 1, kSlotMask = (1u << kSlotBits) - 1;
+constexpr uint32_t kEndFlag = 1u << 31;
 
 inline int nbasis(int order) { return order == 1 ? 4 : 10; }
+inline int nunique(int order) { return order == 1 ? 10 : 55; }
 inline int chunk_items(int order) { return order == 1 ? kChunkP1 : kChunkP2; }
+// Index of the symmetric pair (i, j), i <= j, in row-major upper-triangle order.
+inline __host__ __device__ int sym_index(int i, int j, int nb)
+{
+  if (i > j) { const int t = i; i = j; j = t; }
+  return i * nb - i * (i - 1) / 2 + (j - i);
+}
 
 // One CTA of the assembly kernel: a set of owned rows plus every element that
 // touches one of them.
@@ -55,6 +67,15 @@ struct BlockDesc {
   int32_t acc_used;     // accumulator slots in use
   int32_t pad;
 };
+
+// Contribution words of one chunk: a 64-byte record the kernel stages into
+// shared memory with the chunk's element nodes.
+struct ChunkDesc {
+  int64_t word_begin;         // first word of the chunk in entries[] (multiple of 32)
+  int32_t warp_off[kWarps + 1];  // per-warp offsets relative to word_begin; [kWarps] = chunk size
+  int32_t pad[5];
+};
+static_assert(sizeof(ChunkDesc) == 64, "ChunkDesc must stay 64 bytes");
 
 // Reference-element tables for one (order, quadrature) pair, with the quadrature
 // weights folded in.  stiff[ab][i*nb+j] = sum_q w_q dphi_i/dxi_a dphi_j/dxi_b for
@@ -88,7 +109,8 @@ struct mg_mesh {
   std::vector<int32_t> dofs;        // n_elem * nb
   // device copies
   double4_32a* d_xyz = nullptr;      // (x, y, z, 0)
-  float4* d_xyz_hi = nullptr;    // float pair split: x = hi + lo exactly to ~2^-48
+  float4* d_xyz_hi = nullptr;    // x = hi + mid + lo exactly (three floats)
+  float4* d_xyz_mid = nullptr;
   float4* d_xyz_lo = nullptr;
   int4* d_conn = nullptr;        // vertex node ids
   int32_t* d_dofs = nullptr;     // n_elem * nb
@@ -104,13 +126,18 @@ struct mg_plan {
   int32_t* d_diag = nullptr;  // slot of the diagonal entry of each row
   // assembly schedule
   int32_t nblocks = 0;
-  int64_t n_items = 0, n_chunks = 0, n_entries = 0, n_contrib = 0;
+  int64_t n_items = 0, n_item_slots = 0, n_chunks = 0, n_entries = 0, n_contrib = 0;
   mg::BlockDesc* d_blocks = nullptr;
   int32_t* d_items = nullptr;
   int64_t* d_chunk_ptr = nullptr;  // (kWarps + 1) per chunk, offsets into entries
+  mg::ChunkDesc* d_chunks = nullptr;  // the same offsets as 64-byte records
+  int32_t* d_row_csr = nullptr;       // CSR start of each owned row (schedule order)
   uint32_t* d_entries = nullptr;   // (slot / kThreads) << 16 | source index
   int32_t* d_rows = nullptr;
   int32_t* d_row_acc = nullptr;
+  int4* d_item_conn = nullptr;      // vertex nodes of each item, schedule order
+  uint32_t* d_counters = nullptr;   // [0] work counter, [1] exit counter, [2] device error, [3] detail
+  int64_t max_chunk_entries = 0;
   // reference tables, cached per (quad) on the device
   std::vector<mg::RefTables> tables;
   std::vector<double*> d_tables;  // parallel to tables: stiff (6 nb^2) then mass (nb^2)
@@ -135,6 +162,7 @@ struct HostSchedule {
   std::vector<int64_t> chunk_ptr;
   std::vector<uint32_t> entries;
   int64_t n_contrib = 0;
+  int64_t max_chunk_entries = 0;
 };
 mg_status mesh_device(mg_mesh* m);  // uploads the mesh on first GPU use
 mg_status plan_device(mg_plan* p);  // uploads mesh + plan on first GPU use

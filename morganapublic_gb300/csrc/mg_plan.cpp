@@ -8,16 +8,20 @@
 // Schedule: the rows (dofs) are cut into blocks along a Morton curve of the dof
 // positions, each holding at most kAccMax CSR entries.  One CTA owns one block:
 // it recomputes every element touching one of its rows ("items", sorted by
-// element id) and sums each owned CSR entry in shared memory.  Accumulator slot
-// s of a block is only ever updated by thread s % kThreads, so the reduction
-// needs neither atomics nor a second pass, and every slot adds its element
-// contributions in increasing element order -- the order in which the
-// reference inserts them.  The contribution lists are stored per chunk of
-// items, per warp, interleaved by lane ([k][lane]) and padded to the warp's
-// longest list, so that phase 2 of the kernel reads them fully coalesced.
+// element id) and sums each owned CSR entry in shared memory.  The items are
+// processed in chunks; the contributions of a chunk are sorted by accumulator
+// slot into segments (one per slot, in element order), and the segments are
+// dealt to the CTA's threads longest-first to the least-loaded thread.  A
+// thread sums each of its segments sequentially and adds the sum to the slot,
+// so within a chunk every slot is written by exactly one thread: no atomics, no
+// second pass, and a summation order fixed by the plan (bitwise reproducible).
+// Each thread's words are interleaved by lane ([k][lane]) within its warp and
+// padded to the warp's longest list, so the chunk is one contiguous, 128-byte
+// aligned region the kernel stages into shared memory with a bulk copy.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <numeric>
 
 #include "mg_internal.h"
@@ -186,28 +190,48 @@ static mg_status build_schedule(mg_plan* p, HostSchedule* hs)
       for (int u = 0; u < n; ++u) hs->items[f[bs[u]]++] = (int32_t)e;
     }
   }
+  // pad every block's item list to a multiple of 4 (16-byte aligned bulk copies)
+  {
+    std::vector<int32_t> padded;
+    padded.reserve(hs->items.size() + 4 * (size_t)nbk);
+    for (int32_t b = 0; b < nbk; ++b) {
+      const int64_t i0 = bcount[b], i1 = bcount[b + 1];
+      hs->blocks[b].item_begin = (int32_t)padded.size();
+      hs->blocks[b].item_count = (int32_t)(i1 - i0);
+      for (int64_t k = i0; k < i1; ++k) padded.push_back(hs->items[k]);
+      while (padded.size() % 4) padded.push_back(-1);
+    }
+    if ((int64_t)padded.size() >= INT32_MAX) return set_error(MG_ERR_SIZE, "assembly items above 2^31-1");
+    hs->items.swap(padded);
+  }
   int64_t nchunk_tot = 0;
   for (int32_t b = 0; b < nbk; ++b) {
     BlockDesc& d = hs->blocks[b];
-    d.item_begin = (int32_t)bcount[b];
-    d.item_count = (int32_t)(bcount[b + 1] - bcount[b]);
     d.chunk_begin = (int32_t)nchunk_tot;
     d.nchunks = (d.item_count + CI - 1) / CI;
     nchunk_tot += d.nchunks;
   }
   // contribution lists, per block in parallel, then concatenated
+  const int nu = nunique(m->order);
+  const uint32_t zero_src = (uint32_t)(nu * CI);
+  if (zero_src > kSrcMask) return set_error(MG_ERR_SIZE, "chunk buffer above the 13-bit source index");
+  if (kAccMax > (int)kSlotMask + 1) return set_error(MG_ERR_SIZE, "accumulator above the 14-bit slot index");
   std::vector<std::vector<uint32_t>> ent(nbk);
   std::vector<std::vector<int64_t>> cptr(nbk);
-  std::vector<int64_t> contrib(nbk, 0);
-  const int32_t zero_src = CI * nb2;
+  std::vector<int64_t> contrib(nbk, 0), maxc(nbk, 0);
 #pragma omp parallel
   {
+    struct Seg { int32_t slot, begin, len; };
     std::vector<std::vector<uint32_t>> per(kThreads);
+    std::vector<std::pair<int32_t, uint32_t>> list;  // (slot, src) in item order
+    std::vector<Seg> segs;
+    std::vector<uint32_t> srcs;
+    std::vector<int64_t> heap;
 #pragma omp for schedule(dynamic, 1)
     for (int32_t b = 0; b < nbk; ++b) {
       const BlockDesc& d = hs->blocks[b];
       for (int32_t c = 0; c < d.nchunks; ++c) {
-        for (auto& v : per) v.clear();
+        list.clear();
         const int32_t i0 = c * CI, i1 = std::min(d.item_count, i0 + CI);
         for (int32_t it = i0; it < i1; ++it) {
           const int64_t e = hs->items[d.item_begin + it];
@@ -221,12 +245,43 @@ static mg_status build_schedule(mg_plan* p, HostSchedule* hs)
               const int32_t* c1 = p->colind.data() + p->rowptr[row + 1];
               const int32_t pos = (int32_t)(std::lower_bound(c0, c1, col) - c0);
               const int32_t acc = row_acc_of[row] + pos;
-              const uint32_t src = (uint32_t)((i * nb + j) * CI + t);
-              per[acc % kThreads].push_back(((uint32_t)(acc / kThreads) << 16) | src);
-              contrib[b]++;
+              list.emplace_back(acc, (uint32_t)(sym_index(i, j, nb) * CI + t));
             }
           }
         }
+        contrib[b] += (int64_t)list.size();
+        // segments: one per slot, contributions kept in item (= element) order
+        std::stable_sort(list.begin(), list.end(),
+                         [](const std::pair<int32_t, uint32_t>& x, const std::pair<int32_t, uint32_t>& y) {
+                           return x.first < y.first;
+                         });
+        segs.clear();
+        srcs.clear();
+        for (size_t k = 0; k < list.size(); ++k) {
+          if (k == 0 || list[k].first != list[k - 1].first) segs.push_back({list[k].first, (int32_t)k, 0});
+          segs.back().len++;
+          srcs.push_back(list[k].second);
+        }
+        // longest segment first, to the least-loaded thread (ties: lowest thread)
+        std::stable_sort(segs.begin(), segs.end(), [](const Seg& x, const Seg& y) { return x.len > y.len; });
+        for (auto& v : per) v.clear();
+        // min-heap of (load, thread): pops the least-loaded, lowest-numbered thread
+        heap.clear();
+        for (int t = 0; t < kThreads; ++t) heap.push_back(((int64_t)0 << 32) | t);
+        std::make_heap(heap.begin(), heap.end(), std::greater<int64_t>());
+        for (const Seg& sg : segs) {
+          std::pop_heap(heap.begin(), heap.end(), std::greater<int64_t>());
+          const int64_t top = heap.back();
+          const int best = (int)(top & 0xffffffff);
+          heap.back() = (((top >> 32) + sg.len) << 32) | best;
+          std::push_heap(heap.begin(), heap.end(), std::greater<int64_t>());
+          for (int k = 0; k < sg.len; ++k) {
+            uint32_t w = srcs[sg.begin + k] | ((uint32_t)sg.slot << kSrcBits);
+            if (k == sg.len - 1) w |= kEndFlag;
+            per[best].push_back(w);
+          }
+        }
+        const int64_t base = (int64_t)ent[b].size();
         for (int w = 0; w < kWarps; ++w) {
           cptr[b].push_back((int64_t)ent[b].size());
           size_t K = 0;
@@ -234,10 +289,11 @@ static mg_status build_schedule(mg_plan* p, HostSchedule* hs)
           for (size_t k = 0; k < K; ++k)
             for (int l = 0; l < 32; ++l) {
               const auto& v = per[32 * w + l];
-              ent[b].push_back(k < v.size() ? v[k] : (uint32_t)zero_src);
+              ent[b].push_back(k < v.size() ? v[k] : zero_src);
             }
         }
         cptr[b].push_back((int64_t)ent[b].size());
+        maxc[b] = std::max(maxc[b], (int64_t)ent[b].size() - base);
       }
     }
   }
@@ -252,13 +308,17 @@ static mg_status build_schedule(mg_plan* p, HostSchedule* hs)
     ck += hs->blocks[b].nchunks;
     off += (int64_t)ent[b].size();
     hs->n_contrib += contrib[b];
+    hs->max_chunk_entries = std::max(hs->max_chunk_entries, maxc[b]);
     std::vector<uint32_t>().swap(ent[b]);
   }
   p->nblocks = nbk;
-  p->n_items = (int64_t)hs->items.size();
+  p->n_items = 0;
+  for (int32_t b = 0; b < nbk; ++b) p->n_items += hs->blocks[b].item_count;
+  p->n_item_slots = (int64_t)hs->items.size();
   p->n_chunks = nchunk_tot;
   p->n_entries = total;
   p->n_contrib = hs->n_contrib;
+  p->max_chunk_entries = hs->max_chunk_entries;
   return MG_OK;
 }
 
@@ -287,9 +347,34 @@ mg_status plan_device(mg_plan* p)
   MG_TRY(upload(&p->d_blocks, hs.blocks));
   MG_TRY(upload(&p->d_items, hs.items));
   MG_TRY(upload(&p->d_chunk_ptr, hs.chunk_ptr));
+  {
+    const int64_t nc = (int64_t)hs.chunk_ptr.size() / (kWarps + 1);
+    std::vector<ChunkDesc> cd(nc);
+    for (int64_t c = 0; c < nc; ++c) {
+      const int64_t* cp = &hs.chunk_ptr[c * (kWarps + 1)];
+      cd[c].word_begin = cp[0];
+      for (int w = 0; w <= kWarps; ++w) cd[c].warp_off[w] = (int32_t)(cp[w] - cp[0]);
+      for (int k = 0; k < 5; ++k) cd[c].pad[k] = 0;
+    }
+    MG_TRY(upload(&p->d_chunks, cd));
+    std::vector<int32_t> rc(hs.rows.size());
+    for (size_t k = 0; k < hs.rows.size(); ++k) rc[k] = p->rowptr[hs.rows[k]];
+    MG_TRY(upload(&p->d_row_csr, rc));
+  }
   MG_TRY(upload(&p->d_entries, hs.entries));
   MG_TRY(upload(&p->d_rows, hs.rows));
   MG_TRY(upload(&p->d_row_acc, hs.row_acc));
+  {
+    std::vector<int4> ic(hs.items.size());
+    for (size_t k = 0; k < hs.items.size(); ++k) {
+      const int32_t e = hs.items[k];
+      ic[k] = e < 0 ? make_int4(0, 0, 0, 0)
+                    : make_int4(p->mesh->conn[4 * (int64_t)e], p->mesh->conn[4 * (int64_t)e + 1],
+                                p->mesh->conn[4 * (int64_t)e + 2], p->mesh->conn[4 * (int64_t)e + 3]);
+    }
+    MG_TRY(upload(&p->d_item_conn, ic));
+  }
+  MG_TRY(upload(&p->d_counters, std::vector<uint32_t>(8, 0u)));
   MG_CUDA(cudaMallocHost(&p->h_pinned, 64 * sizeof(double)));
   delete p->host_schedule;
   p->host_schedule = nullptr;
@@ -306,9 +391,13 @@ static void free_plan(mg_plan* p)
   cudaFree(p->d_blocks);
   cudaFree(p->d_items);
   cudaFree(p->d_chunk_ptr);
+  cudaFree(p->d_chunks);
+  cudaFree(p->d_row_csr);
   cudaFree(p->d_entries);
   cudaFree(p->d_rows);
   cudaFree(p->d_row_acc);
+  cudaFree(p->d_item_conn);
+  cudaFree(p->d_counters);
   for (double* t : p->d_tables) cudaFree(t);
   cudaFree(p->d_work);
   cudaFree(p->d_tmp_values);
@@ -328,8 +417,15 @@ mg_status plan_tables(mg_plan* p, int quad, const RefTables** t, const double** 
     }
   RefTables rt;
   MG_TRY(build_ref_tables(p->mesh->order, quad, &rt));
-  std::vector<double> flat(rt.stiff);
-  flat.insert(flat.end(), rt.mass.begin(), rt.mass.end());
+  // device layout: unique (i <= j, sym_index order) entries, stiff[6][nu] then mass[nu]
+  const int nb = rt.nb, nu = nb * (nb + 1) / 2;
+  std::vector<double> flat(7 * nu);
+  for (int i = 0; i < nb; ++i)
+    for (int j = i; j < nb; ++j) {
+      const int u = sym_index(i, j, nb);
+      for (int q = 0; q < 6; ++q) flat[q * nu + u] = rt.stiff[q * nb * nb + i * nb + j];
+      flat[6 * nu + u] = rt.mass[i * nb + j];
+    }
   double* d = nullptr;
   MG_CUDA(cudaMalloc(&d, sizeof(double) * flat.size()));
   MG_CUDA(cudaMemcpy(d, flat.data(), sizeof(double) * flat.size(), cudaMemcpyHostToDevice));
@@ -421,6 +517,8 @@ mg_status mg_plan_schedule_info(const mg_plan* p, mg_schedule_info* info)
   info->n_chunks = p->n_chunks;
   info->n_entries = p->n_entries;
   info->n_contrib = p->n_contrib;
+  info->n_item_slots = p->n_item_slots;
+  info->max_chunk_entries = p->max_chunk_entries;
   return MG_OK;
 }
 

@@ -34,12 +34,13 @@ struct CgScalars {
   uint32_t ticket[4];
 };
 
+// Lanes per row: the smallest group whose kUnroll-deep pass covers the mean row.
 static int row_group(const mg_plan* p)
 {
   const double mean = p->ndof > 0 ? (double)p->nnz / (double)p->ndof : 1.0;
-  if (mean >= 24) return 32;
-  if (mean >= 12) return 16;
-  if (mean >= 6) return 8;
+  if (mean > 64) return 32;
+  if (mean > 32) return 16;
+  if (mean > 16) return 8;
   return 4;
 }
 
@@ -54,15 +55,33 @@ __device__ __forceinline__ unsigned group_mask()
   }
 }
 
+// Dot product of one CSR row with x by a group of G lanes.  Each pass issues
+// kUnroll independent loads of (column, value) per lane before any gather of x,
+// so every lane keeps kUnroll requests in flight; the G partial sums are then
+// combined by xor shuffles in a fixed order.
+constexpr int kUnroll = 4;
+
 template <typename V, int G>
 __device__ __forceinline__ double row_dot(int64_t row, const int32_t* __restrict__ rp,
                                           const int32_t* __restrict__ ci, const V* __restrict__ val,
                                           const V* __restrict__ x)
 {
   const int lane = threadIdx.x & (G - 1);
-  const int s0 = rp[row], s1 = rp[row + 1];
+  const int s0 = __ldg(rp + row), s1 = __ldg(rp + row + 1);
   V sum = V(0);
-  for (int s = s0 + lane; s < s1; s += G) sum += val[s] * __ldg(x + ci[s]);
+  for (int base = s0 + lane; base < s1; base += G * kUnroll) {
+    int c[kUnroll];
+    V v[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) {
+      const int s = base + u * G;
+      c[u] = s < s1 ? __ldg(ci + s) : -1;
+      v[u] = s < s1 ? __ldg(val + s) : V(0);
+    }
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u)
+      if (c[u] >= 0) sum += v[u] * __ldg(x + c[u]);
+  }
 #pragma unroll
   for (int off = G / 2; off > 0; off >>= 1) sum += __shfl_xor_sync(group_mask<G>(), sum, off, G);
   return (double)sum;

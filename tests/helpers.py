@@ -17,13 +17,21 @@ def row_scaled_err(rowptr, ref_vals, vals):
     return float(np.max(np.abs(ref_vals - vals) / scale)) if len(vals) else 0.0
 
 
+def sym_index(i, j, nb):
+    if i > j:
+        i, j = j, i
+    return i * nb - i * (i - 1) // 2 + (j - i)
+
+
 def emulate_schedule(sched, order, local_mats, nnz, rowptr):
     """Runs the assembly kernel's two phases on the host with given element
     matrices (local_mats[e] = [field i, test j]) -- checks the schedule only."""
     info = sched["info"]
     nb = 4 if order == 1 else 10
-    nb2 = nb * nb
-    CI, T, W = info.chunk_items, info.threads, info.warps
+    nu = nb * (nb + 1) // 2
+    pairs = [(i, j) for i in range(nb) for j in range(i, nb)]
+    assert [sym_index(i, j, nb) for i, j in pairs] == list(range(nu))
+    CI, W = info.chunk_items, info.warps
     out = np.zeros(nnz)
     blocks, items, cptr, ent = sched["blocks"], sched["items"], sched["chunk_ptr"], sched["entries"]
     rows, racc = sched["rows"], sched["row_acc"]
@@ -31,17 +39,21 @@ def emulate_schedule(sched, order, local_mats, nnz, rowptr):
         ib, ic, cb, nc, rb, rc = (int(v) for v in blocks[b, :6])
         acc = np.zeros(info.acc_max)
         for c in range(nc):
-            buf = np.zeros(CI * nb2 + 1)
+            buf = np.zeros(nu * CI + 1)
             for t in range(min(CI, ic - c * CI)):
                 e = items[ib + c * CI + t]
-                buf[np.arange(nb2) * CI + t] = local_mats[e].reshape(-1)
+                for u, (i, j) in enumerate(pairs):
+                    buf[u * CI + t] = local_mats[e][i, j]
             base = (cb + c) * (W + 1)
             for w in range(W):
                 seg = ent[cptr[base + w]:cptr[base + w + 1]].reshape(-1, 32)
-                for k in range(seg.shape[0]):
-                    words = seg[k]
-                    slot = (words >> 16).astype(np.int64) * T + 32 * w + np.arange(32)
-                    acc[slot] += buf[(words & 0xffff).astype(np.int64)]
+                for lane in range(32):
+                    s = 0.0
+                    for word in seg[:, lane]:
+                        s += buf[int(word) & 0x1fff]
+                        if int(word) >> 31:
+                            acc[(int(word) >> 13) & 0x3fff] += s
+                            s = 0.0
         for r in range(rc):
             row, a0 = rows[rb + r], racc[rb + r]
             ln = rowptr[row + 1] - rowptr[row]

@@ -11,7 +11,7 @@ import pytest
 import morganapublic_gb300 as mg
 import oracle as orc
 from morganapublic_gb300 import meshgen
-from helpers import emulate_schedule
+from helpers import emulate_schedule, row_scaled_err
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = os.path.join(ROOT, "tests", "golden")
@@ -68,9 +68,10 @@ def test_pattern_sizes_of_survey_formulas():
 
 @pytest.mark.parametrize("order,op,quad", [(1, "stiff_kappa", 4), (1, "mass", 4), (2, "stiff_kappa", 15),
                                            (2, "mass_coeff", 15)])
-def test_schedule_emulation_is_bitwise_oracle(order, op, quad):
+def test_schedule_emulation_matches_oracle(order, op, quad):
     """The exported schedule, run on the host with the oracle's element matrices,
-    reproduces the oracle's CSR values bit for bit (same summation order)."""
+    reproduces the oracle's CSR values (same terms; the per-slot association of
+    the sum differs, so to a few ulps of the row)."""
     m = meshgen.kuhn_cube(3, jitter=0.2, seed=4, permute=True)
     kappa = meshgen.lognormal(len(m.conn), 1.0, 9)
     mesh = mg.Mesh(m.xyz, m.conn, order=order)
@@ -83,7 +84,7 @@ def test_schedule_emulation_is_bitwise_oracle(order, op, quad):
     dofs, rp, ci, vals = orc.full_operator(op, order, quad, m.xyz, m.conn, coeff=kappa)
     mats = np.stack([orc.local_matrix(op, order, quad, m.xyz, m.conn[e], kappa=kappa[e]) for e in range(len(m.conn))])
     got = emulate_schedule(sched, order, mats, builder.nnz, rp)
-    assert np.array_equal(got, vals)
+    assert row_scaled_err(rp, vals, got) <= 1e-14
 
 
 def test_schedule_covers_every_row_once():
@@ -168,3 +169,6 @@ def test_export_schedule_info_fields():
     info = b.schedule_info()
     assert info.threads == 256 and info.warps == 8 and info.acc_max == 8192 and info.host_copy == 1
     assert info.n_entries >= info.n_contrib
+    s = b.export_schedule()
+    # every block's item list is padded to a multiple of 4 with -1
+    assert len(s["items"]) % 4 == 0 and (s["items"] >= -1).all()
