@@ -384,25 +384,39 @@ struct AsmArgs {
   int ent_cap;           // words of the shared-memory contribution buffer
 };
 
+constexpr size_t align16(size_t n) { return (n + 15) / 16 * 16; }
+
+// Shared-memory layout of k_assemble.  Every region starts on a 16-byte
+// boundary: the bulk copies (element nodes, ids, chunk records, contribution
+// words) require 16-byte aligned destinations, the mbarriers 8-byte.
 template <int ORDER, int MODE>
 struct AsmLayout {
   using T = typename Arith<MODE>::T;
   static constexpr int NB = ORDER == 1 ? 4 : 10;
   static constexpr int NU = ORDER == 1 ? 10 : 55;
   static constexpr int CI = ORDER == 1 ? kChunkP1 : kChunkP2;
-  static constexpr size_t acc_bytes = sizeof(T) * kAccMax;
-  static constexpr size_t buf_bytes = (sizeof(T) * (NU * CI + 1) + 15) / 16 * 16;
-  static constexpr size_t tab_bytes = (sizeof(T) * 7 * NU + 15) / 16 * 16;
-  static constexpr size_t conn_bytes = 16 * CI;  // per stage (two stages)
-  static constexpr size_t ids_bytes = 4 * CI;    // per stage (two stages)
-  static constexpr size_t desc_bytes = sizeof(ChunkDesc);  // per stage (two stages)
-  static constexpr int kRowBatch = kThreads;       // owned rows written per batch
-  static constexpr size_t rowmeta_bytes = 8 * (kRowBatch + 1);
-  static size_t total(int ent_cap)
-  {
-    return acc_bytes + buf_bytes + tab_bytes + 2 * (conn_bytes + ids_bytes + desc_bytes) + rowmeta_bytes +
-           ((size_t)ent_cap * 4 + 15) / 16 * 16 + 32;
-  }
+  static constexpr int kRowBatch = kThreads;  // owned rows written per batch
+  static constexpr size_t acc_bytes = align16(sizeof(T) * kAccMax);
+  static constexpr size_t buf_bytes = align16(sizeof(T) * (NU * CI + 1));
+  static constexpr size_t tab_bytes = align16(sizeof(T) * 7 * NU);
+  static constexpr size_t conn_bytes = align16(16 * CI);              // per stage (two stages)
+  static constexpr size_t ids_bytes = align16(4 * CI);                // per stage (two stages)
+  static constexpr size_t desc_bytes = align16(sizeof(ChunkDesc));    // per stage (two stages)
+  static constexpr size_t rowmeta_bytes = align16(4 * (2 * kRowBatch + 1));
+  // offsets
+  static constexpr size_t off_buf = acc_bytes;
+  static constexpr size_t off_tab = off_buf + buf_bytes;
+  static constexpr size_t off_conn = off_tab + tab_bytes;
+  static constexpr size_t off_ids = off_conn + 2 * conn_bytes;
+  static constexpr size_t off_desc = off_ids + 2 * ids_bytes;
+  static constexpr size_t off_rowmeta = off_desc + 2 * desc_bytes;
+  static constexpr size_t off_words = off_rowmeta + rowmeta_bytes;
+  static_assert(off_buf % 16 == 0 && off_tab % 16 == 0 && off_conn % 16 == 0 && off_ids % 16 == 0 &&
+                    off_desc % 16 == 0 && off_rowmeta % 16 == 0 && off_words % 16 == 0,
+                "shared-memory regions must start on 16-byte boundaries");
+  __host__ __device__ static size_t words_bytes(int ent_cap) { return ((size_t)ent_cap * 4 + 15) / 16 * 16; }
+  __host__ __device__ static size_t off_bars(int ent_cap) { return off_words + words_bytes(ent_cap); }
+  __host__ __device__ static size_t total(int ent_cap) { return off_bars(ent_cap) + 32; }
 };
 
 // Pipeline of one block of c = 0 .. nchunks-1 (stage = c & 1 for the element
@@ -423,25 +437,16 @@ __global__ void __launch_bounds__(kThreads, 2) k_assemble(AsmArgs a)
   constexpr int NU = L::NU, CI = L::CI;
   constexpr int TPI = ORDER == 1 ? 1 : kP2ThreadsPerItem;  // threads per item
   extern __shared__ __align__(16) unsigned char smem[];
-  unsigned char* ptr = smem;
-  T* acc = reinterpret_cast<T*>(ptr);
-  ptr += L::acc_bytes;
-  T* buf = reinterpret_cast<T*>(ptr);
-  ptr += L::buf_bytes;
-  T* tab = reinterpret_cast<T*>(ptr);
-  ptr += L::tab_bytes;
-  int4* sconn = reinterpret_cast<int4*>(ptr);  // [2][CI]
-  ptr += 2 * L::conn_bytes;
-  int32_t* sids = reinterpret_cast<int32_t*>(ptr);  // [2][CI]
-  ptr += 2 * L::ids_bytes;
-  ChunkDesc* sdesc = reinterpret_cast<ChunkDesc*>(ptr);  // [2]
-  ptr += 2 * L::desc_bytes;
-  int32_t* s_rcsr = reinterpret_cast<int32_t*>(ptr);  // [kRowBatch]
-  int32_t* s_racc = s_rcsr + L::kRowBatch;            // [kRowBatch + 1]
-  ptr += L::rowmeta_bytes;
-  uint32_t* sent = reinterpret_cast<uint32_t*>(ptr);
-  ptr += ((size_t)a.ent_cap * 4 + 15) / 16 * 16;
-  uint64_t* bar_nodes = reinterpret_cast<uint64_t*>(ptr);  // [2]
+  T* acc = reinterpret_cast<T*>(smem);
+  T* buf = reinterpret_cast<T*>(smem + L::off_buf);
+  T* tab = reinterpret_cast<T*>(smem + L::off_tab);
+  int4* sconn = reinterpret_cast<int4*>(smem + L::off_conn);        // [2][CI]
+  int32_t* sids = reinterpret_cast<int32_t*>(smem + L::off_ids);    // [2][CI]
+  ChunkDesc* sdesc = reinterpret_cast<ChunkDesc*>(smem + L::off_desc);  // [2]
+  int32_t* s_rcsr = reinterpret_cast<int32_t*>(smem + L::off_rowmeta);  // [kRowBatch]
+  int32_t* s_racc = s_rcsr + L::kRowBatch;                              // [kRowBatch + 1]
+  uint32_t* sent = reinterpret_cast<uint32_t*>(smem + L::off_words);
+  uint64_t* bar_nodes = reinterpret_cast<uint64_t*>(smem + L::off_bars(a.ent_cap));  // [2]
   uint64_t* bar_ent = bar_nodes + 2;
   __shared__ int s_block;
 
