@@ -240,6 +240,26 @@ mg_status mg_cg_refined(mg_plan* plan, const double* d_values64, const float* d_
                         int32_t max_inner, double inner_rtol, int32_t precond, mg_cg_info* info,
                         void* stream);
 
+/* FP64 preconditioned CG that allocates nothing: no cudaMalloc, cudaFree,
+   event, graph or pinned buffer.  No counterpart in the reference; it serves
+   callers that cannot allocate device memory in the solve -- a host code whose
+   device memory belongs to another allocator (a caching allocator such as
+   PyTorch's, or an arena sized at start-up), or a time-stepping loop that must
+   not take the implicit device synchronisation of cudaMalloc/cudaFree.  Same
+   arguments, iteration and stopping rule as mg_cg_solve.
+   Its work space (five vectors and the reduction scalars) is a fixed 16 MiB
+   array in the library's device memory, held by every GPU that loads the
+   library until the process exits; ndof is limited to MG_CG_NOALLOC_MAX_NDOF
+   (larger plans get MG_ERR_SIZE).  The plan must already be resident on the
+   device (any earlier GPU call on it, e.g. mg_assemble), else MG_ERR_INVALID_ARG.
+   The first call on a device looks up the array's device address; make that
+   first call before any stream capture.  All calls share the one array: calls
+   that overlap on the GPU (other streams, other host threads) race and must be
+   serialised by the caller.  Each call re-initialises what it reads. */
+#define MG_CG_NOALLOC_MAX_NDOF 400000
+mg_status mg_cg_solve_noalloc(mg_plan* plan, const double* d_values, const double* d_b, double* d_x,
+                              double rtol, int32_t maxit, int32_t precond, mg_cg_info* info, void* stream);
+
 /* ------------------------------------------------------------- adjoint -- */
 
 /* Build addition: per-element gradient of J(kappa) for the P0 coefficient of

@@ -94,6 +94,7 @@ SIGNATURES = {
     "mg_spmv": [_P, _I32, _P, _P, _P, _P],
     "mg_cg_solve": [_P, _P, _P, _P, _D, _I32, _I32, ctypes.POINTER(CgInfo), _P],
     "mg_cg_refined": [_P, _P, _P, _P, _P, _D, _I32, _I32, _D, _I32, ctypes.POINTER(CgInfo), _P],
+    "mg_cg_solve_noalloc": [_P, _P, _P, _P, _D, _I32, _I32, ctypes.POINTER(CgInfo), _P],
     "mg_adjoint_grad": [_P, _P, _P, _I32, _P, _P],
     "mg_status_string": [_I32],
     "mg_last_error": [],

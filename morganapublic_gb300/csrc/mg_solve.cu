@@ -18,7 +18,10 @@
 // several iterations can be replayed without a host round trip per iteration.
 // Dot products accumulate in FP64 in both precisions; the order of every
 // floating-point sum is fixed, so a solve is bitwise reproducible.
+#include <chrono>
 #include <cmath>
+#include <mutex>
+#include <string>
 #include <vector>
 
 #include "mg_internal.h"
@@ -482,11 +485,93 @@ static mg_status cg_start(mg_plan* p, const V* vals, const V* b, const V* x, int
   return MG_OK;
 }
 
+// ------------------------------------------------- CG without allocation --
+// Work space of mg_cg_solve_noalloc: a file-scope device array (16 MiB, 256-byte
+// aligned), enough for the CG vectors of MG_CG_NOALLOC_MAX_NDOF dofs.  Host code
+// must not use the symbol itself as a pointer: its device address is looked up
+// once per device with cudaGetSymbolAddress.
+constexpr size_t kNoAllocScratchBytes = size_t(16) << 20;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+static_assert(MG_CG_NOALLOC_MAX_NDOF > 0, "limit");
+
+constexpr int kNoAllocMaxDevices = 64;
+static std::mutex g_noalloc_mutex;
+static void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+static mg_status noalloc_scratch(void** out)
+{
+  int dev = 0;
+  MG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return set_error(MG_ERR_UNSUPPORTED, "device index above 63");
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void* ptr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_error(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+    g_noalloc_ptr[dev] = ptr;
+  }
+  *out = g_noalloc_ptr[dev];
+  return MG_OK;
+}
+
 }  // namespace mg
 
 using namespace mg;
 
 extern "C" {
+
+mg_status mg_cg_solve_noalloc(mg_plan* p, const double* d_values, const double* d_b, double* d_x, double rtol,
+                              int32_t maxit, int32_t precond, mg_cg_info* info, void* stream)
+{
+  if (!p || !d_values || !d_b || !d_x) return set_error(MG_ERR_INVALID_ARG, "mg_cg_solve_noalloc: null argument");
+  if (!(rtol > 0.0) || maxit < 0)
+    return set_error(MG_ERR_INVALID_ARG, "mg_cg_solve_noalloc: rtol must be > 0, maxit >= 0");
+  if (p->ndof > MG_CG_NOALLOC_MAX_NDOF)
+    return set_error(MG_ERR_SIZE, "mg_cg_solve_noalloc: ndof " + std::to_string(p->ndof) +
+                                      " exceeds MG_CG_NOALLOC_MAX_NDOF (" +
+                                      std::to_string(MG_CG_NOALLOC_MAX_NDOF) + ") of the fixed work array");
+  if (!p->on_device)
+    return set_error(MG_ERR_INVALID_ARG,
+                     "mg_cg_solve_noalloc: the plan is not resident on the device yet (make one regular GPU call "
+                     "on it first, e.g. mg_assemble)");
+  if (cg_work_bytes<double>(p->ndof) > kNoAllocScratchBytes)
+    return set_error(MG_ERR_SIZE, "mg_cg_solve_noalloc: work space above the fixed array");
+  void* base = nullptr;
+  MG_TRY(noalloc_scratch(&base));
+  cudaStream_t st = (cudaStream_t)stream;
+  CgWork<double> w = cg_work_carve<double>(base, p->ndof);
+  const int G = row_group(p), nb = solve_blocks(p, G);
+  const int64_t n = p->ndof;
+  const int vb = (int)std::max<int64_t>(1, std::min<int64_t>((n + kSolveThreads - 1) / kSolveThreads, kMaxSolveBlocks));
+  const auto t0 = std::chrono::steady_clock::now();
+  // cg_start writes the scalars from the host (tickets and flags start at zero)
+  MG_TRY(cg_start<double>(p, d_values, d_b, d_x, 0, precond == MG_PREC_JACOBI, rtol, maxit, w, G, nb, st));
+  CgScalars hs{};
+  for (int launched = 0;; launched += kGraphIters) {
+    for (int k = 0; k < kGraphIters; ++k) {
+      MG_DISPATCH_G(G, (k_cg_spmv<double, g><<<nb, kSolveThreads, 0, st>>>(n, p->d_rowptr, p->d_colind, d_values,
+                                                                              w.p, w.q, w.partials, w.s)));
+      k_cg_update<double><<<vb, kSolveThreads, 0, st>>>(n, d_x, w.r, w.z, w.p, w.q, w.dinv, w.partials, w.s);
+      k_cg_dir<double><<<vb, kSolveThreads, 0, st>>>(n, w.z, w.p, w.s);
+    }
+    MG_CUDA(cudaGetLastError());
+    MG_CUDA(cudaMemcpyAsync(&hs, w.s, sizeof(CgScalars), cudaMemcpyDeviceToHost, st));
+    MG_CUDA(cudaStreamSynchronize(st));
+    if (hs.done) break;
+    if (launched + kGraphIters > maxit + kGraphIters) break;
+  }
+  const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (info) {
+    info->iterations = hs.iter;
+    info->outer_iterations = 0;
+    info->converged = hs.done == 1;
+    info->rel_residual = std::sqrt(hs.rr / hs.bb);
+    info->seconds = secs;
+  }
+  if (hs.done == 2) return set_error(MG_ERR_NOT_CONVERGED, "CG breakdown: p.Ap <= 0");
+  if (hs.done != 1) return set_error(MG_ERR_NOT_CONVERGED, "CG reached maxit");
+  return MG_OK;
+}
 
 mg_status mg_spmv(mg_plan* plan, int32_t prec, const void* d_values, const void* d_x, void* d_y, void* stream)
 {
