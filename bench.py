@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-cg", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--only", default=None, choices=["asm64", "asm32", "spmv64", "spmv32"],
+    ap.add_argument("--only", default=None, choices=["asm64", "asm32", "spmv64", "spmv32", "cg64", "cg32"],
                     help="run warmup + steps launches of one kernel only (for profilers) and print its timing")
     return ap.parse_args()
 
@@ -231,6 +231,27 @@ def run_only(a):
     v32 = b.assemble("stiff_kappa", coeff=kappa, prec="f32")
     x32, y, y32 = x.float(), torch.empty_like(x), torch.empty_like(x, dtype=torch.float32)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    if a.only in ("cg64", "cg32"):
+        # a fixed number of PCG iterations on the Dirichlet system (f = 1)
+        rhs = b.build_vector(quad=4)
+        mask = torch.from_numpy(m.boundary)
+        b.apply_dirichlet(v64, mask, rhs)
+        b.apply_dirichlet(v32, mask)
+        ts = []
+        with torch.cuda.stream(stream):
+            for r in range(a.warmup + a.steps):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                if a.only == "cg64":
+                    _, info = b.cg(v64, rhs, rtol=1e-30, maxit=64, stream=stream, raise_on_fail=False)
+                else:
+                    _, info = b.cg_refined(v64, v32, rhs, rtol=1e-30, max_outer=1, max_inner=64, stream=stream,
+                                           raise_on_fail=False)
+                torch.cuda.synchronize()
+                if r >= a.warmup:
+                    ts.append((time.perf_counter() - t0) * 1e3 / max(1, info.iterations))
+        print(json.dumps({"only": a.only, "n": a.n, "ms_per_iteration": statistics.median(ts)}))
+        return 0
     fn = {"asm64": lambda: b.assemble("stiff_kappa", coeff=kappa, prec="f64", out=v64, stream=stream),
           "asm32": lambda: b.assemble("stiff_kappa", coeff=kappa, prec="f32", out=v32, stream=stream),
           "spmv64": lambda: b.apply(v64, x, out=y, stream=stream),

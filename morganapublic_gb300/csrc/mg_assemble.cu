@@ -10,9 +10,9 @@
 //            its element matrices are computed;
 //   phase 1  one thread per P1 element (eight per P2 element) computes the
 //            symmetric element matrix into shared memory, entry-major;
-//   phase 2  every thread sums its own slot-sorted segments of contribution
-//            words sequentially and adds each segment's sum to its accumulator
-//            slot -- within a chunk a slot belongs to exactly one thread.
+//   phase 2  every thread walks its own slot-sorted segments of contribution
+//            words and adds each contribution to its accumulator slot -- within
+//            a chunk a slot belongs to exactly one thread.
 // The owned rows are then written to their contiguous CSR ranges.  No atomics
 // touch values; the per-slot summation order is fixed by the plan, so the
 // results are bitwise reproducible.
@@ -70,7 +70,7 @@ template <> struct Arith<kDW> {
   __device__ static void acc_add(Acc& s, T x) { ff_acc_add(s, x); }
   __device__ static T acc_value(const Acc& s) { return ff_acc_value(s); }
   using Out = double;
-  __device__ static T from(double x) { return ff_from_double(x); }
+  __device__ static T from(double x) { return ff_from_double_bits(x); }
   __device__ static T zero() { return ff{0.0f, 0.0f}; }
   __device__ static Out out(T v) { return ff_to_double(v); }
 };
@@ -165,63 +165,64 @@ __device__ __forceinline__ void cofactors(const T J[3][3], Cof<T>& f)
 }
 
 struct GeoPtrs {
-  const double4_32a* xyz;
-  const float4* hi;
-  const float4* mid;
-  const float4* lo;
+  const double4_32a* xyz;  // (x, y, z, 0)
+  const float4* rec;       // 2 per node: (hx, hy, hz, mx), (my, mz, lx, ly)
+  const float* loz;        // lz
 };
-
-__device__ __forceinline__ float comp(const float4& v, int r) { return r == 0 ? v.x : (r == 1 ? v.y : v.z); }
-__device__ __forceinline__ double comp(const double4_32a& v, int r) { return r == 0 ? v.x : (r == 1 ? v.y : v.z); }
 
 // The global loads an element needs (vertex coordinates and coefficient), issued
 // one chunk ahead of their use so that their latency overlaps the previous
-// chunk's arithmetic and reduction.
+// chunk's arithmetic and reduction.  FP32 reads one 32-byte sector per vertex
+// (hi + mid); double-word adds lo.z.
 template <int MODE> struct Fetch;
 template <> struct Fetch<kF32> {
-  float h[4][3], m[4][3];
+  float4 a[4], b[4];
   int4 n;
   double coef;
 };
 template <> struct Fetch<kDW> {
-  float h[4][3], m[4][3], l[4][3];
+  float4 a[4], b[4];
+  float lz[4];
   double coef;
 };
 template <> struct Fetch<kF64> {
-  double x[4][3];
+  double4_32a x[4];
   double coef;
 };
-
-__device__ __forceinline__ void load3(const float4* p, int i, float* o)
-{
-  const float4 v = p[i];
-  o[0] = v.x; o[1] = v.y; o[2] = v.z;
-}
-__device__ __forceinline__ void load3(const double4_32a* p, int i, double* o)
-{
-  const double4_32a v = p[i];
-  o[0] = v.x; o[1] = v.y; o[2] = v.z;
-}
 
 __device__ __forceinline__ void fetch(const GeoPtrs& g, int4 n, Fetch<kF32>& F)
 {
   const int id[4] = {n.x, n.y, n.z, n.w};
 #pragma unroll
-  for (int s = 0; s < 4; ++s) { load3(g.hi, id[s], F.h[s]); load3(g.mid, id[s], F.m[s]); }
+  for (int s = 0; s < 4; ++s) {
+    F.a[s] = g.rec[2 * (int64_t)id[s]];
+    F.b[s] = g.rec[2 * (int64_t)id[s] + 1];
+  }
   F.n = n;
 }
 __device__ __forceinline__ void fetch(const GeoPtrs& g, int4 n, Fetch<kDW>& F)
 {
   const int id[4] = {n.x, n.y, n.z, n.w};
 #pragma unroll
-  for (int s = 0; s < 4; ++s) { load3(g.hi, id[s], F.h[s]); load3(g.mid, id[s], F.m[s]); load3(g.lo, id[s], F.l[s]); }
+  for (int s = 0; s < 4; ++s) {
+    F.a[s] = g.rec[2 * (int64_t)id[s]];
+    F.b[s] = g.rec[2 * (int64_t)id[s] + 1];
+    F.lz[s] = g.loz[id[s]];
+  }
 }
 __device__ __forceinline__ void fetch(const GeoPtrs& g, int4 n, Fetch<kF64>& F)
 {
   const int id[4] = {n.x, n.y, n.z, n.w};
 #pragma unroll
-  for (int s = 0; s < 4; ++s) load3(g.xyz, id[s], F.x[s]);
+  for (int s = 0; s < 4; ++s) F.x[s] = g.xyz[id[s]];
 }
+
+// components of a vertex record: hi, mid, lo
+__device__ __forceinline__ float rec_hi(const float4& a, int r) { return r == 0 ? a.x : (r == 1 ? a.y : a.z); }
+__device__ __forceinline__ float rec_mid(const float4& a, const float4& b, int r) { return r == 0 ? a.w : (r == 1 ? b.x : b.y); }
+__device__ __forceinline__ float rec_lo(const float4& b, float lz, int r) { return r == 0 ? b.z : (r == 1 ? b.w : lz); }
+
+__device__ __forceinline__ double comp(const double4_32a& v, int r) { return r == 0 ? v.x : (r == 1 ? v.y : v.z); }
 
 __device__ __forceinline__ void geometry(const GeoPtrs&, const Fetch<kF64>& F, Cof<double>& f)
 {
@@ -229,7 +230,7 @@ __device__ __forceinline__ void geometry(const GeoPtrs&, const Fetch<kF64>& F, C
 #pragma unroll
   for (int r = 0; r < 3; ++r)
 #pragma unroll
-    for (int k = 0; k < 3; ++k) J[r][k] = F.x[k + 1][r] - F.x[0][r];
+    for (int k = 0; k < 3; ++k) J[r][k] = comp(F.x[k + 1], r) - comp(F.x[0], r);
   cofactors<double>(J, f);
 }
 
@@ -242,7 +243,9 @@ __device__ __forceinline__ void geometry(const GeoPtrs& g, const Fetch<kF32>& F,
 #pragma unroll
   for (int r = 0; r < 3; ++r)
 #pragma unroll
-    for (int k = 0; k < 3; ++k) J[r][k] = (F.h[k + 1][r] - F.h[0][r]) + (F.m[k + 1][r] - F.m[0][r]);
+    for (int k = 0; k < 3; ++k)
+      J[r][k] = (rec_hi(F.a[k + 1], r) - rec_hi(F.a[0], r)) +
+                (rec_mid(F.a[k + 1], F.b[k + 1], r) - rec_mid(F.a[0], F.b[0], r));
   cofactors<float>(J, f);
   float nn[3];
 #pragma unroll
@@ -278,7 +281,8 @@ __device__ __forceinline__ void geometry(const GeoPtrs&, const Fetch<kDW>& F, Co
   for (int r = 0; r < 3; ++r)
 #pragma unroll
     for (int k = 0; k < 3; ++k)
-      J[r][k] = dw_diff(F.h[k + 1][r], F.h[0][r], F.m[k + 1][r], F.m[0][r], F.l[k + 1][r], F.l[0][r]);
+      J[r][k] = dw_diff(rec_hi(F.a[k + 1], r), rec_hi(F.a[0], r), rec_mid(F.a[k + 1], F.b[k + 1], r),
+                        rec_mid(F.a[0], F.b[0], r), rec_lo(F.b[k + 1], F.lz[k + 1], r), rec_lo(F.b[0], F.lz[0], r));
   f.c[0][0] = ff_cross(J[1][1], J[2][2], J[1][2], J[2][1]);
   f.c[0][1] = ff_cross(J[1][2], J[2][0], J[1][0], J[2][2]);
   f.c[0][2] = ff_cross(J[1][0], J[2][1], J[1][1], J[2][0]);
@@ -396,7 +400,7 @@ struct AsmLayout {
   static constexpr int NU = ORDER == 1 ? 10 : 55;
   static constexpr int CI = ORDER == 1 ? kChunkP1 : kChunkP2;
   static constexpr int kRowBatch = kThreads;  // owned rows written per batch
-  static constexpr size_t acc_bytes = align16(sizeof(T) * kAccMax);
+  static constexpr size_t acc_bytes = align16(sizeof(T) * (kAccMax + 1));  // + the padding words' dummy slot
   static constexpr size_t buf_bytes = align16(sizeof(T) * (NU * CI + 1));
   static constexpr size_t tab_bytes = align16(sizeof(T) * 7 * NU);
   static constexpr size_t conn_bytes = align16(16 * CI);              // per stage (two stages)
@@ -414,22 +418,29 @@ struct AsmLayout {
   static_assert(off_buf % 16 == 0 && off_tab % 16 == 0 && off_conn % 16 == 0 && off_ids % 16 == 0 &&
                     off_desc % 16 == 0 && off_rowmeta % 16 == 0 && off_words % 16 == 0,
                 "shared-memory regions must start on 16-byte boundaries");
+  // two word buffers (chunk c uses buffer c & 1)
   __host__ __device__ static size_t words_bytes(int ent_cap) { return ((size_t)ent_cap * 4 + 15) / 16 * 16; }
-  __host__ __device__ static size_t off_bars(int ent_cap) { return off_words + words_bytes(ent_cap); }
+  __host__ __device__ static size_t off_bars(int ent_cap) { return off_words + 2 * words_bytes(ent_cap); }
   __host__ __device__ static size_t total(int ent_cap) { return off_bars(ent_cap) + 32; }
 };
 
-// Pipeline of one block of c = 0 .. nchunks-1 (stage = c & 1 for the element
-// nodes and ids, one buffer for the contribution words):
-//   before chunk c      nodes(c) and nodes(c+1) staged; coordinates of chunk c
-//                       already in registers (R)
-//   start of chunk c    wait nodes(c+1), load its coordinates into P
+// Pipeline of one block of c = 0 .. nchunks-1 (stage c & 1 for the element
+// nodes, ids, chunk record and contribution words):
+//   before chunk c      nodes(c+1), nodes(c+2) and words(c) staged or in
+//                       flight; chunk c's coordinates in registers (R) and its
+//                       per-warp word range in registers
+//   start of chunk c    wait nodes(c+1); bulk copy words(c+1) into the buffer
+//                       chunk c-1 released; read chunk c+1's word range; load
+//                       chunk c+1's coordinates into P
 //   phase 1 (c)         element matrices from R
-//   barrier             stage c & 1 is free: bulk copy nodes(c+2) into it
-//   phase 2 (c)         wait words(c) (copied during phase 1), segmented sums
-//   barrier             bulk copy words(c+1); R = P
+//   barrier             stage (c+1) & 1 has been read: copy nodes(c+3) into it
+//   phase 2 (c)         wait words(c), add the contributions
+//   barrier             R = P
+// so every copy has more than one chunk of work to land.
+// The double-word variants need 8-byte accumulators and element entries, so
+// shared memory admits one CTA per SM; they get the full register file.
 template <int ORDER, int MODE>
-__global__ void __launch_bounds__(kThreads, 2) k_assemble(AsmArgs a)
+__global__ void __launch_bounds__(kThreads, MODE == kDW ? 1 : 2) k_assemble(AsmArgs a)
 {
   using A = Arith<MODE>;
   using T = typename A::T;
@@ -445,9 +456,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_assemble(AsmArgs a)
   ChunkDesc* sdesc = reinterpret_cast<ChunkDesc*>(smem + L::off_desc);  // [2]
   int32_t* s_rcsr = reinterpret_cast<int32_t*>(smem + L::off_rowmeta);  // [kRowBatch]
   int32_t* s_racc = s_rcsr + L::kRowBatch;                              // [kRowBatch + 1]
-  uint32_t* sent = reinterpret_cast<uint32_t*>(smem + L::off_words);
+  uint32_t* sent = reinterpret_cast<uint32_t*>(smem + L::off_words);  // [2][words_bytes / 4]
+  const int went = (int)(L::words_bytes(a.ent_cap) / 4);
   uint64_t* bar_nodes = reinterpret_cast<uint64_t*>(smem + L::off_bars(a.ent_cap));  // [2]
-  uint64_t* bar_ent = bar_nodes + 2;
+  uint64_t* bar_ent = bar_nodes + 2;                                                  // [2]
   __shared__ int s_block;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -457,15 +469,16 @@ __global__ void __launch_bounds__(kThreads, 2) k_assemble(AsmArgs a)
     buf[NU * CI] = A::zero();
     mbar_init(&bar_nodes[0], 1);
     mbar_init(&bar_nodes[1], 1);
-    mbar_init(bar_ent, 1);
+    mbar_init(&bar_ent[0], 1);
+    mbar_init(&bar_ent[1], 1);
     mbar_fence_init();
   }
   __syncthreads();
   const T wsum = A::from(a.wsum);
-  // bit st of ph_nodes: parity of the next completion of stage st's barrier;
-  // bit st of pend_nodes: a copy into stage st is in flight
-  uint32_t ph_nodes = 0, ph_ent = 0, pend_nodes = 0;
-  bool pend_ent = false, failed = false;
+  // bit st of ph_nodes / ph_ent: parity of the next completion of stage st's
+  // barrier; bit st of pend_nodes / pend_ent: a copy into stage st is in flight
+  uint32_t ph_nodes = 0, ph_ent = 0, pend_nodes = 0, pend_ent = 0;
+  bool failed = false;
 
   for (;;) {
     if (tid == 0) s_block = (int)atomicAdd(&a.counters[0], 1u);
@@ -486,10 +499,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_assemble(AsmArgs a)
     };
     // needs the staged descriptor of chunk c (stage c & 1)
     auto issue_entries = [&](int c) {
-      const ChunkDesc& cd = sdesc[c & 1];
+      const int st = c & 1;
+      const ChunkDesc& cd = sdesc[st];
       const uint32_t bytes = (uint32_t)cd.warp_off[kWarps] * 4u;
-      mbar_expect_tx(bar_ent, bytes);
-      if (bytes) bulk_g2s(sent, a.entries + cd.word_begin, bytes, bar_ent);
+      mbar_expect_tx(&bar_ent[st], bytes);
+      if (bytes) bulk_g2s(sent + st * went, a.entries + cd.word_begin, bytes, &bar_ent[st]);
     };
     // waits on a stage barrier; false (uniformly) when the wait gave up
     auto wait_nodes = [&](int c) -> bool {
@@ -521,17 +535,36 @@ __global__ void __launch_bounds__(kThreads, 2) k_assemble(AsmArgs a)
 
     Fetch<MODE> R, P;
     bool have_r = false, have_p = false;
+    int w_beg = 0, w_end = 0, nw_beg = 0, nw_end = 0;  // this warp's word range of chunks c and c + 1
     if (d.nchunks > 0) {
       if (!wait_nodes(0)) { failed = true; break; }
       if (tid == 0) issue_entries(0);
-      pend_ent = true;
+      pend_ent |= 1u;
+      nw_beg = sdesc[0].warp_off[warp];
+      nw_end = sdesc[0].warp_off[warp + 1];
       have_r = prefetch(0, R);
+      __syncthreads();  // stage 0 has been read: refill it with chunk 2
+      if (d.nchunks > 2) {
+        if (tid == 0) {
+          fence_proxy_async();
+          issue_nodes(2);
+        }
+        pend_nodes |= 1u;
+      }
     }
     for (int c = 0; c < d.nchunks; ++c) {
-      // this warp's slice of chunk c's words, read before stage c & 1 is reused
-      const int w_beg = sdesc[c & 1].warp_off[warp], w_end = sdesc[c & 1].warp_off[warp + 1];
+      w_beg = nw_beg;
+      w_end = nw_end;
       if (c + 1 < d.nchunks) {
         if (!wait_nodes(c + 1)) { failed = true; break; }
+        // word buffer (c + 1) & 1 was released by the barrier that ended chunk c - 1
+        if (tid == 0) {
+          fence_proxy_async();
+          issue_entries(c + 1);
+        }
+        pend_ent |= 1u << ((c + 1) & 1);
+        nw_beg = sdesc[(c + 1) & 1].warp_off[warp];
+        nw_end = sdesc[(c + 1) & 1].warp_off[warp + 1];
         have_p = prefetch(c + 1, P);
       }
       // ---- phase 1: element matrices of chunk c
@@ -565,38 +598,44 @@ __global__ void __launch_bounds__(kThreads, 2) k_assemble(AsmArgs a)
         }
       }
       __syncthreads();
-      if (tid == 0 && c + 2 < d.nchunks) {
+      // stage (c + 1) & 1 was read at the top of this chunk: refill it with chunk c + 3
+      if (tid == 0 && c + 3 < d.nchunks) {
         fence_proxy_async();
-        issue_nodes(c + 2);
+        issue_nodes(c + 3);
       }
-      if (c + 2 < d.nchunks) pend_nodes |= 1u << (c & 1);
+      if (c + 3 < d.nchunks) pend_nodes |= 1u << ((c + 1) & 1);
       // ---- phase 2: segmented sums into owned slots
       {
-        const bool ok = mbar_wait(bar_ent, ph_ent);
+        const int st = c & 1;
+        const bool ok = mbar_wait(&bar_ent[st], (ph_ent >> st) & 1u);
         if (__syncthreads_or(!ok)) { failed = true; break; }
-        ph_ent ^= 1;
-        pend_ent = false;
+        ph_ent ^= 1u << st;
+        pend_ent &= ~(1u << st);
       }
       {
-        const uint32_t* ew = sent + w_beg + lane;
-        const int K = (w_end - w_beg) >> 5;
-        typename A::Acc sum{};
+        // pieces of PW words of one slot: summed in registers, one update of
+        // the slot per piece; within a chunk every slot belongs to one thread
+        constexpr int PW = piece_words(ORDER);
+        const int K = (w_end - w_beg) / (32 * PW);
+        const uint32_t* ew = sent + (c & 1) * went + w_beg + lane * PW;
+#pragma unroll 2
         for (int k = 0; k < K; ++k) {
-          const uint32_t w = ew[k * 32];
-          A::acc_add(sum, buf[w & kSrcMask]);
-          if (w & kEndFlag) {
-            const uint32_t slot = (w >> kSrcBits) & kSlotMask;
-            acc[slot] = acc[slot] + A::acc_value(sum);
-            sum = typename A::Acc{};
+          uint32_t w[PW];
+          if constexpr (PW == 4) {
+            const uint4 q = *reinterpret_cast<const uint4*>(ew + k * 32 * PW);
+            w[0] = q.x; w[1] = q.y; w[2] = q.z; w[3] = q.w;
+          } else {
+            const uint2 q = *reinterpret_cast<const uint2*>(ew + k * 32 * PW);
+            w[0] = q.x; w[1] = q.y;
           }
+          const uint32_t slot = (w[0] >> kSrcBits) & kSlotMask;
+          T v = buf[w[0] & kSrcMask];
+#pragma unroll
+          for (int q = 1; q < PW; ++q) v = v + buf[w[q] & kSrcMask];
+          acc[slot] = acc[slot] + v;
         }
       }
       __syncthreads();
-      if (tid == 0 && c + 1 < d.nchunks) {
-        fence_proxy_async();
-        issue_entries(c + 1);
-      }
-      pend_ent = c + 1 < d.nchunks;
       R = P;
       have_r = have_p;
       have_p = false;
@@ -626,7 +665,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_assemble(AsmArgs a)
     // let copies still in flight land before the CTA's shared memory goes away
     for (int st = 0; st < 2; ++st)
       if ((pend_nodes >> st) & 1u) mbar_wait(&bar_nodes[st], (ph_nodes >> st) & 1u);
-    if (pend_ent) mbar_wait(bar_ent, ph_ent);
+    for (int st = 0; st < 2; ++st)
+      if ((pend_ent >> st) & 1u) mbar_wait(&bar_ent[st], (ph_ent >> st) & 1u);
     if (tid == 0) {
       atomicExch(&a.counters[2], (uint32_t)kDevErrTimeout);
       atomicExch(&a.counters[3], (uint32_t)blockIdx.x);
@@ -698,7 +738,7 @@ mg_status launch_assemble(mg_plan* p, int op, const double* d_coeff, double c, i
   a.entries = p->d_entries;
   a.row_csr = p->d_row_csr;
   a.row_acc = p->d_row_acc;
-  a.geo = GeoPtrs{m->d_xyz, m->d_xyz_hi, m->d_xyz_mid, m->d_xyz_lo};
+  a.geo = GeoPtrs{m->d_xyz, m->d_node_rec, m->d_lo_z};
   a.coeff = needs_coeff ? d_coeff : nullptr;
   a.cconst = op == MG_OP_STIFF_CONST ? c : 1.0;
   a.tables = d_tab;
@@ -879,7 +919,7 @@ mg_status mg_adjoint_grad(mg_plan* p, const double* d_u, const double* d_lambda,
   const int threads = 256;
   const int blocks = (int)((m->n_elem + threads - 1) / threads);
   cudaStream_t st = (cudaStream_t)stream;
-  const GeoPtrs geo{m->d_xyz, m->d_xyz_hi, m->d_xyz_mid, m->d_xyz_lo};
+  const GeoPtrs geo{m->d_xyz, m->d_node_rec, m->d_lo_z};
   if (blocks > 0) {
     if (m->order == 1)
       k_adjoint<1><<<blocks, threads, 0, st>>>(m->n_elem, m->d_conn, m->d_dofs, geo, d_tab, t->wsum, d_u, d_lambda,

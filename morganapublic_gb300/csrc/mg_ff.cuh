@@ -129,13 +129,15 @@ __device__ __forceinline__ ff ff_mul(ff a, ff b)
 // a * b + c * d with one renormalisation (the cofactor pattern)
 __device__ __forceinline__ ff ff_mul_add(ff a, ff b, ff c, ff d) { return ff_add(ff_mul(a, b), ff_mul(c, d)); }
 
-// Division: q1 = a.hi / b.hi, remainder r = a - q1 b in double-word, one
-// correction q2 = r.hi / b.hi (Newton step); relative error ~2^-46.
+// Division: q1 = a.hi * rcp(b.hi), remainder r = a - q1 b in double-word, one
+// correction q2 = r.hi * rcp(b.hi) (a Newton step on the quotient); relative
+// error ~2^-45 with the correctly rounded reciprocal.
 __device__ __forceinline__ ff ff_div(ff a, ff b)
 {
-  const float q1 = __fdiv_rn(a.hi, b.hi);
+  const float rb = __frcp_rn(b.hi);
+  const float q1 = __fmul_rn(a.hi, rb);
   const ff r = ff_sub(a, ff_mul(b, ff_make(q1)));
-  const float q2 = __fdiv_rn(r.hi, b.hi);
+  const float q2 = __fmul_rn(r.hi, rb);
   return fast_two_sum(q1, q2);
 }
 
@@ -150,5 +152,42 @@ __device__ __forceinline__ ff ff_from_double(double x)
 }
 
 __device__ __forceinline__ double ff_to_double(ff a) { return (double)a.hi + (double)a.lo; }
+
+// The same two conversions with integer operations, for hot loops: GB300 runs
+// FP32<->FP64 conversions on its FP64 pipe (~1/60 of the FP32 rate).
+// float -> double by re-biasing the exponent (exact for normal floats; zero
+// and subnormals map to zero, Inf/NaN fall back to the conversion).
+__device__ __forceinline__ double f2d_bits(float f)
+{
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t e = (u >> 23) & 0xffu;
+  if (e == 0u) return 0.0;
+  if (e == 0xffu) return (double)f;
+  const uint64_t d = ((uint64_t)(u >> 31) << 63) | ((uint64_t)(e + (1023u - 127u)) << 52) |
+                     ((uint64_t)(u & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)d);
+}
+
+// hi + lo as a double: both parts exact, one FP64 addition.
+__device__ __forceinline__ double ff_to_double_bits(ff a) { return f2d_bits(a.hi) + f2d_bits(a.lo); }
+
+// double -> hi + lo: hi keeps the top 24 bits of the significand (truncated,
+// exact), lo the next 24 bits rounded -- |x - hi - lo| <= 2^-48 |x|.  For
+// |x| in the normal float range (about 1e-38 .. 3e38) and x = 0; other values
+// fall back to the FP64 conversions.
+__device__ __forceinline__ ff ff_from_double_bits(double x)
+{
+  const uint64_t u = (uint64_t)__double_as_longlong(x);
+  const int e = (int)((u >> 52) & 0x7ff) - 1023;  // unbiased exponent
+  if (e < -120 || e > 120) return ff_from_double(x);
+  const uint32_t sign = (uint32_t)(u >> 63) << 31;
+  const uint64_t m = u & ((1ull << 52) - 1);
+  const float hi = __uint_as_float(sign | ((uint32_t)(e + 127) << 23) | (uint32_t)(m >> 29));
+  // remaining 29 bits, value m_lo * 2^(e - 52)
+  const uint32_t m_lo = (uint32_t)(m & ((1u << 29) - 1));
+  float lo = __uint2float_rn(m_lo) * __uint_as_float((uint32_t)(e - 52 + 127) << 23);
+  lo = sign ? -lo : lo;
+  return ff{hi, lo};
+}
 
 }  // namespace mg

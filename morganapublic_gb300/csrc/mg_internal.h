@@ -40,10 +40,15 @@ constexpr int kChunkP2 = 32;
 constexpr int kP2ThreadsPerItem = kThreads / kChunkP2;
 // Contribution-list word: source (13 bits) | accumulator slot (14 bits) << 13 |
 // end-of-segment flag << 31.  The source indexes the chunk's element matrices,
-// stored symmetric (nb (nb + 1) / 2 unique entries) and entry-major.
+// stored symmetric (nb (nb + 1) / 2 unique entries) and entry-major.  Padding
+// words carry the zero source; padding pieces the dummy slot kAccMax.
 constexpr uint32_t kSrcBits = 13, kSlotBits = 14;
 constexpr uint32_t kSrcMask = (1u << kSrcBits) - 1, kSlotMask = (1u << kSlotBits) - 1;
 constexpr uint32_t kEndFlag = 1u << 31;
+// Contributions are applied in pieces of piece_words(order) words: all words of a
+// piece belong to one accumulator slot (carried by the piece's first word); the
+// kernel sums a piece in registers and updates the slot once.
+inline __host__ __device__ constexpr int piece_words(int order) { return order == 1 ? 4 : 2; }
 
 inline int nbasis(int order) { return order == 1 ? 4 : 10; }
 inline int nunique(int order) { return order == 1 ? 10 : 55; }
@@ -65,7 +70,7 @@ struct BlockDesc {
   int32_t row_begin;    // into rows[] / row_acc[]
   int32_t row_count;
   int32_t acc_used;     // accumulator slots in use
-  int32_t pad;
+  int32_t word_begin32; // first contribution word of the block / 32
 };
 
 // Contribution words of one chunk: a 64-byte record the kernel stages into
@@ -109,9 +114,10 @@ struct mg_mesh {
   std::vector<int32_t> dofs;        // n_elem * nb
   // device copies
   double4_32a* d_xyz = nullptr;      // (x, y, z, 0)
-  float4* d_xyz_hi = nullptr;    // x = hi + mid + lo exactly (three floats)
-  float4* d_xyz_mid = nullptr;
-  float4* d_xyz_lo = nullptr;
+  // x = hi + mid + lo exactly (three floats per coordinate), packed so that
+  // one 32-byte sector holds a node's (hi.xyz, mid.xyz, lo.x, lo.y); lo.z apart
+  float4* d_node_rec = nullptr;  // 2 float4 per node
+  float* d_lo_z = nullptr;
   int4* d_conn = nullptr;        // vertex node ids
   int32_t* d_dofs = nullptr;     // n_elem * nb
   bool on_device = false;

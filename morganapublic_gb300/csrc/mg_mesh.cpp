@@ -262,7 +262,8 @@ mg_status mesh_device(mg_mesh* m)
   MG_CUDA(cudaGetDevice(&m->device));
   const int64_t N = m->n_nodes, E = m->n_elem;
   std::vector<double4_32a> x64(N);
-  std::vector<float4> hi(N), mid(N), lo(N);
+  std::vector<float4> rec(2 * N);
+  std::vector<float> loz(N);
   for (int64_t i = 0; i < N; ++i) {
     double c[3] = {m->xyz[3 * i], m->xyz[3 * i + 1], m->xyz[3 * i + 2]};
     float h[3], md[3], l[3];
@@ -273,20 +274,18 @@ mg_status mesh_device(mg_mesh* m)
       l[k] = (float)(r1 - (double)md[k]);
     }
     x64[i] = make_double4_32a(c[0], c[1], c[2], 0.0);
-    hi[i] = make_float4(h[0], h[1], h[2], 0.f);
-    mid[i] = make_float4(md[0], md[1], md[2], 0.f);
-    lo[i] = make_float4(l[0], l[1], l[2], 0.f);
+    rec[2 * i] = make_float4(h[0], h[1], h[2], md[0]);
+    rec[2 * i + 1] = make_float4(md[1], md[2], l[0], l[1]);
+    loz[i] = l[2];
   }
   MG_CUDA(cudaMalloc(&m->d_xyz, sizeof(double4_32a) * std::max<int64_t>(N, 1)));
-  MG_CUDA(cudaMalloc(&m->d_xyz_hi, sizeof(float4) * std::max<int64_t>(N, 1)));
-  MG_CUDA(cudaMalloc(&m->d_xyz_mid, sizeof(float4) * std::max<int64_t>(N, 1)));
-  MG_CUDA(cudaMalloc(&m->d_xyz_lo, sizeof(float4) * std::max<int64_t>(N, 1)));
+  MG_CUDA(cudaMalloc(&m->d_node_rec, 2 * sizeof(float4) * std::max<int64_t>(N, 1)));
+  MG_CUDA(cudaMalloc(&m->d_lo_z, sizeof(float) * std::max<int64_t>(N, 1)));
   MG_CUDA(cudaMalloc(&m->d_conn, sizeof(int4) * std::max<int64_t>(E, 1)));
   MG_CUDA(cudaMalloc(&m->d_dofs, sizeof(int32_t) * std::max<int64_t>(E * m->nb, 1)));
   MG_CUDA(cudaMemcpy(m->d_xyz, x64.data(), sizeof(double4_32a) * N, cudaMemcpyHostToDevice));
-  MG_CUDA(cudaMemcpy(m->d_xyz_hi, hi.data(), sizeof(float4) * N, cudaMemcpyHostToDevice));
-  MG_CUDA(cudaMemcpy(m->d_xyz_mid, mid.data(), sizeof(float4) * N, cudaMemcpyHostToDevice));
-  MG_CUDA(cudaMemcpy(m->d_xyz_lo, lo.data(), sizeof(float4) * N, cudaMemcpyHostToDevice));
+  MG_CUDA(cudaMemcpy(m->d_node_rec, rec.data(), 2 * sizeof(float4) * N, cudaMemcpyHostToDevice));
+  MG_CUDA(cudaMemcpy(m->d_lo_z, loz.data(), sizeof(float) * N, cudaMemcpyHostToDevice));
   MG_CUDA(cudaMemcpy(m->d_conn, m->conn.data(), sizeof(int4) * E, cudaMemcpyHostToDevice));
   MG_CUDA(cudaMemcpy(m->d_dofs, m->dofs.data(), sizeof(int32_t) * E * m->nb, cudaMemcpyHostToDevice));
   m->on_device = true;
@@ -297,9 +296,8 @@ static void free_mesh(mg_mesh* m)
 {
   if (!m) return;
   cudaFree(m->d_xyz);
-  cudaFree(m->d_xyz_hi);
-  cudaFree(m->d_xyz_mid);
-  cudaFree(m->d_xyz_lo);
+  cudaFree(m->d_node_rec);
+  cudaFree(m->d_lo_z);
   cudaFree(m->d_conn);
   cudaFree(m->d_dofs);
   delete m;

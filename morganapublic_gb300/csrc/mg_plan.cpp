@@ -7,8 +7,9 @@
 //
 // Schedule: the rows (dofs) are cut into blocks along a Morton curve of the dof
 // positions, each holding at most kAccMax CSR entries.  One CTA owns one block:
-// it recomputes every element touching one of its rows ("items", sorted by
-// element id) and sums each owned CSR entry in shared memory.  The items are
+// it recomputes every element touching one of its rows ("items", ordered along
+// a Morton curve of the element centroids) and sums each owned CSR entry in
+// shared memory.  The items are
 // processed in chunks; the contributions of a chunk are sorted by accumulator
 // slot into segments (one per slot, in element order), and the segments are
 // dealt to the CTA's threads longest-first to the least-loaded thread.  A
@@ -190,8 +191,30 @@ static mg_status build_schedule(mg_plan* p, HostSchedule* hs)
       for (int u = 0; u < n; ++u) hs->items[f[bs[u]]++] = (int32_t)e;
     }
   }
-  // pad every block's item list to a multiple of 4 (16-byte aligned bulk copies)
+  // order each block's items along the Morton curve of the element centroids, so
+  // that a chunk covers a compact patch (its contributions to a CSR entry fall in
+  // one segment, its vertices are neighbours in L2); ties by element id.  Then
+  // pad every block's list to a multiple of 4 (16-byte aligned bulk copies).
   {
+    std::vector<uint64_t> ekey(E);
+#pragma omp parallel for
+    for (int64_t e = 0; e < E; ++e) {
+      double x[3] = {0, 0, 0};
+      for (int v = 0; v < 4; ++v)
+        for (int k = 0; k < 3; ++k) x[k] += 0.25 * m->xyz[3 * (int64_t)m->conn[4 * e + v] + k];
+      uint64_t c = 0;
+      for (int k = 0; k < 3; ++k) {
+        double t = hi[k] > lo[k] ? (x[k] - lo[k]) / (hi[k] - lo[k]) : 0.0;
+        uint64_t q = (uint64_t)std::min(2097151.0, std::max(0.0, t * 2097151.0));
+        c |= spread21(q) << k;
+      }
+      ekey[e] = c;
+    }
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int32_t b = 0; b < nbk; ++b)
+      std::sort(hs->items.begin() + bcount[b], hs->items.begin() + bcount[b + 1], [&](int32_t x, int32_t y) {
+        return ekey[x] != ekey[y] ? ekey[x] < ekey[y] : x < y;
+      });
     std::vector<int32_t> padded;
     padded.reserve(hs->items.size() + 4 * (size_t)nbk);
     for (int32_t b = 0; b < nbk; ++b) {
@@ -215,7 +238,9 @@ static mg_status build_schedule(mg_plan* p, HostSchedule* hs)
   const int nu = nunique(m->order);
   const uint32_t zero_src = (uint32_t)(nu * CI);
   if (zero_src > kSrcMask) return set_error(MG_ERR_SIZE, "chunk buffer above the 13-bit source index");
-  if (kAccMax > (int)kSlotMask + 1) return set_error(MG_ERR_SIZE, "accumulator above the 14-bit slot index");
+  if (kAccMax + 1 > (int)kSlotMask + 1) return set_error(MG_ERR_SIZE, "accumulator above the 14-bit slot index");
+  const uint32_t pad_word = zero_src | ((uint32_t)kAccMax << kSrcBits);
+  const int PW = piece_words(m->order);
   std::vector<std::vector<uint32_t>> ent(nbk);
   std::vector<std::vector<int64_t>> cptr(nbk);
   std::vector<int64_t> contrib(nbk, 0), maxc(nbk, 0);
@@ -223,6 +248,7 @@ static mg_status build_schedule(mg_plan* p, HostSchedule* hs)
   {
     struct Seg { int32_t slot, begin, len; };
     std::vector<std::vector<uint32_t>> per(kThreads);
+    std::vector<std::vector<int32_t>> tseg(kThreads);
     std::vector<std::pair<int32_t, uint32_t>> list;  // (slot, src) in item order
     std::vector<Seg> segs;
     std::vector<uint32_t> srcs;
@@ -264,32 +290,49 @@ static mg_status build_schedule(mg_plan* p, HostSchedule* hs)
         }
         // longest segment first, to the least-loaded thread (ties: lowest thread)
         std::stable_sort(segs.begin(), segs.end(), [](const Seg& x, const Seg& y) { return x.len > y.len; });
-        for (auto& v : per) v.clear();
+        for (auto& v : tseg) v.clear();
         // min-heap of (load, thread): pops the least-loaded, lowest-numbered thread
         heap.clear();
         for (int t = 0; t < kThreads; ++t) heap.push_back(((int64_t)0 << 32) | t);
         std::make_heap(heap.begin(), heap.end(), std::greater<int64_t>());
-        for (const Seg& sg : segs) {
+        for (size_t q = 0; q < segs.size(); ++q) {
+          const Seg& sg = segs[q];
           std::pop_heap(heap.begin(), heap.end(), std::greater<int64_t>());
           const int64_t top = heap.back();
           const int best = (int)(top & 0xffffffff);
-          heap.back() = (((top >> 32) + sg.len) << 32) | best;
+          heap.back() = (((top >> 32) + (sg.len + PW - 1) / PW) << 32) | best;
           std::push_heap(heap.begin(), heap.end(), std::greater<int64_t>());
-          for (int k = 0; k < sg.len; ++k) {
-            uint32_t w = srcs[sg.begin + k] | ((uint32_t)sg.slot << kSrcBits);
-            if (k == sg.len - 1) w |= kEndFlag;
-            per[best].push_back(w);
+          tseg[best].push_back((int32_t)q);
+        }
+        // each thread's segments cut into pieces of PW words (the last piece of
+        // a segment padded with zero-source words); pieces keep element order
+        for (int t = 0; t < kThreads; ++t) {
+          auto& v = per[t];
+          v.clear();
+          for (int32_t q : tseg[t]) {
+            const Seg& sg = segs[q];
+            for (int k0 = 0; k0 < sg.len; k0 += PW)
+              for (int k = k0; k < k0 + PW; ++k) {
+                const uint32_t slot_bits = (uint32_t)sg.slot << kSrcBits;
+                uint32_t w = k < sg.len ? (srcs[sg.begin + k] | slot_bits) : (zero_src | slot_bits);
+                if (k == sg.len - 1) w |= kEndFlag;
+                v.push_back(w);
+              }
           }
         }
         const int64_t base = (int64_t)ent[b].size();
         for (int w = 0; w < kWarps; ++w) {
           cptr[b].push_back((int64_t)ent[b].size());
-          size_t K = 0;
-          for (int l = 0; l < 32; ++l) K = std::max(K, per[32 * w + l].size());
+          size_t K = 0;  // pieces
+          for (int l = 0; l < 32; ++l) K = std::max(K, per[32 * w + l].size() / PW);
+          // layout [piece][lane][PW]: one PW*4-byte load per lane and piece
           for (size_t k = 0; k < K; ++k)
             for (int l = 0; l < 32; ++l) {
               const auto& v = per[32 * w + l];
-              ent[b].push_back(k < v.size() ? v[k] : zero_src);
+              for (int q = 0; q < PW; ++q) {
+                const size_t i = k * PW + q;
+                ent[b].push_back(i < v.size() ? v[i] : pad_word);
+              }
             }
         }
         cptr[b].push_back((int64_t)ent[b].size());
@@ -306,6 +349,8 @@ static mg_status build_schedule(mg_plan* p, HostSchedule* hs)
     std::copy(ent[b].begin(), ent[b].end(), hs->entries.begin() + off);
     for (size_t k = 0; k < cptr[b].size(); ++k) hs->chunk_ptr[ck * (kWarps + 1) + k] = cptr[b][k] + off;
     ck += hs->blocks[b].nchunks;
+    if (off % 32 != 0 || off / 32 >= INT32_MAX) return set_error(MG_ERR_SIZE, "contribution words above 2^36");
+    hs->blocks[b].word_begin32 = (int32_t)(off / 32);
     off += (int64_t)ent[b].size();
     hs->n_contrib += contrib[b];
     hs->max_chunk_entries = std::max(hs->max_chunk_entries, maxc[b]);

@@ -18,18 +18,20 @@
 // several iterations can be replayed without a host round trip per iteration.
 // Dot products accumulate in FP64 in both precisions; the order of every
 // floating-point sum is fixed, so a solve is bitwise reproducible.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <mutex>
 #include <string>
 #include <vector>
 
+#include "mg_ff.cuh"
 #include "mg_internal.h"
 
 namespace mg {
 
 constexpr int kSolveThreads = 256;
-constexpr int kMaxSolveBlocks = 1216;  // 8 CTAs of 256 threads on each of 152 SMs
+constexpr int kMaxSolveBlocks = 2048;  // bound of the per-CTA partial arrays
 
 struct CgScalars {
   double rz, alpha, beta, rr, bb, tol2, pq, pad;
@@ -37,14 +39,51 @@ struct CgScalars {
   uint32_t ticket[4];
 };
 
-// Lanes per row: the smallest group whose kUnroll-deep pass covers the mean row.
+// ------------------------------------------------------------ launch shape --
+// GB300 issues FP64 at ~1/60 of its FP32 rate, below the rate at which HBM
+// delivers doubles, so FP64 kernels are shaped to issue few FP64 operations per
+// entry: 2 lanes x 8 entries per CSR row (one FP64 shuffle-add per lane) and
+// several vector entries per thread (the block reduction tree is paid once per
+// thread).  FP32 kernels use 4 lanes x 4 entries and more threads.
+static int sm_count()
+{
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  return sms;
+}
+
+template <typename V> constexpr int kEntriesPerLane = sizeof(V) == 8 ? 8 : 4;
+
+// Lanes per row: the smallest group whose pass covers the mean row length.
+template <typename V>
 static int row_group(const mg_plan* p)
 {
   const double mean = p->ndof > 0 ? (double)p->nnz / (double)p->ndof : 1.0;
-  if (mean > 64) return 32;
-  if (mean > 32) return 16;
-  if (mean > 16) return 8;
-  return 4;
+  const int U = kEntriesPerLane<V>;
+  for (int g = sizeof(V) == 8 ? 2 : 4; g < 32; g *= 2)
+    if (mean <= g * U) return g;
+  return 32;
+}
+
+// CTAs of a row kernel (G lanes per row) and of a vector kernel.
+template <typename V>
+static int row_blocks(const mg_plan* p, int G)
+{
+  const int64_t need = (p->ndof * G + kSolveThreads - 1) / kSolveThreads;
+  const int cap = (sizeof(V) == 8 ? 4 : 8) * sm_count();
+  return (int)std::max<int64_t>(1, std::min<int64_t>({need, (int64_t)cap, (int64_t)kMaxSolveBlocks}));
+}
+template <typename V>
+static int vec_blocks(int64_t n)
+{
+  const int64_t need = (n + kSolveThreads - 1) / kSolveThreads;
+  const int cap = (sizeof(V) == 8 ? 2 : 4) * sm_count();
+  return (int)std::max<int64_t>(1, std::min<int64_t>({need, (int64_t)cap, (int64_t)kMaxSolveBlocks}));
 }
 
 template <int G>
@@ -59,47 +98,112 @@ __device__ __forceinline__ unsigned group_mask()
 }
 
 // Dot product of one CSR row with x by a group of G lanes.  Each pass issues
-// kUnroll independent loads of (column, value) per lane before any gather of x,
-// so every lane keeps kUnroll requests in flight; the G partial sums are then
-// combined by xor shuffles in a fixed order.
-constexpr int kUnroll = 4;
-
+// U independent loads of (column, value) per lane before any gather of x, so
+// every lane keeps U requests in flight; the G partial sums are combined by xor
+// shuffles in a fixed order.
 template <typename V, int G>
-__device__ __forceinline__ double row_dot(int64_t row, const int32_t* __restrict__ rp,
-                                          const int32_t* __restrict__ ci, const V* __restrict__ val,
-                                          const V* __restrict__ x)
+__device__ __forceinline__ V row_dot(int64_t row, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                                     const V* __restrict__ val, const V* __restrict__ x)
 {
+  constexpr int U = kEntriesPerLane<V>;
   const int lane = threadIdx.x & (G - 1);
   const int s0 = __ldg(rp + row), s1 = __ldg(rp + row + 1);
   V sum = V(0);
-  for (int base = s0 + lane; base < s1; base += G * kUnroll) {
-    int c[kUnroll];
-    V v[kUnroll];
+  for (int base = s0 + lane; base < s1; base += G * U) {
+    int c[U];
+    V v[U];
 #pragma unroll
-    for (int u = 0; u < kUnroll; ++u) {
+    for (int u = 0; u < U; ++u) {
       const int s = base + u * G;
       c[u] = s < s1 ? __ldg(ci + s) : -1;
       v[u] = s < s1 ? __ldg(val + s) : V(0);
     }
 #pragma unroll
-    for (int u = 0; u < kUnroll; ++u)
+    for (int u = 0; u < U; ++u)
       if (c[u] >= 0) sum += v[u] * __ldg(x + c[u]);
   }
 #pragma unroll
   for (int off = G / 2; off > 0; off >>= 1) sum += __shfl_xor_sync(group_mask<G>(), sum, off, G);
-  return (double)sum;
+  return sum;
+}
+
+// Dot-product accumulation: FP64 for FP64 vectors; for FP32 vectors a
+// double-word (float pair) sum of exact float products on the FP32 pipes, as
+// accurate as FP64 here and free of FP64 operations.
+template <typename V> struct Dot;
+template <> struct Dot<double> {
+  using A = double;
+  __device__ static A zero() { return 0.0; }
+  __device__ static void mac(A& s, double a, double b) { s = __fma_rn(a, b, s); }
+  __device__ static A add(A a, A b) { return a + b; }
+  __device__ static A shfl(A v, int off) { return __shfl_xor_sync(0xffffffffu, v, off); }
+  __device__ static double to_double(A v) { return v; }
+};
+template <> struct Dot<float> {
+  using A = ff;
+  __device__ static A zero() { return ff{0.0f, 0.0f}; }
+  __device__ static void mac(A& s, float a, float b) { s = ff_add_s(s, two_prod(a, b)); }
+  __device__ static A add(A a, A b) { return ff_add_s(a, b); }
+  __device__ static A shfl(A v, int off)
+  {
+    return ff{__shfl_xor_sync(0xffffffffu, v.hi, off), __shfl_xor_sync(0xffffffffu, v.lo, off)};
+  }
+  __device__ static double to_double(A v) { return (double)v.hi + (double)v.lo; }
+};
+
+// Block-wide sum in a fixed tree; the result (as double) is valid in thread 0.
+template <typename V>
+__device__ __forceinline__ double block_sum(typename Dot<V>::A v, typename Dot<V>::A* sh)
+{
+  using D = Dot<V>;
+  const int tid = threadIdx.x;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v = D::add(v, D::shfl(v, off));
+  if ((tid & 31) == 0) sh[tid >> 5] = v;
+  __syncthreads();
+  double out = 0.0;
+  if (tid < 32) {
+    v = tid < (kSolveThreads / 32) ? sh[tid] : D::zero();
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v = D::add(v, D::shfl(v, off));
+    if (tid == 0) out = D::to_double(v);
+  }
+  __syncthreads();
+  return out;
+}
+
+// Sum of partials[0..n) in a fixed order by one CTA (valid in thread 0).
+__device__ __forceinline__ double reduce_partials(const double* partials, int n, double* sh)
+{
+  double v = 0.0;
+  for (int i = threadIdx.x; i < n; i += kSolveThreads) v += partials[i];
+  return block_sum<double>(v, sh);
+}
+
+// Last-CTA detection: returns true in the single CTA that finishes last.
+__device__ __forceinline__ bool last_block(uint32_t* ticket)
+{
+  __shared__ bool last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const uint32_t t = atomicAdd(ticket, 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (last) __threadfence();
+  return last;
 }
 
 template <typename V, int G>
 __global__ void __launch_bounds__(kSolveThreads) k_spmv(int64_t n, const int32_t* __restrict__ rp,
-                                                        const int32_t* __restrict__ ci,
-                                                        const V* __restrict__ val, const V* __restrict__ x,
-                                                        V* __restrict__ y)
+                                                        const int32_t* __restrict__ ci, const V* __restrict__ val,
+                                                        const V* __restrict__ x, V* __restrict__ y)
 {
   const int64_t groups = (int64_t)gridDim.x * (kSolveThreads / G);
   for (int64_t row = (blockIdx.x * (int64_t)kSolveThreads + threadIdx.x) / G; row < n; row += groups) {
-    const double s = row_dot<V, G>(row, rp, ci, val, x);
-    if ((threadIdx.x & (G - 1)) == 0) y[row] = (V)s;
+    const V s = row_dot<V, G>(row, rp, ci, val, x);
+    if ((threadIdx.x & (G - 1)) == 0) y[row] = s;
   }
 }
 
@@ -112,68 +216,30 @@ __global__ void k_rowsum(int64_t n, const int32_t* rp, const double* val, double
   y[r] = s;
 }
 
-// Block-wide sum of one double per thread in a fixed tree.
-__device__ __forceinline__ double block_sum(double v, double* sh)
-{
-  const int tid = threadIdx.x;
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-  if ((tid & 31) == 0) sh[tid >> 5] = v;
-  __syncthreads();
-  if (tid < 32) {
-    v = tid < (kSolveThreads / 32) ? sh[tid] : 0.0;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-  }
-  __syncthreads();
-  return v;  // valid in thread 0
-}
-
-// Sum of partials[0..n) in a fixed order by one CTA (valid in thread 0).
-__device__ __forceinline__ double reduce_partials(const double* partials, int n, double* sh)
-{
-  double v = 0.0;
-  for (int i = threadIdx.x; i < n; i += kSolveThreads) v += partials[i];
-  return block_sum(v, sh);
-}
-
-// Last-CTA detection: returns true in the single CTA that finishes last.
-__device__ __forceinline__ bool last_block(uint32_t* ticket)
-{
-  __shared__ bool last;
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    const uint32_t t = atomicAdd(ticket, 1u);
-    last = (t == gridDim.x - 1);
-  }
-  __syncthreads();
-  if (last) __threadfence();
-  return last;
-}
-
 // K1: q = A p, alpha = rz / (p . q)
 template <typename V, int G>
 __global__ void __launch_bounds__(kSolveThreads) k_cg_spmv(int64_t n, const int32_t* __restrict__ rp,
-                                                           const int32_t* __restrict__ ci,
-                                                           const V* __restrict__ val, const V* __restrict__ p,
-                                                           V* __restrict__ q, double* partials, CgScalars* s)
+                                                           const int32_t* __restrict__ ci, const V* __restrict__ val,
+                                                           const V* __restrict__ p, V* __restrict__ q,
+                                                           double* partials, CgScalars* s)
 {
-  __shared__ double sh[32];
+  using D = Dot<V>;
+  __shared__ typename D::A sh[32];
+  __shared__ double shd[32];
   if (s->done) return;
   const int64_t groups = (int64_t)gridDim.x * (kSolveThreads / G);
-  double acc = 0.0;
+  typename D::A acc = D::zero();
   for (int64_t row = (blockIdx.x * (int64_t)kSolveThreads + threadIdx.x) / G; row < n; row += groups) {
-    const double v = row_dot<V, G>(row, rp, ci, val, p);
+    const V v = row_dot<V, G>(row, rp, ci, val, p);
     if ((threadIdx.x & (G - 1)) == 0) {
-      q[row] = (V)v;
-      acc += (double)p[row] * (double)(V)v;
+      q[row] = v;
+      D::mac(acc, p[row], v);
     }
   }
-  const double b = block_sum(acc, sh);
+  const double b = block_sum<V>(acc, sh);
   if (threadIdx.x == 0) partials[blockIdx.x] = b;
   if (last_block(&s->ticket[0])) {
-    const double pq = reduce_partials(partials, gridDim.x, sh);
+    const double pq = reduce_partials(partials, gridDim.x, shd);
     if (threadIdx.x == 0) {
       s->pq = pq;
       s->alpha = s->rz / pq;
@@ -190,10 +256,13 @@ __global__ void __launch_bounds__(kSolveThreads) k_cg_update(int64_t n, V* __res
                                                              const V* __restrict__ q, const V* __restrict__ dinv,
                                                              double* partials, CgScalars* s)
 {
-  __shared__ double sh[32];
+  using D = Dot<V>;
+  __shared__ typename D::A sh[32];
+  __shared__ double shd[32];
   if (s->done) return;
   const V alpha = (V)s->alpha;
-  double prz = 0.0, prr = 0.0;
+  typename D::A prz = D::zero(), prr = D::zero();
+#pragma unroll 4
   for (int64_t i = blockIdx.x * (int64_t)kSolveThreads + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * kSolveThreads) {
     x[i] += alpha * p[i];
@@ -201,18 +270,18 @@ __global__ void __launch_bounds__(kSolveThreads) k_cg_update(int64_t n, V* __res
     r[i] = ri;
     const V zi = dinv[i] * ri;
     z[i] = zi;
-    prz += (double)ri * (double)zi;
-    prr += (double)ri * (double)ri;
+    D::mac(prz, ri, zi);
+    D::mac(prr, ri, ri);
   }
-  const double b1 = block_sum(prz, sh);
-  const double b2 = block_sum(prr, sh);
+  const double b1 = block_sum<V>(prz, sh);
+  const double b2 = block_sum<V>(prr, sh);
   if (threadIdx.x == 0) {
     partials[blockIdx.x] = b1;
     partials[gridDim.x + blockIdx.x] = b2;
   }
   if (last_block(&s->ticket[1])) {
-    const double rz = reduce_partials(partials, gridDim.x, sh);
-    const double rr = reduce_partials(partials + gridDim.x, gridDim.x, sh);
+    const double rz = reduce_partials(partials, gridDim.x, shd);
+    const double rr = reduce_partials(partials + gridDim.x, gridDim.x, shd);
     if (threadIdx.x == 0) {
       s->beta = rz / s->rz;
       s->rz = rz;
@@ -232,6 +301,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_cg_dir(int64_t n, const V* __
 {
   if (s->done) return;
   const V beta = (V)s->beta;
+#pragma unroll 4
   for (int64_t i = blockIdx.x * (int64_t)kSolveThreads + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * kSolveThreads)
     p[i] = z[i] + beta * p[i];
@@ -241,43 +311,44 @@ __global__ void __launch_bounds__(kSolveThreads) k_cg_dir(int64_t n, const V* __
 // D^-1 from the diagonal, partials of r.z, r.r, b.b.
 template <typename V, int G>
 __global__ void __launch_bounds__(kSolveThreads) k_cg_start(int64_t n, const int32_t* __restrict__ rp,
-                                                            const int32_t* __restrict__ ci,
-                                                            const V* __restrict__ val, const int32_t* __restrict__ diag,
-                                                            const V* __restrict__ b, const V* __restrict__ x,
-                                                            int zero_x, int jacobi, V* __restrict__ r,
-                                                            V* __restrict__ z, V* __restrict__ p,
+                                                            const int32_t* __restrict__ ci, const V* __restrict__ val,
+                                                            const int32_t* __restrict__ diag, const V* __restrict__ b,
+                                                            const V* __restrict__ x, int zero_x, int jacobi,
+                                                            V* __restrict__ r, V* __restrict__ z, V* __restrict__ p,
                                                             V* __restrict__ dinv, double* partials, CgScalars* s)
 {
-  __shared__ double sh[32];
+  using D = Dot<V>;
+  __shared__ typename D::A sh[32];
+  __shared__ double shd[32];
   const int64_t groups = (int64_t)gridDim.x * (kSolveThreads / G);
-  double prz = 0.0, prr = 0.0, pbb = 0.0;
+  typename D::A prz = D::zero(), prr = D::zero(), pbb = D::zero();
   for (int64_t row = (blockIdx.x * (int64_t)kSolveThreads + threadIdx.x) / G; row < n; row += groups) {
-    double ax = 0.0;
+    V ax = V(0);
     if (!zero_x) ax = row_dot<V, G>(row, rp, ci, val, x);
     if ((threadIdx.x & (G - 1)) == 0) {
       const V dv = val[diag[row]];
       const V di = (jacobi && dv != V(0)) ? V(1) / dv : V(1);
-      const V ri = (V)((double)b[row] - ax);
+      const V ri = b[row] - ax;
       const V zi = di * ri;
       dinv[row] = di;
       r[row] = ri;
       z[row] = zi;
       p[row] = zi;
-      prz += (double)ri * (double)zi;
-      prr += (double)ri * (double)ri;
-      pbb += (double)b[row] * (double)b[row];
+      D::mac(prz, ri, zi);
+      D::mac(prr, ri, ri);
+      D::mac(pbb, b[row], b[row]);
     }
   }
-  const double b1 = block_sum(prz, sh), b2 = block_sum(prr, sh), b3 = block_sum(pbb, sh);
+  const double b1 = block_sum<V>(prz, sh), b2 = block_sum<V>(prr, sh), b3 = block_sum<V>(pbb, sh);
   if (threadIdx.x == 0) {
     partials[blockIdx.x] = b1;
     partials[gridDim.x + blockIdx.x] = b2;
     partials[2 * gridDim.x + blockIdx.x] = b3;
   }
   if (last_block(&s->ticket[2])) {
-    const double rz = reduce_partials(partials, gridDim.x, sh);
-    const double rr = reduce_partials(partials + gridDim.x, gridDim.x, sh);
-    const double bb = reduce_partials(partials + 2 * gridDim.x, gridDim.x, sh);
+    const double rz = reduce_partials(partials, gridDim.x, shd);
+    const double rr = reduce_partials(partials + gridDim.x, gridDim.x, shd);
+    const double bb = reduce_partials(partials + 2 * gridDim.x, gridDim.x, shd);
     if (threadIdx.x == 0) {
       s->rz = rz;
       s->rr = rr;
@@ -289,16 +360,15 @@ __global__ void __launch_bounds__(kSolveThreads) k_cg_start(int64_t n, const int
   }
 }
 
-// Refinement residual: r64 = b - A64 x, rr = r64 . r64 (last CTA), and the
-// scaled FP32 right-hand side r32 = r64 / ||r64|| is written by k_scale_cast.
+// Refinement residual: r64 = b - A64 x, rr = r64 . r64 (last CTA); the scaled
+// FP32 right-hand side r32 = r64 / ||r64|| is then written by k_scale_cast.
 template <int G>
 __global__ void __launch_bounds__(kSolveThreads) k_residual64(int64_t n, const int32_t* __restrict__ rp,
                                                               const int32_t* __restrict__ ci,
                                                               const double* __restrict__ val,
                                                               const double* __restrict__ b,
-                                                              const double* __restrict__ x,
-                                                              double* __restrict__ r, double* partials,
-                                                              CgScalars* s)
+                                                              const double* __restrict__ x, double* __restrict__ r,
+                                                              double* partials, CgScalars* s)
 {
   __shared__ double sh[32];
   const int64_t groups = (int64_t)gridDim.x * (kSolveThreads / G);
@@ -308,11 +378,11 @@ __global__ void __launch_bounds__(kSolveThreads) k_residual64(int64_t n, const i
     if ((threadIdx.x & (G - 1)) == 0) {
       const double ri = b[row] - ax;
       r[row] = ri;
-      prr += ri * ri;
-      pbb += b[row] * b[row];
+      prr = __fma_rn(ri, ri, prr);
+      pbb = __fma_rn(b[row], b[row], pbb);
     }
   }
-  const double b1 = block_sum(prr, sh), b2 = block_sum(pbb, sh);
+  const double b1 = block_sum<double>(prr, sh), b2 = block_sum<double>(pbb, sh);
   if (threadIdx.x == 0) {
     partials[blockIdx.x] = b1;
     partials[gridDim.x + blockIdx.x] = b2;
@@ -342,34 +412,28 @@ __global__ void k_correct(int64_t n, double* x, const float* d32, double scale)
     x[i] += scale * (double)d32[i];
 }
 
-static int solve_blocks(const mg_plan* p, int G)
-{
-  const int64_t rows_per_block = kSolveThreads / G;
-  const int64_t need = (p->ndof + rows_per_block - 1) / rows_per_block;
-  return (int)std::max<int64_t>(1, std::min<int64_t>(need, kMaxSolveBlocks));
-}
-
-#define MG_DISPATCH_G(G, ...)          \
-  switch (G) {                          \
-    case 32: { constexpr int g = 32; __VA_ARGS__; } break; \
-    case 16: { constexpr int g = 16; __VA_ARGS__; } break; \
-    case 8: { constexpr int g = 8; __VA_ARGS__; } break;   \
-    default: { constexpr int g = 4; __VA_ARGS__; } break;  \
+#define MG_DISPATCH_G(G, ...)                                \
+  switch (G) {                                               \
+    case 32: { constexpr int g = 32; __VA_ARGS__; } break;   \
+    case 16: { constexpr int g = 16; __VA_ARGS__; } break;   \
+    case 8: { constexpr int g = 8; __VA_ARGS__; } break;     \
+    case 4: { constexpr int g = 4; __VA_ARGS__; } break;     \
+    default: { constexpr int g = 2; __VA_ARGS__; } break;    \
   }
 
 mg_status launch_spmv(mg_plan* p, int prec, const void* vals, const void* x, void* y, cudaStream_t st)
 {
   if (prec != MG_F64 && prec != MG_F32) return set_error(MG_ERR_INVALID_ARG, "bad precision");
+  if (p->ndof == 0) return MG_OK;
   if (!vals || !x || !y) return set_error(MG_ERR_INVALID_ARG, "mg_spmv: null argument");
   MG_TRY(plan_device(p));
-  const int G = row_group(p);
-  const int nb = solve_blocks(p, G);
-  if (p->ndof == 0) return MG_OK;
   if (prec == MG_F64) {
+    const int G = row_group<double>(p), nb = row_blocks<double>(p, G);
     MG_DISPATCH_G(G, (k_spmv<double, g><<<nb, kSolveThreads, 0, st>>>(p->ndof, p->d_rowptr, p->d_colind,
                                                                          (const double*)vals, (const double*)x,
                                                                          (double*)y)));
   } else {
+    const int G = row_group<float>(p), nb = row_blocks<float>(p, G);
     MG_DISPATCH_G(G, (k_spmv<float, g><<<nb, kSolveThreads, 0, st>>>(p->ndof, p->d_rowptr, p->d_colind,
                                                                         (const float*)vals, (const float*)x,
                                                                         (float*)y)));
@@ -429,7 +493,7 @@ static mg_status cg_iterate(mg_plan* p, const V* vals, V* x, CgWork<V>& w, int G
                             cudaStream_t st, CgScalars* h_s)
 {
   const int64_t n = p->ndof;
-  const int vb = (int)std::max<int64_t>(1, std::min<int64_t>((n + kSolveThreads - 1) / kSolveThreads, kMaxSolveBlocks));
+  const int vb = vec_blocks<V>(n);
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   bool use_graph = true;
@@ -540,9 +604,9 @@ mg_status mg_cg_solve_noalloc(mg_plan* p, const double* d_values, const double* 
   MG_TRY(noalloc_scratch(&base));
   cudaStream_t st = (cudaStream_t)stream;
   CgWork<double> w = cg_work_carve<double>(base, p->ndof);
-  const int G = row_group(p), nb = solve_blocks(p, G);
+  const int G = row_group<double>(p), nb = row_blocks<double>(p, G);
   const int64_t n = p->ndof;
-  const int vb = (int)std::max<int64_t>(1, std::min<int64_t>((n + kSolveThreads - 1) / kSolveThreads, kMaxSolveBlocks));
+  const int vb = vec_blocks<double>(n);
   const auto t0 = std::chrono::steady_clock::now();
   // cg_start writes the scalars from the host (tickets and flags start at zero)
   MG_TRY(cg_start<double>(p, d_values, d_b, d_x, 0, precond == MG_PREC_JACOBI, rtol, maxit, w, G, nb, st));
@@ -589,7 +653,7 @@ mg_status mg_cg_solve(mg_plan* p, const double* d_values, const double* d_b, dou
   void* base = nullptr;
   MG_TRY(plan_work(p, cg_work_bytes<double>(p->ndof), &base));
   CgWork<double> w = cg_work_carve<double>(base, p->ndof);
-  const int G = row_group(p), nb = solve_blocks(p, G);
+  const int G = row_group<double>(p), nb = row_blocks<double>(p, G);
   cudaEvent_t e0, e1;
   MG_CUDA(cudaEventCreate(&e0));
   MG_CUDA(cudaEventCreate(&e1));
@@ -637,8 +701,9 @@ mg_status mg_cg_refined(mg_plan* p, const double* d_values64, const float* d_val
   double* r64 = (double*)((char*)base + wbytes);
   float* d32 = (float*)((char*)r64 + v64);
   float* r32 = (float*)((char*)d32 + v32);
-  const int G = row_group(p), nb = solve_blocks(p, G);
-  const int eb = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 4 * kMaxSolveBlocks));
+  const int G64 = row_group<double>(p), nb64 = row_blocks<double>(p, G64);
+  const int G = row_group<float>(p), nb = row_blocks<float>(p, G);
+  const int eb = vec_blocks<float>(n);
   CgScalars* hs = reinterpret_cast<CgScalars*>(p->h_pinned);
   MG_CUDA(cudaMemsetAsync(w.s, 0, sizeof(CgScalars), st));
   cudaEvent_t e0, e1;
@@ -650,8 +715,8 @@ mg_status mg_cg_refined(mg_plan* p, const double* d_values64, const float* d_val
   double relres = INFINITY;
   mg_status s = MG_OK;
   for (; outer <= max_outer; ++outer) {
-    MG_DISPATCH_G(G, (k_residual64<g><<<nb, kSolveThreads, 0, st>>>(n, p->d_rowptr, p->d_colind, d_values64, d_b,
-                                                                      d_x, r64, w.partials, w.s)));
+    MG_DISPATCH_G(G64, (k_residual64<g><<<nb64, kSolveThreads, 0, st>>>(n, p->d_rowptr, p->d_colind, d_values64,
+                                                                          d_b, d_x, r64, w.partials, w.s)));
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpyAsync(hs, w.s, sizeof(CgScalars), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);

@@ -37,7 +37,7 @@ def emulate_schedule(sched, order, local_mats, nnz, rowptr):
     rows, racc = sched["rows"], sched["row_acc"]
     for b in range(info.nblocks):
         ib, ic, cb, nc, rb, rc = (int(v) for v in blocks[b, :6])
-        acc = np.zeros(info.acc_max)
+        acc = np.zeros(info.acc_max + 1)  # + the padding words' dummy slot
         for c in range(nc):
             buf = np.zeros(nu * CI + 1)
             for t in range(min(CI, ic - c * CI)):
@@ -46,14 +46,15 @@ def emulate_schedule(sched, order, local_mats, nnz, rowptr):
                     buf[u * CI + t] = local_mats[e][i, j]
             base = (cb + c) * (W + 1)
             for w in range(W):
-                seg = ent[cptr[base + w]:cptr[base + w + 1]].reshape(-1, 32)
+                # [piece][lane][PW]: a piece's words go to the slot of its first word
+                PW = 4 if order == 1 else 2
+                seg = ent[cptr[base + w]:cptr[base + w + 1]].reshape(-1, 32, PW)
                 for lane in range(32):
-                    s = 0.0
-                    for word in seg[:, lane]:
-                        s += buf[int(word) & 0x1fff]
-                        if int(word) >> 31:
-                            acc[(int(word) >> 13) & 0x3fff] += s
-                            s = 0.0
+                    for piece in seg[:, lane, :]:
+                        v = buf[int(piece[0]) & 0x1fff]
+                        for word in piece[1:]:
+                            v += buf[int(word) & 0x1fff]
+                        acc[(int(piece[0]) >> 13) & 0x3fff] += v
         for r in range(rc):
             row, a0 = rows[rb + r], racc[rb + r]
             ln = rowptr[row + 1] - rowptr[row]

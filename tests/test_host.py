@@ -172,3 +172,35 @@ def test_export_schedule_info_fields():
     s = b.export_schedule()
     # every block's item list is padded to a multiple of 4 with -1
     assert len(s["items"]) % 4 == 0 and (s["items"] >= -1).all()
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_schedule_slots_have_one_writer_per_chunk(order):
+    """Within a chunk each accumulator slot is written by exactly one thread (the
+    kernel's race freedom); a piece's first word carries its slot and a real
+    source; padding pieces target only the dummy slot with zero sources; real
+    slots lie inside the block."""
+    m = meshgen.kuhn_cube(4, jitter=0.2, seed=2, permute=True)
+    b = mg.MatrixBuilder(mg.Mesh(m.xyz, m.conn, order=order))
+    s = b.export_schedule()
+    info = s["info"]
+    nu = 10 if order == 1 else 55
+    zero = nu * info.chunk_items
+    for bk in range(info.nblocks):
+        cb, nc, used = s["blocks"][bk, 2], s["blocks"][bk, 3], s["blocks"][bk, 6]
+        for c in range(cb, cb + nc):
+            cp = s["chunk_ptr"][c * (info.warps + 1):(c + 1) * (info.warps + 1)]
+            owner = {}
+            PW = 4 if order == 1 else 2
+            for w in range(info.warps):
+                seg = s["entries"][cp[w]:cp[w + 1]].reshape(-1, 32, PW)
+                for lane in range(32):
+                    t = 32 * w + lane
+                    for piece in seg[:, lane, :]:
+                        slot = (int(piece[0]) >> 13) & 0x3fff
+                        srcs = [int(x) & 0x1fff for x in piece]
+                        if slot == info.acc_max:
+                            assert all(x == zero for x in srcs)
+                            continue
+                        assert slot < used and all(x <= zero for x in srcs) and srcs[0] < zero
+                        assert owner.setdefault(slot, t) == t
