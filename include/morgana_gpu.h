@@ -159,6 +159,9 @@ typedef struct {
   int64_t n_contrib;   /* element-matrix entries scattered (= n_elements * nb^2) */
   int64_t n_item_slots;      /* length of the exported item array (padding included) */
   int64_t max_chunk_entries; /* words of the largest chunk (its shared-memory staging buffer) */
+  int64_t max_chunk_vertices;     /* distinct vertices of the largest chunk (padded to 4) */
+  int64_t max_chunk_record_bytes; /* largest chunk record: element ids, local vertex indices,
+                                     vertex coordinates (its shared-memory stage) */
 } mg_schedule_info;
 
 mg_status mg_plan_schedule_info(const mg_plan* plan, mg_schedule_info* info);

@@ -65,7 +65,8 @@ class ScheduleInfo(ctypes.Structure):
                 ("acc_max", ctypes.c_int32), ("chunk_items", ctypes.c_int32), ("host_copy", ctypes.c_int32),
                 ("n_items", ctypes.c_int64), ("n_chunks", ctypes.c_int64), ("n_entries", ctypes.c_int64),
                 ("n_contrib", ctypes.c_int64), ("n_item_slots", ctypes.c_int64),
-                ("max_chunk_entries", ctypes.c_int64)]
+                ("max_chunk_entries", ctypes.c_int64), ("max_chunk_vertices", ctypes.c_int64),
+                ("max_chunk_record_bytes", ctypes.c_int64)]
 
 
 _P = ctypes.c_void_p

@@ -170,36 +170,22 @@ struct GeoPtrs {
   const float* loz;        // lz
 };
 
-// The global loads an element needs (vertex coordinates and coefficient), issued
-// one chunk ahead of their use so that their latency overlaps the previous
-// chunk's arithmetic and reduction.  FP32 reads one 32-byte sector per vertex
-// (hi + mid); double-word adds lo.z.
+// The coordinates an element needs.  The assembly kernel reads them from the
+// chunk record staged in shared memory (local vertex indices); the adjoint
+// kernel reads them from the mesh arrays in global memory.  FP32 uses hi + mid
+// of each coordinate, double-word hi + mid + lo, native FP64 their exact sum.
 template <int MODE> struct Fetch;
 template <> struct Fetch<kF32> {
   float4 a[4], b[4];
-  int4 n;
-  double coef;
 };
 template <> struct Fetch<kDW> {
   float4 a[4], b[4];
   float lz[4];
-  double coef;
 };
 template <> struct Fetch<kF64> {
   double4_32a x[4];
-  double coef;
 };
 
-__device__ __forceinline__ void fetch(const GeoPtrs& g, int4 n, Fetch<kF32>& F)
-{
-  const int id[4] = {n.x, n.y, n.z, n.w};
-#pragma unroll
-  for (int s = 0; s < 4; ++s) {
-    F.a[s] = g.rec[2 * (int64_t)id[s]];
-    F.b[s] = g.rec[2 * (int64_t)id[s] + 1];
-  }
-  F.n = n;
-}
 __device__ __forceinline__ void fetch(const GeoPtrs& g, int4 n, Fetch<kDW>& F)
 {
   const int id[4] = {n.x, n.y, n.z, n.w};
@@ -210,11 +196,38 @@ __device__ __forceinline__ void fetch(const GeoPtrs& g, int4 n, Fetch<kDW>& F)
     F.lz[s] = g.loz[id[s]];
   }
 }
-__device__ __forceinline__ void fetch(const GeoPtrs& g, int4 n, Fetch<kF64>& F)
+
+// from a staged chunk record: rec = 2 float4 per vertex, loz = lo.z per vertex
+__device__ __forceinline__ void fetch_staged(const float4* rec, const float*, ushort4 lc, Fetch<kF32>& F)
 {
-  const int id[4] = {n.x, n.y, n.z, n.w};
+  const int id[4] = {lc.x, lc.y, lc.z, lc.w};
 #pragma unroll
-  for (int s = 0; s < 4; ++s) F.x[s] = g.xyz[id[s]];
+  for (int s = 0; s < 4; ++s) {
+    F.a[s] = rec[2 * id[s]];
+    F.b[s] = rec[2 * id[s] + 1];
+  }
+}
+__device__ __forceinline__ void fetch_staged(const float4* rec, const float* loz, ushort4 lc, Fetch<kDW>& F)
+{
+  const int id[4] = {lc.x, lc.y, lc.z, lc.w};
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    F.a[s] = rec[2 * id[s]];
+    F.b[s] = rec[2 * id[s] + 1];
+    F.lz[s] = loz[id[s]];
+  }
+}
+// hi + mid + lo summed in FP64 is exact (the three parts are the successive
+// float roundings of the coordinate's remainders)
+__device__ __forceinline__ void fetch_staged(const float4* rec, const float* loz, ushort4 lc, Fetch<kF64>& F)
+{
+  const int id[4] = {lc.x, lc.y, lc.z, lc.w};
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    const float4 u = rec[2 * id[s]], v = rec[2 * id[s] + 1];
+    F.x[s] = make_double4_32a(((double)u.x + (double)u.w) + (double)v.z, ((double)u.y + (double)v.x) + (double)v.w,
+                              ((double)u.z + (double)v.y) + (double)loz[id[s]], 0.0);
+  }
 }
 
 // components of a vertex record: hi, mid, lo
@@ -224,7 +237,7 @@ __device__ __forceinline__ float rec_lo(const float4& b, float lz, int r) { retu
 
 __device__ __forceinline__ double comp(const double4_32a& v, int r) { return r == 0 ? v.x : (r == 1 ? v.y : v.z); }
 
-__device__ __forceinline__ void geometry(const GeoPtrs&, const Fetch<kF64>& F, Cof<double>& f)
+__device__ __forceinline__ void geometry(const Fetch<kF64>& F, Cof<double>& f)
 {
   double J[3][3];
 #pragma unroll
@@ -235,9 +248,10 @@ __device__ __forceinline__ void geometry(const GeoPtrs&, const Fetch<kF64>& F, C
 }
 
 // FP32: edge vectors (hi_k - hi_0) + (mid_k - mid_0), accurate to a few float
-// ulps of the edge itself; flat elements recompute the cofactors in FP64.
+// ulps of the edge itself; flat elements recompute the cofactors in FP64 from
+// hi + mid.
 constexpr float kFlatTol = 1e-3f;
-__device__ __forceinline__ void geometry(const GeoPtrs& g, const Fetch<kF32>& F, Cof<float>& f)
+__device__ __forceinline__ void geometry(const Fetch<kF32>& F, Cof<float>& f)
 {
   float J[3][3];
 #pragma unroll
@@ -251,10 +265,13 @@ __device__ __forceinline__ void geometry(const GeoPtrs& g, const Fetch<kF32>& F,
 #pragma unroll
   for (int k = 0; k < 3; ++k) nn[k] = J[0][k] * J[0][k] + J[1][k] * J[1][k] + J[2][k] * J[2][k];
   if (f.det * f.det < kFlatTol * kFlatTol * nn[0] * nn[1] * nn[2]) {
-    Fetch<kF64> D;
-    fetch(g, F.n, D);
+    Fetch<kF64> D;  // hi + mid: coordinates to 2^-48 relative
+#pragma unroll
+    for (int s = 0; s < 4; ++s)
+      D.x[s] = make_double4_32a((double)F.a[s].x + (double)F.a[s].w, (double)F.a[s].y + (double)F.b[s].x,
+                                (double)F.a[s].z + (double)F.b[s].y, 0.0);
     Cof<double> d;
-    geometry(g, D, d);
+    geometry(D, d);
     for (int r = 0; r < 3; ++r)
       for (int k = 0; k < 3; ++k) f.c[r][k] = (float)d.c[r][k];
     f.det = (float)d.det;
@@ -274,7 +291,7 @@ __device__ __forceinline__ ff dw_diff(float hb, float ha, float mb, float ma, fl
   return two_sum(s.hi, t);
 }
 
-__device__ __forceinline__ void geometry(const GeoPtrs&, const Fetch<kDW>& F, Cof<ff>& f)
+__device__ __forceinline__ void geometry(const Fetch<kDW>& F, Cof<ff>& f)
 {
   ff J[3][3];
 #pragma unroll
@@ -301,7 +318,7 @@ __device__ __forceinline__ void geometry_now(const GeoPtrs& g, int4 n, Cof<typen
 {
   Fetch<MODE> F;
   fetch(g, n, F);
-  geometry(g, F, f);
+  geometry(F, f);
 }
 
 // ------------------------------------------------------- element matrices --
@@ -370,13 +387,10 @@ __device__ __forceinline__ void metric(const Cof<T>& f, T s, T g[6])
 
 struct AsmArgs {
   const BlockDesc* blocks;
-  const int32_t* items;
-  const int4* item_conn;
-  const ChunkDesc* chunks;
+  const unsigned char* chunk_data;  // chunk records (layout at ChunkDesc)
+  const int2* chunk_rec;            // (offset / 16, bytes) per chunk
   const uint32_t* entries;
-  const int32_t* row_csr;
-  const int32_t* row_acc;
-  GeoPtrs geo;
+  const int2* row_meta;             // (accumulator base, CSR start - base) per owned row
   const double* coeff;   // per element, or null
   double cconst;         // used when coeff is null
   const double* tables;  // unique-entry tables: stiff[6][nu] then mass[nu]
@@ -385,58 +399,59 @@ struct AsmArgs {
   uint32_t* counters;
   int nblocks;
   int stiff;
-  int ent_cap;           // words of the shared-memory contribution buffer
+  int ent_cap;           // words of one shared-memory contribution buffer
+  int stage_cap;         // bytes of one chunk-record stage (the largest record)
 };
 
 constexpr size_t align16(size_t n) { return (n + 15) / 16 * 16; }
 
 // Shared-memory layout of k_assemble.  Every region starts on a 16-byte
-// boundary: the bulk copies (element nodes, ids, chunk records, contribution
-// words) require 16-byte aligned destinations, the mbarriers 8-byte.
+// boundary: the bulk copies (chunk records, contribution words, row metadata)
+// require 16-byte aligned destinations, the mbarriers 8-byte.
 template <int ORDER, int MODE>
 struct AsmLayout {
   using T = typename Arith<MODE>::T;
   static constexpr int NB = ORDER == 1 ? 4 : 10;
   static constexpr int NU = ORDER == 1 ? 10 : 55;
   static constexpr int CI = ORDER == 1 ? kChunkP1 : kChunkP2;
-  static constexpr int kRowBatch = kThreads;  // owned rows written per batch
+  static constexpr int kStages = 3;  // chunk-record stages
+  static constexpr int kBars = kStages + 2 + 1;  // records, words, row metadata
   static constexpr size_t acc_bytes = align16(sizeof(T) * (kAccMax + 1));  // + the padding words' dummy slot
   static constexpr size_t buf_bytes = align16(sizeof(T) * (NU * CI + 1));
   static constexpr size_t tab_bytes = align16(sizeof(T) * 7 * NU);
-  static constexpr size_t conn_bytes = align16(16 * CI);              // per stage (two stages)
-  static constexpr size_t ids_bytes = align16(4 * CI);                // per stage (two stages)
-  static constexpr size_t desc_bytes = align16(sizeof(ChunkDesc));    // per stage (two stages)
-  static constexpr size_t rowmeta_bytes = align16(4 * (2 * kRowBatch + 1));
-  // offsets
   static constexpr size_t off_buf = acc_bytes;
   static constexpr size_t off_tab = off_buf + buf_bytes;
-  static constexpr size_t off_conn = off_tab + tab_bytes;
-  static constexpr size_t off_ids = off_conn + 2 * conn_bytes;
-  static constexpr size_t off_desc = off_ids + 2 * ids_bytes;
-  static constexpr size_t off_rowmeta = off_desc + 2 * desc_bytes;
-  static constexpr size_t off_words = off_rowmeta + rowmeta_bytes;
-  static_assert(off_buf % 16 == 0 && off_tab % 16 == 0 && off_conn % 16 == 0 && off_ids % 16 == 0 &&
-                    off_desc % 16 == 0 && off_rowmeta % 16 == 0 && off_words % 16 == 0,
+  static constexpr size_t off_stage = off_tab + tab_bytes;
+  static_assert(off_buf % 16 == 0 && off_tab % 16 == 0 && off_stage % 16 == 0,
                 "shared-memory regions must start on 16-byte boundaries");
-  // two word buffers (chunk c uses buffer c & 1)
+  __host__ __device__ static size_t stage_bytes(int stage_cap) { return ((size_t)stage_cap + 15) / 16 * 16; }
   __host__ __device__ static size_t words_bytes(int ent_cap) { return ((size_t)ent_cap * 4 + 15) / 16 * 16; }
-  __host__ __device__ static size_t off_bars(int ent_cap) { return off_words + 2 * words_bytes(ent_cap); }
-  __host__ __device__ static size_t total(int ent_cap) { return off_bars(ent_cap) + 32; }
+  __host__ __device__ static size_t off_words(int stage_cap) { return off_stage + kStages * stage_bytes(stage_cap); }
+  __host__ __device__ static size_t off_bars(int ent_cap, int stage_cap)
+  {
+    return off_words(stage_cap) + 2 * words_bytes(ent_cap);
+  }
+  __host__ __device__ static size_t total(int ent_cap, int stage_cap) { return off_bars(ent_cap, stage_cap) + 8 * kBars; }
+  // owned rows per write-out batch: the row metadata reuses the stage area
+  // (an aligned copy of nr rows spans at most nr + 3 entries of 8 bytes)
+  __host__ __device__ static int meta_rows(int stage_cap) { return (int)(kStages * stage_bytes(stage_cap) / 8) - 4; }
 };
 
-// Pipeline of one block of c = 0 .. nchunks-1 (stage c & 1 for the element
-// nodes, ids, chunk record and contribution words):
-//   before chunk c      nodes(c+1), nodes(c+2) and words(c) staged or in
-//                       flight; chunk c's coordinates in registers (R) and its
-//                       per-warp word range in registers
-//   start of chunk c    wait nodes(c+1); bulk copy words(c+1) into the buffer
-//                       chunk c-1 released; read chunk c+1's word range; load
-//                       chunk c+1's coordinates into P
-//   phase 1 (c)         element matrices from R
-//   barrier             stage (c+1) & 1 has been read: copy nodes(c+3) into it
-//   phase 2 (c)         wait words(c), add the contributions
-//   barrier             R = P
-// so every copy has more than one chunk of work to land.
+// Per block, chunk c = 0 .. nchunks-1 uses record stage c % 3 and word buffer
+// c & 1:
+//   block start        copy records 0, 1, 2 (offsets from chunk_rec)
+//   top of chunk c     wait record c+1; copy words(c+1) into the buffer chunk
+//                      c-1 released; read chunk c+1's word range and gather
+//                      its element coefficients into registers
+//   phase 1 (c)        element matrices from record c's staged vertices
+//   barrier            record c has been read: copy record c+3 into its stage
+//                      (its offset is in record c); after the last chunk's
+//                      phase 1, copy the first batch of row metadata into the
+//                      stage area instead
+//   phase 2 (c)        wait words(c), add the contributions
+//   barrier
+// then the owned rows are written out batch by batch.  Every copy has at least
+// one chunk of work to land behind.
 // The double-word variants need 8-byte accumulators and element entries, so
 // shared memory admits one CTA per SM; they get the full register file.
 template <int ORDER, int MODE>
@@ -445,21 +460,21 @@ __global__ void __launch_bounds__(kThreads, MODE == kDW ? 1 : 2) k_assemble(AsmA
   using A = Arith<MODE>;
   using T = typename A::T;
   using L = AsmLayout<ORDER, MODE>;
-  constexpr int NU = L::NU, CI = L::CI;
+  constexpr int NU = L::NU, CI = L::CI, NS = L::kStages;
   constexpr int TPI = ORDER == 1 ? 1 : kP2ThreadsPerItem;  // threads per item
   extern __shared__ __align__(16) unsigned char smem[];
   T* acc = reinterpret_cast<T*>(smem);
   T* buf = reinterpret_cast<T*>(smem + L::off_buf);
   T* tab = reinterpret_cast<T*>(smem + L::off_tab);
-  int4* sconn = reinterpret_cast<int4*>(smem + L::off_conn);        // [2][CI]
-  int32_t* sids = reinterpret_cast<int32_t*>(smem + L::off_ids);    // [2][CI]
-  ChunkDesc* sdesc = reinterpret_cast<ChunkDesc*>(smem + L::off_desc);  // [2]
-  int32_t* s_rcsr = reinterpret_cast<int32_t*>(smem + L::off_rowmeta);  // [kRowBatch]
-  int32_t* s_racc = s_rcsr + L::kRowBatch;                              // [kRowBatch + 1]
-  uint32_t* sent = reinterpret_cast<uint32_t*>(smem + L::off_words);  // [2][words_bytes / 4]
+  unsigned char* stage = smem + L::off_stage;  // [NS][sbytes]
+  const int sbytes = (int)L::stage_bytes(a.stage_cap);
+  const int2* smeta = reinterpret_cast<const int2*>(stage);  // row metadata (write-out only)
+  uint32_t* sent = reinterpret_cast<uint32_t*>(smem + L::off_words(a.stage_cap));  // [2][went]
   const int went = (int)(L::words_bytes(a.ent_cap) / 4);
-  uint64_t* bar_nodes = reinterpret_cast<uint64_t*>(smem + L::off_bars(a.ent_cap));  // [2]
-  uint64_t* bar_ent = bar_nodes + 2;                                                  // [2]
+  uint64_t* bar_rec = reinterpret_cast<uint64_t*>(smem + L::off_bars(a.ent_cap, a.stage_cap));  // [NS]
+  uint64_t* bar_ent = bar_rec + NS;                                                            // [2]
+  uint64_t* bar_meta = bar_ent + 2;                                                            // [1]
+  const int meta_rows = L::meta_rows(a.stage_cap);
   __shared__ int s_block;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -467,17 +482,14 @@ __global__ void __launch_bounds__(kThreads, MODE == kDW ? 1 : 2) k_assemble(AsmA
   for (int i = tid; i < 7 * NU; i += kThreads) tab[i] = A::from(a.tables[i]);
   if (tid == 0) {
     buf[NU * CI] = A::zero();
-    mbar_init(&bar_nodes[0], 1);
-    mbar_init(&bar_nodes[1], 1);
-    mbar_init(&bar_ent[0], 1);
-    mbar_init(&bar_ent[1], 1);
+    for (int k = 0; k < L::kBars; ++k) mbar_init(&bar_rec[k], 1);
     mbar_fence_init();
   }
   __syncthreads();
   const T wsum = A::from(a.wsum);
-  // bit st of ph_nodes / ph_ent: parity of the next completion of stage st's
-  // barrier; bit st of pend_nodes / pend_ent: a copy into stage st is in flight
-  uint32_t ph_nodes = 0, ph_ent = 0, pend_nodes = 0, pend_ent = 0;
+  // bit k of ph_*: parity of the next completion of barrier k; bit k of
+  // pend_*: a copy onto barrier k is in flight (the same in every thread)
+  uint32_t ph_rec = 0, ph_ent = 0, ph_meta = 0, pend_rec = 0, pend_ent = 0, pend_meta = 0;
   bool failed = false;
 
   for (;;) {
@@ -488,90 +500,94 @@ __global__ void __launch_bounds__(kThreads, MODE == kDW ? 1 : 2) k_assemble(AsmA
     if (b >= a.nblocks) break;
     const BlockDesc d = a.blocks[b];
 
-    auto issue_nodes = [&](int c) {
-      const int st = c & 1;
-      const int n = min(CI, d.item_count - c * CI), n4 = (n + 3) & ~3;
-      const int64_t first = (int64_t)d.item_begin + (int64_t)c * CI;
-      mbar_expect_tx(&bar_nodes[st], (uint32_t)(n4 * 20 + sizeof(ChunkDesc)));
-      bulk_g2s(sconn + st * CI, a.item_conn + first, (uint32_t)(n4 * 16), &bar_nodes[st]);
-      bulk_g2s(sids + st * CI, a.items + first, (uint32_t)(n4 * 4), &bar_nodes[st]);
-      bulk_g2s(sdesc + st, a.chunks + d.chunk_begin + c, (uint32_t)sizeof(ChunkDesc), &bar_nodes[st]);
+    auto stage_of = [&](int c) { return stage + (c % NS) * sbytes; };
+    auto desc_of = [&](int c) { return reinterpret_cast<const ChunkDesc*>(stage_of(c)); };
+    auto items_in = [&](int c) { return (min(CI, d.item_count - c * CI) + 3) & ~3; };
+    // thread 0 only
+    auto issue_rec = [&](int c, int off16, int bytes) {
+      uint64_t* bar = &bar_rec[c % NS];
+      mbar_expect_tx(bar, (uint32_t)bytes);
+      bulk_g2s(stage_of(c), a.chunk_data + (int64_t)off16 * 16, (uint32_t)bytes, bar);
     };
-    // needs the staged descriptor of chunk c (stage c & 1)
-    auto issue_entries = [&](int c) {
-      const int st = c & 1;
-      const ChunkDesc& cd = sdesc[st];
+    auto issue_entries = [&](int c) {  // needs record c staged
+      const ChunkDesc& cd = *desc_of(c);
       const uint32_t bytes = (uint32_t)cd.warp_off[kWarps] * 4u;
-      mbar_expect_tx(&bar_ent[st], bytes);
-      if (bytes) bulk_g2s(sent + st * went, a.entries + cd.word_begin, bytes, &bar_ent[st]);
+      mbar_expect_tx(&bar_ent[c & 1], bytes);
+      if (bytes) bulk_g2s(sent + (c & 1) * went, a.entries + cd.word_begin, bytes, &bar_ent[c & 1]);
     };
-    // waits on a stage barrier; false (uniformly) when the wait gave up
-    auto wait_nodes = [&](int c) -> bool {
-      const int st = c & 1;
-      const bool ok = mbar_wait(&bar_nodes[st], (ph_nodes >> st) & 1u);
+    auto issue_meta = [&](int r0) {  // rows r0 .. r0 + nr (+ one) of the block, 16-byte aligned
+      const int nr = min(meta_rows, d.row_count - r0);
+      const int g0 = d.row_begin + r0, i0 = g0 & ~1, i1 = (g0 + nr + 2) & ~1;
+      mbar_expect_tx(bar_meta, (uint32_t)(i1 - i0) * 8u);
+      bulk_g2s(stage, a.row_meta + i0, (uint32_t)(i1 - i0) * 8u, bar_meta);
+    };
+    // waits on a barrier; false (uniformly) when the wait gave up
+    auto wait_bar = [&](uint64_t* bar, uint32_t& ph, uint32_t& pend, int k) -> bool {
+      const bool ok = mbar_wait(bar, (ph >> k) & 1u);
       if (__syncthreads_or(!ok)) return false;
-      ph_nodes ^= 1u << st;
-      pend_nodes &= ~(1u << st);
+      ph ^= 1u << k;
+      pend &= ~(1u << k);
       return true;
     };
-    // loads the coordinates and coefficient of this thread's item of chunk c
-    auto prefetch = [&](int c, Fetch<MODE>& F) -> bool {
-      const int it = c * CI + local;
-      if (it >= d.item_count) return false;
-      const int st = c & 1;
-      const int e = sids[st * CI + local];
-      fetch(a.geo, sconn[st * CI + local], F);
-      F.coef = a.coeff ? __ldg(a.coeff + e) : a.cconst;
+    // coefficient of this thread's item of chunk c (record c staged)
+    auto load_coef = [&](int c, double& coef) -> bool {
+      if (c * CI + local >= d.item_count) return false;
+      const int e = reinterpret_cast<const int32_t*>(stage_of(c) + sizeof(ChunkDesc))[local];
+      coef = a.coeff ? __ldg(a.coeff + e) : a.cconst;
       return true;
     };
 
     for (int i = tid; i < kAccMax; i += kThreads) acc[i] = A::zero();
-    if (tid == 0 && d.nchunks > 0) {
+    const int npro = min(NS, d.nchunks);
+    if (tid == 0 && npro > 0) {
+      int2 r[NS];
+      for (int c = 0; c < npro; ++c) r[c] = a.chunk_rec[d.chunk_begin + c];
       fence_proxy_async();
-      issue_nodes(0);
-      if (d.nchunks > 1) issue_nodes(1);
+      for (int c = 0; c < npro; ++c) issue_rec(c, r[c].x, r[c].y);
     }
-    pend_nodes = (d.nchunks > 0 ? 1u : 0u) | (d.nchunks > 1 ? 2u : 0u);
+    pend_rec |= (1u << npro) - 1u;
 
-    Fetch<MODE> R, P;
+    double coef_r = 0.0, coef_p = 0.0;
     bool have_r = false, have_p = false;
     int w_beg = 0, w_end = 0, nw_beg = 0, nw_end = 0;  // this warp's word range of chunks c and c + 1
     if (d.nchunks > 0) {
-      if (!wait_nodes(0)) { failed = true; break; }
-      if (tid == 0) issue_entries(0);
-      pend_ent |= 1u;
-      nw_beg = sdesc[0].warp_off[warp];
-      nw_end = sdesc[0].warp_off[warp + 1];
-      have_r = prefetch(0, R);
-      __syncthreads();  // stage 0 has been read: refill it with chunk 2
-      if (d.nchunks > 2) {
-        if (tid == 0) {
-          fence_proxy_async();
-          issue_nodes(2);
-        }
-        pend_nodes |= 1u;
+      if (!wait_bar(&bar_rec[0], ph_rec, pend_rec, 0)) { failed = true; break; }
+      if (tid == 0) {
+        fence_proxy_async();
+        issue_entries(0);
       }
+      pend_ent |= 1u;
+      nw_beg = desc_of(0)->warp_off[warp];
+      nw_end = desc_of(0)->warp_off[warp + 1];
+      have_r = load_coef(0, coef_r);
     }
     for (int c = 0; c < d.nchunks; ++c) {
       w_beg = nw_beg;
       w_end = nw_end;
       if (c + 1 < d.nchunks) {
-        if (!wait_nodes(c + 1)) { failed = true; break; }
+        if (!wait_bar(&bar_rec[(c + 1) % NS], ph_rec, pend_rec, (c + 1) % NS)) { failed = true; break; }
         // word buffer (c + 1) & 1 was released by the barrier that ended chunk c - 1
         if (tid == 0) {
           fence_proxy_async();
           issue_entries(c + 1);
         }
         pend_ent |= 1u << ((c + 1) & 1);
-        nw_beg = sdesc[(c + 1) & 1].warp_off[warp];
-        nw_end = sdesc[(c + 1) & 1].warp_off[warp + 1];
-        have_p = prefetch(c + 1, P);
+        nw_beg = desc_of(c + 1)->warp_off[warp];
+        nw_end = desc_of(c + 1)->warp_off[warp + 1];
+        have_p = load_coef(c + 1, coef_p);
       }
-      // ---- phase 1: element matrices of chunk c
+      // ---- phase 1: element matrices of chunk c from its staged record
       if (have_r) {
-        const T coef = A::from(R.coef);
+        const unsigned char* rb = stage_of(c);
+        const int n4 = items_in(c), nn = desc_of(c)->n_nodes;
+        const ushort4 lc = reinterpret_cast<const ushort4*>(rb + sizeof(ChunkDesc) + 4 * n4)[local];
+        const float4* vrec = reinterpret_cast<const float4*>(rb + sizeof(ChunkDesc) + 12 * n4);
+        const float* vloz = reinterpret_cast<const float*>(rb + sizeof(ChunkDesc) + 12 * n4 + 32 * nn);
+        Fetch<MODE> F;
+        fetch_staged(vrec, vloz, lc, F);
+        const T coef = A::from(coef_r);
         Cof<T> f;
-        geometry(a.geo, R, f);
+        geometry(F, f);
         if (ORDER == 1) {
           T K[10];
           if (a.stiff) {
@@ -598,20 +614,24 @@ __global__ void __launch_bounds__(kThreads, MODE == kDW ? 1 : 2) k_assemble(AsmA
         }
       }
       __syncthreads();
-      // stage (c + 1) & 1 was read at the top of this chunk: refill it with chunk c + 3
-      if (tid == 0 && c + 3 < d.nchunks) {
-        fence_proxy_async();
-        issue_nodes(c + 3);
+      if (c + NS < d.nchunks) {
+        // record c has been read: bring record c + 3 into its stage
+        if (tid == 0) {
+          const int off16 = desc_of(c)->next_off16, bytes = desc_of(c)->next_bytes;
+          fence_proxy_async();
+          issue_rec(c + NS, off16, bytes);
+        }
+        pend_rec |= 1u << (c % NS);
+      } else if (c == d.nchunks - 1) {
+        // every record has been read: the stage area takes the row metadata
+        if (tid == 0) {
+          fence_proxy_async();
+          issue_meta(0);
+        }
+        pend_meta = 1u;
       }
-      if (c + 3 < d.nchunks) pend_nodes |= 1u << ((c + 1) & 1);
       // ---- phase 2: segmented sums into owned slots
-      {
-        const int st = c & 1;
-        const bool ok = mbar_wait(&bar_ent[st], (ph_ent >> st) & 1u);
-        if (__syncthreads_or(!ok)) { failed = true; break; }
-        ph_ent ^= 1u << st;
-        pend_ent &= ~(1u << st);
-      }
+      if (!wait_bar(&bar_ent[c & 1], ph_ent, pend_ent, c & 1)) { failed = true; break; }
       {
         // pieces of PW words of one slot: summed in registers, one update of
         // the slot per piece; within a chunk every slot belongs to one thread
@@ -636,37 +656,58 @@ __global__ void __launch_bounds__(kThreads, MODE == kDW ? 1 : 2) k_assemble(AsmA
         }
       }
       __syncthreads();
-      R = P;
+      coef_r = coef_p;
       have_r = have_p;
       have_p = false;
     }
     if (failed) break;
-    // ---- write the owned rows, kRowBatch at a time: their CSR starts and
-    // accumulator bases are loaded in parallel, then one warp per row stores
-    // the row's contiguous range
+    // ---- write the owned rows, one batch of row metadata at a time.  A warp
+    // takes 32 consecutive rows (their slots are contiguous in acc); each lane
+    // takes one slot per pass, finds its row by a binary search over the
+    // lanes' row bases (shuffles) and stores to CSR start + offset.
     using Out = typename A::Out;
     Out* out = reinterpret_cast<Out*>(a.values);
-    for (int r0 = 0; r0 < d.row_count; r0 += L::kRowBatch) {
-      const int nr = min(L::kRowBatch, d.row_count - r0);
-      if (tid < nr) {
-        s_rcsr[tid] = a.row_csr[d.row_begin + r0 + tid];
-        s_racc[tid] = a.row_acc[d.row_begin + r0 + tid];
+    for (int r0 = 0; r0 < d.row_count; r0 += meta_rows) {
+      if (r0 > 0 || d.nchunks == 0) {
+        if (tid == 0) {
+          fence_proxy_async();
+          issue_meta(r0);
+        }
+        pend_meta = 1u;
       }
-      if (tid == 0) s_racc[nr] = (r0 + nr < d.row_count) ? a.row_acc[d.row_begin + r0 + nr] : d.acc_used;
-      __syncthreads();
-      for (int r = warp; r < nr; r += kWarps) {
-        const int s0 = s_rcsr[r], a0 = s_racc[r], len = s_racc[r + 1] - a0;
-        for (int k = lane; k < len; k += 32) out[s0 + k] = A::out(acc[a0 + k]);
+      if (!wait_bar(bar_meta, ph_meta, pend_meta, 0)) { failed = true; break; }
+      const int nr = min(meta_rows, d.row_count - r0);
+      const int m0 = (d.row_begin + r0) & 1;  // smeta[m0 + j] is row r0 + j
+      const int bend = (r0 + nr < d.row_count) ? smeta[m0 + nr].x : d.acc_used;
+      for (int t0 = 32 * warp; t0 < nr; t0 += 32 * kWarps) {
+        const int nrow = min(32, nr - t0);
+        int2 m = make_int2(0x7fffffff, 0);
+        if (lane < nrow) m = smeta[m0 + t0 + lane];
+        const int A0 = __shfl_sync(0xffffffffu, m.x, 0);
+        const int A1 = (t0 + 32 < nr) ? smeta[m0 + t0 + 32].x : bend;
+        for (int k0 = A0; k0 < A1; k0 += 32) {
+          const int k = k0 + lane;
+          int lo = 0;  // last row j (< nrow) with base_j <= k
+#pragma unroll
+          for (int s = 16; s >= 1; s >>= 1) {
+            const int v = __shfl_sync(0xffffffffu, m.x, (lo + s) & 31);
+            if (lo + s < nrow && v <= k) lo += s;
+          }
+          const int off = __shfl_sync(0xffffffffu, m.y, lo);
+          if (k < A1) out[k + off] = A::out(acc[k]);
+        }
       }
       __syncthreads();
     }
+    if (failed) break;
   }
   if (failed) {
     // let copies still in flight land before the CTA's shared memory goes away
-    for (int st = 0; st < 2; ++st)
-      if ((pend_nodes >> st) & 1u) mbar_wait(&bar_nodes[st], (ph_nodes >> st) & 1u);
+    for (int st = 0; st < NS; ++st)
+      if ((pend_rec >> st) & 1u) mbar_wait(&bar_rec[st], (ph_rec >> st) & 1u);
     for (int st = 0; st < 2; ++st)
       if ((pend_ent >> st) & 1u) mbar_wait(&bar_ent[st], (ph_ent >> st) & 1u);
+    if (pend_meta & 1u) mbar_wait(bar_meta, ph_meta & 1u);
     if (tid == 0) {
       atomicExch(&a.counters[2], (uint32_t)kDevErrTimeout);
       atomicExch(&a.counters[3], (uint32_t)blockIdx.x);
@@ -686,7 +727,9 @@ __global__ void __launch_bounds__(kThreads, MODE == kDW ? 1 : 2) k_assemble(AsmA
 template <int ORDER, int MODE>
 static mg_status launch_assemble_t(AsmArgs a, cudaStream_t st)
 {
-  const size_t smem = AsmLayout<ORDER, MODE>::total(a.ent_cap);
+  using L = AsmLayout<ORDER, MODE>;
+  const size_t smem = L::total(a.ent_cap, a.stage_cap);
+  if (L::meta_rows(a.stage_cap) < 32) return set_error(MG_ERR_SIZE, "assembly stage too small for row metadata");
   static size_t configured = 0;
   static int per_sm = 0, sms = 0;
   if (configured != smem) {
@@ -732,13 +775,10 @@ mg_status launch_assemble(mg_plan* p, int op, const double* d_coeff, double c, i
   mg_mesh* m = p->mesh;
   AsmArgs a;
   a.blocks = p->d_blocks;
-  a.items = p->d_items;
-  a.item_conn = p->d_item_conn;
-  a.chunks = p->d_chunks;
+  a.chunk_data = p->d_chunk_data;
+  a.chunk_rec = p->d_chunk_rec;
   a.entries = p->d_entries;
-  a.row_csr = p->d_row_csr;
-  a.row_acc = p->d_row_acc;
-  a.geo = GeoPtrs{m->d_xyz, m->d_node_rec, m->d_lo_z};
+  a.row_meta = p->d_row_meta;
   a.coeff = needs_coeff ? d_coeff : nullptr;
   a.cconst = op == MG_OP_STIFF_CONST ? c : 1.0;
   a.tables = d_tab;
@@ -748,6 +788,7 @@ mg_status launch_assemble(mg_plan* p, int op, const double* d_coeff, double c, i
   a.nblocks = p->nblocks;
   a.stiff = (op == MG_OP_STIFF_KAPPA || op == MG_OP_STIFF_CONST);
   a.ent_cap = (int)((p->max_chunk_entries + 3) / 4 * 4);
+  a.stage_cap = std::max(p->max_rec_bytes, 64);
   if (m->order == 1) {
     if (prec == MG_F32) return launch_assemble_t<1, kF32>(a, st);
     return native_f64() ? launch_assemble_t<1, kF64>(a, st) : launch_assemble_t<1, kDW>(a, st);

@@ -73,12 +73,19 @@ struct BlockDesc {
   int32_t word_begin32; // first contribution word of the block / 32
 };
 
-// Contribution words of one chunk: a 64-byte record the kernel stages into
-// shared memory with the chunk's element nodes.
+// Head of a chunk record.  The plan lays out, per chunk, one contiguous record
+// the kernel stages into shared memory with a single bulk copy:
+//   ChunkDesc (64 B) | element ids (4 B x n4) | local vertex indices (4 x 2 B x n4)
+//   | vertex records (2 float4 x nn: hi.xyz mid.x, mid.yz lo.xy) | lo.z (4 B x nn)
+// n4 = the chunk's items rounded up to 4, nn = n_nodes (a multiple of 4), so
+// every part starts on a 16-byte boundary.
 struct ChunkDesc {
-  int64_t word_begin;         // first word of the chunk in entries[] (multiple of 32)
+  int64_t word_begin;         // first contribution word of the chunk (multiple of 32)
   int32_t warp_off[kWarps + 1];  // per-warp offsets relative to word_begin; [kWarps] = chunk size
-  int32_t pad[5];
+  int32_t n_nodes;            // distinct vertices of the chunk's elements (multiple of 4)
+  int32_t next_off16;         // record of chunk + 3 of the same block: offset / 16
+  int32_t next_bytes;         //   and size (0 when the block has no such chunk)
+  int32_t pad[2];
 };
 static_assert(sizeof(ChunkDesc) == 64, "ChunkDesc must stay 64 bytes");
 
@@ -134,14 +141,12 @@ struct mg_plan {
   int32_t nblocks = 0;
   int64_t n_items = 0, n_item_slots = 0, n_chunks = 0, n_entries = 0, n_contrib = 0;
   mg::BlockDesc* d_blocks = nullptr;
-  int32_t* d_items = nullptr;
-  int64_t* d_chunk_ptr = nullptr;  // (kWarps + 1) per chunk, offsets into entries
-  mg::ChunkDesc* d_chunks = nullptr;  // the same offsets as 64-byte records
-  int32_t* d_row_csr = nullptr;       // CSR start of each owned row (schedule order)
-  uint32_t* d_entries = nullptr;   // (slot / kThreads) << 16 | source index
-  int32_t* d_rows = nullptr;
-  int32_t* d_row_acc = nullptr;
-  int4* d_item_conn = nullptr;      // vertex nodes of each item, schedule order
+  unsigned char* d_chunk_data = nullptr;  // chunk records (see ChunkDesc), 16-byte aligned
+  int2* d_chunk_rec = nullptr;            // (offset / 16, bytes) of each chunk record
+  int32_t max_rec_bytes = 0;
+  int32_t max_chunk_nodes = 0;
+  int2* d_row_meta = nullptr;  // owned rows, schedule order: (accumulator base, CSR start - base)
+  uint32_t* d_entries = nullptr;   // contribution words
   uint32_t* d_counters = nullptr;   // [0] work counter, [1] exit counter, [2] device error, [3] detail
   int64_t max_chunk_entries = 0;
   // reference tables, cached per (quad) on the device
@@ -169,6 +174,12 @@ struct HostSchedule {
   std::vector<uint32_t> entries;
   int64_t n_contrib = 0;
   int64_t max_chunk_entries = 0;
+  // per chunk: its distinct vertices (first-appearance order, padded to 4) and,
+  // per item, the local indices of the item's four vertices
+  std::vector<int32_t> chunk_node_begin, chunk_n_nodes;
+  std::vector<int32_t> chunk_nodes;  // global node ids
+  std::vector<uint16_t> item_lconn;  // 4 per item slot
+  int32_t max_chunk_nodes = 0;
 };
 mg_status mesh_device(mg_mesh* m);  // uploads the mesh on first GPU use
 mg_status plan_device(mg_plan* p);  // uploads mesh + plan on first GPU use

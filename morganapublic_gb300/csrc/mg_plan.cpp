@@ -234,6 +234,66 @@ static mg_status build_schedule(mg_plan* p, HostSchedule* hs)
     d.nchunks = (d.item_count + CI - 1) / CI;
     nchunk_tot += d.nchunks;
   }
+  // chunk vertex tables: the distinct vertices of each chunk's elements in
+  // first-appearance order (padded to a multiple of 4 with the chunk's first
+  // vertex) and each item's local vertex indices
+  {
+    hs->chunk_node_begin.assign(nchunk_tot, 0);
+    hs->chunk_n_nodes.assign(nchunk_tot, 0);
+    hs->item_lconn.assign(hs->items.size() * 4, 0);
+    std::vector<std::vector<int32_t>> cn(nchunk_tot);
+    int32_t maxn = 0;
+#pragma omp parallel reduction(max : maxn)
+    {
+      std::vector<int32_t> stamp(N, -1), local(N, 0);
+#pragma omp for schedule(dynamic, 4)
+      for (int32_t b = 0; b < nbk; ++b) {
+        const BlockDesc& d = hs->blocks[b];
+        for (int32_t c = 0; c < d.nchunks; ++c) {
+          const int32_t ck = d.chunk_begin + c;
+          auto& v = cn[ck];
+          const int32_t i0 = c * CI, i1 = std::min(d.item_count, i0 + CI);
+          for (int32_t it = i0; it < i1; ++it) {
+            const int64_t slot = (int64_t)d.item_begin + it;
+            const int64_t e = hs->items[slot];
+            for (int k = 0; k < 4; ++k) {
+              const int32_t nd = m->conn[4 * e + k];
+              if (stamp[nd] != ck) {
+                stamp[nd] = ck;
+                local[nd] = (int32_t)v.size();
+                v.push_back(nd);
+              }
+              hs->item_lconn[4 * slot + k] = (uint16_t)local[nd];
+            }
+          }
+          while (v.size() % 4) v.push_back(v.empty() ? 0 : v[0]);
+          maxn = std::max(maxn, (int32_t)v.size());
+        }
+      }
+    }
+    if (maxn > 65535) return set_error(MG_ERR_SIZE, "a chunk touches more than 65535 vertices");
+    int64_t tot = 0;
+    for (int64_t ck = 0; ck < nchunk_tot; ++ck) {
+      if (tot >= INT32_MAX) return set_error(MG_ERR_SIZE, "chunk vertex records above 2^31-1");
+      hs->chunk_node_begin[ck] = (int32_t)tot;
+      hs->chunk_n_nodes[ck] = (int32_t)cn[ck].size();
+      tot += (int64_t)cn[ck].size();
+    }
+    hs->chunk_nodes.resize(tot);
+    for (int64_t ck = 0; ck < nchunk_tot; ++ck)
+      std::copy(cn[ck].begin(), cn[ck].end(), hs->chunk_nodes.begin() + hs->chunk_node_begin[ck]);
+    hs->max_chunk_nodes = maxn;
+    p->max_chunk_nodes = maxn;
+    // largest chunk record (layout at ChunkDesc)
+    int64_t maxb = 0;
+    for (int32_t b = 0; b < nbk; ++b)
+      for (int32_t c = 0; c < hs->blocks[b].nchunks; ++c) {
+        const int64_t n4 = (std::min(CI, hs->blocks[b].item_count - c * CI) + 3) & ~3;
+        maxb = std::max(maxb, (int64_t)sizeof(ChunkDesc) + 12 * n4 + 36 * (int64_t)hs->chunk_n_nodes[hs->blocks[b].chunk_begin + c]);
+      }
+    if (maxb >= INT32_MAX) return set_error(MG_ERR_SIZE, "chunk record above 2 GiB");
+    p->max_rec_bytes = (int32_t)maxb;
+  }
   // contribution lists, per block in parallel, then concatenated
   const int nu = nunique(m->order);
   const uint32_t zero_src = (uint32_t)(nu * CI);
@@ -390,34 +450,83 @@ mg_status plan_device(mg_plan* p)
   }
   MG_TRY(upload(&p->d_diag, diag));
   MG_TRY(upload(&p->d_blocks, hs.blocks));
-  MG_TRY(upload(&p->d_items, hs.items));
-  MG_TRY(upload(&p->d_chunk_ptr, hs.chunk_ptr));
-  {
-    const int64_t nc = (int64_t)hs.chunk_ptr.size() / (kWarps + 1);
-    std::vector<ChunkDesc> cd(nc);
-    for (int64_t c = 0; c < nc; ++c) {
-      const int64_t* cp = &hs.chunk_ptr[c * (kWarps + 1)];
-      cd[c].word_begin = cp[0];
-      for (int w = 0; w <= kWarps; ++w) cd[c].warp_off[w] = (int32_t)(cp[w] - cp[0]);
-      for (int k = 0; k < 5; ++k) cd[c].pad[k] = 0;
-    }
-    MG_TRY(upload(&p->d_chunks, cd));
-    std::vector<int32_t> rc(hs.rows.size());
-    for (size_t k = 0; k < hs.rows.size(); ++k) rc[k] = p->rowptr[hs.rows[k]];
-    MG_TRY(upload(&p->d_row_csr, rc));
-  }
   MG_TRY(upload(&p->d_entries, hs.entries));
-  MG_TRY(upload(&p->d_rows, hs.rows));
-  MG_TRY(upload(&p->d_row_acc, hs.row_acc));
   {
-    std::vector<int4> ic(hs.items.size());
-    for (size_t k = 0; k < hs.items.size(); ++k) {
-      const int32_t e = hs.items[k];
-      ic[k] = e < 0 ? make_int4(0, 0, 0, 0)
-                    : make_int4(p->mesh->conn[4 * (int64_t)e], p->mesh->conn[4 * (int64_t)e + 1],
-                                p->mesh->conn[4 * (int64_t)e + 2], p->mesh->conn[4 * (int64_t)e + 3]);
+    // owned-row metadata in schedule order, padded by two entries so that the
+    // kernel's 16-byte aligned copies of a row range stay inside the array
+    std::vector<int2> meta(hs.rows.size() + 2, make_int2(0, 0));
+    for (size_t k = 0; k < hs.rows.size(); ++k)
+      meta[k] = make_int2(hs.row_acc[k], p->rowptr[hs.rows[k]] - hs.row_acc[k]);
+    MG_TRY(upload(&p->d_row_meta, meta));
+  }
+  {
+    // chunk records (layout at ChunkDesc): sizes, offsets, then the contents
+    const int CI = chunk_items(p->mesh->order);
+    const int64_t nc = (int64_t)hs.chunk_ptr.size() / (kWarps + 1);
+    std::vector<int32_t> blk(nc), pos(nc);  // owning block, chunk index within it
+    for (size_t b = 0; b < hs.blocks.size(); ++b)
+      for (int32_t c = 0; c < hs.blocks[b].nchunks; ++c) {
+        blk[hs.blocks[b].chunk_begin + c] = (int32_t)b;
+        pos[hs.blocks[b].chunk_begin + c] = c;
+      }
+    auto n_items = [&](int64_t ck) {
+      const BlockDesc& d = hs.blocks[blk[ck]];
+      return std::min(CI, d.item_count - pos[ck] * CI);
+    };
+    std::vector<int2> rec(nc);
+    std::vector<int64_t> off(nc + 1, 0);
+    int64_t maxb = 0;
+    for (int64_t ck = 0; ck < nc; ++ck) {
+      const int64_t n4 = (n_items(ck) + 3) & ~3, nn = hs.chunk_n_nodes[ck];
+      const int64_t bytes = (int64_t)sizeof(ChunkDesc) + 12 * n4 + 36 * nn;
+      off[ck + 1] = off[ck] + bytes;
+      maxb = std::max(maxb, bytes);
     }
-    MG_TRY(upload(&p->d_item_conn, ic));
+    if (off[nc] / 16 >= INT32_MAX || maxb >= INT32_MAX)
+      return set_error(MG_ERR_SIZE, "chunk records above 32 GiB");
+    for (int64_t ck = 0; ck < nc; ++ck) rec[ck] = make_int2((int32_t)(off[ck] / 16), (int32_t)(off[ck + 1] - off[ck]));
+    std::vector<unsigned char> data(std::max<int64_t>(off[nc], 16), 0);
+    const std::vector<double>& xyz = p->mesh->xyz;
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t ck = 0; ck < nc; ++ck) {
+      unsigned char* r = data.data() + off[ck];
+      const BlockDesc& d = hs.blocks[blk[ck]];
+      const int32_t c = pos[ck];
+      const int64_t n4 = (n_items(ck) + 3) & ~3, nn = hs.chunk_n_nodes[ck];
+      ChunkDesc cd{};
+      const int64_t* cp = &hs.chunk_ptr[ck * (kWarps + 1)];
+      cd.word_begin = cp[0];
+      for (int w = 0; w <= kWarps; ++w) cd.warp_off[w] = (int32_t)(cp[w] - cp[0]);
+      cd.n_nodes = (int32_t)nn;
+      if (c + 3 < d.nchunks) {
+        cd.next_off16 = rec[ck + 3].x;
+        cd.next_bytes = rec[ck + 3].y;
+      }
+      std::memcpy(r, &cd, sizeof cd);
+      const int64_t first = (int64_t)d.item_begin + (int64_t)c * CI;
+      std::memcpy(r + 64, &hs.items[first], 4 * n4);
+      std::memcpy(r + 64 + 4 * n4, &hs.item_lconn[4 * first], 8 * n4);
+      float4* vr = reinterpret_cast<float4*>(r + 64 + 12 * n4);
+      float* vz = reinterpret_cast<float*>(r + 64 + 12 * n4 + 32 * nn);
+      for (int64_t i = 0; i < nn; ++i) {
+        // x = hi + mid + lo exactly: hi = fl(x), mid = fl(x - hi), lo = fl(x - hi - mid)
+        const int64_t nd = hs.chunk_nodes[hs.chunk_node_begin[ck] + i];
+        float h[3], md[3], l[3];
+        for (int k = 0; k < 3; ++k) {
+          const double x = xyz[3 * nd + k];
+          h[k] = (float)x;
+          const double r1 = x - (double)h[k];
+          md[k] = (float)r1;
+          l[k] = (float)(r1 - (double)md[k]);
+        }
+        vr[2 * i] = make_float4(h[0], h[1], h[2], md[0]);
+        vr[2 * i + 1] = make_float4(md[1], md[2], l[0], l[1]);
+        vz[i] = l[2];
+      }
+    }
+    MG_TRY(upload(&p->d_chunk_data, data));
+    MG_TRY(upload(&p->d_chunk_rec, rec));
+    if (maxb != p->max_rec_bytes) return set_error(MG_ERR_SIZE, "chunk record size mismatch");
   }
   MG_TRY(upload(&p->d_counters, std::vector<uint32_t>(8, 0u)));
   MG_CUDA(cudaMallocHost(&p->h_pinned, 64 * sizeof(double)));
@@ -434,14 +543,10 @@ static void free_plan(mg_plan* p)
   cudaFree(p->d_colind);
   cudaFree(p->d_diag);
   cudaFree(p->d_blocks);
-  cudaFree(p->d_items);
-  cudaFree(p->d_chunk_ptr);
-  cudaFree(p->d_chunks);
-  cudaFree(p->d_row_csr);
+  cudaFree(p->d_chunk_data);
+  cudaFree(p->d_chunk_rec);
+  cudaFree(p->d_row_meta);
   cudaFree(p->d_entries);
-  cudaFree(p->d_rows);
-  cudaFree(p->d_row_acc);
-  cudaFree(p->d_item_conn);
   cudaFree(p->d_counters);
   for (double* t : p->d_tables) cudaFree(t);
   cudaFree(p->d_work);
@@ -564,6 +669,8 @@ mg_status mg_plan_schedule_info(const mg_plan* p, mg_schedule_info* info)
   info->n_contrib = p->n_contrib;
   info->n_item_slots = p->n_item_slots;
   info->max_chunk_entries = p->max_chunk_entries;
+  info->max_chunk_vertices = p->max_chunk_nodes;
+  info->max_chunk_record_bytes = p->max_rec_bytes;
   return MG_OK;
 }
 
