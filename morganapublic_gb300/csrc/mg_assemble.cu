@@ -72,7 +72,7 @@ template <> struct Arith<kDW> {
   using Out = double;
   __device__ static T from(double x) { return ff_from_double_bits(x); }
   __device__ static T zero() { return ff{0.0f, 0.0f}; }
-  __device__ static Out out(T v) { return ff_to_double(v); }
+  __device__ static Out out(T v) { return ff_to_double_bits(v); }
 };
 template <> struct Arith<kF64> {
   using T = double;
@@ -405,6 +405,28 @@ struct AsmArgs {
 
 constexpr size_t align16(size_t n) { return (n + 15) / 16 * 16; }
 
+// Barriers of k_assemble (mbarriers in shared memory).  "full" barriers complete
+// when a bulk copy has landed (producer arrival + transaction bytes); "empty"
+// barriers when the consumers have finished with a buffer; the two token
+// barriers hand the right to update the accumulators from one consumer group
+// to the other.
+enum {
+  kBarRecFull = 0,                        // [kRecStages] chunk-record stages
+  kBarRecEmpty = kBarRecFull + kRecStages,  // [kRecStages]
+  kBarEntFull = kBarRecEmpty + kRecStages,  // [2] contribution-word buffers (one per group)
+  kBarEntEmpty = kBarEntFull + 2,           // [2]
+  kBarMetaFull = kBarEntEmpty + 2,          // row metadata of a block
+  kBarMetaEmpty = kBarMetaFull + 1,
+  kBarBlkFull = kBarMetaEmpty + 1,          // [2] block descriptors
+  kBarBlkEmpty = kBarBlkFull + 2,           // [2]
+  kBarToken = kBarBlkEmpty + 2,             // [2] group g may run phase 2
+  kNumBars = kBarToken + 2
+};
+
+constexpr int kGroups = 2;                          // consumer groups of kThreads threads
+constexpr int kConsumers = kGroups * kThreads;
+constexpr int kAsmThreads = kConsumers + 32;        // + the producer warp
+
 // Shared-memory layout of k_assemble.  Every region starts on a 16-byte
 // boundary: the bulk copies (chunk records, contribution words, row metadata)
 // require 16-byte aligned destinations, the mbarriers 8-byte.
@@ -414,304 +436,334 @@ struct AsmLayout {
   static constexpr int NB = ORDER == 1 ? 4 : 10;
   static constexpr int NU = ORDER == 1 ? 10 : 55;
   static constexpr int CI = ORDER == 1 ? kChunkP1 : kChunkP2;
-  static constexpr int kStages = 3;  // chunk-record stages
-  static constexpr int kBars = kStages + 2 + 1;  // records, words, row metadata
   static constexpr size_t acc_bytes = align16(sizeof(T) * (kAccMax + 1));  // + the padding words' dummy slot
-  static constexpr size_t buf_bytes = align16(sizeof(T) * (NU * CI + 1));
+  static constexpr size_t buf_bytes = align16(sizeof(T) * (NU * CI + 1));  // per group, + the zero source
   static constexpr size_t tab_bytes = align16(sizeof(T) * 7 * NU);
+  // an aligned copy of a block's rows (and the row after) spans at most kRowsMax + 3 entries
+  static constexpr size_t meta_bytes = align16(8 * (kRowsMax + 4));
+  static constexpr size_t blk_bytes = 2 * sizeof(BlockDesc);
   static constexpr size_t off_buf = acc_bytes;
-  static constexpr size_t off_tab = off_buf + buf_bytes;
-  static constexpr size_t off_stage = off_tab + tab_bytes;
-  static_assert(off_buf % 16 == 0 && off_tab % 16 == 0 && off_stage % 16 == 0,
+  static constexpr size_t off_tab = off_buf + kGroups * buf_bytes;
+  static constexpr size_t off_meta = off_tab + tab_bytes;
+  static constexpr size_t off_blk = off_meta + meta_bytes;
+  static constexpr size_t off_bars = off_blk + blk_bytes;
+  static constexpr size_t off_stage = off_bars + align16(8 * kNumBars);
+  static_assert(off_buf % 16 == 0 && off_tab % 16 == 0 && off_meta % 16 == 0 && off_blk % 16 == 0 &&
+                    off_bars % 16 == 0 && off_stage % 16 == 0 && buf_bytes % 16 == 0,
                 "shared-memory regions must start on 16-byte boundaries");
   __host__ __device__ static size_t stage_bytes(int stage_cap) { return ((size_t)stage_cap + 15) / 16 * 16; }
   __host__ __device__ static size_t words_bytes(int ent_cap) { return ((size_t)ent_cap * 4 + 15) / 16 * 16; }
-  __host__ __device__ static size_t off_words(int stage_cap) { return off_stage + kStages * stage_bytes(stage_cap); }
-  __host__ __device__ static size_t off_bars(int ent_cap, int stage_cap)
+  __host__ __device__ static size_t off_words(int stage_cap) { return off_stage + kRecStages * stage_bytes(stage_cap); }
+  __host__ __device__ static size_t total(int ent_cap, int stage_cap)
   {
     return off_words(stage_cap) + 2 * words_bytes(ent_cap);
   }
-  __host__ __device__ static size_t total(int ent_cap, int stage_cap) { return off_bars(ent_cap, stage_cap) + 8 * kBars; }
-  // owned rows per write-out batch: the row metadata reuses the stage area
-  // (an aligned copy of nr rows spans at most nr + 3 entries of 8 bytes)
-  __host__ __device__ static int meta_rows(int stage_cap) { return (int)(kStages * stage_bytes(stage_cap) / 8) - 4; }
 };
 
-// Per block, chunk c = 0 .. nchunks-1 uses record stage c % 3 and word buffer
-// c & 1:
-//   block start        copy records 0, 1, 2 (offsets from chunk_rec)
-//   top of chunk c     wait record c+1; copy words(c+1) into the buffer chunk
-//                      c-1 released; read chunk c+1's word range and gather
-//                      its element coefficients into registers
-//   phase 1 (c)        element matrices from record c's staged vertices
-//   barrier            record c has been read: copy record c+3 into its stage
-//                      (its offset is in record c); after the last chunk's
-//                      phase 1, copy the first batch of row metadata into the
-//                      stage area instead
-//   phase 2 (c)        wait words(c), add the contributions
-//   barrier
-// then the owned rows are written out batch by batch.  Every copy has at least
-// one chunk of work to land behind.
-// The double-word variants need 8-byte accumulators and element entries, so
-// shared memory admits one CTA per SM; they get the full register file.
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar)
+{
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+// Named barriers among consumer threads (the producer warp never takes part):
+// id 1 = all consumers, id 2 + g = consumer group g.  The _or forms return the
+// OR of `pred` over the participants.
+template <int ID, int COUNT>
+__device__ __forceinline__ void named_sync()
+{
+  asm volatile("bar.sync %0, %1;" ::"n"(ID), "n"(COUNT) : "memory");
+}
+template <int ID, int COUNT>
+__device__ __forceinline__ bool named_sync_or(bool pred)
+{
+  uint32_t r;
+  asm volatile(
+      "{\n"
+      " .reg .pred p, q;\n"
+      " setp.ne.u32 p, %1, 0;\n"
+      " bar.red.or.pred q, %2, %3, p;\n"
+      " selp.u32 %0, 1, 0, q;\n"
+      "}\n"
+      : "=r"(r)
+      : "r"((uint32_t)pred), "n"(ID), "n"(COUNT)
+      : "memory");
+  return r != 0;
+}
+__device__ __forceinline__ bool group_sync_or(int g, bool pred)
+{
+  return g == 0 ? named_sync_or<2, kThreads>(pred) : named_sync_or<3, kThreads>(pred);
+}
+
+// k_assemble: a persistent, warp-specialised kernel; per CTA one producer warp
+// and two consumer groups of kThreads threads.
+//
+// The producer (one thread) takes blocks from the work counter and streams, for
+// chunk q of the CTA (counted across its blocks), the chunk record into stage
+// q % kRecStages and the contribution words into buffer q % 2, then each
+// block's row metadata; it waits on an "empty" barrier before reusing a buffer
+// and runs several chunks (and across block boundaries) ahead.
+//
+// Consumer group g takes the chunks q with q % 2 == g:
+//   phase 1    wait record q; gather the element coefficients; element
+//              matrices from the staged vertices -> the group's buf
+//   barrier    (group) release record q
+//   phase 2    wait words q and the token (the other group finished phase 2 of
+//              chunk q - 1); add the contributions to the owned slots; pass
+//              the token on
+//   barrier    (group) release words q
+// so one group's phase 1 runs beside the other's phase 2, while the
+// accumulator updates stay in chunk order (the sums are bitwise reproducible).
+// Per block both groups zero the accumulators first and write the owned rows
+// last.  Every wait is bounded; after a wait gives up the consumers keep their
+// barrier sequence but skip the work, leave together at the end of the block,
+// the producer stops issuing and lets its copies in flight land, and the CTA
+// records the failure.
 template <int ORDER, int MODE>
-__global__ void __launch_bounds__(kThreads, MODE == kDW ? 1 : 2) k_assemble(AsmArgs a)
+__global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
 {
   using A = Arith<MODE>;
   using T = typename A::T;
   using L = AsmLayout<ORDER, MODE>;
-  constexpr int NU = L::NU, CI = L::CI, NS = L::kStages;
+  constexpr int NU = L::NU, CI = L::CI, NS = kRecStages;
   constexpr int TPI = ORDER == 1 ? 1 : kP2ThreadsPerItem;  // threads per item
   extern __shared__ __align__(16) unsigned char smem[];
   T* acc = reinterpret_cast<T*>(smem);
-  T* buf = reinterpret_cast<T*>(smem + L::off_buf);
   T* tab = reinterpret_cast<T*>(smem + L::off_tab);
+  int2* smeta = reinterpret_cast<int2*>(smem + L::off_meta);
+  BlockDesc* sblk = reinterpret_cast<BlockDesc*>(smem + L::off_blk);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + L::off_bars);
   unsigned char* stage = smem + L::off_stage;  // [NS][sbytes]
   const int sbytes = (int)L::stage_bytes(a.stage_cap);
-  const int2* smeta = reinterpret_cast<const int2*>(stage);  // row metadata (write-out only)
   uint32_t* sent = reinterpret_cast<uint32_t*>(smem + L::off_words(a.stage_cap));  // [2][went]
   const int went = (int)(L::words_bytes(a.ent_cap) / 4);
-  uint64_t* bar_rec = reinterpret_cast<uint64_t*>(smem + L::off_bars(a.ent_cap, a.stage_cap));  // [NS]
-  uint64_t* bar_ent = bar_rec + NS;                                                            // [2]
-  uint64_t* bar_meta = bar_ent + 2;                                                            // [1]
-  const int meta_rows = L::meta_rows(a.stage_cap);
-  __shared__ int s_block;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int local = tid / TPI, sub = tid % TPI;
-  for (int i = tid; i < 7 * NU; i += kThreads) tab[i] = A::from(a.tables[i]);
+  for (int i = tid; i < 7 * NU; i += blockDim.x) tab[i] = A::from(a.tables[i]);
   if (tid == 0) {
-    buf[NU * CI] = A::zero();
-    for (int k = 0; k < L::kBars; ++k) mbar_init(&bar_rec[k], 1);
+    for (int g = 0; g < kGroups; ++g)
+      reinterpret_cast<T*>(smem + L::off_buf + g * L::buf_bytes)[NU * CI] = A::zero();
+    for (int k = 0; k < kNumBars; ++k) {
+      uint32_t count = 1;
+      if (k == kBarBlkEmpty || k == kBarBlkEmpty + 1) count = kConsumers;
+      if (k == kBarToken || k == kBarToken + 1) count = kThreads;
+      mbar_init(&bars[k], count);
+    }
     mbar_fence_init();
   }
   __syncthreads();
-  const T wsum = A::from(a.wsum);
-  // bit k of ph_*: parity of the next completion of barrier k; bit k of
-  // pend_*: a copy onto barrier k is in flight (the same in every thread)
-  uint32_t ph_rec = 0, ph_ent = 0, ph_meta = 0, pend_rec = 0, pend_ent = 0, pend_meta = 0;
+  auto stage_of = [&](int q) { return stage + (q % NS) * sbytes; };
+  auto desc_of = [&](int q) { return reinterpret_cast<const ChunkDesc*>(stage_of(q)); };
   bool failed = false;
 
-  for (;;) {
-    if (tid == 0) s_block = (int)atomicAdd(&a.counters[0], 1u);
-    __syncthreads();
-    const int b = s_block;
-    __syncthreads();
-    if (b >= a.nblocks) break;
-    const BlockDesc d = a.blocks[b];
-
-    auto stage_of = [&](int c) { return stage + (c % NS) * sbytes; };
-    auto desc_of = [&](int c) { return reinterpret_cast<const ChunkDesc*>(stage_of(c)); };
-    auto items_in = [&](int c) { return (min(CI, d.item_count - c * CI) + 3) & ~3; };
-    // thread 0 only
-    auto issue_rec = [&](int c, int off16, int bytes) {
-      uint64_t* bar = &bar_rec[c % NS];
-      mbar_expect_tx(bar, (uint32_t)bytes);
-      bulk_g2s(stage_of(c), a.chunk_data + (int64_t)off16 * 16, (uint32_t)bytes, bar);
-    };
-    auto issue_entries = [&](int c) {  // needs record c staged
-      const ChunkDesc& cd = *desc_of(c);
-      const uint32_t bytes = (uint32_t)cd.warp_off[kWarps] * 4u;
-      mbar_expect_tx(&bar_ent[c & 1], bytes);
-      if (bytes) bulk_g2s(sent + (c & 1) * went, a.entries + cd.word_begin, bytes, &bar_ent[c & 1]);
-    };
-    auto issue_meta = [&](int r0) {  // rows r0 .. r0 + nr (+ one) of the block, 16-byte aligned
-      const int nr = min(meta_rows, d.row_count - r0);
-      const int g0 = d.row_begin + r0, i0 = g0 & ~1, i1 = (g0 + nr + 2) & ~1;
-      mbar_expect_tx(bar_meta, (uint32_t)(i1 - i0) * 8u);
-      bulk_g2s(stage, a.row_meta + i0, (uint32_t)(i1 - i0) * 8u, bar_meta);
-    };
-    // waits on a barrier; false (uniformly) when the wait gave up
-    auto wait_bar = [&](uint64_t* bar, uint32_t& ph, uint32_t& pend, int k) -> bool {
-      const bool ok = mbar_wait(bar, (ph >> k) & 1u);
-      if (__syncthreads_or(!ok)) return false;
-      ph ^= 1u << k;
-      pend &= ~(1u << k);
-      return true;
-    };
-    // coefficient of this thread's item of chunk c (record c staged)
-    auto load_coef = [&](int c, double& coef) -> bool {
-      if (c * CI + local >= d.item_count) return false;
-      const int e = reinterpret_cast<const int32_t*>(stage_of(c) + sizeof(ChunkDesc))[local];
-      coef = a.coeff ? __ldg(a.coeff + e) : a.cconst;
-      return true;
-    };
-
-    for (int i = tid; i < kAccMax; i += kThreads) acc[i] = A::zero();
-    const int npro = min(NS, d.nchunks);
-    if (tid == 0 && npro > 0) {
-      int2 r[NS];
-      for (int c = 0; c < npro; ++c) r[c] = a.chunk_rec[d.chunk_begin + c];
-      fence_proxy_async();
-      for (int c = 0; c < npro; ++c) issue_rec(c, r[c].x, r[c].y);
-    }
-    pend_rec |= (1u << npro) - 1u;
-
-    double coef_r = 0.0, coef_p = 0.0;
-    bool have_r = false, have_p = false;
-    int w_beg = 0, w_end = 0, nw_beg = 0, nw_end = 0;  // this warp's word range of chunks c and c + 1
-    if (d.nchunks > 0) {
-      if (!wait_bar(&bar_rec[0], ph_rec, pend_rec, 0)) { failed = true; break; }
-      if (tid == 0) {
+  if (warp == kConsumers / 32) {
+    // ------------------------------------------------------------ producer
+    if (lane == 0) {
+      int last_rec[NS], last_ent[2] = {-1, -1}, last_meta = -1;
+      for (int s = 0; s < NS; ++s) last_rec[s] = -1;
+      auto wait = [&](int k, int parity) {
+        if (!failed && !mbar_wait(&bars[k], (uint32_t)parity)) failed = true;
+        return !failed;
+      };
+      auto put_rec = [&](int q, int off16, int bytes) {  // record fill q
+        if (q >= NS && !wait(kBarRecEmpty + q % NS, (q / NS - 1) & 1)) return;
         fence_proxy_async();
-        issue_entries(0);
-      }
-      pend_ent |= 1u;
-      nw_beg = desc_of(0)->warp_off[warp];
-      nw_end = desc_of(0)->warp_off[warp + 1];
-      have_r = load_coef(0, coef_r);
-    }
-    for (int c = 0; c < d.nchunks; ++c) {
-      w_beg = nw_beg;
-      w_end = nw_end;
-      if (c + 1 < d.nchunks) {
-        if (!wait_bar(&bar_rec[(c + 1) % NS], ph_rec, pend_rec, (c + 1) % NS)) { failed = true; break; }
-        // word buffer (c + 1) & 1 was released by the barrier that ended chunk c - 1
-        if (tid == 0) {
-          fence_proxy_async();
-          issue_entries(c + 1);
+        mbar_expect_tx(&bars[kBarRecFull + q % NS], (uint32_t)bytes);
+        bulk_g2s(stage_of(q), a.chunk_data + (int64_t)off16 * 16, (uint32_t)bytes, &bars[kBarRecFull + q % NS]);
+        last_rec[q % NS] = q;
+      };
+      int q = 0;
+      for (int j = 0;; ++j) {
+        const int b = (int)atomicAdd(&a.counters[0], 1u);
+        if (j >= 2 && !wait(kBarBlkEmpty + (j & 1), ((j >> 1) - 1) & 1)) break;
+        BlockDesc d;
+        if (b < a.nblocks) {
+          d = a.blocks[b];
+        } else {
+          d = BlockDesc{};
+          d.nchunks = -1;  // no more blocks
         }
-        pend_ent |= 1u << ((c + 1) & 1);
-        nw_beg = desc_of(c + 1)->warp_off[warp];
-        nw_end = desc_of(c + 1)->warp_off[warp + 1];
-        have_p = load_coef(c + 1, coef_p);
+        sblk[j & 1] = d;
+        mbar_arrive(&bars[kBarBlkFull + (j & 1)]);
+        if (d.nchunks < 0) break;
+        const int n = d.nchunks;
+        int2 r0[NS];
+        for (int c = 0; c < n && c < NS; ++c) r0[c] = a.chunk_rec[d.chunk_begin + c];
+        for (int c = 0; c < n && c < NS; ++c) put_rec(q + c, r0[c].x, r0[c].y);
+        for (int c = 0; c < n && !failed; ++c) {
+          const int qq = q + c;
+          if (!wait(kBarRecFull + qq % NS, (qq / NS) & 1)) break;
+          const ChunkDesc* cd = desc_of(qq);
+          if (qq >= 2 && !wait(kBarEntEmpty + (qq & 1), ((qq >> 1) - 1) & 1)) break;
+          const uint32_t bytes = (uint32_t)cd->warp_off[kWarps] * 4u;
+          fence_proxy_async();
+          mbar_expect_tx(&bars[kBarEntFull + (qq & 1)], bytes);
+          if (bytes) bulk_g2s(sent + (qq & 1) * went, a.entries + cd->word_begin, bytes, &bars[kBarEntFull + (qq & 1)]);
+          last_ent[qq & 1] = qq;
+          // record c + NS goes into record c's stage once the consumers release
+          // it; its place is in record c, which nothing has overwritten yet
+          if (c + NS < n) {
+            if (!wait(kBarRecEmpty + qq % NS, (qq / NS) & 1)) break;
+            const int off16 = cd->next_off16, nb = cd->next_bytes;
+            fence_proxy_async();
+            mbar_expect_tx(&bars[kBarRecFull + qq % NS], (uint32_t)nb);
+            bulk_g2s(stage_of(qq), a.chunk_data + (int64_t)off16 * 16, (uint32_t)nb, &bars[kBarRecFull + qq % NS]);
+            last_rec[qq % NS] = qq + NS;
+          }
+        }
+        if (failed) break;
+        q += n;
+        // the block's row metadata: rows row_begin .. row_begin + row_count and
+        // the row after, 16-byte aligned
+        if (j >= 1 && !wait(kBarMetaEmpty, (j - 1) & 1)) break;
+        const int i0 = d.row_begin & ~1, i1 = (d.row_begin + d.row_count + 2) & ~1;
+        fence_proxy_async();
+        mbar_expect_tx(&bars[kBarMetaFull], (uint32_t)(i1 - i0) * 8u);
+        bulk_g2s(smeta, a.row_meta + i0, (uint32_t)(i1 - i0) * 8u, &bars[kBarMetaFull]);
+        last_meta = j;
       }
-      // ---- phase 1: element matrices of chunk c from its staged record
-      if (have_r) {
-        const unsigned char* rb = stage_of(c);
-        const int n4 = items_in(c), nn = desc_of(c)->n_nodes;
-        const ushort4 lc = reinterpret_cast<const ushort4*>(rb + sizeof(ChunkDesc) + 4 * n4)[local];
-        const float4* vrec = reinterpret_cast<const float4*>(rb + sizeof(ChunkDesc) + 12 * n4);
-        const float* vloz = reinterpret_cast<const float*>(rb + sizeof(ChunkDesc) + 12 * n4 + 32 * nn);
-        Fetch<MODE> F;
-        fetch_staged(vrec, vloz, lc, F);
-        const T coef = A::from(coef_r);
-        Cof<T> f;
-        geometry(F, f);
-        if (ORDER == 1) {
-          T K[10];
-          if (a.stiff) {
-            p1_stiff_unique<T>(f, coef * wsum / f.det, K);
+      if (failed) {
+        // let the copies in flight land before the CTA's shared memory goes away
+        for (int s = 0; s < NS; ++s)
+          if (last_rec[s] >= 0) mbar_wait(&bars[kBarRecFull + s], (uint32_t)((last_rec[s] / NS) & 1));
+        for (int s = 0; s < 2; ++s)
+          if (last_ent[s] >= 0) mbar_wait(&bars[kBarEntFull + s], (uint32_t)((last_ent[s] >> 1) & 1));
+        if (last_meta >= 0) mbar_wait(&bars[kBarMetaFull], (uint32_t)(last_meta & 1));
+      }
+    }
+    __syncwarp();
+  } else {
+    // ----------------------------------------------------------- consumers
+    const int g = tid / kThreads;           // group
+    const int gtid = tid - g * kThreads;    // thread within the group
+    const int gwarp = gtid >> 5;
+    const int local = gtid / TPI, sub = gtid % TPI;
+    T* buf = reinterpret_cast<T*>(smem + L::off_buf + g * L::buf_bytes);
+    const T wsum = A::from(a.wsum);
+    int q = 0, ntok = 0;  // chunks before this block; token waits so far
+    for (int j = 0;; ++j) {
+      if (!mbar_wait(&bars[kBarBlkFull + (j & 1)], (uint32_t)((j >> 1) & 1))) failed = true;
+      if (named_sync_or<1, kConsumers>(failed)) { failed = true; break; }
+      const BlockDesc d = sblk[j & 1];
+      mbar_arrive(&bars[kBarBlkEmpty + (j & 1)]);
+      if (d.nchunks < 0) break;
+      const int n = d.nchunks;
+      for (int i = tid; i < kAccMax; i += kConsumers) acc[i] = A::zero();
+      named_sync<1, kConsumers>();  // zeroed before any phase 2
+
+      for (int c = (g - q) & 1; c < n; c += kGroups) {
+        const int qq = q + c;
+        // ---- phase 1: element matrices of chunk c from its staged record
+        if (!failed && !mbar_wait(&bars[kBarRecFull + qq % NS], (uint32_t)((qq / NS) & 1))) failed = true;
+        int w_beg = 0, w_end = 0;  // this warp's contribution words (read before the record is released)
+        if (!failed) {
+          w_beg = desc_of(qq)->warp_off[gwarp];
+          w_end = desc_of(qq)->warp_off[gwarp + 1];
+        }
+        if (!failed && c * CI + local < d.item_count) {
+          const unsigned char* rb = stage_of(qq);
+          const int n4 = (min(CI, d.item_count - c * CI) + 3) & ~3, nn = desc_of(qq)->n_nodes;
+          const int e = reinterpret_cast<const int32_t*>(rb + sizeof(ChunkDesc))[local];
+          const double coef_d = a.coeff ? __ldg(a.coeff + e) : a.cconst;  // latency covered by the geometry
+          const ushort4 lc = reinterpret_cast<const ushort4*>(rb + sizeof(ChunkDesc) + 4 * n4)[local];
+          const float4* vrec = reinterpret_cast<const float4*>(rb + sizeof(ChunkDesc) + 12 * n4);
+          const float* vloz = reinterpret_cast<const float*>(rb + sizeof(ChunkDesc) + 12 * n4 + 32 * nn);
+          Fetch<MODE> F;
+          fetch_staged(vrec, vloz, lc, F);
+          Cof<T> f;
+          geometry(F, f);
+          const T coef = A::from(coef_d);
+          if (ORDER == 1) {
+            T K[10];
+            if (a.stiff) {
+              p1_stiff_unique<T>(f, coef * wsum / f.det, K);
+            } else {
+              const T sc = coef * f.det;
+#pragma unroll
+              for (int u = 0; u < 10; ++u) K[u] = sc * tab[6 * NU + u];
+            }
+#pragma unroll
+            for (int u = 0; u < 10; ++u) buf[u * CI + local] = K[u];
+          } else if (a.stiff) {
+            T gm[6];
+            metric<T>(f, coef / f.det, gm);
+            for (int u = sub; u < NU; u += TPI) {
+              T v = gm[0] * tab[u];
+#pragma unroll
+              for (int k = 1; k < 6; ++k) v = v + gm[k] * tab[k * NU + u];
+              buf[u * CI + local] = v;
+            }
           } else {
             const T sc = coef * f.det;
-#pragma unroll
-            for (int u = 0; u < 10; ++u) K[u] = sc * tab[6 * NU + u];
+            for (int u = sub; u < NU; u += TPI) buf[u * CI + local] = sc * tab[6 * NU + u];
           }
-#pragma unroll
-          for (int u = 0; u < 10; ++u) buf[u * CI + local] = K[u];
-        } else if (a.stiff) {
-          T g[6];
-          metric<T>(f, coef / f.det, g);
-          for (int u = sub; u < NU; u += TPI) {
-            T v = g[0] * tab[u];
-#pragma unroll
-            for (int q = 1; q < 6; ++q) v = v + g[q] * tab[q * NU + u];
-            buf[u * CI + local] = v;
-          }
-        } else {
-          const T sc = coef * f.det;
-          for (int u = sub; u < NU; u += TPI) buf[u * CI + local] = sc * tab[6 * NU + u];
         }
-      }
-      __syncthreads();
-      if (c + NS < d.nchunks) {
-        // record c has been read: bring record c + 3 into its stage
-        if (tid == 0) {
-          const int off16 = desc_of(c)->next_off16, bytes = desc_of(c)->next_bytes;
-          fence_proxy_async();
-          issue_rec(c + NS, off16, bytes);
+        failed = group_sync_or(g, failed);
+        if (gtid == 0) mbar_arrive(&bars[kBarRecEmpty + qq % NS]);
+        // ---- phase 2: segmented sums into owned slots.  Pieces of PW words of
+        // one slot are summed in registers and update the slot once; within a
+        // chunk every slot belongs to one thread, and the token orders the
+        // chunks.
+        if (!failed && !mbar_wait(&bars[kBarEntFull + (qq & 1)], (uint32_t)((qq >> 1) & 1))) failed = true;
+        if (c >= 1) {
+          if (!failed && !mbar_wait(&bars[kBarToken + g], (uint32_t)(ntok & 1))) failed = true;
+          ++ntok;
         }
-        pend_rec |= 1u << (c % NS);
-      } else if (c == d.nchunks - 1) {
-        // every record has been read: the stage area takes the row metadata
-        if (tid == 0) {
-          fence_proxy_async();
-          issue_meta(0);
-        }
-        pend_meta = 1u;
-      }
-      // ---- phase 2: segmented sums into owned slots
-      if (!wait_bar(&bar_ent[c & 1], ph_ent, pend_ent, c & 1)) { failed = true; break; }
-      {
-        // pieces of PW words of one slot: summed in registers, one update of
-        // the slot per piece; within a chunk every slot belongs to one thread
-        constexpr int PW = piece_words(ORDER);
-        const int K = (w_end - w_beg) / (32 * PW);
-        const uint32_t* ew = sent + (c & 1) * went + w_beg + lane * PW;
+        if (!failed) {
+          constexpr int PW = piece_words(ORDER);
+          const int K = (w_end - w_beg) / (32 * PW);
+          const uint32_t* ew = sent + (qq & 1) * went + w_beg + lane * PW;
 #pragma unroll 2
-        for (int k = 0; k < K; ++k) {
-          uint32_t w[PW];
-          if constexpr (PW == 4) {
-            const uint4 q = *reinterpret_cast<const uint4*>(ew + k * 32 * PW);
-            w[0] = q.x; w[1] = q.y; w[2] = q.z; w[3] = q.w;
-          } else {
-            const uint2 q = *reinterpret_cast<const uint2*>(ew + k * 32 * PW);
-            w[0] = q.x; w[1] = q.y;
-          }
-          const uint32_t slot = (w[0] >> kSrcBits) & kSlotMask;
-          T v = buf[w[0] & kSrcMask];
+          for (int k = 0; k < K; ++k) {
+            uint32_t w[PW];
+            if constexpr (PW == 4) {
+              const uint4 v = *reinterpret_cast<const uint4*>(ew + k * 32 * PW);
+              w[0] = v.x; w[1] = v.y; w[2] = v.z; w[3] = v.w;
+            } else {
+              const uint2 v = *reinterpret_cast<const uint2*>(ew + k * 32 * PW);
+              w[0] = v.x; w[1] = v.y;
+            }
+            const uint32_t slot = (w[0] >> kSrcBits) & kSlotMask;
+            T v = buf[w[0] & kSrcMask];
 #pragma unroll
-          for (int q = 1; q < PW; ++q) v = v + buf[w[q] & kSrcMask];
-          acc[slot] = acc[slot] + v;
-        }
-      }
-      __syncthreads();
-      coef_r = coef_p;
-      have_r = have_p;
-      have_p = false;
-    }
-    if (failed) break;
-    // ---- write the owned rows, one batch of row metadata at a time.  A warp
-    // takes 32 consecutive rows (their slots are contiguous in acc); each lane
-    // takes one slot per pass, finds its row by a binary search over the
-    // lanes' row bases (shuffles) and stores to CSR start + offset.
-    using Out = typename A::Out;
-    Out* out = reinterpret_cast<Out*>(a.values);
-    for (int r0 = 0; r0 < d.row_count; r0 += meta_rows) {
-      if (r0 > 0 || d.nchunks == 0) {
-        if (tid == 0) {
-          fence_proxy_async();
-          issue_meta(r0);
-        }
-        pend_meta = 1u;
-      }
-      if (!wait_bar(bar_meta, ph_meta, pend_meta, 0)) { failed = true; break; }
-      const int nr = min(meta_rows, d.row_count - r0);
-      const int m0 = (d.row_begin + r0) & 1;  // smeta[m0 + j] is row r0 + j
-      const int bend = (r0 + nr < d.row_count) ? smeta[m0 + nr].x : d.acc_used;
-      for (int t0 = 32 * warp; t0 < nr; t0 += 32 * kWarps) {
-        const int nrow = min(32, nr - t0);
-        int2 m = make_int2(0x7fffffff, 0);
-        if (lane < nrow) m = smeta[m0 + t0 + lane];
-        const int A0 = __shfl_sync(0xffffffffu, m.x, 0);
-        const int A1 = (t0 + 32 < nr) ? smeta[m0 + t0 + 32].x : bend;
-        for (int k0 = A0; k0 < A1; k0 += 32) {
-          const int k = k0 + lane;
-          int lo = 0;  // last row j (< nrow) with base_j <= k
-#pragma unroll
-          for (int s = 16; s >= 1; s >>= 1) {
-            const int v = __shfl_sync(0xffffffffu, m.x, (lo + s) & 31);
-            if (lo + s < nrow && v <= k) lo += s;
+            for (int p = 1; p < PW; ++p) v = v + buf[w[p] & kSrcMask];
+            acc[slot] = acc[slot] + v;
           }
-          const int off = __shfl_sync(0xffffffffu, m.y, lo);
-          if (k < A1) out[k + off] = A::out(acc[k]);
         }
+        if (c + 1 < n) mbar_arrive(&bars[kBarToken + (g ^ 1)]);  // release: the updates above precede
+        failed = group_sync_or(g, failed);
+        if (gtid == 0) mbar_arrive(&bars[kBarEntEmpty + (qq & 1)]);
       }
-      __syncthreads();
+      q += n;
+      if (!failed && !mbar_wait(&bars[kBarMetaFull], (uint32_t)(j & 1))) failed = true;
+      if (named_sync_or<1, kConsumers>(failed)) { failed = true; break; }
+      // ---- write the owned rows, one row per thread: the stores of a pass go
+      // to 32 rows at once, the accumulator reads (consecutive rows) spread
+      // over the banks
+      using Out = typename A::Out;
+      Out* out = reinterpret_cast<Out*>(a.values);
+      const int2* sm = smeta + (d.row_begin & 1);  // sm[i]: row i of the block
+      for (int r = tid; r - tid < d.row_count; r += kConsumers) {
+        int base = 0, len = 0, off = 0;
+        if (r < d.row_count) {
+          const int2 m = sm[r];
+          base = m.x;
+          off = m.y;
+          len = ((r + 1 < d.row_count) ? sm[r + 1].x : d.acc_used) - base;
+        }
+        const int maxlen = __reduce_max_sync(0xffffffffu, len);
+        Out* o = out + base + off;
+        const T* s0 = acc + base;
+#pragma unroll 4
+        for (int k = 0; k < maxlen; ++k)
+          if (k < len) o[k] = A::out(s0[k]);
+      }
+      named_sync<1, kConsumers>();
+      if (tid == 0) mbar_arrive(&bars[kBarMetaEmpty]);
     }
-    if (failed) break;
   }
-  if (failed) {
-    // let copies still in flight land before the CTA's shared memory goes away
-    for (int st = 0; st < NS; ++st)
-      if ((pend_rec >> st) & 1u) mbar_wait(&bar_rec[st], (ph_rec >> st) & 1u);
-    for (int st = 0; st < 2; ++st)
-      if ((pend_ent >> st) & 1u) mbar_wait(&bar_ent[st], (ph_ent >> st) & 1u);
-    if (pend_meta & 1u) mbar_wait(bar_meta, ph_meta & 1u);
-    if (tid == 0) {
-      atomicExch(&a.counters[2], (uint32_t)kDevErrTimeout);
-      atomicExch(&a.counters[3], (uint32_t)blockIdx.x);
-    }
+  if (failed && (tid == 0 || tid == kConsumers)) {
+    atomicExch(&a.counters[2], (uint32_t)kDevErrTimeout);
+    atomicExch(&a.counters[3], (uint32_t)blockIdx.x);
   }
   __syncthreads();
   if (tid == 0) {
@@ -729,20 +781,23 @@ static mg_status launch_assemble_t(AsmArgs a, cudaStream_t st)
 {
   using L = AsmLayout<ORDER, MODE>;
   const size_t smem = L::total(a.ent_cap, a.stage_cap);
-  if (L::meta_rows(a.stage_cap) < 32) return set_error(MG_ERR_SIZE, "assembly stage too small for row metadata");
   static size_t configured = 0;
-  static int per_sm = 0, sms = 0;
+  static int per_sm = 0, sms = 0, max_smem = 0;
   if (configured != smem) {
-    MG_CUDA(cudaFuncSetAttribute(k_assemble<ORDER, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_assemble<ORDER, MODE>, kThreads, smem));
     int dev = 0;
     MG_CUDA(cudaGetDevice(&dev));
     MG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    MG_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    if (smem > (size_t)max_smem)
+      return set_error(MG_ERR_SIZE, "assembly CTA needs " + std::to_string(smem) + " bytes of shared memory, above " +
+                                        std::to_string(max_smem) + " (chunks touch too many vertices)");
+    MG_CUDA(cudaFuncSetAttribute(k_assemble<ORDER, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_assemble<ORDER, MODE>, kAsmThreads, smem));
     configured = smem;
   }
   if (per_sm < 1) return set_error(MG_ERR_SIZE, "assembly CTA does not fit on an SM (shared memory)");
   const int grid = std::max(1, std::min(a.nblocks, per_sm * sms));
-  if (a.nblocks > 0) k_assemble<ORDER, MODE><<<grid, kThreads, smem, st>>>(a);
+  if (a.nblocks > 0) k_assemble<ORDER, MODE><<<grid, kAsmThreads, smem, st>>>(a);
   MG_CUDA(cudaGetLastError());
   return MG_OK;
 }

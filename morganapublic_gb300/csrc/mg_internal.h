@@ -34,6 +34,13 @@ constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 // Accumulator slots (CSR entries of the rows a CTA owns) held in shared memory.
 constexpr int kAccMax = 8192;
+// Owned rows per block (rows of elements have at least nb >= 4 entries, so only
+// dofs outside every element can reach it); the kernel stages one block's row
+// metadata in shared memory at once.
+constexpr int kRowsMax = kAccMax / 4;
+// Chunk-record stages of the assembly kernel: record c + kRecStages is copied
+// into the stage of record c, its place read from record c.
+constexpr int kRecStages = 4;
 // Elements ("items") per chunk: one thread per P1 element, eight per P2 element.
 constexpr int kChunkP1 = 256;
 constexpr int kChunkP2 = 32;
@@ -83,7 +90,7 @@ struct ChunkDesc {
   int64_t word_begin;         // first contribution word of the chunk (multiple of 32)
   int32_t warp_off[kWarps + 1];  // per-warp offsets relative to word_begin; [kWarps] = chunk size
   int32_t n_nodes;            // distinct vertices of the chunk's elements (multiple of 4)
-  int32_t next_off16;         // record of chunk + 3 of the same block: offset / 16
+  int32_t next_off16;         // record of chunk + kRecStages of the same block: offset / 16
   int32_t next_bytes;         //   and size (0 when the block has no such chunk)
   int32_t pad[2];
 };

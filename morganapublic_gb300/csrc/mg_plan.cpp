@@ -128,18 +128,20 @@ static mg_status build_schedule(mg_plan* p, HostSchedule* hs)
   std::sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
     return key[a] != key[b] ? key[a] < key[b] : a < b;
   });
-  // greedy blocks of at most kAccMax accumulator slots
+  // greedy blocks of at most kAccMax accumulator slots and kRowsMax rows
   std::vector<int32_t> block_of(nd);
   std::vector<int64_t> bstart;  // into order
-  int64_t used = kAccMax + 1;
+  int64_t used = kAccMax + 1, nrows = 0;
   for (int64_t t = 0; t < nd; ++t) {
     const int32_t r = order[t];
     const int64_t l = p->rowptr[r + 1] - p->rowptr[r];
-    if (used + l > kAccMax) {
+    if (used + l > kAccMax || nrows == kRowsMax) {
       bstart.push_back(t);
       used = 0;
+      nrows = 0;
     }
     used += l;
+    ++nrows;
     block_of[r] = (int32_t)bstart.size() - 1;
   }
   bstart.push_back(nd);
@@ -498,9 +500,9 @@ mg_status plan_device(mg_plan* p)
       cd.word_begin = cp[0];
       for (int w = 0; w <= kWarps; ++w) cd.warp_off[w] = (int32_t)(cp[w] - cp[0]);
       cd.n_nodes = (int32_t)nn;
-      if (c + 3 < d.nchunks) {
-        cd.next_off16 = rec[ck + 3].x;
-        cd.next_bytes = rec[ck + 3].y;
+      if (c + kRecStages < d.nchunks) {
+        cd.next_off16 = rec[ck + kRecStages].x;
+        cd.next_bytes = rec[ck + kRecStages].y;
       }
       std::memcpy(r, &cd, sizeof cd);
       const int64_t first = (int64_t)d.item_begin + (int64_t)c * CI;
