@@ -46,6 +46,9 @@ def parse():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-cg", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--config", type=int, default=2, choices=[2, 3, 5],
+                    help="2: the headline step (default); 3: P2 48^3 mixed-precision vs FP64 CG; "
+                         "5: P1 128^3 kernels as fractions of the HBM roofline")
     ap.add_argument("--only", default=None, choices=["asm64", "asm32", "spmv64", "spmv32", "cg64", "cg32"],
                     help="run warmup + steps launches of one kernel only (for profilers) and print its timing")
     return ap.parse_args()
@@ -275,6 +278,165 @@ def run_only(a):
     return 0
 
 
+def _timed_cuda(torch, stream, fn, reps, flush=None):
+    """median CUDA-event time (ms) of fn on `stream`; L2 flushed before each rep when `flush` is given"""
+    ts = []
+    with torch.cuda.stream(stream):
+        for r in range(reps + 2):
+            if flush is not None:
+                flush.fill_(float(r))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if r >= 2:
+                ts.append(e0.elapsed_time(e1))
+    return statistics.median(ts)
+
+
+def run_config3(a):
+    """P2 (10-node) kappa-stiffness on 48^3 cells x 6 tets, Keast 11-point rule, kappa lognormal sigma 0.5.
+    The right-hand side is A u_I for the P2 interpolant u_I of sin(pi x) sin(pi y) sin(pi z) (zero on the
+    boundary, Dirichlet rows eliminated), so u_I is the exact discrete solution and each solver's error
+    against it is its solve error.  FP64 Jacobi-PCG vs FP32-inner/FP64-refined CG, both to a 1e-10 relative
+    residual; each solve run twice, the second timed."""
+    import numpy as np
+    import torch
+    import morganapublic_gb300 as mg
+    from morganapublic_gb300 import meshgen
+    n, q = 48, 11
+    stream = torch.cuda.Stream()
+    peak, peak_kind = peaks()
+    m = meshgen.kuhn_cube(n)
+    kappa_h = meshgen.lognormal(len(m.conn), 0.5, a.seed)
+    mesh = mg.Mesh(m.xyz, m.conn, order=2)
+    b = mg.MatrixBuilder(mesh)
+    E, ndof, nnz = len(m.conn), b.ndof, b.nnz
+    en, _ = mesh.edges()
+    X = np.concatenate([m.xyz, 0.5 * (m.xyz[en[:, 0]] + m.xyz[en[:, 1]])])
+    bmask = meshgen.p2_boundary(m.boundary, en)
+    uI = np.sin(np.pi * X[:, 0]) * np.sin(np.pi * X[:, 1]) * np.sin(np.pi * X[:, 2])
+    uI[bmask] = 0.0
+    kappa = torch.from_numpy(kappa_h).cuda()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    with torch.cuda.stream(stream):
+        A64 = b.assemble("stiff_kappa", coeff=kappa, quad=q, prec="f64", stream=stream)
+        A32 = b.assemble("stiff_kappa", coeff=kappa, quad=q, prec="f32", stream=stream)
+        mask = torch.from_numpy(bmask)
+        b.apply_dirichlet(A64, mask, stream=stream)
+        b.apply_dirichlet(A32, mask, stream=stream)
+        uI_d = torch.from_numpy(uI).cuda()
+        rhs = b.apply(A64, uI_d, stream=stream)
+    torch.cuda.synchronize()
+    t64 = _timed_cuda(torch, stream, lambda: b.assemble("stiff_kappa", coeff=kappa, quad=q, prec="f64", out=A64,
+                                                        stream=stream), 5, flush)
+    t32 = _timed_cuda(torch, stream, lambda: b.assemble("stiff_kappa", coeff=kappa, quad=q, prec="f32", out=A32,
+                                                        stream=stream), 5, flush)
+    with torch.cuda.stream(stream):
+        b.apply_dirichlet(A64, mask, stream=stream)
+        b.apply_dirichlet(A32, mask, stream=stream)
+    y = torch.empty_like(rhs)
+    ts64 = _timed_cuda(torch, stream, lambda: b.apply(A64, uI_d, out=y, stream=stream), 10, flush)
+    res = {}
+    for rep in range(2):
+        with torch.cuda.stream(stream):
+            xs, i64 = b.cg(A64, rhs, rtol=1e-10, maxit=50000, stream=stream)
+            xr, imx = b.cg_refined(A64, A32, rhs, rtol=1e-10, inner_rtol=1e-2, stream=stream)
+        torch.cuda.synchronize()
+    err64 = float(torch.linalg.norm(xs - uI_d) / torch.linalg.norm(uI_d))
+    errmx = float(torch.linalg.norm(xr - uI_d) / torch.linalg.norm(uI_d))
+    diff = float(torch.linalg.norm(xr - xs) / torch.linalg.norm(xs))
+    B64, B32 = asm_bytes(E, len(m.xyz), nnz, 8, nb=10), asm_bytes(E, len(m.xyz), nnz, 4, nb=10)
+    S64 = spmv_bytes(ndof, nnz, 8)
+    line = {"config": {"workload": f"P2 kappa-stiffness, {n}^3 cells x 6 tets ({E} tets, {ndof} dofs, {nnz} CSR entries), "
+                                   "Keast 11-point rule, lognormal kappa sigma 0.5, rhs = A u_I (u_I = P2 interpolant "
+                                   "of sin(pi x) sin(pi y) sin(pi z)), Dirichlet u = 0",
+                       "tets": E, "dofs": ndof, "nnz": nnz},
+            "assembly_f64": {"ms": t64, "tets_per_s": E / (t64 * 1e-3), "gbs": B64 / (t64 * 1e-3) / 1e9,
+                             "frac_of_hbm": B64 / (t64 * 1e-3) / 1e9 / peak},
+            "assembly_f32": {"ms": t32, "tets_per_s": E / (t32 * 1e-3), "gbs": B32 / (t32 * 1e-3) / 1e9,
+                             "frac_of_hbm": B32 / (t32 * 1e-3) / 1e9 / peak},
+            "spmv_f64_cold": {"ms": ts64, "gbs": S64 / (ts64 * 1e-3) / 1e9, "frac_of_hbm": S64 / (ts64 * 1e-3) / 1e9 / peak},
+            "cg": {"fp64_pcg": i64.as_dict(), "fp32_refined": imx.as_dict(),
+                   "speedup_refined_vs_fp64": i64.seconds / imx.seconds if imx.seconds > 0 else None,
+                   "fp64_error_vs_exact_discrete": err64, "refined_error_vs_exact_discrete": errmx,
+                   "refined_vs_fp64_rel_diff": diff, "precond": "jacobi", "rtol": 1e-10, "inner_rtol": 1e-2},
+            "peak_gbs": peak, "peak_kind": peak_kind}
+    print(json.dumps(line))
+    return 0
+
+
+def run_config5(a):
+    """P1 128^3 x 6 tets, jitter +-0.25h, element permutation, kappa lognormal sigma 1.5 (seed 3): FP64 and
+    FP32 assembly, FP64 and FP32 SpMV (L2 flushed before each), FP64 CG and FP32-refined CG to 1e-10 with
+    Dirichlet u = 0 and f = 1, and the adjoint gradient kernel; each kernel against the measured HBM peak."""
+    import numpy as np
+    import torch
+    import morganapublic_gb300 as mg
+    from morganapublic_gb300 import meshgen
+    n = 128
+    stream = torch.cuda.Stream()
+    peak, peak_kind = peaks()
+    t0 = time.perf_counter()
+    m = meshgen.kuhn_cube(n, jitter=0.25, seed=3, permute=True)
+    kappa_h = meshgen.lognormal(len(m.conn), 1.5, 3)
+    mesh = mg.Mesh(m.xyz, m.conn, order=1)
+    b = mg.MatrixBuilder(mesh)
+    t_plan = time.perf_counter() - t0
+    E, N, ndof, nnz = len(m.conn), len(m.xyz), b.ndof, b.nnz
+    kappa = torch.from_numpy(kappa_h).cuda()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    v64 = torch.empty(nnz, dtype=torch.float64, device="cuda")
+    v32 = torch.empty(nnz, dtype=torch.float32, device="cuda")
+    x = torch.from_numpy(np.random.default_rng(3).uniform(-1, 1, ndof)).cuda()
+    x32 = x.float()
+    y, y32 = torch.empty_like(x), torch.empty_like(x32)
+    ta64 = _timed_cuda(torch, stream, lambda: b.assemble("stiff_kappa", coeff=kappa, quad=4, prec="f64", out=v64,
+                                                         stream=stream), 5, flush)
+    ta32 = _timed_cuda(torch, stream, lambda: b.assemble("stiff_kappa", coeff=kappa, quad=4, prec="f32", out=v32,
+                                                         stream=stream), 5, flush)
+    ts64 = _timed_cuda(torch, stream, lambda: b.apply(v64, x, out=y, stream=stream), 10, flush)
+    ts32 = _timed_cuda(torch, stream, lambda: b.apply(v32, x32, out=y32, stream=stream), 10, flush)
+    with torch.cuda.stream(stream):
+        rhs = b.build_vector(quad=4, stream=stream)
+        mask = torch.from_numpy(m.boundary)
+        b.apply_dirichlet(v64, mask, rhs, stream=stream)
+        b.apply_dirichlet(v32, mask, stream=stream)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        xs, i64 = b.cg(v64, rhs, rtol=1e-10, maxit=50000, stream=stream)
+        xr, imx = b.cg_refined(v64, v32, rhs, rtol=1e-10, inner_rtol=1e-2, stream=stream)
+    torch.cuda.synchronize()
+    diff = float(torch.linalg.norm(xr - xs) / torch.linalg.norm(xs))
+    lam = torch.from_numpy(np.random.default_rng(4).uniform(-1, 1, ndof)).cuda()
+    g = torch.empty(E, dtype=torch.float64, device="cuda")
+    tg = _timed_cuda(torch, stream, lambda: b.adjoint_grad(xs, lam, quad=4, out=g, stream=stream), 10, flush)
+
+    def rec(bytes_, ms, units=None):
+        gbs = bytes_ / (ms * 1e-3) / 1e9
+        d = {"ms": ms, "gbs": gbs, "frac_of_hbm": gbs / peak, "algorithmic_bytes": bytes_}
+        if units:
+            d["tets_per_s"] = units / (ms * 1e-3)
+        return d
+
+    line = {"config": {"workload": f"P1 kappa-diffusion, {n}^3 cells x 6 tets ({E} tets, {N} nodes, {nnz} CSR entries), "
+                                   "jitter +-0.25h, element permutation and lognormal kappa sigma 1.5 (seed 3), "
+                                   "4-point rule; L2 flushed before each kernel timing",
+                       "tets": E, "nodes": N, "nnz": nnz, "host_plan_seconds": t_plan},
+            "assembly_f64": rec(asm_bytes(E, N, nnz, 8), ta64, E),
+            "assembly_f32": rec(asm_bytes(E, N, nnz, 4), ta32, E),
+            "spmv_f64": rec(spmv_bytes(ndof, nnz, 8), ts64),
+            "spmv_f32": rec(spmv_bytes(ndof, nnz, 4), ts32),
+            "adjoint_grad": rec(24 * E + 24 * N + 16 * ndof, tg, E),
+            "cg": {"fp64_pcg": i64.as_dict(), "fp32_refined": imx.as_dict(),
+                   "speedup_refined_vs_fp64": i64.seconds / imx.seconds if imx.seconds > 0 else None,
+                   "refined_vs_fp64_rel_diff": diff, "precond": "jacobi", "rtol": 1e-10},
+            "peak_gbs": peak, "peak_kind": peak_kind}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     a = parse()
     if a.impl == "reference":
@@ -284,6 +446,10 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if a.only:
         return run_only(a)
+    if a.config == 3:
+        return run_config3(a)
+    if a.config == 5:
+        return run_config5(a)
     cpu_base = None
     if rank == 0 and not a.no_cpu_baseline:
         cpu_base = cpu_baseline_port(a)  # before any CUDA work
@@ -409,10 +575,10 @@ def main():
                 b.apply_dirichlet(A32, mask, stream=stream)
                 torch.cuda.synchronize()
                 xs, i64 = b.cg(A64, rhs, rtol=1e-10, maxit=20000, stream=stream)
-                xr, imx = b.cg_refined(A64, A32, rhs, rtol=1e-10, inner_rtol=1e-4, stream=stream)
+                xr, imx = b.cg_refined(A64, A32, rhs, rtol=1e-10, inner_rtol=1e-2, stream=stream)
                 torch.cuda.synchronize()
                 xs, i64 = b.cg(A64, rhs, rtol=1e-10, maxit=20000, stream=stream)
-                xr, imx = b.cg_refined(A64, A32, rhs, rtol=1e-10, inner_rtol=1e-4, stream=stream)
+                xr, imx = b.cg_refined(A64, A32, rhs, rtol=1e-10, inner_rtol=1e-2, stream=stream)
                 torch.cuda.synchronize()
             diff = float(torch.linalg.norm(xr - xs) / torch.linalg.norm(xs))
             extras["cg"] = {"fp64_pcg": i64.as_dict(), "fp32_refined": imx.as_dict(),

@@ -233,11 +233,17 @@ mg_status mg_spmv(mg_plan* plan, int32_t prec, const void* d_values, const void*
 mg_status mg_cg_solve(mg_plan* plan, const double* d_values, const double* d_b, double* d_x,
                       double rtol, int32_t maxit, int32_t precond, mg_cg_info* info, void* stream);
 
-/* Mixed-precision solve: FP64 iterative refinement around an inner CG that
-   runs on the FP32 operator with FP32 vectors and FP64 dot products.  The
-   residual r = b - A64 x, its norm and the update x += d stay in FP64.
-   Stops when ||b - A64 x||_2 <= rtol ||b||_2.  Build addition (no reference
-   counterpart); same role as mg_cg_solve. */
+/* Mixed-precision solve: one Jacobi-preconditioned CG sequence on the FP32
+   operator with FP32 vectors and FP64 dot products, anchored to FP64 by
+   reliable updates.  Whenever the FP32 recursive residual has dropped by the
+   factor inner_rtol since the last anchor (or reaches the target), the FP32
+   correction is added to the FP64 solution, r = b - A64 x is recomputed in FP64
+   and replaces the FP32 residual; the search direction is kept, so the Krylov
+   sequence is not restarted.  Stops when ||b - A64 x||_2 <= rtol ||b||_2 (true
+   FP64 residual).  max_outer bounds the number of FP64 anchors, max_inner the
+   FP32 iterations in total.  mg_cg_info.iterations counts FP32 iterations,
+   outer_iterations the anchors.  Build addition (no reference counterpart);
+   same role as mg_cg_solve. */
 mg_status mg_cg_refined(mg_plan* plan, const double* d_values64, const float* d_values32,
                         const double* d_b, double* d_x, double rtol, int32_t max_outer,
                         int32_t max_inner, double inner_rtol, int32_t precond, mg_cg_info* info,

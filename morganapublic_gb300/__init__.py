@@ -342,8 +342,8 @@ class MatrixBuilder:
             _check(st, "mg_cg_solve")
         return x, info
 
-    def cg_refined(self, values64, values32, b, x0=None, rtol: float = 1e-10, max_outer: int = 50,
-                   max_inner: int = 10000, inner_rtol: float = 1e-4, precond="jacobi", stream=None,
+    def cg_refined(self, values64, values32, b, x0=None, rtol: float = 1e-10, max_outer: int = 200,
+                   max_inner: int = 100000, inner_rtol: float = 1e-2, precond="jacobi", stream=None,
                    raise_on_fail: bool = True):
         torch = _torch()
         x = torch.zeros_like(b) if x0 is None else x0.clone()

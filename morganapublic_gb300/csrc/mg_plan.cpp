@@ -92,6 +92,18 @@ static mg_status build_pattern(mg_plan* p)
   return MG_OK;
 }
 
+// SMs of the current device (one persistent assembly CTA each); GB300's 152
+// when no device is visible.
+static int64_t sm_count_hint()
+{
+  int n = 0, dev = 0, sms = 0;
+  if (cudaGetDeviceCount(&n) == cudaSuccess && n > 0 && cudaGetDevice(&dev) == cudaSuccess &&
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && sms > 0)
+    return sms;
+  cudaGetLastError();
+  return 152;
+}
+
 static mg_status build_schedule(mg_plan* p, HostSchedule* hs)
 {
   mg_mesh* m = p->mesh;
@@ -128,21 +140,39 @@ static mg_status build_schedule(mg_plan* p, HostSchedule* hs)
   std::sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
     return key[a] != key[b] ? key[a] < key[b] : a < b;
   });
-  // greedy blocks of at most kAccMax accumulator slots and kRowsMax rows
+  // greedy blocks of at most `cap` accumulator slots and kRowsMax rows.  The
+  // kernel runs one persistent CTA per SM, so the cap is lowered until the
+  // number of blocks is a multiple of the SM count (no partial last wave).
   std::vector<int32_t> block_of(nd);
   std::vector<int64_t> bstart;  // into order
-  int64_t used = kAccMax + 1, nrows = 0;
-  for (int64_t t = 0; t < nd; ++t) {
-    const int32_t r = order[t];
-    const int64_t l = p->rowptr[r + 1] - p->rowptr[r];
-    if (used + l > kAccMax || nrows == kRowsMax) {
-      bstart.push_back(t);
-      used = 0;
-      nrows = 0;
+  auto cut = [&](int64_t cap) {
+    bstart.clear();
+    int64_t used = cap + 1, nrows = 0;
+    for (int64_t t = 0; t < nd; ++t) {
+      const int32_t r = order[t];
+      const int64_t l = p->rowptr[r + 1] - p->rowptr[r];
+      if (used + l > cap || nrows == kRowsMax) {
+        bstart.push_back(t);
+        used = 0;
+        nrows = 0;
+      }
+      used += l;
+      ++nrows;
     }
-    used += l;
-    ++nrows;
-    block_of[r] = (int32_t)bstart.size() - 1;
+    return (int64_t)bstart.size();
+  };
+  {
+    const int64_t n0 = cut(kAccMax), sms = sm_count_hint();
+    const int64_t target = (n0 + sms - 1) / sms * sms;
+    if (n0 > sms / 2 && target > n0) {
+      int64_t cap = std::max<int64_t>(1, (p->nnz + target - 1) / target);
+      while (cap < kAccMax && cut(cap) > target) cap += 8;
+      if (cap >= kAccMax) cut(kAccMax);
+    }
+    for (size_t b = 0; b < bstart.size(); ++b) {
+      const int64_t t1 = b + 1 < bstart.size() ? bstart[b + 1] : nd;
+      for (int64_t t = bstart[b]; t < t1; ++t) block_of[order[t]] = (int32_t)b;
+    }
   }
   bstart.push_back(nd);
   const int32_t nbk = (int32_t)bstart.size() - 1;
@@ -418,6 +448,10 @@ static mg_status build_schedule(mg_plan* p, HostSchedule* hs)
     hs->max_chunk_entries = std::max(hs->max_chunk_entries, maxc[b]);
     std::vector<uint32_t>().swap(ent[b]);
   }
+  // blocks taken largest first (the work counter hands them out in array
+  // order), so the last ones to start are the shortest
+  std::stable_sort(hs->blocks.begin(), hs->blocks.end(),
+                   [](const BlockDesc& x, const BlockDesc& y) { return x.nchunks > y.nchunks; });
   p->nblocks = nbk;
   p->n_items = 0;
   for (int32_t b = 0; b < nbk; ++b) p->n_items += hs->blocks[b].item_count;

@@ -1,9 +1,10 @@
 // CSR SpMV and conjugate-gradient solvers for sm_103a.
 //
-// SpMV: a group of G lanes per row (G from the mean row length: 16 for P1
-// stiffness rows of ~15 entries, 32 for P2), values and column indices read
-// coalesced, x gathered through the read-only path, the row sum reduced with
-// xor shuffles in a fixed tree -- deterministic.
+// SpMV: FP64 one thread per row (the FP64 pipe, not HBM, is the narrow
+// resource on GB300); FP32 a group of G lanes per row (G from the mean row
+// length), values and column indices read coalesced, x gathered through the
+// read-only path, the row sum reduced with xor shuffles in a fixed tree --
+// deterministic.
 //
 // CG: the reference hands the assembled Epetra operator to Belos BlockCG
 // (src/morganaTrilinos/belosBlockCG.hpp:46-82 in morganaPublic); here every
@@ -16,6 +17,9 @@
 //   K3  p = z + beta p.
 // Once `done` is set the remaining kernels return at entry, so a CUDA graph of
 // several iterations can be replayed without a host round trip per iteration.
+// Kernels are launched with programmatic dependent launch: a kernel's launch and
+// prologue overlap the tail of the one before, and it waits (griddepcontrol)
+// before touching memory that kernel wrote.
 // Dot products accumulate in FP64 in both precisions; the order of every
 // floating-point sum is fixed, so a solve is bitwise reproducible.
 #include <algorithm>
@@ -23,6 +27,7 @@
 #include <cmath>
 #include <mutex>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "mg_ff.cuh"
@@ -33,18 +38,50 @@ namespace mg {
 constexpr int kSolveThreads = 256;
 constexpr int kMaxSolveBlocks = 2048;  // bound of the per-CTA partial arrays
 
+// Programmatic dependent launch: wait for the preceding kernel's memory (a no-op
+// when there is no programmatic dependency), and let the next kernel be
+// scheduled once every CTA of this one has started.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_k(bool pdl, void (*kernel)(KArgs...), int grid, int block, cudaStream_t st,
+                            Args&&... args)
+{
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3((unsigned)block);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_pdl(void (*kernel)(KArgs...), int grid, int block, cudaStream_t st, Args&&... args)
+{
+  return launch_k(true, kernel, grid, block, st, std::forward<Args>(args)...);
+}
+
 struct CgScalars {
-  double rz, alpha, beta, rr, bb, tol2, pq, pad;
+  double rz, alpha, beta, rr, bb, tol2, pq, rz_prev;
+  double rr_anchor, delta2, pad[2];  // reliable updates: r.r at the last anchor, trigger ratio^2 (0 = off)
   int32_t done, iter, maxit, pad2;
   uint32_t ticket[4];
 };
+// done: 0 running, 1 converged (recursive residual), 2 breakdown (p.Ap <= 0),
+// 3 maxit, 5 pause for a reliable update
 
 // ------------------------------------------------------------ launch shape --
 // GB300 issues FP64 at ~1/60 of its FP32 rate, below the rate at which HBM
-// delivers doubles, so FP64 kernels are shaped to issue few FP64 operations per
-// entry: 2 lanes x 8 entries per CSR row (one FP64 shuffle-add per lane) and
+// delivers doubles, so FP64 kernels are shaped to issue as few FP64 operations
+// per entry as possible: one thread per CSR row (one FMA per entry, no
+// shuffle-adds) with 16 entries loaded per pass and two accumulators, and
 // several vector entries per thread (the block reduction tree is paid once per
-// thread).  FP32 kernels use 4 lanes x 4 entries and more threads.
+// thread).  FP32 kernels use 4 lanes x 4 entries per row and more threads.
 static int sm_count()
 {
   static int sms = 0;
@@ -57,27 +94,52 @@ static int sm_count()
   return sms;
 }
 
-template <typename V> constexpr int kEntriesPerLane = sizeof(V) == 8 ? 8 : 4;
+template <typename V> constexpr int kEntriesPerLane = sizeof(V) == 8 ? 16 : 4;
 
-// Lanes per row: the smallest group whose pass covers the mean row length.
+// Lanes per row of the standalone SpMV: one for FP64; for FP32 the smallest
+// group whose pass covers the mean row length.
 template <typename V>
 static int row_group(const mg_plan* p)
 {
+  if (sizeof(V) == 8) return 1;
   const double mean = p->ndof > 0 ? (double)p->nnz / (double)p->ndof : 1.0;
   const int U = kEntriesPerLane<V>;
-  for (int g = sizeof(V) == 8 ? 2 : 4; g < 32; g *= 2)
+  for (int g = 4; g < 32; g *= 2)
     if (mean <= g * U) return g;
   return 32;
 }
 
-// CTAs of a row kernel (G lanes per row) and of a vector kernel.
+// CTAs of a row kernel with G lanes per row, at most `per_sm` per SM.
+static int row_blocks(const mg_plan* p, int G, int per_sm)
+{
+  const int64_t need = (p->ndof * G + kSolveThreads - 1) / kSolveThreads;
+  const int cap = per_sm * sm_count();
+  return (int)std::max<int64_t>(1, std::min<int64_t>({need, (int64_t)cap, (int64_t)kMaxSolveBlocks}));
+}
 template <typename V>
 static int row_blocks(const mg_plan* p, int G)
 {
-  const int64_t need = (p->ndof * G + kSolveThreads - 1) / kSolveThreads;
-  const int cap = (sizeof(V) == 8 ? 4 : 8) * sm_count();
-  return (int)std::max<int64_t>(1, std::min<int64_t>({need, (int64_t)cap, (int64_t)kMaxSolveBlocks}));
+  return row_blocks(p, G, 8);
 }
+
+// Shape of the CG kernels (measured on GB300 at 64^3 P1 and 32^3 / 48^3 P2):
+// FP64 rows by 2 lanes x 8 entries (the FP64 pipe bounds K1), at most 4 CTAs
+// per SM (fewer partials for the last CTA to sum), launched without
+// programmatic dependent launch (it slowed the FP64 iteration); FP32 as the
+// standalone SpMV, with programmatic dependent launch.
+template <typename V> struct CgShape {
+  static constexpr int U = sizeof(V) == 8 ? 8 : kEntriesPerLane<V>;
+  static constexpr bool pdl = sizeof(V) == 4;
+  static int group(const mg_plan* p)
+  {
+    const double mean = p->ndof > 0 ? (double)p->nnz / (double)p->ndof : 1.0;
+    for (int g = sizeof(V) == 8 ? 2 : 4; g < 32; g *= 2)
+      if (mean <= g * U) return g;
+    return 32;
+  }
+  static int blocks(const mg_plan* p, int G) { return row_blocks(p, G, sizeof(V) == 8 ? 4 : 8); }
+};
+
 template <typename V>
 static int vec_blocks(int64_t n)
 {
@@ -101,14 +163,15 @@ __device__ __forceinline__ unsigned group_mask()
 // U independent loads of (column, value) per lane before any gather of x, so
 // every lane keeps U requests in flight; the G partial sums are combined by xor
 // shuffles in a fixed order.
-template <typename V, int G>
+// Entries u of a pass alternate between two accumulators (halving the chain of
+// dependent FMAs), added at the end.
+template <typename V, int G, int U = kEntriesPerLane<V>>
 __device__ __forceinline__ V row_dot(int64_t row, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
                                      const V* __restrict__ val, const V* __restrict__ x)
 {
-  constexpr int U = kEntriesPerLane<V>;
   const int lane = threadIdx.x & (G - 1);
   const int s0 = __ldg(rp + row), s1 = __ldg(rp + row + 1);
-  V sum = V(0);
+  V sa = V(0), sb = V(0);
   for (int base = s0 + lane; base < s1; base += G * U) {
     int c[U];
     V v[U];
@@ -119,9 +182,13 @@ __device__ __forceinline__ V row_dot(int64_t row, const int32_t* __restrict__ rp
       v[u] = s < s1 ? __ldg(val + s) : V(0);
     }
 #pragma unroll
-    for (int u = 0; u < U; ++u)
-      if (c[u] >= 0) sum += v[u] * __ldg(x + c[u]);
+    for (int u = 0; u < U; ++u) {
+      const V xv = c[u] >= 0 ? __ldg(x + c[u]) : V(0);
+      if (u & 1) sb = fma(v[u], xv, sb);
+      else sa = fma(v[u], xv, sa);
+    }
   }
+  V sum = sa + sb;
 #pragma unroll
   for (int off = G / 2; off > 0; off >>= 1) sum += __shfl_xor_sync(group_mask<G>(), sum, off, G);
   return sum;
@@ -200,6 +267,8 @@ __global__ void __launch_bounds__(kSolveThreads) k_spmv(int64_t n, const int32_t
                                                         const int32_t* __restrict__ ci, const V* __restrict__ val,
                                                         const V* __restrict__ x, V* __restrict__ y)
 {
+  pdl_wait();
+  pdl_trigger();
   const int64_t groups = (int64_t)gridDim.x * (kSolveThreads / G);
   for (int64_t row = (blockIdx.x * (int64_t)kSolveThreads + threadIdx.x) / G; row < n; row += groups) {
     const V s = row_dot<V, G>(row, rp, ci, val, x);
@@ -226,11 +295,13 @@ __global__ void __launch_bounds__(kSolveThreads) k_cg_spmv(int64_t n, const int3
   using D = Dot<V>;
   __shared__ typename D::A sh[32];
   __shared__ double shd[32];
+  pdl_wait();
+  pdl_trigger();
   if (s->done) return;
   const int64_t groups = (int64_t)gridDim.x * (kSolveThreads / G);
   typename D::A acc = D::zero();
   for (int64_t row = (blockIdx.x * (int64_t)kSolveThreads + threadIdx.x) / G; row < n; row += groups) {
-    const V v = row_dot<V, G>(row, rp, ci, val, p);
+    const V v = row_dot<V, G, CgShape<V>::U>(row, rp, ci, val, p);
     if ((threadIdx.x & (G - 1)) == 0) {
       q[row] = v;
       D::mac(acc, p[row], v);
@@ -259,6 +330,8 @@ __global__ void __launch_bounds__(kSolveThreads) k_cg_update(int64_t n, V* __res
   using D = Dot<V>;
   __shared__ typename D::A sh[32];
   __shared__ double shd[32];
+  pdl_wait();
+  pdl_trigger();
   if (s->done) return;
   const V alpha = (V)s->alpha;
   typename D::A prz = D::zero(), prr = D::zero();
@@ -283,12 +356,14 @@ __global__ void __launch_bounds__(kSolveThreads) k_cg_update(int64_t n, V* __res
     const double rz = reduce_partials(partials, gridDim.x, shd);
     const double rr = reduce_partials(partials + gridDim.x, gridDim.x, shd);
     if (threadIdx.x == 0) {
+      s->rz_prev = s->rz;
       s->beta = rz / s->rz;
       s->rz = rz;
       s->rr = rr;
       s->iter += 1;
       if (rr <= s->tol2 * s->bb) s->done = 1;
       else if (s->iter >= s->maxit) s->done = 3;
+      else if (rr <= s->delta2 * s->rr_anchor) s->done = 5;  // K3 is skipped: the host re-anchors first
       s->ticket[1] = 0;
     }
   }
@@ -299,6 +374,8 @@ template <typename V>
 __global__ void __launch_bounds__(kSolveThreads) k_cg_dir(int64_t n, const V* __restrict__ z, V* __restrict__ p,
                                                           const CgScalars* s)
 {
+  pdl_wait();
+  pdl_trigger();
   if (s->done) return;
   const V beta = (V)s->beta;
 #pragma unroll 4
@@ -324,7 +401,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_cg_start(int64_t n, const int
   typename D::A prz = D::zero(), prr = D::zero(), pbb = D::zero();
   for (int64_t row = (blockIdx.x * (int64_t)kSolveThreads + threadIdx.x) / G; row < n; row += groups) {
     V ax = V(0);
-    if (!zero_x) ax = row_dot<V, G>(row, rp, ci, val, x);
+    if (!zero_x) ax = row_dot<V, G, CgShape<V>::U>(row, rp, ci, val, x);
     if ((threadIdx.x & (G - 1)) == 0) {
       const V dv = val[diag[row]];
       const V di = (jacobi && dv != V(0)) ? V(1) / dv : V(1);
@@ -374,7 +451,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_residual64(int64_t n, const i
   const int64_t groups = (int64_t)gridDim.x * (kSolveThreads / G);
   double prr = 0.0, pbb = 0.0;
   for (int64_t row = (blockIdx.x * (int64_t)kSolveThreads + threadIdx.x) / G; row < n; row += groups) {
-    const double ax = row_dot<double, G>(row, rp, ci, val, x);
+    const double ax = row_dot<double, G, CgShape<double>::U>(row, rp, ci, val, x);
     if ((threadIdx.x & (G - 1)) == 0) {
       const double ri = b[row] - ax;
       r[row] = ri;
@@ -406,10 +483,53 @@ __global__ void k_scale_cast(int64_t n, const double* r, double scale, float* r3
   }
 }
 
-__global__ void k_correct(int64_t n, double* x, const float* d32, double scale)
+// Reliable update, part 1: x64 += x32, x32 = 0.
+__global__ void k_anchor_x(int64_t n, double* __restrict__ x, float* __restrict__ x32)
 {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    x[i] += scale * (double)d32[i];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] += (double)x32[i];
+    x32[i] = 0.0f;
+  }
+}
+
+// Reliable update, part 2 (after r64 = b - A64 x): r32 = r64, z32 = D^-1 r32,
+// r.z and r.r of the replaced residual; the last CTA forms beta with the r.z
+// of the iteration that paused, re-anchors and resumes (K3 then runs).
+__global__ void __launch_bounds__(kSolveThreads) k_anchor_r(int64_t n, const double* __restrict__ r64,
+                                                            float* __restrict__ r, float* __restrict__ z,
+                                                            const float* __restrict__ dinv, double* partials,
+                                                            CgScalars* s)
+{
+  using D = Dot<float>;
+  __shared__ D::A sh[32];
+  __shared__ double shd[32];
+  D::A prz = D::zero(), prr = D::zero();
+  for (int64_t i = blockIdx.x * (int64_t)kSolveThreads + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * kSolveThreads) {
+    const float ri = (float)r64[i];
+    const float zi = dinv[i] * ri;
+    r[i] = ri;
+    z[i] = zi;
+    D::mac(prz, ri, zi);
+    D::mac(prr, ri, ri);
+  }
+  const double b1 = block_sum<float>(prz, sh), b2 = block_sum<float>(prr, sh);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = b1;
+    partials[gridDim.x + blockIdx.x] = b2;
+  }
+  if (last_block(&s->ticket[1])) {
+    const double rz = reduce_partials(partials, gridDim.x, shd);
+    const double rr = reduce_partials(partials + gridDim.x, gridDim.x, shd);
+    if (threadIdx.x == 0) {
+      s->beta = rz / s->rz_prev;
+      s->rz = rz;
+      s->rr = rr;
+      s->rr_anchor = rr;
+      s->done = 0;
+      s->ticket[1] = 0;
+    }
+  }
 }
 
 #define MG_DISPATCH_G(G, ...)                                \
@@ -418,7 +538,8 @@ __global__ void k_correct(int64_t n, double* x, const float* d32, double scale)
     case 16: { constexpr int g = 16; __VA_ARGS__; } break;   \
     case 8: { constexpr int g = 8; __VA_ARGS__; } break;     \
     case 4: { constexpr int g = 4; __VA_ARGS__; } break;     \
-    default: { constexpr int g = 2; __VA_ARGS__; } break;    \
+    case 2: { constexpr int g = 2; __VA_ARGS__; } break;     \
+    default: { constexpr int g = 1; __VA_ARGS__; } break;    \
   }
 
 mg_status launch_spmv(mg_plan* p, int prec, const void* vals, const void* x, void* y, cudaStream_t st)
@@ -429,14 +550,12 @@ mg_status launch_spmv(mg_plan* p, int prec, const void* vals, const void* x, voi
   MG_TRY(plan_device(p));
   if (prec == MG_F64) {
     const int G = row_group<double>(p), nb = row_blocks<double>(p, G);
-    MG_DISPATCH_G(G, (k_spmv<double, g><<<nb, kSolveThreads, 0, st>>>(p->ndof, p->d_rowptr, p->d_colind,
-                                                                         (const double*)vals, (const double*)x,
-                                                                         (double*)y)));
+    MG_DISPATCH_G(G, (launch_pdl(k_spmv<double, g>, nb, kSolveThreads, st, p->ndof, (const int32_t*)p->d_rowptr,
+                                 (const int32_t*)p->d_colind, (const double*)vals, (const double*)x, (double*)y)));
   } else {
     const int G = row_group<float>(p), nb = row_blocks<float>(p, G);
-    MG_DISPATCH_G(G, (k_spmv<float, g><<<nb, kSolveThreads, 0, st>>>(p->ndof, p->d_rowptr, p->d_colind,
-                                                                        (const float*)vals, (const float*)x,
-                                                                        (float*)y)));
+    MG_DISPATCH_G(G, (launch_pdl(k_spmv<float, g>, nb, kSolveThreads, st, p->ndof, (const int32_t*)p->d_rowptr,
+                                 (const int32_t*)p->d_colind, (const float*)vals, (const float*)x, (float*)y)));
   }
   MG_CUDA(cudaGetLastError());
   return MG_OK;
@@ -500,11 +619,13 @@ static mg_status cg_iterate(mg_plan* p, const V* vals, V* x, CgWork<V>& w, int G
   cudaStreamCaptureStatus cs;
   MG_CUDA(cudaStreamIsCapturing(st, &cs));
   if (cs != cudaStreamCaptureStatusNone || st == nullptr) use_graph = false;  // no nested capture; legacy stream cannot capture
+  constexpr bool pdl = CgShape<V>::pdl;
   auto body = [&]() {
-    MG_DISPATCH_G(G, (k_cg_spmv<V, g><<<nb, kSolveThreads, 0, st>>>(n, p->d_rowptr, p->d_colind, vals, w.p, w.q,
-                                                                      w.partials, w.s)));
-    k_cg_update<V><<<vb, kSolveThreads, 0, st>>>(n, x, w.r, w.z, w.p, w.q, w.dinv, w.partials, w.s);
-    k_cg_dir<V><<<vb, kSolveThreads, 0, st>>>(n, w.z, w.p, w.s);
+    MG_DISPATCH_G(G, (launch_k(pdl, k_cg_spmv<V, g>, nb, kSolveThreads, st, n, (const int32_t*)p->d_rowptr,
+                               (const int32_t*)p->d_colind, vals, (const V*)w.p, w.q, w.partials, w.s)));
+    launch_k(pdl, k_cg_update<V>, vb, kSolveThreads, st, n, x, w.r, w.z, (const V*)w.p, (const V*)w.q,
+             (const V*)w.dinv, w.partials, w.s);
+    launch_k(pdl, k_cg_dir<V>, vb, kSolveThreads, st, n, (const V*)w.z, w.p, (const CgScalars*)w.s);
   };
   if (use_graph) {
     MG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -604,7 +725,7 @@ mg_status mg_cg_solve_noalloc(mg_plan* p, const double* d_values, const double* 
   MG_TRY(noalloc_scratch(&base));
   cudaStream_t st = (cudaStream_t)stream;
   CgWork<double> w = cg_work_carve<double>(base, p->ndof);
-  const int G = row_group<double>(p), nb = row_blocks<double>(p, G);
+  const int G = CgShape<double>::group(p), nb = CgShape<double>::blocks(p, G);
   const int64_t n = p->ndof;
   const int vb = vec_blocks<double>(n);
   const auto t0 = std::chrono::steady_clock::now();
@@ -613,10 +734,12 @@ mg_status mg_cg_solve_noalloc(mg_plan* p, const double* d_values, const double* 
   CgScalars hs{};
   for (int launched = 0;; launched += kGraphIters) {
     for (int k = 0; k < kGraphIters; ++k) {
-      MG_DISPATCH_G(G, (k_cg_spmv<double, g><<<nb, kSolveThreads, 0, st>>>(n, p->d_rowptr, p->d_colind, d_values,
-                                                                              w.p, w.q, w.partials, w.s)));
-      k_cg_update<double><<<vb, kSolveThreads, 0, st>>>(n, d_x, w.r, w.z, w.p, w.q, w.dinv, w.partials, w.s);
-      k_cg_dir<double><<<vb, kSolveThreads, 0, st>>>(n, w.z, w.p, w.s);
+      constexpr bool pdl = CgShape<double>::pdl;
+      MG_DISPATCH_G(G, (launch_k(pdl, k_cg_spmv<double, g>, nb, kSolveThreads, st, n, (const int32_t*)p->d_rowptr,
+                                 (const int32_t*)p->d_colind, d_values, (const double*)w.p, w.q, w.partials, w.s)));
+      launch_k(pdl, k_cg_update<double>, vb, kSolveThreads, st, n, d_x, w.r, w.z, (const double*)w.p,
+               (const double*)w.q, (const double*)w.dinv, w.partials, w.s);
+      launch_k(pdl, k_cg_dir<double>, vb, kSolveThreads, st, n, (const double*)w.z, w.p, (const CgScalars*)w.s);
     }
     MG_CUDA(cudaGetLastError());
     MG_CUDA(cudaMemcpyAsync(&hs, w.s, sizeof(CgScalars), cudaMemcpyDeviceToHost, st));
@@ -653,7 +776,7 @@ mg_status mg_cg_solve(mg_plan* p, const double* d_values, const double* d_b, dou
   void* base = nullptr;
   MG_TRY(plan_work(p, cg_work_bytes<double>(p->ndof), &base));
   CgWork<double> w = cg_work_carve<double>(base, p->ndof);
-  const int G = row_group<double>(p), nb = row_blocks<double>(p, G);
+  const int G = CgShape<double>::group(p), nb = CgShape<double>::blocks(p, G);
   cudaEvent_t e0, e1;
   MG_CUDA(cudaEventCreate(&e0));
   MG_CUDA(cudaEventCreate(&e1));
@@ -687,50 +810,79 @@ mg_status mg_cg_refined(mg_plan* p, const double* d_values64, const float* d_val
 {
   if (!p || !d_values64 || !d_values32 || !d_b || !d_x)
     return set_error(MG_ERR_INVALID_ARG, "mg_cg_refined: null argument");
-  if (!(rtol > 0.0) || !(inner_rtol > 0.0) || max_outer < 1 || max_inner < 1)
+  if (!(rtol > 0.0) || !(inner_rtol > 0.0) || !(inner_rtol < 1.0) || max_outer < 1 || max_inner < 1)
     return set_error(MG_ERR_INVALID_ARG, "mg_cg_refined: bad tolerance or iteration limits");
   MG_TRY(plan_device(p));
   cudaStream_t st = (cudaStream_t)stream;
   const int64_t n = p->ndof;
-  // layout: [CgWork<float>][r64][d32][r32]
+  // layout: [CgWork<float>][r64][x32][scalars of the FP64 residual]
   const size_t wbytes = cg_work_bytes<float>(n);
   const size_t v64 = ((size_t)n * 8 + 255) / 256 * 256, v32 = ((size_t)n * 4 + 255) / 256 * 256;
   void* base = nullptr;
-  MG_TRY(plan_work(p, wbytes + v64 + 2 * v32, &base));
+  MG_TRY(plan_work(p, wbytes + v64 + v32 + 256, &base));
   CgWork<float> w = cg_work_carve<float>(base, n);
   double* r64 = (double*)((char*)base + wbytes);
-  float* d32 = (float*)((char*)r64 + v64);
-  float* r32 = (float*)((char*)d32 + v32);
-  const int G64 = row_group<double>(p), nb64 = row_blocks<double>(p, G64);
-  const int G = row_group<float>(p), nb = row_blocks<float>(p, G);
+  float* x32 = (float*)((char*)r64 + v64);
+  CgScalars* s64 = (CgScalars*)((char*)x32 + v32);
+  const int G64 = CgShape<double>::group(p), nb64 = CgShape<double>::blocks(p, G64);
+  const int G = CgShape<float>::group(p), nb = CgShape<float>::blocks(p, G);
   const int eb = vec_blocks<float>(n);
   CgScalars* hs = reinterpret_cast<CgScalars*>(p->h_pinned);
-  MG_CUDA(cudaMemsetAsync(w.s, 0, sizeof(CgScalars), st));
   cudaEvent_t e0, e1;
   MG_CUDA(cudaEventCreate(&e0));
   MG_CUDA(cudaEventCreate(&e1));
   MG_CUDA(cudaEventRecord(e0, st));
-  int outer = 0, inner_total = 0;
+  int anchors = 0, inner = 0;
   bool converged = false;
-  double relres = INFINITY;
+  double relres = INFINITY, bb64 = 1.0;
   mg_status s = MG_OK;
-  for (; outer <= max_outer; ++outer) {
+  // FP64 residual of the current x (into r64, s64->rr, s64->bb)
+  auto residual64 = [&]() -> mg_status {
+    MG_CUDA(cudaMemsetAsync(s64, 0, sizeof(CgScalars), st));
     MG_DISPATCH_G(G64, (k_residual64<g><<<nb64, kSolveThreads, 0, st>>>(n, p->d_rowptr, p->d_colind, d_values64,
-                                                                          d_b, d_x, r64, w.partials, w.s)));
-    cudaError_t e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaMemcpyAsync(hs, w.s, sizeof(CgScalars), cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) { s = cuda_error(e, "refinement residual"); break; }
+                                                                          d_b, d_x, r64, w.partials, s64)));
+    MG_CUDA(cudaGetLastError());
+    MG_CUDA(cudaMemcpyAsync(hs, s64, sizeof(CgScalars), cudaMemcpyDeviceToHost, st));
+    MG_CUDA(cudaStreamSynchronize(st));
+    bb64 = hs->bb;
     relres = std::sqrt(hs->rr / hs->bb);
-    if (relres <= rtol) { converged = true; break; }
-    if (outer == max_outer) break;
-    const double rn = std::sqrt(hs->rr);
-    k_scale_cast<<<eb, 256, 0, st>>>(n, r64, 1.0 / rn, r32, d32);
-    s = cg_start<float>(p, d_values32, r32, d32, 1, precond == MG_PREC_JACOBI, inner_rtol, max_inner, w, G, nb, st);
-    if (s == MG_OK) s = cg_iterate<float>(p, d_values32, d32, w, G, nb, max_inner, st, hs);
-    if (s != MG_OK) break;
-    inner_total += hs->iter;
-    k_correct<<<eb, 256, 0, st>>>(n, d_x, d32, rn);
+    return MG_OK;
+  };
+  s = residual64();
+  if (s == MG_OK && relres <= rtol) converged = true;
+  if (s == MG_OK && !converged) {
+    // first anchor: a plain FP32 CG start on r32 = r64 (x32 = 0), then the
+    // target and the reliable-update trigger in its scalars
+    k_scale_cast<<<eb, 256, 0, st>>>(n, r64, 1.0, w.r, x32);
+    s = cg_start<float>(p, d_values32, w.r, x32, 1, precond == MG_PREC_JACOBI, 1.0, max_inner, w, G, nb, st);
+    if (s == MG_OK) {
+      MG_CUDA(cudaMemcpyAsync(hs, w.s, sizeof(CgScalars), cudaMemcpyDeviceToHost, st));
+      MG_CUDA(cudaStreamSynchronize(st));
+      hs->bb = 1.0;
+      hs->tol2 = rtol * rtol * bb64;  // recursive-residual target: ||r|| <= rtol ||b||
+      hs->rr_anchor = hs->rr;
+      hs->delta2 = inner_rtol * inner_rtol;
+      hs->done = 0;
+      MG_CUDA(cudaMemcpyAsync(w.s, hs, sizeof(CgScalars), cudaMemcpyHostToDevice, st));
+    }
+    while (s == MG_OK) {
+      s = cg_iterate<float>(p, d_values32, x32, w, G, nb, max_inner, st, hs);
+      if (s != MG_OK) break;
+      inner = hs->iter;
+      const int why = hs->done;
+      if (why == 2) { s = set_error(MG_ERR_NOT_CONVERGED, "refined CG breakdown: p.Ap <= 0"); break; }
+      // anchor: x += x32, r64 = b - A64 x
+      k_anchor_x<<<eb, 256, 0, st>>>(n, d_x, x32);
+      ++anchors;
+      s = residual64();
+      if (s != MG_OK) break;
+      if (relres <= rtol) { converged = true; break; }
+      if (why == 3 || anchors >= max_outer) break;
+      // replace the FP32 residual, keep the direction, resume
+      k_anchor_r<<<eb, kSolveThreads, 0, st>>>(n, r64, w.r, w.z, w.dinv, w.partials, w.s);
+      launch_k(false, k_cg_dir<float>, eb, kSolveThreads, st, n, (const float*)w.z, w.p, (const CgScalars*)w.s);
+      MG_CUDA(cudaGetLastError());
+    }
   }
   MG_CUDA(cudaEventRecord(e1, st));
   MG_CUDA(cudaEventSynchronize(e1));
@@ -740,13 +892,13 @@ mg_status mg_cg_refined(mg_plan* p, const double* d_values64, const float* d_val
   cudaEventDestroy(e1);
   if (s != MG_OK) return s;
   if (info) {
-    info->iterations = inner_total;
-    info->outer_iterations = outer;
+    info->iterations = inner;
+    info->outer_iterations = anchors;
     info->converged = converged;
     info->rel_residual = relres;
     info->seconds = ms * 1e-3;
   }
-  if (!converged) return set_error(MG_ERR_NOT_CONVERGED, "refinement reached max_outer");
+  if (!converged) return set_error(MG_ERR_NOT_CONVERGED, "refined CG: no convergence within max_outer / max_inner");
   return MG_OK;
 }
 
