@@ -70,6 +70,19 @@ def workload_config(a, E, N, nnz):
             "l2": "flushed before every step (256 MB write)", "parallelism": f"replicas x{a.gpus}"}
 
 
+def profiled_traffic(kernel):
+    """DRAM bytes per launch of `kernel` inside the step, from the committed ncu summary of the step"""
+    p = os.path.join(ROOT, "profiles", "launches_step_p1_64cube.md")
+    try:
+        for line in open(p):
+            f = line.split()
+            if len(f) == 3 and f[0] == "traffic_bytes_per_launch" and f[1] == kernel:
+                return float(f[2]), "profiles/launches_step_p1_64cube.md (ncu --cache-control none, mean over the step's launches)"
+    except OSError:
+        pass
+    return None, "no committed ncu capture for this kernel"
+
+
 def asm_bytes(E, nv, nnz, sv, nb=4):
     """algorithmic bytes of one assembly: E (16 conn + 8 kappa + 4 nb^2 slot map) + 24 n_v + s_v nnz"""
     return E * (16 + 8 + 4 * nb * nb) + 24 * nv + sv * nnz
@@ -613,10 +626,14 @@ def main():
 
         dom = "assembly_f64" if statistics.median(t_asm) >= N_SPMV * ts64_warm else "spmv_f64_in_step"
         rl = extras[dom]
-        roofline = {"bound": "hbm", "kernel": "k_assemble<1,double>" if dom == "assembly_f64" else "k_spmv<double,16>",
+        kname = "k_assemble<1,kDW>" if dom == "assembly_f64" else "k_spmv<double,1>"
+        traffic, tnote = profiled_traffic(kname)
+        roofline = {"bound": "hbm", "kernel": kname,
                     "achieved": rl["gbs"], "peak": peak, "unit": "GB/s", "frac": rl["gbs"] / peak,
                     "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
-                    "traffic": None}
+                    "traffic": traffic, "traffic_note": tnote,
+                    "note": "achieved = algorithmic bytes per launch / CUDA-event time per launch in the step; "
+                            "the step's SpMVs are served from L2 (traffic = DRAM bytes per launch)"}
         clocks = clk.summary()
         line = {"metric": METRIC, "value": value, "unit": "tets/s", "n_gpus": world, "steps": a.steps,
                 "warmup": a.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",

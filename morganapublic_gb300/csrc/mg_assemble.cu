@@ -873,35 +873,52 @@ __global__ void k_dirichlet(int64_t ndof, const int32_t* rowptr, const int32_t* 
 // stiffness of element e (symmetric).  Double-word arithmetic on the FP32
 // pipes; u and lambda are FP64 and enter as double-word values.
 template <int ORDER>
-__global__ void __launch_bounds__(256) k_adjoint(int64_t n_elem, const int4* conn, const int32_t* dofs, GeoPtrs geo,
-                                                 const double* tables, double wsum, const double* u,
+// Elements are visited along a Morton curve of their centroids (elem_order,
+// dofs_m = their dofs in that order), so neighbouring threads gather
+// neighbouring vertices and dof values.
+__global__ void __launch_bounds__(256) k_adjoint(int64_t n_elem, const int32_t* elem_order, const int32_t* dofs_m,
+                                                 GeoPtrs geo, const double* tables, double wsum, const double* u,
                                                  const double* lam, double* grad)
 {
   constexpr int NB = ORDER == 1 ? 4 : 10, NU = ORDER == 1 ? 10 : 55;
   __shared__ ff tab[6 * NU];
   for (int i = threadIdx.x; i < 6 * NU; i += blockDim.x) tab[i] = ff_from_double(tables[i]);
   __syncthreads();
-  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (e >= n_elem) return;
-  const int4 n = conn[e];
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n_elem) return;
+  const int64_t e = elem_order[i];
+  const int32_t* dofs = dofs_m + i * NB;  // this element's dofs; the first four are its vertices
+  const int4 n = ORDER == 1 ? reinterpret_cast<const int4*>(dofs_m)[i] : make_int4(dofs[0], dofs[1], dofs[2], dofs[3]);
   Cof<ff> f;
   geometry_now<kDW>(geo, n, f);
-  ff ue[NB], le[NB];
-#pragma unroll
-  for (int i = 0; i < NB; ++i) {
-    const int dof = dofs[e * NB + i];
-    ue[i] = ff_from_double(u[dof]);
-    le[i] = ff_from_double(lam[dof]);
-  }
   ff s = ff_make(0.0f);
   if (ORDER == 1) {
-    ff K[10];
-    p1_stiff_unique<ff>(f, ff_from_double(wsum) / f.det, K);
+    // K has zero row sums: lambda^T K u = (wsum / det) (sum_b dl_b C_b) . (sum_b du_b C_b)
+    // with du_b = u_{b+1} - u_0 (FP64 differences, exact for nearby values) and
+    // C_b the cofactor columns
+    const int id[4] = {n.x, n.y, n.z, n.w};
+    const double u0 = u[id[0]], l0 = lam[id[0]];
+    ff gu[3], gl[3];
+    for (int r = 0; r < 3; ++r) gu[r] = gl[r] = ff_make(0.0f);
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int b = 0; b < 3; ++b) {
+      const ff du = ff_from_double_bits(u[id[b + 1]] - u0);
+      const ff dl = ff_from_double_bits(lam[id[b + 1]] - l0);
 #pragma unroll
-      for (int j = 0; j < 4; ++j) s = s + le[j] * K[sym_index(i, j, 4)] * ue[i];
+      for (int r = 0; r < 3; ++r) {
+        gu[r] = gu[r] + du * f.c[r][b];
+        gl[r] = gl[r] + dl * f.c[r][b];
+      }
+    }
+    s = ff_dot3(gl, gu) * (ff_from_double_bits(wsum) / f.det);
   } else {
+    ff ue[NB], le[NB];
+#pragma unroll
+    for (int i = 0; i < NB; ++i) {
+      const int dof = dofs[i];
+      ue[i] = ff_from_double_bits(u[dof]);
+      le[i] = ff_from_double_bits(lam[dof]);
+    }
     ff g[6];
     metric<ff>(f, ff_make(1.0f) / f.det, g);
     for (int i = 0; i < NB; ++i) {
@@ -916,7 +933,7 @@ __global__ void __launch_bounds__(256) k_adjoint(int64_t n_elem, const int4* con
       s = s + row * ue[i];
     }
   }
-  grad[e] = -ff_to_double(s);
+  grad[e] = -ff_to_double_bits(s);
 }
 
 }  // namespace mg
@@ -1018,11 +1035,11 @@ mg_status mg_adjoint_grad(mg_plan* p, const double* d_u, const double* d_lambda,
   const GeoPtrs geo{m->d_xyz, m->d_node_rec, m->d_lo_z};
   if (blocks > 0) {
     if (m->order == 1)
-      k_adjoint<1><<<blocks, threads, 0, st>>>(m->n_elem, m->d_conn, m->d_dofs, geo, d_tab, t->wsum, d_u, d_lambda,
-                                               d_grad);
+      k_adjoint<1><<<blocks, threads, 0, st>>>(m->n_elem, p->d_elem_order, p->d_dofs_morton, geo, d_tab, t->wsum,
+                                               d_u, d_lambda, d_grad);
     else
-      k_adjoint<2><<<blocks, threads, 0, st>>>(m->n_elem, m->d_conn, m->d_dofs, geo, d_tab, t->wsum, d_u, d_lambda,
-                                               d_grad);
+      k_adjoint<2><<<blocks, threads, 0, st>>>(m->n_elem, p->d_elem_order, p->d_dofs_morton, geo, d_tab, t->wsum,
+                                               d_u, d_lambda, d_grad);
   }
   MG_CUDA(cudaGetLastError());
   return MG_OK;

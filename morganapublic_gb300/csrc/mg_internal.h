@@ -153,6 +153,8 @@ struct mg_plan {
   int32_t max_rec_bytes = 0;
   int32_t max_chunk_nodes = 0;
   int2* d_row_meta = nullptr;  // owned rows, schedule order: (accumulator base, CSR start - base)
+  int32_t* d_elem_order = nullptr;  // elements along a Morton curve of their centroids
+  int32_t* d_dofs_morton = nullptr; // their dofs (nb each) in that order
   uint32_t* d_entries = nullptr;   // contribution words
   uint32_t* d_counters = nullptr;   // [0] work counter, [1] exit counter, [2] device error, [3] detail
   int64_t max_chunk_entries = 0;
@@ -186,6 +188,7 @@ struct HostSchedule {
   std::vector<int32_t> chunk_node_begin, chunk_n_nodes;
   std::vector<int32_t> chunk_nodes;  // global node ids
   std::vector<uint16_t> item_lconn;  // 4 per item slot
+  std::vector<int32_t> elem_order;   // all elements along a Morton curve of their centroids
   int32_t max_chunk_nodes = 0;
 };
 mg_status mesh_device(mg_mesh* m);  // uploads the mesh on first GPU use

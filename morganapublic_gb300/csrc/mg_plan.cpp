@@ -247,6 +247,12 @@ static mg_status build_schedule(mg_plan* p, HostSchedule* hs)
       std::sort(hs->items.begin() + bcount[b], hs->items.begin() + bcount[b + 1], [&](int32_t x, int32_t y) {
         return ekey[x] != ekey[y] ? ekey[x] < ekey[y] : x < y;
       });
+    // the same order over all elements, for the per-element kernels (adjoint)
+    hs->elem_order.resize(E);
+    std::iota(hs->elem_order.begin(), hs->elem_order.end(), 0);
+    std::sort(hs->elem_order.begin(), hs->elem_order.end(), [&](int32_t x, int32_t y) {
+      return ekey[x] != ekey[y] ? ekey[x] < ekey[y] : x < y;
+    });
     std::vector<int32_t> padded;
     padded.reserve(hs->items.size() + 4 * (size_t)nbk);
     for (int32_t b = 0; b < nbk; ++b) {
@@ -488,6 +494,15 @@ mg_status plan_device(mg_plan* p)
   MG_TRY(upload(&p->d_blocks, hs.blocks));
   MG_TRY(upload(&p->d_entries, hs.entries));
   {
+    const int nb = p->mesh->nb;
+    std::vector<int32_t> dm((size_t)hs.elem_order.size() * nb);
+#pragma omp parallel for
+    for (int64_t i = 0; i < (int64_t)hs.elem_order.size(); ++i)
+      for (int k = 0; k < nb; ++k) dm[i * nb + k] = p->mesh->dofs[(int64_t)hs.elem_order[i] * nb + k];
+    MG_TRY(upload(&p->d_elem_order, hs.elem_order));
+    MG_TRY(upload(&p->d_dofs_morton, dm));
+  }
+  {
     // owned-row metadata in schedule order, padded by two entries so that the
     // kernel's 16-byte aligned copies of a row range stay inside the array
     std::vector<int2> meta(hs.rows.size() + 2, make_int2(0, 0));
@@ -582,6 +597,8 @@ static void free_plan(mg_plan* p)
   cudaFree(p->d_chunk_data);
   cudaFree(p->d_chunk_rec);
   cudaFree(p->d_row_meta);
+  cudaFree(p->d_elem_order);
+  cudaFree(p->d_dofs_morton);
   cudaFree(p->d_entries);
   cudaFree(p->d_counters);
   for (double* t : p->d_tables) cudaFree(t);

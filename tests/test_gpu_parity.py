@@ -161,6 +161,43 @@ def test_cg_and_refined_vs_oracle(order):
     assert np.linalg.norm(r) <= 1.01e-10 * np.linalg.norm(rhs)
 
 
+def test_manufactured_p2_mixed_vs_fp64_against_oracle():
+    """The P2 mixed-precision workload in small: rhs = A u_I for the P2 interpolant
+    u_I of sin(pi x) sin(pi y) sin(pi z) (zero on the boundary, Dirichlet rows
+    eliminated), so u_I is the exact discrete solution.  FP64 CG and the
+    reliable-update mixed-precision CG (default trigger) both reach 1e-10; their
+    solutions are compared with the oracle's FP64 CG solution and with u_I, and
+    the FP32 Krylov sequence is not restarted (iterations close to FP64's)."""
+    n, quad = 5, 15
+    m, kappa = _case(n, 0.0, 11, False, 0.5)
+    mesh = mg.Mesh(m.xyz, m.conn, order=2)
+    b = mg.MatrixBuilder(mesh)
+    dofs, rp, ci, K = orc.full_operator("stiff_kappa", 2, quad, m.xyz, m.conn, coeff=kappa)
+    en = mesh.edges()[0]
+    mask = meshgen.p2_boundary(m.boundary, en)
+    X = np.concatenate([m.xyz, 0.5 * (m.xyz[en[:, 0]] + m.xyz[en[:, 1]])])
+    uI = np.sin(np.pi * X[:, 0]) * np.sin(np.pi * X[:, 1]) * np.sin(np.pi * X[:, 2])
+    uI[mask] = 0.0
+    orc.apply_dirichlet(rp, ci, mask, K)
+    rhs = orc.spmv(rp, ci, K, uI)
+    x_ref, it_ref, _, rc = orc.cg(rp, ci, K, rhs, rtol=1e-13)
+    assert rc == 0
+    v64 = b.assemble("stiff_kappa", coeff=kappa, quad=quad, prec="f64")
+    v32 = b.assemble("stiff_kappa", coeff=kappa, quad=quad, prec="f32")
+    mk = torch.from_numpy(mask)
+    b.apply_dirichlet(v64, mk)
+    b.apply_dirichlet(v32, mk)
+    bt = b.apply(v64, torch.from_numpy(uI).cuda())
+    assert np.max(np.abs(bt.cpu().numpy() - rhs)) <= 1e-12 * np.abs(rhs).max()
+    x, info = b.cg(v64, bt, rtol=1e-10)
+    xr, infor = b.cg_refined(v64, v32, bt, rtol=1e-10)
+    assert info.converged and infor.converged and infor.rel_residual <= 1e-10
+    for sol in (x.cpu().numpy(), xr.cpu().numpy()):
+        assert np.linalg.norm(sol - x_ref) / np.linalg.norm(x_ref) <= 1e-8
+        assert np.linalg.norm(sol - uI) / np.linalg.norm(uI) <= 1e-8
+    assert infor.iterations <= 1.5 * info.iterations + 20
+
+
 def test_cg_deterministic_and_maxit_status():
     m, kappa, mesh, b, dofs, rp, ci, K, mask, rhs, quad = _dirichlet_system(5, 1, 1.0, 6)
     v = b.assemble("stiff_kappa", coeff=kappa, quad=quad)
