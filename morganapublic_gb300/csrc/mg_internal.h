@@ -144,6 +144,7 @@ struct mg_plan {
   int32_t* d_rowptr = nullptr;
   int32_t* d_colind = nullptr;
   int32_t* d_diag = nullptr;  // slot of the diagonal entry of each row
+  int16_t* d_coloff = nullptr; // col - row of every entry when all fit in 16 bits (else null): SpMV index stream
   // assembly schedule
   int32_t nblocks = 0;
   int64_t n_items = 0, n_item_slots = 0, n_chunks = 0, n_entries = 0, n_contrib = 0;

@@ -491,6 +491,20 @@ mg_status plan_device(mg_plan* p)
     diag[r] = p->rowptr[r] + (int32_t)(std::lower_bound(c0, c1, (int32_t)r) - c0);
   }
   MG_TRY(upload(&p->d_diag, diag));
+  {
+    // 16-bit column offsets (col - row) when every entry fits: 2 bytes per entry
+    // less for the SpMV and CG kernels; the CSR arrays stay the reference's
+    bool fits = true;
+    std::vector<int16_t> off(p->colind.size());
+#pragma omp parallel for reduction(&& : fits)
+    for (int64_t r = 0; r < p->ndof; ++r)
+      for (int32_t k = p->rowptr[r]; k < p->rowptr[r + 1]; ++k) {
+        const int64_t d = (int64_t)p->colind[k] - r;
+        if (d < INT16_MIN || d > INT16_MAX) fits = false;
+        else off[k] = (int16_t)d;
+      }
+    if (fits && !off.empty()) MG_TRY(upload(&p->d_coloff, off));
+  }
   MG_TRY(upload(&p->d_blocks, hs.blocks));
   MG_TRY(upload(&p->d_entries, hs.entries));
   {
@@ -593,6 +607,7 @@ static void free_plan(mg_plan* p)
   cudaFree(p->d_rowptr);
   cudaFree(p->d_colind);
   cudaFree(p->d_diag);
+  cudaFree(p->d_coloff);
   cudaFree(p->d_blocks);
   cudaFree(p->d_chunk_data);
   cudaFree(p->d_chunk_rec);

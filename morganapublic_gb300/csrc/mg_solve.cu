@@ -165,8 +165,17 @@ __device__ __forceinline__ unsigned group_mask()
 // shuffles in a fixed order.
 // Entries u of a pass alternate between two accumulators (halving the chain of
 // dependent FMAs), added at the end.
-template <typename V, int G, int U = kEntriesPerLane<V>>
-__device__ __forceinline__ V row_dot(int64_t row, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+// Column of entry s of `row`: int32 columns, or 16-bit offsets col - row (the
+// plan's compressed index stream).
+template <typename I>
+__device__ __forceinline__ int column(const I* __restrict__ ci, int s, int64_t row)
+{
+  if constexpr (sizeof(I) == 2) return (int)row + (int)__ldg(ci + s);
+  else return __ldg(ci + s);
+}
+
+template <typename V, int G, int U = kEntriesPerLane<V>, typename I = int32_t>
+__device__ __forceinline__ V row_dot(int64_t row, const int32_t* __restrict__ rp, const I* __restrict__ ci,
                                      const V* __restrict__ val, const V* __restrict__ x)
 {
   const int lane = threadIdx.x & (G - 1);
@@ -178,7 +187,7 @@ __device__ __forceinline__ V row_dot(int64_t row, const int32_t* __restrict__ rp
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       const int s = base + u * G;
-      c[u] = s < s1 ? __ldg(ci + s) : -1;
+      c[u] = s < s1 ? column<I>(ci, s, row) : -1;
       v[u] = s < s1 ? __ldg(val + s) : V(0);
     }
 #pragma unroll
@@ -262,16 +271,16 @@ __device__ __forceinline__ bool last_block(uint32_t* ticket)
   return last;
 }
 
-template <typename V, int G>
+template <typename V, int G, typename I>
 __global__ void __launch_bounds__(kSolveThreads) k_spmv(int64_t n, const int32_t* __restrict__ rp,
-                                                        const int32_t* __restrict__ ci, const V* __restrict__ val,
+                                                        const I* __restrict__ ci, const V* __restrict__ val,
                                                         const V* __restrict__ x, V* __restrict__ y)
 {
   pdl_wait();
   pdl_trigger();
   const int64_t groups = (int64_t)gridDim.x * (kSolveThreads / G);
   for (int64_t row = (blockIdx.x * (int64_t)kSolveThreads + threadIdx.x) / G; row < n; row += groups) {
-    const V s = row_dot<V, G>(row, rp, ci, val, x);
+    const V s = row_dot<V, G, kEntriesPerLane<V>, I>(row, rp, ci, val, x);
     if ((threadIdx.x & (G - 1)) == 0) y[row] = s;
   }
 }
@@ -286,9 +295,9 @@ __global__ void k_rowsum(int64_t n, const int32_t* rp, const double* val, double
 }
 
 // K1: q = A p, alpha = rz / (p . q)
-template <typename V, int G>
+template <typename V, int G, typename I>
 __global__ void __launch_bounds__(kSolveThreads) k_cg_spmv(int64_t n, const int32_t* __restrict__ rp,
-                                                           const int32_t* __restrict__ ci, const V* __restrict__ val,
+                                                           const I* __restrict__ ci, const V* __restrict__ val,
                                                            const V* __restrict__ p, V* __restrict__ q,
                                                            double* partials, CgScalars* s)
 {
@@ -301,7 +310,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_cg_spmv(int64_t n, const int3
   const int64_t groups = (int64_t)gridDim.x * (kSolveThreads / G);
   typename D::A acc = D::zero();
   for (int64_t row = (blockIdx.x * (int64_t)kSolveThreads + threadIdx.x) / G; row < n; row += groups) {
-    const V v = row_dot<V, G, CgShape<V>::U>(row, rp, ci, val, p);
+    const V v = row_dot<V, G, CgShape<V>::U, I>(row, rp, ci, val, p);
     if ((threadIdx.x & (G - 1)) == 0) {
       q[row] = v;
       D::mac(acc, p[row], v);
@@ -550,12 +559,26 @@ mg_status launch_spmv(mg_plan* p, int prec, const void* vals, const void* x, voi
   MG_TRY(plan_device(p));
   if (prec == MG_F64) {
     const int G = row_group<double>(p), nb = row_blocks<double>(p, G);
-    MG_DISPATCH_G(G, (launch_pdl(k_spmv<double, g>, nb, kSolveThreads, st, p->ndof, (const int32_t*)p->d_rowptr,
-                                 (const int32_t*)p->d_colind, (const double*)vals, (const double*)x, (double*)y)));
+    if (p->d_coloff) {
+      MG_DISPATCH_G(G, (launch_pdl(k_spmv<double, g, int16_t>, nb, kSolveThreads, st, p->ndof,
+                                   (const int32_t*)p->d_rowptr, (const int16_t*)p->d_coloff, (const double*)vals,
+                                   (const double*)x, (double*)y)));
+    } else {
+      MG_DISPATCH_G(G, (launch_pdl(k_spmv<double, g, int32_t>, nb, kSolveThreads, st, p->ndof,
+                                   (const int32_t*)p->d_rowptr, (const int32_t*)p->d_colind, (const double*)vals,
+                                   (const double*)x, (double*)y)));
+    }
   } else {
     const int G = row_group<float>(p), nb = row_blocks<float>(p, G);
-    MG_DISPATCH_G(G, (launch_pdl(k_spmv<float, g>, nb, kSolveThreads, st, p->ndof, (const int32_t*)p->d_rowptr,
-                                 (const int32_t*)p->d_colind, (const float*)vals, (const float*)x, (float*)y)));
+    if (p->d_coloff) {
+      MG_DISPATCH_G(G, (launch_pdl(k_spmv<float, g, int16_t>, nb, kSolveThreads, st, p->ndof,
+                                   (const int32_t*)p->d_rowptr, (const int16_t*)p->d_coloff, (const float*)vals,
+                                   (const float*)x, (float*)y)));
+    } else {
+      MG_DISPATCH_G(G, (launch_pdl(k_spmv<float, g, int32_t>, nb, kSolveThreads, st, p->ndof,
+                                   (const int32_t*)p->d_rowptr, (const int32_t*)p->d_colind, (const float*)vals,
+                                   (const float*)x, (float*)y)));
+    }
   }
   MG_CUDA(cudaGetLastError());
   return MG_OK;
@@ -621,8 +644,15 @@ static mg_status cg_iterate(mg_plan* p, const V* vals, V* x, CgWork<V>& w, int G
   if (cs != cudaStreamCaptureStatusNone || st == nullptr) use_graph = false;  // no nested capture; legacy stream cannot capture
   constexpr bool pdl = CgShape<V>::pdl;
   auto body = [&]() {
-    MG_DISPATCH_G(G, (launch_k(pdl, k_cg_spmv<V, g>, nb, kSolveThreads, st, n, (const int32_t*)p->d_rowptr,
-                               (const int32_t*)p->d_colind, vals, (const V*)w.p, w.q, w.partials, w.s)));
+    if (p->d_coloff) {
+      MG_DISPATCH_G(G, (launch_k(pdl, k_cg_spmv<V, g, int16_t>, nb, kSolveThreads, st, n,
+                                 (const int32_t*)p->d_rowptr, (const int16_t*)p->d_coloff, vals, (const V*)w.p, w.q,
+                                 w.partials, w.s)));
+    } else {
+      MG_DISPATCH_G(G, (launch_k(pdl, k_cg_spmv<V, g, int32_t>, nb, kSolveThreads, st, n,
+                                 (const int32_t*)p->d_rowptr, (const int32_t*)p->d_colind, vals, (const V*)w.p, w.q,
+                                 w.partials, w.s)));
+    }
     launch_k(pdl, k_cg_update<V>, vb, kSolveThreads, st, n, x, w.r, w.z, (const V*)w.p, (const V*)w.q,
              (const V*)w.dinv, w.partials, w.s);
     launch_k(pdl, k_cg_dir<V>, vb, kSolveThreads, st, n, (const V*)w.z, w.p, (const CgScalars*)w.s);
@@ -735,8 +765,15 @@ mg_status mg_cg_solve_noalloc(mg_plan* p, const double* d_values, const double* 
   for (int launched = 0;; launched += kGraphIters) {
     for (int k = 0; k < kGraphIters; ++k) {
       constexpr bool pdl = CgShape<double>::pdl;
-      MG_DISPATCH_G(G, (launch_k(pdl, k_cg_spmv<double, g>, nb, kSolveThreads, st, n, (const int32_t*)p->d_rowptr,
-                                 (const int32_t*)p->d_colind, d_values, (const double*)w.p, w.q, w.partials, w.s)));
+      if (p->d_coloff) {
+        MG_DISPATCH_G(G, (launch_k(pdl, k_cg_spmv<double, g, int16_t>, nb, kSolveThreads, st, n,
+                                   (const int32_t*)p->d_rowptr, (const int16_t*)p->d_coloff, d_values,
+                                   (const double*)w.p, w.q, w.partials, w.s)));
+      } else {
+        MG_DISPATCH_G(G, (launch_k(pdl, k_cg_spmv<double, g, int32_t>, nb, kSolveThreads, st, n,
+                                   (const int32_t*)p->d_rowptr, (const int32_t*)p->d_colind, d_values,
+                                   (const double*)w.p, w.q, w.partials, w.s)));
+      }
       launch_k(pdl, k_cg_update<double>, vb, kSolveThreads, st, n, d_x, w.r, w.z, (const double*)w.p,
                (const double*)w.q, (const double*)w.dinv, w.partials, w.s);
       launch_k(pdl, k_cg_dir<double>, vb, kSolveThreads, st, n, (const double*)w.z, w.p, (const CgScalars*)w.s);
