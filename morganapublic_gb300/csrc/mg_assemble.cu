@@ -54,9 +54,14 @@ __device__ __forceinline__ ff operator*(ff a, ff b) { return ff_mul(a, b); }
 __device__ __forceinline__ ff operator/(ff a, ff b) { return ff_div(a, b); }
 
 template <int MODE> struct Arith;
+// sum_into(s, x): s += x for the phase-2 sums.  The double-word form defers
+// renormalisation: the high words are added error-free (two_sum), the low
+// words and errors collect in s.lo, which may exceed half an ulp of s.hi (the
+// final hi + lo is formed in FP64 when the value is written).
 template <> struct Arith<kF32> {
   using T = float;
   using Acc = float;
+  __device__ static void sum_into(T& s, T x) { s += x; }
   __device__ static void acc_add(Acc& s, T x) { s += x; }
   __device__ static T acc_value(const Acc& s) { return s; }
   using Out = float;
@@ -67,6 +72,12 @@ template <> struct Arith<kF32> {
 template <> struct Arith<kDW> {
   using T = ff;
   using Acc = ff_acc;
+  __device__ static void sum_into(T& s, T x)
+  {
+    const ff t = two_sum(s.hi, x.hi);
+    s.hi = t.hi;
+    s.lo = __fadd_rn(s.lo, __fadd_rn(t.lo, x.lo));
+  }
   __device__ static void acc_add(Acc& s, T x) { ff_acc_add(s, x); }
   __device__ static T acc_value(const Acc& s) { return ff_acc_value(s); }
   using Out = double;
@@ -77,6 +88,7 @@ template <> struct Arith<kDW> {
 template <> struct Arith<kF64> {
   using T = double;
   using Acc = double;
+  __device__ static void sum_into(T& s, T x) { s += x; }
   __device__ static void acc_add(Acc& s, T x) { s += x; }
   __device__ static T acc_value(const Acc& s) { return s; }
   using Out = double;
@@ -385,6 +397,35 @@ __device__ __forceinline__ void metric(const Cof<T>& f, T s, T g[6])
     g[p] = s * (f.c[0][pa[p]] * f.c[0][pb[p]] + f.c[1][pa[p]] * f.c[1][pb[p]] + f.c[2][pa[p]] * f.c[2][pb[p]]);
 }
 
+// sum_{p<6} g[p] tab[p * NU + u] (the P2 metric contraction).  Double-word:
+// error-free products of the high words chained with two_sum, the low-order
+// terms in one float, one renormalisation (instead of one per operation).
+template <typename T>
+__device__ __forceinline__ T metric_dot(const T g[6], const T* tab, int NU, int u)
+{
+  T v = g[0] * tab[u];
+#pragma unroll
+  for (int k = 1; k < 6; ++k) v = v + g[k] * tab[k * NU + u];
+  return v;
+}
+template <>
+__device__ __forceinline__ ff metric_dot<ff>(const ff g[6], const ff* tab, int NU, int u)
+{
+  const ff t0 = tab[u];
+  const ff p0 = two_prod(g[0].hi, t0.hi);
+  float hi = p0.hi;
+  float lo = __fmaf_rn(g[0].hi, t0.lo, __fmaf_rn(g[0].lo, t0.hi, p0.lo));
+#pragma unroll
+  for (int k = 1; k < 6; ++k) {
+    const ff t = tab[k * NU + u];
+    const ff q = two_prod(g[k].hi, t.hi);
+    const ff s = two_sum(hi, q.hi);
+    hi = s.hi;
+    lo = __fadd_rn(lo, __fadd_rn(s.lo, __fmaf_rn(g[k].hi, t.lo, __fmaf_rn(g[k].lo, t.hi, q.lo))));
+  }
+  return two_sum(hi, lo);
+}
+
 struct AsmArgs {
   const BlockDesc* blocks;
   const unsigned char* chunk_data;  // chunk records (layout at ChunkDesc)
@@ -444,11 +485,14 @@ struct AsmLayout {
   static constexpr size_t blk_bytes = 2 * sizeof(BlockDesc);
   static constexpr size_t off_buf = acc_bytes;
   static constexpr size_t off_tab = off_buf + kGroups * buf_bytes;
-  static constexpr size_t off_meta = off_tab + tab_bytes;
+  // P2: per group, the 6 scale factors of each item of a chunk (computed once per item)
+  static constexpr size_t geo_bytes = ORDER == 2 ? align16(sizeof(T) * CI * 6) : 0;
+  static constexpr size_t off_geo = off_tab + tab_bytes;
+  static constexpr size_t off_meta = off_geo + kGroups * geo_bytes;
   static constexpr size_t off_blk = off_meta + meta_bytes;
   static constexpr size_t off_bars = off_blk + blk_bytes;
   static constexpr size_t off_stage = off_bars + align16(8 * kNumBars);
-  static_assert(off_buf % 16 == 0 && off_tab % 16 == 0 && off_meta % 16 == 0 && off_blk % 16 == 0 &&
+  static_assert(off_buf % 16 == 0 && off_tab % 16 == 0 && off_geo % 16 == 0 && off_meta % 16 == 0 && off_blk % 16 == 0 &&
                     off_bars % 16 == 0 && off_stage % 16 == 0 && buf_bytes % 16 == 0,
                 "shared-memory regions must start on 16-byte boundaries");
   __host__ __device__ static size_t stage_bytes(int stage_cap) { return ((size_t)stage_cap + 15) / 16 * 16; }
@@ -638,6 +682,7 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
     const int gwarp = gtid >> 5;
     const int local = gtid / TPI, sub = gtid % TPI;
     T* buf = reinterpret_cast<T*>(smem + L::off_buf + g * L::buf_bytes);
+    T* sgeo = reinterpret_cast<T*>(smem + L::off_geo + g * L::geo_bytes);  // P2: [CI][6]
     const T wsum = A::from(a.wsum);
     int q = 0, ntok = 0;  // chunks before this block; token waits so far
     for (int j = 0;; ++j) {
@@ -659,20 +704,42 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
           w_beg = desc_of(qq)->warp_off[gwarp];
           w_end = desc_of(qq)->warp_off[gwarp + 1];
         }
-        if (!failed && c * CI + local < d.item_count) {
+        // geometry and coefficient of item `it` of chunk c (from the staged record)
+        auto item_geometry = [&](int it, Cof<T>& f, T& coef) {
           const unsigned char* rb = stage_of(qq);
           const int n4 = (min(CI, d.item_count - c * CI) + 3) & ~3, nn = desc_of(qq)->n_nodes;
-          const int e = reinterpret_cast<const int32_t*>(rb + sizeof(ChunkDesc))[local];
+          const int e = reinterpret_cast<const int32_t*>(rb + sizeof(ChunkDesc))[it];
           const double coef_d = a.coeff ? __ldg(a.coeff + e) : a.cconst;  // latency covered by the geometry
-          const ushort4 lc = reinterpret_cast<const ushort4*>(rb + sizeof(ChunkDesc) + 4 * n4)[local];
+          const ushort4 lc = reinterpret_cast<const ushort4*>(rb + sizeof(ChunkDesc) + 4 * n4)[it];
           const float4* vrec = reinterpret_cast<const float4*>(rb + sizeof(ChunkDesc) + 12 * n4);
           const float* vloz = reinterpret_cast<const float*>(rb + sizeof(ChunkDesc) + 12 * n4 + 32 * nn);
           Fetch<MODE> F;
           fetch_staged(vrec, vloz, lc, F);
-          Cof<T> f;
           geometry(F, f);
-          const T coef = A::from(coef_d);
-          if (ORDER == 1) {
+          coef = A::from(coef_d);
+        };
+        // P2 in the FP64 modes: the double-word geometry is worth computing once per
+        // item; FP32 recomputes it in each of the item's threads (no extra barrier)
+        constexpr bool kGeoOnce = ORDER == 2 && MODE != kF32;
+        if (ORDER == 2 && !kGeoOnce) {
+          if (!failed && c * CI + local < d.item_count) {
+            Cof<T> f;
+            T coef;
+            item_geometry(local, f, coef);
+            if (a.stiff) {
+              T gm[6];
+              metric<T>(f, coef / f.det, gm);
+              for (int u = sub; u < NU; u += TPI) buf[u * CI + local] = metric_dot<T>(gm, tab, NU, u);
+            } else {
+              const T sc = coef * f.det;
+              for (int u = sub; u < NU; u += TPI) buf[u * CI + local] = sc * tab[6 * NU + u];
+            }
+          }
+        } else if (ORDER == 1) {
+          if (!failed && c * CI + local < d.item_count) {
+            Cof<T> f;
+            T coef;
+            item_geometry(local, f, coef);
             T K[10];
             if (a.stiff) {
               p1_stiff_unique<T>(f, coef * wsum / f.det, K);
@@ -683,18 +750,35 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
             }
 #pragma unroll
             for (int u = 0; u < 10; ++u) buf[u * CI + local] = K[u];
-          } else if (a.stiff) {
-            T gm[6];
-            metric<T>(f, coef / f.det, gm);
-            for (int u = sub; u < NU; u += TPI) {
-              T v = gm[0] * tab[u];
+          }
+        } else {
+          // P2: the first warp of the group computes each item's scale factors
+          // once (6 metric coefficients, or coef * det for the mass); then every
+          // thread forms its share of the item's 55 entries
+          if (!failed && gwarp == 0 && c * CI + lane < d.item_count) {
+            Cof<T> f;
+            T coef;
+            item_geometry(lane, f, coef);
+            if (a.stiff) {
+              T gm[6];
+              metric<T>(f, coef / f.det, gm);
 #pragma unroll
-              for (int k = 1; k < 6; ++k) v = v + gm[k] * tab[k * NU + u];
-              buf[u * CI + local] = v;
+              for (int k = 0; k < 6; ++k) sgeo[lane * 6 + k] = gm[k];
+            } else {
+              sgeo[lane * 6] = coef * f.det;
             }
-          } else {
-            const T sc = coef * f.det;
-            for (int u = sub; u < NU; u += TPI) buf[u * CI + local] = sc * tab[6 * NU + u];
+          }
+          failed = group_sync_or(g, failed);
+          if (!failed && c * CI + local < d.item_count) {
+            if (a.stiff) {
+              T gm[6];
+#pragma unroll
+              for (int k = 0; k < 6; ++k) gm[k] = sgeo[local * 6 + k];
+              for (int u = sub; u < NU; u += TPI) buf[u * CI + local] = metric_dot<T>(gm, tab, NU, u);
+            } else {
+              const T sc = sgeo[local * 6];
+              for (int u = sub; u < NU; u += TPI) buf[u * CI + local] = sc * tab[6 * NU + u];
+            }
           }
         }
         failed = group_sync_or(g, failed);
@@ -725,8 +809,10 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
             const uint32_t slot = (w[0] >> kSrcBits) & kSlotMask;
             T v = buf[w[0] & kSrcMask];
 #pragma unroll
-            for (int p = 1; p < PW; ++p) v = v + buf[w[p] & kSrcMask];
-            acc[slot] = acc[slot] + v;
+            for (int p = 1; p < PW; ++p) A::sum_into(v, buf[w[p] & kSrcMask]);
+            T a = acc[slot];
+            A::sum_into(a, v);
+            acc[slot] = a;
           }
         }
         if (c + 1 < n) mbar_arrive(&bars[kBarToken + (g ^ 1)]);  // release: the updates above precede
