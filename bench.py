@@ -185,23 +185,25 @@ def run_reference(a):
     import oracle as orc
     orc.build()
     nproc = os.cpu_count() or 1
-    steps = a.warmup + a.steps
-    # bounded sample: the full mesh split over all host cores, few steps
+    # bounded sample: the full mesh split over all host cores, at most 1 warm-up
+    # and 5 timed steps (each step takes about a second on the host)
+    warm, timed = min(a.warmup, 1), max(1, min(a.steps, 5))
+    steps = warm + timed
     ctx = mp.get_context("spawn")
     with ctx.Pool(nproc) as pool:
         res = pool.map(_ref_worker, [(a.n, a.jitter, a.seed, a.sigma, r, nproc, steps) for r in range(nproc)])
-    per_step = [max(r[0][s] for r in res) for s in range(a.warmup, steps)]
+    per_step = [max(r[0][s] for r in res) for s in range(warm, steps)]
     E = sum(r[1] for r in res)
     t = statistics.mean(per_step)
     val = E / t
     line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "tets/s", "n_gpus": a.gpus,
-            "steps": a.steps, "warmup": a.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+            "steps": timed, "warmup": warm, "ms_per_step": t * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": f"P1 kappa-diffusion operator, {a.n}^3 cells x 6 tets, step = FP64 assembly "
                                    f"(pattern + values) + {N_SPMV} SpMV, elements split over {nproc} host processes",
                        "n_cells": a.n, "tets": E},
             "cpu_baseline": {"value": val, "unit": "tets/s", "cores": nproc, "kind": "port",
-                             "sample": f"full {a.n}^3 mesh, {a.steps} timed steps, {nproc} processes x 1 thread, "
+                             "sample": f"full {a.n}^3 mesh, {timed} timed steps, {nproc} processes x 1 thread, "
                                        "CPU restatement of the reference algorithm (reference binary not buildable: "
                                        "needs MPI, Boost, Trilinos)"},
             "e2e": {"value": val, "unit": "tets/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -645,14 +647,28 @@ def main():
         kap_d = torch.empty_like(kappa)
         x_d = torch.empty_like(x)
 
+        # copies on a second stream overlap the kernels that do not need them: x
+        # arrives during the assembly, the CSR values leave during the SpMVs
+        cstream = torch.cuda.Stream()
+        ev_x, ev_asm, ev_v = (torch.cuda.Event() for _ in range(3))
+
         def e2e_step():
             kap_d.copy_(kap_pin, non_blocking=True)
-            x_d.copy_(x_pin, non_blocking=True)
+            cstream.wait_stream(stream)
+            with torch.cuda.stream(cstream):
+                x_d.copy_(x_pin, non_blocking=True)
+                ev_x.record(cstream)
             b.assemble("stiff_kappa", coeff=kap_d, quad=4, prec="f64", out=v64, stream=stream)
-            v_pin.copy_(v64, non_blocking=True)
+            ev_asm.record(stream)
+            with torch.cuda.stream(cstream):
+                cstream.wait_event(ev_asm)
+                v_pin.copy_(v64, non_blocking=True)
+                ev_v.record(cstream)
+            stream.wait_event(ev_x)
             for _ in range(N_SPMV):
                 b.apply(v64, x_d, out=y, stream=stream)
             y_pin.copy_(y, non_blocking=True)
+            stream.wait_event(ev_v)
 
         te2e = timed(e2e_step, reps=max(3, min(a.steps, 10)))
         h2d = 8 * E + 8 * ndof
@@ -660,7 +676,8 @@ def main():
         del ctypes
         e2e = {"value": world * E / (te2e * 1e-3), "unit": "tets/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "ms_per_step": te2e,
-               "note": "kappa and x copied in from pinned host memory, CSR values and y copied out, per step"}
+               "note": "kappa and x copied in from pinned host memory, CSR values and y copied out, per step; the x "
+                       "upload overlaps the assembly and the values download overlaps the SpMVs (second stream)"}
 
         dom = "assembly_f64" if statistics.median(t_asm) >= N_SPMV * ts64_warm else "spmv_f64_in_step"
         rl = extras[dom]
