@@ -294,6 +294,19 @@ def run_only(a):
     return 0
 
 
+def replica_throughput(ms_local, units_local, world, device):
+    """Replicas: every rank runs the whole step on its own GPU.  Returns the step
+    time as the maximum over ranks and the job throughput world * units / time."""
+    ms = ms_local
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([ms_local], device=device, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, world * units_local / (ms * 1e-3)
+
+
 def _timed_cuda(torch, stream, fn, reps, flush=None):
     """median CUDA-event time (ms) of fn on `stream`; L2 flushed before each rep when `flush` is given"""
     ts = []
@@ -559,12 +572,7 @@ def main():
         t_asm = [e[0].elapsed_time(e[1]) for e in evs2]
         t_spmv = [e[1].elapsed_time(e[2]) / N_SPMV for e in evs2]
         t_step_eager = [e[0].elapsed_time(e[2]) for e in evs2]
-    ms_step = statistics.mean(t_step)
-    if world > 1:
-        t = torch.tensor([ms_step], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = float(t.item())
-    value = world * E / (ms_step * 1e-3)
+    ms_step, value = replica_throughput(statistics.mean(t_step), E, world, "cuda")
 
     # ---------------------------------------------------------- extra metrics (untimed above)
     extras = {}

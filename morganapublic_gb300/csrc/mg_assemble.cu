@@ -60,10 +60,7 @@ template <int MODE> struct Arith;
 // final hi + lo is formed in FP64 when the value is written).
 template <> struct Arith<kF32> {
   using T = float;
-  using Acc = float;
   __device__ static void sum_into(T& s, T x) { s += x; }
-  __device__ static void acc_add(Acc& s, T x) { s += x; }
-  __device__ static T acc_value(const Acc& s) { return s; }
   using Out = float;
   __device__ static T from(double x) { return (float)x; }
   __device__ static T zero() { return 0.0f; }
@@ -71,15 +68,12 @@ template <> struct Arith<kF32> {
 };
 template <> struct Arith<kDW> {
   using T = ff;
-  using Acc = ff_acc;
   __device__ static void sum_into(T& s, T x)
   {
     const ff t = two_sum(s.hi, x.hi);
     s.hi = t.hi;
     s.lo = __fadd_rn(s.lo, __fadd_rn(t.lo, x.lo));
   }
-  __device__ static void acc_add(Acc& s, T x) { ff_acc_add(s, x); }
-  __device__ static T acc_value(const Acc& s) { return ff_acc_value(s); }
   using Out = double;
   __device__ static T from(double x) { return ff_from_double_bits(x); }
   __device__ static T zero() { return ff{0.0f, 0.0f}; }
@@ -87,10 +81,7 @@ template <> struct Arith<kDW> {
 };
 template <> struct Arith<kF64> {
   using T = double;
-  using Acc = double;
   __device__ static void sum_into(T& s, T x) { s += x; }
-  __device__ static void acc_add(Acc& s, T x) { s += x; }
-  __device__ static T acc_value(const Acc& s) { return s; }
   using Out = double;
   __device__ static T from(double x) { return x; }
   __device__ static T zero() { return 0.0; }
