@@ -198,6 +198,28 @@ def test_manufactured_p2_mixed_vs_fp64_against_oracle():
     assert infor.iterations <= 1.5 * info.iterations + 20
 
 
+def test_unreferenced_nodes_give_empty_rows():
+    """Nodes no element references (common in Gmsh files) own empty CSR rows.
+    3000 of them scattered through a 4^3 mesh put more than 2048 rows (the
+    per-block row cap) into a block of few entries; pattern, values and SpMV
+    still match the oracle."""
+    m, kappa = _case(4, 0.2, 9, True, 1.0)
+    extra = np.random.default_rng(9).uniform(0.0, 1.0, (3000, 3))
+    xyz = np.concatenate([m.xyz, extra])
+    b = mg.MatrixBuilder(mg.Mesh(xyz, m.conn, order=1))
+    assert b.ndof == len(xyz)
+    dofs, rp, ci, ref = orc.full_operator("stiff_kappa", 1, 4, xyz, m.conn, coeff=kappa)
+    rph, cih = b.pattern()
+    assert np.array_equal(rph, rp) and np.array_equal(cih, ci)
+    assert np.all(np.diff(rp)[len(m.xyz):] == 0)
+    v = b.assemble("stiff_kappa", coeff=kappa, quad=4)
+    assert row_scaled_err(rp, ref, v.cpu().numpy()) <= F64_TOL
+    x = np.random.default_rng(1).uniform(-1, 1, len(xyz))
+    y = b.apply(v, torch.from_numpy(x).cuda()).cpu().numpy()
+    y_ref = orc.spmv(rp, ci, ref, x)
+    assert np.max(np.abs(y - y_ref)) <= 1e-12 * np.abs(y_ref).max()
+
+
 def test_cg_deterministic_and_maxit_status():
     m, kappa, mesh, b, dofs, rp, ci, K, mask, rhs, quad = _dirichlet_system(5, 1, 1.0, 6)
     v = b.assemble("stiff_kappa", coeff=kappa, quad=quad)
