@@ -174,22 +174,28 @@ struct GeoPtrs {
 };
 
 // The coordinates an element needs.  The assembly kernel reads them from the
-// chunk record staged in shared memory (local vertex indices); the adjoint
-// kernel reads them from the mesh arrays in global memory.  FP32 uses hi + mid
-// of each coordinate, double-word hi + mid + lo, native FP64 their exact sum.
+// chunk record staged in shared memory (local vertex indices): coordinates
+// relative to the chunk's first vertex, split r = hi + lo (two floats).  The
+// adjoint kernel reads the mesh's absolute coordinates (x = hi + mid + lo) from
+// global memory.
 template <int MODE> struct Fetch;
 template <> struct Fetch<kF32> {
-  float4 a[4], b[4];
+  float4 a[4];  // hi.xyz, lo.x
+  float2 b[4];  // lo.y, lo.z
 };
 template <> struct Fetch<kDW> {
-  float4 a[4], b[4];
-  float lz[4];
+  float4 a[4];
+  float2 b[4];
 };
 template <> struct Fetch<kF64> {
   double4_32a x[4];
 };
+struct FetchAbs {  // absolute coordinates (adjoint kernel)
+  float4 a[4], b[4];
+  float lz[4];
+};
 
-__device__ __forceinline__ void fetch(const GeoPtrs& g, int4 n, Fetch<kDW>& F)
+__device__ __forceinline__ void fetch(const GeoPtrs& g, int4 n, FetchAbs& F)
 {
   const int id[4] = {n.x, n.y, n.z, n.w};
 #pragma unroll
@@ -200,40 +206,34 @@ __device__ __forceinline__ void fetch(const GeoPtrs& g, int4 n, Fetch<kDW>& F)
   }
 }
 
-// from a staged chunk record: rec = 2 float4 per vertex, loz = lo.z per vertex
-__device__ __forceinline__ void fetch_staged(const float4* rec, const float*, ushort4 lc, Fetch<kF32>& F)
+// from a staged chunk record: va = (hi.xyz, lo.x), vb = (lo.y, lo.z) per vertex
+template <int MODE>
+__device__ __forceinline__ void fetch_staged(const float4* va, const float2* vb, ushort4 lc, Fetch<MODE>& F)
 {
   const int id[4] = {lc.x, lc.y, lc.z, lc.w};
 #pragma unroll
   for (int s = 0; s < 4; ++s) {
-    F.a[s] = rec[2 * id[s]];
-    F.b[s] = rec[2 * id[s] + 1];
+    F.a[s] = va[id[s]];
+    F.b[s] = vb[id[s]];
   }
 }
-__device__ __forceinline__ void fetch_staged(const float4* rec, const float* loz, ushort4 lc, Fetch<kDW>& F)
+// hi + lo summed in FP64 (to 2^-48 of the relative coordinate)
+template <>
+__device__ __forceinline__ void fetch_staged<kF64>(const float4* va, const float2* vb, ushort4 lc, Fetch<kF64>& F)
 {
   const int id[4] = {lc.x, lc.y, lc.z, lc.w};
 #pragma unroll
   for (int s = 0; s < 4; ++s) {
-    F.a[s] = rec[2 * id[s]];
-    F.b[s] = rec[2 * id[s] + 1];
-    F.lz[s] = loz[id[s]];
-  }
-}
-// hi + mid + lo summed in FP64 is exact (the three parts are the successive
-// float roundings of the coordinate's remainders)
-__device__ __forceinline__ void fetch_staged(const float4* rec, const float* loz, ushort4 lc, Fetch<kF64>& F)
-{
-  const int id[4] = {lc.x, lc.y, lc.z, lc.w};
-#pragma unroll
-  for (int s = 0; s < 4; ++s) {
-    const float4 u = rec[2 * id[s]], v = rec[2 * id[s] + 1];
-    F.x[s] = make_double4_32a(((double)u.x + (double)u.w) + (double)v.z, ((double)u.y + (double)v.x) + (double)v.w,
-                              ((double)u.z + (double)v.y) + (double)loz[id[s]], 0.0);
+    const float4 u = va[id[s]];
+    const float2 v = vb[id[s]];
+    F.x[s] = make_double4_32a((double)u.x + (double)u.w, (double)u.y + (double)v.x, (double)u.z + (double)v.y, 0.0);
   }
 }
 
-// components of a vertex record: hi, mid, lo
+// components of a staged vertex: hi, lo
+__device__ __forceinline__ float vhi(const float4& a, int r) { return r == 0 ? a.x : (r == 1 ? a.y : a.z); }
+__device__ __forceinline__ float vlo(const float4& a, const float2& b, int r) { return r == 0 ? a.w : (r == 1 ? b.x : b.y); }
+// components of an absolute mesh record: hi, mid, lo
 __device__ __forceinline__ float rec_hi(const float4& a, int r) { return r == 0 ? a.x : (r == 1 ? a.y : a.z); }
 __device__ __forceinline__ float rec_mid(const float4& a, const float4& b, int r) { return r == 0 ? a.w : (r == 1 ? b.x : b.y); }
 __device__ __forceinline__ float rec_lo(const float4& b, float lz, int r) { return r == 0 ? b.z : (r == 1 ? b.w : lz); }
@@ -250,9 +250,9 @@ __device__ __forceinline__ void geometry(const Fetch<kF64>& F, Cof<double>& f)
   cofactors<double>(J, f);
 }
 
-// FP32: edge vectors (hi_k - hi_0) + (mid_k - mid_0), accurate to a few float
-// ulps of the edge itself; flat elements recompute the cofactors in FP64 from
-// hi + mid.
+// FP32: edge vectors (hi_k - hi_0) + (lo_k - lo_0) of the chunk-relative
+// coordinates, accurate to a few float ulps of the edge itself; flat elements
+// recompute the cofactors in FP64 from hi + lo.
 constexpr float kFlatTol = 1e-3f;
 __device__ __forceinline__ void geometry(const Fetch<kF32>& F, Cof<float>& f)
 {
@@ -261,14 +261,13 @@ __device__ __forceinline__ void geometry(const Fetch<kF32>& F, Cof<float>& f)
   for (int r = 0; r < 3; ++r)
 #pragma unroll
     for (int k = 0; k < 3; ++k)
-      J[r][k] = (rec_hi(F.a[k + 1], r) - rec_hi(F.a[0], r)) +
-                (rec_mid(F.a[k + 1], F.b[k + 1], r) - rec_mid(F.a[0], F.b[0], r));
+      J[r][k] = (vhi(F.a[k + 1], r) - vhi(F.a[0], r)) + (vlo(F.a[k + 1], F.b[k + 1], r) - vlo(F.a[0], F.b[0], r));
   cofactors<float>(J, f);
   float nn[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) nn[k] = J[0][k] * J[0][k] + J[1][k] * J[1][k] + J[2][k] * J[2][k];
   if (f.det * f.det < kFlatTol * kFlatTol * nn[0] * nn[1] * nn[2]) {
-    Fetch<kF64> D;  // hi + mid: coordinates to 2^-48 relative
+    Fetch<kF64> D;
 #pragma unroll
     for (int s = 0; s < 4; ++s)
       D.x[s] = make_double4_32a((double)F.a[s].x + (double)F.a[s].w, (double)F.a[s].y + (double)F.b[s].x,
@@ -281,28 +280,9 @@ __device__ __forceinline__ void geometry(const Fetch<kF32>& F, Cof<float>& f)
   }
 }
 
-// Double-word: x = hi + mid + lo exactly, so
-//   x_k - x_0 = (hi_k - hi_0) + (mid_k - mid_0) + (lo_k - lo_0)
-// with the two leading differences taken error-free (two_sum) and the result
-// renormalised -- relative error ~2^-47 of the edge vector itself.
-__device__ __forceinline__ ff dw_diff(float hb, float ha, float mb, float ma, float lb, float la)
+// Double-word cofactors and determinant from double-word edge vectors.
+__device__ __forceinline__ void dw_cofactors(const ff J[3][3], Cof<ff>& f)
 {
-  const ff s1 = two_sum(hb, -ha);
-  const ff s2 = two_sum(mb, -ma);
-  const ff s = two_sum(s1.hi, s2.hi);
-  const float t = __fadd_rn(__fadd_rn(__fadd_rn(s.lo, s1.lo), s2.lo), __fsub_rn(lb, la));
-  return two_sum(s.hi, t);
-}
-
-__device__ __forceinline__ void geometry(const Fetch<kDW>& F, Cof<ff>& f)
-{
-  ff J[3][3];
-#pragma unroll
-  for (int r = 0; r < 3; ++r)
-#pragma unroll
-    for (int k = 0; k < 3; ++k)
-      J[r][k] = dw_diff(rec_hi(F.a[k + 1], r), rec_hi(F.a[0], r), rec_mid(F.a[k + 1], F.b[k + 1], r),
-                        rec_mid(F.a[0], F.b[0], r), rec_lo(F.b[k + 1], F.lz[k + 1], r), rec_lo(F.b[0], F.lz[0], r));
   f.c[0][0] = ff_cross(J[1][1], J[2][2], J[1][2], J[2][1]);
   f.c[0][1] = ff_cross(J[1][2], J[2][0], J[1][0], J[2][2]);
   f.c[0][2] = ff_cross(J[1][0], J[2][1], J[1][1], J[2][0]);
@@ -315,13 +295,50 @@ __device__ __forceinline__ void geometry(const Fetch<kDW>& F, Cof<ff>& f)
   f.det = ff_dot3(J[0], f.c[0]);
 }
 
-// one geometry entry point for the adjoint kernel (loads and computes at once)
-template <int MODE>
-__device__ __forceinline__ void geometry_now(const GeoPtrs& g, int4 n, Cof<typename Arith<MODE>::T>& f)
+// Double-word, chunk-relative coordinates r = hi + lo (|r - hi - lo| <= 2^-48 |r|,
+// |r| a few edge lengths): r_k - r_0 = (hi_k - hi_0) + (lo_k - lo_0), the
+// leading difference error-free (two_sum) -- relative error ~2^-46 of the edge.
+__device__ __forceinline__ ff dw_diff2(float hb, float ha, float lb, float la)
 {
-  Fetch<MODE> F;
+  const ff s1 = two_sum(hb, -ha);
+  return two_sum(s1.hi, __fadd_rn(s1.lo, __fsub_rn(lb, la)));
+}
+
+__device__ __forceinline__ void geometry(const Fetch<kDW>& F, Cof<ff>& f)
+{
+  ff J[3][3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      J[r][k] = dw_diff2(vhi(F.a[k + 1], r), vhi(F.a[0], r), vlo(F.a[k + 1], F.b[k + 1], r), vlo(F.a[0], F.b[0], r));
+  dw_cofactors(J, f);
+}
+
+// Double-word, absolute coordinates x = hi + mid + lo exactly (the adjoint
+// kernel):  x_k - x_0 = (hi_k - hi_0) + (mid_k - mid_0) + (lo_k - lo_0) with
+// the two leading differences error-free -- relative error ~2^-47 of the edge.
+__device__ __forceinline__ ff dw_diff3(float hb, float ha, float mb, float ma, float lb, float la)
+{
+  const ff s1 = two_sum(hb, -ha);
+  const ff s2 = two_sum(mb, -ma);
+  const ff s = two_sum(s1.hi, s2.hi);
+  const float t = __fadd_rn(__fadd_rn(__fadd_rn(s.lo, s1.lo), s2.lo), __fsub_rn(lb, la));
+  return two_sum(s.hi, t);
+}
+
+__device__ __forceinline__ void geometry_abs(const GeoPtrs& g, int4 n, Cof<ff>& f)
+{
+  FetchAbs F;
   fetch(g, n, F);
-  geometry(F, f);
+  ff J[3][3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      J[r][k] = dw_diff3(rec_hi(F.a[k + 1], r), rec_hi(F.a[0], r), rec_mid(F.a[k + 1], F.b[k + 1], r),
+                         rec_mid(F.a[0], F.b[0], r), rec_lo(F.b[k + 1], F.lz[k + 1], r), rec_lo(F.b[0], F.lz[0], r));
+  dw_cofactors(J, f);
 }
 
 // ------------------------------------------------------- element matrices --
@@ -702,10 +719,10 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
           const int e = reinterpret_cast<const int32_t*>(rb + sizeof(ChunkDesc))[it];
           const double coef_d = a.coeff ? __ldg(a.coeff + e) : a.cconst;  // latency covered by the geometry
           const ushort4 lc = reinterpret_cast<const ushort4*>(rb + sizeof(ChunkDesc) + 4 * n4)[it];
-          const float4* vrec = reinterpret_cast<const float4*>(rb + sizeof(ChunkDesc) + 12 * n4);
-          const float* vloz = reinterpret_cast<const float*>(rb + sizeof(ChunkDesc) + 12 * n4 + 32 * nn);
+          const float4* va = reinterpret_cast<const float4*>(rb + sizeof(ChunkDesc) + 12 * n4);
+          const float2* vb = reinterpret_cast<const float2*>(rb + sizeof(ChunkDesc) + 12 * n4 + 16 * nn);
           Fetch<MODE> F;
-          fetch_staged(vrec, vloz, lc, F);
+          fetch_staged<MODE>(va, vb, lc, F);
           geometry(F, f);
           coef = A::from(coef_d);
         };
@@ -967,7 +984,7 @@ __global__ void __launch_bounds__(256) k_adjoint(int64_t n_elem, const int32_t* 
   const int32_t* dofs = dofs_m + i * NB;  // this element's dofs; the first four are its vertices
   const int4 n = ORDER == 1 ? reinterpret_cast<const int4*>(dofs_m)[i] : make_int4(dofs[0], dofs[1], dofs[2], dofs[3]);
   Cof<ff> f;
-  geometry_now<kDW>(geo, n, f);
+  geometry_abs(geo, n, f);
   ff s = ff_make(0.0f);
   if (ORDER == 1) {
     // K has zero row sums: lambda^T K u = (wsum / det) (sum_b dl_b C_b) . (sum_b du_b C_b)

@@ -83,9 +83,11 @@ struct BlockDesc {
 // Head of a chunk record.  The plan lays out, per chunk, one contiguous record
 // the kernel stages into shared memory with a single bulk copy:
 //   ChunkDesc (64 B) | element ids (4 B x n4) | local vertex indices (4 x 2 B x n4)
-//   | vertex records (2 float4 x nn: hi.xyz mid.x, mid.yz lo.xy) | lo.z (4 B x nn)
+//   | vertex coordinates relative to the chunk's first vertex, split r = hi + lo:
+//     float4 (hi.xyz, lo.x) x nn | float2 (lo.y, lo.z) x nn
 // n4 = the chunk's items rounded up to 4, nn = n_nodes (a multiple of 4), so
-// every part starts on a 16-byte boundary.
+// every part starts on a 16-byte boundary.  Element matrices depend on edge
+// vectors only, so the origin is not needed.
 struct ChunkDesc {
   int64_t word_begin;         // first contribution word of the chunk (multiple of 32)
   int32_t warp_off[kWarps + 1];  // per-warp offsets relative to word_begin; [kWarps] = chunk size

@@ -327,7 +327,7 @@ static mg_status build_schedule(mg_plan* p, HostSchedule* hs)
     for (int32_t b = 0; b < nbk; ++b)
       for (int32_t c = 0; c < hs->blocks[b].nchunks; ++c) {
         const int64_t n4 = (std::min(CI, hs->blocks[b].item_count - c * CI) + 3) & ~3;
-        maxb = std::max(maxb, (int64_t)sizeof(ChunkDesc) + 12 * n4 + 36 * (int64_t)hs->chunk_n_nodes[hs->blocks[b].chunk_begin + c]);
+        maxb = std::max(maxb, (int64_t)sizeof(ChunkDesc) + 12 * n4 + 24 * (int64_t)hs->chunk_n_nodes[hs->blocks[b].chunk_begin + c]);
       }
     if (maxb >= INT32_MAX) return set_error(MG_ERR_SIZE, "chunk record above 2 GiB");
     p->max_rec_bytes = (int32_t)maxb;
@@ -543,7 +543,7 @@ mg_status plan_device(mg_plan* p)
     int64_t maxb = 0;
     for (int64_t ck = 0; ck < nc; ++ck) {
       const int64_t n4 = (n_items(ck) + 3) & ~3, nn = hs.chunk_n_nodes[ck];
-      const int64_t bytes = (int64_t)sizeof(ChunkDesc) + 12 * n4 + 36 * nn;
+      const int64_t bytes = (int64_t)sizeof(ChunkDesc) + 12 * n4 + 24 * nn;
       off[ck + 1] = off[ck] + bytes;
       maxb = std::max(maxb, bytes);
     }
@@ -571,22 +571,20 @@ mg_status plan_device(mg_plan* p)
       const int64_t first = (int64_t)d.item_begin + (int64_t)c * CI;
       std::memcpy(r + 64, &hs.items[first], 4 * n4);
       std::memcpy(r + 64 + 4 * n4, &hs.item_lconn[4 * first], 8 * n4);
-      float4* vr = reinterpret_cast<float4*>(r + 64 + 12 * n4);
-      float* vz = reinterpret_cast<float*>(r + 64 + 12 * n4 + 32 * nn);
+      float4* va = reinterpret_cast<float4*>(r + 64 + 12 * n4);
+      float2* vb = reinterpret_cast<float2*>(r + 64 + 12 * n4 + 16 * nn);
+      const int64_t n0 = hs.chunk_nodes[hs.chunk_node_begin[ck]];  // origin: the chunk's first vertex
       for (int64_t i = 0; i < nn; ++i) {
-        // x = hi + mid + lo exactly: hi = fl(x), mid = fl(x - hi), lo = fl(x - hi - mid)
+        // r = x - origin (FP64), then r = hi + lo: hi = fl(r), lo = fl(r - hi)
         const int64_t nd = hs.chunk_nodes[hs.chunk_node_begin[ck] + i];
-        float h[3], md[3], l[3];
+        float h[3], l[3];
         for (int k = 0; k < 3; ++k) {
-          const double x = xyz[3 * nd + k];
-          h[k] = (float)x;
-          const double r1 = x - (double)h[k];
-          md[k] = (float)r1;
-          l[k] = (float)(r1 - (double)md[k]);
+          const double rr = xyz[3 * nd + k] - xyz[3 * n0 + k];
+          h[k] = (float)rr;
+          l[k] = (float)(rr - (double)h[k]);
         }
-        vr[2 * i] = make_float4(h[0], h[1], h[2], md[0]);
-        vr[2 * i + 1] = make_float4(md[1], md[2], l[0], l[1]);
-        vz[i] = l[2];
+        va[i] = make_float4(h[0], h[1], h[2], l[0]);
+        vb[i] = make_float2(l[1], l[2]);
       }
     }
     MG_TRY(upload(&p->d_chunk_data, data));
