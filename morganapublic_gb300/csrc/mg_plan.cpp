@@ -25,6 +25,9 @@
 #include <functional>
 #include <numeric>
 
+#include <omp.h>
+#include <parallel/algorithm>
+
 #include "mg_internal.h"
 
 namespace mg {
@@ -45,25 +48,54 @@ static mg_status build_pattern(mg_plan* p)
   mg_mesh* m = p->mesh;
   const int nb = m->nb;
   const int64_t E = m->n_elem, nd = m->ndof;
+  // dof -> incident elements (the order inside a row does not matter: the
+  // row's columns are de-duplicated and sorted below)
   std::vector<int64_t> start(nd + 1, 0);
-  for (int64_t k = 0; k < E * nb; ++k) start[m->dofs[k] + 1]++;
+#pragma omp parallel for
+  for (int64_t k = 0; k < E * nb; ++k) {
+#pragma omp atomic
+    start[m->dofs[k] + 1]++;
+  }
   for (int64_t r = 0; r < nd; ++r) start[r + 1] += start[r];
   std::vector<int64_t> fill(start.begin(), start.end() - 1);
   std::vector<int32_t> inc(E * nb);
-  for (int64_t k = 0; k < E * nb; ++k) inc[fill[m->dofs[k]]++] = (int32_t)(k / nb);
+#pragma omp parallel for
+  for (int64_t k = 0; k < E * nb; ++k) {
+    int64_t slot;
+#pragma omp atomic capture
+    slot = fill[m->dofs[k]]++;
+    inc[slot] = (int32_t)(k / nb);
+  }
+  // one pass over the rows: the union of the incident elements' dofs,
+  // de-duplicated with a per-thread stamp array (so only the ~15 unique columns
+  // of a P1 row are sorted), kept per thread and copied after the prefix sum
   std::vector<int32_t> len(nd, 0);
   int bad = 0;
-#pragma omp parallel
+  const int nth = std::max(1, omp_get_max_threads());
+  std::vector<std::vector<int32_t>> cols(nth);
+  std::vector<int64_t> chunk_row0(nth + 1, 0);
+#pragma omp parallel num_threads(nth)
   {
+    const int t = omp_get_thread_num();
+    const int64_t r0 = nd * t / nth, r1 = nd * (t + 1) / nth;
+    chunk_row0[t] = r0;
+    std::vector<int32_t> stamp(nd, -1);
+    std::vector<int32_t>& out = cols[t];
     std::vector<int32_t> tmp;
-#pragma omp for schedule(dynamic, 1024)
-    for (int64_t r = 0; r < nd; ++r) {
+    for (int64_t r = r0; r < r1; ++r) {
       tmp.clear();
-      for (int64_t t = start[r]; t < start[r + 1]; ++t)
-        for (int i = 0; i < nb; ++i) tmp.push_back(m->dofs[(int64_t)inc[t] * nb + i]);
+      for (int64_t k = start[r]; k < start[r + 1]; ++k)
+        for (int i = 0; i < nb; ++i) {
+          const int32_t c = m->dofs[(int64_t)inc[k] * nb + i];
+          if (stamp[c] != (int32_t)r) {
+            stamp[c] = (int32_t)r;
+            tmp.push_back(c);
+          }
+        }
       std::sort(tmp.begin(), tmp.end());
-      len[r] = (int32_t)(std::unique(tmp.begin(), tmp.end()) - tmp.begin());
+      len[r] = (int32_t)tmp.size();
       if (len[r] > kAccMax) bad = 1;
+      out.insert(out.end(), tmp.begin(), tmp.end());
     }
   }
   if (bad) return set_error(MG_ERR_SIZE, "a CSR row has more than 8192 entries");
@@ -75,19 +107,9 @@ static mg_status build_pattern(mg_plan* p)
   }
   p->nnz = p->rowptr[nd];
   p->colind.resize(p->nnz);
-#pragma omp parallel
-  {
-    std::vector<int32_t> tmp;
-#pragma omp for schedule(dynamic, 1024)
-    for (int64_t r = 0; r < nd; ++r) {
-      tmp.clear();
-      for (int64_t t = start[r]; t < start[r + 1]; ++t)
-        for (int i = 0; i < nb; ++i) tmp.push_back(m->dofs[(int64_t)inc[t] * nb + i]);
-      std::sort(tmp.begin(), tmp.end());
-      tmp.erase(std::unique(tmp.begin(), tmp.end()), tmp.end());
-      std::copy(tmp.begin(), tmp.end(), p->colind.begin() + p->rowptr[r]);
-    }
-  }
+#pragma omp parallel for num_threads(nth)
+  for (int t = 0; t < nth; ++t)
+    std::copy(cols[t].begin(), cols[t].end(), p->colind.begin() + p->rowptr[chunk_row0[t]]);
   p->ndof = nd;
   return MG_OK;
 }
@@ -242,17 +264,27 @@ static mg_status build_schedule(mg_plan* p, HostSchedule* hs)
       }
       ekey[e] = c;
     }
-#pragma omp parallel for schedule(dynamic, 16)
-    for (int32_t b = 0; b < nbk; ++b)
-      std::sort(hs->items.begin() + bcount[b], hs->items.begin() + bcount[b + 1], [&](int32_t x, int32_t y) {
-        return ekey[x] != ekey[y] ? ekey[x] < ekey[y] : x < y;
-      });
+#pragma omp parallel
+    {
+      std::vector<std::pair<uint64_t, int32_t>> kv;
+#pragma omp for schedule(dynamic, 16)
+      for (int32_t b = 0; b < nbk; ++b) {
+        kv.clear();
+        for (int64_t k = bcount[b]; k < bcount[b + 1]; ++k) kv.emplace_back(ekey[hs->items[k]], hs->items[k]);
+        std::sort(kv.begin(), kv.end());  // by key, ties by element id
+        for (int64_t k = bcount[b]; k < bcount[b + 1]; ++k) hs->items[k] = kv[k - bcount[b]].second;
+      }
+    }
     // the same order over all elements, for the per-element kernels (adjoint)
-    hs->elem_order.resize(E);
-    std::iota(hs->elem_order.begin(), hs->elem_order.end(), 0);
-    std::sort(hs->elem_order.begin(), hs->elem_order.end(), [&](int32_t x, int32_t y) {
-      return ekey[x] != ekey[y] ? ekey[x] < ekey[y] : x < y;
-    });
+    {
+      std::vector<std::pair<uint64_t, int32_t>> kv(E);
+#pragma omp parallel for
+      for (int64_t e = 0; e < E; ++e) kv[e] = std::make_pair(ekey[e], (int32_t)e);
+      __gnu_parallel::sort(kv.begin(), kv.end());
+      hs->elem_order.resize(E);
+#pragma omp parallel for
+      for (int64_t e = 0; e < E; ++e) hs->elem_order[e] = kv[e].second;
+    }
     std::vector<int32_t> padded;
     padded.reserve(hs->items.size() + 4 * (size_t)nbk);
     for (int32_t b = 0; b < nbk; ++b) {
@@ -442,16 +474,19 @@ static mg_status build_schedule(mg_plan* p, HostSchedule* hs)
   for (int32_t b = 0; b < nbk; ++b) total += (int64_t)ent[b].size();
   hs->entries.resize(total);
   hs->chunk_ptr.resize(nchunk_tot * (kWarps + 1));
-  int64_t off = 0, ck = 0;
+  std::vector<int64_t> boff(nbk + 1, 0);
   for (int32_t b = 0; b < nbk; ++b) {
-    std::copy(ent[b].begin(), ent[b].end(), hs->entries.begin() + off);
-    for (size_t k = 0; k < cptr[b].size(); ++k) hs->chunk_ptr[ck * (kWarps + 1) + k] = cptr[b][k] + off;
-    ck += hs->blocks[b].nchunks;
-    if (off % 32 != 0 || off / 32 >= INT32_MAX) return set_error(MG_ERR_SIZE, "contribution words above 2^36");
-    hs->blocks[b].word_begin32 = (int32_t)(off / 32);
-    off += (int64_t)ent[b].size();
+    boff[b + 1] = boff[b] + (int64_t)ent[b].size();
+    if (boff[b] % 32 != 0 || boff[b] / 32 >= INT32_MAX) return set_error(MG_ERR_SIZE, "contribution words above 2^36");
+    hs->blocks[b].word_begin32 = (int32_t)(boff[b] / 32);
     hs->n_contrib += contrib[b];
     hs->max_chunk_entries = std::max(hs->max_chunk_entries, maxc[b]);
+  }
+#pragma omp parallel for schedule(dynamic, 4)
+  for (int32_t b = 0; b < nbk; ++b) {
+    std::copy(ent[b].begin(), ent[b].end(), hs->entries.begin() + boff[b]);
+    const int64_t ck = hs->blocks[b].chunk_begin;
+    for (size_t k = 0; k < cptr[b].size(); ++k) hs->chunk_ptr[ck * (kWarps + 1) + k] = cptr[b][k] + boff[b];
     std::vector<uint32_t>().swap(ent[b]);
   }
   // blocks taken largest first (the work counter hands them out in array
