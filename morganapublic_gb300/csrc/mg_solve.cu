@@ -81,7 +81,7 @@ struct CgScalars {
 // per entry as possible: one thread per CSR row (one FMA per entry, no
 // shuffle-adds) with 16 entries loaded per pass and two accumulators, and
 // several vector entries per thread (the block reduction tree is paid once per
-// thread).  FP32 kernels use 4 lanes x 4 entries per row and more threads.
+// thread).  FP32 kernels use groups of 2+ lanes x 8 entries per row and more threads.
 static int sm_count()
 {
   static int sms = 0;
@@ -94,17 +94,19 @@ static int sm_count()
   return sms;
 }
 
-template <typename V> constexpr int kEntriesPerLane = sizeof(V) == 8 ? 16 : 4;
+template <typename V> constexpr int kEntriesPerLane = sizeof(V) == 8 ? 16 : 8;
 
-// Lanes per row of the standalone SpMV: one for FP64; for FP32 the smallest
-// group whose pass covers the mean row length.
+// Lanes per row of the standalone SpMV (measured on GB300 at P1 128^3 and P2
+// 48^3): FP64 one lane per row up to 16 entries on average (P1), two above
+// (P2); FP32 the smallest group of at least 2 lanes whose pass covers the mean
+// row length.
 template <typename V>
 static int row_group(const mg_plan* p)
 {
-  if (sizeof(V) == 8) return 1;
   const double mean = p->ndof > 0 ? (double)p->nnz / (double)p->ndof : 1.0;
+  if (sizeof(V) == 8) return mean > 16.0 ? 2 : 1;
   const int U = kEntriesPerLane<V>;
-  for (int g = 4; g < 32; g *= 2)
+  for (int g = 2; g < 32; g *= 2)
     if (mean <= g * U) return g;
   return 32;
 }
@@ -123,17 +125,17 @@ static int row_blocks(const mg_plan* p, int G)
 }
 
 // Shape of the CG kernels (measured on GB300 at 64^3 P1 and 32^3 / 48^3 P2):
-// FP64 rows by 2 lanes x 8 entries (the FP64 pipe bounds K1), at most 4 CTAs
-// per SM (fewer partials for the last CTA to sum), launched without
-// programmatic dependent launch (it slowed the FP64 iteration); FP32 as the
-// standalone SpMV, with programmatic dependent launch.
+// rows by 2 lanes x 8 entries (more lanes for longer rows); FP64 at most 4
+// CTAs per SM (fewer partials for the last CTA to sum) and launched without
+// programmatic dependent launch (it slowed the FP64 iteration); FP32 up to 8
+// CTAs per SM, with programmatic dependent launch.
 template <typename V> struct CgShape {
-  static constexpr int U = sizeof(V) == 8 ? 8 : kEntriesPerLane<V>;
+  static constexpr int U = 8;
   static constexpr bool pdl = sizeof(V) == 4;
   static int group(const mg_plan* p)
   {
     const double mean = p->ndof > 0 ? (double)p->nnz / (double)p->ndof : 1.0;
-    for (int g = sizeof(V) == 8 ? 2 : 4; g < 32; g *= 2)
+    for (int g = 2; g < 32; g *= 2)
       if (mean <= g * U) return g;
     return 32;
   }
