@@ -192,9 +192,10 @@ mg_status mg_assemble(mg_plan* plan, int32_t op, const double* d_coeff, double c
                       int32_t prec, void* d_values, void* stream);
 
 /* Synchronises the device and reports a failure recorded by an earlier
-   asynchronous assembly on this plan (a bounded wait inside the kernel that
-   gave up: the values of that call are incomplete).  Clears the record.
-   No reference counterpart (the reference asserts). */
+   asynchronous assembly on this plan: MG_ERR_CUDA when a bounded wait inside
+   the kernel gave up (the values of that call are incomplete),
+   MG_ERR_INVALID_ARG when the coefficient array held NaN or Inf.  Clears the
+   record.  No reference counterpart (the reference asserts). */
 mg_status mg_plan_status(mg_plan* plan);
 
 /* Host-buffer form of mg_assemble, the call an Epetra/Tpetra adapter makes:

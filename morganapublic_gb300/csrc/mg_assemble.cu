@@ -725,6 +725,9 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
           fetch_staged<MODE>(va, vb, lc, F);
           geometry(F, f);
           coef = A::from(coef_d);
+          // NaN / Inf coefficient: recorded for mg_plan_status (checked after the
+          // geometry, where the load has long landed)
+          if (((__double_as_longlong(coef_d) >> 52) & 0x7ff) == 0x7ff) atomicOr(&a.counters[4], 1u);
         };
         // P2 in the FP64 modes: the double-word geometry is worth computing once per
         // item; FP32 recomputes it in each of the item's threads (no extra barrier)
@@ -1039,6 +1042,7 @@ extern "C" {
 mg_status mg_assemble(mg_plan* plan, int32_t op, const double* d_coeff, double c, int32_t quad, int32_t prec,
                       void* d_values, void* stream)
 {
+  NvtxRange nvtx_range("mg_assemble");
   if (!plan) return set_error(MG_ERR_INVALID_ARG, "mg_assemble: null plan");
   return launch_assemble(plan, op, d_coeff, c, quad, prec, d_values, (cudaStream_t)stream);
 }
@@ -1048,20 +1052,24 @@ mg_status mg_plan_status(mg_plan* p)
   if (!p) return set_error(MG_ERR_INVALID_ARG, "mg_plan_status: null plan");
   if (!p->on_device) return MG_OK;
   MG_CUDA(cudaDeviceSynchronize());
-  uint32_t c[4];
+  uint32_t c[5];
   MG_CUDA(cudaMemcpy(c, p->d_counters, sizeof(c), cudaMemcpyDeviceToHost));
-  if (c[2]) {
-    const uint32_t zero[2] = {0u, 0u};
+  if (c[2] || c[4]) {
+    const uint32_t zero[3] = {0u, 0u, 0u};
     MG_CUDA(cudaMemcpy(p->d_counters + 2, zero, sizeof(zero), cudaMemcpyHostToDevice));
+  }
+  if (c[2])
     return set_error(MG_ERR_CUDA, "assembly kernel: a bulk-copy wait timed out in CTA " + std::to_string(c[3]) +
                                       "; the values of that call are incomplete");
-  }
+  if (c[4])
+    return set_error(MG_ERR_INVALID_ARG, "assembly: the coefficient array holds NaN or Inf (the values are not usable)");
   return MG_OK;
 }
 
 mg_status mg_assemble_host(mg_plan* p, int32_t op, const double* h_coeff, double c, int32_t quad, int32_t prec,
                            void* h_values, void* stream)
 {
+  NvtxRange nvtx_range("mg_assemble_host");
   if (!p || (!h_values && p->nnz > 0)) return set_error(MG_ERR_INVALID_ARG, "mg_assemble_host: null argument");
   MG_TRY(plan_device(p));
   cudaStream_t st = (cudaStream_t)stream;
@@ -1095,6 +1103,7 @@ mg_status mg_assemble_host(mg_plan* p, int32_t op, const double* h_coeff, double
 mg_status mg_apply_dirichlet(mg_plan* p, const uint8_t* d_mask, int32_t prec, void* d_values, double* d_b,
                              void* stream)
 {
+  NvtxRange nvtx_range("mg_apply_dirichlet");
   if (!p || !d_mask || !d_values) return set_error(MG_ERR_INVALID_ARG, "mg_apply_dirichlet: null argument");
   if (prec != MG_F64 && prec != MG_F32) return set_error(MG_ERR_INVALID_ARG, "bad precision");
   MG_TRY(plan_device(p));
@@ -1116,6 +1125,7 @@ mg_status mg_apply_dirichlet(mg_plan* p, const uint8_t* d_mask, int32_t prec, vo
 mg_status mg_adjoint_grad(mg_plan* p, const double* d_u, const double* d_lambda, int32_t quad, double* d_grad,
                           void* stream)
 {
+  NvtxRange nvtx_range("mg_adjoint_grad");
   if (!p || !d_u || !d_lambda || (!d_grad && p->mesh->n_elem > 0))
     return set_error(MG_ERR_INVALID_ARG, "mg_adjoint_grad: null argument");
   const RefTables* t = nullptr;
@@ -1142,6 +1152,7 @@ mg_status mg_adjoint_grad(mg_plan* p, const double* d_u, const double* d_lambda,
 mg_status mg_assemble_rhs(mg_plan* p, const double* d_field, const double* d_elem_scale, int32_t quad, double* d_b,
                           void* stream)
 {
+  NvtxRange nvtx_range("mg_assemble_rhs");
   if (!p || !d_b) return set_error(MG_ERR_INVALID_ARG, "mg_assemble_rhs: null argument");
   MG_TRY(plan_device(p));
   cudaStream_t st = (cudaStream_t)stream;

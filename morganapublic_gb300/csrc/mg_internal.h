@@ -6,6 +6,7 @@
 #include <vector>
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include "morgana_gpu.h"
 
@@ -20,6 +21,13 @@ mg_status cuda_error(cudaError_t e, const char* what);
     cudaError_t _e = (call);                                   \
     if (_e != cudaSuccess) return ::mg::cuda_error(_e, #call); \
   } while (0)
+
+// NVTX range over one C-ABI call (header-only NVTX3: no cost and no library
+// dependency unless a profiler is attached)
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+};
 
 #define MG_TRY(call)                  \
   do {                                \

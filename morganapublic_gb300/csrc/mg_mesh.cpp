@@ -370,6 +370,7 @@ extern "C" {
 mg_status mg_mesh_create(mg_mesh** out, int64_t n_nodes, const double* h_xyz, int64_t n_elements,
                          const int32_t* h_conn, int32_t order, int32_t edge_rule)
 {
+  NvtxRange nvtx_range("mg_mesh_create");
   if (!out || n_nodes < 0 || n_elements < 0 || (n_nodes > 0 && !h_xyz) ||
       (n_elements > 0 && !h_conn))
     return set_error(MG_ERR_INVALID_ARG, "mg_mesh_create: null or negative argument");
@@ -398,6 +399,7 @@ mg_status mg_mesh_create(mg_mesh** out, int64_t n_nodes, const double* h_xyz, in
 
 mg_status mg_mesh_load_gmsh(mg_mesh** out, const char* path, int32_t order, int32_t edge_rule)
 {
+  NvtxRange nvtx_range("mg_mesh_load_gmsh");
   if (!out || !path) return set_error(MG_ERR_INVALID_ARG, "mg_mesh_load_gmsh: null argument");
   std::ifstream f(path);
   if (!f) return set_error(MG_ERR_IO, std::string("cannot open ") + path);

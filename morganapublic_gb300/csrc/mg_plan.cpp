@@ -708,6 +708,7 @@ extern "C" {
 
 mg_status mg_pattern_build(mg_mesh* mesh, mg_plan** out)
 {
+  NvtxRange nvtx_range("mg_pattern_build");
   if (!mesh || !out) return set_error(MG_ERR_INVALID_ARG, "mg_pattern_build: null argument");
   *out = nullptr;
   mg_plan* p = new mg_plan();

@@ -740,6 +740,7 @@ extern "C" {
 mg_status mg_cg_solve_noalloc(mg_plan* p, const double* d_values, const double* d_b, double* d_x, double rtol,
                               int32_t maxit, int32_t precond, mg_cg_info* info, void* stream)
 {
+  NvtxRange nvtx_range("mg_cg_solve_noalloc");
   if (!p || !d_values || !d_b || !d_x) return set_error(MG_ERR_INVALID_ARG, "mg_cg_solve_noalloc: null argument");
   if (!(rtol > 0.0) || maxit < 0)
     return set_error(MG_ERR_INVALID_ARG, "mg_cg_solve_noalloc: rtol must be > 0, maxit >= 0");
@@ -801,6 +802,7 @@ mg_status mg_cg_solve_noalloc(mg_plan* p, const double* d_values, const double* 
 
 mg_status mg_spmv(mg_plan* plan, int32_t prec, const void* d_values, const void* d_x, void* d_y, void* stream)
 {
+  NvtxRange nvtx_range("mg_spmv");
   if (!plan) return set_error(MG_ERR_INVALID_ARG, "mg_spmv: null plan");
   return launch_spmv(plan, prec, d_values, d_x, d_y, (cudaStream_t)stream);
 }
@@ -808,6 +810,7 @@ mg_status mg_spmv(mg_plan* plan, int32_t prec, const void* d_values, const void*
 mg_status mg_cg_solve(mg_plan* p, const double* d_values, const double* d_b, double* d_x, double rtol,
                       int32_t maxit, int32_t precond, mg_cg_info* info, void* stream)
 {
+  NvtxRange nvtx_range("mg_cg_solve");
   if (!p || !d_values || !d_b || !d_x) return set_error(MG_ERR_INVALID_ARG, "mg_cg_solve: null argument");
   if (!(rtol > 0.0) || maxit < 0) return set_error(MG_ERR_INVALID_ARG, "mg_cg_solve: rtol must be > 0, maxit >= 0");
   MG_TRY(plan_device(p));
@@ -847,6 +850,7 @@ mg_status mg_cg_refined(mg_plan* p, const double* d_values64, const float* d_val
                         double* d_x, double rtol, int32_t max_outer, int32_t max_inner, double inner_rtol,
                         int32_t precond, mg_cg_info* info, void* stream)
 {
+  NvtxRange nvtx_range("mg_cg_refined");
   if (!p || !d_values64 || !d_values32 || !d_b || !d_x)
     return set_error(MG_ERR_INVALID_ARG, "mg_cg_refined: null argument");
   if (!(rtol > 0.0) || !(inner_rtol > 0.0) || !(inner_rtol < 1.0) || max_outer < 1 || max_inner < 1)

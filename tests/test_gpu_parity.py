@@ -220,6 +220,26 @@ def test_unreferenced_nodes_give_empty_rows():
     assert np.max(np.abs(y - y_ref)) <= 1e-12 * np.abs(y_ref).max()
 
 
+def test_nonfinite_coefficient_is_reported():
+    """A NaN or Inf in the per-element coefficient is an error returned through
+    the C ABI (mg_plan_status; the host-buffer call checks it itself); a clean
+    assembly afterwards reports nothing."""
+    m, kappa = _case(3, 0.2, 12, True, 1.0)
+    b = mg.MatrixBuilder(mg.Mesh(m.xyz, m.conn, order=1))
+    for bad in (np.nan, np.inf):
+        k = kappa.copy()
+        k[len(k) // 2] = bad
+        b.assemble("stiff_kappa", coeff=torch.from_numpy(k).cuda(), quad=4)
+        with pytest.raises(mg.MorganaError) as e:
+            b.status()
+        assert e.value.status == mg.MG_ERR_INVALID_ARG
+        with pytest.raises(mg.MorganaError) as e:
+            b.build_crs("stiff_kappa", coeff=k, quad=4)
+        assert e.value.status == mg.MG_ERR_INVALID_ARG
+    b.assemble("stiff_kappa", coeff=torch.from_numpy(kappa).cuda(), quad=4)
+    b.status()
+
+
 def test_cg_deterministic_and_maxit_status():
     m, kappa, mesh, b, dofs, rp, ci, K, mask, rhs, quad = _dirichlet_system(5, 1, 1.0, 6)
     v = b.assemble("stiff_kappa", coeff=kappa, quad=quad)
