@@ -242,7 +242,9 @@ mg_status mg_cg_solve(mg_plan* plan, const double* d_values, const double* d_b, 
    and replaces the FP32 residual; the search direction is kept, so the Krylov
    sequence is not restarted.  Stops when ||b - A64 x||_2 <= rtol ||b||_2 (true
    FP64 residual).  max_outer bounds the number of FP64 anchors, max_inner the
-   FP32 iterations in total.  mg_cg_info.iterations counts FP32 iterations,
+   FP32 iterations in total.  Useful inner_rtol: 1e-3 .. 0.5 (1e-2 works well);
+   smaller values are raised to 1e-3, because the FP32 recursion drifts from the
+   true residual over more than ~3 decades.  mg_cg_info.iterations counts FP32 iterations,
    outer_iterations the anchors.  Build addition (no reference counterpart);
    same role as mg_cg_solve. */
 mg_status mg_cg_refined(mg_plan* plan, const double* d_values64, const float* d_values32,

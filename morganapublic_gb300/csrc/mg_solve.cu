@@ -628,6 +628,9 @@ static CgWork<V> cg_work_carve(void* base, int64_t n)
   return w;
 }
 
+// Smallest reliable-update trigger ratio of the mixed-precision CG.
+constexpr double kMinAnchorRatio = 1e-3;
+
 // Iterations per replay of the captured CG graph between two host checks.
 constexpr int kGraphIters = 16;
 
@@ -904,7 +907,10 @@ mg_status mg_cg_refined(mg_plan* p, const double* d_values64, const float* d_val
       hs->bb = 1.0;
       hs->tol2 = rtol * rtol * bb64;  // recursive-residual target: ||r|| <= rtol ||b||
       hs->rr_anchor = hs->rr;
-      hs->delta2 = inner_rtol * inner_rtol;
+      // the FP32 recursion drifts from the true residual beyond ~3 decades
+      // between anchors (measured: 1e-4 took 33x the iterations on P2 48^3)
+      const double delta = std::max(inner_rtol, kMinAnchorRatio);
+      hs->delta2 = delta * delta;
       hs->done = 0;
       MG_CUDA(cudaMemcpyAsync(w.s, hs, sizeof(CgScalars), cudaMemcpyHostToDevice, st));
     }
