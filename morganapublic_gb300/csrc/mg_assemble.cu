@@ -77,7 +77,7 @@ template <> struct Arith<kDW> {
   using Out = double;
   __device__ static T from(double x) { return ff_from_double_bits(x); }
   __device__ static T zero() { return ff{0.0f, 0.0f}; }
-  __device__ static Out out(T v) { return ff_to_double_bits(v); }
+  __device__ static Out out(T v) { return ff_to_double_int(v); }
 };
 template <> struct Arith<kF64> {
   using T = double;

@@ -171,6 +171,26 @@ __device__ __forceinline__ double f2d_bits(float f)
 // hi + lo as a double: both parts exact, one FP64 addition.
 __device__ __forceinline__ double ff_to_double_bits(ff a) { return f2d_bits(a.hi) + f2d_bits(a.lo); }
 
+// hi + lo as a double without FP64 arithmetic: after renormalisation
+// (|lo| <= ulp(hi)/2), lo is expressed in units of the double ulp of hi
+// (a power-of-two scaling, exact) and rounded to an integer n, which is added
+// to the bit pattern of double(hi) -- integer carries cross binades correctly,
+// so the result is within half a double ulp of hi + lo.  Outside the range
+// where the scaling stays a normal float (|hi| below ~2^-74 or above ~2^127),
+// and for zero, Inf or NaN, it falls back to ff_to_double_bits.
+__device__ __forceinline__ double ff_to_double_int(ff a)
+{
+  const ff n = fast_two_sum(a.hi, a.lo);
+  const uint32_t u = __float_as_uint(n.hi);
+  const int e = (int)((u >> 23) & 0xffu) - 127;  // unbiased exponent of hi
+  if (e < -74 || e > 126 || n.hi == 0.0f) return ff_to_double_bits(n);
+  const float scale = __uint_as_float((uint32_t)(52 - e + 127) << 23);  // 2^(52 - e)
+  int k = __float2int_rn(__fmul_rn(n.lo, scale));                    // lo / ulp_double(hi)
+  if (u >> 31) k = -k;  // magnitudes: the bit pattern grows with |x|
+  const long long bits = __double_as_longlong(f2d_bits(n.hi)) + (long long)k;
+  return __longlong_as_double(bits);
+}
+
 // double -> hi + lo: hi keeps the top 24 bits of the significand (truncated,
 // exact), lo the next 24 bits rounded -- |x - hi - lo| <= 2^-48 |x|.  For
 // |x| in the normal float range (about 1e-38 .. 3e38) and x = 0; other values
