@@ -38,6 +38,7 @@
 // kF64 stays available for comparison (MG_ASSEMBLY_NATIVE_F64=1).
 #include <cstdio>
 #include <cstdlib>
+#include <mutex>
 
 #include "mg_ff.cuh"
 #include "mg_internal.h"
@@ -873,25 +874,42 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
   }
 }
 
+// Per kernel instantiation and device: SM count, opt-in shared-memory limit and
+// the dynamic shared-memory size the kernel attribute has been raised to
+// (only ever raised, so plans of different sizes and threads can share it).
+struct KernelLaunchCache {
+  static constexpr int kMaxDevices = 64;
+  std::mutex mu;
+  int sms[kMaxDevices] = {};
+  int max_smem[kMaxDevices] = {};
+  size_t attr_smem[kMaxDevices] = {};
+};
+
 template <int ORDER, int MODE>
 static mg_status launch_assemble_t(AsmArgs a, cudaStream_t st)
 {
   using L = AsmLayout<ORDER, MODE>;
   const size_t smem = L::total(a.ent_cap, a.stage_cap);
-  static size_t configured = 0;
-  static int per_sm = 0, sms = 0, max_smem = 0;
-  if (configured != smem) {
-    int dev = 0;
-    MG_CUDA(cudaGetDevice(&dev));
-    MG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    MG_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    if (smem > (size_t)max_smem)
+  static KernelLaunchCache cache;
+  int dev = 0, sms = 0, per_sm = 0;
+  MG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= KernelLaunchCache::kMaxDevices) return set_error(MG_ERR_UNSUPPORTED, "device index above 63");
+  {
+    std::lock_guard<std::mutex> lock(cache.mu);
+    if (!cache.sms[dev]) {
+      MG_CUDA(cudaDeviceGetAttribute(&cache.sms[dev], cudaDevAttrMultiProcessorCount, dev));
+      MG_CUDA(cudaDeviceGetAttribute(&cache.max_smem[dev], cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    }
+    if (smem > (size_t)cache.max_smem[dev])
       return set_error(MG_ERR_SIZE, "assembly CTA needs " + std::to_string(smem) + " bytes of shared memory, above " +
-                                        std::to_string(max_smem) + " (chunks touch too many vertices)");
-    MG_CUDA(cudaFuncSetAttribute(k_assemble<ORDER, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_assemble<ORDER, MODE>, kAsmThreads, smem));
-    configured = smem;
+                                        std::to_string(cache.max_smem[dev]) + " (chunks touch too many vertices)");
+    if (cache.attr_smem[dev] < smem) {
+      MG_CUDA(cudaFuncSetAttribute(k_assemble<ORDER, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      cache.attr_smem[dev] = smem;
+    }
+    sms = cache.sms[dev];
   }
+  MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_assemble<ORDER, MODE>, kAsmThreads, smem));
   if (per_sm < 1) return set_error(MG_ERR_SIZE, "assembly CTA does not fit on an SM (shared memory)");
   const int grid = std::max(1, std::min(a.nblocks, per_sm * sms));
   if (a.nblocks > 0) k_assemble<ORDER, MODE><<<grid, kAsmThreads, smem, st>>>(a);

@@ -23,6 +23,7 @@
 // Dot products accumulate in FP64 in both precisions; the order of every
 // floating-point sum is fixed, so a solve is bitwise reproducible.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <mutex>
@@ -82,14 +83,19 @@ struct CgScalars {
 // shuffle-adds) with 16 entries loaded per pass and two accumulators, and
 // several vector entries per thread (the block reduction tree is paid once per
 // thread).  FP32 kernels use groups of 2+ lanes x 8 entries per row and more threads.
+// SMs of the current device (cached per device; racing first calls store the
+// same value)
 static int sm_count()
 {
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
+  static std::atomic<int> cached[64];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  int sms = cached[dev].load(std::memory_order_relaxed);
+  if (sms <= 0) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (sms <= 0) sms = 1;
+    cached[dev].store(sms, std::memory_order_relaxed);
   }
   return sms;
 }

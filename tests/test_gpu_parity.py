@@ -240,6 +240,46 @@ def test_nonfinite_coefficient_is_reported():
     b.status()
 
 
+def test_concurrent_plans_on_host_threads():
+    """One handle per host thread: two threads assemble and apply plans of
+    different sizes (different shared-memory needs) on their own streams at the
+    same time; every result equals the one computed alone, bit for bit."""
+    import threading
+    cases = []
+    for n, order in ((5, 1), (3, 2)):
+        m, kappa = _case(n, 0.2, 20 + n, True, 1.0)
+        b = mg.MatrixBuilder(mg.Mesh(m.xyz, m.conn, order=order))
+        kap = torch.from_numpy(kappa).cuda()
+        x = torch.from_numpy(np.random.default_rng(n).uniform(-1, 1, b.ndof)).cuda()
+        q = 4 if order == 1 else 15
+        ref_v = b.assemble("stiff_kappa", coeff=kap, quad=q)
+        ref_y = b.apply(ref_v, x)
+        torch.cuda.synchronize()
+        cases.append((b, kap, x, q, ref_v, ref_y))
+    errors = []
+
+    def work(case):
+        b, kap, x, q, ref_v, ref_y = case
+        st = torch.cuda.Stream()
+        try:
+            for _ in range(5):
+                v = b.assemble("stiff_kappa", coeff=kap, quad=q, stream=st)
+                y = b.apply(v, x, stream=st)
+                st.synchronize()
+                if not (torch.equal(v, ref_v) and torch.equal(y, ref_y)):
+                    errors.append("mismatch")
+            b.status()
+        except Exception as ex:  # reported to the main thread
+            errors.append(repr(ex))
+
+    ts = [threading.Thread(target=work, args=(c,)) for c in cases]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    assert not errors, errors
+
+
 def test_cg_deterministic_and_maxit_status():
     m, kappa, mesh, b, dofs, rp, ci, K, mask, rhs, quad = _dirichlet_system(5, 1, 1.0, 6)
     v = b.assemble("stiff_kappa", coeff=kappa, quad=quad)
