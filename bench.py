@@ -50,7 +50,9 @@ def parse():
     ap.add_argument("--config", type=int, default=2, choices=[2, 3, 5],
                     help="2: the headline step (default); 3: P2 48^3 mixed-precision vs FP64 CG; "
                          "5: P1 128^3 kernels as fractions of the HBM roofline")
-    ap.add_argument("--only", default=None, choices=["asm64", "asm32", "spmv64", "spmv32", "cg64", "cg32"],
+    ap.add_argument("--order", type=int, default=1, choices=[1, 2], help="element order of the --only modes")
+    ap.add_argument("--only", default=None,
+                    choices=["asm64", "asm32", "spmv64", "spmv32", "cg64", "cg32", "adj", "suite"],
                     help="run warmup + steps launches of one kernel only (for profilers) and print its timing")
     return ap.parse_args()
 
@@ -87,6 +89,11 @@ def profiled_traffic(kernel):
 def asm_bytes(E, nv, nnz, sv, nb=4):
     """algorithmic bytes of one assembly: E (16 conn + 8 kappa + 4 nb^2 slot map) + 24 n_v + s_v nnz"""
     return E * (16 + 8 + 4 * nb * nb) + 24 * nv + sv * nnz
+
+
+def adj_bytes(E, nv, ndof, nb=4):
+    """E (4 element id + 4 nb dofs + 8 gradient) + 36 n_v (node record) + 16 ndof (u, lambda)"""
+    return E * (12 + 4 * nb) + 36 * nv + 16 * ndof
 
 
 def spmv_bytes(ndof, nnz, sv):
@@ -243,17 +250,42 @@ def run_only(a):
     from morganapublic_gb300 import meshgen
     m = meshgen.kuhn_cube(a.n, jitter=a.jitter, seed=a.seed, permute=True)
     kappa = torch.from_numpy(meshgen.lognormal(len(m.conn), a.sigma, a.seed)).cuda()
-    b = mg.MatrixBuilder(mg.Mesh(m.xyz, m.conn, order=1))
+    mesh = mg.Mesh(m.xyz, m.conn, order=a.order)
+    b = mg.MatrixBuilder(mesh)
+    quad = 4 if a.order == 1 else 11
     stream = torch.cuda.Stream()
     x = torch.from_numpy(np.random.default_rng(a.seed).uniform(-1, 1, b.ndof)).cuda()
-    v64 = b.assemble("stiff_kappa", coeff=kappa, prec="f64")
-    v32 = b.assemble("stiff_kappa", coeff=kappa, prec="f32")
+    v64 = b.assemble("stiff_kappa", coeff=kappa, quad=quad, prec="f64")
+    v32 = b.assemble("stiff_kappa", coeff=kappa, quad=quad, prec="f32")
     x32, y, y32 = x.float(), torch.empty_like(x), torch.empty_like(x, dtype=torch.float32)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    if a.only == "suite":
+        # every kernel of the path once per round (for a per-kernel ncu launch list):
+        # assembly FP64 + FP32, load vector, Dirichlet elimination, SpMV FP64 + FP32,
+        # a few PCG iterations FP64 and FP32-refined, adjoint gradient
+        mask = torch.from_numpy(m.boundary if a.order == 1 else meshgen.p2_boundary(m.boundary, mesh.edges()[0]))
+        lam = torch.from_numpy(np.random.default_rng(a.seed + 1).uniform(-1, 1, b.ndof)).cuda()
+        g = torch.empty(len(m.conn), dtype=torch.float64, device="cuda")
+        with torch.cuda.stream(stream):
+            for r in range(a.warmup + a.steps):
+                b.assemble("stiff_kappa", coeff=kappa, quad=quad, prec="f64", out=v64, stream=stream)
+                b.assemble("stiff_kappa", coeff=kappa, quad=quad, prec="f32", out=v32, stream=stream)
+                rhs = b.build_vector(quad=quad, stream=stream)
+                b.apply_dirichlet(v64, mask, rhs, stream=stream)
+                b.apply_dirichlet(v32, mask, stream=stream)
+                b.apply(v64, x, out=y, stream=stream)
+                b.apply(v32, x32, out=y32, stream=stream)
+                b.cg(v64, rhs, rtol=1e-30, maxit=16, stream=stream, raise_on_fail=False)
+                b.cg_refined(v64, v32, rhs, rtol=1e-30, max_outer=2, max_inner=16, stream=stream,
+                             raise_on_fail=False)
+                b.adjoint_grad(x, lam, quad=quad, out=g, stream=stream)
+        torch.cuda.synchronize()
+        print(json.dumps({"only": a.only, "n": a.n, "order": a.order, "rounds": a.warmup + a.steps}))
+        return 0
     if a.only in ("cg64", "cg32"):
         # a fixed number of PCG iterations on the Dirichlet system (f = 1)
-        rhs = b.build_vector(quad=4)
-        mask = torch.from_numpy(m.boundary)
+        rhs = b.build_vector(quad=quad)
+        mask = torch.from_numpy(m.boundary if a.order == 1 else meshgen.p2_boundary(m.boundary, mesh.edges()[0]))
         b.apply_dirichlet(v64, mask, rhs)
         b.apply_dirichlet(v32, mask)
         ts = []
@@ -271,12 +303,18 @@ def run_only(a):
                     ts.append((time.perf_counter() - t0) * 1e3 / max(1, info.iterations))
         print(json.dumps({"only": a.only, "n": a.n, "ms_per_iteration": statistics.median(ts)}))
         return 0
-    fn = {"asm64": lambda: b.assemble("stiff_kappa", coeff=kappa, prec="f64", out=v64, stream=stream),
-          "asm32": lambda: b.assemble("stiff_kappa", coeff=kappa, prec="f32", out=v32, stream=stream),
+    lam = torch.from_numpy(np.random.default_rng(a.seed + 1).uniform(-1, 1, b.ndof)).cuda()
+    g = torch.empty(len(m.conn), dtype=torch.float64, device="cuda")
+    nb = 4 if a.order == 1 else 10
+    fn = {"asm64": lambda: b.assemble("stiff_kappa", coeff=kappa, quad=quad, prec="f64", out=v64, stream=stream),
+          "asm32": lambda: b.assemble("stiff_kappa", coeff=kappa, quad=quad, prec="f32", out=v32, stream=stream),
           "spmv64": lambda: b.apply(v64, x, out=y, stream=stream),
-          "spmv32": lambda: b.apply(v32, x32, out=y32, stream=stream)}[a.only]
-    byts = {"asm64": asm_bytes(len(m.conn), len(m.xyz), b.nnz, 8), "asm32": asm_bytes(len(m.conn), len(m.xyz), b.nnz, 4),
-            "spmv64": spmv_bytes(b.ndof, b.nnz, 8), "spmv32": spmv_bytes(b.ndof, b.nnz, 4)}[a.only]
+          "spmv32": lambda: b.apply(v32, x32, out=y32, stream=stream),
+          "adj": lambda: b.adjoint_grad(x, lam, quad=quad, out=g, stream=stream)}[a.only]
+    E, nv = len(m.conn), len(m.xyz)
+    byts = {"asm64": asm_bytes(E, nv, b.nnz, 8, nb), "asm32": asm_bytes(E, nv, b.nnz, 4, nb),
+            "spmv64": spmv_bytes(b.ndof, b.nnz, 8), "spmv32": spmv_bytes(b.ndof, b.nnz, 4),
+            "adj": adj_bytes(E, nv, b.ndof, nb)}[a.only]
     ts = []
     torch.cuda.synchronize()
     with torch.cuda.stream(stream):
@@ -290,7 +328,8 @@ def run_only(a):
             if r >= a.warmup:
                 ts.append(e0.elapsed_time(e1))
     ms = statistics.median(ts)
-    print(json.dumps({"only": a.only, "n": a.n, "ms": ms, "gbs": byts / ms / 1e6, "algorithmic_bytes": byts}))
+    print(json.dumps({"only": a.only, "n": a.n, "order": a.order, "ms": ms, "gbs": byts / ms / 1e6,
+                      "algorithmic_bytes": byts}))
     return 0
 
 
@@ -457,7 +496,7 @@ def run_config5(a):
             "assembly_f32": rec(asm_bytes(E, N, nnz, 4), ta32, E),
             "spmv_f64": rec(spmv_bytes(ndof, nnz, 8), ts64),
             "spmv_f32": rec(spmv_bytes(ndof, nnz, 4), ts32),
-            "adjoint_grad": rec(24 * E + 24 * N + 16 * ndof, tg, E),
+            "adjoint_grad": rec(adj_bytes(E, N, ndof), tg, E),
             "cg": {"fp64_pcg": i64.as_dict(), "fp32_refined": imx.as_dict(),
                    "speedup_refined_vs_fp64": i64.seconds / imx.seconds if imx.seconds > 0 else None,
                    "refined_vs_fp64_rel_diff": diff, "precond": "jacobi", "rtol": 1e-10},
