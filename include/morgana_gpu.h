@@ -56,8 +56,17 @@ enum {
   MG_OP_MASS_COEFF = 3   /* opEL3dM: kappa_e u v              (opEL3dM.hpp:129-158) */
 };
 
-/* Value precision of an assembled operator / vector. */
-enum { MG_F64 = 0, MG_F32 = 1 };
+/* Value precision of an assembled operator / vector.
+   MG_F64: double values; the assembly computes them in double-word FP32
+     arithmetic (two floats per number, ~48-bit significand, FP64-accurate to
+     1e-12) while element-matrix scales (coefficient x geometry) stay within
+     2^-96 .. 2^112 in magnitude; outside that range it records a failure that
+     mg_plan_status reports (MG_ERR_UNSUPPORTED).
+   MG_F32: float values, FP32 arithmetic.
+   MG_F64_NATIVE: double values assembled in native FP64 arithmetic (the full
+     FP64 range; bound by the FP64 pipe, several times slower).  Every other
+     entry point treats it as MG_F64. */
+enum { MG_F64 = 0, MG_F32 = 1, MG_F64_NATIVE = 2 };
 
 /* Quadrature: the reference's linearTetra STANDARD cards
    (src/morganaIntegrator/intStaticCards.cpp:707-991) plus the published 11-point
@@ -194,8 +203,10 @@ mg_status mg_assemble(mg_plan* plan, int32_t op, const double* d_coeff, double c
 /* Synchronises the device and reports a failure recorded by an earlier
    asynchronous assembly on this plan: MG_ERR_CUDA when a bounded wait inside
    the kernel gave up (the values of that call are incomplete),
-   MG_ERR_INVALID_ARG when the coefficient array held NaN or Inf.  Clears the
-   record.  No reference counterpart (the reference asserts). */
+   MG_ERR_INVALID_ARG when the coefficient array held NaN or Inf,
+   MG_ERR_UNSUPPORTED when an MG_F64 assembly met element-matrix scales outside
+   its double-word range (assemble with MG_F64_NATIVE, or rescale the
+   coefficient by a power of two).  Clears the record.  No reference counterpart (the reference asserts). */
 mg_status mg_plan_status(mg_plan* plan);
 
 /* Host-buffer form of mg_assemble, the call an Epetra/Tpetra adapter makes:

@@ -35,7 +35,7 @@ MG_OK, MG_ERR_INVALID_ARG, MG_ERR_CUDA, MG_ERR_ALLOC, MG_ERR_BAD_MESH = 0, 1, 2,
 MG_ERR_NOT_CONVERGED, MG_ERR_UNSUPPORTED, MG_ERR_IO, MG_ERR_SIZE = 5, 6, 7, 8
 EDGES = {"lex": 0, "first": 1}
 OPS = {"stiff_kappa": 0, "stiff_const": 1, "mass": 2, "mass_coeff": 3}
-PRECS = {"f64": 0, "f32": 1}
+PRECS = {"f64": 0, "f32": 1, "f64_native": 2}  # f64_native: assembly in native FP64 (full range)
 PRECOND = {None: 0, "none": 0, "jacobi": 1}
 
 
@@ -277,7 +277,7 @@ class MatrixBuilder:
                  out=None, stream=None):
         """CSR values on the GPU (torch tensor of nnz float64/float32)."""
         torch = _torch()
-        dt = torch.float64 if prec == "f64" else torch.float32
+        dt = torch.float32 if prec == "f32" else torch.float64
         if out is None:
             out = torch.empty(self.nnz, dtype=dt, device="cuda")
         if coeff is not None:
@@ -290,7 +290,7 @@ class MatrixBuilder:
                   prec: str = "f64") -> Csr:
         """Host-buffer assembly (what buildEpetraCrs hands to Epetra): pattern + values."""
         _torch()
-        vals = np.empty(self.nnz, dtype=np.float64 if prec == "f64" else np.float32)
+        vals = np.empty(self.nnz, dtype=np.float32 if prec == "f32" else np.float64)
         cf = None if coeff is None else np.ascontiguousarray(coeff, dtype=np.float64)
         _check(lib().mg_assemble_host(self._h, OPS[op], _ptr(cf), float(c), quad, PRECS[prec], _ptr(vals),
                                       _stream_ptr(None)), "mg_assemble_host")

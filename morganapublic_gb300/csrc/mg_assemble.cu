@@ -35,7 +35,7 @@
 // Arithmetic modes: kF32 (FP32 values), kDW (FP64-accurate values from
 // double-word float arithmetic on the FP32 pipes, written as IEEE doubles), kF64
 // (native FP64).  GB300 runs FP64 at ~1/60 of its FP32 rate, so MG_F64 uses kDW;
-// kF64 stays available for comparison (MG_ASSEMBLY_NATIVE_F64=1).
+// MG_F64_NATIVE selects kF64 (the full FP64 exponent range).
 #include <cstdio>
 #include <cstdlib>
 #include <mutex>
@@ -53,6 +53,15 @@ __device__ __forceinline__ ff operator-(ff a, ff b) { return ff_add_s(a, ff_neg(
 __device__ __forceinline__ ff operator-(ff a) { return ff_neg(a); }
 __device__ __forceinline__ ff operator*(ff a, ff b) { return ff_mul(a, b); }
 __device__ __forceinline__ ff operator/(ff a, ff b) { return ff_div(a, b); }
+
+// An element's scale factor inside the range where the double-word assembly is
+// FP64-accurate: zero, or |v| in 2^-96 .. 2^112 (the error terms of products
+// stay normal floats and no intermediate overflows).
+__device__ __forceinline__ bool dw_scale_ok(ff v)
+{
+  const uint32_t ex = (__float_as_uint(v.hi) >> 23) & 0xffu;
+  return v.hi == 0.0f || (ex >= 127u - 96u && ex <= 127u + 112u);
+}
 
 template <int MODE> struct Arith;
 // sum_into(s, x): s += x for the phase-2 sums.  The double-word form defers
@@ -730,6 +739,11 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
           // geometry, where the load has long landed)
           if (((__double_as_longlong(coef_d) >> 52) & 0x7ff) == 0x7ff) atomicOr(&a.counters[4], 1u);
         };
+        // double-word range of an element's scale factors, recorded for mg_plan_status
+        auto check_scale = [&](const T& x, const T& y) {
+          if constexpr (MODE == kDW)
+            if (!dw_scale_ok(x) || !dw_scale_ok(y)) atomicOr(&a.counters[4], 2u);
+        };
         // P2 in the FP64 modes: the double-word geometry is worth computing once per
         // item; FP32 recomputes it in each of the item's threads (no extra barrier)
         constexpr bool kGeoOnce = ORDER == 2 && MODE != kF32;
@@ -754,9 +768,12 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
             item_geometry(local, f, coef);
             T K[10];
             if (a.stiff) {
-              p1_stiff_unique<T>(f, coef * wsum / f.det, K);
+              const T sc = coef * wsum / f.det;
+              p1_stiff_unique<T>(f, sc, K);
+              check_scale(sc, K[4]);
             } else {
               const T sc = coef * f.det;
+              check_scale(sc, sc);
 #pragma unroll
               for (int u = 0; u < 10; ++u) K[u] = sc * tab[6 * NU + u];
             }
@@ -773,11 +790,15 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
             item_geometry(lane, f, coef);
             if (a.stiff) {
               T gm[6];
-              metric<T>(f, coef / f.det, gm);
+              const T sc = coef / f.det;
+              metric<T>(f, sc, gm);
+              check_scale(sc, gm[0]);
 #pragma unroll
               for (int k = 0; k < 6; ++k) sgeo[lane * 6 + k] = gm[k];
             } else {
-              sgeo[lane * 6] = coef * f.det;
+              const T sc = coef * f.det;
+              check_scale(sc, sc);
+              sgeo[lane * 6] = sc;
             }
           }
           failed = group_sync_or(g, failed);
@@ -917,22 +938,12 @@ static mg_status launch_assemble_t(AsmArgs a, cudaStream_t st)
   return MG_OK;
 }
 
-static bool native_f64()
-{
-  static int v = -1;
-  if (v < 0) {
-    const char* e = std::getenv("MG_ASSEMBLY_NATIVE_F64");
-    v = (e && e[0] == '1') ? 1 : 0;
-  }
-  return v == 1;
-}
-
 mg_status launch_assemble(mg_plan* p, int op, const double* d_coeff, double c, int quad, int prec,
                           void* d_values, cudaStream_t st)
 {
   if (op < MG_OP_STIFF_KAPPA || op > MG_OP_MASS_COEFF)
     return set_error(MG_ERR_INVALID_ARG, "unknown operator " + std::to_string(op));
-  if (prec != MG_F64 && prec != MG_F32) return set_error(MG_ERR_INVALID_ARG, "prec must be MG_F64 or MG_F32");
+  if (!prec_valid(prec)) return set_error(MG_ERR_INVALID_ARG, "prec must be MG_F64, MG_F32 or MG_F64_NATIVE");
   const bool needs_coeff = (op == MG_OP_STIFF_KAPPA || op == MG_OP_MASS_COEFF);
   if (needs_coeff && !d_coeff && p->mesh->n_elem > 0)
     return set_error(MG_ERR_INVALID_ARG, "this operator needs the per-element coefficient array");
@@ -961,10 +972,10 @@ mg_status launch_assemble(mg_plan* p, int op, const double* d_coeff, double c, i
   a.stage_cap = std::max(p->max_rec_bytes, 64);
   if (m->order == 1) {
     if (prec == MG_F32) return launch_assemble_t<1, kF32>(a, st);
-    return native_f64() ? launch_assemble_t<1, kF64>(a, st) : launch_assemble_t<1, kDW>(a, st);
+    return prec == MG_F64_NATIVE ? launch_assemble_t<1, kF64>(a, st) : launch_assemble_t<1, kDW>(a, st);
   }
   if (prec == MG_F32) return launch_assemble_t<2, kF32>(a, st);
-  return native_f64() ? launch_assemble_t<2, kF64>(a, st) : launch_assemble_t<2, kDW>(a, st);
+  return prec == MG_F64_NATIVE ? launch_assemble_t<2, kF64>(a, st) : launch_assemble_t<2, kDW>(a, st);
 }
 
 // --------------------------------------------------------------- Dirichlet --
@@ -985,12 +996,40 @@ __global__ void k_dirichlet(int64_t ndof, const int32_t* rowptr, const int32_t* 
 
 // ----------------------------------------------------------------- adjoint --
 // grad_e = -sum_{i,j} lambda[dof_j] Khat_ij u[dof_i], Khat the kappa = 1
-// stiffness of element e (symmetric).  Double-word arithmetic on the FP32
-// pipes; u and lambda are FP64 and enter as double-word values.
-template <int ORDER>
+// stiffness of element e (symmetric, rows summing to zero).  Because of the
+// zero row sums the form only sees differences to the element's first vertex:
+// grad_e = -sum_{i,j >= 1} (lambda_j - lambda_0) Khat_ij (u_i - u_0), which removes
+// the cancellation of a smooth field against the stiffness.  The differences
+// are FP64 (exact for nearby values); each group (u or lambda) is rescaled by
+// the power of two of its largest difference, so the double-word arithmetic on
+// the FP32 pipes sees values near 1 whatever the scale of u and lambda, and the
+// result is scaled back in FP64.
+
+// biased FP64 exponent
+__device__ __forceinline__ int dexp(double v) { return (int)((__double_as_longlong(v) >> 52) & 0x7ff); }
+
+// v * 2^(1023 - emax) as a double-word value, by exponent arithmetic (emax = the
+// largest biased exponent of the group, a normal number).  Parts more than 2^-74
+// below the largest are dropped (a relative 2^-74 of the group).
+__device__ __forceinline__ ff ff_rescaled(double v, int emax)
+{
+  const long long b = __double_as_longlong(v);
+  if (dexp(v) + 74 < emax) return ff{0.0f, 0.0f};
+  return ff_from_double_bits(__longlong_as_double(b - ((long long)(emax - 1023) << 52)));
+}
+
+// v * 2^k for |k| <= 2044 (two exact power-of-two products unless the result
+// leaves the FP64 range)
+__device__ __forceinline__ double scale_pow2(double v, int k)
+{
+  const int k1 = k / 2, k2 = k - k1;
+  return v * __longlong_as_double((long long)(k1 + 1023) << 52) * __longlong_as_double((long long)(k2 + 1023) << 52);
+}
+
 // Elements are visited along a Morton curve of their centroids (elem_order,
 // dofs_m = their dofs in that order), so neighbouring threads gather
 // neighbouring vertices and dof values.
+template <int ORDER>
 __global__ void __launch_bounds__(256) k_adjoint(int64_t n_elem, const int32_t* elem_order, const int32_t* dofs_m,
                                                  GeoPtrs geo, const double* tables, double wsum, const double* u,
                                                  const double* lam, double* grad)
@@ -1004,51 +1043,68 @@ __global__ void __launch_bounds__(256) k_adjoint(int64_t n_elem, const int32_t* 
   const int64_t e = elem_order[i];
   const int32_t* dofs = dofs_m + i * NB;  // this element's dofs; the first four are its vertices
   const int4 n = ORDER == 1 ? reinterpret_cast<const int4*>(dofs_m)[i] : make_int4(dofs[0], dofs[1], dofs[2], dofs[3]);
+  // FP64 differences to the first dof and the largest exponent of each group
+  double du[NB - 1], dl[NB - 1];
+  int eu = 0, el = 0;
+  {
+    const double u0 = u[n.x], l0 = lam[n.x];
+#pragma unroll
+    for (int k = 1; k < NB; ++k) {
+      const int dof = ORDER == 1 ? (k == 1 ? n.y : k == 2 ? n.z : n.w) : dofs[k];
+      du[k - 1] = u[dof] - u0;
+      dl[k - 1] = lam[dof] - l0;
+      eu = max(eu, dexp(du[k - 1]));
+      el = max(el, dexp(dl[k - 1]));
+    }
+  }
+  if (eu == 0x7ff || el == 0x7ff) {  // Inf or NaN among u, lambda
+    grad[e] = __longlong_as_double(0x7ff8000000000000ll);
+    return;
+  }
+  if (eu == 0 || el == 0) {  // constant (or denormal-scale) u or lambda on the element
+    grad[e] = -0.0;
+    return;
+  }
   Cof<ff> f;
   geometry_abs(geo, n, f);
   ff s = ff_make(0.0f);
   if (ORDER == 1) {
-    // K has zero row sums: lambda^T K u = (wsum / det) (sum_b dl_b C_b) . (sum_b du_b C_b)
-    // with du_b = u_{b+1} - u_0 (FP64 differences, exact for nearby values) and
-    // C_b the cofactor columns
-    const int id[4] = {n.x, n.y, n.z, n.w};
-    const double u0 = u[id[0]], l0 = lam[id[0]];
+    // lambda^T K u = (wsum / det) (sum_b dl_b C_b) . (sum_b du_b C_b), C_b the cofactor columns
     ff gu[3], gl[3];
     for (int r = 0; r < 3; ++r) gu[r] = gl[r] = ff_make(0.0f);
 #pragma unroll
     for (int b = 0; b < 3; ++b) {
-      const ff du = ff_from_double_bits(u[id[b + 1]] - u0);
-      const ff dl = ff_from_double_bits(lam[id[b + 1]] - l0);
+      const ff a = ff_rescaled(du[b], eu);
+      const ff c = ff_rescaled(dl[b], el);
 #pragma unroll
       for (int r = 0; r < 3; ++r) {
-        gu[r] = gu[r] + du * f.c[r][b];
-        gl[r] = gl[r] + dl * f.c[r][b];
+        gu[r] = gu[r] + a * f.c[r][b];
+        gl[r] = gl[r] + c * f.c[r][b];
       }
     }
     s = ff_dot3(gl, gu) * (ff_from_double_bits(wsum) / f.det);
   } else {
-    ff ue[NB], le[NB];
+    ff ue[NB - 1], le[NB - 1];
 #pragma unroll
-    for (int i = 0; i < NB; ++i) {
-      const int dof = dofs[i];
-      ue[i] = ff_from_double_bits(u[dof]);
-      le[i] = ff_from_double_bits(lam[dof]);
+    for (int k = 0; k < NB - 1; ++k) {
+      ue[k] = ff_rescaled(du[k], eu);
+      le[k] = ff_rescaled(dl[k], el);
     }
     ff g[6];
     metric<ff>(f, ff_make(1.0f) / f.det, g);
-    for (int i = 0; i < NB; ++i) {
+    for (int a = 1; a < NB; ++a) {
       ff row = ff_make(0.0f);
-      for (int j = 0; j < NB; ++j) {
-        const int uidx = sym_index(i, j, NB);
+      for (int b = 1; b < NB; ++b) {
+        const int uidx = sym_index(a, b, NB);
         ff v = g[0] * tab[uidx];
 #pragma unroll
         for (int p = 1; p < 6; ++p) v = v + g[p] * tab[p * NU + uidx];
-        row = row + le[j] * v;
+        row = row + le[b - 1] * v;
       }
-      s = s + row * ue[i];
+      s = s + row * ue[a - 1];
     }
   }
-  grad[e] = -ff_to_double_bits(s);
+  grad[e] = -scale_pow2(ff_to_double_bits(s), (eu - 1023) + (el - 1023));
 }
 
 }  // namespace mg
@@ -1079,8 +1135,12 @@ mg_status mg_plan_status(mg_plan* p)
   if (c[2])
     return set_error(MG_ERR_CUDA, "assembly kernel: a bulk-copy wait timed out in CTA " + std::to_string(c[3]) +
                                       "; the values of that call are incomplete");
-  if (c[4])
+  if (c[4] & 1u)
     return set_error(MG_ERR_INVALID_ARG, "assembly: the coefficient array holds NaN or Inf (the values are not usable)");
+  if (c[4] & 2u)
+    return set_error(MG_ERR_UNSUPPORTED,
+                     "assembly: element-matrix scales outside 2^-96 .. 2^112, where the double-word MG_F64 "
+                     "assembly keeps 1e-12 accuracy; use MG_F64_NATIVE or rescale the coefficient by a power of two");
   return MG_OK;
 }
 
@@ -1091,7 +1151,7 @@ mg_status mg_assemble_host(mg_plan* p, int32_t op, const double* h_coeff, double
   if (!p || (!h_values && p->nnz > 0)) return set_error(MG_ERR_INVALID_ARG, "mg_assemble_host: null argument");
   MG_TRY(plan_device(p));
   cudaStream_t st = (cudaStream_t)stream;
-  const size_t vbytes = (size_t)p->nnz * (prec == MG_F64 ? 8 : 4);
+  const size_t vbytes = (size_t)p->nnz * (prec_is_f64(prec) ? 8 : 4);
   if (p->tmp_values_bytes < vbytes) {
     cudaFree(p->d_tmp_values);
     p->d_tmp_values = nullptr;
@@ -1123,13 +1183,13 @@ mg_status mg_apply_dirichlet(mg_plan* p, const uint8_t* d_mask, int32_t prec, vo
 {
   NvtxRange nvtx_range("mg_apply_dirichlet");
   if (!p || !d_mask || !d_values) return set_error(MG_ERR_INVALID_ARG, "mg_apply_dirichlet: null argument");
-  if (prec != MG_F64 && prec != MG_F32) return set_error(MG_ERR_INVALID_ARG, "bad precision");
+  if (!prec_valid(prec)) return set_error(MG_ERR_INVALID_ARG, "bad precision");
   MG_TRY(plan_device(p));
   const int threads = 256;
   const int blocks = (int)((p->ndof + threads - 1) / threads);
   cudaStream_t st = (cudaStream_t)stream;
   if (blocks > 0) {
-    if (prec == MG_F64)
+    if (prec_is_f64(prec))
       k_dirichlet<double><<<blocks, threads, 0, st>>>(p->ndof, p->d_rowptr, p->d_colind, d_mask, (double*)d_values,
                                                       d_b);
     else

@@ -192,21 +192,29 @@ __device__ __forceinline__ double ff_to_double_int(ff a)
 }
 
 // double -> hi + lo: hi keeps the top 24 bits of the significand (truncated,
-// exact), lo the next 24 bits rounded -- |x - hi - lo| <= 2^-48 |x|.  For
-// |x| in the normal float range (about 1e-38 .. 3e38) and x = 0; other values
+// exact), lo the next 29 bits rounded to nearest -- |x - hi - lo| <= 2^-48 |x|.
+// lo is built without an integer-to-float conversion (which GB300 issues at a
+// small fraction of the FP32 rate): with mlo the low 29 significand bits, lo =
+// RN(mlo 2^(e-52)) is the float sum of two exact terms, the top 23 and the low 6
+// bits of mlo, each obtained as (2^k (1 + bits 2^-23)) - 2^k from a float built
+// with that exponent.  For |x| in about 2^-74 .. 2^127 and x = 0; other values
 // fall back to the FP64 conversions.
 __device__ __forceinline__ ff ff_from_double_bits(double x)
 {
   const uint64_t u = (uint64_t)__double_as_longlong(x);
-  const int e = (int)((u >> 52) & 0x7ff) - 1023;  // unbiased exponent
-  if (e < -120 || e > 120) return ff_from_double(x);
-  const uint32_t sign = (uint32_t)(u >> 63) << 31;
-  const uint64_t m = u & ((1ull << 52) - 1);
-  const float hi = __uint_as_float(sign | ((uint32_t)(e + 127) << 23) | (uint32_t)(m >> 29));
-  // remaining 29 bits, value m_lo * 2^(e - 52)
-  const uint32_t m_lo = (uint32_t)(m & ((1u << 29) - 1));
-  float lo = __uint2float_rn(m_lo) * __uint_as_float((uint32_t)(e - 52 + 127) << 23);
-  lo = sign ? -lo : lo;
+  const uint32_t H = (uint32_t)(u >> 32), L = (uint32_t)u;
+  const uint32_t E = (H >> 20) & 0x7ffu;  // biased exponent
+  if (E == 0u && (u << 1) == 0u) return ff{0.0f, 0.0f};
+  if (E < 949u || E > 1150u) return ff_from_double(x);
+  const uint32_t sign = H & 0x80000000u;
+  // top 24 significand bits with the exponent re-biased from 1023 to 127
+  const uint32_t t = __funnelshift_l(L, H, 3);
+  const float hi = __uint_as_float(((t - (384u << 23)) & 0x7fffffffu) | sign);
+  const uint32_t k1 = (E - 919u) << 23;  // 2^(e - 23): unit of bit 6 of mlo is 2^(e - 46)
+  const uint32_t k2 = (E - 925u) << 23;  // 2^(e - 29): unit of bit 0 is 2^(e - 52)
+  const float f1 = __fsub_rn(__uint_as_float(k1 | ((L >> 6) & 0x7fffffu)), __uint_as_float(k1));
+  const float f2 = __fsub_rn(__uint_as_float(k2 | (L & 63u)), __uint_as_float(k2));
+  const float lo = __uint_as_float(__float_as_uint(__fadd_rn(f1, f2)) ^ sign);
   return ff{hi, lo};
 }
 

@@ -65,6 +65,10 @@ constexpr uint32_t kEndFlag = 1u << 31;
 // kernel sums a piece in registers and updates the slot once.
 inline __host__ __device__ constexpr int piece_words(int order) { return order == 1 ? 4 : 2; }
 
+// Values of precision `prec` are doubles (MG_F64, MG_F64_NATIVE) or floats (MG_F32).
+inline bool prec_valid(int prec) { return prec == MG_F64 || prec == MG_F32 || prec == MG_F64_NATIVE; }
+inline bool prec_is_f64(int prec) { return prec == MG_F64 || prec == MG_F64_NATIVE; }
+
 inline int nbasis(int order) { return order == 1 ? 4 : 10; }
 inline int nunique(int order) { return order == 1 ? 10 : 55; }
 inline int chunk_items(int order) { return order == 1 ? kChunkP1 : kChunkP2; }

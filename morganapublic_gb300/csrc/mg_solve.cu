@@ -561,11 +561,11 @@ __global__ void __launch_bounds__(kSolveThreads) k_anchor_r(int64_t n, const dou
 
 mg_status launch_spmv(mg_plan* p, int prec, const void* vals, const void* x, void* y, cudaStream_t st)
 {
-  if (prec != MG_F64 && prec != MG_F32) return set_error(MG_ERR_INVALID_ARG, "bad precision");
+  if (!prec_valid(prec)) return set_error(MG_ERR_INVALID_ARG, "bad precision");
   if (p->ndof == 0) return MG_OK;
   if (!vals || !x || !y) return set_error(MG_ERR_INVALID_ARG, "mg_spmv: null argument");
   MG_TRY(plan_device(p));
-  if (prec == MG_F64) {
+  if (prec_is_f64(prec)) {
     const int G = row_group<double>(p), nb = row_blocks<double>(p, G);
     if (p->d_coloff) {
       MG_DISPATCH_G(G, (launch_pdl(k_spmv<double, g, int16_t>, nb, kSolveThreads, st, p->ndof,

@@ -327,6 +327,44 @@ def test_adjoint_gradient(order):
         assert abs(fd - g[e]) <= 1e-5 * np.abs(g).max() + 1e-6 * abs(fd)
 
 
+@pytest.mark.parametrize("scale", [1e-30, 1e-24, 1e-12, 1.0, 1e12, 1e24, 1e36])
+def test_extreme_scales_assembly_and_adjoint(scale):
+    """Coefficients, u and lambda far from 1.  The double-word (MG_F64) assembly
+    keeps FP64 parity while element scales stay within 2^-96 .. 2^112 and reports
+    MG_ERR_UNSUPPORTED through mg_plan_status outside it; MG_F64_NATIVE covers
+    the whole range.  The adjoint rescales each element's differences by powers
+    of two, so it keeps parity at every scale (conversions inside and outside
+    the integer-conversion range, zero coefficients and zero values included)."""
+    m, kappa = _case(4, 0.2, 11, True, 1.0)
+    kappa = kappa * scale
+    kappa[::7] = 0.0
+    mesh = mg.Mesh(m.xyz, m.conn, order=1)
+    b = mg.MatrixBuilder(mesh)
+    dofs, rp, ci, ref = orc.full_operator("stiff_kappa", 1, 4, m.xyz, m.conn, coeff=kappa)
+    kt = torch.from_numpy(kappa).cuda()
+    in_range = 1e-24 <= scale <= 1e24
+    vals = b.assemble("stiff_kappa", coeff=kt, quad=4, prec="f64").cpu().numpy()
+    if in_range:
+        b.status()
+        assert row_scaled_err(rp, ref, vals) <= F64_TOL
+    else:
+        with pytest.raises(mg.MorganaError) as e:
+            b.status()
+        assert e.value.status == mg.MG_ERR_UNSUPPORTED
+    nat = b.assemble("stiff_kappa", coeff=kt, quad=4, prec="f64_native").cpu().numpy()
+    b.status()
+    assert nat.dtype == np.float64
+    assert row_scaled_err(rp, ref, nat) <= F64_TOL
+    rng = np.random.default_rng(5)
+    u = rng.uniform(-1, 1, b.ndof) * scale
+    lam = rng.uniform(-1, 1, b.ndof) * scale
+    u[::5] = 0.0
+    g = b.adjoint_grad(torch.from_numpy(u).cuda(), torch.from_numpy(lam).cuda(), quad=4).cpu().numpy()
+    g_ref = orc.adjoint_grad(1, 4, m.xyz, m.conn, dofs, u, lam)
+    assert np.all(np.isfinite(g))
+    assert np.max(np.abs(g - g_ref)) <= 1e-12 * np.abs(g_ref).max()
+
+
 def test_gmsh_loaded_mesh_assembles(tmp_path):
     m, kappa = _case(4, 0.2, 8, True, 1.0)
     p = str(tmp_path / "c.msh")
