@@ -52,7 +52,7 @@ def parse():
                          "5: P1 128^3 kernels as fractions of the HBM roofline")
     ap.add_argument("--order", type=int, default=1, choices=[1, 2], help="element order of the --only modes")
     ap.add_argument("--only", default=None,
-                    choices=["asm64", "asm32", "spmv64", "spmv32", "cg64", "cg32", "adj", "suite"],
+                    choices=["asm64", "asm32", "spmv64", "spmv32", "cg64", "cg32", "adj", "rhs", "suite"],
                     help="run warmup + steps launches of one kernel only (for profilers) and print its timing")
     return ap.parse_args()
 
@@ -94,6 +94,12 @@ def asm_bytes(E, nv, nnz, sv, nb=4):
 def adj_bytes(E, nv, ndof, nb=4):
     """E (4 element id + 4 nb dofs + 8 gradient) + 36 n_v (node record) + 16 ndof (u, lambda)"""
     return E * (12 + 4 * nb) + 36 * nv + 16 * ndof
+
+
+def rhs_bytes(E, nv, ndof, nb=4):
+    """element pass E (4 position + 4 nb dofs + 8 scale + 8 nb out) + 36 n_v + 8 ndof (field);
+    dof pass 4 (ndof + 1) + 12 E nb (slot + entry) + 8 ndof (b)"""
+    return E * (16 + 12 * nb) + 36 * nv + 8 * ndof + 4 * (ndof + 1) + 12 * E * nb + 8 * ndof
 
 
 def spmv_bytes(ndof, nnz, sv):
@@ -310,11 +316,12 @@ def run_only(a):
           "asm32": lambda: b.assemble("stiff_kappa", coeff=kappa, quad=quad, prec="f32", out=v32, stream=stream),
           "spmv64": lambda: b.apply(v64, x, out=y, stream=stream),
           "spmv32": lambda: b.apply(v32, x32, out=y32, stream=stream),
-          "adj": lambda: b.adjoint_grad(x, lam, quad=quad, out=g, stream=stream)}[a.only]
+          "adj": lambda: b.adjoint_grad(x, lam, quad=quad, out=g, stream=stream),
+          "rhs": lambda: b.build_vector(field=x, elem_scale=kappa, quad=quad, out=y, stream=stream)}[a.only]
     E, nv = len(m.conn), len(m.xyz)
     byts = {"asm64": asm_bytes(E, nv, b.nnz, 8, nb), "asm32": asm_bytes(E, nv, b.nnz, 4, nb),
             "spmv64": spmv_bytes(b.ndof, b.nnz, 8), "spmv32": spmv_bytes(b.ndof, b.nnz, 4),
-            "adj": adj_bytes(E, nv, b.ndof, nb)}[a.only]
+            "adj": adj_bytes(E, nv, b.ndof, nb), "rhs": rhs_bytes(E, nv, b.ndof, nb)}[a.only]
     ts = []
     torch.cuda.synchronize()
     with torch.cuda.stream(stream):

@@ -216,7 +216,11 @@ mg_status mg_assemble_host(mg_plan* plan, int32_t op, const double* h_coeff, dou
 
 /* Load vector b_i = sum_e s_e int_e f_h phi_i (f_h the nodal P1/P2 field d_field,
    or 1 when d_field is NULL; s_e = d_elem_scale[e] or 1 when NULL), written to
-   d_b (ndof doubles).
+   d_b (ndof doubles).  Element vectors in double-word arithmetic (FP64-accurate
+   at any scale of s and f), then one FP64 sum per dof in a fixed order:
+   deterministic, no atomics.  The first call on a plan builds the dof-to-slot
+   map (host, 4 bytes per element-vector entry) and a work buffer of 8 bytes per
+   entry on the device.
    Replaces: vectorBuilder<localVectorEL3d<fnEL3dA|fnEL3dB>>::buildEpetraVector
    (src/morganaFiniteElements/traitsVectorBuilder.hpp:214-274). */
 mg_status mg_assemble_rhs(mg_plan* plan, const double* d_field, const double* d_elem_scale,

@@ -44,7 +44,8 @@ def _run(cmd):
 def build(verbose: bool = False, force: bool = False) -> str:
     """Compiles and links the library; returns its path."""
     os.makedirs(OUT_DIR, exist_ok=True)
-    headers = [os.path.join(CSRC, "mg_internal.h"), os.path.join(INCLUDE, "morgana_gpu.h")]
+    headers = [os.path.join(CSRC, h) for h in sorted(os.listdir(CSRC)) if h.endswith((".h", ".cuh"))]
+    headers.append(os.path.join(INCLUDE, "morgana_gpu.h"))
     jobs = []
     objs = []
     for s in CU_SOURCES:

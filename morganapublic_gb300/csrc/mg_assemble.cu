@@ -1019,11 +1019,24 @@ __device__ __forceinline__ ff ff_rescaled(double v, int emax)
 }
 
 // v * 2^k for |k| <= 2044 (two exact power-of-two products unless the result
-// leaves the FP64 range)
-__device__ __forceinline__ double scale_pow2(double v, int k)
+// leaves the FP64 range); out of line, like the other rare FP64 paths
+__device__ __noinline__ double scale_pow2(double v, int k)
 {
   const int k1 = k / 2, k2 = k - k1;
   return v * __longlong_as_double((long long)(k1 + 1023) << 52) * __longlong_as_double((long long)(k2 + 1023) << 52);
+}
+
+// a * 2^k as a double: scaled on the floats when the result stays well inside
+// the normal-float range (then one FP64 addition), else in FP64
+__device__ __forceinline__ double ff_to_double_pow2(ff a, int k)
+{
+  if (a.hi == 0.0f) return 0.0;
+  const int ex = (int)((__float_as_uint(a.hi) >> 23) & 0xffu) - 127 + k;
+  if (k >= -100 && k <= 100 && ex >= -90 && ex <= 100) {
+    const float fs = __uint_as_float((uint32_t)(k + 127) << 23);
+    return ff_to_double_bits(ff{a.hi * fs, a.lo * fs});
+  }
+  return scale_pow2(ff_to_double_bits(a), k);
 }
 
 // Elements are visited along a Morton curve of their centroids (elem_order,
@@ -1092,8 +1105,10 @@ __global__ void __launch_bounds__(256) k_adjoint(int64_t n_elem, const int32_t* 
     }
     ff g[6];
     metric<ff>(f, ff_make(1.0f) / f.det, g);
+#pragma unroll
     for (int a = 1; a < NB; ++a) {
       ff row = ff_make(0.0f);
+#pragma unroll
       for (int b = 1; b < NB; ++b) {
         const int uidx = sym_index(a, b, NB);
         ff v = g[0] * tab[uidx];
@@ -1104,7 +1119,106 @@ __global__ void __launch_bounds__(256) k_adjoint(int64_t n_elem, const int32_t* 
       s = s + row * ue[a - 1];
     }
   }
-  grad[e] = -scale_pow2(ff_to_double_bits(s), (eu - 1023) + (el - 1023));
+  grad[e] = -ff_to_double_pow2(s, (eu - 1023) + (el - 1023));
+}
+
+// ------------------------------------------------------------- load vector --
+// b_i = sum_e s_e int_e f_h phi_i with f_h = sum_k f_k phi_k (f = 1 without a
+// field): the reference's vector builder (fnEL3dA / fnEL3dB under
+// traitsVectorBuilder) as two deterministic passes.
+// Pass 1, one thread per element along the Morton order (position p): the
+// element vector y[p nb + l] = s_e det_e sum_k Mhat_lk f_k, Mhat the reference
+// mass table of the quadrature card.  Double-word arithmetic; s_e and the f_k
+// are rescaled by powers of two (their largest exponents), so the result keeps
+// FP64 accuracy at any scale, and is written as an IEEE double.
+template <int ORDER>
+__global__ void __launch_bounds__(256) k_rhs_elem(int64_t n_elem, const int32_t* elem_order, const int32_t* dofs_m,
+                                                  GeoPtrs geo, const double* mass, const double* field,
+                                                  const double* scale, double* y)
+{
+  constexpr int NB = ORDER == 1 ? 4 : 10, NU = ORDER == 1 ? 10 : 55;
+  __shared__ ff tab[NU];
+  __shared__ ff rsum[NB];
+  for (int i = threadIdx.x; i < NU; i += blockDim.x) tab[i] = ff_from_double(mass[i]);
+  if (threadIdx.x < NB) {
+    double r = 0.0;
+    for (int j = 0; j < NB; ++j) r += mass[sym_index((int)threadIdx.x, j, NB)];
+    rsum[threadIdx.x] = ff_from_double(r);
+  }
+  __syncthreads();
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= n_elem) return;
+  const int32_t* dofs = dofs_m + p * NB;
+  const double sd = scale ? scale[elem_order[p]] : 1.0;
+  const int es = dexp(sd);
+  double f[NB];
+  int ef = 1023;  // exponent of 1 without a field
+  if (field) {
+    ef = 0;
+#pragma unroll
+    for (int k = 0; k < NB; ++k) {
+      f[k] = field[dofs[k]];
+      ef = max(ef, dexp(f[k]));
+    }
+  }
+  double2* out = reinterpret_cast<double2*>(y + p * NB);
+  if (es == 0x7ff || ef == 0x7ff || es == 0 || ef == 0) {
+    // Inf / NaN in s or f: NaN; zero (or denormal-scale) s or f: zero
+    const double v = (es == 0x7ff || ef == 0x7ff) ? __longlong_as_double(0x7ff8000000000000ll) : 0.0;
+#pragma unroll
+    for (int l = 0; l < NB / 2; ++l) out[l] = make_double2(v, v);
+    return;
+  }
+  const int4 n = ORDER == 1 ? reinterpret_cast<const int4*>(dofs_m)[p] : make_int4(dofs[0], dofs[1], dofs[2], dofs[3]);
+  Cof<ff> c;
+  geometry_abs(geo, n, c);
+  const ff sdet = ff_rescaled(sd, es) * c.det;
+  ff v[NB];
+  if (field) {
+    ff fr[NB];
+#pragma unroll
+    for (int k = 0; k < NB; ++k) fr[k] = ff_rescaled(f[k], ef);
+#pragma unroll
+    for (int l = 0; l < NB; ++l) {
+      ff a = tab[sym_index(l, 0, NB)] * fr[0];
+#pragma unroll
+      for (int k = 1; k < NB; ++k) a = a + tab[sym_index(l, k, NB)] * fr[k];
+      v[l] = a * sdet;
+    }
+  } else {
+#pragma unroll
+    for (int l = 0; l < NB; ++l) v[l] = rsum[l] * sdet;
+  }
+  // back to the true scale 2^k2
+  const int k2 = (es - 1023) + (ef - 1023);
+#pragma unroll
+  for (int l = 0; l < NB / 2; ++l)
+    out[l] = make_double2(ff_to_double_pow2(v[2 * l], k2), ff_to_double_pow2(v[2 * l + 1], k2));
+}
+
+// Pass 2, one thread per dof: b_i = the FP64 sum of its element-vector entries
+// in ascending slot order (a fixed order: bitwise reproducible, no atomics).
+__global__ void __launch_bounds__(256) k_rhs_gather(int64_t ndof, const int32_t* __restrict__ ptr,
+                                                    const int32_t* __restrict__ slot, const double* __restrict__ y,
+                                                    double* __restrict__ b)
+{
+  constexpr int U = 8;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= ndof) return;
+  const int s0 = __ldg(ptr + i), s1 = __ldg(ptr + i + 1);
+  double acc = 0.0;
+  for (int base = s0; base < s1; base += U) {
+    int q[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) q[u] = base + u < s1 ? __ldg(slot + base + u) : -1;
+    double t[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) t[u] = q[u] >= 0 ? __ldg(y + q[u]) : 0.0;
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+      if (q[u] >= 0) acc += t[u];
+  }
+  b[i] = acc;
 }
 
 }  // namespace mg
@@ -1231,23 +1345,32 @@ mg_status mg_assemble_rhs(mg_plan* p, const double* d_field, const double* d_ele
                           void* stream)
 {
   NvtxRange nvtx_range("mg_assemble_rhs");
-  if (!p || !d_b) return set_error(MG_ERR_INVALID_ARG, "mg_assemble_rhs: null argument");
+  if (!p || (!d_b && p->ndof > 0)) return set_error(MG_ERR_INVALID_ARG, "mg_assemble_rhs: null argument");
+  const RefTables* t = nullptr;
+  const double* d_tab = nullptr;
+  MG_TRY(plan_tables(p, quad, &t, &d_tab));  // validates quad
+  if (p->ndof == 0) return MG_OK;
   MG_TRY(plan_device(p));
+  MG_TRY(plan_rhs_map(p));
+  mg_mesh* m = p->mesh;
   cudaStream_t st = (cudaStream_t)stream;
-  // b = M_s f with M_s the (element-scaled) mass matrix: the same integral as
-  // sum_e s_e int_e f_h phi_i, since f_h = sum_k f_k phi_k on every element.
-  const size_t vbytes = (size_t)p->nnz * 8;
-  if (p->tmp_values_bytes < vbytes) {
-    cudaFree(p->d_tmp_values);
-    p->d_tmp_values = nullptr;
-    p->tmp_values_bytes = 0;
-    MG_CUDA(cudaMalloc(&p->d_tmp_values, vbytes));
-    p->tmp_values_bytes = vbytes;
+  const int threads = 256;
+  const int nu = m->nb * (m->nb + 1) / 2;
+  const GeoPtrs geo{m->d_xyz, m->d_node_rec, m->d_lo_z};
+  const int eblocks = (int)((m->n_elem + threads - 1) / threads);
+  if (eblocks > 0) {
+    if (m->order == 1)
+      k_rhs_elem<1><<<eblocks, threads, 0, st>>>(m->n_elem, p->d_elem_order, p->d_dofs_morton, geo, d_tab + 6 * nu,
+                                                 d_field, d_elem_scale, p->d_rhs_y);
+    else
+      k_rhs_elem<2><<<eblocks, threads, 0, st>>>(m->n_elem, p->d_elem_order, p->d_dofs_morton, geo, d_tab + 6 * nu,
+                                                 d_field, d_elem_scale, p->d_rhs_y);
+    MG_CUDA(cudaGetLastError());
   }
-  MG_TRY(launch_assemble(p, d_elem_scale ? MG_OP_MASS_COEFF : MG_OP_MASS, d_elem_scale, 1.0, quad, MG_F64,
-                         p->d_tmp_values, st));
-  if (d_field) return launch_spmv(p, MG_F64, p->d_tmp_values, d_field, d_b, st);
-  return launch_rowsum(p, (const double*)p->d_tmp_values, d_b, st);
+  k_rhs_gather<<<(int)((p->ndof + threads - 1) / threads), threads, 0, st>>>(p->ndof, p->d_rhs_ptr, p->d_rhs_slot,
+                                                                             p->d_rhs_y, d_b);
+  MG_CUDA(cudaGetLastError());
+  return MG_OK;
 }
 
 }  // extern "C"

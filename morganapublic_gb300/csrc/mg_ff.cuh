@@ -153,6 +153,13 @@ __device__ __forceinline__ ff ff_from_double(double x)
 
 __device__ __forceinline__ double ff_to_double(ff a) { return (double)a.hi + (double)a.lo; }
 
+// Rare-case paths of the integer conversions below, kept out of line: inlined,
+// the compiler if-converts them into the hot path, and their predicated FP64
+// instructions still occupy GB300's narrow FP64 pipe (measured: ~20 FP64-pipe
+// instructions per element instead of ~5 in the element kernels).
+static __device__ __noinline__ ff ff_from_double_slow(double x) { return ff_from_double(x); }
+static __device__ __noinline__ double f2d_slow(float f) { return (double)f; }
+
 // The same two conversions with integer operations, for hot loops: GB300 runs
 // FP32<->FP64 conversions on its FP64 pipe (~1/60 of the FP32 rate).
 // float -> double by re-biasing the exponent (exact for normal floats; zero
@@ -162,7 +169,7 @@ __device__ __forceinline__ double f2d_bits(float f)
   const uint32_t u = __float_as_uint(f);
   const uint32_t e = (u >> 23) & 0xffu;
   if (e == 0u) return 0.0;
-  if (e == 0xffu) return (double)f;
+  if (e == 0xffu) return f2d_slow(f);
   const uint64_t d = ((uint64_t)(u >> 31) << 63) | ((uint64_t)(e + (1023u - 127u)) << 52) |
                      ((uint64_t)(u & 0x7fffffu) << 29);
   return __longlong_as_double((long long)d);
@@ -170,6 +177,7 @@ __device__ __forceinline__ double f2d_bits(float f)
 
 // hi + lo as a double: both parts exact, one FP64 addition.
 __device__ __forceinline__ double ff_to_double_bits(ff a) { return f2d_bits(a.hi) + f2d_bits(a.lo); }
+static __device__ __noinline__ double ff_to_double_slow(ff a) { return ff_to_double_bits(a); }
 
 // hi + lo as a double without FP64 arithmetic: after renormalisation
 // (|lo| <= ulp(hi)/2), lo is expressed in units of the double ulp of hi
@@ -177,13 +185,14 @@ __device__ __forceinline__ double ff_to_double_bits(ff a) { return f2d_bits(a.hi
 // to the bit pattern of double(hi) -- integer carries cross binades correctly,
 // so the result is within half a double ulp of hi + lo.  Outside the range
 // where the scaling stays a normal float (|hi| below ~2^-74 or above ~2^127),
-// and for zero, Inf or NaN, it falls back to ff_to_double_bits.
+// and for Inf or NaN, it falls back to ff_to_double_bits (zero gives +0).
 __device__ __forceinline__ double ff_to_double_int(ff a)
 {
   const ff n = fast_two_sum(a.hi, a.lo);
   const uint32_t u = __float_as_uint(n.hi);
   const int e = (int)((u >> 23) & 0xffu) - 127;  // unbiased exponent of hi
-  if (e < -74 || e > 126 || n.hi == 0.0f) return ff_to_double_bits(n);
+  if (n.hi == 0.0f) return 0.0;
+  if (e < -74 || e > 126) return ff_to_double_slow(n);
   const float scale = __uint_as_float((uint32_t)(52 - e + 127) << 23);  // 2^(52 - e)
   int k = __float2int_rn(__fmul_rn(n.lo, scale));                    // lo / ulp_double(hi)
   if (u >> 31) k = -k;  // magnitudes: the bit pattern grows with |x|
@@ -205,7 +214,7 @@ __device__ __forceinline__ ff ff_from_double_bits(double x)
   const uint32_t H = (uint32_t)(u >> 32), L = (uint32_t)u;
   const uint32_t E = (H >> 20) & 0x7ffu;  // biased exponent
   if (E == 0u && (u << 1) == 0u) return ff{0.0f, 0.0f};
-  if (E < 949u || E > 1150u) return ff_from_double(x);
+  if (E < 949u || E > 1150u) return ff_from_double_slow(x);
   const uint32_t sign = H & 0x80000000u;
   // top 24 significand bits with the exponent re-biased from 1023 to 127
   const uint32_t t = __funnelshift_l(L, H, 3);

@@ -173,6 +173,13 @@ struct mg_plan {
   uint32_t* d_entries = nullptr;   // contribution words
   uint32_t* d_counters = nullptr;   // [0] work counter, [1] exit counter, [2] device error, [3] detail
   int64_t max_chunk_entries = 0;
+  // load vector (built on the first mg_assemble_rhs): per dof, the slots p * nb + l
+  // (p = Morton position of an element touching it, l = the dof's local index)
+  // of the element vectors it sums, ascending; and the element-vector buffer
+  std::vector<int32_t> h_elem_order;  // host copy of the Morton element order
+  int32_t* d_rhs_ptr = nullptr;       // ndof + 1
+  int32_t* d_rhs_slot = nullptr;      // n_elem * nb
+  double* d_rhs_y = nullptr;          // n_elem * nb
   // reference tables, cached per (quad) on the device
   std::vector<mg::RefTables> tables;
   std::vector<double*> d_tables;  // parallel to tables: stiff (6 nb^2) then mass (nb^2)
@@ -210,9 +217,9 @@ mg_status mesh_device(mg_mesh* m);  // uploads the mesh on first GPU use
 mg_status plan_device(mg_plan* p);  // uploads mesh + plan on first GPU use
 mg_status plan_tables(mg_plan* p, int quad, const RefTables** t, const double** d_tab);
 mg_status plan_work(mg_plan* p, size_t bytes, void** ptr);
+mg_status plan_rhs_map(mg_plan* p);  // the load-vector slot map (once per plan)
 mg_status ensure_edges(mg_mesh* m);
 mg_status launch_assemble(mg_plan* p, int op, const double* d_coeff, double c, int quad, int prec,
                           void* d_values, cudaStream_t st);
 mg_status launch_spmv(mg_plan* p, int prec, const void* vals, const void* x, void* y, cudaStream_t st);
-mg_status launch_rowsum(mg_plan* p, const double* vals, double* y, cudaStream_t st);
 }  // namespace mg

@@ -628,6 +628,7 @@ mg_status plan_device(mg_plan* p)
   }
   MG_TRY(upload(&p->d_counters, std::vector<uint32_t>(8, 0u)));
   MG_CUDA(cudaMallocHost(&p->h_pinned, 64 * sizeof(double)));
+  p->h_elem_order.swap(p->host_schedule->elem_order);  // kept for the load-vector map
   delete p->host_schedule;
   p->host_schedule = nullptr;
   p->on_device = true;
@@ -647,6 +648,9 @@ static void free_plan(mg_plan* p)
   cudaFree(p->d_row_meta);
   cudaFree(p->d_elem_order);
   cudaFree(p->d_dofs_morton);
+  cudaFree(p->d_rhs_ptr);
+  cudaFree(p->d_rhs_slot);
+  cudaFree(p->d_rhs_y);
   cudaFree(p->d_entries);
   cudaFree(p->d_counters);
   for (double* t : p->d_tables) cudaFree(t);
@@ -684,6 +688,46 @@ mg_status plan_tables(mg_plan* p, int quad, const RefTables** t, const double** 
   p->d_tables.push_back(d);
   *t = &p->tables.back();
   *d_tab = d;
+  return MG_OK;
+}
+
+// Load-vector map: for each dof (natural order), the element-vector slots
+// q = p * nb + l with dofs_morton[q] == dof, ascending -- the fixed order in
+// which the gather kernel sums them.  A parallel counting transpose, then each
+// dof's short list sorted.
+mg_status plan_rhs_map(mg_plan* p)
+{
+  if (p->d_rhs_ptr) return MG_OK;
+  const mg_mesh* m = p->mesh;
+  const int nb = m->nb;
+  const int64_t E = m->n_elem, nd = p->ndof, pairs = E * nb;
+  if (pairs >= INT32_MAX) return set_error(MG_ERR_SIZE, "load-vector map above 2^31 element-vector entries");
+  if ((int64_t)p->h_elem_order.size() != E) return set_error(MG_ERR_INVALID_ARG, "plan without an element order");
+  const int32_t* eo = p->h_elem_order.data();
+  const int32_t* dofs = m->dofs.data();
+  auto dof_of = [&](int64_t q) { return dofs[(int64_t)eo[q / nb] * nb + q % nb]; };
+  std::vector<int32_t> ptr(nd + 1, 0), slot(std::max<int64_t>(pairs, 1));
+#pragma omp parallel for
+  for (int64_t q = 0; q < pairs; ++q) {
+    const int32_t d = dof_of(q);
+#pragma omp atomic
+    ptr[d + 1]++;
+  }
+  for (int64_t d = 0; d < nd; ++d) ptr[d + 1] += ptr[d];
+  std::vector<int32_t> cur(ptr.begin(), ptr.end() - 1);
+#pragma omp parallel for
+  for (int64_t q = 0; q < pairs; ++q) {
+    const int32_t d = dof_of(q);
+    int32_t at;
+#pragma omp atomic capture
+    at = cur[d]++;
+    slot[at] = (int32_t)q;
+  }
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (int64_t d = 0; d < nd; ++d) std::sort(slot.begin() + ptr[d], slot.begin() + ptr[d + 1]);
+  MG_TRY(upload(&p->d_rhs_ptr, ptr));
+  MG_TRY(upload(&p->d_rhs_slot, slot));
+  MG_CUDA(cudaMalloc(&p->d_rhs_y, sizeof(double) * std::max<int64_t>(pairs, 1)));
   return MG_OK;
 }
 

@@ -293,15 +293,6 @@ __global__ void __launch_bounds__(kSolveThreads) k_spmv(int64_t n, const int32_t
   }
 }
 
-__global__ void k_rowsum(int64_t n, const int32_t* rp, const double* val, double* y)
-{
-  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (r >= n) return;
-  double s = 0.0;
-  for (int k = rp[r]; k < rp[r + 1]; ++k) s += val[k];
-  y[r] = s;
-}
-
 // K1: q = A p, alpha = rz / (p . q)
 template <typename V, int G, typename I>
 __global__ void __launch_bounds__(kSolveThreads) k_cg_spmv(int64_t n, const int32_t* __restrict__ rp,
@@ -592,14 +583,6 @@ mg_status launch_spmv(mg_plan* p, int prec, const void* vals, const void* x, voi
   return MG_OK;
 }
 
-mg_status launch_rowsum(mg_plan* p, const double* vals, double* y, cudaStream_t st)
-{
-  MG_TRY(plan_device(p));
-  const int blocks = (int)((p->ndof + 255) / 256);
-  if (blocks > 0) k_rowsum<<<blocks, 256, 0, st>>>(p->ndof, p->d_rowptr, vals, y);
-  MG_CUDA(cudaGetLastError());
-  return MG_OK;
-}
 
 // Workspace of one CG run over vectors of type V.
 template <typename V>
