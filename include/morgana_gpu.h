@@ -219,8 +219,9 @@ mg_status mg_assemble_host(mg_plan* plan, int32_t op, const double* h_coeff, dou
    d_b (ndof doubles).  Element vectors in double-word arithmetic (FP64-accurate
    at any scale of s and f), then one FP64 sum per dof in a fixed order:
    deterministic, no atomics.  The first call on a plan builds the dof-to-slot
-   map (host, 4 bytes per element-vector entry) and a work buffer of 8 bytes per
-   entry on the device.
+   map (4 bytes per element-vector entry), a work buffer of 8 bytes per entry
+   and the element-geometry cache (80 bytes per element) on the device, and
+   waits for them: make that first call before capturing a CUDA graph.
    Replaces: vectorBuilder<localVectorEL3d<fnEL3dA|fnEL3dB>>::buildEpetraVector
    (src/morganaFiniteElements/traitsVectorBuilder.hpp:214-274). */
 mg_status mg_assemble_rhs(mg_plan* plan, const double* d_field, const double* d_elem_scale,
@@ -292,7 +293,10 @@ mg_status mg_cg_solve_noalloc(mg_plan* plan, const double* d_values, const doubl
 /* Build addition: per-element gradient of J(kappa) for the P0 coefficient of
    MG_OP_STIFF_KAPPA, d_grad[e] = -lambda_e^T Khat_e u_e, with Khat_e the
    element stiffness at kappa_e = 1, u the state and lambda the adjoint
-   solution (ndof doubles each). */
+   solution (ndof doubles each).  FP64-accurate at any scale of u and lambda.
+   The first call on a plan (or the first mg_assemble_rhs) builds the plan's
+   element-geometry cache (80 bytes per element on the device) and waits for
+   it: make that first call before capturing a CUDA graph. */
 mg_status mg_adjoint_grad(mg_plan* plan, const double* d_u, const double* d_lambda, int32_t quad,
                           double* d_grad, void* stream);
 

@@ -1039,13 +1039,48 @@ __device__ __forceinline__ double ff_to_double_pow2(ff a, int k)
   return scale_pow2(ff_to_double_bits(a), k);
 }
 
+// Element geometry cache: the double-word Jacobian determinant and cofactors of
+// every element (from the exact three-float node coordinates), written once per
+// plan in the Morton order p, structure of arrays (coalesced for the kernels
+// that read them: load vector, adjoint).
+template <int NB>
+__global__ void __launch_bounds__(256) k_elem_geometry(int64_t n_elem, const int32_t* dofs_m, GeoPtrs geo,
+                                                       float2* det, float2* cof)
+{
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= n_elem) return;
+  const int32_t* d = dofs_m + p * NB;
+  const int4 n = NB == 4 ? reinterpret_cast<const int4*>(dofs_m)[p] : make_int4(d[0], d[1], d[2], d[3]);
+  Cof<ff> f;
+  geometry_abs(geo, n, f);
+  det[p] = make_float2(f.det.hi, f.det.lo);
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) cof[(3 * r + c) * n_elem + p] = make_float2(f.c[r][c].hi, f.c[r][c].lo);
+}
+
+__device__ __forceinline__ void cached_geometry(const float2* det, const float2* cof, int64_t n_elem, int64_t p,
+                                                Cof<ff>& f)
+{
+  const float2 d = det[p];
+  f.det = ff{d.x, d.y};
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float2 v = cof[(3 * r + c) * n_elem + p];
+      f.c[r][c] = ff{v.x, v.y};
+    }
+}
+
 // Elements are visited along a Morton curve of their centroids (elem_order,
 // dofs_m = their dofs in that order), so neighbouring threads gather
-// neighbouring vertices and dof values.
+// neighbouring dof values.
 template <int ORDER>
 __global__ void __launch_bounds__(256) k_adjoint(int64_t n_elem, const int32_t* elem_order, const int32_t* dofs_m,
-                                                 GeoPtrs geo, const double* tables, double wsum, const double* u,
-                                                 const double* lam, double* grad)
+                                                 const float2* gdet, const float2* gcof, const double* tables,
+                                                 double wsum, const double* u, const double* lam, double* grad)
 {
   constexpr int NB = ORDER == 1 ? 4 : 10, NU = ORDER == 1 ? 10 : 55;
   __shared__ ff tab[6 * NU];
@@ -1079,7 +1114,7 @@ __global__ void __launch_bounds__(256) k_adjoint(int64_t n_elem, const int32_t* 
     return;
   }
   Cof<ff> f;
-  geometry_abs(geo, n, f);
+  cached_geometry(gdet, gcof, n_elem, i, f);
   ff s = ff_make(0.0f);
   if (ORDER == 1) {
     // lambda^T K u = (wsum / det) (sum_b dl_b C_b) . (sum_b du_b C_b), C_b the cofactor columns
@@ -1133,7 +1168,7 @@ __global__ void __launch_bounds__(256) k_adjoint(int64_t n_elem, const int32_t* 
 // FP64 accuracy at any scale, and is written as an IEEE double.
 template <int ORDER>
 __global__ void __launch_bounds__(256) k_rhs_elem(int64_t n_elem, const int32_t* elem_order, const int32_t* dofs_m,
-                                                  GeoPtrs geo, const double* mass, const double* field,
+                                                  const float2* gdet, const double* mass, const double* field,
                                                   const double* scale, double* y)
 {
   constexpr int NB = ORDER == 1 ? 4 : 10, NU = ORDER == 1 ? 10 : 55;
@@ -1169,10 +1204,8 @@ __global__ void __launch_bounds__(256) k_rhs_elem(int64_t n_elem, const int32_t*
     for (int l = 0; l < NB / 2; ++l) out[l] = make_double2(v, v);
     return;
   }
-  const int4 n = ORDER == 1 ? reinterpret_cast<const int4*>(dofs_m)[p] : make_int4(dofs[0], dofs[1], dofs[2], dofs[3]);
-  Cof<ff> c;
-  geometry_abs(geo, n, c);
-  const ff sdet = ff_rescaled(sd, es) * c.det;
+  const float2 dt = gdet[p];
+  const ff sdet = ff_rescaled(sd, es) * ff{dt.x, dt.y};
   ff v[NB];
   if (field) {
     ff fr[NB];
@@ -1314,6 +1347,36 @@ mg_status mg_apply_dirichlet(mg_plan* p, const uint8_t* d_mask, int32_t prec, vo
   return MG_OK;
 }
 
+// The element geometry cache (once per plan; the mesh is immutable).  Built on
+// the caller's stream and waited for, so later calls on any stream see it.
+static mg_status plan_geometry(mg_plan* p, cudaStream_t st)
+{
+  if (p->d_geo_det) return MG_OK;
+  mg_mesh* m = p->mesh;
+  const int64_t E = m->n_elem;
+  if (E == 0) return MG_OK;
+  float2 *det = nullptr, *cof = nullptr;
+  MG_CUDA(cudaMalloc(&det, sizeof(float2) * E));
+  if (cudaMalloc(&cof, sizeof(float2) * 9 * E) != cudaSuccess) {
+    cudaFree(det);
+    return set_error(MG_ERR_ALLOC, "element geometry cache: out of device memory");
+  }
+  const GeoPtrs geo{m->d_xyz, m->d_node_rec, m->d_lo_z};
+  const int blocks = (int)((E + 255) / 256);
+  if (m->order == 1) k_elem_geometry<4><<<blocks, 256, 0, st>>>(E, p->d_dofs_morton, geo, det, cof);
+  else k_elem_geometry<10><<<blocks, 256, 0, st>>>(E, p->d_dofs_morton, geo, det, cof);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    cudaFree(det);
+    cudaFree(cof);
+    return cuda_error(e, "element geometry cache");
+  }
+  p->d_geo_det = det;
+  p->d_geo_cof = cof;
+  return MG_OK;
+}
+
 mg_status mg_adjoint_grad(mg_plan* p, const double* d_u, const double* d_lambda, int32_t quad, double* d_grad,
                           void* stream)
 {
@@ -1328,14 +1391,14 @@ mg_status mg_adjoint_grad(mg_plan* p, const double* d_u, const double* d_lambda,
   const int threads = 256;
   const int blocks = (int)((m->n_elem + threads - 1) / threads);
   cudaStream_t st = (cudaStream_t)stream;
-  const GeoPtrs geo{m->d_xyz, m->d_node_rec, m->d_lo_z};
+  MG_TRY(plan_geometry(p, st));
   if (blocks > 0) {
     if (m->order == 1)
-      k_adjoint<1><<<blocks, threads, 0, st>>>(m->n_elem, p->d_elem_order, p->d_dofs_morton, geo, d_tab, t->wsum,
-                                               d_u, d_lambda, d_grad);
+      k_adjoint<1><<<blocks, threads, 0, st>>>(m->n_elem, p->d_elem_order, p->d_dofs_morton, p->d_geo_det,
+                                               p->d_geo_cof, d_tab, t->wsum, d_u, d_lambda, d_grad);
     else
-      k_adjoint<2><<<blocks, threads, 0, st>>>(m->n_elem, p->d_elem_order, p->d_dofs_morton, geo, d_tab, t->wsum,
-                                               d_u, d_lambda, d_grad);
+      k_adjoint<2><<<blocks, threads, 0, st>>>(m->n_elem, p->d_elem_order, p->d_dofs_morton, p->d_geo_det,
+                                               p->d_geo_cof, d_tab, t->wsum, d_u, d_lambda, d_grad);
   }
   MG_CUDA(cudaGetLastError());
   return MG_OK;
@@ -1356,15 +1419,15 @@ mg_status mg_assemble_rhs(mg_plan* p, const double* d_field, const double* d_ele
   cudaStream_t st = (cudaStream_t)stream;
   const int threads = 256;
   const int nu = m->nb * (m->nb + 1) / 2;
-  const GeoPtrs geo{m->d_xyz, m->d_node_rec, m->d_lo_z};
+  MG_TRY(plan_geometry(p, st));
   const int eblocks = (int)((m->n_elem + threads - 1) / threads);
   if (eblocks > 0) {
     if (m->order == 1)
-      k_rhs_elem<1><<<eblocks, threads, 0, st>>>(m->n_elem, p->d_elem_order, p->d_dofs_morton, geo, d_tab + 6 * nu,
-                                                 d_field, d_elem_scale, p->d_rhs_y);
+      k_rhs_elem<1><<<eblocks, threads, 0, st>>>(m->n_elem, p->d_elem_order, p->d_dofs_morton, p->d_geo_det,
+                                                 d_tab + 6 * nu, d_field, d_elem_scale, p->d_rhs_y);
     else
-      k_rhs_elem<2><<<eblocks, threads, 0, st>>>(m->n_elem, p->d_elem_order, p->d_dofs_morton, geo, d_tab + 6 * nu,
-                                                 d_field, d_elem_scale, p->d_rhs_y);
+      k_rhs_elem<2><<<eblocks, threads, 0, st>>>(m->n_elem, p->d_elem_order, p->d_dofs_morton, p->d_geo_det,
+                                                 d_tab + 6 * nu, d_field, d_elem_scale, p->d_rhs_y);
     MG_CUDA(cudaGetLastError());
   }
   k_rhs_gather<<<(int)((p->ndof + threads - 1) / threads), threads, 0, st>>>(p->ndof, p->d_rhs_ptr, p->d_rhs_slot,

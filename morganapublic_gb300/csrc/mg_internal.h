@@ -180,6 +180,11 @@ struct mg_plan {
   int32_t* d_rhs_ptr = nullptr;       // ndof + 1
   int32_t* d_rhs_slot = nullptr;      // n_elem * nb
   double* d_rhs_y = nullptr;          // n_elem * nb
+  // element geometry in double-word form (built on the first call that needs it:
+  // load vector, adjoint), Morton order p: det[p] and cofactor k of element p at
+  // cof[k * n_elem + p] (k = 3 r + c), each (hi, lo) floats
+  float2* d_geo_det = nullptr;
+  float2* d_geo_cof = nullptr;
   // reference tables, cached per (quad) on the device
   std::vector<mg::RefTables> tables;
   std::vector<double*> d_tables;  // parallel to tables: stiff (6 nb^2) then mass (nb^2)

@@ -651,6 +651,8 @@ static void free_plan(mg_plan* p)
   cudaFree(p->d_rhs_ptr);
   cudaFree(p->d_rhs_slot);
   cudaFree(p->d_rhs_y);
+  cudaFree(p->d_geo_det);
+  cudaFree(p->d_geo_cof);
   cudaFree(p->d_entries);
   cudaFree(p->d_counters);
   for (double* t : p->d_tables) cudaFree(t);
