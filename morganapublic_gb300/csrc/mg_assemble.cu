@@ -1229,21 +1229,23 @@ __global__ void __launch_bounds__(256) k_rhs_elem(int64_t n_elem, const int32_t*
     out[l] = make_double2(ff_to_double_pow2(v[2 * l], k2), ff_to_double_pow2(v[2 * l + 1], k2));
 }
 
-// Pass 2, one thread per dof: b_i = the FP64 sum of its element-vector entries
-// in ascending slot order (a fixed order: bitwise reproducible, no atomics).
+// Pass 2, G lanes per dof: b_i = the FP64 sum of its element-vector entries,
+// each lane over every G-th entry in ascending slot order, the lanes combined
+// by xor shuffles in a fixed tree (bitwise reproducible, no atomics).
+template <int G, int U>
 __global__ void __launch_bounds__(256) k_rhs_gather(int64_t ndof, const int32_t* __restrict__ ptr,
                                                     const int32_t* __restrict__ slot, const double* __restrict__ y,
                                                     double* __restrict__ b)
 {
-  constexpr int U = 8;
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= ndof) return;
+  const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / G;
+  const int lane = threadIdx.x & (G - 1);
+  if (i >= ndof) return;  // whole groups: G divides the block
   const int s0 = __ldg(ptr + i), s1 = __ldg(ptr + i + 1);
   double acc = 0.0;
-  for (int base = s0; base < s1; base += U) {
+  for (int base = s0 + lane; base < s1; base += G * U) {
     int q[U];
 #pragma unroll
-    for (int u = 0; u < U; ++u) q[u] = base + u < s1 ? __ldg(slot + base + u) : -1;
+    for (int u = 0; u < U; ++u) q[u] = base + u * G < s1 ? __ldg(slot + base + u * G) : -1;
     double t[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) t[u] = q[u] >= 0 ? __ldg(y + q[u]) : 0.0;
@@ -1251,7 +1253,12 @@ __global__ void __launch_bounds__(256) k_rhs_gather(int64_t ndof, const int32_t*
     for (int u = 0; u < U; ++u)
       if (q[u] >= 0) acc += t[u];
   }
-  b[i] = acc;
+  if constexpr (G > 1) {
+    const unsigned mask = ((1u << G) - 1u) << ((threadIdx.x & 31u) & ~(unsigned)(G - 1));
+#pragma unroll
+    for (int off = G / 2; off > 0; off >>= 1) acc += __shfl_xor_sync(mask, acc, off, G);
+  }
+  if (lane == 0) b[i] = acc;
 }
 
 }  // namespace mg
@@ -1430,8 +1437,14 @@ mg_status mg_assemble_rhs(mg_plan* p, const double* d_field, const double* d_ele
                                                  d_tab + 6 * nu, d_field, d_elem_scale, p->d_rhs_y);
     MG_CUDA(cudaGetLastError());
   }
-  k_rhs_gather<<<(int)((p->ndof + threads - 1) / threads), threads, 0, st>>>(p->ndof, p->d_rhs_ptr, p->d_rhs_slot,
-                                                                             p->d_rhs_y, d_b);
+  // two lanes per dof when dofs sum more than 16 entries on average (P1: ~24),
+  // else one (P2: ~7); measured on GB300 at P1 64^3 / 128^3 and P2 48^3
+  if (m->n_elem * m->nb > 16 * p->ndof)
+    k_rhs_gather<2, 8><<<(int)((p->ndof * 2 + threads - 1) / threads), threads, 0, st>>>(
+        p->ndof, p->d_rhs_ptr, p->d_rhs_slot, p->d_rhs_y, d_b);
+  else
+    k_rhs_gather<1, 8><<<(int)((p->ndof + threads - 1) / threads), threads, 0, st>>>(
+        p->ndof, p->d_rhs_ptr, p->d_rhs_slot, p->d_rhs_y, d_b);
   MG_CUDA(cudaGetLastError());
   return MG_OK;
 }
