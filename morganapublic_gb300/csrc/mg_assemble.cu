@@ -698,9 +698,13 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
     const int g = tid / kThreads;           // group
     const int gtid = tid - g * kThreads;    // thread within the group
     const int gwarp = gtid >> 5;
-    const int local = gtid / TPI, sub = gtid % TPI;
+    // item of the chunk and share of its entries: for P2 the lanes of a warp take
+    // the 32 items and the warps the entries (u = warp + 8k), so the entry-major
+    // stores buf[u * CI + item] of a warp hit consecutive words (the other way
+    // round, 8-way bank conflicts)
+    const int local = gtid % CI, sub = gtid / CI;
     T* buf = reinterpret_cast<T*>(smem + L::off_buf + g * L::buf_bytes);
-    T* sgeo = reinterpret_cast<T*>(smem + L::off_geo + g * L::geo_bytes);  // P2: [CI][6]
+    T* sgeo = reinterpret_cast<T*>(smem + L::off_geo + g * L::geo_bytes);  // P2: [6][CI]
     const T wsum = A::from(a.wsum);
     int q = 0, ntok = 0;  // chunks before this block; token waits so far
     for (int j = 0;; ++j) {
@@ -794,11 +798,11 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
               metric<T>(f, sc, gm);
               check_scale(sc, gm[0]);
 #pragma unroll
-              for (int k = 0; k < 6; ++k) sgeo[lane * 6 + k] = gm[k];
+              for (int k = 0; k < 6; ++k) sgeo[k * CI + lane] = gm[k];
             } else {
               const T sc = coef * f.det;
               check_scale(sc, sc);
-              sgeo[lane * 6] = sc;
+              sgeo[lane] = sc;
             }
           }
           failed = group_sync_or(g, failed);
@@ -806,10 +810,10 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
             if (a.stiff) {
               T gm[6];
 #pragma unroll
-              for (int k = 0; k < 6; ++k) gm[k] = sgeo[local * 6 + k];
+              for (int k = 0; k < 6; ++k) gm[k] = sgeo[k * CI + local];
               for (int u = sub; u < NU; u += TPI) buf[u * CI + local] = metric_dot<T>(gm, tab, NU, u);
             } else {
-              const T sc = sgeo[local * 6];
+              const T sc = sgeo[local];
               for (int u = sub; u < NU; u += TPI) buf[u * CI + local] = sc * tab[6 * NU + u];
             }
           }
