@@ -379,10 +379,11 @@ static mg_status build_schedule(mg_plan* p, HostSchedule* hs)
     struct Seg { int32_t slot, begin, len; };
     std::vector<std::vector<uint32_t>> per(kThreads);
     std::vector<std::vector<int32_t>> tseg(kThreads);
-    std::vector<std::pair<int32_t, uint32_t>> list;  // (slot, src) in item order
-    std::vector<Seg> segs;
+    std::vector<std::pair<int32_t, uint32_t>> list, tmp;  // (slot, src) in item order
+    std::vector<Seg> segs, segs_by_len;
     std::vector<uint32_t> srcs;
     std::vector<int64_t> heap;
+    std::vector<int32_t> cnt;
 #pragma omp for schedule(dynamic, 1)
     for (int32_t b = 0; b < nbk; ++b) {
       const BlockDesc& d = hs->blocks[b];
@@ -397,20 +398,29 @@ static mg_status build_schedule(mg_plan* p, HostSchedule* hs)
             for (int j = 0; j < nb; ++j) {    // test (row)
               const int32_t row = m->dofs[e * nb + j];
               if (block_of[row] != b) continue;
+              // position of col in the row's sorted columns (rows are short:
+              // a branch-free count beats a binary search)
               const int32_t* c0 = p->colind.data() + p->rowptr[row];
-              const int32_t* c1 = p->colind.data() + p->rowptr[row + 1];
-              const int32_t pos = (int32_t)(std::lower_bound(c0, c1, col) - c0);
+              const int32_t len = p->rowptr[row + 1] - p->rowptr[row];
+              int32_t pos = 0;
+              for (int32_t k = 0; k < len; ++k) pos += c0[k] < col;
               const int32_t acc = row_acc_of[row] + pos;
               list.emplace_back(acc, (uint32_t)(sym_index(i, j, nb) * CI + t));
             }
           }
         }
         contrib[b] += (int64_t)list.size();
-        // segments: one per slot, contributions kept in item (= element) order
-        std::stable_sort(list.begin(), list.end(),
-                         [](const std::pair<int32_t, uint32_t>& x, const std::pair<int32_t, uint32_t>& y) {
-                           return x.first < y.first;
-                         });
+        // segments: one per slot, contributions kept in item (= element) order --
+        // a stable sort by slot (< 2^14: two 7-bit counting passes)
+        tmp.resize(list.size());
+        for (int pass = 0; pass < 2; ++pass) {
+          const int sh = 7 * pass;
+          cnt.assign(129, 0);
+          for (const auto& x : list) cnt[((x.first >> sh) & 127) + 1]++;
+          for (int k = 0; k < 128; ++k) cnt[k + 1] += cnt[k];
+          for (const auto& x : list) tmp[cnt[(x.first >> sh) & 127]++] = x;
+          list.swap(tmp);
+        }
         segs.clear();
         srcs.clear();
         for (size_t k = 0; k < list.size(); ++k) {
@@ -418,8 +428,18 @@ static mg_status build_schedule(mg_plan* p, HostSchedule* hs)
           segs.back().len++;
           srcs.push_back(list[k].second);
         }
-        // longest segment first, to the least-loaded thread (ties: lowest thread)
-        std::stable_sort(segs.begin(), segs.end(), [](const Seg& x, const Seg& y) { return x.len > y.len; });
+        // longest segment first (a stable counting sort by length, descending),
+        // to the least-loaded thread (ties: lowest thread)
+        {
+          int32_t maxlen = 0;
+          for (const Seg& sg : segs) maxlen = std::max(maxlen, sg.len);
+          cnt.assign(maxlen + 2, 0);
+          for (const Seg& sg : segs) cnt[maxlen - sg.len + 1]++;
+          for (int32_t k = 0; k <= maxlen; ++k) cnt[k + 1] += cnt[k];
+          segs_by_len.resize(segs.size());
+          for (const Seg& sg : segs) segs_by_len[cnt[maxlen - sg.len]++] = sg;
+          segs.swap(segs_by_len);
+        }
         for (auto& v : tseg) v.clear();
         // min-heap of (load, thread): pops the least-loaded, lowest-numbered thread
         heap.clear();
