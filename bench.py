@@ -92,14 +92,14 @@ def asm_bytes(E, nv, nnz, sv, nb=4):
 
 
 def adj_bytes(E, nv, ndof, nb=4):
-    """E (4 element id + 4 nb dofs + 8 gradient) + 36 n_v (node record) + 16 ndof (u, lambda)"""
-    return E * (12 + 4 * nb) + 36 * nv + 16 * ndof
+    """E (4 element id + 4 nb dofs + 80 cached geometry + 8 gradient) + 16 ndof (u, lambda)"""
+    return E * (92 + 4 * nb) + 16 * ndof
 
 
 def rhs_bytes(E, nv, ndof, nb=4):
-    """element pass E (4 position + 4 nb dofs + 8 scale + 8 nb out) + 36 n_v + 8 ndof (field);
+    """element pass E (4 element id + 4 nb dofs + 8 cached det + 8 scale + 8 nb out) + 8 ndof (field);
     dof pass 4 (ndof + 1) + 12 E nb (slot + entry) + 8 ndof (b)"""
-    return E * (16 + 12 * nb) + 36 * nv + 8 * ndof + 4 * (ndof + 1) + 12 * E * nb + 8 * ndof
+    return E * (24 + 12 * nb) + 8 * ndof + 4 * (ndof + 1) + 12 * E * nb + 8 * ndof
 
 
 def spmv_bytes(ndof, nnz, sv):
@@ -422,6 +422,11 @@ def run_config3(a):
     err64 = float(torch.linalg.norm(xs - uI_d) / torch.linalg.norm(uI_d))
     errmx = float(torch.linalg.norm(xr - uI_d) / torch.linalg.norm(uI_d))
     diff = float(torch.linalg.norm(xr - xs) / torch.linalg.norm(xs))
+    g = torch.empty(E, dtype=torch.float64, device="cuda")
+    yb = torch.empty_like(rhs)
+    tadj = _timed_cuda(torch, stream, lambda: b.adjoint_grad(xs, xr, quad=q, out=g, stream=stream), 10, flush)
+    trhs = _timed_cuda(torch, stream, lambda: b.build_vector(field=uI_d, elem_scale=kappa, quad=q, out=yb,
+                                                             stream=stream), 10, flush)
     B64, B32 = asm_bytes(E, len(m.xyz), nnz, 8, nb=10), asm_bytes(E, len(m.xyz), nnz, 4, nb=10)
     S64 = spmv_bytes(ndof, nnz, 8)
     line = {"config": {"workload": f"P2 kappa-stiffness, {n}^3 cells x 6 tets ({E} tets, {ndof} dofs, {nnz} CSR entries), "
@@ -433,6 +438,10 @@ def run_config3(a):
             "assembly_f32": {"ms": t32, "tets_per_s": E / (t32 * 1e-3), "gbs": B32 / (t32 * 1e-3) / 1e9,
                              "frac_of_hbm": B32 / (t32 * 1e-3) / 1e9 / peak},
             "spmv_f64_cold": {"ms": ts64, "gbs": S64 / (ts64 * 1e-3) / 1e9, "frac_of_hbm": S64 / (ts64 * 1e-3) / 1e9 / peak},
+            "adjoint_grad": {"ms": tadj, "tets_per_s": E / (tadj * 1e-3),
+                             "gbs": adj_bytes(E, len(m.xyz), ndof, 10) / (tadj * 1e-3) / 1e9},
+            "load_vector": {"ms": trhs, "tets_per_s": E / (trhs * 1e-3),
+                            "gbs": rhs_bytes(E, len(m.xyz), ndof, 10) / (trhs * 1e-3) / 1e9},
             "cg": {"fp64_pcg": i64.as_dict(), "fp32_refined": imx.as_dict(),
                    "speedup_refined_vs_fp64": i64.seconds / imx.seconds if imx.seconds > 0 else None,
                    "fp64_error_vs_exact_discrete": err64, "refined_error_vs_exact_discrete": errmx,
@@ -487,6 +496,9 @@ def run_config5(a):
     lam = torch.from_numpy(np.random.default_rng(4).uniform(-1, 1, ndof)).cuda()
     g = torch.empty(E, dtype=torch.float64, device="cuda")
     tg = _timed_cuda(torch, stream, lambda: b.adjoint_grad(xs, lam, quad=4, out=g, stream=stream), 10, flush)
+    yb = torch.empty_like(xs)
+    tb = _timed_cuda(torch, stream, lambda: b.build_vector(field=xs, elem_scale=kappa, quad=4, out=yb,
+                                                           stream=stream), 10, flush)
 
     def rec(bytes_, ms, units=None):
         gbs = bytes_ / (ms * 1e-3) / 1e9
@@ -504,6 +516,7 @@ def run_config5(a):
             "spmv_f64": rec(spmv_bytes(ndof, nnz, 8), ts64),
             "spmv_f32": rec(spmv_bytes(ndof, nnz, 4), ts32),
             "adjoint_grad": rec(adj_bytes(E, N, ndof), tg, E),
+            "load_vector": rec(rhs_bytes(E, N, ndof), tb, E),
             "cg": {"fp64_pcg": i64.as_dict(), "fp32_refined": imx.as_dict(),
                    "speedup_refined_vs_fp64": i64.seconds / imx.seconds if imx.seconds > 0 else None,
                    "refined_vs_fp64_rel_diff": diff, "precond": "jacobi", "rtol": 1e-10},
