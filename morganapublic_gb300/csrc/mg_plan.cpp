@@ -158,10 +158,14 @@ static mg_status build_schedule(mg_plan* p, HostSchedule* hs)
     key[d] = c;
   }
   std::vector<int32_t> order(nd);
-  std::iota(order.begin(), order.end(), 0);
-  std::sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
-    return key[a] != key[b] ? key[a] < key[b] : a < b;
-  });
+  {
+    std::vector<std::pair<uint64_t, int32_t>> kv(nd);
+#pragma omp parallel for
+    for (int64_t d = 0; d < nd; ++d) kv[d] = std::make_pair(key[d], (int32_t)d);
+    __gnu_parallel::sort(kv.begin(), kv.end());  // by key, ties by dof id
+#pragma omp parallel for
+    for (int64_t d = 0; d < nd; ++d) order[d] = kv[d].second;
+  }
   // greedy blocks of at most `cap` accumulator slots and kRowsMax rows.  The
   // kernel runs one persistent CTA per SM, so the cap is lowered until the
   // number of blocks is a multiple of the SM count (no partial last wave).
@@ -203,6 +207,7 @@ static mg_status build_schedule(mg_plan* p, HostSchedule* hs)
   hs->rows.resize(nd);
   hs->row_acc.resize(nd);
   hs->blocks.assign(nbk, BlockDesc{});
+#pragma omp parallel for schedule(dynamic, 16)
   for (int32_t b = 0; b < nbk; ++b) {
     std::vector<int32_t> rs(order.begin() + bstart[b], order.begin() + bstart[b + 1]);
     std::sort(rs.begin(), rs.end());
@@ -229,20 +234,42 @@ static mg_status build_schedule(mg_plan* p, HostSchedule* hs)
     }
     return n;
   };
-  for (int64_t e = 0; e < E; ++e) {
-    int32_t bs[10];
-    int n = blocks_of_elem(e, bs);
-    for (int u = 0; u < n; ++u) bcount[bs[u] + 1]++;
-  }
-  for (int32_t b = 0; b < nbk; ++b) bcount[b + 1] += bcount[b];
-  if (bcount[nbk] >= INT32_MAX) return set_error(MG_ERR_SIZE, "assembly items above 2^31-1");
-  hs->items.resize(bcount[nbk]);
   {
-    std::vector<int64_t> f(bcount.begin(), bcount.end() - 1);
-    for (int64_t e = 0; e < E; ++e) {
-      int32_t bs[10];
-      int n = blocks_of_elem(e, bs);
-      for (int u = 0; u < n; ++u) hs->items[f[bs[u]]++] = (int32_t)e;
+    // per-thread counts over a static split of the elements, then each thread
+    // fills its own ranges in the same split (each block's list is sorted below
+    // by key, then element id)
+    const int nth = std::max(1, omp_get_max_threads());
+    std::vector<int64_t> tc((size_t)nth * nbk, 0);
+#pragma omp parallel num_threads(nth)
+    {
+      int64_t* c = tc.data() + (size_t)omp_get_thread_num() * nbk;
+#pragma omp for schedule(static)
+      for (int64_t e = 0; e < E; ++e) {
+        int32_t bs[10];
+        const int n = blocks_of_elem(e, bs);
+        for (int u = 0; u < n; ++u) c[bs[u]]++;
+      }
+    }
+    for (int32_t b = 0; b < nbk; ++b) {
+      int64_t at = bcount[b];
+      for (int t = 0; t < nth; ++t) {
+        const int64_t k = tc[(size_t)t * nbk + b];
+        tc[(size_t)t * nbk + b] = at;
+        at += k;
+      }
+      bcount[b + 1] = at;
+    }
+    if (bcount[nbk] >= INT32_MAX) return set_error(MG_ERR_SIZE, "assembly items above 2^31-1");
+    hs->items.resize(bcount[nbk]);
+#pragma omp parallel num_threads(nth)
+    {
+      int64_t* f = tc.data() + (size_t)omp_get_thread_num() * nbk;
+#pragma omp for schedule(static)
+      for (int64_t e = 0; e < E; ++e) {
+        int32_t bs[10];
+        const int n = blocks_of_elem(e, bs);
+        for (int u = 0; u < n; ++u) hs->items[f[bs[u]]++] = (int32_t)e;
+      }
     }
   }
   // order each block's items along the Morton curve of the element centroids, so
