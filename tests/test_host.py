@@ -204,3 +204,41 @@ def test_schedule_slots_have_one_writer_per_chunk(order):
                             continue
                         assert slot < used and all(x <= zero for x in srcs) and srcs[0] < zero
                         assert owner.setdefault(slot, t) == t
+
+
+_SCHEDULE_DUMP = r"""
+import sys, pickle
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+import morganapublic_gb300 as mg
+from morganapublic_gb300 import meshgen
+out = {}
+for n, order in ((12, 1), (5, 2)):
+    m = meshgen.kuhn_cube(n, jitter=0.25, seed=3, permute=True)
+    b = mg.MatrixBuilder(mg.Mesh(m.xyz, m.conn, order=order))
+    rp, ci = b.pattern()
+    sched = b.export_schedule()
+    out[(n, order)] = (rp, ci, {k: np.asarray(v) for k, v in sched.items() if k != "info"})
+pickle.dump(out, open(sys.argv[2], "wb"))
+"""
+
+
+def test_plan_independent_of_thread_count(tmp_path):
+    """The host plan (pattern and assembly schedule) is built with OpenMP; its
+    per-thread counts and fills must give the same arrays for any thread count."""
+    import pickle
+    import subprocess
+    import sys
+    script = tmp_path / "dump.py"
+    script.write_text(_SCHEDULE_DUMP)
+    res = {}
+    for nth in (1, 4):
+        env = dict(os.environ, OMP_NUM_THREADS=str(nth))
+        out = tmp_path / f"s{nth}.pkl"
+        subprocess.run([sys.executable, str(script), ROOT, str(out)], env=env, check=True, timeout=300)
+        res[nth] = pickle.load(open(out, "rb"))
+    for key, (rp, ci, sched) in res[1].items():
+        rp4, ci4, sched4 = res[4][key]
+        assert np.array_equal(rp, rp4) and np.array_equal(ci, ci4)
+        for name, arr in sched.items():
+            assert np.array_equal(arr, sched4[name]), (key, name)
