@@ -92,8 +92,9 @@ def asm_bytes(E, nv, nnz, sv, nb=4):
 
 
 def adj_bytes(E, nv, ndof, nb=4):
-    """E (4 element id + 4 nb dofs + 80 cached geometry + 8 gradient) + 16 ndof (u, lambda)"""
-    return E * (92 + 4 * nb) + 16 * ndof
+    """E (4*4 connectivity + 8 gradient) + 3*8 n_v + 2*8 ndof (u, lambda).  The kernel reads the plan's
+    80-byte per-element geometry cache instead of the coordinates, so it moves more than this."""
+    return E * (4 * 4 + 8) + 3 * 8 * nv + 2 * 8 * ndof
 
 
 def rhs_bytes(E, nv, ndof, nb=4):
