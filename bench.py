@@ -406,14 +406,14 @@ def run_config3(a):
         rhs = b.apply(A64, uI_d, stream=stream)
     torch.cuda.synchronize()
     t64 = _timed_cuda(torch, stream, lambda: b.assemble("stiff_kappa", coeff=kappa, quad=q, prec="f64", out=A64,
-                                                        stream=stream), 5, flush)
+                                                        stream=stream), 20, flush)
     t32 = _timed_cuda(torch, stream, lambda: b.assemble("stiff_kappa", coeff=kappa, quad=q, prec="f32", out=A32,
-                                                        stream=stream), 5, flush)
+                                                        stream=stream), 20, flush)
     with torch.cuda.stream(stream):
         b.apply_dirichlet(A64, mask, stream=stream)
         b.apply_dirichlet(A32, mask, stream=stream)
     y = torch.empty_like(rhs)
-    ts64 = _timed_cuda(torch, stream, lambda: b.apply(A64, uI_d, out=y, stream=stream), 10, flush)
+    ts64 = _timed_cuda(torch, stream, lambda: b.apply(A64, uI_d, out=y, stream=stream), 20, flush)
     res = {}
     for rep in range(2):
         with torch.cuda.stream(stream):
@@ -425,9 +425,9 @@ def run_config3(a):
     diff = float(torch.linalg.norm(xr - xs) / torch.linalg.norm(xs))
     g = torch.empty(E, dtype=torch.float64, device="cuda")
     yb = torch.empty_like(rhs)
-    tadj = _timed_cuda(torch, stream, lambda: b.adjoint_grad(xs, xr, quad=q, out=g, stream=stream), 10, flush)
+    tadj = _timed_cuda(torch, stream, lambda: b.adjoint_grad(xs, xr, quad=q, out=g, stream=stream), 20, flush)
     trhs = _timed_cuda(torch, stream, lambda: b.build_vector(field=uI_d, elem_scale=kappa, quad=q, out=yb,
-                                                             stream=stream), 10, flush)
+                                                             stream=stream), 20, flush)
     B64, B32 = asm_bytes(E, len(m.xyz), nnz, 8, nb=10), asm_bytes(E, len(m.xyz), nnz, 4, nb=10)
     S64 = spmv_bytes(ndof, nnz, 8)
     line = {"config": {"workload": f"P2 kappa-stiffness, {n}^3 cells x 6 tets ({E} tets, {ndof} dofs, {nnz} CSR entries), "
@@ -478,11 +478,11 @@ def run_config5(a):
     x32 = x.float()
     y, y32 = torch.empty_like(x), torch.empty_like(x32)
     ta64 = _timed_cuda(torch, stream, lambda: b.assemble("stiff_kappa", coeff=kappa, quad=4, prec="f64", out=v64,
-                                                         stream=stream), 5, flush)
+                                                         stream=stream), 20, flush)
     ta32 = _timed_cuda(torch, stream, lambda: b.assemble("stiff_kappa", coeff=kappa, quad=4, prec="f32", out=v32,
-                                                         stream=stream), 5, flush)
-    ts64 = _timed_cuda(torch, stream, lambda: b.apply(v64, x, out=y, stream=stream), 10, flush)
-    ts32 = _timed_cuda(torch, stream, lambda: b.apply(v32, x32, out=y32, stream=stream), 10, flush)
+                                                         stream=stream), 20, flush)
+    ts64 = _timed_cuda(torch, stream, lambda: b.apply(v64, x, out=y, stream=stream), 20, flush)
+    ts32 = _timed_cuda(torch, stream, lambda: b.apply(v32, x32, out=y32, stream=stream), 20, flush)
     with torch.cuda.stream(stream):
         rhs = b.build_vector(quad=4, stream=stream)
         mask = torch.from_numpy(m.boundary)
@@ -496,10 +496,10 @@ def run_config5(a):
     diff = float(torch.linalg.norm(xr - xs) / torch.linalg.norm(xs))
     lam = torch.from_numpy(np.random.default_rng(4).uniform(-1, 1, ndof)).cuda()
     g = torch.empty(E, dtype=torch.float64, device="cuda")
-    tg = _timed_cuda(torch, stream, lambda: b.adjoint_grad(xs, lam, quad=4, out=g, stream=stream), 10, flush)
+    tg = _timed_cuda(torch, stream, lambda: b.adjoint_grad(xs, lam, quad=4, out=g, stream=stream), 20, flush)
     yb = torch.empty_like(xs)
     tb = _timed_cuda(torch, stream, lambda: b.build_vector(field=xs, elem_scale=kappa, quad=4, out=yb,
-                                                           stream=stream), 10, flush)
+                                                           stream=stream), 20, flush)
 
     def rec(bytes_, ms, units=None):
         gbs = bytes_ / (ms * 1e-3) / 1e9
@@ -637,7 +637,7 @@ def main():
     # ---------------------------------------------------------- extra metrics (untimed above)
     extras = {}
     if rank == 0:
-        def timed(fn, reps=10, flush_each=True):
+        def timed(fn, reps=20, flush_each=True):
             ts = []
             with torch.cuda.stream(stream):
                 for r in range(reps + 2):
