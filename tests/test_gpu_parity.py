@@ -300,6 +300,20 @@ def test_cg_deterministic_and_maxit_status():
     assert e.value.status == mg.MG_ERR_NOT_CONVERGED
 
 
+@pytest.mark.parametrize("op", ["stiff_kappa", "mass_coeff"])
+def test_p2_native_f64_assembly(op):
+    """MG_F64_NATIVE (native FP64 element arithmetic) on P2 against the oracle, and
+    against the double-word MG_F64 values."""
+    m, kappa = _case(3, 0.2, 13, True, 1.0)
+    b = mg.MatrixBuilder(mg.Mesh(m.xyz, m.conn, order=2))
+    _, rp, ci, ref = orc.full_operator(op, 2, 15, m.xyz, m.conn, coeff=kappa)
+    nat = b.assemble(op, coeff=kappa, quad=15, prec="f64_native").cpu().numpy()
+    dw = b.assemble(op, coeff=kappa, quad=15, prec="f64").cpu().numpy()
+    b.status()
+    assert row_scaled_err(rp, ref, nat) <= F64_TOL
+    assert row_scaled_err(rp, nat, dw) <= F64_TOL
+
+
 @pytest.mark.parametrize("order,quad", [(1, 1), (1, 4), (1, 15), (2, 4), (2, 11), (2, 15)])
 @pytest.mark.parametrize("scale", [1e-30, 1.0, 1e30])
 def test_load_vector_against_oracle(order, quad, scale):
