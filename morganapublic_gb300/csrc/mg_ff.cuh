@@ -99,20 +99,6 @@ __device__ __forceinline__ ff ff_cross(ff a, ff b, ff c, ff d)
   return two_sum(s.hi, lo);
 }
 
-// Running sum with deferred renormalisation: hi + lo are accumulated apart
-// (two_sum on the high parts, low parts and errors in one float) and
-// renormalised once at the end by ff_acc_value.
-struct ff_acc {
-  float hi, lo;
-};
-__device__ __forceinline__ void ff_acc_add(ff_acc& s, ff x)
-{
-  const ff t = two_sum(s.hi, x.hi);
-  s.hi = t.hi;
-  s.lo = __fadd_rn(s.lo, __fadd_rn(t.lo, x.lo));
-}
-__device__ __forceinline__ ff ff_acc_value(const ff_acc& s) { return two_sum(s.hi, s.lo); }
-
 __device__ __forceinline__ ff ff_neg(ff a) { return ff{-a.hi, -a.lo}; }
 __device__ __forceinline__ ff ff_sub(ff a, ff b) { return ff_add(a, ff_neg(b)); }
 
@@ -125,9 +111,6 @@ __device__ __forceinline__ ff ff_mul(ff a, ff b)
   p.lo = __fadd_rn(p.lo, t);
   return fast_two_sum(p.hi, p.lo);
 }
-
-// a * b + c * d with one renormalisation (the cofactor pattern)
-__device__ __forceinline__ ff ff_mul_add(ff a, ff b, ff c, ff d) { return ff_add(ff_mul(a, b), ff_mul(c, d)); }
 
 // Division: q1 = a.hi * rcp(b.hi), remainder r = a - q1 b in double-word, one
 // correction q2 = r.hi * rcp(b.hi) (a Newton step on the quotient); relative
@@ -150,8 +133,6 @@ __device__ __forceinline__ ff ff_from_double(double x)
   const float lo = __double2float_rn(x - (double)hi);
   return ff{hi, lo};
 }
-
-__device__ __forceinline__ double ff_to_double(ff a) { return (double)a.hi + (double)a.lo; }
 
 // Rare-case paths of the integer conversions below, kept out of line: inlined,
 // the compiler if-converts them into the hot path, and their predicated FP64
