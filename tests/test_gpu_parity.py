@@ -427,8 +427,19 @@ def test_single_tet_and_empty():
     K = b.assemble("stiff_kappa", coeff=np.ones(1)).cpu().numpy().reshape(4, 4)
     assert np.allclose(K, np.array([[3, -1, -1, -1], [-1, 1, 0, 0], [-1, 0, 1, 0], [-1, 0, 0, 1]]) / 6.0,
                        atol=1e-15)
+    # load vector of the reference tet: each vertex gets volume / 4
+    f = b.build_vector(quad=4).cpu().numpy()
+    assert np.allclose(f, np.full(4, 1.0 / 24.0), rtol=1e-15, atol=0)
+    # u = x, lambda = y: grad = -(grad lambda . grad u) vol = 0; u = lambda = x: -vol
+    g = b.adjoint_grad(torch.from_numpy(xyz[:, 0].copy()).cuda(), torch.from_numpy(xyz[:, 0].copy()).cuda(),
+                       quad=4).cpu().numpy()
+    assert abs(g[0] + 1.0 / 6.0) <= 1e-16
+    # a mesh of nodes without elements: empty pattern, zero load vector, empty gradient
     e = mg.MatrixBuilder(mg.Mesh(xyz, np.zeros((0, 4), dtype=np.int32)))
     assert e.assemble("mass").numel() == 0
+    assert np.all(e.build_vector(quad=4).cpu().numpy() == 0.0)
+    assert e.adjoint_grad(torch.zeros(4, dtype=torch.float64, device="cuda"),
+                          torch.zeros(4, dtype=torch.float64, device="cuda")).numel() == 0
 
 
 def test_invalid_arguments_fail_loudly():
