@@ -479,6 +479,11 @@ def run_config5(a):
     b.assemble("stiff_kappa", coeff=kappa, quad=4, prec="f64", out=v64)  # first use: chunk records + upload
     torch.cuda.synchronize()
     t_upload = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    bd = mg.MatrixBuilder(mesh, pattern_on_device=True)  # the same plan, CSR pattern built on the GPU
+    t_plan_dev = time.perf_counter() - t0
+    same_pattern = all(np.array_equal(u, w) for u, w in zip(b.pattern(), bd.pattern()))
+    bd.close()
     x = torch.from_numpy(np.random.default_rng(3).uniform(-1, 1, ndof)).cuda()
     x32 = x.float()
     y, y32 = torch.empty_like(x), torch.empty_like(x32)
@@ -517,7 +522,8 @@ def run_config5(a):
                                    "jitter +-0.25h, element permutation and lognormal kappa sigma 1.5 (seed 3), "
                                    "4-point rule; L2 flushed before each kernel timing",
                        "tets": E, "nodes": N, "nnz": nnz, "host_plan_seconds": t_plan,
-                       "first_use_seconds": t_upload},
+                       "first_use_seconds": t_upload, "plan_seconds_pattern_on_device": t_plan_dev,
+                       "device_pattern_identical": same_pattern},
             "assembly_f64": rec(asm_bytes(E, N, nnz, 8), ta64, E),
             "assembly_f32": rec(asm_bytes(E, N, nnz, 4), ta32, E),
             "spmv_f64": rec(spmv_bytes(ndof, nnz, 8), ts64),

@@ -141,6 +141,13 @@ mg_status mg_mesh_export_geometry(const mg_mesh* mesh, double* h_xyz, int32_t* h
    Replaces: the pattern half of traitsMatrixBuilder::buildEpetraCrs / numEntPerRow
    (src/morganaFiniteElements/traitsMatrixBuilder.hpp:363-544). */
 mg_status mg_pattern_build(mg_mesh* mesh, mg_plan** out);
+/* The same plan with the CSR pattern computed on the GPU (element couplings
+   as 64-bit keys, radix-sorted and de-duplicated on the device; identical
+   rowptr / colind), the assembly schedule then built on the host.  Needs a
+   device; waits for its own work on `stream`.  Up to 2^31 element couplings
+   (E nb^2), else MG_ERR_SIZE.
+   Replaces: the same pattern half of buildEpetraCrs. */
+mg_status mg_pattern_build_device(mg_mesh* mesh, mg_plan** out, void* stream);
 mg_status mg_plan_destroy(mg_plan* plan);
 mg_status mg_pattern_info(const mg_plan* plan, int64_t* ndof, int64_t* nnz);
 

@@ -81,6 +81,7 @@ SIGNATURES = {
     "mg_mesh_export_edges": [_P, _P, _P],
     "mg_mesh_export_geometry": [_P, _P, _P],
     "mg_pattern_build": [_P, ctypes.POINTER(_P)],
+    "mg_pattern_build_device": [_P, ctypes.POINTER(_P), _P],
     "mg_plan_destroy": [_P],
     "mg_pattern_info": [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64)],
     "mg_pattern_export": [_P, _P, _P],
@@ -227,10 +228,17 @@ class MatrixBuilder:
     """CSR pattern + GPU assembly schedule of a mesh (mg_plan); the counterpart of
     the reference's matrixBuilder / vectorBuilder and of the operator Belos uses."""
 
-    def __init__(self, mesh: Mesh):
+    def __init__(self, mesh: Mesh, pattern_on_device: bool = False, stream=None):
+        """pattern_on_device: compute the CSR pattern on the GPU (mg_pattern_build_device)
+        instead of the host; the result is identical."""
         self.mesh = mesh
         h = _P()
-        _check(lib().mg_pattern_build(mesh._h, ctypes.byref(h)), "mg_pattern_build")
+        if pattern_on_device:
+            _torch()
+            _check(lib().mg_pattern_build_device(mesh._h, ctypes.byref(h), _stream_ptr(stream)),
+                   "mg_pattern_build_device")
+        else:
+            _check(lib().mg_pattern_build(mesh._h, ctypes.byref(h)), "mg_pattern_build")
         self._h = h
         nd, nz = _I64(), _I64()
         _check(lib().mg_pattern_info(h, ctypes.byref(nd), ctypes.byref(nz)), "mg_pattern_info")

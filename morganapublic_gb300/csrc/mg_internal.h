@@ -223,6 +223,7 @@ mg_status plan_device(mg_plan* p);  // uploads mesh + plan on first GPU use
 mg_status plan_tables(mg_plan* p, int quad, const RefTables** t, const double** d_tab);
 mg_status plan_work(mg_plan* p, size_t bytes, void** ptr);
 mg_status plan_rhs_map(mg_plan* p);  // the load-vector slot map (once per plan)
+mg_status build_pattern_device(mg_plan* p, cudaStream_t st);  // CSR pattern on the GPU (mg_pattern.cu)
 mg_status ensure_edges(mg_mesh* m);
 mg_status launch_assemble(mg_plan* p, int op, const double* d_coeff, double c, int quad, int prec,
                           void* d_values, cudaStream_t st);

@@ -817,6 +817,24 @@ mg_status mg_pattern_build(mg_mesh* mesh, mg_plan** out)
   return MG_OK;
 }
 
+mg_status mg_pattern_build_device(mg_mesh* mesh, mg_plan** out, void* stream)
+{
+  NvtxRange nvtx_range("mg_pattern_build_device");
+  if (!mesh || !out) return set_error(MG_ERR_INVALID_ARG, "mg_pattern_build_device: null argument");
+  *out = nullptr;
+  mg_plan* p = new mg_plan();
+  p->mesh = mesh;
+  p->host_schedule = new HostSchedule();
+  mg_status s = build_pattern_device(p, (cudaStream_t)stream);
+  if (s == MG_OK) s = build_schedule(p, p->host_schedule);
+  if (s != MG_OK) {
+    free_plan(p);
+    return s;
+  }
+  *out = p;
+  return MG_OK;
+}
+
 mg_status mg_plan_destroy(mg_plan* plan)
 {
   free_plan(plan);

@@ -225,6 +225,42 @@ def test_unreferenced_nodes_give_empty_rows():
     assert np.max(np.abs(r - r_ref)) <= 1e-13 * np.abs(r_ref).max()
 
 
+@pytest.mark.parametrize("case", ["p1", "p2_lex", "p2_first", "extra_nodes", "single", "no_elements"])
+def test_device_pattern_build_matches_host(case):
+    """mg_pattern_build_device (CSR pattern from sorted element-coupling keys on
+    the GPU) gives the host build's rowptr / colind bit for bit, hence the same
+    assembly schedule and values."""
+    xyz1 = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], dtype=np.float64)
+    if case == "single":
+        xyz, conn, order, rule = xyz1, np.array([[0, 1, 2, 3]], dtype=np.int32), 1, "lex"
+    elif case == "no_elements":
+        xyz, conn, order, rule = xyz1, np.zeros((0, 4), dtype=np.int32), 1, "lex"
+    else:
+        m = meshgen.kuhn_cube(6 if case.startswith("p1") or case == "extra_nodes" else 4, jitter=0.2, seed=17,
+                              permute=True)
+        xyz, conn = m.xyz, m.conn
+        if case == "extra_nodes":
+            xyz = np.concatenate([xyz, np.random.default_rng(3).uniform(0, 1, (500, 3))])
+        order = 2 if case.startswith("p2") else 1
+        rule = "first" if case == "p2_first" else "lex"
+    mesh = mg.Mesh(xyz, conn, order=order, edge_rule=rule)
+    host = mg.MatrixBuilder(mesh)
+    dev = mg.MatrixBuilder(mesh, pattern_on_device=True)
+    assert (dev.ndof, dev.nnz) == (host.ndof, host.nnz)
+    rp_h, ci_h = host.pattern()
+    rp_d, ci_d = dev.pattern()
+    assert np.array_equal(rp_h, rp_d) and np.array_equal(ci_h, ci_d)
+    sh, sd = host.export_schedule(), dev.export_schedule()
+    for k in sh:
+        if k != "info":
+            assert np.array_equal(np.asarray(sh[k]), np.asarray(sd[k])), k
+    if len(conn):
+        kappa = meshgen.lognormal(len(conn), 1.0, 5)
+        vh = host.assemble("stiff_kappa", coeff=kappa, quad=4).cpu().numpy()
+        vd = dev.assemble("stiff_kappa", coeff=kappa, quad=4).cpu().numpy()
+        assert np.array_equal(vh.view(np.int64), vd.view(np.int64))
+
+
 def test_nonfinite_coefficient_is_reported():
     """A NaN or Inf in the per-element coefficient is an error returned through
     the C ABI (mg_plan_status; the host-buffer call checks it itself); a clean
