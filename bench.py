@@ -386,8 +386,22 @@ def run_config3(a):
     peak, peak_kind = peaks()
     m = meshgen.kuhn_cube(n)
     kappa_h = meshgen.lognormal(len(m.conn), 0.5, a.seed)
+    setup = {}
+    t0 = time.perf_counter()
     mesh = mg.Mesh(m.xyz, m.conn, order=2)
+    setup["mesh_edges_host_s"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
     b = mg.MatrixBuilder(mesh)
+    setup["plan_host_s"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    mesh_d = mg.Mesh(m.xyz, m.conn, order=2, edges_on_device=True)
+    setup["mesh_edges_device_s"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    b_d = mg.MatrixBuilder(mesh_d, pattern_on_device=True)
+    setup["plan_pattern_on_device_s"] = time.perf_counter() - t0
+    setup["identical"] = bool(np.array_equal(mesh.elem_dofs(), mesh_d.elem_dofs()) and
+                              all(np.array_equal(u, w) for u, w in zip(b.pattern(), b_d.pattern())))
+    b_d.close()
     E, ndof, nnz = len(m.conn), b.ndof, b.nnz
     en, _ = mesh.edges()
     X = np.concatenate([m.xyz, 0.5 * (m.xyz[en[:, 0]] + m.xyz[en[:, 1]])])
@@ -433,7 +447,7 @@ def run_config3(a):
     line = {"config": {"workload": f"P2 kappa-stiffness, {n}^3 cells x 6 tets ({E} tets, {ndof} dofs, {nnz} CSR entries), "
                                    "Keast 11-point rule, lognormal kappa sigma 0.5, rhs = A u_I (u_I = P2 interpolant "
                                    "of sin(pi x) sin(pi y) sin(pi z)), Dirichlet u = 0",
-                       "tets": E, "dofs": ndof, "nnz": nnz},
+                       "tets": E, "dofs": ndof, "nnz": nnz, "setup": setup},
             "assembly_f64": {"ms": t64, "tets_per_s": E / (t64 * 1e-3), "gbs": B64 / (t64 * 1e-3) / 1e9,
                              "frac_of_hbm": B64 / (t64 * 1e-3) / 1e9 / peak},
             "assembly_f32": {"ms": t32, "tets_per_s": E / (t32 * 1e-3), "gbs": B32 / (t32 * 1e-3) / 1e9,

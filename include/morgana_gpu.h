@@ -111,6 +111,13 @@ typedef struct {
    Returns MG_ERR_BAD_MESH when a tet has detJ <= 0 at a reference vertex. */
 mg_status mg_mesh_create(mg_mesh** out, int64_t n_nodes, const double* h_xyz, int64_t n_elements,
                          const int32_t* h_conn, int32_t order, int32_t edge_rule);
+/* The same mesh with the P2 edges enumerated and numbered on the GPU (element
+   edges as sorted node-pair keys, radix-sorted with their incidence index; LEX
+   ids from the run heads, FIRST ids by a second sort on first incidence):
+   identical edge table, element-to-edge table and dof map.  Needs a device;
+   waits for its own work on `stream`.  Up to 2^31 edge incidences (6 E). */
+mg_status mg_mesh_create_device(mg_mesh** out, int64_t n_nodes, const double* h_xyz, int64_t n_elements,
+                                const int32_t* h_conn, int32_t order, int32_t edge_rule, void* stream);
 
 /* Loads a Gmsh 2.x ASCII mesh: node id = line order in $Nodes (the file's own
    node label is ignored), tetrahedra = element type 4 in file order.

@@ -74,6 +74,7 @@ _I32, _I64, _D = ctypes.c_int32, ctypes.c_int64, ctypes.c_double
 # name -> argtypes; every function returns mg_status (int) unless listed in _RESTYPES
 SIGNATURES = {
     "mg_mesh_create": [ctypes.POINTER(_P), _I64, _P, _I64, _P, _I32, _I32],
+    "mg_mesh_create_device": [ctypes.POINTER(_P), _I64, _P, _I64, _P, _I32, _I32, _P],
     "mg_mesh_load_gmsh": [ctypes.POINTER(_P), ctypes.c_char_p, _I32, _I32],
     "mg_mesh_destroy": [_P],
     "mg_mesh_get_info": [_P, ctypes.POINTER(_MeshInfo)],
@@ -154,14 +155,22 @@ def _torch():
 class Mesh:
     """Tetrahedral mesh with its P1/P2 dof map (mg_mesh)."""
 
-    def __init__(self, xyz, conn, order: int = 1, edge_rule: str = "lex", _handle=None):
+    def __init__(self, xyz, conn, order: int = 1, edge_rule: str = "lex", _handle=None,
+                 edges_on_device: bool = False, stream=None):
+        """edges_on_device: enumerate the P2 edges on the GPU (mg_mesh_create_device); identical result."""
         L = lib()
         h = _P()
         if _handle is None:
             xyz = np.ascontiguousarray(xyz, dtype=np.float64)
             conn = np.ascontiguousarray(conn, dtype=np.int32)
-            _check(L.mg_mesh_create(ctypes.byref(h), xyz.shape[0], _ptr(xyz), conn.shape[0], _ptr(conn),
-                                    order, EDGES[edge_rule]), "mg_mesh_create")
+            if edges_on_device:
+                _torch()
+                _check(L.mg_mesh_create_device(ctypes.byref(h), xyz.shape[0], _ptr(xyz), conn.shape[0],
+                                               _ptr(conn), order, EDGES[edge_rule], _stream_ptr(stream)),
+                       "mg_mesh_create_device")
+            else:
+                _check(L.mg_mesh_create(ctypes.byref(h), xyz.shape[0], _ptr(xyz), conn.shape[0], _ptr(conn),
+                                        order, EDGES[edge_rule]), "mg_mesh_create")
         else:
             h = _handle
         self._h = h

@@ -133,6 +133,8 @@ namespace mg { struct HostSchedule; }
 // ---------------------------------------------------------------- handles --
 struct mg_mesh {
   int order = 1, edge_rule = MG_EDGES_LEX, nb = 4, device = 0;
+  bool edges_on_device = false;  // P2 edge enumeration on the GPU (mg_mesh_create_device)
+  void* edge_stream = nullptr;
   int64_t n_nodes = 0, n_elem = 0, n_edges = -1, ndof = 0;
   double min_det = 0.0;
   std::vector<double> xyz;          // n_nodes * 3
@@ -224,6 +226,7 @@ mg_status plan_tables(mg_plan* p, int quad, const RefTables** t, const double** 
 mg_status plan_work(mg_plan* p, size_t bytes, void** ptr);
 mg_status plan_rhs_map(mg_plan* p);  // the load-vector slot map (once per plan)
 mg_status build_pattern_device(mg_plan* p, cudaStream_t st);  // CSR pattern on the GPU (mg_pattern.cu)
+mg_status build_edges_device(mg_mesh* m, cudaStream_t st);    // edges on the GPU (mg_pattern.cu)
 mg_status ensure_edges(mg_mesh* m);
 mg_status launch_assemble(mg_plan* p, int op, const double* d_coeff, double c, int quad, int prec,
                           void* d_values, cudaStream_t st);

@@ -349,7 +349,8 @@ static mg_status finish_mesh(mg_mesh* m)
   }
   // dof map
   m->nb = nbasis(m->order);
-  if (m->order == 2) MG_TRY(ensure_edges(m));
+  if (m->order == 2)
+    MG_TRY(m->edges_on_device ? build_edges_device(m, (cudaStream_t)m->edge_stream) : ensure_edges(m));
   m->ndof = m->order == 1 ? N : N + m->n_edges;
   m->dofs.resize(E * m->nb);
   for (int64_t e = 0; e < E; ++e) {
@@ -367,10 +368,9 @@ using namespace mg;
 
 extern "C" {
 
-mg_status mg_mesh_create(mg_mesh** out, int64_t n_nodes, const double* h_xyz, int64_t n_elements,
-                         const int32_t* h_conn, int32_t order, int32_t edge_rule)
+static mg_status create_mesh(mg_mesh** out, int64_t n_nodes, const double* h_xyz, int64_t n_elements,
+                             const int32_t* h_conn, int32_t order, int32_t edge_rule, bool on_device, void* stream)
 {
-  NvtxRange nvtx_range("mg_mesh_create");
   if (!out || n_nodes < 0 || n_elements < 0 || (n_nodes > 0 && !h_xyz) ||
       (n_elements > 0 && !h_conn))
     return set_error(MG_ERR_INVALID_ARG, "mg_mesh_create: null or negative argument");
@@ -383,6 +383,8 @@ mg_status mg_mesh_create(mg_mesh** out, int64_t n_nodes, const double* h_xyz, in
   mg_mesh* m = new mg_mesh();
   m->order = order;
   m->edge_rule = edge_rule;
+  m->edges_on_device = on_device;
+  m->edge_stream = stream;
   m->nb = nbasis(order);
   m->n_nodes = n_nodes;
   m->n_elem = n_elements;
@@ -395,6 +397,20 @@ mg_status mg_mesh_create(mg_mesh** out, int64_t n_nodes, const double* h_xyz, in
   }
   *out = m;
   return MG_OK;
+}
+
+mg_status mg_mesh_create(mg_mesh** out, int64_t n_nodes, const double* h_xyz, int64_t n_elements,
+                         const int32_t* h_conn, int32_t order, int32_t edge_rule)
+{
+  NvtxRange nvtx_range("mg_mesh_create");
+  return create_mesh(out, n_nodes, h_xyz, n_elements, h_conn, order, edge_rule, false, nullptr);
+}
+
+mg_status mg_mesh_create_device(mg_mesh** out, int64_t n_nodes, const double* h_xyz, int64_t n_elements,
+                                const int32_t* h_conn, int32_t order, int32_t edge_rule, void* stream)
+{
+  NvtxRange nvtx_range("mg_mesh_create_device");
+  return create_mesh(out, n_nodes, h_xyz, n_elements, h_conn, order, edge_rule, true, stream);
 }
 
 mg_status mg_mesh_load_gmsh(mg_mesh** out, const char* path, int32_t order, int32_t edge_rule)

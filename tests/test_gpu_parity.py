@@ -261,6 +261,26 @@ def test_device_pattern_build_matches_host(case):
         assert np.array_equal(vh.view(np.int64), vd.view(np.int64))
 
 
+@pytest.mark.parametrize("rule", ["lex", "first"])
+@pytest.mark.parametrize("n,permute", [(1, False), (3, True), (7, True)])
+def test_device_edges_match_host(rule, n, permute):
+    """mg_mesh_create_device (P2 edges enumerated on the GPU) gives the host's edge
+    table, element-to-edge table and dof map bit for bit, for both numbering rules."""
+    m = meshgen.kuhn_cube(n, jitter=0.2 if n > 1 else 0.0, seed=23, permute=permute)
+    host = mg.Mesh(m.xyz, m.conn, order=2, edge_rule=rule)
+    dev = mg.Mesh(m.xyz, m.conn, order=2, edge_rule=rule, edges_on_device=True)
+    en_h, ee_h = host.edges()
+    en_d, ee_d = dev.edges()
+    assert np.array_equal(en_h, en_d) and np.array_equal(ee_h, ee_d)
+    assert np.array_equal(host.elem_dofs(), dev.elem_dofs())
+    if n == 3:
+        en_o, ee_o = orc.edges(len(m.xyz), m.conn, rule)
+        assert np.array_equal(en_d, en_o) and np.array_equal(ee_d, ee_o)
+    # P1 meshes and meshes without elements take the same entry point
+    assert mg.Mesh(m.xyz, m.conn, order=1, edges_on_device=True).ndof == len(m.xyz)
+    assert mg.Mesh(m.xyz, np.zeros((0, 4), dtype=np.int32), order=2, edges_on_device=True).ndof == len(m.xyz)
+
+
 def test_nonfinite_coefficient_is_reported():
     """A NaN or Inf in the per-element coefficient is an error returned through
     the C ABI (mg_plan_status; the host-buffer call checks it itself); a clean
