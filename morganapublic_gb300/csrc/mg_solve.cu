@@ -256,12 +256,58 @@ __device__ __forceinline__ double block_sum(typename Dot<V>::A v, typename Dot<V
   return out;
 }
 
+// NV block-wide sums at once (each value the same fixed tree as block_sum, so
+// the results are those of NV separate calls, with two barriers instead of 2 NV);
+// sh holds NV * 32 values.  Valid in thread 0.
+template <typename V, int NV>
+__device__ __forceinline__ void block_sum_n(typename Dot<V>::A (&v)[NV], typename Dot<V>::A* sh, double (&out)[NV])
+{
+  using D = Dot<V>;
+  const int tid = threadIdx.x;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+    for (int k = 0; k < NV; ++k) v[k] = D::add(v[k], D::shfl(v[k], off));
+  if ((tid & 31) == 0)
+#pragma unroll
+    for (int k = 0; k < NV; ++k) sh[k * 32 + (tid >> 5)] = v[k];
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < NV; ++k) out[k] = 0.0;
+  if (tid < 32) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) v[k] = tid < (kSolveThreads / 32) ? sh[k * 32 + tid] : D::zero();
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+      for (int k = 0; k < NV; ++k) v[k] = D::add(v[k], D::shfl(v[k], off));
+    if (tid == 0)
+#pragma unroll
+      for (int k = 0; k < NV; ++k) out[k] = D::to_double(v[k]);
+  }
+  __syncthreads();
+}
+
 // Sum of partials[0..n) in a fixed order by one CTA (valid in thread 0).
 __device__ __forceinline__ double reduce_partials(const double* partials, int n, double* sh)
 {
   double v = 0.0;
   for (int i = threadIdx.x; i < n; i += kSolveThreads) v += partials[i];
   return block_sum<double>(v, sh);
+}
+
+// NV arrays of partials (partials[k * n + i]) reduced together, each in the
+// order of reduce_partials; sh holds NV * 32 doubles.
+template <int NV>
+__device__ __forceinline__ void reduce_partials_n(const double* partials, int n, double* sh, double (&out)[NV])
+{
+  double v[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) v[k] = 0.0;
+  for (int i = threadIdx.x; i < n; i += kSolveThreads)
+#pragma unroll
+    for (int k = 0; k < NV; ++k) v[k] += partials[k * n + i];
+  block_sum_n<double, NV>(v, sh, out);
 }
 
 // Last-CTA detection: returns true in the single CTA that finishes last.
@@ -336,8 +382,8 @@ __global__ void __launch_bounds__(kSolveThreads) k_cg_update(int64_t n, V* __res
                                                              double* partials, CgScalars* s)
 {
   using D = Dot<V>;
-  __shared__ typename D::A sh[32];
-  __shared__ double shd[32];
+  __shared__ typename D::A sh[2 * 32];
+  __shared__ double shd[2 * 32];
   pdl_wait();
   pdl_trigger();
   if (s->done) return;
@@ -354,15 +400,17 @@ __global__ void __launch_bounds__(kSolveThreads) k_cg_update(int64_t n, V* __res
     D::mac(prz, ri, zi);
     D::mac(prr, ri, ri);
   }
-  const double b1 = block_sum<V>(prz, sh);
-  const double b2 = block_sum<V>(prr, sh);
+  typename D::A acc2[2] = {prz, prr};
+  double bl[2];
+  block_sum_n<V, 2>(acc2, sh, bl);
   if (threadIdx.x == 0) {
-    partials[blockIdx.x] = b1;
-    partials[gridDim.x + blockIdx.x] = b2;
+    partials[blockIdx.x] = bl[0];
+    partials[gridDim.x + blockIdx.x] = bl[1];
   }
   if (last_block(&s->ticket[1])) {
-    const double rz = reduce_partials(partials, gridDim.x, shd);
-    const double rr = reduce_partials(partials + gridDim.x, gridDim.x, shd);
+    double tot[2];
+    reduce_partials_n<2>(partials, gridDim.x, shd, tot);
+    const double rz = tot[0], rr = tot[1];
     if (threadIdx.x == 0) {
       s->rz_prev = s->rz;
       s->beta = rz / s->rz;
@@ -403,8 +451,8 @@ __global__ void __launch_bounds__(kSolveThreads) k_cg_start(int64_t n, const int
                                                             V* __restrict__ dinv, double* partials, CgScalars* s)
 {
   using D = Dot<V>;
-  __shared__ typename D::A sh[32];
-  __shared__ double shd[32];
+  __shared__ typename D::A sh[3 * 32];
+  __shared__ double shd[3 * 32];
   const int64_t groups = (int64_t)gridDim.x * (kSolveThreads / G);
   typename D::A prz = D::zero(), prr = D::zero(), pbb = D::zero();
   for (int64_t row = (blockIdx.x * (int64_t)kSolveThreads + threadIdx.x) / G; row < n; row += groups) {
@@ -424,16 +472,18 @@ __global__ void __launch_bounds__(kSolveThreads) k_cg_start(int64_t n, const int
       D::mac(pbb, b[row], b[row]);
     }
   }
-  const double b1 = block_sum<V>(prz, sh), b2 = block_sum<V>(prr, sh), b3 = block_sum<V>(pbb, sh);
+  typename D::A acc3[3] = {prz, prr, pbb};
+  double bl[3];
+  block_sum_n<V, 3>(acc3, sh, bl);
   if (threadIdx.x == 0) {
-    partials[blockIdx.x] = b1;
-    partials[gridDim.x + blockIdx.x] = b2;
-    partials[2 * gridDim.x + blockIdx.x] = b3;
+    partials[blockIdx.x] = bl[0];
+    partials[gridDim.x + blockIdx.x] = bl[1];
+    partials[2 * gridDim.x + blockIdx.x] = bl[2];
   }
   if (last_block(&s->ticket[2])) {
-    const double rz = reduce_partials(partials, gridDim.x, shd);
-    const double rr = reduce_partials(partials + gridDim.x, gridDim.x, shd);
-    const double bb = reduce_partials(partials + 2 * gridDim.x, gridDim.x, shd);
+    double tot[3];
+    reduce_partials_n<3>(partials, gridDim.x, shd, tot);
+    const double rz = tot[0], rr = tot[1], bb = tot[2];
     if (threadIdx.x == 0) {
       s->rz = rz;
       s->rr = rr;
@@ -455,7 +505,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_residual64(int64_t n, const i
                                                               const double* __restrict__ x, double* __restrict__ r,
                                                               double* partials, CgScalars* s)
 {
-  __shared__ double sh[32];
+  __shared__ double sh[2 * 32];
   const int64_t groups = (int64_t)gridDim.x * (kSolveThreads / G);
   double prr = 0.0, pbb = 0.0;
   for (int64_t row = (blockIdx.x * (int64_t)kSolveThreads + threadIdx.x) / G; row < n; row += groups) {
@@ -467,14 +517,16 @@ __global__ void __launch_bounds__(kSolveThreads) k_residual64(int64_t n, const i
       pbb = __fma_rn(b[row], b[row], pbb);
     }
   }
-  const double b1 = block_sum<double>(prr, sh), b2 = block_sum<double>(pbb, sh);
+  double acc2[2] = {prr, pbb}, bl[2];
+  block_sum_n<double, 2>(acc2, sh, bl);
   if (threadIdx.x == 0) {
-    partials[blockIdx.x] = b1;
-    partials[gridDim.x + blockIdx.x] = b2;
+    partials[blockIdx.x] = bl[0];
+    partials[gridDim.x + blockIdx.x] = bl[1];
   }
   if (last_block(&s->ticket[3])) {
-    const double rr = reduce_partials(partials, gridDim.x, sh);
-    const double bb = reduce_partials(partials + gridDim.x, gridDim.x, sh);
+    double tot[2];
+    reduce_partials_n<2>(partials, gridDim.x, sh, tot);
+    const double rr = tot[0], bb = tot[1];
     if (threadIdx.x == 0) {
       s->rr = rr;
       s->bb = bb > 0.0 ? bb : 1.0;
@@ -509,8 +561,8 @@ __global__ void __launch_bounds__(kSolveThreads) k_anchor_r(int64_t n, const dou
                                                             CgScalars* s)
 {
   using D = Dot<float>;
-  __shared__ D::A sh[32];
-  __shared__ double shd[32];
+  __shared__ D::A sh[2 * 32];
+  __shared__ double shd[2 * 32];
   D::A prz = D::zero(), prr = D::zero();
   for (int64_t i = blockIdx.x * (int64_t)kSolveThreads + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * kSolveThreads) {
@@ -521,14 +573,17 @@ __global__ void __launch_bounds__(kSolveThreads) k_anchor_r(int64_t n, const dou
     D::mac(prz, ri, zi);
     D::mac(prr, ri, ri);
   }
-  const double b1 = block_sum<float>(prz, sh), b2 = block_sum<float>(prr, sh);
+  D::A acc2[2] = {prz, prr};
+  double bl[2];
+  block_sum_n<float, 2>(acc2, sh, bl);
   if (threadIdx.x == 0) {
-    partials[blockIdx.x] = b1;
-    partials[gridDim.x + blockIdx.x] = b2;
+    partials[blockIdx.x] = bl[0];
+    partials[gridDim.x + blockIdx.x] = bl[1];
   }
   if (last_block(&s->ticket[1])) {
-    const double rz = reduce_partials(partials, gridDim.x, shd);
-    const double rr = reduce_partials(partials + gridDim.x, gridDim.x, shd);
+    double tot[2];
+    reduce_partials_n<2>(partials, gridDim.x, shd, tot);
+    const double rz = tot[0], rr = tot[1];
     if (threadIdx.x == 0) {
       s->beta = rz / s->rz_prev;
       s->rz = rz;
