@@ -423,6 +423,8 @@ def run_config3(a):
                                                         stream=stream), 20, flush)
     t32 = _timed_cuda(torch, stream, lambda: b.assemble("stiff_kappa", coeff=kappa, quad=q, prec="f32", out=A32,
                                                         stream=stream), 20, flush)
+    t64n = _timed_cuda(torch, stream, lambda: b.assemble("stiff_kappa", coeff=kappa, quad=q, prec="f64_native",
+                                                         out=A64, stream=stream), 20, flush)
     with torch.cuda.stream(stream):
         b.apply_dirichlet(A64, mask, stream=stream)
         b.apply_dirichlet(A32, mask, stream=stream)
@@ -452,6 +454,8 @@ def run_config3(a):
                              "frac_of_hbm": B64 / (t64 * 1e-3) / 1e9 / peak},
             "assembly_f32": {"ms": t32, "tets_per_s": E / (t32 * 1e-3), "gbs": B32 / (t32 * 1e-3) / 1e9,
                              "frac_of_hbm": B32 / (t32 * 1e-3) / 1e9 / peak},
+            "assembly_f64_native": {"ms": t64n, "tets_per_s": E / (t64n * 1e-3),
+                                    "note": "native FP64 element arithmetic (MG_F64_NATIVE), for comparison"},
             "spmv_f64_cold": {"ms": ts64, "gbs": S64 / (ts64 * 1e-3) / 1e9, "frac_of_hbm": S64 / (ts64 * 1e-3) / 1e9 / peak},
             "adjoint_grad": {"ms": tadj, "tets_per_s": E / (tadj * 1e-3),
                              "gbs": adj_bytes(E, len(m.xyz), ndof, 10) / (tadj * 1e-3) / 1e9},
@@ -506,6 +510,8 @@ def run_config5(a):
                                                          stream=stream), 20, flush)
     ta32 = _timed_cuda(torch, stream, lambda: b.assemble("stiff_kappa", coeff=kappa, quad=4, prec="f32", out=v32,
                                                          stream=stream), 20, flush)
+    ta64n = _timed_cuda(torch, stream, lambda: b.assemble("stiff_kappa", coeff=kappa, quad=4, prec="f64_native",
+                                                          out=v64, stream=stream), 20, flush)
     ts64 = _timed_cuda(torch, stream, lambda: b.apply(v64, x, out=y, stream=stream), 20, flush)
     ts32 = _timed_cuda(torch, stream, lambda: b.apply(v32, x32, out=y32, stream=stream), 20, flush)
     with torch.cuda.stream(stream):
@@ -541,6 +547,7 @@ def run_config5(a):
                        "device_pattern_identical": same_pattern},
             "assembly_f64": rec(asm_bytes(E, N, nnz, 8), ta64, E),
             "assembly_f32": rec(asm_bytes(E, N, nnz, 4), ta32, E),
+            "assembly_f64_native": rec(asm_bytes(E, N, nnz, 8), ta64n, E),
             "spmv_f64": rec(spmv_bytes(ndof, nnz, 8), ts64),
             "spmv_f32": rec(spmv_bytes(ndof, nnz, 4), ts32),
             "adjoint_grad": rec(adj_bytes(E, N, ndof), tg, E),
