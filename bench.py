@@ -52,7 +52,7 @@ def parse():
                          "5: P1 128^3 kernels as fractions of the HBM roofline")
     ap.add_argument("--order", type=int, default=1, choices=[1, 2], help="element order of the --only modes")
     ap.add_argument("--only", default=None,
-                    choices=["asm64", "asm32", "spmv64", "spmv32", "cg64", "cg32", "adj", "rhs", "suite"],
+                    choices=["asm64", "asm32", "spmv64", "spmv32", "cg64", "cg32", "adj", "rhs", "suite", "setup"],
                     help="run warmup + steps launches of one kernel only (for profilers) and print its timing")
     return ap.parse_args()
 
@@ -256,6 +256,28 @@ def run_only(a):
     import morganapublic_gb300 as mg
     from morganapublic_gb300 import meshgen
     m = meshgen.kuhn_cube(a.n, jitter=a.jitter, seed=a.seed, permute=True)
+    if a.only == "setup":
+        # mesh preprocessing on the GPU (P2 edges, CSR pattern) against the host builds
+        res = {}
+        for r in range(a.warmup + a.steps):
+            t0 = time.perf_counter()
+            mh = mg.Mesh(m.xyz, m.conn, order=a.order)
+            t1 = time.perf_counter()
+            bh = mg.MatrixBuilder(mh)
+            t2 = time.perf_counter()
+            md = mg.Mesh(m.xyz, m.conn, order=a.order, edges_on_device=True)
+            t3 = time.perf_counter()
+            bd = mg.MatrixBuilder(md, pattern_on_device=True)
+            t4 = time.perf_counter()
+            same = all(np.array_equal(u, w) for u, w in zip(bh.pattern(), bd.pattern()))
+            if r >= a.warmup:
+                for k, v in (("mesh_host_s", t1 - t0), ("plan_host_s", t2 - t1), ("mesh_device_s", t3 - t2),
+                             ("plan_device_pattern_s", t4 - t3)):
+                    res.setdefault(k, []).append(v)
+            bh.close(), bd.close(), mh.close(), md.close()
+        print(json.dumps({"only": "setup", "n": a.n, "order": a.order, "identical": same,
+                          **{k: statistics.median(v) for k, v in res.items()}}))
+        return 0
     kappa = torch.from_numpy(meshgen.lognormal(len(m.conn), a.sigma, a.seed)).cuda()
     mesh = mg.Mesh(m.xyz, m.conn, order=a.order)
     b = mg.MatrixBuilder(mesh)
