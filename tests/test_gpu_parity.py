@@ -58,9 +58,14 @@ def test_p2_assembly_f64(op, rule):
     b = mg.MatrixBuilder(mesh)
     dofs, rp, ci, ref = orc.full_operator(op, 2, 15, m.xyz, m.conn, coeff=kappa, c=0.75, edge_rule=rule)
     assert np.array_equal(mesh.elem_dofs(), dofs)
-    for quad in (15, 11):  # Keast 11 is exact for these degree <= 4 integrands on affine tets
+    for quad in (15, 11, 64):  # 11 and 64 are exact for these degree <= 4 integrands on affine tets
         vals = b.assemble(op, coeff=kappa, c=0.75, quad=quad, prec="f64").cpu().numpy()
         assert row_scaled_err(rp, ref, vals) <= F64_TOL, quad
+    # the under-integrating cards against the oracle with the same card
+    for quad in (1, 4):
+        _, _, _, ref_q = orc.full_operator(op, 2, quad, m.xyz, m.conn, coeff=kappa, c=0.75, edge_rule=rule)
+        vals = b.assemble(op, coeff=kappa, c=0.75, quad=quad, prec="f64").cpu().numpy()
+        assert row_scaled_err(rp, ref_q, vals) <= F64_TOL, quad
 
 
 def test_p2_assembly_f32():
@@ -370,7 +375,7 @@ def test_p2_native_f64_assembly(op):
     assert row_scaled_err(rp, nat, dw) <= F64_TOL
 
 
-@pytest.mark.parametrize("order,quad", [(1, 1), (1, 4), (1, 15), (2, 4), (2, 11), (2, 15)])
+@pytest.mark.parametrize("order,quad", [(1, 1), (1, 4), (1, 15), (1, 64), (2, 4), (2, 11), (2, 15), (2, 64)])
 @pytest.mark.parametrize("scale", [1e-30, 1.0, 1e30])
 def test_load_vector_against_oracle(order, quad, scale):
     """mg_assemble_rhs (element vectors + fixed-order per-dof sums) against the
