@@ -161,12 +161,15 @@ __device__ __forceinline__ double ff_to_double_bits(ff a) { return f2d_bits(a.hi
 static __device__ __noinline__ double ff_to_double_slow(ff a) { return ff_to_double_bits(a); }
 
 // hi + lo as a double without FP64 arithmetic: after renormalisation
-// (|lo| <= ulp(hi)/2), lo is expressed in units of the double ulp of hi
-// (a power-of-two scaling, exact) and rounded to an integer n, which is added
-// to the bit pattern of double(hi) -- integer carries cross binades correctly,
-// so the result is within half a double ulp of hi + lo.  Outside the range
-// where the scaling stays a normal float (|hi| below ~2^-74 or above ~2^127),
-// and for Inf or NaN, it falls back to ff_to_double_bits (zero gives +0).
+// (|lo| <= ulp(hi)/2), lo is expressed in units of the double ulp of the
+// binade hi + lo lies in (a power-of-two scaling, exact) and rounded to an
+// integer k, which is added to the bit pattern of double(hi).  That binade is
+// hi's own, except when |hi| is a power of two and lo points towards zero: then
+// hi + lo lies in the binade below, whose ulp is half as large (counting in
+// hi's ulp there would move the result by only half of lo).  The result is
+// within half a double ulp of hi + lo.  Outside the range where the scaling
+// stays a normal float (|hi| below ~2^-74 or above ~2^126), and for Inf or NaN,
+// it falls back to ff_to_double_bits (zero gives +0).
 __device__ __forceinline__ double ff_to_double_int(ff a)
 {
   const ff n = fast_two_sum(a.hi, a.lo);
@@ -174,8 +177,10 @@ __device__ __forceinline__ double ff_to_double_int(ff a)
   const int e = (int)((u >> 23) & 0xffu) - 127;  // unbiased exponent of hi
   if (n.hi == 0.0f) return 0.0;
   if (e < -74 || e > 126) return ff_to_double_slow(n);
-  const float scale = __uint_as_float((uint32_t)(52 - e + 127) << 23);  // 2^(52 - e)
-  int k = __float2int_rn(__fmul_rn(n.lo, scale));                    // lo / ulp_double(hi)
+  // one binade down when hi = +-2^e and lo has the opposite sign
+  const int down = ((u & 0x7fffffu) == 0u && n.lo != 0.0f && ((__float_as_uint(n.lo) ^ u) >> 31)) ? 1 : 0;
+  const float scale = __uint_as_float((uint32_t)(52 - e + down + 127) << 23);  // 1 / ulp_double of hi + lo
+  int k = __float2int_rn(__fmul_rn(n.lo, scale));                           // lo in those units
   if (u >> 31) k = -k;  // magnitudes: the bit pattern grows with |x|
   const long long bits = __double_as_longlong(f2d_bits(n.hi)) + (long long)k;
   return __longlong_as_double(bits);
