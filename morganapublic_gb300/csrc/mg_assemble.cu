@@ -260,10 +260,75 @@ __device__ __forceinline__ void geometry(const Fetch<kF64>& F, Cof<double>& f)
   cofactors<double>(J, f);
 }
 
+// Near-degenerate elements.  The determinant is a cofactor expansion; when its
+// terms cancel (sum_k |J0k C0k| > kCancelTol |det|) the relative error of det,
+// and of every entry scaled by 1/det, is that many times the arithmetic's own
+// (measured on GB300: double-word 2.3e-12 and FP32 7e-6 against the FP64 oracle
+// at a cancellation of ~230).  Such elements recompute J, the cofactors and det
+// in FP64 from the staged coordinates -- out of line, so that the rare FP64
+// path does not occupy the FP64 pipe of every other element.
+constexpr float kCancelTol = 16.0f;
+
+template <typename T>
+__device__ __forceinline__ float hi_of(const T& v);
+template <>
+__device__ __forceinline__ float hi_of<float>(const float& v) { return v; }
+template <>
+__device__ __forceinline__ float hi_of<ff>(const ff& v) { return v.hi; }
+
+// |det| small against its expansion terms
+template <typename T>
+__device__ __forceinline__ bool det_cancels(const T J[3][3], const Cof<T>& f)
+{
+  const float t = fabsf(hi_of(J[0][0]) * hi_of(f.c[0][0])) + fabsf(hi_of(J[0][1]) * hi_of(f.c[0][1])) +
+                  fabsf(hi_of(J[0][2]) * hi_of(f.c[0][2]));
+  return t > kCancelTol * fabsf(hi_of(f.det));
+}
+
+// FP64 geometry from staged hi + lo coordinates (exact as doubles)
+__device__ __forceinline__ void geometry_fp64_staged(const float4* a, const float2* b, Cof<double>& d)
+{
+  Fetch<kF64> D;
+#pragma unroll
+  for (int s = 0; s < 4; ++s)
+    D.x[s] = make_double4_32a((double)a[s].x + (double)a[s].w, (double)a[s].y + (double)b[s].x,
+                              (double)a[s].z + (double)b[s].y, 0.0);
+  geometry(D, d);
+}
+__device__ __forceinline__ void store_geometry(const Cof<double>& d, Cof<float>& f)
+{
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) f.c[r][k] = (float)d.c[r][k];
+  f.det = (float)d.det;
+}
+__device__ __forceinline__ void store_geometry(const Cof<double>& d, Cof<ff>& f)
+{
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) f.c[r][k] = ff_from_double_bits(d.c[r][k]);
+  f.det = ff_from_double_bits(d.det);
+}
+// The FP64 recompute of the lanes that need it, entered only when one lane of
+// the warp does (a warp-uniform branch around a large block: not if-converted,
+// no call and no stack frame on the common path).
+template <typename T>
+__device__ __forceinline__ void fix_near_degenerate(const float4* a, const float2* b, const T J[3][3], Cof<T>& f)
+{
+  const bool need = det_cancels<T>(J, f);
+  if (__any_sync(__activemask(), need)) {
+    if (need) {
+      Cof<double> d;
+      geometry_fp64_staged(a, b, d);
+      store_geometry(d, f);
+    }
+  }
+}
+
 // FP32: edge vectors (hi_k - hi_0) + (lo_k - lo_0) of the chunk-relative
-// coordinates, accurate to a few float ulps of the edge itself; flat elements
-// recompute the cofactors in FP64 from hi + lo.
-constexpr float kFlatTol = 1e-3f;
+// coordinates, accurate to a few float ulps of the edge itself.
 __device__ __forceinline__ void geometry(const Fetch<kF32>& F, Cof<float>& f)
 {
   float J[3][3];
@@ -273,21 +338,7 @@ __device__ __forceinline__ void geometry(const Fetch<kF32>& F, Cof<float>& f)
     for (int k = 0; k < 3; ++k)
       J[r][k] = (vhi(F.a[k + 1], r) - vhi(F.a[0], r)) + (vlo(F.a[k + 1], F.b[k + 1], r) - vlo(F.a[0], F.b[0], r));
   cofactors<float>(J, f);
-  float nn[3];
-#pragma unroll
-  for (int k = 0; k < 3; ++k) nn[k] = J[0][k] * J[0][k] + J[1][k] * J[1][k] + J[2][k] * J[2][k];
-  if (f.det * f.det < kFlatTol * kFlatTol * nn[0] * nn[1] * nn[2]) {
-    Fetch<kF64> D;
-#pragma unroll
-    for (int s = 0; s < 4; ++s)
-      D.x[s] = make_double4_32a((double)F.a[s].x + (double)F.a[s].w, (double)F.a[s].y + (double)F.b[s].x,
-                                (double)F.a[s].z + (double)F.b[s].y, 0.0);
-    Cof<double> d;
-    geometry(D, d);
-    for (int r = 0; r < 3; ++r)
-      for (int k = 0; k < 3; ++k) f.c[r][k] = (float)d.c[r][k];
-    f.det = (float)d.det;
-  }
+  fix_near_degenerate<float>(F.a, F.b, J, f);
 }
 
 // Double-word cofactors and determinant from double-word edge vectors.
@@ -323,6 +374,7 @@ __device__ __forceinline__ void geometry(const Fetch<kDW>& F, Cof<ff>& f)
     for (int k = 0; k < 3; ++k)
       J[r][k] = dw_diff2(vhi(F.a[k + 1], r), vhi(F.a[0], r), vlo(F.a[k + 1], F.b[k + 1], r), vlo(F.a[0], F.b[0], r));
   dw_cofactors(J, f);
+  fix_near_degenerate<ff>(F.a, F.b, J, f);
 }
 
 // Double-word, absolute coordinates x = hi + mid + lo exactly (the adjoint
@@ -337,6 +389,19 @@ __device__ __forceinline__ ff dw_diff3(float hb, float ha, float mb, float ma, f
   return two_sum(s.hi, t);
 }
 
+// near-degenerate elements: FP64 geometry from the mesh's FP64 coordinates
+static __device__ __noinline__ void recompute_fp64_abs(const GeoPtrs& g, int4 n, Cof<ff>& f)
+{
+  Fetch<kF64> D;
+  const int id[4] = {n.x, n.y, n.z, n.w};
+  for (int s = 0; s < 4; ++s) D.x[s] = g.xyz[id[s]];
+  Cof<double> d;
+  geometry(D, d);
+  for (int r = 0; r < 3; ++r)
+    for (int k = 0; k < 3; ++k) f.c[r][k] = ff_from_double_bits(d.c[r][k]);
+  f.det = ff_from_double_bits(d.det);
+}
+
 __device__ __forceinline__ void geometry_abs(const GeoPtrs& g, int4 n, Cof<ff>& f)
 {
   FetchAbs F;
@@ -349,6 +414,7 @@ __device__ __forceinline__ void geometry_abs(const GeoPtrs& g, int4 n, Cof<ff>& 
       J[r][k] = dw_diff3(rec_hi(F.a[k + 1], r), rec_hi(F.a[0], r), rec_mid(F.a[k + 1], F.b[k + 1], r),
                          rec_mid(F.a[0], F.b[0], r), rec_lo(F.b[k + 1], F.lz[k + 1], r), rec_lo(F.b[0], F.lz[0], r));
   dw_cofactors(J, f);
+  if (det_cancels<ff>(J, f)) recompute_fp64_abs(g, n, f);
 }
 
 // ------------------------------------------------------- element matrices --

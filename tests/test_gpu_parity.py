@@ -80,6 +80,32 @@ def test_p2_assembly_f32():
     assert row_scaled_err(rp, ref, vals) <= 2 * F32_TOL
 
 
+@pytest.mark.parametrize("case", ["jitter_s5", "jitter_s6", "jitter_s7", "sliver_1e-2", "sliver_1e-3", "sliver_1e-4"])
+def test_near_degenerate_elements(case):
+    """Elements whose determinant cancels in its cofactor expansion (Kuhn cubes
+    jittered by 0.49 h, cancellation up to ~230; single slivers of relative height
+    1e-2..1e-4 in a rotated plane): those elements take the FP64 geometry path, so
+    the double-word values keep FP64 parity and the FP32 values stay accurate."""
+    if case.startswith("jitter"):
+        seed = int(case[-1])
+        m = meshgen.kuhn_cube(8, jitter=0.49, seed=seed, permute=True)
+        xyz, conn, kappa = m.xyz, m.conn, meshgen.lognormal(len(m.conn), 1.0, seed)
+    else:
+        eps = float(case.split("_")[1])
+        Q, _ = np.linalg.qr(np.random.default_rng(1).standard_normal((3, 3)))
+        base = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0.3, 0.3, eps]], dtype=np.float64)
+        xyz = 0.37 + 0.1 * base @ Q.T
+        d = np.linalg.det(np.stack([xyz[k] - xyz[0] for k in (1, 2, 3)], axis=1))
+        conn = np.array([[0, 1, 2, 3]] if d > 0 else [[0, 2, 1, 3]], dtype=np.int32)
+        kappa = np.ones(1)
+    b = mg.MatrixBuilder(mg.Mesh(xyz, conn, order=1))
+    _, rp, ci, ref = orc.full_operator("stiff_kappa", 1, 4, xyz, conn, coeff=kappa)
+    v64 = b.assemble("stiff_kappa", coeff=kappa, quad=4, prec="f64").cpu().numpy()
+    v32 = b.assemble("stiff_kappa", coeff=kappa, quad=4, prec="f32").cpu().numpy()
+    assert row_scaled_err(rp, ref, v64) <= F64_TOL
+    assert row_scaled_err(rp, ref, v32) <= 1e-5
+
+
 def test_assembly_deterministic_and_host_entry():
     m, kappa = _case(8, 0.25, 3, True, 1.5)
     b = mg.MatrixBuilder(mg.Mesh(m.xyz, m.conn, order=1))
