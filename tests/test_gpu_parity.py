@@ -512,6 +512,32 @@ def test_gmsh_loaded_mesh_assembles(tmp_path):
     assert row_scaled_err(rp, ref, vals) <= F64_TOL
 
 
+@pytest.mark.parametrize("order,rule", [(1, "lex"), (2, "lex"), (2, "first")])
+def test_reference_fixture_mignon3dC(order, rule):
+    """The reference's own unit-test cases on its mignon3dC.msh fixture (7 nodes,
+    8 tets; tests/morganaIntegrator/integratorOEL3d_STDTest1.cpp: opEL3dA with
+    kappa = 12, tests/morganaFiniteElements/localMatrixEL3dTest1.cpp: kappa = 1),
+    loaded through the Gmsh reader and assembled on the GPU with every quadrature
+    card and operator, against the oracle."""
+    import json
+    import os
+    g = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "mignon3dC.json")))
+    xyz = np.array(g["nodes"], dtype=np.float64)
+    conn = np.array(g["tets_1based"], dtype=np.int32) - 1
+    mesh = mg.Mesh(xyz, conn, order=order, edge_rule=rule)
+    b = mg.MatrixBuilder(mesh)
+    for op, coef in (("stiff_kappa", 12.0), ("stiff_kappa", 1.0), ("stiff_const", 12.0), ("mass", 1.0),
+                     ("mass_coeff", 12.0)):
+        kappa = np.full(len(conn), coef)
+        for quad in (1, 4, 15, 64):
+            dofs, rp, ci, ref = orc.full_operator(op, order, quad, xyz, conn, coeff=kappa, c=coef, edge_rule=rule)
+            assert np.array_equal(mesh.elem_dofs(), dofs)
+            rph, cih = b.pattern()
+            assert np.array_equal(rph, rp) and np.array_equal(cih, ci)
+            vals = b.assemble(op, coeff=kappa, c=coef, quad=quad, prec="f64").cpu().numpy()
+            assert row_scaled_err(rp, ref, vals) <= F64_TOL, (op, coef, quad)
+
+
 def test_single_tet_and_empty():
     xyz = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], dtype=np.float64)
     b = mg.MatrixBuilder(mg.Mesh(xyz, np.array([[0, 1, 2, 3]], dtype=np.int32)))
