@@ -253,6 +253,7 @@ mg_status build_pattern_device(mg_plan* p, cudaStream_t st)
   int64_t nnz = 0;
   MG_CUDA(cudaMemcpyAsync(&nnz, d.count, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
   MG_CUDA(cudaStreamSynchronize(st));
+  if (nnz >= INT32_MAX) return set_error(MG_ERR_SIZE, "nnz above 2^31-1");
   MG_CUDA(cudaMalloc(&d.rowptr, sizeof(int32_t) * (nd + 1)));
   MG_CUDA(cudaMalloc(&d.colind, sizeof(int32_t) * std::max<int64_t>(nnz, 1)));
   k_pattern_rows<<<(int)((nd + 1 + threads - 1) / threads), threads, 0, st>>>(nd, nnz, d.a, d.rowptr);

@@ -774,9 +774,24 @@ mg_status plan_rhs_map(mg_plan* p)
   }
 #pragma omp parallel for schedule(dynamic, 1024)
   for (int64_t d = 0; d < nd; ++d) std::sort(slot.begin() + ptr[d], slot.begin() + ptr[d + 1]);
-  MG_TRY(upload(&p->d_rhs_ptr, ptr));
-  MG_TRY(upload(&p->d_rhs_slot, slot));
-  MG_CUDA(cudaMalloc(&p->d_rhs_y, sizeof(double) * std::max<int64_t>(pairs, 1)));
+  // all three buffers or none (the map counts as built once d_rhs_ptr is set)
+  int32_t *d_ptr = nullptr, *d_slot = nullptr;
+  double* d_y = nullptr;
+  mg_status st = upload(&d_ptr, ptr);
+  if (st == MG_OK) st = upload(&d_slot, slot);
+  if (st == MG_OK) {
+    const cudaError_t e = cudaMalloc(&d_y, sizeof(double) * std::max<int64_t>(pairs, 1));
+    if (e != cudaSuccess) st = cuda_error(e, "load-vector buffer");
+  }
+  if (st != MG_OK) {
+    cudaFree(d_ptr);
+    cudaFree(d_slot);
+    cudaFree(d_y);
+    return st;
+  }
+  p->d_rhs_ptr = d_ptr;
+  p->d_rhs_slot = d_slot;
+  p->d_rhs_y = d_y;
   return MG_OK;
 }
 
