@@ -311,25 +311,10 @@ __device__ __forceinline__ void store_geometry(const Cof<double>& d, Cof<ff>& f)
     for (int k = 0; k < 3; ++k) f.c[r][k] = ff_from_double_bits(d.c[r][k]);
   f.det = ff_from_double_bits(d.det);
 }
-// The FP64 recompute of the lanes that need it, entered only when one lane of
-// the warp does (a warp-uniform branch around a large block: not if-converted,
-// no call and no stack frame on the common path).
-template <typename T>
-__device__ __forceinline__ void fix_near_degenerate(const float4* a, const float2* b, const T J[3][3], Cof<T>& f)
-{
-  const bool need = det_cancels<T>(J, f);
-  if (__any_sync(__activemask(), need)) {
-    if (need) {
-      Cof<double> d;
-      geometry_fp64_staged(a, b, d);
-      store_geometry(d, f);
-    }
-  }
-}
-
 // FP32: edge vectors (hi_k - hi_0) + (lo_k - lo_0) of the chunk-relative
 // coordinates, accurate to a few float ulps of the edge itself.
-__device__ __forceinline__ void geometry(const Fetch<kF32>& F, Cof<float>& f)
+// Returns whether the element needs the FP64 geometry (det_cancels).
+__device__ __forceinline__ bool geometry(const Fetch<kF32>& F, Cof<float>& f)
 {
   float J[3][3];
 #pragma unroll
@@ -338,7 +323,7 @@ __device__ __forceinline__ void geometry(const Fetch<kF32>& F, Cof<float>& f)
     for (int k = 0; k < 3; ++k)
       J[r][k] = (vhi(F.a[k + 1], r) - vhi(F.a[0], r)) + (vlo(F.a[k + 1], F.b[k + 1], r) - vlo(F.a[0], F.b[0], r));
   cofactors<float>(J, f);
-  fix_near_degenerate<float>(F.a, F.b, J, f);
+  return det_cancels<float>(J, f);
 }
 
 // Double-word cofactors and determinant from double-word edge vectors.
@@ -365,7 +350,7 @@ __device__ __forceinline__ ff dw_diff2(float hb, float ha, float lb, float la)
   return two_sum(s1.hi, __fadd_rn(s1.lo, __fsub_rn(lb, la)));
 }
 
-__device__ __forceinline__ void geometry(const Fetch<kDW>& F, Cof<ff>& f)
+__device__ __forceinline__ bool geometry(const Fetch<kDW>& F, Cof<ff>& f)
 {
   ff J[3][3];
 #pragma unroll
@@ -374,7 +359,7 @@ __device__ __forceinline__ void geometry(const Fetch<kDW>& F, Cof<ff>& f)
     for (int k = 0; k < 3; ++k)
       J[r][k] = dw_diff2(vhi(F.a[k + 1], r), vhi(F.a[0], r), vlo(F.a[k + 1], F.b[k + 1], r), vlo(F.a[0], F.b[0], r));
   dw_cofactors(J, f);
-  fix_near_degenerate<ff>(F.a, F.b, J, f);
+  return det_cancels<ff>(J, f);
 }
 
 // Double-word, absolute coordinates x = hi + mid + lo exactly (the adjoint
@@ -803,7 +788,23 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
           const float2* vb = reinterpret_cast<const float2*>(rb + sizeof(ChunkDesc) + 12 * n4 + 16 * nn);
           Fetch<MODE> F;
           fetch_staged<MODE>(va, vb, lc, F);
-          geometry(F, f);
+          if constexpr (MODE == kF64) {
+            geometry(F, f);
+          } else {
+            const bool need = geometry(F, f);
+            // near-degenerate elements: FP64 geometry from the staged coordinates
+            // (re-read from shared memory, so the coordinates need not stay live),
+            // entered only when a lane of the warp needs it
+            if (__any_sync(__activemask(), need)) {
+              if (need) {
+                Fetch<kF64> D;
+                fetch_staged<kF64>(va, vb, lc, D);
+                Cof<double> d;
+                geometry(D, d);
+                store_geometry(d, f);
+              }
+            }
+          }
           coef = A::from(coef_d);
           // NaN / Inf coefficient: recorded for mg_plan_status (checked after the
           // geometry, where the load has long landed)
