@@ -1,0 +1,35 @@
+// Test double of the Epetra_FECrsMatrix surface the adapter uses (not
+// Trilinos): records the inserted rows so a test can compare them.
+#pragma once
+#include <map>
+#include <utility>
+#include <vector>
+#include "Epetra_Map.h"
+enum Epetra_DataAccess { Copy, View };
+class Epetra_FECrsMatrix {
+ public:
+  Epetra_FECrsMatrix(Epetra_DataAccess, const Epetra_Map& rowMap, int* numEntriesPerRow)
+      : map_(rowMap), alloc_(numEntriesPerRow, numEntriesPerRow + rowMap.NumMyElements())
+  {
+  }
+  int InsertGlobalValues(int globalRow, int numEntries, double* values, int* indices)
+  {
+    if (filled_ || globalRow < 0 || globalRow >= map_.NumGlobalElements()) return -1;
+    if (numEntries > alloc_[globalRow]) return 1;  // Epetra returns a positive code when it had to grow
+    auto& row = rows_[globalRow];
+    for (int k = 0; k < numEntries; ++k) row.emplace_back(indices[k], values[k]);
+    return 0;
+  }
+  int GlobalAssemble(bool callFillComplete = true)
+  {
+    filled_ = callFillComplete;
+    return 0;
+  }
+  bool Filled() const { return filled_; }
+  const std::map<int, std::vector<std::pair<int, double>>>& Rows() const { return rows_; }
+ private:
+  const Epetra_Map& map_;
+  std::vector<int> alloc_;
+  std::map<int, std::vector<std::pair<int, double>>> rows_;
+  bool filled_ = false;
+};
