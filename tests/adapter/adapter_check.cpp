@@ -1,7 +1,9 @@
-// Drives the Epetra adapter (include/morgana_gpu_epetra.hpp) against the test
-// doubles in mock_trilinos/: reads a mesh and coefficients written by the test,
-// builds the operator through mg_epetra::buildEpetraCrs and applies it through
-// mg_epetra::GpuCrsOperator, and writes what the Epetra side received.
+// Drives the Epetra and Tpetra adapters (include/morgana_gpu_epetra.hpp,
+// include/morgana_gpu_tpetra.hpp) against the test doubles in mock_trilinos/:
+// reads a mesh and coefficients written by the test, builds the operator through
+// mg_epetra::buildEpetraCrs (and checks mg_tpetra::buildTpetraCrs inserts the
+// same rows), applies it through mg_epetra::GpuCrsOperator, and writes what the
+// Epetra side received.
 //   adapter_check in.bin out.bin
 // in.bin : int64 n_nodes, int64 n_elem, int64 order, double xyz[3 n_nodes],
 //          int32 conn[4 n_elem], double kappa[n_elem], double x[ndof]
@@ -12,6 +14,7 @@
 #include <vector>
 
 #include "morgana_gpu_epetra.hpp"
+#include "morgana_gpu_tpetra.hpp"
 
 template <typename T>
 static void rd(FILE* f, T* p, size_t n)
@@ -48,6 +51,19 @@ int main(int argc, char** argv)
     Teuchos::RCP<Epetra_FECrsMatrix> A =
         mg_epetra::buildEpetraCrs(plan, MG_OP_STIFF_KAPPA, kappa.data(), 1.0, MG_QUAD_4, comm);
     if (!A->Filled()) return 4;
+
+    // the Tpetra build inserts the same rows
+    Teuchos::RCP<const Teuchos::Comm<int>> tcomm = Teuchos::rcp(new Teuchos::Comm<int>());
+    Teuchos::RCP<mg_tpetra::crs_type> T =
+        mg_tpetra::buildTpetraCrs(plan, MG_OP_STIFF_KAPPA, kappa.data(), 1.0, MG_QUAD_4, tcomm);
+    if (!T->isFillComplete() || T->Rows().size() != A->Rows().size()) return 9;
+    for (const auto& row : A->Rows()) {
+      auto it = T->Rows().find((long long)row.first);
+      if (it == T->Rows().end() || it->second.size() != row.second.size()) return 9;
+      for (size_t k = 0; k < row.second.size(); ++k)
+        if ((long long)row.second[k].first != it->second[k].first || row.second[k].second != it->second[k].second)
+          return 9;
+    }
 
     // the same operator on the device behind the Epetra_Operator seam
     double* dvals = nullptr;

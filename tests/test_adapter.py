@@ -1,7 +1,8 @@
-"""The Epetra drop-in adapter (include/morgana_gpu_epetra.hpp) compiled against
-test doubles of the Trilinos classes it touches (tests/adapter/mock_trilinos):
-on CPU that it compiles; on the GPU that the operator it hands to the Epetra
-side (rows inserted into the Epetra_FECrsMatrix, Apply through the
+"""The Epetra and Tpetra drop-in adapters (include/morgana_gpu_epetra.hpp,
+include/morgana_gpu_tpetra.hpp) compiled against test doubles of the Trilinos
+classes they touch (tests/adapter/mock_trilinos): on CPU that they compile; on
+the GPU that the operator they hand to the Trilinos side (rows inserted into the
+Epetra_FECrsMatrix, the same rows into the Tpetra::CrsMatrix, Apply through the
 Epetra_Operator seam) is the oracle's."""
 import os
 import subprocess
