@@ -314,6 +314,86 @@ mg_status mg_cg_solve_noalloc(mg_plan* plan, const double* d_values, const doubl
 mg_status mg_adjoint_grad(mg_plan* plan, const double* d_u, const double* d_lambda, int32_t quad,
                           double* d_grad, void* stream);
 
+/* ------------------------------------------- boundary multipliers -- */
+
+/* Dirichlet data the reference way: P1 Lagrange multipliers on boundary
+   triangles, coupled to the field by opLA3dA (u . q over each boundary face),
+   and the saddle system [K B^T; B 0].  FP64 throughout: the boundary work is
+   O(n^2) against the O(n^3) of the volume operator. */
+typedef struct mg_lagrange mg_lagrange;
+
+/* Triangle quadrature cards of the face operator, by point count: the
+   reference's STANDARD linearTriangle cards of precision 1..4
+   (src/morganaIntegrator/intStaticCards.cpp:176-300). */
+enum { MG_FACE_QUAD_1 = 1, MG_FACE_QUAD_3 = 3, MG_FACE_QUAD_4 = 4, MG_FACE_QUAD_6 = 6 };
+
+typedef struct {
+  int64_t n_faces;        /* boundary faces carrying multipliers */
+  int64_t n_multipliers;  /* rows of B */
+  int64_t ndof;           /* columns of B (the plan's field dofs) */
+  int64_t nnz_b;
+  int64_t nnz_saddle;     /* (ndof + n_multipliers) rows */
+} mg_lagrange_info;
+
+/* Multiplier space and patterns, on the host (no device needed).
+   Boundary faces = faces of exactly one tet (connect3d::getFaceIsBoundary),
+   in element then local-face order.  h_tris (n_tris x 3 node ids, any vertex
+   order) selects the boundary triangles that carry multipliers, the geoId
+   filter of the test field (feStaticField2d with dms2d_geoIdMode); NULL = all
+   boundary faces.  Multipliers = the P1 dofs of the selected triangles, one per
+   node, numbered by ascending node id (meshDoctor2d::removeUnusedPoints,
+   src/morganaGeometry/meshDoctor2d.hpp:339-500, then dofMapStatic2d).
+   B (n_multipliers x ndof): each face inserts its full 3 x nb block, explicit
+   zeros included, as traitsMatrixBuilder::buildEpetraCrs does for
+   localMatrixLA3d (src/morganaFiniteElements/localMatrixLA3d.hpp:292-322).
+   Saddle: [K B^T; B 0] (epetraSaddleAssembler::setDiagMatrix + setSymmMatrix,
+   src/morganaTrilinos/epetraSaddleAssembler.cpp), with K the plan's pattern;
+   lam_diag != 0 adds the diagonal of the multiplier block to the pattern
+   (setEye on that block).
+   Errors: MG_ERR_BAD_MESH when a face belongs to more than two tets or a
+   selected triangle is not a boundary face; MG_ERR_INVALID_ARG for a repeated
+   triangle or a node id out of range; MG_ERR_SIZE above 2^31 - 1 entries.
+   The handle keeps a pointer to the plan: destroy it before the plan. */
+mg_status mg_lagrange_build(mg_plan* plan, int64_t n_tris, const int32_t* h_tris, int32_t lam_diag,
+                            mg_lagrange** out);
+mg_status mg_lagrange_destroy(mg_lagrange* lg);
+mg_status mg_lagrange_get_info(const mg_lagrange* lg, mg_lagrange_info* info);
+/* h_lam_node (n_multipliers): node of each multiplier; h_face_elem,
+   h_face_local (n_faces): the selected faces; any pointer may be NULL. */
+mg_status mg_lagrange_export(const mg_lagrange* lg, int32_t* h_lam_node, int32_t* h_face_elem,
+                             int32_t* h_face_local);
+/* CSR of B (n_multipliers + 1, nnz_b) and of the saddle matrix
+   (ndof + n_multipliers + 1, nnz_saddle); any pointer may be NULL. */
+mg_status mg_lagrange_pattern(const mg_lagrange* lg, int32_t* h_b_rowptr, int32_t* h_b_colind,
+                              int32_t* h_s_rowptr, int32_t* h_s_colind);
+
+/* The gather maps the kernels read (for host-side checks of the data flow):
+   h_b_src_ptr (nnz_b + 1) and h_b_src (n_faces * 3 * nb): B entry k sums the
+   face-matrix entries h_b_src[h_b_src_ptr[k] .. h_b_src_ptr[k+1]), each
+   (face * 3 + face vertex) * nb + basis, in that order; h_s_src (nnz_saddle):
+   saddle entry k copies K entry h_s_src[k] (>= 0), B entry -(h_s_src[k] + 1),
+   or the multiplier diagonal (INT32_MIN).  Any pointer may be NULL. */
+mg_status mg_lagrange_export_maps(const mg_lagrange* lg, int32_t* h_b_src_ptr, int32_t* h_b_src,
+                                  int32_t* h_s_src);
+
+/* Values of B (nnz_b doubles, device) with the face card quad (MG_FACE_QUAD_*):
+   one thread per face computes its 3 x nb block, then one thread per entry of
+   B sums its blocks' contributions in the reference's insertion order
+   (deterministic, no atomics). */
+mg_status mg_lagrange_assemble(mg_lagrange* lg, int32_t quad, double* d_b_values, void* stream);
+/* Saddle values (nnz_saddle doubles, device) from K's values (the plan's CSR)
+   and B's: [K + eye_field I, B^T; B, eye_lam I].  eye_lam must be 0 unless the
+   pattern has the multiplier diagonal (lam_diag). */
+mg_status mg_saddle_assemble(mg_lagrange* lg, const double* d_k_values, const double* d_b_values,
+                             double eye_field, double eye_lam, double* d_values, void* stream);
+/* y = S x on the saddle matrix (ndof + n_multipliers doubles each). */
+mg_status mg_saddle_spmv(mg_lagrange* lg, const double* d_values, const double* d_x, double* d_y,
+                         void* stream);
+/* g = B u (u: ndof doubles, g: n_multipliers doubles): the constraint right-hand
+   side of nodal Dirichlet data u. */
+mg_status mg_lagrange_apply(mg_lagrange* lg, const double* d_b_values, const double* d_u, double* d_g,
+                            void* stream);
+
 /* -------------------------------------------------------------- status -- */
 const char* mg_status_string(mg_status status);
 const char* mg_last_error(void);

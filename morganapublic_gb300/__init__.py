@@ -72,6 +72,11 @@ class ScheduleInfo(ctypes.Structure):
 _P = ctypes.c_void_p
 _I32, _I64, _D = ctypes.c_int32, ctypes.c_int64, ctypes.c_double
 # name -> argtypes; every function returns mg_status (int) unless listed in _RESTYPES
+class LagrangeInfo(ctypes.Structure):
+    _fields_ = [("n_faces", _I64), ("n_multipliers", _I64), ("ndof", _I64), ("nnz_b", _I64),
+                ("nnz_saddle", _I64)]
+
+
 SIGNATURES = {
     "mg_mesh_create": [ctypes.POINTER(_P), _I64, _P, _I64, _P, _I32, _I32],
     "mg_mesh_create_device": [ctypes.POINTER(_P), _I64, _P, _I64, _P, _I32, _I32, _P],
@@ -99,6 +104,16 @@ SIGNATURES = {
     "mg_cg_refined": [_P, _P, _P, _P, _P, _D, _I32, _I32, _D, _I32, ctypes.POINTER(CgInfo), _P],
     "mg_cg_solve_noalloc": [_P, _P, _P, _P, _D, _I32, _I32, ctypes.POINTER(CgInfo), _P],
     "mg_adjoint_grad": [_P, _P, _P, _I32, _P, _P],
+    "mg_lagrange_build": [_P, _I64, _P, _I32, ctypes.POINTER(_P)],
+    "mg_lagrange_destroy": [_P],
+    "mg_lagrange_get_info": [_P, ctypes.POINTER(LagrangeInfo)],
+    "mg_lagrange_export": [_P, _P, _P, _P],
+    "mg_lagrange_pattern": [_P, _P, _P, _P, _P],
+    "mg_lagrange_export_maps": [_P, _P, _P, _P],
+    "mg_lagrange_assemble": [_P, _I32, _P, _P],
+    "mg_saddle_assemble": [_P, _P, _P, _D, _D, _P, _P],
+    "mg_saddle_spmv": [_P, _P, _P, _P, _P],
+    "mg_lagrange_apply": [_P, _P, _P, _P, _P],
     "mg_status_string": [_I32],
     "mg_last_error": [],
     "mg_version": [],
@@ -383,6 +398,123 @@ class MatrixBuilder:
     def close(self):
         if getattr(self, "_h", None):
             lib().mg_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class LagrangeBuilder:
+    """Dirichlet data the reference way (mg_lagrange): P1 multipliers on the
+    boundary triangles, B = opLA3dA (multiplier x field) and the saddle matrix
+    [K B^T; B 0] of epetraSaddleAssembler.  Keeps a reference to its
+    MatrixBuilder, whose plan must outlive it."""
+
+    def __init__(self, builder: MatrixBuilder, tris=None, lam_diag: bool = False):
+        """tris: (k, 3) node ids of the boundary triangles that carry multipliers
+        (the test field's geoId filter); None = every boundary face."""
+        self.builder = builder
+        t = None if tris is None else np.ascontiguousarray(tris, dtype=np.int32).reshape(-1, 3)
+        h = _P()
+        _check(lib().mg_lagrange_build(builder._h, 0 if t is None else t.shape[0], _ptr(t), int(lam_diag),
+                                       ctypes.byref(h)), "mg_lagrange_build")
+        self._h = h
+        info = LagrangeInfo()
+        _check(lib().mg_lagrange_get_info(h, ctypes.byref(info)), "mg_lagrange_get_info")
+        self.n_faces, self.n_multipliers = info.n_faces, info.n_multipliers
+        self.ndof, self.nnz_b, self.nnz_saddle = info.ndof, info.nnz_b, info.nnz_saddle
+
+    def multipliers(self):
+        """(node of each multiplier, face element, face local index)."""
+        lam = np.empty(self.n_multipliers, dtype=np.int32)
+        fe = np.empty(self.n_faces, dtype=np.int32)
+        fl = np.empty(self.n_faces, dtype=np.int32)
+        _check(lib().mg_lagrange_export(self._h, _ptr(lam), _ptr(fe), _ptr(fl)), "mg_lagrange_export")
+        return lam, fe, fl
+
+    def pattern(self):
+        """((B rowptr, colind), (saddle rowptr, colind))."""
+        brp = np.empty(self.n_multipliers + 1, dtype=np.int32)
+        bci = np.empty(self.nnz_b, dtype=np.int32)
+        srp = np.empty(self.ndof + self.n_multipliers + 1, dtype=np.int32)
+        sci = np.empty(self.nnz_saddle, dtype=np.int32)
+        _check(lib().mg_lagrange_pattern(self._h, _ptr(brp), _ptr(bci), _ptr(srp), _ptr(sci)),
+               "mg_lagrange_pattern")
+        return (brp, bci), (srp, sci)
+
+    def export_maps(self):
+        """(b_src_ptr, b_src, s_src): the gather maps of the B and saddle kernels."""
+        nb = 4 if self.builder.mesh.order == 1 else 10
+        bp = np.empty(self.nnz_b + 1, dtype=np.int32)
+        bs = np.empty(self.n_faces * 3 * nb, dtype=np.int32)
+        ss = np.empty(self.nnz_saddle, dtype=np.int32)
+        _check(lib().mg_lagrange_export_maps(self._h, _ptr(bp), _ptr(bs), _ptr(ss)), "mg_lagrange_export_maps")
+        return bp, bs, ss
+
+    def assemble(self, quad: int = 1, out=None, stream=None):
+        """Values of B (torch float64, nnz_b) with the face card quad (1, 3, 4, 6)."""
+        torch = _torch()
+        if out is not None:
+            self._need(out, self.nnz_b, "out")
+        if out is None:
+            out = torch.empty(self.nnz_b, dtype=torch.float64, device="cuda")
+        _check(lib().mg_lagrange_assemble(self._h, quad, _ptr(out), _stream_ptr(stream)), "mg_lagrange_assemble")
+        return out
+
+    @staticmethod
+    def _need(t, n, what):
+        torch = _torch()
+        if t is None or not isinstance(t, torch.Tensor) or t.dtype != torch.float64 or not t.is_cuda \
+                or t.numel() < n or not t.is_contiguous():
+            raise ValueError(f"{what}: a contiguous float64 CUDA tensor of at least {n} entries is needed")
+
+    def saddle(self, k_values, b_values, eye_field: float = 0.0, eye_lam: float = 0.0, out=None, stream=None):
+        """Values of [K + eye_field I, B^T; B, eye_lam I] (torch float64, nnz_saddle)."""
+        torch = _torch()
+        self._need(k_values, self.builder.nnz, "K values")
+        if self.nnz_b:
+            self._need(b_values, self.nnz_b, "B values")
+        if out is not None:
+            self._need(out, self.nnz_saddle, "out")
+        if out is None:
+            out = torch.empty(self.nnz_saddle, dtype=torch.float64, device="cuda")
+        _check(lib().mg_saddle_assemble(self._h, _ptr(k_values), _ptr(b_values), float(eye_field), float(eye_lam),
+                                        _ptr(out), _stream_ptr(stream)), "mg_saddle_assemble")
+        return out
+
+    def saddle_apply(self, values, x, out=None, stream=None):
+        torch = _torch()
+        n = self.ndof + self.n_multipliers
+        self._need(values, self.nnz_saddle, "saddle values")
+        self._need(x, n, "x")
+        if out is not None:
+            self._need(out, n, "out")
+        if out is None:
+            out = torch.empty(self.ndof + self.n_multipliers, dtype=torch.float64, device="cuda")
+        _check(lib().mg_saddle_spmv(self._h, _ptr(values), _ptr(x), _ptr(out), _stream_ptr(stream)),
+               "mg_saddle_spmv")
+        return out
+
+    def apply(self, b_values, u, out=None, stream=None):
+        """g = B u: the constraint right-hand side of nodal data u."""
+        torch = _torch()
+        if self.nnz_b:
+            self._need(b_values, self.nnz_b, "B values")
+        self._need(u, self.ndof, "u")
+        if out is not None:
+            self._need(out, self.n_multipliers, "out")
+        if out is None:
+            out = torch.empty(self.n_multipliers, dtype=torch.float64, device="cuda")
+        _check(lib().mg_lagrange_apply(self._h, _ptr(b_values), _ptr(u), _ptr(out), _stream_ptr(stream)),
+               "mg_lagrange_apply")
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().mg_lagrange_destroy(self._h)
             self._h = None
 
     def __del__(self):

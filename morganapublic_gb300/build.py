@@ -23,8 +23,8 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["mg_assemble.cu", "mg_solve.cu", "mg_pattern.cu"]
-CPP_SOURCES = ["mg_mesh.cpp", "mg_plan.cpp"]
+CU_SOURCES = ["mg_assemble.cu", "mg_solve.cu", "mg_pattern.cu", "mg_lagrange.cu"]
+CPP_SOURCES = ["mg_mesh.cpp", "mg_plan.cpp", "mg_lagrange.cpp"]
 
 
 def _newer(src_paths, target):

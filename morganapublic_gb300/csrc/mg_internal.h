@@ -203,6 +203,29 @@ struct mg_plan {
   bool on_device = false;
 };
 
+// Boundary multipliers of a plan (opLA3dA) and the saddle pattern [K B^T; B 0].
+struct mg_lagrange {
+  mg_plan* plan = nullptr;
+  int order = 1, nb = 4;
+  bool lam_diag = false;  // the saddle pattern holds the multiplier block's diagonal
+  int64_t ndof = 0, n_faces = 0, nl = 0, nnz_b = 0, nnz_s = 0;
+  std::vector<int32_t> face_elem, face_local;  // selected boundary faces, element then local-face order
+  std::vector<int32_t> lam_node;               // node of each multiplier, ascending
+  std::vector<int32_t> b_rowptr, b_colind;     // B: nl x ndof
+  // per B entry k, the face-matrix entries it sums, b_src[b_src_ptr[k] .. b_src_ptr[k+1]),
+  // each (f * 3 + a) * nb + i, ascending (the reference's insertion order)
+  std::vector<int32_t> b_src_ptr, b_src;
+  std::vector<int32_t> s_rowptr, s_colind;     // saddle: (ndof + nl) rows
+  // per saddle entry: the K entry it copies (>= 0) or -(k + 1) for B entry k
+  std::vector<int32_t> s_src;
+  // device copies (uploaded on first GPU use)
+  int2* d_faces = nullptr;  // (element, local face)
+  int32_t *d_b_rowptr = nullptr, *d_b_colind = nullptr, *d_b_src_ptr = nullptr, *d_b_src = nullptr;
+  int32_t *d_s_rowptr = nullptr, *d_s_colind = nullptr, *d_s_src = nullptr;
+  double* d_face_mat = nullptr;  // n_faces * 3 * nb
+  bool on_device = false;
+};
+
 namespace mg {
 // Host copy of the assembly schedule, kept until the plan is first used on the GPU.
 struct HostSchedule {
@@ -231,4 +254,8 @@ mg_status ensure_edges(mg_mesh* m);
 mg_status launch_assemble(mg_plan* p, int op, const double* d_coeff, double c, int quad, int prec,
                           void* d_values, cudaStream_t st);
 mg_status launch_spmv(mg_plan* p, int prec, const void* vals, const void* x, void* y, cudaStream_t st);
+// y = A x for any CSR matrix of `rows` rows (FP64 values and vectors)
+mg_status launch_spmv_csr(int64_t rows, int64_t nnz, const int32_t* rowptr, const int32_t* colind,
+                          const double* vals, const double* x, double* y, cudaStream_t st);
+mg_status lagrange_device(mg_lagrange* lg);  // uploads the multiplier tables on first GPU use
 }  // namespace mg

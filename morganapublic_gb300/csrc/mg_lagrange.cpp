@@ -1,0 +1,376 @@
+// Boundary multipliers (host side): boundary faces, the P1 multiplier numbering,
+// the patterns of B = opLA3dA and of the saddle matrix [K B^T; B 0], and the
+// index maps the kernels of mg_lagrange.cu gather through.
+//
+// Reference behaviour restated here (paths relative to the morganaPublic tree):
+//  - boundary faces: faces of exactly one tet (connect3d getFaceIsBoundary),
+//    visited in element then local-face order (the builder's loop over grid3d,
+//    localMatrixLA3d::matrix, src/morganaFiniteElements/localMatrixLA3d.hpp:292-322);
+//  - multipliers: the nodes of the boundary triangles, compacted in ascending
+//    node id (meshDoctor2d::removeUnusedPoints, meshDoctor2d.hpp:339-500), one P1
+//    dof each;
+//  - B: every face inserts its 3 x nb block (rows: the face's multipliers,
+//    columns: all nb dofs of the tet, zeros kept), duplicates summed in insertion
+//    order (traitsMatrixBuilder.hpp:363-441, Epetra_FECrsMatrix::InsertGlobalValues);
+//  - saddle: K on the field block, B on (multiplier, field) and B^T on (field,
+//    multiplier) (epetraSaddleAssembler::setDiagMatrix / setSymmMatrix).
+#include <algorithm>
+#include <climits>
+#include <cstring>
+#include <new>
+#include <numeric>
+
+#include <omp.h>
+#include <parallel/algorithm>
+
+#include "mg_internal.h"
+#include "mg_lagrange.cuh"
+
+namespace mg {
+
+namespace {
+
+constexpr int64_t kInt32Max = 2147483647;
+
+struct Tri {
+  int32_t a, b, c;  // ascending
+  bool operator<(const Tri& o) const { return a != o.a ? a < o.a : (b != o.b ? b < o.b : c < o.c); }
+  bool operator==(const Tri& o) const { return a == o.a && b == o.b && c == o.c; }
+};
+
+Tri sorted_tri(int32_t x, int32_t y, int32_t z)
+{
+  if (x > y) std::swap(x, y);
+  if (y > z) std::swap(y, z);
+  if (x > y) std::swap(x, y);
+  return Tri{x, y, z};
+}
+
+// Flags every local face of every tet: 1 = boundary (one tet), 0 = interior
+// (two tets).  A face found in three or more tets makes the mesh invalid.
+mg_status boundary_flags(const mg_mesh* m, std::vector<uint8_t>* flag)
+{
+  const int64_t N = m->n_nodes, E = m->n_elem;
+  const int32_t* conn = m->conn.data();
+  // node -> incident elements (the order inside a node's list does not matter:
+  // only the number of other tets holding a face is used)
+  std::vector<int64_t> start(N + 1, 0);
+  for (int64_t k = 0; k < 4 * E; ++k) start[conn[k] + 1]++;
+  for (int64_t i = 0; i < N; ++i) start[i + 1] += start[i];
+  std::vector<int32_t> inc(4 * E);
+  {
+    std::vector<int64_t> fill(start.begin(), start.end() - 1);
+    for (int64_t e = 0; e < E; ++e)
+      for (int v = 0; v < 4; ++v) inc[fill[conn[4 * e + v]]++] = (int32_t)e;
+  }
+  flag->assign(4 * E, 0);
+  int bad = 0;
+#pragma omp parallel for schedule(static) reduction(| : bad)
+  for (int64_t e = 0; e < E; ++e) {
+    const int32_t* c = conn + 4 * e;
+    for (int lf = 0; lf < 4; ++lf) {
+      const int32_t x = c[face_vertex(lf, 0)], y = c[face_vertex(lf, 1)], z = c[face_vertex(lf, 2)];
+      int others = 0;
+      for (int64_t k = start[x]; k < start[x + 1]; ++k) {
+        const int32_t e2 = inc[k];
+        if (e2 == e) continue;
+        const int32_t* c2 = conn + 4 * (int64_t)e2;
+        bool hy = false, hz = false;
+        for (int v = 0; v < 4; ++v) {
+          hy |= c2[v] == y;
+          hz |= c2[v] == z;
+        }
+        others += (hy && hz) ? 1 : 0;
+      }
+      if (others >= 2) bad = 1;
+      (*flag)[4 * e + lf] = others == 0 ? 1 : 0;
+    }
+  }
+  if (bad) return set_error(MG_ERR_BAD_MESH, "mg_lagrange_build: a face is shared by more than two tets");
+  return MG_OK;
+}
+
+}  // namespace
+
+static mg_status build_lagrange(mg_lagrange* lg, int64_t n_tris, const int32_t* h_tris, bool lam_diag)
+{
+  const mg_plan* p = lg->plan;
+  const mg_mesh* m = p->mesh;
+  const int nb = m->nb;
+  const int64_t E = m->n_elem, N = m->n_nodes, nd = m->ndof;
+  lg->order = m->order;
+  lg->lam_diag = lam_diag;
+  lg->nb = nb;
+  lg->ndof = nd;
+  if (4 * E > kInt32Max) return set_error(MG_ERR_SIZE, "mg_lagrange_build: more than 2^29 tets");
+
+  // boundary faces, element then local-face order
+  std::vector<uint8_t> flag;
+  MG_TRY(boundary_flags(m, &flag));
+  std::vector<int32_t> ids;
+  for (int64_t k = 0; k < 4 * E; ++k)
+    if (flag[k]) ids.push_back((int32_t)k);
+
+  // selection by the given triangles
+  if (h_tris) {
+    std::vector<Tri> want(n_tris);
+    for (int64_t t = 0; t < n_tris; ++t) {
+      const int32_t* v = h_tris + 3 * t;
+      for (int s = 0; s < 3; ++s)
+        if (v[s] < 0 || v[s] >= N) return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_build: triangle node id out of range");
+      want[t] = sorted_tri(v[0], v[1], v[2]);
+    }
+    std::sort(want.begin(), want.end());
+    if (std::adjacent_find(want.begin(), want.end()) != want.end())
+      return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_build: a triangle is listed twice");
+    std::vector<int32_t> kept;
+    for (const int32_t id : ids) {
+      const int32_t* c = m->conn.data() + 4 * (int64_t)(id / 4);
+      const int lf = id % 4;
+      const Tri t = sorted_tri(c[face_vertex(lf, 0)], c[face_vertex(lf, 1)], c[face_vertex(lf, 2)]);
+      if (std::binary_search(want.begin(), want.end(), t)) kept.push_back(id);
+    }
+    if ((int64_t)kept.size() != n_tris)
+      return set_error(MG_ERR_BAD_MESH, "mg_lagrange_build: a listed triangle is not a boundary face of the mesh");
+    ids.swap(kept);
+  }
+  const int64_t nf = (int64_t)ids.size();
+  if (nf * 3 * nb > kInt32Max) return set_error(MG_ERR_SIZE, "mg_lagrange_build: too many boundary faces");
+  lg->n_faces = nf;
+  lg->face_elem.resize(nf);
+  lg->face_local.resize(nf);
+  for (int64_t f = 0; f < nf; ++f) {
+    lg->face_elem[f] = ids[f] / 4;
+    lg->face_local[f] = ids[f] % 4;
+  }
+
+  // multipliers: nodes of the selected faces, ascending
+  std::vector<int32_t> lam_of(N, -1);
+  for (int64_t f = 0; f < nf; ++f) {
+    const int32_t* c = m->conn.data() + 4 * (int64_t)lg->face_elem[f];
+    for (int a = 0; a < 3; ++a) lam_of[c[face_vertex(lg->face_local[f], a)]] = 0;
+  }
+  lg->lam_node.clear();
+  for (int64_t i = 0; i < N; ++i)
+    if (lam_of[i] == 0) {
+      lam_of[i] = (int32_t)lg->lam_node.size();
+      lg->lam_node.push_back((int32_t)i);
+    }
+  const int64_t nl = (int64_t)lg->lam_node.size();
+  lg->nl = nl;
+
+  // B: (row, column) of every face-matrix entry, sorted by (row, column, source);
+  // sources are generated ascending, so each entry's list is in insertion order
+  struct Pair {
+    uint64_t key;  // row << 32 | column
+    int32_t src;   // (f * 3 + a) * nb + i
+    bool operator<(const Pair& o) const { return key != o.key ? key < o.key : src < o.src; }
+  };
+  std::vector<Pair> pairs(nf * 3 * nb);
+#pragma omp parallel for schedule(static)
+  for (int64_t f = 0; f < nf; ++f) {
+    const int64_t e = lg->face_elem[f];
+    const int32_t* c = m->conn.data() + 4 * e;
+    for (int a = 0; a < 3; ++a) {
+      const uint64_t row = (uint64_t)lam_of[c[face_vertex(lg->face_local[f], a)]];
+      for (int i = 0; i < nb; ++i) {
+        const int64_t s = (f * 3 + a) * nb + i;
+        pairs[s] = Pair{row << 32 | (uint64_t)(uint32_t)m->dofs[e * nb + i], (int32_t)s};
+      }
+    }
+  }
+  __gnu_parallel::sort(pairs.begin(), pairs.end());
+  lg->b_rowptr.assign(nl + 1, 0);
+  lg->b_colind.clear();
+  lg->b_src_ptr.clear();
+  lg->b_src.resize(pairs.size());
+  for (size_t k = 0; k < pairs.size(); ++k) {
+    if (k == 0 || pairs[k].key != pairs[k - 1].key) {
+      lg->b_src_ptr.push_back((int32_t)k);
+      lg->b_colind.push_back((int32_t)(pairs[k].key & 0xffffffffu));
+      lg->b_rowptr[(pairs[k].key >> 32) + 1]++;
+    }
+    lg->b_src[k] = pairs[k].src;
+  }
+  lg->b_src_ptr.push_back((int32_t)pairs.size());
+  for (int64_t l = 0; l < nl; ++l) lg->b_rowptr[l + 1] += lg->b_rowptr[l];
+  lg->nnz_b = (int64_t)lg->b_colind.size();
+
+  // saddle: rows r < nd hold K's row then B^T's (columns nd + l, ascending l);
+  // rows nd + l hold B's row l (columns < nd), then the diagonal if requested
+  const int64_t nk = p->nnz;
+  const int64_t ns = nk + 2 * lg->nnz_b + (lam_diag ? nl : 0);
+  if (ns > kInt32Max || nd + nl > kInt32Max)
+    return set_error(MG_ERR_SIZE, "mg_lagrange_build: the saddle matrix has more than 2^31 - 1 entries");
+  std::vector<int32_t> tcnt(nd + 1, 0);
+  for (int64_t k = 0; k < lg->nnz_b; ++k) tcnt[lg->b_colind[k] + 1]++;
+  for (int64_t r = 0; r < nd; ++r) tcnt[r + 1] += tcnt[r];
+  lg->s_rowptr.assign(nd + nl + 1, 0);
+  for (int64_t r = 0; r < nd; ++r)
+    lg->s_rowptr[r + 1] = lg->s_rowptr[r] + (p->rowptr[r + 1] - p->rowptr[r]) + (tcnt[r + 1] - tcnt[r]);
+  for (int64_t l = 0; l < nl; ++l)
+    lg->s_rowptr[nd + l + 1] = lg->s_rowptr[nd + l] + (lg->b_rowptr[l + 1] - lg->b_rowptr[l]) + (lam_diag ? 1 : 0);
+  lg->nnz_s = lg->s_rowptr[nd + nl];
+  lg->s_colind.resize(ns);
+  lg->s_src.resize(ns);
+  std::vector<int32_t> tfill(nd);
+#pragma omp parallel for schedule(static)
+  for (int64_t r = 0; r < nd; ++r) {  // K part
+    int32_t s = lg->s_rowptr[r];
+    for (int32_t k = p->rowptr[r]; k < p->rowptr[r + 1]; ++k, ++s) {
+      lg->s_colind[s] = p->colind[k];
+      lg->s_src[s] = k;
+    }
+    tfill[r] = s;
+  }
+  for (int64_t l = 0; l < nl; ++l)  // B^T part: rows visited in ascending l
+    for (int32_t k = lg->b_rowptr[l]; k < lg->b_rowptr[l + 1]; ++k) {
+      const int32_t s = tfill[lg->b_colind[k]]++;
+      lg->s_colind[s] = (int32_t)(nd + l);
+      lg->s_src[s] = -(k + 1);
+    }
+#pragma omp parallel for schedule(static)
+  for (int64_t l = 0; l < nl; ++l) {  // B part (+ diagonal)
+    int32_t s = lg->s_rowptr[nd + l];
+    for (int32_t k = lg->b_rowptr[l]; k < lg->b_rowptr[l + 1]; ++k, ++s) {
+      lg->s_colind[s] = lg->b_colind[k];
+      lg->s_src[s] = -(k + 1);
+    }
+    if (lam_diag) {
+      lg->s_colind[s] = (int32_t)(nd + l);
+      lg->s_src[s] = INT32_MIN;  // filled with eye_lam
+    }
+  }
+  return MG_OK;
+}
+
+template <typename T>
+static mg_status upload(T** d, const std::vector<T>& h)
+{
+  MG_CUDA(cudaMalloc(d, sizeof(T) * std::max<size_t>(h.size(), 1)));
+  if (!h.empty()) MG_CUDA(cudaMemcpy(*d, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice));
+  return MG_OK;
+}
+
+static void free_device(mg_lagrange* lg)
+{
+  cudaFree(lg->d_faces);
+  cudaFree(lg->d_b_rowptr);
+  cudaFree(lg->d_b_colind);
+  cudaFree(lg->d_b_src_ptr);
+  cudaFree(lg->d_b_src);
+  cudaFree(lg->d_s_rowptr);
+  cudaFree(lg->d_s_colind);
+  cudaFree(lg->d_s_src);
+  cudaFree(lg->d_face_mat);
+  lg->d_faces = nullptr;
+  lg->d_b_rowptr = lg->d_b_colind = lg->d_b_src_ptr = lg->d_b_src = nullptr;
+  lg->d_s_rowptr = lg->d_s_colind = lg->d_s_src = nullptr;
+  lg->d_face_mat = nullptr;
+  lg->on_device = false;
+}
+
+mg_status lagrange_device(mg_lagrange* lg)
+{
+  if (lg->on_device) return MG_OK;
+  MG_TRY(plan_device(lg->plan));
+  std::vector<int2> faces(lg->n_faces);
+  for (int64_t f = 0; f < lg->n_faces; ++f) faces[f] = make_int2(lg->face_elem[f], lg->face_local[f]);
+  mg_status s = upload(&lg->d_faces, faces);
+  if (s == MG_OK) s = upload(&lg->d_b_rowptr, lg->b_rowptr);
+  if (s == MG_OK) s = upload(&lg->d_b_colind, lg->b_colind);
+  if (s == MG_OK) s = upload(&lg->d_b_src_ptr, lg->b_src_ptr);
+  if (s == MG_OK) s = upload(&lg->d_b_src, lg->b_src);
+  if (s == MG_OK) s = upload(&lg->d_s_rowptr, lg->s_rowptr);
+  if (s == MG_OK) s = upload(&lg->d_s_colind, lg->s_colind);
+  if (s == MG_OK) s = upload(&lg->d_s_src, lg->s_src);
+  if (s == MG_OK) {
+    const cudaError_t e = cudaMalloc(&lg->d_face_mat, sizeof(double) * std::max<int64_t>(lg->n_faces * 3 * lg->nb, 1));
+    if (e != cudaSuccess) s = cuda_error(e, "cudaMalloc(face matrices)");
+  }
+  if (s != MG_OK) {
+    free_device(lg);
+    return s;
+  }
+  lg->on_device = true;
+  return MG_OK;
+}
+
+}  // namespace mg
+
+using namespace mg;
+
+extern "C" {
+
+mg_status mg_lagrange_build(mg_plan* plan, int64_t n_tris, const int32_t* h_tris, int32_t lam_diag, mg_lagrange** out)
+{
+  NvtxRange nvtx_range("mg_lagrange_build");
+  if (!plan || !out) return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_build: null argument");
+  if (n_tris < 0 || (n_tris > 0 && !h_tris)) return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_build: bad triangle list");
+  *out = nullptr;
+  mg_lagrange* lg = new (std::nothrow) mg_lagrange();
+  if (!lg) return set_error(MG_ERR_ALLOC, "mg_lagrange_build: out of host memory");
+  lg->plan = plan;
+  mg_status s;
+  try {
+    s = build_lagrange(lg, n_tris, h_tris, lam_diag != 0);
+  } catch (const std::bad_alloc&) {
+    s = set_error(MG_ERR_ALLOC, "mg_lagrange_build: out of host memory");
+  }
+  if (s != MG_OK) {
+    delete lg;
+    return s;
+  }
+  *out = lg;
+  return MG_OK;
+}
+
+mg_status mg_lagrange_destroy(mg_lagrange* lg)
+{
+  if (!lg) return MG_OK;
+  free_device(lg);
+  delete lg;
+  return MG_OK;
+}
+
+mg_status mg_lagrange_get_info(const mg_lagrange* lg, mg_lagrange_info* info)
+{
+  if (!lg || !info) return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_get_info: null argument");
+  info->n_faces = lg->n_faces;
+  info->n_multipliers = lg->nl;
+  info->ndof = lg->ndof;
+  info->nnz_b = lg->nnz_b;
+  info->nnz_saddle = lg->nnz_s;
+  return MG_OK;
+}
+
+mg_status mg_lagrange_export(const mg_lagrange* lg, int32_t* h_lam_node, int32_t* h_face_elem, int32_t* h_face_local)
+{
+  if (!lg) return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_export: null handle");
+  if (h_lam_node && lg->nl) std::memcpy(h_lam_node, lg->lam_node.data(), sizeof(int32_t) * lg->nl);
+  if (h_face_elem && lg->n_faces) std::memcpy(h_face_elem, lg->face_elem.data(), sizeof(int32_t) * lg->n_faces);
+  if (h_face_local && lg->n_faces) std::memcpy(h_face_local, lg->face_local.data(), sizeof(int32_t) * lg->n_faces);
+  return MG_OK;
+}
+
+mg_status mg_lagrange_pattern(const mg_lagrange* lg, int32_t* h_b_rowptr, int32_t* h_b_colind, int32_t* h_s_rowptr,
+                              int32_t* h_s_colind)
+{
+  if (!lg) return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_pattern: null handle");
+  if (h_b_rowptr) std::memcpy(h_b_rowptr, lg->b_rowptr.data(), sizeof(int32_t) * lg->b_rowptr.size());
+  if (h_b_colind && lg->nnz_b) std::memcpy(h_b_colind, lg->b_colind.data(), sizeof(int32_t) * lg->nnz_b);
+  if (h_s_rowptr) std::memcpy(h_s_rowptr, lg->s_rowptr.data(), sizeof(int32_t) * lg->s_rowptr.size());
+  if (h_s_colind && lg->nnz_s) std::memcpy(h_s_colind, lg->s_colind.data(), sizeof(int32_t) * lg->nnz_s);
+  return MG_OK;
+}
+
+mg_status mg_lagrange_export_maps(const mg_lagrange* lg, int32_t* h_b_src_ptr, int32_t* h_b_src, int32_t* h_s_src)
+{
+  if (!lg) return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_export_maps: null handle");
+  if (h_b_src_ptr) std::memcpy(h_b_src_ptr, lg->b_src_ptr.data(), sizeof(int32_t) * lg->b_src_ptr.size());
+  if (h_b_src && !lg->b_src.empty()) std::memcpy(h_b_src, lg->b_src.data(), sizeof(int32_t) * lg->b_src.size());
+  if (h_s_src && lg->nnz_s) std::memcpy(h_s_src, lg->s_src.data(), sizeof(int32_t) * lg->nnz_s);
+  return MG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,177 @@
+// Boundary multipliers on the GPU: values of B = opLA3dA, of the saddle matrix
+// [K B^T; B 0], and the products with them.
+//
+// B is assembled in two deterministic passes:
+//   k_face_matrix  one thread per boundary face: its 3 x nb local matrix
+//                  (mg_lagrange.cuh) into a staging array, face-major;
+//   k_gather_sum   one thread per entry of B: the staged values it sums, in the
+//                  reference's insertion order (element, local face, face
+//                  vertex, basis), from the host-built list of the entry.
+// No atomics, so every run gives the same bits.  The work is O(boundary faces)
+// (n^2 against the volume operator's n^3) and runs in native FP64.
+// The saddle values are a gather from K's and B's values through a per-entry
+// source map; the products use the CSR SpMV kernel of mg_solve.cu.
+#include <algorithm>
+#include <climits>
+
+#include "mg_internal.h"
+#include "mg_lagrange.cuh"
+
+namespace mg {
+
+namespace {
+
+constexpr int kFaceThreads = 256;
+
+int grid_for(int64_t n)
+{
+  const int64_t b = (n + kFaceThreads - 1) / kFaceThreads;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(b, 65535));
+}
+
+template <int NB>
+__global__ void __launch_bounds__(kFaceThreads) k_face_matrix(int64_t n_faces, const int2* __restrict__ faces,
+                                                          const int4* __restrict__ conn,
+                                                          const double4_32a* __restrict__ xyz, FaceRule rule,
+                                                          double* __restrict__ out)
+{
+  for (int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; f < n_faces; f += (int64_t)gridDim.x * blockDim.x) {
+    const int2 fe = faces[f];
+    const int4 c = conn[fe.x];
+    const int v[4] = {c.x, c.y, c.z, c.w};
+    double P[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const double4_32a p = xyz[v[face_vertex(fe.y, a)]];
+      P[a][0] = p.x;
+      P[a][1] = p.y;
+      P[a][2] = p.z;
+    }
+    double mat[3 * NB];
+    face_matrix<NB>(P, fe.y, rule, mat);
+    double* o = out + f * (3 * NB);
+#pragma unroll
+    for (int k = 0; k < 3 * NB; ++k) o[k] = mat[k];
+  }
+}
+
+// vals[k] = sum of src_vals[src[j]] over j in [ptr[k], ptr[k+1]), in list order
+__global__ void __launch_bounds__(kFaceThreads) k_gather_sum(int64_t n, const int32_t* __restrict__ ptr,
+                                                         const int32_t* __restrict__ src,
+                                                         const double* __restrict__ src_vals,
+                                                         double* __restrict__ vals)
+{
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    const int32_t j1 = ptr[k + 1];
+    for (int32_t j = ptr[k]; j < j1; ++j) s += src_vals[src[j]];
+    vals[k] = s;
+  }
+}
+
+// Saddle entry k: K's entry src (>= 0), B's entry -(src + 1), or eye_lam (INT32_MIN)
+__global__ void __launch_bounds__(kFaceThreads) k_saddle_fill(int64_t n, const int32_t* __restrict__ src,
+                                                          const double* __restrict__ kv,
+                                                          const double* __restrict__ bv, double eye_lam,
+                                                          double* __restrict__ out)
+{
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t s = src[k];
+    out[k] = s >= 0 ? kv[s] : (s == INT32_MIN ? eye_lam : bv[-(s + 1)]);
+  }
+}
+
+// Adds eye to the diagonal of the field block: row r's K entries come first in
+// its saddle row, so K's diagonal slot d (row r) sits at s_rowptr[r] + d - k_rowptr[r].
+// k_diag[r] is the first slot of row r with a column >= r; rows without a
+// diagonal entry (dofs outside every element) are left alone.
+__global__ void __launch_bounds__(kFaceThreads) k_saddle_eye(int64_t nd, const int32_t* __restrict__ s_rowptr,
+                                                         const int32_t* __restrict__ k_rowptr,
+                                                         const int32_t* __restrict__ k_colind,
+                                                         const int32_t* __restrict__ k_diag, double eye,
+                                                         double* __restrict__ out)
+{
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nd; r += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t d = k_diag[r];
+    if (d < k_rowptr[r + 1] && k_colind[d] == (int32_t)r) out[s_rowptr[r] + (d - k_rowptr[r])] += eye;
+  }
+}
+
+}  // namespace
+
+}  // namespace mg
+
+using namespace mg;
+
+extern "C" {
+
+mg_status mg_lagrange_assemble(mg_lagrange* lg, int32_t quad, double* d_b_values, void* stream)
+{
+  NvtxRange nvtx_range("mg_lagrange_assemble");
+  if (!lg) return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_assemble: null handle");
+  FaceRule rule{};
+  if (!face_rule(quad, &rule)) return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_assemble: face card must be 1, 3, 4 or 6");
+  if (lg->nnz_b == 0) return MG_OK;
+  if (!d_b_values) return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_assemble: null values");
+  MG_TRY(lagrange_device(lg));
+  cudaStream_t st = (cudaStream_t)stream;
+  const mg_mesh* m = lg->plan->mesh;
+  const int g = grid_for(lg->n_faces);
+  if (lg->nb == 4)
+    k_face_matrix<4><<<g, kFaceThreads, 0, st>>>(lg->n_faces, lg->d_faces, m->d_conn, m->d_xyz, rule, lg->d_face_mat);
+  else
+    k_face_matrix<10><<<g, kFaceThreads, 0, st>>>(lg->n_faces, lg->d_faces, m->d_conn, m->d_xyz, rule, lg->d_face_mat);
+  MG_CUDA(cudaGetLastError());
+  k_gather_sum<<<grid_for(lg->nnz_b), kFaceThreads, 0, st>>>(lg->nnz_b, lg->d_b_src_ptr, lg->d_b_src, lg->d_face_mat,
+                                                          d_b_values);
+  MG_CUDA(cudaGetLastError());
+  return MG_OK;
+}
+
+mg_status mg_saddle_assemble(mg_lagrange* lg, const double* d_k_values, const double* d_b_values, double eye_field,
+                             double eye_lam, double* d_values, void* stream)
+{
+  NvtxRange nvtx_range("mg_saddle_assemble");
+  if (!lg) return set_error(MG_ERR_INVALID_ARG, "mg_saddle_assemble: null handle");
+  if (eye_lam != 0.0 && !lg->lam_diag)
+    return set_error(MG_ERR_INVALID_ARG, "mg_saddle_assemble: eye_lam needs a pattern built with lam_diag");
+  if (lg->nnz_s == 0) return MG_OK;
+  if (!d_values || (lg->plan->nnz && !d_k_values) || (lg->nnz_b && !d_b_values))
+    return set_error(MG_ERR_INVALID_ARG, "mg_saddle_assemble: null argument");
+  MG_TRY(lagrange_device(lg));
+  cudaStream_t st = (cudaStream_t)stream;
+  k_saddle_fill<<<grid_for(lg->nnz_s), kFaceThreads, 0, st>>>(lg->nnz_s, lg->d_s_src, d_k_values, d_b_values, eye_lam,
+                                                           d_values);
+  MG_CUDA(cudaGetLastError());
+  if (eye_field != 0.0 && lg->ndof > 0) {
+    k_saddle_eye<<<grid_for(lg->ndof), kFaceThreads, 0, st>>>(lg->ndof, lg->d_s_rowptr, lg->plan->d_rowptr,
+                                                           lg->plan->d_colind, lg->plan->d_diag, eye_field,
+                                                           d_values);
+    MG_CUDA(cudaGetLastError());
+  }
+  return MG_OK;
+}
+
+mg_status mg_saddle_spmv(mg_lagrange* lg, const double* d_values, const double* d_x, double* d_y, void* stream)
+{
+  NvtxRange nvtx_range("mg_saddle_spmv");
+  if (!lg) return set_error(MG_ERR_INVALID_ARG, "mg_saddle_spmv: null handle");
+  const int64_t rows = lg->ndof + lg->nl;
+  if (rows == 0) return MG_OK;
+  if (!d_values || !d_x || !d_y) return set_error(MG_ERR_INVALID_ARG, "mg_saddle_spmv: null argument");
+  MG_TRY(lagrange_device(lg));
+  return launch_spmv_csr(rows, lg->nnz_s, lg->d_s_rowptr, lg->d_s_colind, d_values, d_x, d_y, (cudaStream_t)stream);
+}
+
+mg_status mg_lagrange_apply(mg_lagrange* lg, const double* d_b_values, const double* d_u, double* d_g, void* stream)
+{
+  NvtxRange nvtx_range("mg_lagrange_apply");
+  if (!lg) return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_apply: null handle");
+  if (lg->nl == 0) return MG_OK;
+  if (!d_b_values || !d_u || !d_g) return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_apply: null argument");
+  MG_TRY(lagrange_device(lg));
+  return launch_spmv_csr(lg->nl, lg->nnz_b, lg->d_b_rowptr, lg->d_b_colind, d_b_values, d_u, d_g,
+                         (cudaStream_t)stream);
+}
+
+}  // extern "C"

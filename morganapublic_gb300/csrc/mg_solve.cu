@@ -107,22 +107,31 @@ template <typename V> constexpr int kEntriesPerLane = sizeof(V) == 8 ? 16 : 8;
 // (P2); FP32 the smallest group of at least 2 lanes whose pass covers the mean
 // row length.
 template <typename V>
-static int row_group(const mg_plan* p)
+static int row_group(int64_t rows, int64_t nnz)
 {
-  const double mean = p->ndof > 0 ? (double)p->nnz / (double)p->ndof : 1.0;
+  const double mean = rows > 0 ? (double)nnz / (double)rows : 1.0;
   if (sizeof(V) == 8) return mean > 16.0 ? 2 : 1;
   const int U = kEntriesPerLane<V>;
   for (int g = 2; g < 32; g *= 2)
     if (mean <= g * U) return g;
   return 32;
 }
+template <typename V>
+static int row_group(const mg_plan* p)
+{
+  return row_group<V>(p->ndof, p->nnz);
+}
 
 // CTAs of a row kernel with G lanes per row, at most `per_sm` per SM.
-static int row_blocks(const mg_plan* p, int G, int per_sm)
+static int row_blocks(int64_t rows, int G, int per_sm)
 {
-  const int64_t need = (p->ndof * G + kSolveThreads - 1) / kSolveThreads;
+  const int64_t need = (rows * G + kSolveThreads - 1) / kSolveThreads;
   const int cap = per_sm * sm_count();
   return (int)std::max<int64_t>(1, std::min<int64_t>({need, (int64_t)cap, (int64_t)kMaxSolveBlocks}));
+}
+static int row_blocks(const mg_plan* p, int G, int per_sm)
+{
+  return row_blocks(p->ndof, G, per_sm);
 }
 template <typename V>
 static int row_blocks(const mg_plan* p, int G)
@@ -634,6 +643,19 @@ mg_status launch_spmv(mg_plan* p, int prec, const void* vals, const void* x, voi
                                    (const float*)x, (float*)y)));
     }
   }
+  MG_CUDA(cudaGetLastError());
+  return MG_OK;
+}
+
+// y = A x for a CSR matrix of any shape: the standalone SpMV kernel with the
+// lane group of the FP64 path, int32 columns.
+mg_status launch_spmv_csr(int64_t rows, int64_t nnz, const int32_t* rowptr, const int32_t* colind,
+                          const double* vals, const double* x, double* y, cudaStream_t st)
+{
+  if (rows == 0) return MG_OK;
+  const int G = row_group<double>(rows, nnz), nb = row_blocks(rows, G, 8);
+  MG_DISPATCH_G(G, (launch_pdl(k_spmv<double, g, int32_t>, nb, kSolveThreads, st, rows, rowptr, colind, vals, x,
+                               y)));
   MG_CUDA(cudaGetLastError());
   return MG_OK;
 }

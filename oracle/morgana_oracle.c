@@ -36,6 +36,10 @@
  *                        in insertion = element order, columns sorted, zeros kept)
  *   load vector          src/morganaFiniteElements/traitsVectorBuilder.hpp:214-274
  *   CG                   src/morganaTrilinos/belosBlockCG.hpp:46-82 (block size 1)
+ *   boundary faces       src/morganaFiniteElements/localMatrixLA3d.hpp:292-322,
+ *   (opLA3dA)            src/morganaIntegrator/integratorOLA3d_STD.hpp:102-124,
+ *                        src/morganaOperators/opLA3dA.hpp:86-112,
+ *                        src/morganaIntegrator/intStaticCards.cpp:176-300 (triangle cards)
  *
  * Build additions that have no reference counterpart (symmetric Dirichlet
  * elimination, adjoint gradient dJ/dkappa_e = -lambda_e^T Khat_e u_e) are marked
@@ -678,6 +682,107 @@ int or_adjoint_grad(int order, int quad, const double *xyz, int64_t n_elem, cons
       for (int j = 0; j < nb; ++j)
         s += lambda[dofs[nb * e + j]] * mat[i * nb + j] * u[dofs[nb * e + i]];
     grad[e] = -s;
+  }
+  return OR_OK;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Boundary-face Lagrange operator opLA3dA: field = the tet's P1/P2 basis,    */
+/* test = the P1 basis of the boundary triangle (fePr2d<1>).                  */
+/* ------------------------------------------------------------------------- */
+
+/* Triangle cards (intStaticCards.cpp:176-300): precision 1 = centroid,
+   2 = edge midpoints, 3 = the 4-point rule with one negative weight,
+   4 = the 6-point rule.  Y holds (x, y) pairs. */
+int or_tri_rule(int prec, double *Y, double *W)
+{
+  if (prec == 1) {
+    Y[0] = 1.0 / 3.0; Y[1] = 1.0 / 3.0;
+    W[0] = 0.5;
+    return 1;
+  }
+  if (prec == 2) {
+    const double P[3][2] = {{0.5, 0.0}, {0.0, 0.5}, {0.5, 0.5}};
+    for (int i = 0; i < 3; ++i) { Y[2 * i] = P[i][0]; Y[2 * i + 1] = P[i][1]; W[i] = 1.0 / 6.0; }
+    return 3;
+  }
+  if (prec == 3) {
+    const double a = 3.0 / 5.0, b = 1.0 / 5.0, c = 1.0 / 3.0;
+    const double P[4][2] = {{a, b}, {b, a}, {b, b}, {c, c}};
+    const double w[4] = {25.0 / 96.0, 25.0 / 96.0, 25.0 / 96.0, -9.0 / 32.0};
+    for (int i = 0; i < 4; ++i) { Y[2 * i] = P[i][0]; Y[2 * i + 1] = P[i][1]; W[i] = w[i]; }
+    return 4;
+  }
+  if (prec == 4) {
+    const double x1 = 0.091576213509770743, x2 = 0.44594849091596488;
+    const double w1 = 0.054975871827660933, w2 = 0.11169079483900573;
+    const double P[6][2] = {{x1, x1}, {x1, 1 - 2 * x1}, {1 - 2 * x1, x1},
+                            {x2, x2}, {x2, 1 - 2 * x2}, {1 - 2 * x2, x2}};
+    const double w[6] = {w1, w1, w1, w2, w2, w2};
+    for (int i = 0; i < 6; ++i) { Y[2 * i] = P[i][0]; Y[2 * i + 1] = P[i][1]; W[i] = w[i]; }
+    return 6;
+  }
+  return 0;
+}
+
+/* Local faces of linearTetra (geoShapes.cpp:681-688), 0-based vertex indices. */
+static const int FACE_PTS[4][3] = {{0, 2, 1}, {0, 1, 3}, {1, 2, 3}, {0, 3, 2}};
+static const double REF_TET[4][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+
+/* Local matrix of opLA3dA on local face lf (0..3) of a tet: the quadrature
+   loop of integratorOLA3d_STD.hpp:102-124 around the integrand of
+   opLA3dA.hpp:86-112,
+     mat[a * nb + i] = sum_q (phi_i(Yv) psi_a(Ys)) |Vx ^ Vy| w_q,
+   a over the face's points in face order, i over the tet's nb basis functions.
+   Vx, Vy: derivatives of the linear map of the reference triangle onto the
+   face (geoMapInterface.hpp:25-90, point 3 first).  Yv: the same map onto the
+   reference tet's face (supportLagrange3d mapVolumeY).  Ys: the point in the
+   boundary triangle's own coordinates (mapSurfaceY, through mapGlobalToLocal);
+   the boundary triangle has the face's vertices, so psi_a(Ys) is the face
+   barycentric a of the point, which this restatement uses directly (the two
+   agree to rounding). */
+int or_face_matrix(int order, int prec, const double *xyz, const int32_t *nodes4, int lf, double *mat)
+{
+  if (lf < 0 || lf > 3) return OR_ERR_ARG;
+  double Y[12], W[6];
+  const int nq = or_tri_rule(prec, Y, W);
+  if (nq == 0) return OR_ERR_ARG;
+  const int nb = nbasis(order);
+  double P[3][3];
+  for (int a = 0; a < 3; ++a)
+    for (int k = 0; k < 3; ++k) P[a][k] = xyz[3 * nodes4[FACE_PTS[lf][a]] + k];
+  double Vx[3], Vy[3], N[3];
+  for (int k = 0; k < 3; ++k) {
+    Vx[k] = P[2][k] * 0.0 + (P[1][k] * 1.0 + P[0][k] * -1.0);
+    Vy[k] = P[2][k] * 1.0 + (P[1][k] * 0.0 + P[0][k] * -1.0);
+  }
+  N[0] = Vx[1] * Vy[2] - Vx[2] * Vy[1];
+  N[1] = Vx[2] * Vy[0] - Vx[0] * Vy[2];
+  N[2] = Vx[0] * Vy[1] - Vx[1] * Vy[0];
+  const double area2 = sqrt(N[0] * N[0] + N[1] * N[1] + N[2] * N[2]);
+  for (int k = 0; k < 3 * nb; ++k) mat[k] = 0.0;
+  for (int q = 0; q < nq; ++q) {
+    const double x = Y[2 * q], y = Y[2 * q + 1];
+    const double lam[3] = {1.0 - x - y, x, y};
+    double Yv[3], phi[10];
+    for (int k = 0; k < 3; ++k)
+      Yv[k] = REF_TET[FACE_PTS[lf][2]][k] * lam[2] +
+              (REF_TET[FACE_PTS[lf][1]][k] * lam[1] + REF_TET[FACE_PTS[lf][0]][k] * lam[0]);
+    or_basis_eval(order, Yv, phi);
+    for (int a = 0; a < 3; ++a)
+      for (int i = 0; i < nb; ++i) mat[a * nb + i] += phi[i] * lam[a] * area2 * W[q];
+  }
+  return OR_OK;
+}
+
+/* or_face_matrix over a list of faces (face_elem[f], face_local[f]). */
+int or_face_matrices(int order, int prec, const double *xyz, int64_t n_faces, const int32_t *conn,
+                     const int32_t *face_elem, const int32_t *face_local, double *out)
+{
+  const int nb = nbasis(order);
+  for (int64_t f = 0; f < n_faces; ++f) {
+    int rc = or_face_matrix(order, prec, xyz, &conn[4 * (int64_t)face_elem[f]], face_local[f], out + 3 * nb * f);
+    if (rc) return rc;
   }
   return OR_OK;
 }

@@ -22,6 +22,10 @@ OPS = {"stiff_kappa": 0, "stiff_const": 1, "mass": 2, "mass_coeff": 3}
 EDGES = {"lex": 0, "first": 1}
 # quadrature names of the product (1, 4, 15, 64 points) -> reference card precision
 QUAD_PREC = {1: 1, 4: 2, 15: 3, 64: 4}
+# triangle cards of the boundary-face operator by point count -> reference precision
+FACE_QUAD_PREC = {1: 1, 3: 2, 4: 3, 6: 4}
+# local faces of linearTetra (geoShapes.cpp:681-688), 0-based
+FACE_PTS = np.array([[0, 2, 1], [0, 1, 3], [1, 2, 3], [0, 3, 2]])
 
 _lib = None
 
@@ -54,6 +58,9 @@ def lib():
         L.or_adjoint_grad.argtypes = [I32, I32, P, I64, P, P, P, P, P]
         L.or_basis_eval.argtypes = [I32, P, P]
         L.or_basis_grad.argtypes = [I32, P, P, P, P]
+        L.or_tri_rule.argtypes = [I32, P, P]
+        L.or_face_matrix.argtypes = [I32, I32, P, P, I32, P]
+        L.or_face_matrices.argtypes = [I32, I32, P, I64, P, P, P, P]
         _lib = L
     return _lib
 
@@ -172,3 +179,126 @@ def full_operator(op, order, quad, xyz, conn, coeff=None, c=1.0, edge_rule="lex"
     rp, ci = pattern(order, ndof, dofs)
     vals = assemble(op, order, quad, xyz, conn, dofs, rp, ci, coeff, c)
     return dofs, rp, ci, vals
+
+
+# ----------------------------------------------------------------------------
+# Boundary-face Lagrange operator (opLA3dA) and the saddle system
+# ----------------------------------------------------------------------------
+
+def tri_rule(quad: int):
+    Y = np.empty((6, 2))
+    W = np.empty(6)
+    n = lib().or_tri_rule(FACE_QUAD_PREC[quad], _p(Y), _p(W))
+    return Y[:n].copy(), W[:n].copy()
+
+
+def face_matrix(order, quad, xyz, nodes4, lf):
+    nb = 4 if order == 1 else 10
+    mat = np.empty(3 * nb)
+    nodes4 = np.ascontiguousarray(nodes4, dtype=np.int32)
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    assert lib().or_face_matrix(order, FACE_QUAD_PREC[quad], _p(xyz), _p(nodes4), lf, _p(mat)) == 0
+    return mat.reshape(3, nb)  # [face point a, field basis i]
+
+
+def boundary_faces(conn, tris=None):
+    """(element, local face) of every face with one incident tet, in element then
+    local-face order (the loop order of the reference's builder over grid3d and
+    localMatrixLA3d::matrix); with `tris` (k x 3 node ids), only the faces that
+    are among them (the boundary triangles whose geoIds the test field keeps)."""
+    conn = np.asarray(conn)
+    tri = conn[:, FACE_PTS].reshape(-1, 3)
+    key = np.sort(tri, axis=1)
+    _, inv, cnt = np.unique(key, axis=0, return_inverse=True, return_counts=True)
+    inv = inv.reshape(-1)
+    if cnt.max(initial=0) > 2:
+        raise ValueError("a face is shared by more than two tets")
+    idx = np.nonzero(cnt[inv] == 1)[0]
+    if tris is not None:
+        want = {tuple(t) for t in np.sort(np.asarray(tris), axis=1).tolist()}
+        idx = np.array([i for i in idx if tuple(key[i].tolist()) in want], dtype=np.int64)
+    return (idx // 4).astype(np.int32), (idx % 4).astype(np.int32)
+
+
+def lagrange(order, quad, xyz, conn, dofs, ndof, tris=None):
+    """B of opLA3dA with P1 multipliers on the boundary triangles.
+
+    Multipliers: the nodes of the selected boundary faces, numbered by ascending
+    node id (meshDoctor2d.hpp:339-500 compacts the boundary grid's nodes in that
+    order; dofMapStatic2d numbers P1 dofs by node).  Rows = multipliers, columns =
+    field dofs; every face contributes its 3 x nb local block, zeros included
+    (traitsMatrixBuilder.hpp:363-441 inserts the whole block), summed in element,
+    local-face, face-point, basis order.  Returns (lam_node, rowptr, colind,
+    values, face_elem, face_local)."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    conn = np.ascontiguousarray(conn, dtype=np.int32)
+    nb = dofs.shape[1]
+    fe, fl = boundary_faces(conn, tris)
+    nf = fe.shape[0]
+    mats = np.empty((nf, 3, nb))
+    if nf:
+        assert lib().or_face_matrices(order, FACE_QUAD_PREC[quad], _p(xyz), nf, _p(conn), _p(fe), _p(fl),
+                                      _p(mats)) == 0
+    fnodes = conn[fe[:, None], FACE_PTS[fl]] if nf else np.zeros((0, 3), np.int32)
+    lam_node = np.unique(fnodes).astype(np.int32)
+    lam_of = np.full(xyz.shape[0], -1, dtype=np.int64)
+    lam_of[lam_node] = np.arange(lam_node.shape[0])
+    rows = np.broadcast_to(lam_of[fnodes][:, :, None], (nf, 3, nb)).reshape(-1)
+    cols = np.broadcast_to(dofs[fe][:, None, :], (nf, 3, nb)).reshape(-1).astype(np.int64)
+    key = rows * ndof + cols
+    ukey, pos = np.unique(key, return_inverse=True)
+    vals = np.zeros(ukey.shape[0])
+    np.add.at(vals, pos.reshape(-1), mats.reshape(-1))  # sequential: insertion order
+    nl = lam_node.shape[0]
+    rowptr = np.zeros(nl + 1, dtype=np.int32)
+    np.add.at(rowptr, (ukey // ndof) + 1, 1)
+    rowptr = np.cumsum(rowptr).astype(np.int32)
+    colind = (ukey % ndof).astype(np.int32)
+    return lam_node, rowptr, colind, vals, fe, fl
+
+
+def saddle(k_rowptr, k_colind, k_vals, b_rowptr, b_colind, b_vals, ndof, lam_diag=False, eye_field=0.0,
+           eye_lam=0.0):
+    """[K + eye_field I, B^T; B, eye_lam I] over (ndof + n_multipliers) rows, the
+    layout of epetraSaddleAssembler::setDiagMatrix(K, field block) plus
+    setSymmMatrix(B, multiplier block, field block) and setEye on the blocks
+    (epetraSaddleAssembler.cpp); the multiplier diagonal is stored only with
+    lam_diag.  Returns (rowptr, colind, values)."""
+    nl = b_rowptr.shape[0] - 1
+    brow = np.repeat(np.arange(nl), np.diff(b_rowptr))
+    order = np.lexsort((brow, b_colind))  # B^T rows: by field column, then multiplier
+    t_cnt = np.bincount(b_colind, minlength=ndof)
+    t_ptr = np.concatenate([[0], np.cumsum(t_cnt)])
+    t_col = ndof + brow[order]
+    t_val = b_vals[order]
+    cols, vals = [], []
+    for r in range(ndof):
+        k0, k1 = k_rowptr[r], k_rowptr[r + 1]
+        kv = np.array(k_vals[k0:k1], dtype=np.float64)
+        kv[k_colind[k0:k1] == r] += eye_field
+        cols += [k_colind[k0:k1], t_col[t_ptr[r]:t_ptr[r + 1]]]
+        vals += [kv, t_val[t_ptr[r]:t_ptr[r + 1]]]
+    for l in range(nl):
+        cols.append(b_colind[b_rowptr[l]:b_rowptr[l + 1]])
+        vals.append(b_vals[b_rowptr[l]:b_rowptr[l + 1]])
+        if lam_diag:
+            cols.append(np.array([ndof + l]))
+            vals.append(np.array([eye_lam]))
+    lens = [0] * (ndof + nl)
+    i = 0
+    for r in range(ndof):
+        lens[r] = len(cols[i]) + len(cols[i + 1])
+        i += 2
+    for l in range(nl):
+        lens[ndof + l] = len(cols[i]) + (len(cols[i + 1]) if lam_diag else 0)
+        i += 2 if lam_diag else 1
+    rowptr = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+    colind = np.concatenate(cols).astype(np.int32) if cols else np.zeros(0, np.int32)
+    values = np.concatenate(vals).astype(np.float64) if vals else np.zeros(0)
+    return rowptr, colind, values
+
+
+def csr_matvec(rowptr, colind, values, x):
+    """y = A x for a CSR matrix of any shape (plain sums in row order)."""
+    rows = np.repeat(np.arange(rowptr.shape[0] - 1), np.diff(rowptr))
+    return np.bincount(rows, weights=values * np.asarray(x)[colind], minlength=rowptr.shape[0] - 1)

@@ -1,0 +1,25 @@
+// Test harness: the per-face arithmetic of the boundary-face kernel
+// (mg_lagrange.cuh, the body k_face_matrix runs per thread) built for the host,
+// so the CPU tests can compare it with the oracle without a GPU.  Not part of
+// the library.
+#include <cstdint>
+
+#include "mg_lagrange.cuh"
+
+extern "C" int face_check_matrices(int order, int quad, const double* xyz, int64_t n_faces, const int32_t* conn,
+                                   const int32_t* face_elem, const int32_t* face_local, double* out)
+{
+  mg::FaceRule rule{};
+  if (!mg::face_rule(quad, &rule)) return 1;
+  const int nb = order == 1 ? 4 : 10;
+  for (int64_t f = 0; f < n_faces; ++f) {
+    const int32_t* c = conn + 4 * (int64_t)face_elem[f];
+    const int lf = face_local[f];
+    double P[3][3];
+    for (int a = 0; a < 3; ++a)
+      for (int k = 0; k < 3; ++k) P[a][k] = xyz[3 * (int64_t)c[mg::face_vertex(lf, a)] + k];
+    if (nb == 4) mg::face_matrix<4>(P, lf, rule, out + f * 3 * nb);
+    else mg::face_matrix<10>(P, lf, rule, out + f * 3 * nb);
+  }
+  return 0;
+}

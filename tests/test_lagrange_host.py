@@ -1,0 +1,229 @@
+"""Boundary-face Lagrange operator (opLA3dA) and the saddle matrix, CPU side.
+
+The host half of mg_lagrange (boundary faces, multiplier numbering, the
+patterns of B and [K B^T; B 0], the gather maps) runs through the C ABI
+without a device and is compared with the oracle bit for bit.  The per-face
+arithmetic of the kernel (mg_lagrange.cuh) is compiled for the host by
+tests/lagrange/face_check.cpp and run through the exported gather maps, which
+is the data flow of the two kernels, against the oracle's values.
+
+The reference's own tests for this operator (operatorLA3dTest1.cpp) print
+their results and hold no expected values, so the oracle is pinned here by
+properties: the triangle cards integrate monomials exactly to their degree,
+the rows of B sum to the integral of each multiplier's hat function (the field
+basis is a partition of unity), and the P1 x P1 block is the face mass matrix
+area/12 (1 + delta) under a card exact for degree 2."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import morganapublic_gb300 as mg
+import oracle as orc
+from helpers import row_scaled_err
+from morganapublic_gb300 import meshgen
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CARDS = [1, 3, 4, 6]
+DEGREE = {1: 1, 3: 2, 4: 3, 6: 4}
+
+
+@pytest.fixture(scope="module")
+def face_lib(tmp_path_factory):
+    out = str(tmp_path_factory.mktemp("face") / "libface_check.so")
+    subprocess.run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-shared", "-fPIC", "-Wall", "-Werror",
+                    "-I" + os.path.join(ROOT, "morganapublic_gb300", "csrc"),
+                    os.path.join(ROOT, "tests", "lagrange", "face_check.cpp"), "-o", out], check=True)
+    L = ctypes.CDLL(out)
+    P = ctypes.c_void_p
+    L.face_check_matrices.argtypes = [ctypes.c_int, ctypes.c_int, P, ctypes.c_int64, P, P, P, P]
+    return L
+
+
+def _p(a):
+    return a.ctypes.data
+
+
+def kernel_face_matrices(face_lib, order, quad, xyz, conn, fe, fl):
+    nb = 4 if order == 1 else 10
+    out = np.empty((len(fe), 3, nb))
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    conn = np.ascontiguousarray(conn, dtype=np.int32)
+    fe = np.ascontiguousarray(fe, dtype=np.int32)
+    fl = np.ascontiguousarray(fl, dtype=np.int32)
+    assert face_lib.face_check_matrices(order, quad, _p(xyz), len(fe), _p(conn), _p(fe), _p(fl), _p(out)) == 0
+    return out
+
+
+def _mesh(n, order, seed=3):
+    m = meshgen.kuhn_cube(n, jitter=0.2, seed=seed, permute=True)
+    mesh = mg.Mesh(m.xyz, m.conn, order=order)
+    return m, mesh, mg.MatrixBuilder(mesh)
+
+
+# --------------------------------------------------------------- oracle pins --
+@pytest.mark.parametrize("quad", CARDS)
+def test_triangle_cards_exact_to_their_degree(quad):
+    """int over the reference triangle of x^i y^j = i! j! / (i + j + 2)!"""
+    from math import factorial
+    Y, W = orc.tri_rule(quad)
+    assert abs(W.sum() - 0.5) < 1e-15
+    for i in range(DEGREE[quad] + 1):
+        for j in range(DEGREE[quad] + 1 - i):
+            exact = factorial(i) * factorial(j) / factorial(i + j + 2)
+            assert abs(np.sum(W * Y[:, 0] ** i * Y[:, 1] ** j) - exact) < 1e-15, (i, j)
+
+
+@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("quad", CARDS)
+def test_oracle_rows_sum_to_hat_integrals(order, quad):
+    m, mesh, b = _mesh(3, order)
+    dofs = mesh.elem_dofs()
+    lam, rp, ci, v, fe, fl = orc.lagrange(order, quad, m.xyz, m.conn, dofs, b.ndof)
+    fn = m.conn[fe[:, None], orc.FACE_PTS[fl]]
+    P = m.xyz[fn]
+    area = 0.5 * np.linalg.norm(np.cross(P[:, 1] - P[:, 0], P[:, 2] - P[:, 0]), axis=1)
+    want = np.zeros(len(lam))
+    np.add.at(want, np.searchsorted(lam, fn).reshape(-1), np.repeat(area / 3, 3))
+    assert np.abs(np.add.reduceat(v, rp[:-1]) - want).max() < 1e-15
+    assert abs(area.sum() - 6.0) < 1e-12  # the unit cube's surface
+
+
+def test_oracle_p1_block_is_the_face_mass_matrix():
+    m = meshgen.kuhn_cube(2, jitter=0.25, seed=5, permute=False)
+    for e in range(len(m.conn)):
+        for lf in range(4):
+            mat = orc.face_matrix(1, 3, m.xyz, m.conn[e], lf)
+            P = m.xyz[m.conn[e][orc.FACE_PTS[lf]]]
+            area = 0.5 * np.linalg.norm(np.cross(P[1] - P[0], P[2] - P[0]))
+            want = np.zeros((3, 4))
+            for a in range(3):
+                for bb in range(3):
+                    want[a, orc.FACE_PTS[lf][bb]] = area / 12 * (2 if a == bb else 1)
+            assert np.abs(mat - want).max() <= 1e-15 * max(area, 1.0)
+
+
+# ------------------------------------------------------ kernel arithmetic --
+@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("quad", CARDS)
+def test_kernel_face_math_matches_oracle(face_lib, order, quad):
+    m, mesh, b = _mesh(3, order, seed=7)
+    fe, fl = orc.boundary_faces(m.conn)
+    ref = np.stack([orc.face_matrix(order, quad, m.xyz, m.conn[e], l) for e, l in zip(fe, fl)])
+    got = kernel_face_matrices(face_lib, order, quad, m.xyz, m.conn, fe, fl)
+    scale = np.abs(ref).max(axis=(1, 2), keepdims=True)
+    assert np.max(np.abs(got - ref) / scale) < 1e-14
+
+
+# --------------------------------------------------------- host ABI (no GPU) --
+def _tris_on_plane(m, axis, value):
+    fe, fl = orc.boundary_faces(m.conn)
+    fn = m.conn[fe[:, None], orc.FACE_PTS[fl]]
+    on = np.all(np.abs(m.xyz[fn][:, :, axis] - value) < 1e-12, axis=1)
+    return fn[on][:, ::-1].copy()  # any vertex order
+
+
+@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("select", [None, "x0", "x0z1"])
+@pytest.mark.parametrize("lam_diag", [False, True])
+def test_patterns_match_oracle(order, select, lam_diag):
+    m, mesh, b = _mesh(4 if order == 1 else 3, order, seed=11)
+    tris = None
+    if select == "x0":
+        tris = _tris_on_plane(m, 0, 0.0)
+    elif select == "x0z1":
+        tris = np.concatenate([_tris_on_plane(m, 0, 0.0), _tris_on_plane(m, 2, 1.0)])
+    lg = mg.LagrangeBuilder(b, tris=tris, lam_diag=lam_diag)
+    lam, fe, fl = lg.multipliers()
+    (brp, bci), (srp, sci) = lg.pattern()
+    dofs = mesh.elem_dofs()
+    olam, obrp, obci, obv, ofe, ofl = orc.lagrange(order, 1, m.xyz, m.conn, dofs, b.ndof, tris=tris)
+    assert np.array_equal(fe, ofe) and np.array_equal(fl, ofl)
+    assert np.array_equal(lam, olam)
+    assert np.array_equal(brp, obrp) and np.array_equal(bci, obci)
+    rp, ci = b.pattern()
+    orp, oci, _ = orc.saddle(rp, ci, np.zeros(len(ci)), obrp, obci, obv, b.ndof, lam_diag=lam_diag)
+    assert np.array_equal(srp, orp) and np.array_equal(sci, oci)
+    if select is not None:
+        assert lg.n_faces == len(tris)
+
+
+@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("quad", [1, 6])
+def test_kernel_data_flow_matches_oracle(face_lib, order, quad):
+    """The two kernels' data flow on the host: face matrices (the kernel's own
+    arithmetic), the per-entry gather lists of B, the saddle source map."""
+    m, mesh, b = _mesh(4 if order == 1 else 3, order, seed=13)
+    lg = mg.LagrangeBuilder(b, lam_diag=True)
+    lam, fe, fl = lg.multipliers()
+    (brp, bci), (srp, sci) = lg.pattern()
+    bptr, bsrc, ssrc = lg.export_maps()
+    fm = kernel_face_matrices(face_lib, order, quad, m.xyz, m.conn, fe, fl).reshape(-1)
+    bv = np.array([np.sum(fm[bsrc[bptr[k]:bptr[k + 1]]]) for k in range(lg.nnz_b)])
+    dofs = mesh.elem_dofs()
+    _, orp, oci, ov, _, _ = orc.lagrange(order, quad, m.xyz, m.conn, dofs, b.ndof)
+    assert row_scaled_err(orp, ov, bv) <= 1e-13
+    # every face-matrix entry is used exactly once
+    assert np.array_equal(np.sort(bsrc), np.arange(len(fe) * 3 * mesh.nb))
+    # saddle values through the source map
+    rp, ci = b.pattern()
+    kv = np.random.default_rng(1).uniform(-1, 1, len(ci))
+    bidx = np.clip(-(ssrc.astype(np.int64) + 1), 0, lg.nnz_b - 1)
+    sv = np.where(ssrc >= 0, kv[np.maximum(ssrc, 0)], bv[bidx])
+    sv[ssrc == np.iinfo(np.int32).min] = 0.0
+    orp_s, oci_s, osv = orc.saddle(rp, ci, kv, brp, bci, bv, b.ndof, lam_diag=True)
+    assert np.array_equal(srp, orp_s) and np.array_equal(sci, oci_s) and np.array_equal(sv, osv)
+
+def test_selected_triangles_errors():
+    m, mesh, b = _mesh(3, 1)
+    good = _tris_on_plane(m, 0, 0.0)
+    interior = np.array([m.conn[0][[0, 1, 2]]])  # a face of some tet; pick one that is interior
+    fe, fl = orc.boundary_faces(m.conn)
+    bset = {tuple(sorted(t)) for t in m.conn[fe[:, None], orc.FACE_PTS[fl]].tolist()}
+    for e in range(len(m.conn)):
+        for lf in range(4):
+            t = m.conn[e][orc.FACE_PTS[lf]]
+            if tuple(sorted(t.tolist())) not in bset:
+                interior = t[None, :]
+                break
+        else:
+            continue
+        break
+    with pytest.raises(mg.MorganaError) as e:
+        mg.LagrangeBuilder(b, tris=np.concatenate([good, interior]))
+    assert e.value.status == mg.MG_ERR_BAD_MESH
+    with pytest.raises(mg.MorganaError) as e:
+        mg.LagrangeBuilder(b, tris=np.concatenate([good, good[:1]]))
+    assert e.value.status == mg.MG_ERR_INVALID_ARG
+    bad = good.copy()
+    bad[0, 0] = len(m.xyz)
+    with pytest.raises(mg.MorganaError) as e:
+        mg.LagrangeBuilder(b, tris=bad)
+    assert e.value.status == mg.MG_ERR_INVALID_ARG
+    empty = mg.LagrangeBuilder(b, tris=np.zeros((0, 3), dtype=np.int32))
+    assert empty.n_faces == 0 and empty.n_multipliers == 0 and empty.nnz_b == 0
+    rp, ci = b.pattern()
+    assert empty.nnz_saddle == len(ci)
+
+
+def test_face_in_three_tets_is_rejected():
+    xyz = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1], [0, 0, -1], [0.1, 0.1, 2.0]], dtype=np.float64)
+    conn = np.array([[0, 1, 2, 3], [0, 2, 1, 4], [0, 1, 2, 5]], dtype=np.int32)
+    b = mg.MatrixBuilder(mg.Mesh(xyz, conn, order=1))
+    with pytest.raises(mg.MorganaError) as e:
+        mg.LagrangeBuilder(b)
+    assert e.value.status == mg.MG_ERR_BAD_MESH
+
+
+def test_single_tet_all_faces_boundary():
+    xyz = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], dtype=np.float64)
+    conn = np.array([[0, 1, 2, 3]], dtype=np.int32)
+    for order in (1, 2):
+        mesh = mg.Mesh(xyz, conn, order=order)
+        b = mg.MatrixBuilder(mesh)
+        lg = mg.LagrangeBuilder(b)
+        lam, fe, fl = lg.multipliers()
+        assert np.array_equal(lam, [0, 1, 2, 3]) and np.array_equal(fe, [0] * 4) and np.array_equal(fl, range(4))
+        assert lg.nnz_b == 4 * mesh.nb  # every multiplier couples to every dof of the tet
