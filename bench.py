@@ -52,7 +52,8 @@ def parse():
                          "5: P1 128^3 kernels as fractions of the HBM roofline")
     ap.add_argument("--order", type=int, default=1, choices=[1, 2], help="element order of the --only modes")
     ap.add_argument("--only", default=None,
-                    choices=["asm64", "asm32", "spmv64", "spmv32", "cg64", "cg32", "adj", "rhs", "suite", "setup"],
+                    choices=["asm64", "asm32", "spmv64", "spmv32", "cg64", "cg32", "adj", "rhs", "suite", "setup",
+                             "lagrange"],
                     help="run warmup + steps launches of one kernel only (for profilers) and print its timing")
     return ap.parse_args()
 
@@ -310,6 +311,44 @@ def run_only(a):
                 b.adjoint_grad(x, lam, quad=quad, out=g, stream=stream)
         torch.cuda.synchronize()
         print(json.dumps({"only": a.only, "n": a.n, "order": a.order, "rounds": a.warmup + a.steps}))
+        return 0
+    if a.only == "lagrange":
+        # boundary multipliers: host build, B = opLA3dA (face matrices + gather), saddle fill,
+        # saddle SpMV; median CUDA-event time per call, L2 flushed before each
+        t0 = time.perf_counter()
+        lg = mg.LagrangeBuilder(b)
+        build_s = time.perf_counter() - t0
+        bv = lg.assemble(quad=1)
+        sv = lg.saddle(v64, bv)
+        xs = torch.from_numpy(np.random.default_rng(a.seed).uniform(-1, 1, b.ndof + lg.n_multipliers)).cuda()
+        ys = torch.empty_like(xs)
+        calls = {"b_assemble": lambda: lg.assemble(quad=1, out=bv, stream=stream),
+                 "saddle_fill": lambda: lg.saddle(v64, bv, out=sv, stream=stream),
+                 "saddle_spmv": lambda: lg.saddle_apply(sv, xs, out=ys, stream=stream)}
+        res = {}
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            for name, fn in calls.items():
+                ts = []
+                for r in range(a.warmup + a.steps):
+                    flush.fill_(float(r))
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
+                    fn()
+                    e1.record(stream)
+                    torch.cuda.synchronize()
+                    if r >= a.warmup:
+                        ts.append(e0.elapsed_time(e1))
+                res[name + "_ms"] = statistics.median(ts)
+        nb = 4 if a.order == 1 else 10
+        F, nzb, nzs, rows = lg.n_faces, lg.nnz_b, lg.nnz_saddle, b.ndof + lg.n_multipliers
+        byts = {"b_assemble": F * (8 + 16 + 3 * 32 + 2 * 3 * nb * 8) + nzb * 12 + 4 * F * 3 * nb,
+                "saddle_fill": nzs * 20, "saddle_spmv": spmv_bytes(rows, nzs, 8)}
+        print(json.dumps({"only": "lagrange", "n": a.n, "order": a.order, "faces": F, "multipliers": lg.n_multipliers,
+                          "nnz_b": nzb, "nnz_saddle": nzs, "build_s": build_s, **res,
+                          **{k + "_gbs": byts[k] / res[k + "_ms"] / 1e6 for k in byts},
+                          "algorithmic_bytes": byts}))
+        lg.close()
         return 0
     if a.only in ("cg64", "cg32"):
         # a fixed number of PCG iterations on the Dirichlet system (f = 1)
