@@ -48,42 +48,62 @@ Tri sorted_tri(int32_t x, int32_t y, int32_t z)
 
 // Flags every local face of every tet: 1 = boundary (one tet), 0 = interior
 // (two tets).  A face found in three or more tets makes the mesh invalid.
+// Faces are bucketed by their lowest node (parallel counts and scatter with
+// atomics; the order inside a bucket is then fixed by sorting it by (other two
+// nodes, face id)), so the copies of a face meet in one short sorted bucket.
 mg_status boundary_flags(const mg_mesh* m, std::vector<uint8_t>* flag)
 {
-  const int64_t N = m->n_nodes, E = m->n_elem;
+  const int64_t N = m->n_nodes, E = m->n_elem, F = 4 * E;
   const int32_t* conn = m->conn.data();
-  // node -> incident elements (the order inside a node's list does not matter:
-  // only the number of other tets holding a face is used)
+  auto face_of = [conn](int64_t f) {
+    const int32_t* c = conn + 4 * (f >> 2);
+    const int lf = (int)(f & 3);
+    return sorted_tri(c[face_vertex(lf, 0)], c[face_vertex(lf, 1)], c[face_vertex(lf, 2)]);
+  };
   std::vector<int64_t> start(N + 1, 0);
-  for (int64_t k = 0; k < 4 * E; ++k) start[conn[k] + 1]++;
+#pragma omp parallel for schedule(static)
+  for (int64_t f = 0; f < F; ++f) {
+    const int32_t x = face_of(f).a;
+#pragma omp atomic
+    start[x + 1]++;
+  }
   for (int64_t i = 0; i < N; ++i) start[i + 1] += start[i];
-  std::vector<int32_t> inc(4 * E);
+  std::vector<int32_t> bucket(F);
   {
     std::vector<int64_t> fill(start.begin(), start.end() - 1);
-    for (int64_t e = 0; e < E; ++e)
-      for (int v = 0; v < 4; ++v) inc[fill[conn[4 * e + v]]++] = (int32_t)e;
+#pragma omp parallel for schedule(static)
+    for (int64_t f = 0; f < F; ++f) {
+      const int32_t x = face_of(f).a;
+      int64_t pos;
+#pragma omp atomic capture
+      pos = fill[x]++;
+      bucket[pos] = (int32_t)f;
+    }
   }
-  flag->assign(4 * E, 0);
+  flag->assign(F, 0);
   int bad = 0;
-#pragma omp parallel for schedule(static) reduction(| : bad)
-  for (int64_t e = 0; e < E; ++e) {
-    const int32_t* c = conn + 4 * e;
-    for (int lf = 0; lf < 4; ++lf) {
-      const int32_t x = c[face_vertex(lf, 0)], y = c[face_vertex(lf, 1)], z = c[face_vertex(lf, 2)];
-      int others = 0;
+#pragma omp parallel reduction(| : bad)
+  {
+    struct Face {
+      int32_t b, c, id;  // the face's other two nodes (b < c), 4 e + local face
+      bool operator<(const Face& o) const { return b != o.b ? b < o.b : (c != o.c ? c < o.c : id < o.id); }
+    };
+    std::vector<Face> loc;
+#pragma omp for schedule(dynamic, 1024)
+    for (int64_t x = 0; x < N; ++x) {
+      loc.clear();
       for (int64_t k = start[x]; k < start[x + 1]; ++k) {
-        const int32_t e2 = inc[k];
-        if (e2 == e) continue;
-        const int32_t* c2 = conn + 4 * (int64_t)e2;
-        bool hy = false, hz = false;
-        for (int v = 0; v < 4; ++v) {
-          hy |= c2[v] == y;
-          hz |= c2[v] == z;
-        }
-        others += (hy && hz) ? 1 : 0;
+        const Tri t = face_of(bucket[k]);
+        loc.push_back(Face{t.b, t.c, bucket[k]});
       }
-      if (others >= 2) bad = 1;
-      (*flag)[4 * e + lf] = others == 0 ? 1 : 0;
+      std::sort(loc.begin(), loc.end());
+      for (size_t i = 0; i < loc.size();) {
+        size_t j = i + 1;
+        while (j < loc.size() && loc[j].b == loc[i].b && loc[j].c == loc[i].c) ++j;
+        if (j - i == 1) (*flag)[loc[i].id] = 1;
+        if (j - i > 2) bad = 1;
+        i = j;
+      }
     }
   }
   if (bad) return set_error(MG_ERR_BAD_MESH, "mg_lagrange_build: a face is shared by more than two tets");
