@@ -342,11 +342,23 @@ def run_only(a):
                 res[name + "_ms"] = statistics.median(ts)
         nb = 4 if a.order == 1 else 10
         F, nzb, nzs, rows = lg.n_faces, lg.nnz_b, lg.nnz_saddle, b.ndof + lg.n_multipliers
+        # the reference algorithm for B on one host core: face integrals (C restatement) and
+        # insertion-order sums into the pattern; the boundary-face search is outside the timing
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as orc
+        faces = orc.boundary_faces(m.conn)
+        dofs = mesh.elem_dofs()
+        t0 = time.perf_counter()
+        orc.lagrange(a.order, 1, m.xyz, m.conn, dofs, b.ndof, faces=faces)
+        cpu_s = time.perf_counter() - t0
+        cpu = {"value": F / cpu_s, "unit": "faces/s", "cores": 1, "kind": "port",
+               "sample": f"B of all {F} boundary faces once (face integrals in C, -O2; sums in numpy), {cpu_s:.2f} s"}
         byts = {"b_assemble": F * (8 + 16 + 3 * 32 + 2 * 3 * nb * 8) + nzb * 12 + 4 * F * 3 * nb,
                 "saddle_fill": nzs * 20, "saddle_spmv": spmv_bytes(rows, nzs, 8)}
         print(json.dumps({"only": "lagrange", "n": a.n, "order": a.order, "faces": F, "multipliers": lg.n_multipliers,
                           "nnz_b": nzb, "nnz_saddle": nzs, "build_s": build_s, **res,
                           **{k + "_gbs": byts[k] / res[k + "_ms"] / 1e6 for k in byts},
+                          "b_faces_per_s": F / (res["b_assemble_ms"] * 1e-3), "cpu_baseline": cpu,
                           "algorithmic_bytes": byts}))
         lg.close()
         return 0

@@ -209,18 +209,24 @@ def boundary_faces(conn, tris=None):
     conn = np.asarray(conn)
     tri = conn[:, FACE_PTS].reshape(-1, 3)
     key = np.sort(tri, axis=1)
-    _, inv, cnt = np.unique(key, axis=0, return_inverse=True, return_counts=True)
-    inv = inv.reshape(-1)
-    if cnt.max(initial=0) > 2:
+    order = np.lexsort((key[:, 2], key[:, 1], key[:, 0]))
+    ks = key[order]
+    head = np.ones(len(ks), dtype=bool)
+    head[1:] = np.any(ks[1:] != ks[:-1], axis=1)
+    run = np.cumsum(head) - 1
+    counts = np.bincount(run) if len(run) else np.zeros(0, dtype=np.int64)
+    if counts.max(initial=0) > 2:
         raise ValueError("a face is shared by more than two tets")
-    idx = np.nonzero(cnt[inv] == 1)[0]
+    cnt = np.empty(len(ks), dtype=np.int64)
+    cnt[order] = counts[run]
+    idx = np.nonzero(cnt == 1)[0]
     if tris is not None:
         want = {tuple(t) for t in np.sort(np.asarray(tris), axis=1).tolist()}
         idx = np.array([i for i in idx if tuple(key[i].tolist()) in want], dtype=np.int64)
     return (idx // 4).astype(np.int32), (idx % 4).astype(np.int32)
 
 
-def lagrange(order, quad, xyz, conn, dofs, ndof, tris=None):
+def lagrange(order, quad, xyz, conn, dofs, ndof, tris=None, faces=None):
     """B of opLA3dA with P1 multipliers on the boundary triangles.
 
     Multipliers: the nodes of the selected boundary faces, numbered by ascending
@@ -228,12 +234,13 @@ def lagrange(order, quad, xyz, conn, dofs, ndof, tris=None):
     order; dofMapStatic2d numbers P1 dofs by node).  Rows = multipliers, columns =
     field dofs; every face contributes its 3 x nb local block, zeros included
     (traitsMatrixBuilder.hpp:363-441 inserts the whole block), summed in element,
-    local-face, face-point, basis order.  Returns (lam_node, rowptr, colind,
+    local-face, face-point, basis order.  `faces` = (face_elem, face_local) from
+    boundary_faces, to skip that search.  Returns (lam_node, rowptr, colind,
     values, face_elem, face_local)."""
     xyz = np.ascontiguousarray(xyz, dtype=np.float64)
     conn = np.ascontiguousarray(conn, dtype=np.int32)
     nb = dofs.shape[1]
-    fe, fl = boundary_faces(conn, tris)
+    fe, fl = boundary_faces(conn, tris) if faces is None else faces
     nf = fe.shape[0]
     mats = np.empty((nf, 3, nb))
     if nf:
