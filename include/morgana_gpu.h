@@ -381,6 +381,9 @@ mg_status mg_lagrange_export_maps(const mg_lagrange* lg, int32_t* h_b_src_ptr, i
    B sums its blocks' contributions in the reference's insertion order
    (deterministic, no atomics). */
 mg_status mg_lagrange_assemble(mg_lagrange* lg, int32_t quad, double* d_b_values, void* stream);
+/* mg_lagrange_assemble with the values copied to host memory (nnz_b doubles):
+   what buildEpetraCrs hands to Epetra for localMatrixLA3d.  Synchronous. */
+mg_status mg_lagrange_assemble_host(mg_lagrange* lg, int32_t quad, double* h_b_values);
 /* Saddle values (nnz_saddle doubles, device) from K's values (the plan's CSR)
    and B's: [K + eye_field I, B^T; B, eye_lam I].  eye_lam must be 0 unless the
    pattern has the multiplier diagonal (lam_diag). */

@@ -111,6 +111,7 @@ SIGNATURES = {
     "mg_lagrange_pattern": [_P, _P, _P, _P, _P],
     "mg_lagrange_export_maps": [_P, _P, _P, _P],
     "mg_lagrange_assemble": [_P, _I32, _P, _P],
+    "mg_lagrange_assemble_host": [_P, _I32, _P],
     "mg_saddle_assemble": [_P, _P, _P, _D, _D, _P, _P],
     "mg_saddle_spmv": [_P, _P, _P, _P, _P],
     "mg_lagrange_apply": [_P, _P, _P, _P, _P],
@@ -470,6 +471,14 @@ class LagrangeBuilder:
         if t is None or not isinstance(t, torch.Tensor) or t.dtype != torch.float64 or not t.is_cuda \
                 or t.numel() < n or not t.is_contiguous():
             raise ValueError(f"{what}: a contiguous float64 CUDA tensor of at least {n} entries is needed")
+
+    def build_crs(self, quad: int = 1) -> Csr:
+        """B with host buffers (what buildEpetraCrs hands to Epetra for localMatrixLA3d)."""
+        _torch()
+        vals = np.empty(self.nnz_b, dtype=np.float64)
+        _check(lib().mg_lagrange_assemble_host(self._h, quad, _ptr(vals)), "mg_lagrange_assemble_host")
+        (rp, ci), _ = self.pattern()
+        return Csr(rp, ci, vals)
 
     def saddle(self, k_values, b_values, eye_field: float = 0.0, eye_lam: float = 0.0, out=None, stream=None):
         """Values of [K + eye_field I, B^T; B, eye_lam I] (torch float64, nnz_saddle)."""

@@ -128,6 +128,26 @@ mg_status mg_lagrange_assemble(mg_lagrange* lg, int32_t quad, double* d_b_values
   return MG_OK;
 }
 
+mg_status mg_lagrange_assemble_host(mg_lagrange* lg, int32_t quad, double* h_b_values)
+{
+  NvtxRange nvtx_range("mg_lagrange_assemble_host");
+  if (!lg) return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_assemble_host: null handle");
+  FaceRule rule{};
+  if (!face_rule(quad, &rule))
+    return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_assemble_host: face card must be 1, 3, 4 or 6");
+  if (lg->nnz_b == 0) return MG_OK;
+  if (!h_b_values) return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_assemble_host: null values");
+  double* d = nullptr;
+  MG_CUDA(cudaMalloc(&d, sizeof(double) * lg->nnz_b));
+  mg_status s = mg_lagrange_assemble(lg, quad, d, nullptr);
+  if (s == MG_OK) {
+    const cudaError_t e = cudaMemcpy(h_b_values, d, sizeof(double) * lg->nnz_b, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) s = cuda_error(e, "cudaMemcpy(B values)");
+  }
+  cudaFree(d);
+  return s;
+}
+
 mg_status mg_saddle_assemble(mg_lagrange* lg, const double* d_k_values, const double* d_b_values, double eye_field,
                              double eye_lam, double* d_values, void* stream)
 {

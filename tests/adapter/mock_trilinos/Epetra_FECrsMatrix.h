@@ -23,8 +23,18 @@ class Epetra_FECrsMatrix {
   int GlobalAssemble(bool callFillComplete = true)
   {
     filled_ = callFillComplete;
+    domain_ = range_ = map_.NumGlobalElements();
     return 0;
   }
+  int GlobalAssemble(const Epetra_Map& domainMap, const Epetra_Map& rangeMap, bool callFillComplete = true)
+  {
+    filled_ = callFillComplete;
+    domain_ = domainMap.NumGlobalElements();
+    range_ = rangeMap.NumGlobalElements();
+    return 0;
+  }
+  int NumGlobalDomain() const { return domain_; }
+  int NumGlobalRange() const { return range_; }
   bool Filled() const { return filled_; }
   const std::map<int, std::vector<std::pair<int, double>>>& Rows() const { return rows_; }
  private:
@@ -32,4 +42,5 @@ class Epetra_FECrsMatrix {
   std::vector<int> alloc_;
   std::map<int, std::vector<std::pair<int, double>>> rows_;
   bool filled_ = false;
+  int domain_ = 0, range_ = 0;
 };

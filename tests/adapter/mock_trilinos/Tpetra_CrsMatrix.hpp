@@ -27,7 +27,19 @@ template <class Scalar = double, class LO = int, class GO = long long, class Nod
     auto& row = rows_[globalRow];
     for (LO k = 0; k < numEnt; ++k) row.emplace_back(inds[k], vals[k]);
   }
-  void fillComplete() { filled_ = true; }
+  void fillComplete()
+  {
+    filled_ = true;
+    domain_ = range_ = map_->getGlobalNumElements();
+  }
+  void fillComplete(const Teuchos::RCP<const map_type>& domainMap, const Teuchos::RCP<const map_type>& rangeMap)
+  {
+    filled_ = true;
+    domain_ = domainMap->getGlobalNumElements();
+    range_ = rangeMap->getGlobalNumElements();
+  }
+  size_t DomainSize() const { return domain_; }
+  size_t RangeSize() const { return range_; }
   bool isFillComplete() const { return filled_; }
   const std::map<GO, std::vector<std::pair<GO, Scalar>>>& Rows() const { return rows_; }
  private:
@@ -35,5 +47,6 @@ template <class Scalar = double, class LO = int, class GO = long long, class Nod
   std::vector<size_t> alloc_;
   std::map<GO, std::vector<std::pair<GO, Scalar>>> rows_;
   bool filled_ = false;
+  size_t domain_ = 0, range_ = 0;
 };
 }  // namespace Tpetra

@@ -126,3 +126,56 @@ def test_empty_selection_gives_k():
     assert B.numel() == 0
     S = lg.saddle(K, B)
     assert torch.equal(S, K)
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_trilinos_adapters_for_multipliers(tmp_path, order):
+    """buildEpetraLagrange / buildTpetraLagrange rows (test doubles of the
+    Trilinos classes) and GpuSaddleOperator::Apply against the oracle."""
+    import os
+    import subprocess
+    from morganapublic_gb300 import build as mgbuild
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    src = os.path.join(root, "tests", "adapter", "adapter_check.cpp")
+    lib = mgbuild.build()
+    exe = str(tmp_path / "adapter_check")
+    subprocess.run(["g++", "-std=c++17", "-O1", "-I" + os.path.join(root, "include"),
+                    "-I" + os.path.join(root, "tests", "adapter", "mock_trilinos"),
+                    "-I" + os.path.join(mgbuild.CUDA_HOME, "include"), src, "-o", exe, lib,
+                    "-L" + os.path.join(mgbuild.CUDA_HOME, "lib64"), "-lcudart", "-Wl,-rpath," + os.path.dirname(lib),
+                    "-Wl,-rpath," + os.path.join(mgbuild.CUDA_HOME, "lib64")], check=True)
+    m = meshgen.kuhn_cube(4 if order == 1 else 3, jitter=0.2, seed=41, permute=True)
+    kappa = meshgen.lognormal(len(m.conn), 1.0, 41)
+    dofs, rp, ci, kref = orc.full_operator("stiff_kappa", order, 4, m.xyz, m.conn, coeff=kappa)
+    ndof = len(rp) - 1
+    lam, brp, bci, bref, _, _ = orc.lagrange(order, 1, m.xyz, m.conn, dofs, ndof)
+    n = ndof + len(lam)
+    x = np.random.default_rng(4).uniform(-1, 1, n)
+    with open(tmp_path / "in.bin", "wb") as f:
+        np.array([len(m.xyz), len(m.conn), order], dtype=np.int64).tofile(f)
+        m.xyz.astype(np.float64).tofile(f)
+        m.conn.astype(np.int32).tofile(f)
+        kappa.astype(np.float64).tofile(f)
+        x.tofile(f)
+    subprocess.run([exe, str(tmp_path / "in.bin"), str(tmp_path / "out.bin"), "lagrange"], check=True, timeout=300)
+    raw = open(tmp_path / "out.bin", "rb").read()
+    nl, nz = np.frombuffer(raw[:16], dtype=np.int64)
+    off = 16
+    rp_g = np.frombuffer(raw[off:off + 4 * (nl + 1)], dtype=np.int32); off += 4 * (nl + 1)
+    ci_g = np.frombuffer(raw[off:off + 4 * nz], dtype=np.int32); off += 4 * nz
+    va_g = np.frombuffer(raw[off:off + 8 * nz], dtype=np.float64); off += 8 * nz
+    y_g = np.frombuffer(raw[off:off + 8 * n], dtype=np.float64)
+    assert nl == len(lam) and np.array_equal(rp_g, brp) and np.array_equal(ci_g, bci)
+    assert row_scaled_err(brp, bref, va_g) <= 1e-12
+    srp, sci, sref = orc.saddle(rp, ci, kref, brp, bci, bref, ndof)
+    yref = orc.csr_matvec(srp, sci, sref, x)
+    assert np.abs(y_g - yref).max() <= 1e-12 * np.abs(yref).max()
+
+
+def test_host_buffer_b_equals_device_b():
+    m, mesh, b, lg, _ = _setup(3, 2, 26)
+    dev = lg.assemble(quad=4).cpu().numpy()
+    host = lg.build_crs(quad=4)
+    (brp, bci), _ = lg.pattern()
+    assert np.array_equal(host.rowptr, brp) and np.array_equal(host.colind, bci)
+    assert np.array_equal(host.values, dev)
