@@ -15,13 +15,12 @@ def pytest_configure(config):
 
 @pytest.fixture(scope="session", autouse=True)
 def _built():
-    """Builds the product library and the oracle once per session if missing."""
+    """Brings the product library and the oracle up to date once per session
+    (both builds are incremental: they recompile only what changed)."""
     import morganapublic_gb300.build as b
     import oracle as orc
-    if not os.path.exists(b.LIB):
-        b.build()
-    if not os.path.exists(orc.LIB_PATH):
-        orc.build()
+    b.build()
+    orc.build()
     yield
 
 
