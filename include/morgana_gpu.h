@@ -316,7 +316,7 @@ mg_status mg_adjoint_grad(mg_plan* plan, const double* d_u, const double* d_lamb
 
 /* ------------------------------------------- boundary multipliers -- */
 
-/* Dirichlet data the reference way: P1 Lagrange multipliers on boundary
+/* Dirichlet data the reference way: P1 or P0 Lagrange multipliers on boundary
    triangles, coupled to the field by opLA3dA (u . q over each boundary face),
    and the saddle system [K B^T; B 0].  FP64 throughout: the boundary work is
    O(n^2) against the O(n^3) of the volume operator. */
@@ -340,12 +340,19 @@ typedef struct {
    in element then local-face order.  h_tris (n_tris x 3 node ids, any vertex
    order) selects the boundary triangles that carry multipliers, the geoId
    filter of the test field (feStaticField2d with dms2d_geoIdMode); NULL = all
-   boundary faces.  Multipliers = the P1 dofs of the selected triangles, one per
-   node, numbered by ascending node id (meshDoctor2d::removeUnusedPoints,
-   src/morganaGeometry/meshDoctor2d.hpp:339-500, then dofMapStatic2d).
-   B (n_multipliers x ndof): each face inserts its full 3 x nb block, explicit
-   zeros included, as traitsMatrixBuilder::buildEpetraCrs does for
-   localMatrixLA3d (src/morganaFiniteElements/localMatrixLA3d.hpp:292-322).
+   boundary faces.  Multipliers (the test field of opLA3dA):
+   - test_order 1 (fePr2d<1>): the P1 dofs of the selected triangles, one per
+     node, numbered by ascending node id (meshDoctor2d::removeUnusedPoints,
+     src/morganaGeometry/meshDoctor2d.hpp:339-500, then
+     src/morganaFields/dofMapStatic2d.hpp:1166-1380);
+   - test_order 0 (fePr2d<0>): one per triangle, numbered in the boundary
+     grid's element order: the order of h_tris (the Gmsh triangles, whose ids
+     the boundary elements keep: src/morganaGeometry/meshInit3d.hpp:400-430),
+     or the face order when h_tris is NULL.
+   B (n_multipliers x ndof): each face inserts its full nt x nb block (nt = 3
+   for P1, 1 for P0), explicit zeros included, as
+   traitsMatrixBuilder::buildEpetraCrs does for localMatrixLA3d
+   (src/morganaFiniteElements/localMatrixLA3d.hpp:292-322).
    Saddle: [K B^T; B 0] (epetraSaddleAssembler::setDiagMatrix + setSymmMatrix,
    src/morganaTrilinos/epetraSaddleAssembler.cpp), with K the plan's pattern;
    lam_diag != 0 adds the diagonal of the multiplier block to the pattern
@@ -354,12 +361,13 @@ typedef struct {
    selected triangle is not a boundary face; MG_ERR_INVALID_ARG for a repeated
    triangle or a node id out of range; MG_ERR_SIZE above 2^31 - 1 entries.
    The handle keeps a pointer to the plan: destroy it before the plan. */
-mg_status mg_lagrange_build(mg_plan* plan, int64_t n_tris, const int32_t* h_tris, int32_t lam_diag,
-                            mg_lagrange** out);
+mg_status mg_lagrange_build(mg_plan* plan, int32_t test_order, int64_t n_tris, const int32_t* h_tris,
+                            int32_t lam_diag, mg_lagrange** out);
 mg_status mg_lagrange_destroy(mg_lagrange* lg);
 mg_status mg_lagrange_get_info(const mg_lagrange* lg, mg_lagrange_info* info);
-/* h_lam_node (n_multipliers): node of each multiplier; h_face_elem,
-   h_face_local (n_faces): the selected faces; any pointer may be NULL. */
+/* h_lam_node (n_multipliers): node (P1) or selected face (P0, an index into
+   the face list) of each multiplier; h_face_elem, h_face_local (n_faces): the
+   selected faces; any pointer may be NULL. */
 mg_status mg_lagrange_export(const mg_lagrange* lg, int32_t* h_lam_node, int32_t* h_face_elem,
                              int32_t* h_face_local);
 /* CSR of B (n_multipliers + 1, nnz_b) and of the saddle matrix
@@ -368,16 +376,16 @@ mg_status mg_lagrange_pattern(const mg_lagrange* lg, int32_t* h_b_rowptr, int32_
                               int32_t* h_s_rowptr, int32_t* h_s_colind);
 
 /* The gather maps the kernels read (for host-side checks of the data flow):
-   h_b_src_ptr (nnz_b + 1) and h_b_src (n_faces * 3 * nb): B entry k sums the
+   h_b_src_ptr (nnz_b + 1) and h_b_src (n_faces * nt * nb): B entry k sums the
    face-matrix entries h_b_src[h_b_src_ptr[k] .. h_b_src_ptr[k+1]), each
-   (face * 3 + face vertex) * nb + basis, in that order; h_s_src (nnz_saddle):
+   (face * nt + test basis) * nb + field basis, in that order; h_s_src (nnz_saddle):
    saddle entry k copies K entry h_s_src[k] (>= 0), B entry -(h_s_src[k] + 1),
    or the multiplier diagonal (INT32_MIN).  Any pointer may be NULL. */
 mg_status mg_lagrange_export_maps(const mg_lagrange* lg, int32_t* h_b_src_ptr, int32_t* h_b_src,
                                   int32_t* h_s_src);
 
 /* Values of B (nnz_b doubles, device) with the face card quad (MG_FACE_QUAD_*):
-   one thread per face computes its 3 x nb block, then one thread per entry of
+   one thread per face computes its nt x nb block, then one thread per entry of
    B sums its blocks' contributions in the reference's insertion order
    (deterministic, no atomics). */
 mg_status mg_lagrange_assemble(mg_lagrange* lg, int32_t quad, double* d_b_values, void* stream);

@@ -104,7 +104,7 @@ SIGNATURES = {
     "mg_cg_refined": [_P, _P, _P, _P, _P, _D, _I32, _I32, _D, _I32, ctypes.POINTER(CgInfo), _P],
     "mg_cg_solve_noalloc": [_P, _P, _P, _P, _D, _I32, _I32, ctypes.POINTER(CgInfo), _P],
     "mg_adjoint_grad": [_P, _P, _P, _I32, _P, _P],
-    "mg_lagrange_build": [_P, _I64, _P, _I32, ctypes.POINTER(_P)],
+    "mg_lagrange_build": [_P, _I32, _I64, _P, _I32, ctypes.POINTER(_P)],
     "mg_lagrange_destroy": [_P],
     "mg_lagrange_get_info": [_P, ctypes.POINTER(LagrangeInfo)],
     "mg_lagrange_export": [_P, _P, _P, _P],
@@ -414,14 +414,17 @@ class LagrangeBuilder:
     [K B^T; B 0] of epetraSaddleAssembler.  Keeps a reference to its
     MatrixBuilder, whose plan must outlive it."""
 
-    def __init__(self, builder: MatrixBuilder, tris=None, lam_diag: bool = False):
+    def __init__(self, builder: MatrixBuilder, tris=None, lam_diag: bool = False, test_order: int = 1):
         """tris: (k, 3) node ids of the boundary triangles that carry multipliers
-        (the test field's geoId filter); None = every boundary face."""
+        (the test field's geoId filter); None = every boundary face.
+        test_order: 1 = P1 multipliers (one per boundary node), 0 = P0 (one per
+        triangle, in the order of tris)."""
         self.builder = builder
+        self.test_order = test_order
         t = None if tris is None else np.ascontiguousarray(tris, dtype=np.int32).reshape(-1, 3)
         h = _P()
-        _check(lib().mg_lagrange_build(builder._h, 0 if t is None else t.shape[0], _ptr(t), int(lam_diag),
-                                       ctypes.byref(h)), "mg_lagrange_build")
+        _check(lib().mg_lagrange_build(builder._h, int(test_order), 0 if t is None else t.shape[0], _ptr(t),
+                                       int(lam_diag), ctypes.byref(h)), "mg_lagrange_build")
         self._h = h
         info = LagrangeInfo()
         _check(lib().mg_lagrange_get_info(h, ctypes.byref(info)), "mg_lagrange_get_info")
@@ -429,7 +432,7 @@ class LagrangeBuilder:
         self.ndof, self.nnz_b, self.nnz_saddle = info.ndof, info.nnz_b, info.nnz_saddle
 
     def multipliers(self):
-        """(node of each multiplier, face element, face local index)."""
+        """(node (P1) or face index (P0) of each multiplier, face element, face local index)."""
         lam = np.empty(self.n_multipliers, dtype=np.int32)
         fe = np.empty(self.n_faces, dtype=np.int32)
         fl = np.empty(self.n_faces, dtype=np.int32)
@@ -449,8 +452,9 @@ class LagrangeBuilder:
     def export_maps(self):
         """(b_src_ptr, b_src, s_src): the gather maps of the B and saddle kernels."""
         nb = 4 if self.builder.mesh.order == 1 else 10
+        nt = 3 if self.test_order == 1 else 1
         bp = np.empty(self.nnz_b + 1, dtype=np.int32)
-        bs = np.empty(self.n_faces * 3 * nb, dtype=np.int32)
+        bs = np.empty(self.n_faces * nt * nb, dtype=np.int32)
         ss = np.empty(self.nnz_saddle, dtype=np.int32)
         _check(lib().mg_lagrange_export_maps(self._h, _ptr(bp), _ptr(bs), _ptr(ss)), "mg_lagrange_export_maps")
         return bp, bs, ss

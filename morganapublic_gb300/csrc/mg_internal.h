@@ -207,13 +207,14 @@ struct mg_plan {
 struct mg_lagrange {
   mg_plan* plan = nullptr;
   int order = 1, nb = 4;
+  int test_order = 1, nt = 3;  // multiplier basis: P1 (3 per face) or P0 (1 per face)
   bool lam_diag = false;  // the saddle pattern holds the multiplier block's diagonal
   int64_t ndof = 0, n_faces = 0, nl = 0, nnz_b = 0, nnz_s = 0;
   std::vector<int32_t> face_elem, face_local;  // selected boundary faces, element then local-face order
-  std::vector<int32_t> lam_node;               // node of each multiplier, ascending
+  std::vector<int32_t> lam_node;               // node (P1, ascending) or face (P0) of each multiplier
   std::vector<int32_t> b_rowptr, b_colind;     // B: nl x ndof
   // per B entry k, the face-matrix entries it sums, b_src[b_src_ptr[k] .. b_src_ptr[k+1]),
-  // each (f * 3 + a) * nb + i, ascending (the reference's insertion order)
+  // each (f * nt + a) * nb + i, ascending (the reference's insertion order)
   std::vector<int32_t> b_src_ptr, b_src;
   std::vector<int32_t> s_rowptr, s_colind;     // saddle: (ndof + nl) rows
   // per saddle entry: the K entry it copies (>= 0) or -(k + 1) for B entry k
@@ -222,7 +223,7 @@ struct mg_lagrange {
   int2* d_faces = nullptr;  // (element, local face)
   int32_t *d_b_rowptr = nullptr, *d_b_colind = nullptr, *d_b_src_ptr = nullptr, *d_b_src = nullptr;
   int32_t *d_s_rowptr = nullptr, *d_s_colind = nullptr, *d_s_src = nullptr;
-  double* d_face_mat = nullptr;  // n_faces * 3 * nb
+  double* d_face_mat = nullptr;  // n_faces * nt * nb
   bool on_device = false;
 };
 

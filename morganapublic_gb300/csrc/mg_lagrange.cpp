@@ -6,10 +6,12 @@
 //  - boundary faces: faces of exactly one tet (connect3d getFaceIsBoundary),
 //    visited in element then local-face order (the builder's loop over grid3d,
 //    localMatrixLA3d::matrix, src/morganaFiniteElements/localMatrixLA3d.hpp:292-322);
-//  - multipliers: the nodes of the boundary triangles, compacted in ascending
-//    node id (meshDoctor2d::removeUnusedPoints, meshDoctor2d.hpp:339-500), one P1
-//    dof each;
-//  - B: every face inserts its 3 x nb block (rows: the face's multipliers,
+//  - multipliers (fePr2d<1>): the nodes of the boundary triangles, compacted in
+//    ascending node id (meshDoctor2d::removeUnusedPoints, meshDoctor2d.hpp:339-500),
+//    numbered in that order (dofMapStatic2d.hpp:1166-1380); (fePr2d<0>): one per
+//    triangle, in the boundary grid's element order -- the order of the given
+//    triangles, whose ids the boundary elements keep (meshInit3d.hpp:400-430);
+//  - B: every face inserts its nt x nb block (rows: the face's multipliers,
 //    columns: all nb dofs of the tet, zeros kept), duplicates summed in insertion
 //    order (traitsMatrixBuilder.hpp:363-441, Epetra_FECrsMatrix::InsertGlobalValues);
 //  - saddle: K on the field block, B on (multiplier, field) and B^T on (field,
@@ -112,13 +114,17 @@ mg_status boundary_flags(const mg_mesh* m, std::vector<uint8_t>* flag)
 
 }  // namespace
 
-static mg_status build_lagrange(mg_lagrange* lg, int64_t n_tris, const int32_t* h_tris, bool lam_diag)
+static mg_status build_lagrange(mg_lagrange* lg, int test_order, int64_t n_tris, const int32_t* h_tris,
+                                bool lam_diag)
 {
   const mg_plan* p = lg->plan;
   const mg_mesh* m = p->mesh;
   const int nb = m->nb;
   const int64_t E = m->n_elem, N = m->n_nodes, nd = m->ndof;
   lg->order = m->order;
+  lg->test_order = test_order;
+  lg->nt = test_order == 1 ? 3 : 1;
+  const int nt = lg->nt;
   lg->lam_diag = lam_diag;
   lg->nb = nb;
   lg->ndof = nd;
@@ -131,31 +137,42 @@ static mg_status build_lagrange(mg_lagrange* lg, int64_t n_tris, const int32_t* 
   for (int64_t k = 0; k < 4 * E; ++k)
     if (flag[k]) ids.push_back((int32_t)k);
 
-  // selection by the given triangles
+  // selection by the given triangles; `rank` = each kept face's position in the
+  // list (the boundary grid's element order, which numbers P0 multipliers)
+  std::vector<int64_t> rank;
   if (h_tris) {
-    std::vector<Tri> want(n_tris);
+    std::vector<std::pair<Tri, int64_t>> want(n_tris);
     for (int64_t t = 0; t < n_tris; ++t) {
       const int32_t* v = h_tris + 3 * t;
       for (int s = 0; s < 3; ++s)
         if (v[s] < 0 || v[s] >= N) return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_build: triangle node id out of range");
-      want[t] = sorted_tri(v[0], v[1], v[2]);
+      want[t] = {sorted_tri(v[0], v[1], v[2]), t};
     }
-    std::sort(want.begin(), want.end());
-    if (std::adjacent_find(want.begin(), want.end()) != want.end())
-      return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_build: a triangle is listed twice");
+    std::sort(want.begin(), want.end(), [](const auto& x, const auto& y) { return x.first < y.first; });
+    for (int64_t t = 1; t < n_tris; ++t)
+      if (want[t].first == want[t - 1].first)
+        return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_build: a triangle is listed twice");
     std::vector<int32_t> kept;
     for (const int32_t id : ids) {
       const int32_t* c = m->conn.data() + 4 * (int64_t)(id / 4);
       const int lf = id % 4;
       const Tri t = sorted_tri(c[face_vertex(lf, 0)], c[face_vertex(lf, 1)], c[face_vertex(lf, 2)]);
-      if (std::binary_search(want.begin(), want.end(), t)) kept.push_back(id);
+      auto it = std::lower_bound(want.begin(), want.end(), t,
+                                 [](const std::pair<Tri, int64_t>& x, const Tri& y) { return x.first < y; });
+      if (it != want.end() && it->first == t) {
+        kept.push_back(id);
+        rank.push_back(it->second);
+      }
     }
     if ((int64_t)kept.size() != n_tris)
       return set_error(MG_ERR_BAD_MESH, "mg_lagrange_build: a listed triangle is not a boundary face of the mesh");
     ids.swap(kept);
+  } else {
+    rank.resize(ids.size());
+    std::iota(rank.begin(), rank.end(), (int64_t)0);
   }
   const int64_t nf = (int64_t)ids.size();
-  if (nf * 3 * nb > kInt32Max) return set_error(MG_ERR_SIZE, "mg_lagrange_build: too many boundary faces");
+  if (nf * nt * nb > kInt32Max) return set_error(MG_ERR_SIZE, "mg_lagrange_build: too many boundary faces");
   lg->n_faces = nf;
   lg->face_elem.resize(nf);
   lg->face_local.resize(nf);
@@ -164,18 +181,25 @@ static mg_status build_lagrange(mg_lagrange* lg, int64_t n_tris, const int32_t* 
     lg->face_local[f] = ids[f] % 4;
   }
 
-  // multipliers: nodes of the selected faces, ascending
-  std::vector<int32_t> lam_of(N, -1);
-  for (int64_t f = 0; f < nf; ++f) {
-    const int32_t* c = m->conn.data() + 4 * (int64_t)lg->face_elem[f];
-    for (int a = 0; a < 3; ++a) lam_of[c[face_vertex(lg->face_local[f], a)]] = 0;
-  }
+  // multipliers: P1 the nodes of the selected faces, ascending; P0 one per face,
+  // in the order of `rank`
+  std::vector<int32_t> lam_of;
   lg->lam_node.clear();
-  for (int64_t i = 0; i < N; ++i)
-    if (lam_of[i] == 0) {
-      lam_of[i] = (int32_t)lg->lam_node.size();
-      lg->lam_node.push_back((int32_t)i);
+  if (test_order == 1) {
+    lam_of.assign(N, -1);
+    for (int64_t f = 0; f < nf; ++f) {
+      const int32_t* c = m->conn.data() + 4 * (int64_t)lg->face_elem[f];
+      for (int a = 0; a < 3; ++a) lam_of[c[face_vertex(lg->face_local[f], a)]] = 0;
     }
+    for (int64_t i = 0; i < N; ++i)
+      if (lam_of[i] == 0) {
+        lam_of[i] = (int32_t)lg->lam_node.size();
+        lg->lam_node.push_back((int32_t)i);
+      }
+  } else {
+    lg->lam_node.resize(nf);
+    for (int64_t f = 0; f < nf; ++f) lg->lam_node[rank[f]] = (int32_t)f;
+  }
   const int64_t nl = (int64_t)lg->lam_node.size();
   lg->nl = nl;
 
@@ -183,18 +207,19 @@ static mg_status build_lagrange(mg_lagrange* lg, int64_t n_tris, const int32_t* 
   // sources are generated ascending, so each entry's list is in insertion order
   struct Pair {
     uint64_t key;  // row << 32 | column
-    int32_t src;   // (f * 3 + a) * nb + i
+    int32_t src;   // (f * nt + a) * nb + i
     bool operator<(const Pair& o) const { return key != o.key ? key < o.key : src < o.src; }
   };
-  std::vector<Pair> pairs(nf * 3 * nb);
+  std::vector<Pair> pairs(nf * nt * nb);
 #pragma omp parallel for schedule(static)
   for (int64_t f = 0; f < nf; ++f) {
     const int64_t e = lg->face_elem[f];
     const int32_t* c = m->conn.data() + 4 * e;
-    for (int a = 0; a < 3; ++a) {
-      const uint64_t row = (uint64_t)lam_of[c[face_vertex(lg->face_local[f], a)]];
+    for (int a = 0; a < nt; ++a) {
+      const uint64_t row = test_order == 1 ? (uint64_t)lam_of[c[face_vertex(lg->face_local[f], a)]]
+                                           : (uint64_t)rank[f];
       for (int i = 0; i < nb; ++i) {
-        const int64_t s = (f * 3 + a) * nb + i;
+        const int64_t s = (f * nt + a) * nb + i;
         pairs[s] = Pair{row << 32 | (uint64_t)(uint32_t)m->dofs[e * nb + i], (int32_t)s};
       }
     }
@@ -305,7 +330,8 @@ mg_status lagrange_device(mg_lagrange* lg)
   if (s == MG_OK) s = upload(&lg->d_s_colind, lg->s_colind);
   if (s == MG_OK) s = upload(&lg->d_s_src, lg->s_src);
   if (s == MG_OK) {
-    const cudaError_t e = cudaMalloc(&lg->d_face_mat, sizeof(double) * std::max<int64_t>(lg->n_faces * 3 * lg->nb, 1));
+    const cudaError_t e =
+        cudaMalloc(&lg->d_face_mat, sizeof(double) * std::max<int64_t>(lg->n_faces * lg->nt * lg->nb, 1));
     if (e != cudaSuccess) s = cuda_error(e, "cudaMalloc(face matrices)");
   }
   if (s != MG_OK) {
@@ -322,10 +348,13 @@ using namespace mg;
 
 extern "C" {
 
-mg_status mg_lagrange_build(mg_plan* plan, int64_t n_tris, const int32_t* h_tris, int32_t lam_diag, mg_lagrange** out)
+mg_status mg_lagrange_build(mg_plan* plan, int32_t test_order, int64_t n_tris, const int32_t* h_tris,
+                            int32_t lam_diag, mg_lagrange** out)
 {
   NvtxRange nvtx_range("mg_lagrange_build");
   if (!plan || !out) return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_build: null argument");
+  if (test_order != 0 && test_order != 1)
+    return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_build: multipliers are P1 (1) or P0 (0)");
   if (n_tris < 0 || (n_tris > 0 && !h_tris)) return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_build: bad triangle list");
   *out = nullptr;
   mg_lagrange* lg = new (std::nothrow) mg_lagrange();
@@ -333,7 +362,7 @@ mg_status mg_lagrange_build(mg_plan* plan, int64_t n_tris, const int32_t* h_tris
   lg->plan = plan;
   mg_status s;
   try {
-    s = build_lagrange(lg, n_tris, h_tris, lam_diag != 0);
+    s = build_lagrange(lg, test_order, n_tris, h_tris, lam_diag != 0);
   } catch (const std::bad_alloc&) {
     s = set_error(MG_ERR_ALLOC, "mg_lagrange_build: out of host memory");
   }

@@ -2,7 +2,7 @@
 // [K B^T; B 0], and the products with them.
 //
 // B is assembled in two deterministic passes:
-//   k_face_matrix  one thread per boundary face: its 3 x nb local matrix
+//   k_face_matrix  one thread per boundary face: its nt x nb local matrix
 //                  (mg_lagrange.cuh) into a staging array, face-major;
 //   k_gather_sum   one thread per entry of B: the staged values it sums, in the
 //                  reference's insertion order (element, local face, face
@@ -29,7 +29,7 @@ int grid_for(int64_t n)
   return (int)std::max<int64_t>(1, std::min<int64_t>(b, 65535));
 }
 
-template <int NB>
+template <int NB, int NT>
 __global__ void __launch_bounds__(kFaceThreads) k_face_matrix(int64_t n_faces, const int2* __restrict__ faces,
                                                           const int4* __restrict__ conn,
                                                           const double4_32a* __restrict__ xyz, FaceRule rule,
@@ -47,11 +47,11 @@ __global__ void __launch_bounds__(kFaceThreads) k_face_matrix(int64_t n_faces, c
       P[a][1] = p.y;
       P[a][2] = p.z;
     }
-    double mat[3 * NB];
-    face_matrix<NB>(P, fe.y, rule, mat);
-    double* o = out + f * (3 * NB);
+    double mat[NT * NB];
+    face_matrix<NB, NT>(P, fe.y, rule, mat);
+    double* o = out + f * (NT * NB);
 #pragma unroll
-    for (int k = 0; k < 3 * NB; ++k) o[k] = mat[k];
+    for (int k = 0; k < NT * NB; ++k) o[k] = mat[k];
   }
 }
 
@@ -117,10 +117,15 @@ mg_status mg_lagrange_assemble(mg_lagrange* lg, int32_t quad, double* d_b_values
   cudaStream_t st = (cudaStream_t)stream;
   const mg_mesh* m = lg->plan->mesh;
   const int g = grid_for(lg->n_faces);
-  if (lg->nb == 4)
-    k_face_matrix<4><<<g, kFaceThreads, 0, st>>>(lg->n_faces, lg->d_faces, m->d_conn, m->d_xyz, rule, lg->d_face_mat);
+  const int64_t F = lg->n_faces;
+  if (lg->nb == 4 && lg->nt == 3)
+    k_face_matrix<4, 3><<<g, kFaceThreads, 0, st>>>(F, lg->d_faces, m->d_conn, m->d_xyz, rule, lg->d_face_mat);
+  else if (lg->nb == 4)
+    k_face_matrix<4, 1><<<g, kFaceThreads, 0, st>>>(F, lg->d_faces, m->d_conn, m->d_xyz, rule, lg->d_face_mat);
+  else if (lg->nt == 3)
+    k_face_matrix<10, 3><<<g, kFaceThreads, 0, st>>>(F, lg->d_faces, m->d_conn, m->d_xyz, rule, lg->d_face_mat);
   else
-    k_face_matrix<10><<<g, kFaceThreads, 0, st>>>(lg->n_faces, lg->d_faces, m->d_conn, m->d_xyz, rule, lg->d_face_mat);
+    k_face_matrix<10, 1><<<g, kFaceThreads, 0, st>>>(F, lg->d_faces, m->d_conn, m->d_xyz, rule, lg->d_face_mat);
   MG_CUDA(cudaGetLastError());
   k_gather_sum<<<grid_for(lg->nnz_b), kFaceThreads, 0, st>>>(lg->nnz_b, lg->d_b_src_ptr, lg->d_b_src, lg->d_face_mat,
                                                           d_b_values);

@@ -3,9 +3,9 @@
 // the tests compare with the oracle on the CPU.  Plain FP64 arithmetic and
 // integer tables only (no CUDA types, no static arrays).
 //
-// Face f is local face lf of tet e.  Its local matrix, rows = the face's three
-// vertices in face order (the P1 multiplier basis of the boundary triangle),
-// columns = the tet's nb field basis functions, is
+// Face f is local face lf of tet e.  Its local matrix, rows = the test basis of
+// the boundary triangle (P1: the face's three vertices in face order; P0: the
+// constant 1), columns = the tet's nb field basis functions, is
 //   mat[a * nb + i] = sum_q w_q |Vx ^ Vy| psi_a(q) phi_i(q)
 // (integratorOLA3d_STD.hpp:102-124 around opLA3dA.hpp:86-112).  On the face the
 // tet's barycentric coordinates are the face's own (lambda_a at vertex
@@ -79,8 +79,9 @@ inline bool face_rule(int quad, FaceRule* r)
 }
 
 // Local matrix of local face lf; P[a] = coordinates of face vertex a (face
-// order), mat = 3 x NB, row-major (face vertex, field basis).
-template <int NB>
+// order), mat = NT x NB, row-major (test basis, field basis); NT = 3 (P1 test)
+// or 1 (P0 test).
+template <int NB, int NT>
 MG_HD inline void face_matrix(const double P[3][3], int lf, const FaceRule& r, double* mat)
 {
   double vx[3], vy[3];
@@ -92,7 +93,8 @@ MG_HD inline void face_matrix(const double P[3][3], int lf, const FaceRule& r, d
   const double n1 = vx[2] * vy[0] - vx[0] * vy[2];
   const double n2 = vx[0] * vy[1] - vx[1] * vy[0];
   const double area2 = sqrt(n0 * n0 + n1 * n1 + n2 * n2);
-  for (int k = 0; k < 3 * NB; ++k) mat[k] = 0.0;
+  static_assert(NT == 1 || NT == 3, "P0 or P1 test basis");
+  for (int k = 0; k < NT * NB; ++k) mat[k] = 0.0;
   for (int q = 0; q < r.nq; ++q) {
     const double lam[3] = {1.0 - r.x[q] - r.y[q], r.x[q], r.y[q]};
     double L[4] = {0.0, 0.0, 0.0, 0.0};
@@ -105,8 +107,8 @@ MG_HD inline void face_matrix(const double P[3][3], int lf, const FaceRule& r, d
       for (int j = 0; j < 6; ++j) phi[4 + j] = 4.0 * L[edge_vertex(j, 0)] * L[edge_vertex(j, 1)];
     }
     const double s = area2 * r.w[q];
-    for (int a = 0; a < 3; ++a) {
-      const double c = lam[a] * s;
+    for (int a = 0; a < NT; ++a) {
+      const double c = (NT == 3 ? lam[a] : 1.0) * s;
       for (int i = 0; i < NB; ++i) mat[a * NB + i] += phi[i] * c;
     }
   }

@@ -733,7 +733,9 @@ static const double REF_TET[4][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}}
    loop of integratorOLA3d_STD.hpp:102-124 around the integrand of
    opLA3dA.hpp:86-112,
      mat[a * nb + i] = sum_q (phi_i(Yv) psi_a(Ys)) |Vx ^ Vy| w_q,
-   a over the face's points in face order, i over the tet's nb basis functions.
+   i over the tet's nb basis functions and a over the test basis of the
+   boundary triangle: test_order 1 (fePr2d<1>) the face's points in face order,
+   test_order 0 (fePr2d<0>) the one constant psi = 1.
    Vx, Vy: derivatives of the linear map of the reference triangle onto the
    face (geoMapInterface.hpp:25-90, point 3 first).  Yv: the same map onto the
    reference tet's face (supportLagrange3d mapVolumeY).  Ys: the point in the
@@ -741,9 +743,11 @@ static const double REF_TET[4][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}}
    the boundary triangle has the face's vertices, so psi_a(Ys) is the face
    barycentric a of the point, which this restatement uses directly (the two
    agree to rounding). */
-int or_face_matrix(int order, int prec, const double *xyz, const int32_t *nodes4, int lf, double *mat)
+int or_face_matrix(int order, int test_order, int prec, const double *xyz, const int32_t *nodes4, int lf,
+                   double *mat)
 {
-  if (lf < 0 || lf > 3) return OR_ERR_ARG;
+  if (lf < 0 || lf > 3 || (test_order != 0 && test_order != 1)) return OR_ERR_ARG;
+  const int nt = test_order == 1 ? 3 : 1;
   double Y[12], W[6];
   const int nq = or_tri_rule(prec, Y, W);
   if (nq == 0) return OR_ERR_ARG;
@@ -760,28 +764,31 @@ int or_face_matrix(int order, int prec, const double *xyz, const int32_t *nodes4
   N[1] = Vx[2] * Vy[0] - Vx[0] * Vy[2];
   N[2] = Vx[0] * Vy[1] - Vx[1] * Vy[0];
   const double area2 = sqrt(N[0] * N[0] + N[1] * N[1] + N[2] * N[2]);
-  for (int k = 0; k < 3 * nb; ++k) mat[k] = 0.0;
+  for (int k = 0; k < nt * nb; ++k) mat[k] = 0.0;
   for (int q = 0; q < nq; ++q) {
     const double x = Y[2 * q], y = Y[2 * q + 1];
     const double lam[3] = {1.0 - x - y, x, y};
+    const double one[1] = {1.0};
+    const double *psi = test_order == 1 ? lam : one;
     double Yv[3], phi[10];
     for (int k = 0; k < 3; ++k)
       Yv[k] = REF_TET[FACE_PTS[lf][2]][k] * lam[2] +
               (REF_TET[FACE_PTS[lf][1]][k] * lam[1] + REF_TET[FACE_PTS[lf][0]][k] * lam[0]);
     or_basis_eval(order, Yv, phi);
-    for (int a = 0; a < 3; ++a)
-      for (int i = 0; i < nb; ++i) mat[a * nb + i] += phi[i] * lam[a] * area2 * W[q];
+    for (int a = 0; a < nt; ++a)
+      for (int i = 0; i < nb; ++i) mat[a * nb + i] += phi[i] * psi[a] * area2 * W[q];
   }
   return OR_OK;
 }
 
 /* or_face_matrix over a list of faces (face_elem[f], face_local[f]). */
-int or_face_matrices(int order, int prec, const double *xyz, int64_t n_faces, const int32_t *conn,
-                     const int32_t *face_elem, const int32_t *face_local, double *out)
+int or_face_matrices(int order, int test_order, int prec, const double *xyz, int64_t n_faces,
+                     const int32_t *conn, const int32_t *face_elem, const int32_t *face_local, double *out)
 {
-  const int nb = nbasis(order);
+  const int nb = nbasis(order), nt = test_order == 1 ? 3 : 1;
   for (int64_t f = 0; f < n_faces; ++f) {
-    int rc = or_face_matrix(order, prec, xyz, &conn[4 * (int64_t)face_elem[f]], face_local[f], out + 3 * nb * f);
+    int rc = or_face_matrix(order, test_order, prec, xyz, &conn[4 * (int64_t)face_elem[f]], face_local[f],
+                            out + nt * nb * f);
     if (rc) return rc;
   }
   return OR_OK;

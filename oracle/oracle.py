@@ -59,8 +59,8 @@ def lib():
         L.or_basis_eval.argtypes = [I32, P, P]
         L.or_basis_grad.argtypes = [I32, P, P, P, P]
         L.or_tri_rule.argtypes = [I32, P, P]
-        L.or_face_matrix.argtypes = [I32, I32, P, P, I32, P]
-        L.or_face_matrices.argtypes = [I32, I32, P, I64, P, P, P, P]
+        L.or_face_matrix.argtypes = [I32, I32, I32, P, P, I32, P]
+        L.or_face_matrices.argtypes = [I32, I32, I32, P, I64, P, P, P, P]
         _lib = L
     return _lib
 
@@ -192,13 +192,14 @@ def tri_rule(quad: int):
     return Y[:n].copy(), W[:n].copy()
 
 
-def face_matrix(order, quad, xyz, nodes4, lf):
+def face_matrix(order, quad, xyz, nodes4, lf, test_order=1):
     nb = 4 if order == 1 else 10
-    mat = np.empty(3 * nb)
+    nt = 3 if test_order == 1 else 1
+    mat = np.empty(nt * nb)
     nodes4 = np.ascontiguousarray(nodes4, dtype=np.int32)
     xyz = np.ascontiguousarray(xyz, dtype=np.float64)
-    assert lib().or_face_matrix(order, FACE_QUAD_PREC[quad], _p(xyz), _p(nodes4), lf, _p(mat)) == 0
-    return mat.reshape(3, nb)  # [face point a, field basis i]
+    assert lib().or_face_matrix(order, test_order, FACE_QUAD_PREC[quad], _p(xyz), _p(nodes4), lf, _p(mat)) == 0
+    return mat.reshape(nt, nb)  # [test basis a, field basis i]
 
 
 def boundary_faces(conn, tris=None):
@@ -226,32 +227,50 @@ def boundary_faces(conn, tris=None):
     return (idx // 4).astype(np.int32), (idx % 4).astype(np.int32)
 
 
-def lagrange(order, quad, xyz, conn, dofs, ndof, tris=None, faces=None):
-    """B of opLA3dA with P1 multipliers on the boundary triangles.
+def lagrange(order, quad, xyz, conn, dofs, ndof, tris=None, faces=None, test_order=1):
+    """B of opLA3dA with P1 (test_order 1) or P0 (test_order 0) multipliers on
+    the boundary triangles.
 
-    Multipliers: the nodes of the selected boundary faces, numbered by ascending
-    node id (meshDoctor2d.hpp:339-500 compacts the boundary grid's nodes in that
-    order; dofMapStatic2d numbers P1 dofs by node).  Rows = multipliers, columns =
-    field dofs; every face contributes its 3 x nb local block, zeros included
-    (traitsMatrixBuilder.hpp:363-441 inserts the whole block), summed in element,
-    local-face, face-point, basis order.  `faces` = (face_elem, face_local) from
-    boundary_faces, to skip that search.  Returns (lam_node, rowptr, colind,
-    values, face_elem, face_local)."""
+    P1 multipliers: the nodes of the selected boundary faces, numbered by
+    ascending node id (meshDoctor2d.hpp:339-500 compacts the boundary grid's
+    nodes in that order; dofMapStatic2d.hpp:1166-1380 numbers the active
+    vertices in that order).  P0 multipliers: one per selected face, numbered in
+    the boundary grid's element order -- the order of `tris` when given (the
+    Gmsh triangles' order, whose ids the boundary elements keep,
+    meshInit3d.hpp:400-430), else the face order.  Rows = multipliers, columns =
+    field dofs; every face contributes its full local block, zeros included
+    (traitsMatrixBuilder.hpp:363-441 inserts the whole block), summed in
+    element, local-face, test-basis, field-basis order.  `faces` = (face_elem,
+    face_local) from boundary_faces, to skip that search.  Returns (lam_item,
+    rowptr, colind, values, face_elem, face_local), lam_item = the node (P1) or
+    the face index (P0) of each multiplier."""
     xyz = np.ascontiguousarray(xyz, dtype=np.float64)
     conn = np.ascontiguousarray(conn, dtype=np.int32)
     nb = dofs.shape[1]
     fe, fl = boundary_faces(conn, tris) if faces is None else faces
     nf = fe.shape[0]
-    mats = np.empty((nf, 3, nb))
+    nt = 3 if test_order == 1 else 1
+    mats = np.empty((nf, nt, nb))
     if nf:
-        assert lib().or_face_matrices(order, FACE_QUAD_PREC[quad], _p(xyz), nf, _p(conn), _p(fe), _p(fl),
-                                      _p(mats)) == 0
+        assert lib().or_face_matrices(order, test_order, FACE_QUAD_PREC[quad], _p(xyz), nf, _p(conn), _p(fe),
+                                      _p(fl), _p(mats)) == 0
     fnodes = conn[fe[:, None], FACE_PTS[fl]] if nf else np.zeros((0, 3), np.int32)
-    lam_node = np.unique(fnodes).astype(np.int32)
-    lam_of = np.full(xyz.shape[0], -1, dtype=np.int64)
-    lam_of[lam_node] = np.arange(lam_node.shape[0])
-    rows = np.broadcast_to(lam_of[fnodes][:, :, None], (nf, 3, nb)).reshape(-1)
-    cols = np.broadcast_to(dofs[fe][:, None, :], (nf, 3, nb)).reshape(-1).astype(np.int64)
+    if test_order == 1:
+        lam_node = np.unique(fnodes).astype(np.int32)
+        lam_of = np.full(xyz.shape[0], -1, dtype=np.int64)
+        lam_of[lam_node] = np.arange(lam_node.shape[0])
+        face_rows = lam_of[fnodes]
+    else:
+        if tris is None:
+            rank = np.arange(nf)
+        else:
+            pos = {tuple(t): k for k, t in enumerate(np.sort(np.asarray(tris), axis=1).tolist())}
+            rank = np.array([pos[tuple(t)] for t in np.sort(fnodes, axis=1).tolist()], dtype=np.int64)
+        lam_node = np.empty(nf, dtype=np.int32)
+        lam_node[rank] = np.arange(nf)  # the face carrying each multiplier
+        face_rows = rank[:, None]
+    rows = np.broadcast_to(face_rows[:, :, None], (nf, nt, nb)).reshape(-1)
+    cols = np.broadcast_to(dofs[fe][:, None, :], (nf, nt, nb)).reshape(-1).astype(np.int64)
     key = rows * ndof + cols
     ukey, pos = np.unique(key, return_inverse=True)
     vals = np.zeros(ukey.shape[0])

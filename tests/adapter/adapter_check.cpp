@@ -72,7 +72,7 @@ static int run_lagrange(FILE* f, mg_plan* plan, int64_t ndof, int64_t nnz, int64
                         const std::vector<double>& kappa, const char* out_path)
 {
   mg_lagrange* lg = nullptr;
-  mg_epetra::check(mg_lagrange_build(plan, 0, nullptr, 0, &lg));
+  mg_epetra::check(mg_lagrange_build(plan, 1, 0, nullptr, 0, &lg));
   mg_lagrange_info li{};
   mg_epetra::check(mg_lagrange_get_info(lg, &li));
   const int64_t n = ndof + li.n_multipliers;

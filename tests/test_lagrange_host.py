@@ -38,7 +38,7 @@ def face_lib(tmp_path_factory):
                     os.path.join(ROOT, "tests", "lagrange", "face_check.cpp"), "-o", out], check=True)
     L = ctypes.CDLL(out)
     P = ctypes.c_void_p
-    L.face_check_matrices.argtypes = [ctypes.c_int, ctypes.c_int, P, ctypes.c_int64, P, P, P, P]
+    L.face_check_matrices.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, P, ctypes.c_int64, P, P, P, P]
     return L
 
 
@@ -46,14 +46,15 @@ def _p(a):
     return a.ctypes.data
 
 
-def kernel_face_matrices(face_lib, order, quad, xyz, conn, fe, fl):
+def kernel_face_matrices(face_lib, order, quad, xyz, conn, fe, fl, test_order=1):
     nb = 4 if order == 1 else 10
-    out = np.empty((len(fe), 3, nb))
+    out = np.empty((len(fe), 3 if test_order == 1 else 1, nb))
     xyz = np.ascontiguousarray(xyz, dtype=np.float64)
     conn = np.ascontiguousarray(conn, dtype=np.int32)
     fe = np.ascontiguousarray(fe, dtype=np.int32)
     fl = np.ascontiguousarray(fl, dtype=np.int32)
-    assert face_lib.face_check_matrices(order, quad, _p(xyz), len(fe), _p(conn), _p(fe), _p(fl), _p(out)) == 0
+    assert face_lib.face_check_matrices(order, test_order, quad, _p(xyz), len(fe), _p(conn), _p(fe), _p(fl),
+                                        _p(out)) == 0
     return out
 
 
@@ -91,6 +92,26 @@ def test_oracle_rows_sum_to_hat_integrals(order, quad):
     assert abs(area.sum() - 6.0) < 1e-12  # the unit cube's surface
 
 
+@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("quad", CARDS)
+def test_oracle_p0_rows_are_face_areas(order, quad):
+    """P0 multipliers: row f of B holds int_f phi_i, which sums to the face area;
+    with P1 fields every face vertex gets area / 3 (degree 1, exact for every card)."""
+    m, mesh, b = _mesh(3, order)
+    dofs = mesh.elem_dofs()
+    lam, rp, ci, v, fe, fl = orc.lagrange(order, quad, m.xyz, m.conn, dofs, b.ndof, test_order=0)
+    assert np.array_equal(lam, np.arange(len(fe)))  # face order without a triangle list
+    fn = m.conn[fe[:, None], orc.FACE_PTS[fl]]
+    P = m.xyz[fn]
+    area = 0.5 * np.linalg.norm(np.cross(P[:, 1] - P[:, 0], P[:, 2] - P[:, 0]), axis=1)
+    assert np.abs(np.add.reduceat(v, rp[:-1]) - area).max() < 1e-15
+    if order == 1:
+        for f in range(len(fe)):
+            row = dict(zip(ci[rp[f]:rp[f + 1]], v[rp[f]:rp[f + 1]]))
+            for node in fn[f]:
+                assert abs(row[node] - area[f] / 3) < 1e-15
+
+
 def test_oracle_p1_block_is_the_face_mass_matrix():
     m = meshgen.kuhn_cube(2, jitter=0.25, seed=5, permute=False)
     for e in range(len(m.conn)):
@@ -106,13 +127,14 @@ def test_oracle_p1_block_is_the_face_mass_matrix():
 
 
 # ------------------------------------------------------ kernel arithmetic --
+@pytest.mark.parametrize("test_order", [1, 0])
 @pytest.mark.parametrize("order", [1, 2])
 @pytest.mark.parametrize("quad", CARDS)
-def test_kernel_face_math_matches_oracle(face_lib, order, quad):
+def test_kernel_face_math_matches_oracle(face_lib, order, quad, test_order):
     m, mesh, b = _mesh(3, order, seed=7)
     fe, fl = orc.boundary_faces(m.conn)
-    ref = np.stack([orc.face_matrix(order, quad, m.xyz, m.conn[e], l) for e, l in zip(fe, fl)])
-    got = kernel_face_matrices(face_lib, order, quad, m.xyz, m.conn, fe, fl)
+    ref = np.stack([orc.face_matrix(order, quad, m.xyz, m.conn[e], l, test_order) for e, l in zip(fe, fl)])
+    got = kernel_face_matrices(face_lib, order, quad, m.xyz, m.conn, fe, fl, test_order)
     scale = np.abs(ref).max(axis=(1, 2), keepdims=True)
     assert np.max(np.abs(got - ref) / scale) < 1e-14
 
@@ -125,21 +147,24 @@ def _tris_on_plane(m, axis, value):
     return fn[on][:, ::-1].copy()  # any vertex order
 
 
+@pytest.mark.parametrize("test_order", [1, 0])
 @pytest.mark.parametrize("order", [1, 2])
 @pytest.mark.parametrize("select", [None, "x0", "x0z1"])
 @pytest.mark.parametrize("lam_diag", [False, True])
-def test_patterns_match_oracle(order, select, lam_diag):
+def test_patterns_match_oracle(order, select, lam_diag, test_order):
     m, mesh, b = _mesh(4 if order == 1 else 3, order, seed=11)
     tris = None
     if select == "x0":
         tris = _tris_on_plane(m, 0, 0.0)
-    elif select == "x0z1":
-        tris = np.concatenate([_tris_on_plane(m, 0, 0.0), _tris_on_plane(m, 2, 1.0)])
-    lg = mg.LagrangeBuilder(b, tris=tris, lam_diag=lam_diag)
+    elif select == "x0z1":  # in an order unrelated to the faces': P0 multipliers follow it
+        tris = np.concatenate([_tris_on_plane(m, 2, 1.0), _tris_on_plane(m, 0, 0.0)])
+        tris = tris[np.random.default_rng(3).permutation(len(tris))]
+    lg = mg.LagrangeBuilder(b, tris=tris, lam_diag=lam_diag, test_order=test_order)
     lam, fe, fl = lg.multipliers()
     (brp, bci), (srp, sci) = lg.pattern()
     dofs = mesh.elem_dofs()
-    olam, obrp, obci, obv, ofe, ofl = orc.lagrange(order, 1, m.xyz, m.conn, dofs, b.ndof, tris=tris)
+    olam, obrp, obci, obv, ofe, ofl = orc.lagrange(order, 1, m.xyz, m.conn, dofs, b.ndof, tris=tris,
+                                                   test_order=test_order)
     assert np.array_equal(fe, ofe) and np.array_equal(fl, ofl)
     assert np.array_equal(lam, olam)
     assert np.array_equal(brp, obrp) and np.array_equal(bci, obci)
@@ -150,23 +175,24 @@ def test_patterns_match_oracle(order, select, lam_diag):
         assert lg.n_faces == len(tris)
 
 
+@pytest.mark.parametrize("test_order", [1, 0])
 @pytest.mark.parametrize("order", [1, 2])
 @pytest.mark.parametrize("quad", [1, 6])
-def test_kernel_data_flow_matches_oracle(face_lib, order, quad):
+def test_kernel_data_flow_matches_oracle(face_lib, order, quad, test_order):
     """The two kernels' data flow on the host: face matrices (the kernel's own
     arithmetic), the per-entry gather lists of B, the saddle source map."""
     m, mesh, b = _mesh(4 if order == 1 else 3, order, seed=13)
-    lg = mg.LagrangeBuilder(b, lam_diag=True)
+    lg = mg.LagrangeBuilder(b, lam_diag=True, test_order=test_order)
     lam, fe, fl = lg.multipliers()
     (brp, bci), (srp, sci) = lg.pattern()
     bptr, bsrc, ssrc = lg.export_maps()
-    fm = kernel_face_matrices(face_lib, order, quad, m.xyz, m.conn, fe, fl).reshape(-1)
+    fm = kernel_face_matrices(face_lib, order, quad, m.xyz, m.conn, fe, fl, test_order).reshape(-1)
     bv = np.array([np.sum(fm[bsrc[bptr[k]:bptr[k + 1]]]) for k in range(lg.nnz_b)])
     dofs = mesh.elem_dofs()
-    _, orp, oci, ov, _, _ = orc.lagrange(order, quad, m.xyz, m.conn, dofs, b.ndof)
+    _, orp, oci, ov, _, _ = orc.lagrange(order, quad, m.xyz, m.conn, dofs, b.ndof, test_order=test_order)
     assert row_scaled_err(orp, ov, bv) <= 1e-13
     # every face-matrix entry is used exactly once
-    assert np.array_equal(np.sort(bsrc), np.arange(len(fe) * 3 * mesh.nb))
+    assert np.array_equal(np.sort(bsrc), np.arange(len(fe) * (3 if test_order == 1 else 1) * mesh.nb))
     # saddle values through the source map
     rp, ci = b.pattern()
     kv = np.random.default_rng(1).uniform(-1, 1, len(ci))

@@ -179,3 +179,27 @@ def test_host_buffer_b_equals_device_b():
     (brp, bci), _ = lg.pattern()
     assert np.array_equal(host.rowptr, brp) and np.array_equal(host.colind, bci)
     assert np.array_equal(host.values, dev)
+
+
+@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("quad", [1, 3])
+def test_p0_multipliers_match_oracle(order, quad):
+    """fePr2d<0> multipliers (one per triangle, numbered in the order of the
+    given triangles), as in the reference's localMatrixLA3dTest1."""
+    m = meshgen.kuhn_cube(4 if order == 1 else 3, jitter=0.2, seed=27, permute=True)
+    mesh = mg.Mesh(m.xyz, m.conn, order=order)
+    b = mg.MatrixBuilder(mesh)
+    fe, fl = orc.boundary_faces(m.conn)
+    fn = m.conn[fe[:, None], orc.FACE_PTS[fl]]
+    on = np.all(np.abs(m.xyz[fn][:, :, 0]) < 1e-12, axis=1) | np.all(np.abs(m.xyz[fn][:, :, 2] - 1) < 1e-12,
+                                                                     axis=1)
+    tris = fn[on][np.random.default_rng(2).permutation(int(on.sum()))]  # x = 0 and z = 1, shuffled
+    lg = mg.LagrangeBuilder(b, tris=tris, test_order=0)
+    got = lg.assemble(quad=quad)
+    again = lg.assemble(quad=quad)
+    dofs = mesh.elem_dofs()
+    lam, rp, ci, ref, _, _ = orc.lagrange(order, quad, m.xyz, m.conn, dofs, b.ndof, tris=tris, test_order=0)
+    (brp, bci), _ = lg.pattern()
+    assert lg.n_multipliers == len(tris) and np.array_equal(brp, rp) and np.array_equal(bci, ci)
+    assert row_scaled_err(rp, ref, got.cpu().numpy()) <= 1e-12
+    assert torch.equal(got, again)
