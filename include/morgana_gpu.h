@@ -333,7 +333,15 @@ typedef struct {
   int64_t ndof;           /* columns of B (the plan's field dofs) */
   int64_t nnz_b;
   int64_t nnz_saddle;     /* (ndof + n_multipliers) rows */
+  int64_t nnz_mtm;        /* entries of B^T B (MG_SADDLE_MTM), else 0 */
+  int64_t n_mtm_products; /* products B_li B_lj they sum */
 } mg_lagrange_info;
+
+/* Saddle pattern options of mg_lagrange_build. */
+enum {
+  MG_SADDLE_LAM_DIAG = 1, /* store the multiplier block's diagonal (setEye on that block) */
+  MG_SADDLE_MTM = 2       /* add B^T B to the field block (setMTM(B, field block)) */
+};
 
 /* Multiplier space and patterns, on the host (no device needed).
    Boundary faces = faces of exactly one tet (connect3d::getFaceIsBoundary),
@@ -354,15 +362,17 @@ typedef struct {
    traitsMatrixBuilder::buildEpetraCrs does for localMatrixLA3d
    (src/morganaFiniteElements/localMatrixLA3d.hpp:292-322).
    Saddle: [K B^T; B 0] (epetraSaddleAssembler::setDiagMatrix + setSymmMatrix,
-   src/morganaTrilinos/epetraSaddleAssembler.cpp), with K the plan's pattern;
-   lam_diag != 0 adds the diagonal of the multiplier block to the pattern
-   (setEye on that block).
+   src/morganaTrilinos/epetraSaddleAssembler.cpp), with K the plan's pattern.
+   flags: MG_SADDLE_LAM_DIAG adds the diagonal of the multiplier block to the
+   pattern (setEye on that block); MG_SADDLE_MTM merges the structural pattern
+   of B^T B into the field block (setMTM, whose product EpetraExt builds
+   structurally: every pair of entries of a multiplier row couples, zeros kept).
    Errors: MG_ERR_BAD_MESH when a face belongs to more than two tets or a
    selected triangle is not a boundary face; MG_ERR_INVALID_ARG for a repeated
    triangle or a node id out of range; MG_ERR_SIZE above 2^31 - 1 entries.
    The handle keeps a pointer to the plan: destroy it before the plan. */
 mg_status mg_lagrange_build(mg_plan* plan, int32_t test_order, int64_t n_tris, const int32_t* h_tris,
-                            int32_t lam_diag, mg_lagrange** out);
+                            int32_t flags, mg_lagrange** out);
 mg_status mg_lagrange_destroy(mg_lagrange* lg);
 mg_status mg_lagrange_get_info(const mg_lagrange* lg, mg_lagrange_info* info);
 /* h_lam_node (n_multipliers): node (P1) or selected face (P0, an index into
@@ -380,9 +390,15 @@ mg_status mg_lagrange_pattern(const mg_lagrange* lg, int32_t* h_b_rowptr, int32_
    face-matrix entries h_b_src[h_b_src_ptr[k] .. h_b_src_ptr[k+1]), each
    (face * nt + test basis) * nb + field basis, in that order; h_s_src (nnz_saddle):
    saddle entry k copies K entry h_s_src[k] (>= 0), B entry -(h_s_src[k] + 1),
-   or the multiplier diagonal (INT32_MIN).  Any pointer may be NULL. */
+   the multiplier diagonal (INT32_MIN) or starts at zero (INT32_MIN + 1: a B^T B
+   entry outside K's pattern).  Any pointer may be NULL. */
 mg_status mg_lagrange_export_maps(const mg_lagrange* lg, int32_t* h_b_src_ptr, int32_t* h_b_src,
                                   int32_t* h_s_src);
+/* With MG_SADDLE_MTM: B^T B entry m sums B[k1] B[k2] over the pairs
+   h_pairs[h_pair_ptr[m] .. h_pair_ptr[m+1]) (int32 pairs (k1, k2), ascending
+   multiplier row) and adds into saddle entry h_slot[m].  Sizes: nnz_mtm + 1,
+   2 n_mtm_products, nnz_mtm.  Any pointer may be NULL. */
+mg_status mg_lagrange_export_mtm(const mg_lagrange* lg, int32_t* h_pair_ptr, int32_t* h_pairs, int32_t* h_slot);
 
 /* Values of B (nnz_b doubles, device) with the face card quad (MG_FACE_QUAD_*):
    one thread per face computes its nt x nb block, then one thread per entry of
@@ -393,10 +409,13 @@ mg_status mg_lagrange_assemble(mg_lagrange* lg, int32_t quad, double* d_b_values
    what buildEpetraCrs hands to Epetra for localMatrixLA3d.  Synchronous. */
 mg_status mg_lagrange_assemble_host(mg_lagrange* lg, int32_t quad, double* h_b_values);
 /* Saddle values (nnz_saddle doubles, device) from K's values (the plan's CSR)
-   and B's: [K + eye_field I, B^T; B, eye_lam I].  eye_lam must be 0 unless the
-   pattern has the multiplier diagonal (lam_diag). */
+   and B's: [K + eye_field I + mtm_scale B^T B, B^T; B, eye_lam I].  eye_lam
+   must be 0 unless the pattern has the multiplier diagonal
+   (MG_SADDLE_LAM_DIAG), mtm_scale 0 unless it has B^T B (MG_SADDLE_MTM; one
+   thread per entry of B^T B sums its products in ascending multiplier row and
+   adds them to its own saddle entry: deterministic, no atomics). */
 mg_status mg_saddle_assemble(mg_lagrange* lg, const double* d_k_values, const double* d_b_values,
-                             double eye_field, double eye_lam, double* d_values, void* stream);
+                             double eye_field, double eye_lam, double mtm_scale, double* d_values, void* stream);
 /* y = S x on the saddle matrix (ndof + n_multipliers doubles each). */
 mg_status mg_saddle_spmv(mg_lagrange* lg, const double* d_values, const double* d_x, double* d_y,
                          void* stream);

@@ -203,6 +203,10 @@ struct mg_plan {
   bool on_device = false;
 };
 
+// Saddle entry sources other than K and B entries (see mg_lagrange::s_src).
+constexpr int32_t kSrcLamDiag = INT32_MIN;
+constexpr int32_t kSrcZero = INT32_MIN + 1;
+
 // Boundary multipliers of a plan (opLA3dA) and the saddle pattern [K B^T; B 0].
 struct mg_lagrange {
   mg_plan* plan = nullptr;
@@ -217,13 +221,25 @@ struct mg_lagrange {
   // each (f * nt + a) * nb + i, ascending (the reference's insertion order)
   std::vector<int32_t> b_src_ptr, b_src;
   std::vector<int32_t> s_rowptr, s_colind;     // saddle: (ndof + nl) rows
-  // per saddle entry: the K entry it copies (>= 0) or -(k + 1) for B entry k
+  // per saddle entry: the K entry it copies (>= 0), -(k + 1) for B entry k,
+  // kSrcLamDiag (the multiplier diagonal) or kSrcZero (a B^T B entry outside K)
   std::vector<int32_t> s_src;
+  std::vector<int32_t> s_diag;  // saddle entry of each field row's diagonal, or -1
+  // B^T B (setMTM): per entry m, the product pairs (k1, k2) of B entries it sums,
+  // m_pairs[m_pair_ptr[m] .. m_pair_ptr[m+1]) in ascending multiplier row, and the
+  // saddle slot it adds into
+  bool mtm = false;
+  int64_t nnz_m = 0;
+  std::vector<int32_t> m_pair_ptr, m_slot;
+  std::vector<int2> m_pairs;
   // device copies (uploaded on first GPU use)
   int2* d_faces = nullptr;  // (element, local face)
   int32_t *d_b_rowptr = nullptr, *d_b_colind = nullptr, *d_b_src_ptr = nullptr, *d_b_src = nullptr;
   int32_t *d_s_rowptr = nullptr, *d_s_colind = nullptr, *d_s_src = nullptr;
   double* d_face_mat = nullptr;  // n_faces * nt * nb
+  int32_t* d_s_diag = nullptr;
+  int32_t *d_m_pair_ptr = nullptr, *d_m_slot = nullptr;
+  int2* d_m_pairs = nullptr;
   bool on_device = false;
 };
 

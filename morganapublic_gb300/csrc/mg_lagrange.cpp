@@ -115,7 +115,7 @@ mg_status boundary_flags(const mg_mesh* m, std::vector<uint8_t>* flag)
 }  // namespace
 
 static mg_status build_lagrange(mg_lagrange* lg, int test_order, int64_t n_tris, const int32_t* h_tris,
-                                bool lam_diag)
+                                bool lam_diag, bool mtm)
 {
   const mg_plan* p = lg->plan;
   const mg_mesh* m = p->mesh;
@@ -126,6 +126,7 @@ static mg_status build_lagrange(mg_lagrange* lg, int test_order, int64_t n_tris,
   lg->nt = test_order == 1 ? 3 : 1;
   const int nt = lg->nt;
   lg->lam_diag = lam_diag;
+  lg->mtm = mtm;
   lg->nb = nb;
   lg->ndof = nd;
   if (4 * E > kInt32Max) return set_error(MG_ERR_SIZE, "mg_lagrange_build: more than 2^29 tets");
@@ -241,33 +242,110 @@ static mg_status build_lagrange(mg_lagrange* lg, int test_order, int64_t n_tris,
   for (int64_t l = 0; l < nl; ++l) lg->b_rowptr[l + 1] += lg->b_rowptr[l];
   lg->nnz_b = (int64_t)lg->b_colind.size();
 
-  // saddle: rows r < nd hold K's row then B^T's (columns nd + l, ascending l);
-  // rows nd + l hold B's row l (columns < nd), then the diagonal if requested
-  const int64_t nk = p->nnz;
-  const int64_t ns = nk + 2 * lg->nnz_b + (lam_diag ? nl : 0);
-  if (ns > kInt32Max || nd + nl > kInt32Max)
-    return set_error(MG_ERR_SIZE, "mg_lagrange_build: the saddle matrix has more than 2^31 - 1 entries");
+  // B^T B (setMTM): every pair of entries (k1, k2) of a multiplier row l
+  // couples columns (i, j); entry (i, j) sums B[k1] B[k2] over its rows l in
+  // ascending order.  Structural pattern: zeros kept.
+  std::vector<int32_t> m_rowptr, m_colind;
+  if (mtm) {
+    struct Prod {
+      uint64_t key;  // i << 32 | j
+      int32_t l, k1, k2;
+      bool operator<(const Prod& o) const { return key != o.key ? key < o.key : l < o.l; }
+    };
+    std::vector<int64_t> off(nl + 1, 0);
+    for (int64_t l = 0; l < nl; ++l) {
+      const int64_t len = lg->b_rowptr[l + 1] - lg->b_rowptr[l];
+      off[l + 1] = off[l] + len * len;
+    }
+    std::vector<Prod> prods(off[nl]);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t l = 0; l < nl; ++l) {
+      int64_t o = off[l];
+      for (int32_t k1 = lg->b_rowptr[l]; k1 < lg->b_rowptr[l + 1]; ++k1)
+        for (int32_t k2 = lg->b_rowptr[l]; k2 < lg->b_rowptr[l + 1]; ++k2)
+          prods[o++] = Prod{(uint64_t)(uint32_t)lg->b_colind[k1] << 32 | (uint32_t)lg->b_colind[k2], (int32_t)l,
+                            k1, k2};
+    }
+    __gnu_parallel::sort(prods.begin(), prods.end());
+    if ((int64_t)prods.size() > kInt32Max)
+      return set_error(MG_ERR_SIZE, "mg_lagrange_build: B^T B has more than 2^31 - 1 products");
+    m_rowptr.assign(nd + 1, 0);
+    lg->m_pair_ptr.clear();
+    lg->m_pairs.resize(prods.size());
+    for (size_t k = 0; k < prods.size(); ++k) {
+      if (k == 0 || prods[k].key != prods[k - 1].key) {
+        lg->m_pair_ptr.push_back((int32_t)k);
+        m_colind.push_back((int32_t)(prods[k].key & 0xffffffffu));
+        m_rowptr[(prods[k].key >> 32) + 1]++;
+      }
+      lg->m_pairs[k] = make_int2(prods[k].k1, prods[k].k2);
+    }
+    lg->m_pair_ptr.push_back((int32_t)prods.size());
+    for (int64_t r = 0; r < nd; ++r) m_rowptr[r + 1] += m_rowptr[r];
+    lg->nnz_m = (int64_t)m_colind.size();
+  }
+
+  // saddle: rows r < nd hold the union of K's and B^T B's columns, then B^T's
+  // (columns nd + l, ascending l); rows nd + l hold B's row l (columns < nd),
+  // then the diagonal if requested
+  auto union_len = [&](int64_t r) {
+    int64_t n = 0;
+    int32_t a = p->rowptr[r], b = mtm ? m_rowptr[r] : 0;
+    const int32_t a1 = p->rowptr[r + 1], b1 = mtm ? m_rowptr[r + 1] : 0;
+    while (a < a1 || b < b1) {
+      if (b >= b1 || (a < a1 && p->colind[a] < m_colind[b])) ++a;
+      else if (a >= a1 || m_colind[b] < p->colind[a]) ++b;
+      else ++a, ++b;
+      ++n;
+    }
+    return n;
+  };
+  std::vector<int64_t> ulen(nd);
+#pragma omp parallel for schedule(static)
+  for (int64_t r = 0; r < nd; ++r) ulen[r] = union_len(r);
   std::vector<int32_t> tcnt(nd + 1, 0);
   for (int64_t k = 0; k < lg->nnz_b; ++k) tcnt[lg->b_colind[k] + 1]++;
   for (int64_t r = 0; r < nd; ++r) tcnt[r + 1] += tcnt[r];
-  lg->s_rowptr.assign(nd + nl + 1, 0);
-  for (int64_t r = 0; r < nd; ++r)
-    lg->s_rowptr[r + 1] = lg->s_rowptr[r] + (p->rowptr[r + 1] - p->rowptr[r]) + (tcnt[r + 1] - tcnt[r]);
+  int64_t ns = 0;
+  std::vector<int64_t> srp(nd + nl + 1, 0);
+  for (int64_t r = 0; r < nd; ++r) srp[r + 1] = srp[r] + ulen[r] + (tcnt[r + 1] - tcnt[r]);
   for (int64_t l = 0; l < nl; ++l)
-    lg->s_rowptr[nd + l + 1] = lg->s_rowptr[nd + l] + (lg->b_rowptr[l + 1] - lg->b_rowptr[l]) + (lam_diag ? 1 : 0);
-  lg->nnz_s = lg->s_rowptr[nd + nl];
+    srp[nd + l + 1] = srp[nd + l] + (lg->b_rowptr[l + 1] - lg->b_rowptr[l]) + (lam_diag ? 1 : 0);
+  ns = srp[nd + nl];
+  if (ns > kInt32Max || nd + nl > kInt32Max)
+    return set_error(MG_ERR_SIZE, "mg_lagrange_build: the saddle matrix has more than 2^31 - 1 entries");
+  lg->s_rowptr.assign(srp.begin(), srp.end());
+  lg->nnz_s = ns;
   lg->s_colind.resize(ns);
   lg->s_src.resize(ns);
+  lg->m_slot.assign(lg->nnz_m, 0);
   std::vector<int32_t> tfill(nd);
 #pragma omp parallel for schedule(static)
-  for (int64_t r = 0; r < nd; ++r) {  // K part
+  for (int64_t r = 0; r < nd; ++r) {  // K and B^T B part
     int32_t s = lg->s_rowptr[r];
-    for (int32_t k = p->rowptr[r]; k < p->rowptr[r + 1]; ++k, ++s) {
-      lg->s_colind[s] = p->colind[k];
-      lg->s_src[s] = k;
+    int32_t a = p->rowptr[r], b = mtm ? m_rowptr[r] : 0;
+    const int32_t a1 = p->rowptr[r + 1], b1 = mtm ? m_rowptr[r + 1] : 0;
+    for (; a < a1 || b < b1; ++s) {
+      if (b >= b1 || (a < a1 && p->colind[a] < m_colind[b])) {
+        lg->s_colind[s] = p->colind[a];
+        lg->s_src[s] = a++;
+      } else if (a >= a1 || m_colind[b] < p->colind[a]) {
+        lg->s_colind[s] = m_colind[b];
+        lg->s_src[s] = kSrcZero;
+        lg->m_slot[b++] = s;
+      } else {
+        lg->s_colind[s] = p->colind[a];
+        lg->s_src[s] = a++;
+        lg->m_slot[b++] = s;
+      }
     }
     tfill[r] = s;
   }
+  lg->s_diag.assign(nd, -1);  // the diagonal's saddle entry of each field row
+#pragma omp parallel for schedule(static)
+  for (int64_t r = 0; r < nd; ++r)
+    for (int32_t s = lg->s_rowptr[r]; s < tfill[r]; ++s)
+      if (lg->s_colind[s] == (int32_t)r) lg->s_diag[r] = s;
   for (int64_t l = 0; l < nl; ++l)  // B^T part: rows visited in ascending l
     for (int32_t k = lg->b_rowptr[l]; k < lg->b_rowptr[l + 1]; ++k) {
       const int32_t s = tfill[lg->b_colind[k]]++;
@@ -283,7 +361,7 @@ static mg_status build_lagrange(mg_lagrange* lg, int test_order, int64_t n_tris,
     }
     if (lam_diag) {
       lg->s_colind[s] = (int32_t)(nd + l);
-      lg->s_src[s] = INT32_MIN;  // filled with eye_lam
+      lg->s_src[s] = kSrcLamDiag;  // filled with eye_lam
     }
   }
   return MG_OK;
@@ -308,6 +386,13 @@ static void free_device(mg_lagrange* lg)
   cudaFree(lg->d_s_colind);
   cudaFree(lg->d_s_src);
   cudaFree(lg->d_face_mat);
+  cudaFree(lg->d_s_diag);
+  lg->d_s_diag = nullptr;
+  cudaFree(lg->d_m_pair_ptr);
+  cudaFree(lg->d_m_pairs);
+  cudaFree(lg->d_m_slot);
+  lg->d_m_pair_ptr = lg->d_m_slot = nullptr;
+  lg->d_m_pairs = nullptr;
   lg->d_faces = nullptr;
   lg->d_b_rowptr = lg->d_b_colind = lg->d_b_src_ptr = lg->d_b_src = nullptr;
   lg->d_s_rowptr = lg->d_s_colind = lg->d_s_src = nullptr;
@@ -329,6 +414,10 @@ mg_status lagrange_device(mg_lagrange* lg)
   if (s == MG_OK) s = upload(&lg->d_s_rowptr, lg->s_rowptr);
   if (s == MG_OK) s = upload(&lg->d_s_colind, lg->s_colind);
   if (s == MG_OK) s = upload(&lg->d_s_src, lg->s_src);
+  if (s == MG_OK) s = upload(&lg->d_s_diag, lg->s_diag);
+  if (s == MG_OK && lg->mtm) s = upload(&lg->d_m_pair_ptr, lg->m_pair_ptr);
+  if (s == MG_OK && lg->mtm) s = upload(&lg->d_m_pairs, lg->m_pairs);
+  if (s == MG_OK && lg->mtm) s = upload(&lg->d_m_slot, lg->m_slot);
   if (s == MG_OK) {
     const cudaError_t e =
         cudaMalloc(&lg->d_face_mat, sizeof(double) * std::max<int64_t>(lg->n_faces * lg->nt * lg->nb, 1));
@@ -349,12 +438,13 @@ using namespace mg;
 extern "C" {
 
 mg_status mg_lagrange_build(mg_plan* plan, int32_t test_order, int64_t n_tris, const int32_t* h_tris,
-                            int32_t lam_diag, mg_lagrange** out)
+                            int32_t flags, mg_lagrange** out)
 {
   NvtxRange nvtx_range("mg_lagrange_build");
   if (!plan || !out) return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_build: null argument");
   if (test_order != 0 && test_order != 1)
     return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_build: multipliers are P1 (1) or P0 (0)");
+  if (flags & ~(MG_SADDLE_LAM_DIAG | MG_SADDLE_MTM)) return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_build: bad flags");
   if (n_tris < 0 || (n_tris > 0 && !h_tris)) return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_build: bad triangle list");
   *out = nullptr;
   mg_lagrange* lg = new (std::nothrow) mg_lagrange();
@@ -362,7 +452,7 @@ mg_status mg_lagrange_build(mg_plan* plan, int32_t test_order, int64_t n_tris, c
   lg->plan = plan;
   mg_status s;
   try {
-    s = build_lagrange(lg, test_order, n_tris, h_tris, lam_diag != 0);
+    s = build_lagrange(lg, test_order, n_tris, h_tris, (flags & MG_SADDLE_LAM_DIAG) != 0, (flags & MG_SADDLE_MTM) != 0);
   } catch (const std::bad_alloc&) {
     s = set_error(MG_ERR_ALLOC, "mg_lagrange_build: out of host memory");
   }
@@ -390,6 +480,8 @@ mg_status mg_lagrange_get_info(const mg_lagrange* lg, mg_lagrange_info* info)
   info->ndof = lg->ndof;
   info->nnz_b = lg->nnz_b;
   info->nnz_saddle = lg->nnz_s;
+  info->nnz_mtm = lg->nnz_m;
+  info->n_mtm_products = (int64_t)lg->m_pairs.size();
   return MG_OK;
 }
 
@@ -419,6 +511,16 @@ mg_status mg_lagrange_export_maps(const mg_lagrange* lg, int32_t* h_b_src_ptr, i
   if (h_b_src_ptr) std::memcpy(h_b_src_ptr, lg->b_src_ptr.data(), sizeof(int32_t) * lg->b_src_ptr.size());
   if (h_b_src && !lg->b_src.empty()) std::memcpy(h_b_src, lg->b_src.data(), sizeof(int32_t) * lg->b_src.size());
   if (h_s_src && lg->nnz_s) std::memcpy(h_s_src, lg->s_src.data(), sizeof(int32_t) * lg->nnz_s);
+  return MG_OK;
+}
+
+mg_status mg_lagrange_export_mtm(const mg_lagrange* lg, int32_t* h_pair_ptr, int32_t* h_pairs, int32_t* h_slot)
+{
+  if (!lg) return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_export_mtm: null handle");
+  if (!lg->mtm) return MG_OK;
+  if (h_pair_ptr) std::memcpy(h_pair_ptr, lg->m_pair_ptr.data(), sizeof(int32_t) * lg->m_pair_ptr.size());
+  if (h_pairs && !lg->m_pairs.empty()) std::memcpy(h_pairs, lg->m_pairs.data(), sizeof(int2) * lg->m_pairs.size());
+  if (h_slot && lg->nnz_m) std::memcpy(h_slot, lg->m_slot.data(), sizeof(int32_t) * lg->nnz_m);
   return MG_OK;
 }
 

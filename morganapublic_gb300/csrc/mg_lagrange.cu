@@ -10,7 +10,8 @@
 // No atomics, so every run gives the same bits.  The work is O(boundary faces)
 // (n^2 against the volume operator's n^3) and runs in native FP64.
 // The saddle values are a gather from K's and B's values through a per-entry
-// source map; the products use the CSR SpMV kernel of mg_solve.cu.
+// source map (plus, for setMTM, one thread per entry of B^T B summing its
+// products); the products use the CSR SpMV kernel of mg_solve.cu.
 #include <algorithm>
 #include <climits>
 
@@ -69,7 +70,8 @@ __global__ void __launch_bounds__(kFaceThreads) k_gather_sum(int64_t n, const in
   }
 }
 
-// Saddle entry k: K's entry src (>= 0), B's entry -(src + 1), or eye_lam (INT32_MIN)
+// Saddle entry k: K's entry src (>= 0), B's entry -(src + 1), eye_lam
+// (kSrcLamDiag) or zero (kSrcZero, a B^T B entry outside K)
 __global__ void __launch_bounds__(kFaceThreads) k_saddle_fill(int64_t n, const int32_t* __restrict__ src,
                                                           const double* __restrict__ kv,
                                                           const double* __restrict__ bv, double eye_lam,
@@ -77,23 +79,37 @@ __global__ void __launch_bounds__(kFaceThreads) k_saddle_fill(int64_t n, const i
 {
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
     const int32_t s = src[k];
-    out[k] = s >= 0 ? kv[s] : (s == INT32_MIN ? eye_lam : bv[-(s + 1)]);
+    out[k] = s >= 0 ? kv[s] : (s == kSrcLamDiag ? eye_lam : (s == kSrcZero ? 0.0 : bv[-(s + 1)]));
   }
 }
 
-// Adds eye to the diagonal of the field block: row r's K entries come first in
-// its saddle row, so K's diagonal slot d (row r) sits at s_rowptr[r] + d - k_rowptr[r].
-// k_diag[r] is the first slot of row r with a column >= r; rows without a
-// diagonal entry (dofs outside every element) are left alone.
-__global__ void __launch_bounds__(kFaceThreads) k_saddle_eye(int64_t nd, const int32_t* __restrict__ s_rowptr,
-                                                         const int32_t* __restrict__ k_rowptr,
-                                                         const int32_t* __restrict__ k_colind,
-                                                         const int32_t* __restrict__ k_diag, double eye,
+// B^T B entry m: scale * sum of bv[k1] bv[k2] over its pairs (ascending
+// multiplier row), added to its saddle entry (one entry per m: no atomics)
+__global__ void __launch_bounds__(kFaceThreads) k_saddle_mtm(int64_t n, const int32_t* __restrict__ pair_ptr,
+                                                         const int2* __restrict__ pairs,
+                                                         const int32_t* __restrict__ slot,
+                                                         const double* __restrict__ bv, double scale,
                                                          double* __restrict__ out)
 {
+  for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < n; m += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    const int32_t j1 = pair_ptr[m + 1];
+    for (int32_t j = pair_ptr[m]; j < j1; ++j) {
+      const int2 pr = pairs[j];
+      s += bv[pr.x] * bv[pr.y];
+    }
+    out[slot[m]] += scale * s;
+  }
+}
+
+// Adds eye to the diagonal of the field block, at each row's diagonal entry
+// (s_diag[r]; rows without one, dofs outside every element, are left alone).
+__global__ void __launch_bounds__(kFaceThreads) k_saddle_eye(int64_t nd, const int32_t* __restrict__ s_diag,
+                                                         double eye, double* __restrict__ out)
+{
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nd; r += (int64_t)gridDim.x * blockDim.x) {
-    const int32_t d = k_diag[r];
-    if (d < k_rowptr[r + 1] && k_colind[d] == (int32_t)r) out[s_rowptr[r] + (d - k_rowptr[r])] += eye;
+    const int32_t d = s_diag[r];
+    if (d >= 0) out[d] += eye;
   }
 }
 
@@ -154,12 +170,14 @@ mg_status mg_lagrange_assemble_host(mg_lagrange* lg, int32_t quad, double* h_b_v
 }
 
 mg_status mg_saddle_assemble(mg_lagrange* lg, const double* d_k_values, const double* d_b_values, double eye_field,
-                             double eye_lam, double* d_values, void* stream)
+                             double eye_lam, double mtm_scale, double* d_values, void* stream)
 {
   NvtxRange nvtx_range("mg_saddle_assemble");
   if (!lg) return set_error(MG_ERR_INVALID_ARG, "mg_saddle_assemble: null handle");
   if (eye_lam != 0.0 && !lg->lam_diag)
-    return set_error(MG_ERR_INVALID_ARG, "mg_saddle_assemble: eye_lam needs a pattern built with lam_diag");
+    return set_error(MG_ERR_INVALID_ARG, "mg_saddle_assemble: eye_lam needs a pattern built with MG_SADDLE_LAM_DIAG");
+  if (mtm_scale != 0.0 && !lg->mtm)
+    return set_error(MG_ERR_INVALID_ARG, "mg_saddle_assemble: mtm_scale needs a pattern built with MG_SADDLE_MTM");
   if (lg->nnz_s == 0) return MG_OK;
   if (!d_values || (lg->plan->nnz && !d_k_values) || (lg->nnz_b && !d_b_values))
     return set_error(MG_ERR_INVALID_ARG, "mg_saddle_assemble: null argument");
@@ -169,9 +187,12 @@ mg_status mg_saddle_assemble(mg_lagrange* lg, const double* d_k_values, const do
                                                            d_values);
   MG_CUDA(cudaGetLastError());
   if (eye_field != 0.0 && lg->ndof > 0) {
-    k_saddle_eye<<<grid_for(lg->ndof), kFaceThreads, 0, st>>>(lg->ndof, lg->d_s_rowptr, lg->plan->d_rowptr,
-                                                           lg->plan->d_colind, lg->plan->d_diag, eye_field,
-                                                           d_values);
+    k_saddle_eye<<<grid_for(lg->ndof), kFaceThreads, 0, st>>>(lg->ndof, lg->d_s_diag, eye_field, d_values);
+    MG_CUDA(cudaGetLastError());
+  }
+  if (mtm_scale != 0.0 && lg->nnz_m > 0) {
+    k_saddle_mtm<<<grid_for(lg->nnz_m), kFaceThreads, 0, st>>>(lg->nnz_m, lg->d_m_pair_ptr, lg->d_m_pairs,
+                                                               lg->d_m_slot, d_b_values, mtm_scale, d_values);
     MG_CUDA(cudaGetLastError());
   }
   return MG_OK;

@@ -283,13 +283,40 @@ def lagrange(order, quad, xyz, conn, dofs, ndof, tris=None, faces=None, test_ord
     return lam_node, rowptr, colind, vals, fe, fl
 
 
+def mtm(b_rowptr, b_colind, b_vals, ndof):
+    """M^T M of a CSR M (here B): the structural product pattern (every pair of
+    entries of a row couples, zeros kept, as EpetraExt::MatrixMatrix::Multiply
+    builds it for epetraSaddleAssembler::setMTM) with values summed over the rows
+    in ascending order.  Returns (rowptr, colind, values) over ndof rows."""
+    nl = b_rowptr.shape[0] - 1
+    I, J, V = [], [], []
+    for l in range(nl):
+        c = b_colind[b_rowptr[l]:b_rowptr[l + 1]].astype(np.int64)
+        v = b_vals[b_rowptr[l]:b_rowptr[l + 1]]
+        I.append(np.repeat(c, len(c)))
+        J.append(np.tile(c, len(c)))
+        V.append(np.outer(v, v).reshape(-1))
+    if not I:
+        return np.zeros(ndof + 1, np.int32), np.zeros(0, np.int32), np.zeros(0)
+    I, J, V = np.concatenate(I), np.concatenate(J), np.concatenate(V)
+    key = I * ndof + J
+    ukey, pos = np.unique(key, return_inverse=True)
+    vals = np.zeros(len(ukey))
+    np.add.at(vals, pos.reshape(-1), V)  # sequential: ascending multiplier row
+    rowptr = np.zeros(ndof + 1, dtype=np.int64)
+    np.add.at(rowptr, ukey // ndof + 1, 1)
+    return np.cumsum(rowptr).astype(np.int32), (ukey % ndof).astype(np.int32), vals
+
+
 def saddle(k_rowptr, k_colind, k_vals, b_rowptr, b_colind, b_vals, ndof, lam_diag=False, eye_field=0.0,
-           eye_lam=0.0):
-    """[K + eye_field I, B^T; B, eye_lam I] over (ndof + n_multipliers) rows, the
-    layout of epetraSaddleAssembler::setDiagMatrix(K, field block) plus
-    setSymmMatrix(B, multiplier block, field block) and setEye on the blocks
-    (epetraSaddleAssembler.cpp); the multiplier diagonal is stored only with
-    lam_diag.  Returns (rowptr, colind, values)."""
+           eye_lam=0.0, with_mtm=False, mtm_scale=0.0):
+    """[K + eye_field I + mtm_scale B^T B, B^T; B, eye_lam I] over (ndof +
+    n_multipliers) rows, the layout of epetraSaddleAssembler::setDiagMatrix(K,
+    field block) plus setSymmMatrix(B, multiplier block, field block), setMTM(B,
+    field block, scale) and setEye on the blocks (epetraSaddleAssembler.cpp).
+    The field rows hold the union of K's and (with_mtm) B^T B's columns; the
+    multiplier diagonal is stored only with lam_diag.  Returns (rowptr, colind,
+    values)."""
     nl = b_rowptr.shape[0] - 1
     brow = np.repeat(np.arange(nl), np.diff(b_rowptr))
     order = np.lexsort((brow, b_colind))  # B^T rows: by field column, then multiplier
@@ -297,30 +324,32 @@ def saddle(k_rowptr, k_colind, k_vals, b_rowptr, b_colind, b_vals, ndof, lam_dia
     t_ptr = np.concatenate([[0], np.cumsum(t_cnt)])
     t_col = ndof + brow[order]
     t_val = b_vals[order]
-    cols, vals = [], []
+    if with_mtm:
+        m_rp, m_ci, m_v = mtm(b_rowptr, b_colind, b_vals, ndof)
+    rows_c, rows_v = [], []
     for r in range(ndof):
         k0, k1 = k_rowptr[r], k_rowptr[r + 1]
-        kv = np.array(k_vals[k0:k1], dtype=np.float64)
-        kv[k_colind[k0:k1] == r] += eye_field
-        cols += [k_colind[k0:k1], t_col[t_ptr[r]:t_ptr[r + 1]]]
-        vals += [kv, t_val[t_ptr[r]:t_ptr[r + 1]]]
+        acc = {int(c): float(v) for c, v in zip(k_colind[k0:k1], k_vals[k0:k1])}
+        if with_mtm:
+            for c, v in zip(m_ci[m_rp[r]:m_rp[r + 1]], m_v[m_rp[r]:m_rp[r + 1]]):
+                acc[int(c)] = acc.get(int(c), 0.0) + mtm_scale * v
+        if r in acc:
+            acc[r] += eye_field
+        cols = sorted(acc)
+        rows_c.append(np.concatenate([np.array(cols, dtype=np.int64), t_col[t_ptr[r]:t_ptr[r + 1]]]))
+        rows_v.append(np.concatenate([np.array([acc[c] for c in cols]), t_val[t_ptr[r]:t_ptr[r + 1]]]))
     for l in range(nl):
-        cols.append(b_colind[b_rowptr[l]:b_rowptr[l + 1]])
-        vals.append(b_vals[b_rowptr[l]:b_rowptr[l + 1]])
+        c = b_colind[b_rowptr[l]:b_rowptr[l + 1]].astype(np.int64)
+        v = np.asarray(b_vals[b_rowptr[l]:b_rowptr[l + 1]], dtype=np.float64)
         if lam_diag:
-            cols.append(np.array([ndof + l]))
-            vals.append(np.array([eye_lam]))
-    lens = [0] * (ndof + nl)
-    i = 0
-    for r in range(ndof):
-        lens[r] = len(cols[i]) + len(cols[i + 1])
-        i += 2
-    for l in range(nl):
-        lens[ndof + l] = len(cols[i]) + (len(cols[i + 1]) if lam_diag else 0)
-        i += 2 if lam_diag else 1
+            c = np.append(c, ndof + l)
+            v = np.append(v, eye_lam)
+        rows_c.append(c)
+        rows_v.append(v)
+    lens = [len(c) for c in rows_c]
     rowptr = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
-    colind = np.concatenate(cols).astype(np.int32) if cols else np.zeros(0, np.int32)
-    values = np.concatenate(vals).astype(np.float64) if vals else np.zeros(0)
+    colind = np.concatenate(rows_c).astype(np.int32) if rows_c else np.zeros(0, np.int32)
+    values = np.concatenate(rows_v).astype(np.float64) if rows_v else np.zeros(0)
     return rowptr, colind, values
 
 

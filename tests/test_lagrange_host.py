@@ -147,11 +147,12 @@ def _tris_on_plane(m, axis, value):
     return fn[on][:, ::-1].copy()  # any vertex order
 
 
+@pytest.mark.parametrize("mtm", [False, True])
 @pytest.mark.parametrize("test_order", [1, 0])
 @pytest.mark.parametrize("order", [1, 2])
 @pytest.mark.parametrize("select", [None, "x0", "x0z1"])
 @pytest.mark.parametrize("lam_diag", [False, True])
-def test_patterns_match_oracle(order, select, lam_diag, test_order):
+def test_patterns_match_oracle(order, select, lam_diag, test_order, mtm):
     m, mesh, b = _mesh(4 if order == 1 else 3, order, seed=11)
     tris = None
     if select == "x0":
@@ -159,30 +160,34 @@ def test_patterns_match_oracle(order, select, lam_diag, test_order):
     elif select == "x0z1":  # in an order unrelated to the faces': P0 multipliers follow it
         tris = np.concatenate([_tris_on_plane(m, 2, 1.0), _tris_on_plane(m, 0, 0.0)])
         tris = tris[np.random.default_rng(3).permutation(len(tris))]
-    lg = mg.LagrangeBuilder(b, tris=tris, lam_diag=lam_diag, test_order=test_order)
+    lg = mg.LagrangeBuilder(b, tris=tris, lam_diag=lam_diag, test_order=test_order, mtm=mtm)
     lam, fe, fl = lg.multipliers()
     (brp, bci), (srp, sci) = lg.pattern()
     dofs = mesh.elem_dofs()
     olam, obrp, obci, obv, ofe, ofl = orc.lagrange(order, 1, m.xyz, m.conn, dofs, b.ndof, tris=tris,
                                                    test_order=test_order)
+    if mtm:
+        mrp, mci, _ = orc.mtm(obrp, obci, obv, b.ndof)
+        assert lg.nnz_mtm == len(mci)
     assert np.array_equal(fe, ofe) and np.array_equal(fl, ofl)
     assert np.array_equal(lam, olam)
     assert np.array_equal(brp, obrp) and np.array_equal(bci, obci)
     rp, ci = b.pattern()
-    orp, oci, _ = orc.saddle(rp, ci, np.zeros(len(ci)), obrp, obci, obv, b.ndof, lam_diag=lam_diag)
+    orp, oci, _ = orc.saddle(rp, ci, np.zeros(len(ci)), obrp, obci, obv, b.ndof, lam_diag=lam_diag, with_mtm=mtm)
     assert np.array_equal(srp, orp) and np.array_equal(sci, oci)
     if select is not None:
         assert lg.n_faces == len(tris)
 
 
+@pytest.mark.parametrize("mtm", [False, True])
 @pytest.mark.parametrize("test_order", [1, 0])
 @pytest.mark.parametrize("order", [1, 2])
 @pytest.mark.parametrize("quad", [1, 6])
-def test_kernel_data_flow_matches_oracle(face_lib, order, quad, test_order):
+def test_kernel_data_flow_matches_oracle(face_lib, order, quad, test_order, mtm):
     """The two kernels' data flow on the host: face matrices (the kernel's own
     arithmetic), the per-entry gather lists of B, the saddle source map."""
     m, mesh, b = _mesh(4 if order == 1 else 3, order, seed=13)
-    lg = mg.LagrangeBuilder(b, lam_diag=True, test_order=test_order)
+    lg = mg.LagrangeBuilder(b, lam_diag=True, test_order=test_order, mtm=mtm)
     lam, fe, fl = lg.multipliers()
     (brp, bci), (srp, sci) = lg.pattern()
     bptr, bsrc, ssrc = lg.export_maps()
@@ -196,11 +201,28 @@ def test_kernel_data_flow_matches_oracle(face_lib, order, quad, test_order):
     # saddle values through the source map
     rp, ci = b.pattern()
     kv = np.random.default_rng(1).uniform(-1, 1, len(ci))
+    # k_saddle_fill
     bidx = np.clip(-(ssrc.astype(np.int64) + 1), 0, lg.nnz_b - 1)
     sv = np.where(ssrc >= 0, kv[np.maximum(ssrc, 0)], bv[bidx])
-    sv[ssrc == np.iinfo(np.int32).min] = 0.0
-    orp_s, oci_s, osv = orc.saddle(rp, ci, kv, brp, bci, bv, b.ndof, lam_diag=True)
-    assert np.array_equal(srp, orp_s) and np.array_equal(sci, oci_s) and np.array_equal(sv, osv)
+    sv[ssrc == np.iinfo(np.int32).min] = -0.25         # eye_lam
+    sv[ssrc == np.iinfo(np.int32).min + 1] = 0.0        # B^T B entries outside K
+    # k_saddle_eye at each field row's diagonal entry
+    nd = b.ndof
+    for r in range(nd):
+        hit = np.nonzero(sci[srp[r]:srp[r + 1]] == r)[0]
+        if len(hit):
+            sv[srp[r] + hit[0]] += 0.5
+    # k_saddle_mtm
+    if mtm:
+        pp, pairs, slot = lg.export_mtm()
+        for mm in range(lg.nnz_mtm):
+            pr = pairs[pp[mm]:pp[mm + 1]]
+            sv[slot[mm]] += 2.0 * np.sum(bv[pr[:, 0]] * bv[pr[:, 1]])
+        assert len(np.unique(slot)) == lg.nnz_mtm  # one saddle entry per B^T B entry
+    orp_s, oci_s, osv = orc.saddle(rp, ci, kv, brp, bci, bv, nd, lam_diag=True, eye_field=0.5, eye_lam=-0.25,
+                                   with_mtm=mtm, mtm_scale=2.0)
+    assert np.array_equal(srp, orp_s) and np.array_equal(sci, oci_s)
+    assert row_scaled_err(orp_s, osv, sv) <= 1e-14
 
 def test_selected_triangles_errors():
     m, mesh, b = _mesh(3, 1)

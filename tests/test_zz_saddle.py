@@ -203,3 +203,28 @@ def test_p0_multipliers_match_oracle(order, quad):
     assert lg.n_multipliers == len(tris) and np.array_equal(brp, rp) and np.array_equal(bci, ci)
     assert row_scaled_err(rp, ref, got.cpu().numpy()) <= 1e-12
     assert torch.equal(got, again)
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_saddle_with_mtm_matches_oracle(order):
+    """setMTM: K + eye_field I + scale B^T B on the field block (structural
+    B^T B pattern merged into K's), the multiplier diagonal, and the products."""
+    m, mesh, b, _, _ = _setup(4 if order == 1 else 3, order, 28)
+    lg = mg.LagrangeBuilder(b, lam_diag=True, mtm=True)
+    kappa = meshgen.lognormal(len(m.conn), 1.0, 28)
+    K = b.assemble("stiff_kappa", coeff=kappa, quad=4)
+    B = lg.assemble(quad=3)
+    S = lg.saddle(K, B, eye_field=0.5, eye_lam=-0.25, mtm_scale=3.0)
+    S2 = lg.saddle(K, B, eye_field=0.5, eye_lam=-0.25, mtm_scale=3.0)
+    dofs, rp, ci, kref = orc.full_operator("stiff_kappa", order, 4, m.xyz, m.conn, coeff=kappa)
+    _, brp, bci, bref, _, _ = orc.lagrange(order, 3, m.xyz, m.conn, dofs, b.ndof)
+    srp, sci, sref = orc.saddle(rp, ci, kref, brp, bci, bref, b.ndof, lam_diag=True, eye_field=0.5, eye_lam=-0.25,
+                                with_mtm=True, mtm_scale=3.0)
+    (_, _), (gsrp, gsci) = lg.pattern()
+    assert np.array_equal(gsrp, srp) and np.array_equal(gsci, sci)
+    assert row_scaled_err(srp, sref, S.cpu().numpy()) <= 1e-12
+    assert torch.equal(S, S2)
+    x = np.random.default_rng(6).uniform(-1, 1, b.ndof + lg.n_multipliers)
+    y = lg.saddle_apply(S, torch.from_numpy(x).cuda()).cpu().numpy()
+    yref = orc.csr_matvec(srp, sci, sref, x)
+    assert np.abs(y - yref).max() <= 1e-12 * np.abs(yref).max()
