@@ -335,6 +335,7 @@ typedef struct {
   int64_t nnz_saddle;     /* (ndof + n_multipliers) rows */
   int64_t nnz_mtm;        /* entries of B^T B (MG_SADDLE_MTM), else 0 */
   int64_t n_mtm_products; /* products B_li B_lj they sum */
+  int64_t n_edge_multipliers; /* P2: multipliers on boundary edges (the last ones), else 0 */
 } mg_lagrange_info;
 
 /* Saddle pattern options of mg_lagrange_build. */
@@ -356,9 +357,13 @@ enum {
    - test_order 0 (fePr2d<0>): one per triangle, numbered in the boundary
      grid's element order: the order of h_tris (the Gmsh triangles, whose ids
      the boundary elements keep: src/morganaGeometry/meshInit3d.hpp:400-430),
-     or the face order when h_tris is NULL.
+     or the face order when h_tris is NULL;
+   - test_order 2 (fePr2d<2>): the P1 ones, then one per edge of the selected
+     triangles in (min node, max node) order, the boundary grid's edge
+     numbering under pMapItem (src/morganaGeometry/connect2d.hpp:336-451);
+     MG_ERR_UNSUPPORTED on MG_EDGES_FIRST meshes.
    B (n_multipliers x ndof): each face inserts its full nt x nb block (nt = 3
-   for P1, 1 for P0), explicit zeros included, as
+   for P1, 1 for P0, 6 for P2), explicit zeros included, as
    traitsMatrixBuilder::buildEpetraCrs does for localMatrixLA3d
    (src/morganaFiniteElements/localMatrixLA3d.hpp:292-322).
    Saddle: [K B^T; B 0] (epetraSaddleAssembler::setDiagMatrix + setSymmMatrix,
@@ -375,11 +380,13 @@ mg_status mg_lagrange_build(mg_plan* plan, int32_t test_order, int64_t n_tris, c
                             int32_t flags, mg_lagrange** out);
 mg_status mg_lagrange_destroy(mg_lagrange* lg);
 mg_status mg_lagrange_get_info(const mg_lagrange* lg, mg_lagrange_info* info);
-/* h_lam_node (n_multipliers): node (P1) or selected face (P0, an index into
-   the face list) of each multiplier; h_face_elem, h_face_local (n_faces): the
-   selected faces; any pointer may be NULL. */
+/* h_lam_node (n_multipliers): node (P1, P2 vertex), selected face (P0, an
+   index into the face list) or -1 (P2 edge) of each multiplier; h_face_elem,
+   h_face_local (n_faces): the selected faces; any pointer may be NULL. */
 mg_status mg_lagrange_export(const mg_lagrange* lg, int32_t* h_lam_node, int32_t* h_face_elem,
                              int32_t* h_face_local);
+/* P2: (min node, max node) of each edge multiplier, n_edge_multipliers x 2. */
+mg_status mg_lagrange_export_edges(const mg_lagrange* lg, int32_t* h_edge_nodes);
 /* CSR of B (n_multipliers + 1, nnz_b) and of the saddle matrix
    (ndof + n_multipliers + 1, nnz_saddle); any pointer may be NULL. */
 mg_status mg_lagrange_pattern(const mg_lagrange* lg, int32_t* h_b_rowptr, int32_t* h_b_colind,

@@ -74,7 +74,7 @@ _I32, _I64, _D = ctypes.c_int32, ctypes.c_int64, ctypes.c_double
 # name -> argtypes; every function returns mg_status (int) unless listed in _RESTYPES
 class LagrangeInfo(ctypes.Structure):
     _fields_ = [("n_faces", _I64), ("n_multipliers", _I64), ("ndof", _I64), ("nnz_b", _I64),
-                ("nnz_saddle", _I64), ("nnz_mtm", _I64), ("n_mtm_products", _I64)]
+                ("nnz_saddle", _I64), ("nnz_mtm", _I64), ("n_mtm_products", _I64), ("n_edge_multipliers", _I64)]
 
 
 SIGNATURES = {
@@ -114,6 +114,7 @@ SIGNATURES = {
     "mg_lagrange_assemble_host": [_P, _I32, _P],
     "mg_saddle_assemble": [_P, _P, _P, _D, _D, _D, _P, _P],
     "mg_lagrange_export_mtm": [_P, _P, _P, _P],
+    "mg_lagrange_export_edges": [_P, _P],
     "mg_saddle_spmv": [_P, _P, _P, _P, _P],
     "mg_lagrange_apply": [_P, _P, _P, _P, _P],
     "mg_status_string": [_I32],
@@ -420,7 +421,8 @@ class LagrangeBuilder:
         """tris: (k, 3) node ids of the boundary triangles that carry multipliers
         (the test field's geoId filter); None = every boundary face.
         test_order: 1 = P1 multipliers (one per boundary node), 0 = P0 (one per
-        triangle, in the order of tris).  lam_diag: store the multiplier block's
+        triangle, in the order of tris), 2 = P2 (the P1 ones, then one per
+        boundary edge in (min node, max node) order).  lam_diag: store the multiplier block's
         diagonal; mtm: merge B^T B into the field block (setMTM)."""
         self.builder = builder
         self.test_order = test_order
@@ -435,6 +437,7 @@ class LagrangeBuilder:
         self.n_faces, self.n_multipliers = info.n_faces, info.n_multipliers
         self.ndof, self.nnz_b, self.nnz_saddle = info.ndof, info.nnz_b, info.nnz_saddle
         self.nnz_mtm, self.n_mtm_products = info.nnz_mtm, info.n_mtm_products
+        self.n_edge_multipliers = info.n_edge_multipliers
 
     def multipliers(self):
         """(node (P1) or face index (P0) of each multiplier, face element, face local index)."""
@@ -457,7 +460,7 @@ class LagrangeBuilder:
     def export_maps(self):
         """(b_src_ptr, b_src, s_src): the gather maps of the B and saddle kernels."""
         nb = 4 if self.builder.mesh.order == 1 else 10
-        nt = 3 if self.test_order == 1 else 1
+        nt = {0: 1, 1: 3, 2: 6}[self.test_order]
         bp = np.empty(self.nnz_b + 1, dtype=np.int32)
         bs = np.empty(self.n_faces * nt * nb, dtype=np.int32)
         ss = np.empty(self.nnz_saddle, dtype=np.int32)
@@ -488,6 +491,12 @@ class LagrangeBuilder:
         _check(lib().mg_lagrange_assemble_host(self._h, quad, _ptr(vals)), "mg_lagrange_assemble_host")
         (rp, ci), _ = self.pattern()
         return Csr(rp, ci, vals)
+
+    def edge_multipliers(self):
+        """P2: (min node, max node) of each edge multiplier (they follow the vertex ones)."""
+        out = np.empty((self.n_edge_multipliers, 2), dtype=np.int32)
+        _check(lib().mg_lagrange_export_edges(self._h, _ptr(out)), "mg_lagrange_export_edges")
+        return out
 
     def export_mtm(self):
         """(pair_ptr, pairs (n, 2), slot) of the B^T B block (built with mtm=True)."""

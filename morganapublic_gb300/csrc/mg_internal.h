@@ -211,11 +211,13 @@ constexpr int32_t kSrcZero = INT32_MIN + 1;
 struct mg_lagrange {
   mg_plan* plan = nullptr;
   int order = 1, nb = 4;
-  int test_order = 1, nt = 3;  // multiplier basis: P1 (3 per face) or P0 (1 per face)
+  int test_order = 1, nt = 3;  // multiplier basis: P1 (3 per face), P0 (1) or P2 (6)
   bool lam_diag = false;  // the saddle pattern holds the multiplier block's diagonal
   int64_t ndof = 0, n_faces = 0, nl = 0, nnz_b = 0, nnz_s = 0;
   std::vector<int32_t> face_elem, face_local;  // selected boundary faces, element then local-face order
-  std::vector<int32_t> lam_node;               // node (P1, ascending) or face (P0) of each multiplier
+  std::vector<int32_t> lam_node;  // node (P1/P2 vertex, ascending), face (P0) or -1 (P2 edge) per multiplier
+  std::vector<int32_t> lam_edge;  // P2: (min, max) nodes of each edge multiplier, after the vertex ones
+  int64_t n_vertex_lam = 0;
   std::vector<int32_t> b_rowptr, b_colind;     // B: nl x ndof
   // per B entry k, the face-matrix entries it sums, b_src[b_src_ptr[k] .. b_src_ptr[k+1]),
   // each (f * nt + a) * nb + i, ascending (the reference's insertion order)

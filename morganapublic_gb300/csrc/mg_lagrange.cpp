@@ -112,6 +112,15 @@ mg_status boundary_flags(const mg_mesh* m, std::vector<uint8_t>* flag)
   return MG_OK;
 }
 
+// Edge j of the P2 test basis of local face lf of element e: face vertices
+// (j, j + 1 mod 3), as a (min node, max node) key.
+uint64_t face_edge_key(const mg_mesh* m, int32_t e, int lf, int j)
+{
+  const int32_t* c = m->conn.data() + 4 * (int64_t)e;
+  const int32_t p = c[face_vertex(lf, j)], q = c[face_vertex(lf, j == 2 ? 0 : j + 1)];
+  return (uint64_t)(uint32_t)std::min(p, q) << 32 | (uint32_t)std::max(p, q);
+}
+
 }  // namespace
 
 static mg_status build_lagrange(mg_lagrange* lg, int test_order, int64_t n_tris, const int32_t* h_tris,
@@ -123,7 +132,10 @@ static mg_status build_lagrange(mg_lagrange* lg, int test_order, int64_t n_tris,
   const int64_t E = m->n_elem, N = m->n_nodes, nd = m->ndof;
   lg->order = m->order;
   lg->test_order = test_order;
-  lg->nt = test_order == 1 ? 3 : 1;
+  lg->nt = test_order == 2 ? 6 : (test_order == 1 ? 3 : 1);
+  if (test_order == 2 && m->edge_rule != MG_EDGES_LEX)
+    return set_error(MG_ERR_UNSUPPORTED,
+                     "mg_lagrange_build: P2 multipliers follow the boundary edges' LEX numbering (MG_EDGES_LEX meshes)");
   const int nt = lg->nt;
   lg->lam_diag = lam_diag;
   lg->mtm = mtm;
@@ -185,8 +197,10 @@ static mg_status build_lagrange(mg_lagrange* lg, int test_order, int64_t n_tris,
   // multipliers: P1 the nodes of the selected faces, ascending; P0 one per face,
   // in the order of `rank`
   std::vector<int32_t> lam_of;
+  std::vector<uint64_t> edge_keys;  // P2: boundary edges (min << 32 | max), ascending
   lg->lam_node.clear();
-  if (test_order == 1) {
+  lg->lam_edge.clear();
+  if (test_order >= 1) {
     lam_of.assign(N, -1);
     for (int64_t f = 0; f < nf; ++f) {
       const int32_t* c = m->conn.data() + 4 * (int64_t)lg->face_elem[f];
@@ -197,6 +211,19 @@ static mg_status build_lagrange(mg_lagrange* lg, int test_order, int64_t n_tris,
         lam_of[i] = (int32_t)lg->lam_node.size();
         lg->lam_node.push_back((int32_t)i);
       }
+    lg->n_vertex_lam = (int64_t)lg->lam_node.size();
+    if (test_order == 2) {  // then the edges of the selected faces, (min, max) order
+      edge_keys.reserve(3 * nf);
+      for (int64_t f = 0; f < nf; ++f)
+        for (int j = 0; j < 3; ++j) edge_keys.push_back(face_edge_key(m, lg->face_elem[f], lg->face_local[f], j));
+      std::sort(edge_keys.begin(), edge_keys.end());
+      edge_keys.erase(std::unique(edge_keys.begin(), edge_keys.end()), edge_keys.end());
+      for (const uint64_t k : edge_keys) {
+        lg->lam_node.push_back(-1);
+        lg->lam_edge.push_back((int32_t)(k >> 32));
+        lg->lam_edge.push_back((int32_t)(k & 0xffffffffu));
+      }
+    }
   } else {
     lg->lam_node.resize(nf);
     for (int64_t f = 0; f < nf; ++f) lg->lam_node[rank[f]] = (int32_t)f;
@@ -217,8 +244,16 @@ static mg_status build_lagrange(mg_lagrange* lg, int test_order, int64_t n_tris,
     const int64_t e = lg->face_elem[f];
     const int32_t* c = m->conn.data() + 4 * e;
     for (int a = 0; a < nt; ++a) {
-      const uint64_t row = test_order == 1 ? (uint64_t)lam_of[c[face_vertex(lg->face_local[f], a)]]
-                                           : (uint64_t)rank[f];
+      uint64_t row;
+      if (test_order == 0) {
+        row = (uint64_t)rank[f];
+      } else if (a < 3) {
+        row = (uint64_t)lam_of[c[face_vertex(lg->face_local[f], a)]];
+      } else {  // P2 edge function of face edge a - 3
+        const uint64_t key = face_edge_key(m, (int32_t)e, lg->face_local[f], a - 3);
+        row = (uint64_t)(lg->n_vertex_lam + (std::lower_bound(edge_keys.begin(), edge_keys.end(), key) -
+                                             edge_keys.begin()));
+      }
       for (int i = 0; i < nb; ++i) {
         const int64_t s = (f * nt + a) * nb + i;
         pairs[s] = Pair{row << 32 | (uint64_t)(uint32_t)m->dofs[e * nb + i], (int32_t)s};
@@ -442,8 +477,8 @@ mg_status mg_lagrange_build(mg_plan* plan, int32_t test_order, int64_t n_tris, c
 {
   NvtxRange nvtx_range("mg_lagrange_build");
   if (!plan || !out) return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_build: null argument");
-  if (test_order != 0 && test_order != 1)
-    return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_build: multipliers are P1 (1) or P0 (0)");
+  if (test_order < 0 || test_order > 2)
+    return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_build: multipliers are P0 (0), P1 (1) or P2 (2)");
   if (flags & ~(MG_SADDLE_LAM_DIAG | MG_SADDLE_MTM)) return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_build: bad flags");
   if (n_tris < 0 || (n_tris > 0 && !h_tris)) return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_build: bad triangle list");
   *out = nullptr;
@@ -481,6 +516,7 @@ mg_status mg_lagrange_get_info(const mg_lagrange* lg, mg_lagrange_info* info)
   info->nnz_b = lg->nnz_b;
   info->nnz_saddle = lg->nnz_s;
   info->nnz_mtm = lg->nnz_m;
+  info->n_edge_multipliers = (int64_t)lg->lam_edge.size() / 2;
   info->n_mtm_products = (int64_t)lg->m_pairs.size();
   return MG_OK;
 }
@@ -511,6 +547,14 @@ mg_status mg_lagrange_export_maps(const mg_lagrange* lg, int32_t* h_b_src_ptr, i
   if (h_b_src_ptr) std::memcpy(h_b_src_ptr, lg->b_src_ptr.data(), sizeof(int32_t) * lg->b_src_ptr.size());
   if (h_b_src && !lg->b_src.empty()) std::memcpy(h_b_src, lg->b_src.data(), sizeof(int32_t) * lg->b_src.size());
   if (h_s_src && lg->nnz_s) std::memcpy(h_s_src, lg->s_src.data(), sizeof(int32_t) * lg->nnz_s);
+  return MG_OK;
+}
+
+mg_status mg_lagrange_export_edges(const mg_lagrange* lg, int32_t* h_edge_nodes)
+{
+  if (!lg) return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_export_edges: null handle");
+  if (h_edge_nodes && !lg->lam_edge.empty())
+    std::memcpy(h_edge_nodes, lg->lam_edge.data(), sizeof(int32_t) * lg->lam_edge.size());
   return MG_OK;
 }
 

@@ -134,14 +134,18 @@ mg_status mg_lagrange_assemble(mg_lagrange* lg, int32_t quad, double* d_b_values
   const mg_mesh* m = lg->plan->mesh;
   const int g = grid_for(lg->n_faces);
   const int64_t F = lg->n_faces;
-  if (lg->nb == 4 && lg->nt == 3)
-    k_face_matrix<4, 3><<<g, kFaceThreads, 0, st>>>(F, lg->d_faces, m->d_conn, m->d_xyz, rule, lg->d_face_mat);
-  else if (lg->nb == 4)
-    k_face_matrix<4, 1><<<g, kFaceThreads, 0, st>>>(F, lg->d_faces, m->d_conn, m->d_xyz, rule, lg->d_face_mat);
-  else if (lg->nt == 3)
-    k_face_matrix<10, 3><<<g, kFaceThreads, 0, st>>>(F, lg->d_faces, m->d_conn, m->d_xyz, rule, lg->d_face_mat);
-  else
-    k_face_matrix<10, 1><<<g, kFaceThreads, 0, st>>>(F, lg->d_faces, m->d_conn, m->d_xyz, rule, lg->d_face_mat);
+#define MG_FACE_LAUNCH(NB_, NT_) \
+  k_face_matrix<NB_, NT_><<<g, kFaceThreads, 0, st>>>(F, lg->d_faces, m->d_conn, m->d_xyz, rule, lg->d_face_mat)
+  if (lg->nb == 4) {
+    if (lg->nt == 3) MG_FACE_LAUNCH(4, 3);
+    else if (lg->nt == 1) MG_FACE_LAUNCH(4, 1);
+    else MG_FACE_LAUNCH(4, 6);
+  } else {
+    if (lg->nt == 3) MG_FACE_LAUNCH(10, 3);
+    else if (lg->nt == 1) MG_FACE_LAUNCH(10, 1);
+    else MG_FACE_LAUNCH(10, 6);
+  }
+#undef MG_FACE_LAUNCH
   MG_CUDA(cudaGetLastError());
   k_gather_sum<<<grid_for(lg->nnz_b), kFaceThreads, 0, st>>>(lg->nnz_b, lg->d_b_src_ptr, lg->d_b_src, lg->d_face_mat,
                                                           d_b_values);

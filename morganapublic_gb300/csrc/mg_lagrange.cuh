@@ -5,7 +5,9 @@
 //
 // Face f is local face lf of tet e.  Its local matrix, rows = the test basis of
 // the boundary triangle (P1: the face's three vertices in face order; P0: the
-// constant 1), columns = the tet's nb field basis functions, is
+// constant 1; P2: the vertex functions l_a (2 l_a - 1), then 4 l_p l_q on the
+// face's edges (0,1), (1,2), (2,0)), columns = the tet's nb field basis
+// functions, is
 //   mat[a * nb + i] = sum_q w_q |Vx ^ Vy| psi_a(q) phi_i(q)
 // (integratorOLA3d_STD.hpp:102-124 around opLA3dA.hpp:86-112).  On the face the
 // tet's barycentric coordinates are the face's own (lambda_a at vertex
@@ -79,8 +81,8 @@ inline bool face_rule(int quad, FaceRule* r)
 }
 
 // Local matrix of local face lf; P[a] = coordinates of face vertex a (face
-// order), mat = NT x NB, row-major (test basis, field basis); NT = 3 (P1 test)
-// or 1 (P0 test).
+// order), mat = NT x NB, row-major (test basis, field basis); NT = 3 (P1 test),
+// 1 (P0 test) or 6 (P2 test).
 template <int NB, int NT>
 MG_HD inline void face_matrix(const double P[3][3], int lf, const FaceRule& r, double* mat)
 {
@@ -93,7 +95,7 @@ MG_HD inline void face_matrix(const double P[3][3], int lf, const FaceRule& r, d
   const double n1 = vx[2] * vy[0] - vx[0] * vy[2];
   const double n2 = vx[0] * vy[1] - vx[1] * vy[0];
   const double area2 = sqrt(n0 * n0 + n1 * n1 + n2 * n2);
-  static_assert(NT == 1 || NT == 3, "P0 or P1 test basis");
+  static_assert(NT == 1 || NT == 3 || NT == 6, "P0, P1 or P2 test basis");
   for (int k = 0; k < NT * NB; ++k) mat[k] = 0.0;
   for (int q = 0; q < r.nq; ++q) {
     const double lam[3] = {1.0 - r.x[q] - r.y[q], r.x[q], r.y[q]};
@@ -106,9 +108,18 @@ MG_HD inline void face_matrix(const double P[3][3], int lf, const FaceRule& r, d
       for (int v = 0; v < 4; ++v) phi[v] = L[v] * (2.0 * L[v] - 1.0);
       for (int j = 0; j < 6; ++j) phi[4 + j] = 4.0 * L[edge_vertex(j, 0)] * L[edge_vertex(j, 1)];
     }
+    double psi[NT];
+    if constexpr (NT == 1) {
+      psi[0] = 1.0;
+    } else if constexpr (NT == 3) {
+      for (int a = 0; a < 3; ++a) psi[a] = lam[a];
+    } else {
+      for (int a = 0; a < 3; ++a) psi[a] = lam[a] * (2.0 * lam[a] - 1.0);
+      for (int j = 0; j < 3; ++j) psi[3 + j] = 4.0 * lam[j] * lam[j == 2 ? 0 : j + 1];
+    }
     const double s = area2 * r.w[q];
     for (int a = 0; a < NT; ++a) {
-      const double c = (NT == 3 ? lam[a] : 1.0) * s;
+      const double c = psi[a] * s;
       for (int i = 0; i < NB; ++i) mat[a * NB + i] += phi[i] * c;
     }
   }

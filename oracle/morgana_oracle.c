@@ -735,7 +735,9 @@ static const double REF_TET[4][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}}
      mat[a * nb + i] = sum_q (phi_i(Yv) psi_a(Ys)) |Vx ^ Vy| w_q,
    i over the tet's nb basis functions and a over the test basis of the
    boundary triangle: test_order 1 (fePr2d<1>) the face's points in face order,
-   test_order 0 (fePr2d<0>) the one constant psi = 1.
+   test_order 0 (fePr2d<0>) the one constant psi = 1, test_order 2 (fePr2d<2>)
+   the three vertex functions l_a (2 l_a - 1) then the edge functions
+   4 l_p l_q of the face's edges (0,1), (1,2), (2,0).
    Vx, Vy: derivatives of the linear map of the reference triangle onto the
    face (geoMapInterface.hpp:25-90, point 3 first).  Yv: the same map onto the
    reference tet's face (supportLagrange3d mapVolumeY).  Ys: the point in the
@@ -746,8 +748,8 @@ static const double REF_TET[4][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}}
 int or_face_matrix(int order, int test_order, int prec, const double *xyz, const int32_t *nodes4, int lf,
                    double *mat)
 {
-  if (lf < 0 || lf > 3 || (test_order != 0 && test_order != 1)) return OR_ERR_ARG;
-  const int nt = test_order == 1 ? 3 : 1;
+  if (lf < 0 || lf > 3 || test_order < 0 || test_order > 2) return OR_ERR_ARG;
+  const int nt = test_order == 2 ? 6 : (test_order == 1 ? 3 : 1);
   double Y[12], W[6];
   const int nq = or_tri_rule(prec, Y, W);
   if (nq == 0) return OR_ERR_ARG;
@@ -769,7 +771,9 @@ int or_face_matrix(int order, int test_order, int prec, const double *xyz, const
     const double x = Y[2 * q], y = Y[2 * q + 1];
     const double lam[3] = {1.0 - x - y, x, y};
     const double one[1] = {1.0};
-    const double *psi = test_order == 1 ? lam : one;
+    const double p2[6] = {lam[0] * (2 * lam[0] - 1), lam[1] * (2 * lam[1] - 1), lam[2] * (2 * lam[2] - 1),
+                          4 * lam[0] * lam[1], 4 * lam[1] * lam[2], 4 * lam[2] * lam[0]};
+    const double *psi = test_order == 2 ? p2 : (test_order == 1 ? lam : one);
     double Yv[3], phi[10];
     for (int k = 0; k < 3; ++k)
       Yv[k] = REF_TET[FACE_PTS[lf][2]][k] * lam[2] +
@@ -785,7 +789,7 @@ int or_face_matrix(int order, int test_order, int prec, const double *xyz, const
 int or_face_matrices(int order, int test_order, int prec, const double *xyz, int64_t n_faces,
                      const int32_t *conn, const int32_t *face_elem, const int32_t *face_local, double *out)
 {
-  const int nb = nbasis(order), nt = test_order == 1 ? 3 : 1;
+  const int nb = nbasis(order), nt = test_order == 2 ? 6 : (test_order == 1 ? 3 : 1);
   for (int64_t f = 0; f < n_faces; ++f) {
     int rc = or_face_matrix(order, test_order, prec, xyz, &conn[4 * (int64_t)face_elem[f]], face_local[f],
                             out + nt * nb * f);

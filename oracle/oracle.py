@@ -192,9 +192,13 @@ def tri_rule(quad: int):
     return Y[:n].copy(), W[:n].copy()
 
 
+TEST_BASIS = {0: 1, 1: 3, 2: 6}  # test functions per boundary triangle (fePr2d<0/1/2>)
+TRI_EDGES = np.array([[0, 1], [1, 2], [2, 0]])  # face-local edges of the P2 test basis
+
+
 def face_matrix(order, quad, xyz, nodes4, lf, test_order=1):
     nb = 4 if order == 1 else 10
-    nt = 3 if test_order == 1 else 1
+    nt = TEST_BASIS[test_order]
     mat = np.empty(nt * nb)
     nodes4 = np.ascontiguousarray(nodes4, dtype=np.int32)
     xyz = np.ascontiguousarray(xyz, dtype=np.float64)
@@ -228,8 +232,8 @@ def boundary_faces(conn, tris=None):
 
 
 def lagrange(order, quad, xyz, conn, dofs, ndof, tris=None, faces=None, test_order=1):
-    """B of opLA3dA with P1 (test_order 1) or P0 (test_order 0) multipliers on
-    the boundary triangles.
+    """B of opLA3dA with P1 (test_order 1), P0 (0) or P2 (2) multipliers on the
+    boundary triangles.
 
     P1 multipliers: the nodes of the selected boundary faces, numbered by
     ascending node id (meshDoctor2d.hpp:339-500 compacts the boundary grid's
@@ -237,7 +241,10 @@ def lagrange(order, quad, xyz, conn, dofs, ndof, tris=None, faces=None, test_ord
     vertices in that order).  P0 multipliers: one per selected face, numbered in
     the boundary grid's element order -- the order of `tris` when given (the
     Gmsh triangles' order, whose ids the boundary elements keep,
-    meshInit3d.hpp:400-430), else the face order.  Rows = multipliers, columns =
+    meshInit3d.hpp:400-430), else the face order.  P2 multipliers: the P1 ones,
+    then one per edge of the selected faces in (min node, max node) order (the
+    boundary grid's edges numbered under pMapItem, connect2d.hpp:336-451, kept
+    in that order by dofMapStatic2d.hpp:1166-1380).  Rows = multipliers, columns =
     field dofs; every face contributes its full local block, zeros included
     (traitsMatrixBuilder.hpp:363-441 inserts the whole block), summed in
     element, local-face, test-basis, field-basis order.  `faces` = (face_elem,
@@ -249,17 +256,23 @@ def lagrange(order, quad, xyz, conn, dofs, ndof, tris=None, faces=None, test_ord
     nb = dofs.shape[1]
     fe, fl = boundary_faces(conn, tris) if faces is None else faces
     nf = fe.shape[0]
-    nt = 3 if test_order == 1 else 1
+    nt = TEST_BASIS[test_order]
     mats = np.empty((nf, nt, nb))
     if nf:
         assert lib().or_face_matrices(order, test_order, FACE_QUAD_PREC[quad], _p(xyz), nf, _p(conn), _p(fe),
                                       _p(fl), _p(mats)) == 0
     fnodes = conn[fe[:, None], FACE_PTS[fl]] if nf else np.zeros((0, 3), np.int32)
-    if test_order == 1:
+    if test_order in (1, 2):
         lam_node = np.unique(fnodes).astype(np.int32)
         lam_of = np.full(xyz.shape[0], -1, dtype=np.int64)
         lam_of[lam_node] = np.arange(lam_node.shape[0])
         face_rows = lam_of[fnodes]
+        if test_order == 2:
+            ends = np.sort(fnodes[:, TRI_EDGES], axis=2).astype(np.int64)  # nf x 3 x 2
+            ekey = ends[:, :, 0] * xyz.shape[0] + ends[:, :, 1]
+            uedge = np.unique(ekey)
+            face_rows = np.concatenate([face_rows, len(lam_node) + np.searchsorted(uedge, ekey)], axis=1)
+            lam_node = np.concatenate([lam_node, np.full(len(uedge), -1, dtype=np.int32)])
     else:
         if tris is None:
             rank = np.arange(nf)

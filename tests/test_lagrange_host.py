@@ -48,7 +48,7 @@ def _p(a):
 
 def kernel_face_matrices(face_lib, order, quad, xyz, conn, fe, fl, test_order=1):
     nb = 4 if order == 1 else 10
-    out = np.empty((len(fe), 3 if test_order == 1 else 1, nb))
+    out = np.empty((len(fe), orc.TEST_BASIS[test_order], nb))
     xyz = np.ascontiguousarray(xyz, dtype=np.float64)
     conn = np.ascontiguousarray(conn, dtype=np.int32)
     fe = np.ascontiguousarray(fe, dtype=np.int32)
@@ -112,6 +112,28 @@ def test_oracle_p0_rows_are_face_areas(order, quad):
                 assert abs(row[node] - area[f] / 3) < 1e-15
 
 
+@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("quad", [3, 4, 6])
+def test_oracle_p2_rows_integrate_the_test_functions(order, quad):
+    """P2 multipliers: row a of B sums to int psi_a (the field basis is a partition
+    of unity): 0 for every vertex function l (2 l - 1), area / 3 per face for an
+    edge function 4 l_p l_q (degree 2: exact for the cards of 3 points and up)."""
+    m, mesh, b = _mesh(3, order)
+    dofs = mesh.elem_dofs()
+    lam, rp, ci, v, fe, fl = orc.lagrange(order, quad, m.xyz, m.conn, dofs, b.ndof, test_order=2)
+    nv = int((lam >= 0).sum())
+    fn = m.conn[fe[:, None], orc.FACE_PTS[fl]]
+    P = m.xyz[fn]
+    area = 0.5 * np.linalg.norm(np.cross(P[:, 1] - P[:, 0], P[:, 2] - P[:, 0]), axis=1)
+    rows = np.add.reduceat(v, rp[:-1])
+    assert np.abs(rows[:nv]).max() < 1e-15
+    ends = np.sort(fn[:, orc.TRI_EDGES], axis=2)
+    keys = ends[:, :, 0].astype(np.int64) * len(m.xyz) + ends[:, :, 1]
+    want = np.zeros(len(lam) - nv)
+    np.add.at(want, np.searchsorted(np.unique(keys), keys).reshape(-1), np.repeat(area / 3, 3))
+    assert np.abs(rows[nv:] - want).max() < 1e-15
+
+
 def test_oracle_p1_block_is_the_face_mass_matrix():
     m = meshgen.kuhn_cube(2, jitter=0.25, seed=5, permute=False)
     for e in range(len(m.conn)):
@@ -127,7 +149,7 @@ def test_oracle_p1_block_is_the_face_mass_matrix():
 
 
 # ------------------------------------------------------ kernel arithmetic --
-@pytest.mark.parametrize("test_order", [1, 0])
+@pytest.mark.parametrize("test_order", [1, 0, 2])
 @pytest.mark.parametrize("order", [1, 2])
 @pytest.mark.parametrize("quad", CARDS)
 def test_kernel_face_math_matches_oracle(face_lib, order, quad, test_order):
@@ -148,7 +170,7 @@ def _tris_on_plane(m, axis, value):
 
 
 @pytest.mark.parametrize("mtm", [False, True])
-@pytest.mark.parametrize("test_order", [1, 0])
+@pytest.mark.parametrize("test_order", [1, 0, 2])
 @pytest.mark.parametrize("order", [1, 2])
 @pytest.mark.parametrize("select", [None, "x0", "x0z1"])
 @pytest.mark.parametrize("lam_diag", [False, True])
@@ -171,6 +193,10 @@ def test_patterns_match_oracle(order, select, lam_diag, test_order, mtm):
         assert lg.nnz_mtm == len(mci)
     assert np.array_equal(fe, ofe) and np.array_equal(fl, ofl)
     assert np.array_equal(lam, olam)
+    if test_order == 2:  # edge multipliers: the selected faces' edges in (min, max) order
+        fn = m.conn[ofe[:, None], orc.FACE_PTS[ofl]]
+        ends = np.unique(np.sort(fn[:, orc.TRI_EDGES], axis=2).reshape(-1, 2), axis=0)
+        assert np.array_equal(lg.edge_multipliers(), ends)
     assert np.array_equal(brp, obrp) and np.array_equal(bci, obci)
     rp, ci = b.pattern()
     orp, oci, _ = orc.saddle(rp, ci, np.zeros(len(ci)), obrp, obci, obv, b.ndof, lam_diag=lam_diag, with_mtm=mtm)
@@ -180,7 +206,7 @@ def test_patterns_match_oracle(order, select, lam_diag, test_order, mtm):
 
 
 @pytest.mark.parametrize("mtm", [False, True])
-@pytest.mark.parametrize("test_order", [1, 0])
+@pytest.mark.parametrize("test_order", [1, 0, 2])
 @pytest.mark.parametrize("order", [1, 2])
 @pytest.mark.parametrize("quad", [1, 6])
 def test_kernel_data_flow_matches_oracle(face_lib, order, quad, test_order, mtm):
@@ -197,7 +223,7 @@ def test_kernel_data_flow_matches_oracle(face_lib, order, quad, test_order, mtm)
     _, orp, oci, ov, _, _ = orc.lagrange(order, quad, m.xyz, m.conn, dofs, b.ndof, test_order=test_order)
     assert row_scaled_err(orp, ov, bv) <= 1e-13
     # every face-matrix entry is used exactly once
-    assert np.array_equal(np.sort(bsrc), np.arange(len(fe) * (3 if test_order == 1 else 1) * mesh.nb))
+    assert np.array_equal(np.sort(bsrc), np.arange(len(fe) * orc.TEST_BASIS[test_order] * mesh.nb))
     # saddle values through the source map
     rp, ci = b.pattern()
     kv = np.random.default_rng(1).uniform(-1, 1, len(ci))
@@ -254,6 +280,15 @@ def test_selected_triangles_errors():
     assert empty.n_faces == 0 and empty.n_multipliers == 0 and empty.nnz_b == 0
     rp, ci = b.pattern()
     assert empty.nnz_saddle == len(ci)
+
+
+def test_p2_multipliers_need_lex_edges():
+    m = meshgen.kuhn_cube(2, jitter=0.2, seed=3, permute=True)
+    b = mg.MatrixBuilder(mg.Mesh(m.xyz, m.conn, order=2, edge_rule="first"))
+    with pytest.raises(mg.MorganaError) as e:
+        mg.LagrangeBuilder(b, test_order=2)
+    assert e.value.status == mg.MG_ERR_UNSUPPORTED
+    assert mg.LagrangeBuilder(b, test_order=1).n_multipliers > 0
 
 
 def test_face_in_three_tets_is_rejected():

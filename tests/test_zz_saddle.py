@@ -228,3 +228,20 @@ def test_saddle_with_mtm_matches_oracle(order):
     y = lg.saddle_apply(S, torch.from_numpy(x).cuda()).cpu().numpy()
     yref = orc.csr_matvec(srp, sci, sref, x)
     assert np.abs(y - yref).max() <= 1e-12 * np.abs(yref).max()
+
+
+@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("quad", [3, 6])
+def test_p2_multipliers_match_oracle(order, quad):
+    """fePr2d<2> multipliers: the boundary nodes, then the boundary edges in
+    (min node, max node) order."""
+    m, mesh, b, _, _ = _setup(4 if order == 1 else 3, order, 29)
+    lg = mg.LagrangeBuilder(b, test_order=2)
+    got = lg.assemble(quad=quad)
+    again = lg.assemble(quad=quad)
+    dofs = mesh.elem_dofs()
+    lam, rp, ci, ref, _, _ = orc.lagrange(order, quad, m.xyz, m.conn, dofs, b.ndof, test_order=2)
+    (brp, bci), _ = lg.pattern()
+    assert lg.n_multipliers == len(lam) and np.array_equal(brp, rp) and np.array_equal(bci, ci)
+    assert row_scaled_err(rp, ref, got.cpu().numpy()) <= 1e-12
+    assert torch.equal(got, again)
