@@ -120,9 +120,18 @@ mg_status mg_mesh_create_device(mg_mesh** out, int64_t n_nodes, const double* h_
                                 const int32_t* h_conn, int32_t order, int32_t edge_rule, void* stream);
 
 /* Loads a Gmsh 2.x ASCII mesh: node id = line order in $Nodes (the file's own
-   node label is ignored), tetrahedra = element type 4 in file order.
+   node label is ignored), tetrahedra = element type 4 in file order; the
+   triangles (type 2) are kept for mg_mesh_export_triangles.
    Replaces: loadMesh::gmMeshParallel, 3d (src/morganaFile/loadMesh.hpp:2065-2330). */
 mg_status mg_mesh_load_gmsh(mg_mesh** out, const char* path, int32_t order, int32_t edge_rule);
+/* The Gmsh file's triangles (element type 2), file order: h_tris (n x 3
+   0-based node ids, as written) and h_geo_ids (n: the 2nd tag, the geoId
+   loadMesh::gmMeshParallel gives the boundary elements,
+   src/morganaFile/loadMesh.hpp:2248-2290).  Selecting those of some geoIds and
+   passing them to mg_lagrange_build is the reference's test-field geoId
+   filter.  n_tris receives the count (0 for meshes not read from Gmsh); the
+   arrays may be NULL. */
+mg_status mg_mesh_export_triangles(const mg_mesh* mesh, int64_t* n_tris, int32_t* h_tris, int32_t* h_geo_ids);
 
 mg_status mg_mesh_destroy(mg_mesh* mesh);
 mg_status mg_mesh_get_info(const mg_mesh* mesh, mg_mesh_info* info);

@@ -86,6 +86,7 @@ SIGNATURES = {
     "mg_mesh_export_dofs": [_P, _P],
     "mg_mesh_export_edges": [_P, _P, _P],
     "mg_mesh_export_geometry": [_P, _P, _P],
+    "mg_mesh_export_triangles": [_P, ctypes.POINTER(_I64), _P, _P],
     "mg_pattern_build": [_P, ctypes.POINTER(_P)],
     "mg_pattern_build_device": [_P, ctypes.POINTER(_P), _P],
     "mg_plan_destroy": [_P],
@@ -231,6 +232,20 @@ class Mesh:
         conn = np.empty((self.n_elements, 4), dtype=np.int32)
         _check(lib().mg_mesh_export_geometry(self._h, _ptr(xyz), _ptr(conn)), "mg_mesh_export_geometry")
         return xyz, conn
+
+    def triangles(self, geo_ids=None):
+        """The Gmsh file's triangles (k, 3), file order, and their geoIds; with
+        geo_ids, only the triangles of those geoIds (the test field's filter)."""
+        n = _I64()
+        _check(lib().mg_mesh_export_triangles(self._h, ctypes.byref(n), None, None), "mg_mesh_export_triangles")
+        tris = np.empty((n.value, 3), dtype=np.int32)
+        geo = np.empty(n.value, dtype=np.int32)
+        _check(lib().mg_mesh_export_triangles(self._h, ctypes.byref(n), _ptr(tris), _ptr(geo)),
+               "mg_mesh_export_triangles")
+        if geo_ids is not None:
+            keep = np.isin(geo, np.asarray(list(geo_ids)))
+            tris, geo = tris[keep], geo[keep]
+        return tris, geo
 
     def close(self):
         if getattr(self, "_h", None):

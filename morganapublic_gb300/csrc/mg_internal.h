@@ -142,6 +142,8 @@ struct mg_mesh {
   std::vector<int32_t> elem_edge;   // n_elem * 6 (when built)
   std::vector<int32_t> edge_nodes;  // n_edges * 2 (when built)
   std::vector<int32_t> dofs;        // n_elem * nb
+  std::vector<int32_t> tri_nodes;   // Gmsh ingest: boundary triangles (3 node ids each), file order
+  std::vector<int32_t> tri_geo;     //   and their geoIds (2nd tag)
   // device copies
   double4_32a* d_xyz = nullptr;      // (x, y, z, 0)
   // x = hi + mid + lo exactly (three floats per coordinate), packed so that

@@ -421,7 +421,7 @@ mg_status mg_mesh_load_gmsh(mg_mesh** out, const char* path, int32_t order, int3
   if (!f) return set_error(MG_ERR_IO, std::string("cannot open ") + path);
   std::string line;
   std::vector<double> xyz;
-  std::vector<int32_t> conn;
+  std::vector<int32_t> conn, tris, tri_geo;
   int64_t n_nodes = -1;
   while (std::getline(f, line)) {
     if (line.find("$Nodes") != std::string::npos) {
@@ -445,6 +445,14 @@ mg_status mg_mesh_load_gmsh(mg_mesh** out, const char* path, int32_t order, int3
         int64_t t;
         while (is >> t) v.push_back(t);
         if (v.size() < 3) return set_error(MG_ERR_IO, "bad element line: " + line);
+        if (v[1] == 2) {  // boundary triangle: kept with its geoId (2nd tag) for the multipliers
+          const int64_t nt = v[2];
+          if ((nt != 2 && nt != 3) || (int64_t)v.size() != 3 + nt + 3)
+            return set_error(MG_ERR_IO, "triangle with unsupported tag count: " + line);
+          for (int k = 0; k < 3; ++k) tris.push_back((int32_t)(v[3 + nt + k] - 1));
+          tri_geo.push_back((int32_t)v[4]);
+          continue;
+        }
         if (v[1] != 4) continue;  // only tetrahedra feed the volume operators
         const int64_t ntags = v[2];
         if ((ntags != 2 && ntags != 3) || (int64_t)v.size() != 3 + ntags + 4)
@@ -454,8 +462,22 @@ mg_status mg_mesh_load_gmsh(mg_mesh** out, const char* path, int32_t order, int3
     }
   }
   if (n_nodes < 0) return set_error(MG_ERR_IO, "no $Nodes section");
-  return mg_mesh_create(out, n_nodes, xyz.data(), (int64_t)conn.size() / 4, conn.data(), order,
-                        edge_rule);
+  for (const int32_t t : tris)
+    if (t < 0 || t >= n_nodes) return set_error(MG_ERR_BAD_MESH, "triangle node id out of range");
+  MG_TRY(mg_mesh_create(out, n_nodes, xyz.data(), (int64_t)conn.size() / 4, conn.data(), order, edge_rule));
+  (*out)->tri_nodes.swap(tris);
+  (*out)->tri_geo.swap(tri_geo);
+  return MG_OK;
+}
+
+mg_status mg_mesh_export_triangles(const mg_mesh* m, int64_t* n_tris, int32_t* h_tris, int32_t* h_geo_ids)
+{
+  if (!m) return set_error(MG_ERR_INVALID_ARG, "mg_mesh_export_triangles: null mesh");
+  const int64_t n = (int64_t)m->tri_geo.size();
+  if (n_tris) *n_tris = n;
+  if (h_tris && n) std::memcpy(h_tris, m->tri_nodes.data(), sizeof(int32_t) * 3 * n);
+  if (h_geo_ids && n) std::memcpy(h_geo_ids, m->tri_geo.data(), sizeof(int32_t) * n);
+  return MG_OK;
 }
 
 mg_status mg_mesh_destroy(mg_mesh* mesh)

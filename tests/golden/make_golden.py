@@ -4,6 +4,10 @@ test data, read as text from a morganaPublic checkout (default
 
   mignon3dC.json         tests/morganaMeshes/mignon3dC.msh: 7 nodes, 8 tets
                          (file order, node ids as written, geoId = 2nd tag)
+                         and its boundary triangles with their geoIds
+  mignon3dB.json         tests/morganaMeshes/mignon3dB.msh, the same way (the
+                         mesh of localMatrixLA3dTest1, whose multipliers live
+                         on the triangles of geoId 2)
   connect3d_edges.json   tests/morganaGeometry/logs/connect3dTest2.log: the
                          rank-0 element's local edges in lid order with their
                          node pair as stored (first-appearance enumeration)
@@ -27,14 +31,14 @@ def read(rel):
         return f.read()
 
 
-def mesh_fixture():
-    lines = read("tests/morganaMeshes/mignon3dC.msh").splitlines()
+def mesh_fixture(name="mignon3dC"):
+    lines = read(f"tests/morganaMeshes/{name}.msh").splitlines()
     i = next(k for k, l in enumerate(lines) if l.strip() == "$Nodes")
     n = int(lines[i + 1])
     nodes = [[float(v) for v in lines[i + 2 + k].split()[1:4]] for k in range(n)]
     j = next(k for k, l in enumerate(lines) if l.strip() == "$Elements")
     m = int(lines[j + 1])
-    tets, geo, tris = [], [], []
+    tets, geo, tris, tgeo = [], [], [], []
     for k in range(m):
         v = [int(t) for t in lines[j + 2 + k].split()]
         ntags = v[2]
@@ -43,8 +47,9 @@ def mesh_fixture():
             geo.append(v[4])
         elif v[1] == 2:
             tris.append(v[3 + ntags:3 + ntags + 3])
-    return {"source": "tests/morganaMeshes/mignon3dC.msh", "nodes": nodes, "tets_1based": tets,
-            "geo_ids": geo, "triangles_1based": tris}
+            tgeo.append(v[4])
+    return {"source": f"tests/morganaMeshes/{name}.msh", "nodes": nodes, "tets_1based": tets,
+            "geo_ids": geo, "triangles_1based": tris, "triangle_geo_ids": tgeo}
 
 
 def edge_fixture():
@@ -66,8 +71,8 @@ def dof_counts():
 
 
 if __name__ == "__main__":
-    for name, data in (("mignon3dC.json", mesh_fixture()), ("connect3d_edges.json", edge_fixture()),
-                       ("dofmap_counts.json", dof_counts())):
+    for name, data in (("mignon3dC.json", mesh_fixture("mignon3dC")), ("mignon3dB.json", mesh_fixture("mignon3dB")),
+                       ("connect3d_edges.json", edge_fixture()), ("dofmap_counts.json", dof_counts())):
         with open(os.path.join(OUT, name), "w") as f:
             json.dump(data, f, indent=1)
         print("wrote", name)

@@ -310,3 +310,54 @@ def test_single_tet_all_faces_boundary():
         lam, fe, fl = lg.multipliers()
         assert np.array_equal(lam, [0, 1, 2, 3]) and np.array_equal(fe, [0] * 4) and np.array_equal(fl, range(4))
         assert lg.nnz_b == 4 * mesh.nb  # every multiplier couples to every dof of the tet
+
+
+def _write_gmsh(path, g):
+    """The fixture in the Gmsh 2 layout it was read from (3 tags: physical, geoId, partition)."""
+    nodes, tets, tris = g["nodes"], g["tets_1based"], g["triangles_1based"]
+    with open(path, "w") as f:
+        f.write("$MeshFormat\n2.1 0 8\n$EndMeshFormat\n$Nodes\n%d\n" % len(nodes))
+        for k, x in enumerate(nodes):
+            f.write("%d %r %r %r\n" % (k + 1, *x))
+        f.write("$EndNodes\n$Elements\n%d\n" % (len(tets) + len(tris)))
+        k = 1
+        for t, gid in zip(tris, g["triangle_geo_ids"]):
+            f.write("%d 2 3 0 %d 0 %d %d %d\n" % (k, gid, *t))
+            k += 1
+        for t, gid in zip(tets, g["geo_ids"]):
+            f.write("%d 4 3 0 %d 0 %d %d %d %d\n" % (k, gid, *t))
+            k += 1
+        f.write("$EndElements\n")
+
+
+@pytest.mark.parametrize("test_order", [0, 1, 2])
+def test_reference_mesh_mignon3dB_multipliers_on_geo_id_2(face_lib, tmp_path, test_order):
+    """The configuration of the reference's localMatrixLA3dTest1: mignon3dB.msh,
+    P1 field, multipliers on the triangles of geoId 2 (fePr2d<0> there),
+    triangle card of precision 2; here also P1 / P2 multipliers."""
+    import json
+    g = json.load(open(os.path.join(ROOT, "tests", "golden", "mignon3dB.json")))
+    p = str(tmp_path / "mignon3dB.msh")
+    _write_gmsh(p, g)
+    mesh = mg.Mesh.load_gmsh(p, order=1)
+    tris, geo = mesh.triangles()
+    assert np.array_equal(tris, np.array(g["triangles_1based"]) - 1)
+    assert np.array_equal(geo, g["triangle_geo_ids"])
+    sel, _ = mesh.triangles(geo_ids=[2])
+    assert len(sel) == 4
+    b = mg.MatrixBuilder(mesh)
+    lg = mg.LagrangeBuilder(b, tris=sel, test_order=test_order)
+    xyz, conn = mesh.geometry()
+    dofs = mesh.elem_dofs()
+    lam, rp, ci, ref, fe, fl = orc.lagrange(1, 3, xyz, conn, dofs, b.ndof, tris=sel, test_order=test_order)
+    glam, gfe, gfl = lg.multipliers()
+    (brp, bci), _ = lg.pattern()
+    assert np.array_equal(glam, lam) and np.array_equal(gfe, fe) and np.array_equal(brp, rp)
+    assert np.array_equal(bci, ci)
+    if test_order == 0:  # one multiplier per triangle, in file order
+        fn = np.sort(conn[fe[:, None], orc.FACE_PTS[fl]], axis=1)
+        assert np.array_equal(fn[glam], np.sort(sel, axis=1))
+    bptr, bsrc, _ = lg.export_maps()
+    fm = kernel_face_matrices(face_lib, 1, 3, xyz, conn, gfe, gfl, test_order).reshape(-1)
+    bv = np.array([np.sum(fm[bsrc[bptr[k]:bptr[k + 1]]]) for k in range(lg.nnz_b)])
+    assert row_scaled_err(rp, ref, bv) <= 1e-13

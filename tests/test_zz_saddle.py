@@ -245,3 +245,22 @@ def test_p2_multipliers_match_oracle(order, quad):
     assert lg.n_multipliers == len(lam) and np.array_equal(brp, rp) and np.array_equal(bci, ci)
     assert row_scaled_err(rp, ref, got.cpu().numpy()) <= 1e-12
     assert torch.equal(got, again)
+
+
+def test_reference_mesh_mignon3dB_geo_id_2(tmp_path):
+    """localMatrixLA3dTest1's configuration on the GPU: mignon3dB.msh, P1 field,
+    P0 multipliers on the triangles of geoId 2, triangle card of precision 2."""
+    import json
+    import os
+    from test_lagrange_host import _write_gmsh
+    g = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "mignon3dB.json")))
+    p = str(tmp_path / "mignon3dB.msh")
+    _write_gmsh(p, g)
+    mesh = mg.Mesh.load_gmsh(p, order=1)
+    sel, _ = mesh.triangles(geo_ids=[2])
+    b = mg.MatrixBuilder(mesh)
+    lg = mg.LagrangeBuilder(b, tris=sel, test_order=0)
+    got = lg.assemble(quad=3).cpu().numpy()
+    xyz, conn = mesh.geometry()
+    lam, rp, ci, ref, _, _ = orc.lagrange(1, 3, xyz, conn, mesh.elem_dofs(), b.ndof, tris=sel, test_order=0)
+    assert lg.n_multipliers == 4 and row_scaled_err(rp, ref, got) <= 1e-12
