@@ -121,118 +121,104 @@ uint64_t face_edge_key(const mg_mesh* m, int32_t e, int lf, int j)
   return (uint64_t)(uint32_t)std::min(p, q) << 32 | (uint32_t)std::max(p, q);
 }
 
-}  // namespace
-
-static mg_status build_lagrange(mg_lagrange* lg, int test_order, int64_t n_tris, const int32_t* h_tris,
-                                bool lam_diag, bool mtm)
+// Boundary faces, element then local-face order, kept as ids 4 e + local face;
+// with a triangle list, only those faces, and rank[f] = the list position of
+// face f (the boundary grid's element order, which numbers P0 multipliers),
+// else rank[f] = f.
+mg_status select_faces(const mg_mesh* m, int64_t n_tris, const int32_t* h_tris, std::vector<int32_t>* ids,
+                       std::vector<int64_t>* rank)
 {
-  const mg_plan* p = lg->plan;
-  const mg_mesh* m = p->mesh;
-  const int nb = m->nb;
-  const int64_t E = m->n_elem, N = m->n_nodes, nd = m->ndof;
-  lg->order = m->order;
-  lg->test_order = test_order;
-  lg->nt = test_order == 2 ? 6 : (test_order == 1 ? 3 : 1);
-  if (test_order == 2 && m->edge_rule != MG_EDGES_LEX)
-    return set_error(MG_ERR_UNSUPPORTED,
-                     "mg_lagrange_build: P2 multipliers follow the boundary edges' LEX numbering (MG_EDGES_LEX meshes)");
-  const int nt = lg->nt;
-  lg->lam_diag = lam_diag;
-  lg->mtm = mtm;
-  lg->nb = nb;
-  lg->ndof = nd;
-  if (4 * E > kInt32Max) return set_error(MG_ERR_SIZE, "mg_lagrange_build: more than 2^29 tets");
-
-  // boundary faces, element then local-face order
+  const int64_t E = m->n_elem, N = m->n_nodes;
   std::vector<uint8_t> flag;
   MG_TRY(boundary_flags(m, &flag));
-  std::vector<int32_t> ids;
+  ids->clear();
   for (int64_t k = 0; k < 4 * E; ++k)
-    if (flag[k]) ids.push_back((int32_t)k);
-
-  // selection by the given triangles; `rank` = each kept face's position in the
-  // list (the boundary grid's element order, which numbers P0 multipliers)
-  std::vector<int64_t> rank;
-  if (h_tris) {
-    std::vector<std::pair<Tri, int64_t>> want(n_tris);
-    for (int64_t t = 0; t < n_tris; ++t) {
-      const int32_t* v = h_tris + 3 * t;
-      for (int s = 0; s < 3; ++s)
-        if (v[s] < 0 || v[s] >= N) return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_build: triangle node id out of range");
-      want[t] = {sorted_tri(v[0], v[1], v[2]), t};
-    }
-    std::sort(want.begin(), want.end(), [](const auto& x, const auto& y) { return x.first < y.first; });
-    for (int64_t t = 1; t < n_tris; ++t)
-      if (want[t].first == want[t - 1].first)
-        return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_build: a triangle is listed twice");
-    std::vector<int32_t> kept;
-    for (const int32_t id : ids) {
-      const int32_t* c = m->conn.data() + 4 * (int64_t)(id / 4);
-      const int lf = id % 4;
-      const Tri t = sorted_tri(c[face_vertex(lf, 0)], c[face_vertex(lf, 1)], c[face_vertex(lf, 2)]);
-      auto it = std::lower_bound(want.begin(), want.end(), t,
-                                 [](const std::pair<Tri, int64_t>& x, const Tri& y) { return x.first < y; });
-      if (it != want.end() && it->first == t) {
-        kept.push_back(id);
-        rank.push_back(it->second);
-      }
-    }
-    if ((int64_t)kept.size() != n_tris)
-      return set_error(MG_ERR_BAD_MESH, "mg_lagrange_build: a listed triangle is not a boundary face of the mesh");
-    ids.swap(kept);
-  } else {
-    rank.resize(ids.size());
-    std::iota(rank.begin(), rank.end(), (int64_t)0);
+    if (flag[k]) ids->push_back((int32_t)k);
+  rank->clear();
+  if (!h_tris) {
+    rank->resize(ids->size());
+    std::iota(rank->begin(), rank->end(), (int64_t)0);
+    return MG_OK;
   }
-  const int64_t nf = (int64_t)ids.size();
-  if (nf * nt * nb > kInt32Max) return set_error(MG_ERR_SIZE, "mg_lagrange_build: too many boundary faces");
-  lg->n_faces = nf;
-  lg->face_elem.resize(nf);
-  lg->face_local.resize(nf);
-  for (int64_t f = 0; f < nf; ++f) {
-    lg->face_elem[f] = ids[f] / 4;
-    lg->face_local[f] = ids[f] % 4;
+  std::vector<std::pair<Tri, int64_t>> want(n_tris);
+  for (int64_t t = 0; t < n_tris; ++t) {
+    const int32_t* v = h_tris + 3 * t;
+    for (int s = 0; s < 3; ++s)
+      if (v[s] < 0 || v[s] >= N) return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_build: triangle node id out of range");
+    want[t] = {sorted_tri(v[0], v[1], v[2]), t};
   }
+  std::sort(want.begin(), want.end(), [](const auto& x, const auto& y) { return x.first < y.first; });
+  for (int64_t t = 1; t < n_tris; ++t)
+    if (want[t].first == want[t - 1].first)
+      return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_build: a triangle is listed twice");
+  std::vector<int32_t> kept;
+  for (const int32_t id : *ids) {
+    const int32_t* c = m->conn.data() + 4 * (int64_t)(id / 4);
+    const int lf = id % 4;
+    const Tri t = sorted_tri(c[face_vertex(lf, 0)], c[face_vertex(lf, 1)], c[face_vertex(lf, 2)]);
+    auto it = std::lower_bound(want.begin(), want.end(), t,
+                               [](const std::pair<Tri, int64_t>& x, const Tri& y) { return x.first < y; });
+    if (it != want.end() && it->first == t) {
+      kept.push_back(id);
+      rank->push_back(it->second);
+    }
+  }
+  if ((int64_t)kept.size() != n_tris)
+    return set_error(MG_ERR_BAD_MESH, "mg_lagrange_build: a listed triangle is not a boundary face of the mesh");
+  ids->swap(kept);
+  return MG_OK;
+}
 
-  // multipliers: P1 the nodes of the selected faces, ascending; P0 one per face,
-  // in the order of `rank`
-  std::vector<int32_t> lam_of;
-  std::vector<uint64_t> edge_keys;  // P2: boundary edges (min << 32 | max), ascending
+// Multipliers: P1 the nodes of the selected faces, ascending (lam_of[node] =
+// its multiplier); P2 those, then the faces' edges in (min, max) order
+// (edge_keys); P0 one per face, in the order of `rank`.
+void number_multipliers(mg_lagrange* lg, const mg_mesh* m, const std::vector<int64_t>& rank,
+                        std::vector<int32_t>* lam_of, std::vector<uint64_t>* edge_keys)
+{
+  const int64_t N = m->n_nodes, nf = lg->n_faces;
   lg->lam_node.clear();
   lg->lam_edge.clear();
-  if (test_order >= 1) {
-    lam_of.assign(N, -1);
-    for (int64_t f = 0; f < nf; ++f) {
-      const int32_t* c = m->conn.data() + 4 * (int64_t)lg->face_elem[f];
-      for (int a = 0; a < 3; ++a) lam_of[c[face_vertex(lg->face_local[f], a)]] = 0;
-    }
-    for (int64_t i = 0; i < N; ++i)
-      if (lam_of[i] == 0) {
-        lam_of[i] = (int32_t)lg->lam_node.size();
-        lg->lam_node.push_back((int32_t)i);
-      }
-    lg->n_vertex_lam = (int64_t)lg->lam_node.size();
-    if (test_order == 2) {  // then the edges of the selected faces, (min, max) order
-      edge_keys.reserve(3 * nf);
-      for (int64_t f = 0; f < nf; ++f)
-        for (int j = 0; j < 3; ++j) edge_keys.push_back(face_edge_key(m, lg->face_elem[f], lg->face_local[f], j));
-      std::sort(edge_keys.begin(), edge_keys.end());
-      edge_keys.erase(std::unique(edge_keys.begin(), edge_keys.end()), edge_keys.end());
-      for (const uint64_t k : edge_keys) {
-        lg->lam_node.push_back(-1);
-        lg->lam_edge.push_back((int32_t)(k >> 32));
-        lg->lam_edge.push_back((int32_t)(k & 0xffffffffu));
-      }
-    }
-  } else {
+  lam_of->clear();
+  edge_keys->clear();
+  if (lg->test_order == 0) {
     lg->lam_node.resize(nf);
     for (int64_t f = 0; f < nf; ++f) lg->lam_node[rank[f]] = (int32_t)f;
+    lg->nl = nf;
+    return;
   }
-  const int64_t nl = (int64_t)lg->lam_node.size();
-  lg->nl = nl;
+  lam_of->assign(N, -1);
+  for (int64_t f = 0; f < nf; ++f) {
+    const int32_t* c = m->conn.data() + 4 * (int64_t)lg->face_elem[f];
+    for (int a = 0; a < 3; ++a) (*lam_of)[c[face_vertex(lg->face_local[f], a)]] = 0;
+  }
+  for (int64_t i = 0; i < N; ++i)
+    if ((*lam_of)[i] == 0) {
+      (*lam_of)[i] = (int32_t)lg->lam_node.size();
+      lg->lam_node.push_back((int32_t)i);
+    }
+  lg->n_vertex_lam = (int64_t)lg->lam_node.size();
+  if (lg->test_order == 2) {
+    edge_keys->reserve(3 * nf);
+    for (int64_t f = 0; f < nf; ++f)
+      for (int j = 0; j < 3; ++j) edge_keys->push_back(face_edge_key(m, lg->face_elem[f], lg->face_local[f], j));
+    std::sort(edge_keys->begin(), edge_keys->end());
+    edge_keys->erase(std::unique(edge_keys->begin(), edge_keys->end()), edge_keys->end());
+    for (const uint64_t k : *edge_keys) {
+      lg->lam_node.push_back(-1);
+      lg->lam_edge.push_back((int32_t)(k >> 32));
+      lg->lam_edge.push_back((int32_t)(k & 0xffffffffu));
+    }
+  }
+  lg->nl = (int64_t)lg->lam_node.size();
+}
 
-  // B: (row, column) of every face-matrix entry, sorted by (row, column, source);
-  // sources are generated ascending, so each entry's list is in insertion order
+// B: (row, column) of every face-matrix entry, sorted by (row, column, source);
+// sources are generated ascending, so each entry's list is in insertion order.
+void build_b(mg_lagrange* lg, const mg_mesh* m, const std::vector<int64_t>& rank, const std::vector<int32_t>& lam_of,
+             const std::vector<uint64_t>& edge_keys)
+{
+  const int nb = lg->nb, nt = lg->nt;
+  const int64_t nf = lg->n_faces, nl = lg->nl;
   struct Pair {
     uint64_t key;  // row << 32 | column
     int32_t src;   // (f * nt + a) * nb + i
@@ -245,14 +231,14 @@ static mg_status build_lagrange(mg_lagrange* lg, int test_order, int64_t n_tris,
     const int32_t* c = m->conn.data() + 4 * e;
     for (int a = 0; a < nt; ++a) {
       uint64_t row;
-      if (test_order == 0) {
+      if (lg->test_order == 0) {
         row = (uint64_t)rank[f];
       } else if (a < 3) {
         row = (uint64_t)lam_of[c[face_vertex(lg->face_local[f], a)]];
       } else {  // P2 edge function of face edge a - 3
         const uint64_t key = face_edge_key(m, (int32_t)e, lg->face_local[f], a - 3);
-        row = (uint64_t)(lg->n_vertex_lam + (std::lower_bound(edge_keys.begin(), edge_keys.end(), key) -
-                                             edge_keys.begin()));
+        row = (uint64_t)(lg->n_vertex_lam +
+                         (std::lower_bound(edge_keys.begin(), edge_keys.end(), key) - edge_keys.begin()));
       }
       for (int i = 0; i < nb; ++i) {
         const int64_t s = (f * nt + a) * nb + i;
@@ -276,111 +262,113 @@ static mg_status build_lagrange(mg_lagrange* lg, int test_order, int64_t n_tris,
   lg->b_src_ptr.push_back((int32_t)pairs.size());
   for (int64_t l = 0; l < nl; ++l) lg->b_rowptr[l + 1] += lg->b_rowptr[l];
   lg->nnz_b = (int64_t)lg->b_colind.size();
+}
 
-  // B^T B (setMTM): every pair of entries (k1, k2) of a multiplier row l
-  // couples columns (i, j); entry (i, j) sums B[k1] B[k2] over its rows l in
-  // ascending order.  Structural pattern: zeros kept.
-  std::vector<int32_t> m_rowptr, m_colind;
-  if (mtm) {
-    struct Prod {
-      uint64_t key;  // i << 32 | j
-      int32_t l, k1, k2;
-      bool operator<(const Prod& o) const { return key != o.key ? key < o.key : l < o.l; }
-    };
-    std::vector<int64_t> off(nl + 1, 0);
-    for (int64_t l = 0; l < nl; ++l) {
-      const int64_t len = lg->b_rowptr[l + 1] - lg->b_rowptr[l];
-      off[l + 1] = off[l] + len * len;
-    }
-    std::vector<Prod> prods(off[nl]);
-#pragma omp parallel for schedule(dynamic, 64)
-    for (int64_t l = 0; l < nl; ++l) {
-      int64_t o = off[l];
-      for (int32_t k1 = lg->b_rowptr[l]; k1 < lg->b_rowptr[l + 1]; ++k1)
-        for (int32_t k2 = lg->b_rowptr[l]; k2 < lg->b_rowptr[l + 1]; ++k2)
-          prods[o++] = Prod{(uint64_t)(uint32_t)lg->b_colind[k1] << 32 | (uint32_t)lg->b_colind[k2], (int32_t)l,
-                            k1, k2};
-    }
-    __gnu_parallel::sort(prods.begin(), prods.end());
-    if ((int64_t)prods.size() > kInt32Max)
-      return set_error(MG_ERR_SIZE, "mg_lagrange_build: B^T B has more than 2^31 - 1 products");
-    m_rowptr.assign(nd + 1, 0);
-    lg->m_pair_ptr.clear();
-    lg->m_pairs.resize(prods.size());
-    for (size_t k = 0; k < prods.size(); ++k) {
-      if (k == 0 || prods[k].key != prods[k - 1].key) {
-        lg->m_pair_ptr.push_back((int32_t)k);
-        m_colind.push_back((int32_t)(prods[k].key & 0xffffffffu));
-        m_rowptr[(prods[k].key >> 32) + 1]++;
-      }
-      lg->m_pairs[k] = make_int2(prods[k].k1, prods[k].k2);
-    }
-    lg->m_pair_ptr.push_back((int32_t)prods.size());
-    for (int64_t r = 0; r < nd; ++r) m_rowptr[r + 1] += m_rowptr[r];
-    lg->nnz_m = (int64_t)m_colind.size();
+// B^T B (setMTM): every pair of entries (k1, k2) of a multiplier row l couples
+// columns (i, j); entry (i, j) sums B[k1] B[k2] over its rows l in ascending
+// order.  Structural pattern: zeros kept.  Returns its CSR (ndof rows).
+mg_status build_mtm(mg_lagrange* lg, std::vector<int32_t>* m_rowptr, std::vector<int32_t>* m_colind)
+{
+  const int64_t nl = lg->nl, nd = lg->ndof;
+  struct Prod {
+    uint64_t key;  // i << 32 | j
+    int32_t l, k1, k2;
+    bool operator<(const Prod& o) const { return key != o.key ? key < o.key : l < o.l; }
+  };
+  std::vector<int64_t> off(nl + 1, 0);
+  for (int64_t l = 0; l < nl; ++l) {
+    const int64_t len = lg->b_rowptr[l + 1] - lg->b_rowptr[l];
+    off[l + 1] = off[l] + len * len;
   }
+  if (off[nl] > kInt32Max) return set_error(MG_ERR_SIZE, "mg_lagrange_build: B^T B has more than 2^31 - 1 products");
+  std::vector<Prod> prods(off[nl]);
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int64_t l = 0; l < nl; ++l) {
+    int64_t o = off[l];
+    for (int32_t k1 = lg->b_rowptr[l]; k1 < lg->b_rowptr[l + 1]; ++k1)
+      for (int32_t k2 = lg->b_rowptr[l]; k2 < lg->b_rowptr[l + 1]; ++k2)
+        prods[o++] = Prod{(uint64_t)(uint32_t)lg->b_colind[k1] << 32 | (uint32_t)lg->b_colind[k2], (int32_t)l, k1, k2};
+  }
+  __gnu_parallel::sort(prods.begin(), prods.end());
+  m_rowptr->assign(nd + 1, 0);
+  m_colind->clear();
+  lg->m_pair_ptr.clear();
+  lg->m_pairs.resize(prods.size());
+  for (size_t k = 0; k < prods.size(); ++k) {
+    if (k == 0 || prods[k].key != prods[k - 1].key) {
+      lg->m_pair_ptr.push_back((int32_t)k);
+      m_colind->push_back((int32_t)(prods[k].key & 0xffffffffu));
+      (*m_rowptr)[(prods[k].key >> 32) + 1]++;
+    }
+    lg->m_pairs[k] = make_int2(prods[k].k1, prods[k].k2);
+  }
+  lg->m_pair_ptr.push_back((int32_t)prods.size());
+  for (int64_t r = 0; r < nd; ++r) (*m_rowptr)[r + 1] += (*m_rowptr)[r];
+  lg->nnz_m = (int64_t)m_colind->size();
+  return MG_OK;
+}
 
-  // saddle: rows r < nd hold the union of K's and B^T B's columns, then B^T's
-  // (columns nd + l, ascending l); rows nd + l hold B's row l (columns < nd),
-  // then the diagonal if requested
-  auto union_len = [&](int64_t r) {
-    int64_t n = 0;
+// Saddle: rows r < nd hold the union of K's and (setMTM) B^T B's columns, then
+// B^T's (columns nd + l, ascending l); rows nd + l hold B's row l (columns <
+// nd), then the diagonal if requested.  Fills s_rowptr / s_colind, the source
+// map s_src, each field row's diagonal entry s_diag and the B^T B slots m_slot.
+mg_status build_saddle(mg_lagrange* lg, const std::vector<int32_t>& m_rowptr, const std::vector<int32_t>& m_colind)
+{
+  const mg_plan* p = lg->plan;
+  const int64_t nd = lg->ndof, nl = lg->nl;
+  const bool mtm = lg->mtm;
+  // K row r and B^T B row r merged by column: calls f(column, K entry or -1, B^T B entry or -1)
+  auto merge = [&](int64_t r, auto&& f) {
     int32_t a = p->rowptr[r], b = mtm ? m_rowptr[r] : 0;
     const int32_t a1 = p->rowptr[r + 1], b1 = mtm ? m_rowptr[r + 1] : 0;
     while (a < a1 || b < b1) {
-      if (b >= b1 || (a < a1 && p->colind[a] < m_colind[b])) ++a;
-      else if (a >= a1 || m_colind[b] < p->colind[a]) ++b;
-      else ++a, ++b;
-      ++n;
+      if (b >= b1 || (a < a1 && p->colind[a] < m_colind[b])) {
+        f(p->colind[a], a, -1);
+        ++a;
+      } else if (a >= a1 || m_colind[b] < p->colind[a]) {
+        f(m_colind[b], -1, b);
+        ++b;
+      } else {
+        f(p->colind[a], a, b);
+        ++a, ++b;
+      }
     }
-    return n;
   };
-  std::vector<int64_t> ulen(nd);
-#pragma omp parallel for schedule(static)
-  for (int64_t r = 0; r < nd; ++r) ulen[r] = union_len(r);
   std::vector<int32_t> tcnt(nd + 1, 0);
   for (int64_t k = 0; k < lg->nnz_b; ++k) tcnt[lg->b_colind[k] + 1]++;
   for (int64_t r = 0; r < nd; ++r) tcnt[r + 1] += tcnt[r];
-  int64_t ns = 0;
   std::vector<int64_t> srp(nd + nl + 1, 0);
-  for (int64_t r = 0; r < nd; ++r) srp[r + 1] = srp[r] + ulen[r] + (tcnt[r + 1] - tcnt[r]);
+#pragma omp parallel for schedule(static)
+  for (int64_t r = 0; r < nd; ++r) {
+    int64_t n = 0;
+    merge(r, [&n](int32_t, int32_t, int32_t) { ++n; });
+    srp[r + 1] = n + (tcnt[r + 1] - tcnt[r]);
+  }
+  for (int64_t r = 0; r < nd; ++r) srp[r + 1] += srp[r];
   for (int64_t l = 0; l < nl; ++l)
-    srp[nd + l + 1] = srp[nd + l] + (lg->b_rowptr[l + 1] - lg->b_rowptr[l]) + (lam_diag ? 1 : 0);
-  ns = srp[nd + nl];
+    srp[nd + l + 1] = srp[nd + l] + (lg->b_rowptr[l + 1] - lg->b_rowptr[l]) + (lg->lam_diag ? 1 : 0);
+  const int64_t ns = srp[nd + nl];
   if (ns > kInt32Max || nd + nl > kInt32Max)
     return set_error(MG_ERR_SIZE, "mg_lagrange_build: the saddle matrix has more than 2^31 - 1 entries");
   lg->s_rowptr.assign(srp.begin(), srp.end());
   lg->nnz_s = ns;
   lg->s_colind.resize(ns);
   lg->s_src.resize(ns);
+  lg->s_diag.assign(nd, -1);
   lg->m_slot.assign(lg->nnz_m, 0);
   std::vector<int32_t> tfill(nd);
 #pragma omp parallel for schedule(static)
   for (int64_t r = 0; r < nd; ++r) {  // K and B^T B part
     int32_t s = lg->s_rowptr[r];
-    int32_t a = p->rowptr[r], b = mtm ? m_rowptr[r] : 0;
-    const int32_t a1 = p->rowptr[r + 1], b1 = mtm ? m_rowptr[r + 1] : 0;
-    for (; a < a1 || b < b1; ++s) {
-      if (b >= b1 || (a < a1 && p->colind[a] < m_colind[b])) {
-        lg->s_colind[s] = p->colind[a];
-        lg->s_src[s] = a++;
-      } else if (a >= a1 || m_colind[b] < p->colind[a]) {
-        lg->s_colind[s] = m_colind[b];
-        lg->s_src[s] = kSrcZero;
-        lg->m_slot[b++] = s;
-      } else {
-        lg->s_colind[s] = p->colind[a];
-        lg->s_src[s] = a++;
-        lg->m_slot[b++] = s;
-      }
-    }
+    merge(r, [&](int32_t col, int32_t ka, int32_t mb) {
+      lg->s_colind[s] = col;
+      lg->s_src[s] = ka >= 0 ? ka : kSrcZero;
+      if (mb >= 0) lg->m_slot[mb] = s;
+      if (col == (int32_t)r) lg->s_diag[r] = s;
+      ++s;
+    });
     tfill[r] = s;
   }
-  lg->s_diag.assign(nd, -1);  // the diagonal's saddle entry of each field row
-#pragma omp parallel for schedule(static)
-  for (int64_t r = 0; r < nd; ++r)
-    for (int32_t s = lg->s_rowptr[r]; s < tfill[r]; ++s)
-      if (lg->s_colind[s] == (int32_t)r) lg->s_diag[r] = s;
   for (int64_t l = 0; l < nl; ++l)  // B^T part: rows visited in ascending l
     for (int32_t k = lg->b_rowptr[l]; k < lg->b_rowptr[l + 1]; ++k) {
       const int32_t s = tfill[lg->b_colind[k]]++;
@@ -394,12 +382,52 @@ static mg_status build_lagrange(mg_lagrange* lg, int test_order, int64_t n_tris,
       lg->s_colind[s] = lg->b_colind[k];
       lg->s_src[s] = -(k + 1);
     }
-    if (lam_diag) {
+    if (lg->lam_diag) {
       lg->s_colind[s] = (int32_t)(nd + l);
       lg->s_src[s] = kSrcLamDiag;  // filled with eye_lam
     }
   }
   return MG_OK;
+}
+
+}  // namespace
+
+static mg_status build_lagrange(mg_lagrange* lg, int test_order, int64_t n_tris, const int32_t* h_tris,
+                                bool lam_diag, bool mtm)
+{
+  const mg_mesh* m = lg->plan->mesh;
+  lg->order = m->order;
+  lg->nb = m->nb;
+  lg->ndof = m->ndof;
+  lg->test_order = test_order;
+  lg->nt = test_order == 2 ? 6 : (test_order == 1 ? 3 : 1);
+  lg->lam_diag = lam_diag;
+  lg->mtm = mtm;
+  if (test_order == 2 && m->edge_rule != MG_EDGES_LEX)
+    return set_error(MG_ERR_UNSUPPORTED,
+                     "mg_lagrange_build: P2 multipliers follow the boundary edges' LEX numbering (MG_EDGES_LEX meshes)");
+  if (4 * m->n_elem > kInt32Max) return set_error(MG_ERR_SIZE, "mg_lagrange_build: more than 2^29 tets");
+
+  std::vector<int32_t> ids;
+  std::vector<int64_t> rank;
+  MG_TRY(select_faces(m, n_tris, h_tris, &ids, &rank));
+  const int64_t nf = (int64_t)ids.size();
+  if (nf * lg->nt * lg->nb > kInt32Max) return set_error(MG_ERR_SIZE, "mg_lagrange_build: too many boundary faces");
+  lg->n_faces = nf;
+  lg->face_elem.resize(nf);
+  lg->face_local.resize(nf);
+  for (int64_t f = 0; f < nf; ++f) {
+    lg->face_elem[f] = ids[f] / 4;
+    lg->face_local[f] = ids[f] % 4;
+  }
+
+  std::vector<int32_t> lam_of;
+  std::vector<uint64_t> edge_keys;
+  number_multipliers(lg, m, rank, &lam_of, &edge_keys);
+  build_b(lg, m, rank, lam_of, edge_keys);
+  std::vector<int32_t> m_rowptr, m_colind;
+  if (mtm) MG_TRY(build_mtm(lg, &m_rowptr, &m_colind));
+  return build_saddle(lg, m_rowptr, m_colind);
 }
 
 template <typename T>
