@@ -345,13 +345,22 @@ typedef struct {
   int64_t nnz_mtm;        /* entries of B^T B (MG_SADDLE_MTM), else 0 */
   int64_t n_mtm_products; /* products B_li B_lj they sum */
   int64_t n_edge_multipliers; /* P2: multipliers on boundary edges (the last ones), else 0 */
+  int64_t nnz_mmt;        /* entries of B B^T (MG_SADDLE_MMT), else 0 */
+  int64_t n_mmt_products; /* products they sum */
 } mg_lagrange_info;
 
 /* Saddle pattern options of mg_lagrange_build. */
 enum {
   MG_SADDLE_LAM_DIAG = 1, /* store the multiplier block's diagonal (setEye on that block) */
-  MG_SADDLE_MTM = 2       /* add B^T B to the field block (setMTM(B, field block)) */
+  MG_SADDLE_MTM = 2,      /* add B^T B to the field block (setMTM(B, field block)) */
+  MG_SADDLE_MMT = 4       /* add B B^T to the multiplier block (setMMT(B, multiplier block)) */
 };
+
+/* Scales of the saddle blocks (mg_saddle_assemble): setEye on the field and
+   multiplier blocks, setMTM and setMMT. */
+typedef struct {
+  double eye_field, eye_lam, mtm, mmt;
+} mg_saddle_scales;
 
 /* Multiplier space and patterns, on the host (no device needed).
    Boundary faces = faces of exactly one tet (connect3d::getFaceIsBoundary),
@@ -380,7 +389,9 @@ enum {
    flags: MG_SADDLE_LAM_DIAG adds the diagonal of the multiplier block to the
    pattern (setEye on that block); MG_SADDLE_MTM merges the structural pattern
    of B^T B into the field block (setMTM, whose product EpetraExt builds
-   structurally: every pair of entries of a multiplier row couples, zeros kept).
+   structurally: every pair of entries of a multiplier row couples, zeros
+   kept); MG_SADDLE_MMT merges B B^T into the multiplier block (setMMT: every
+   pair of entries of a field column couples).
    Errors: MG_ERR_BAD_MESH when a face belongs to more than two tets or a
    selected triangle is not a boundary face; MG_ERR_INVALID_ARG for a repeated
    triangle or a node id out of range; MG_ERR_SIZE above 2^31 - 1 entries.
@@ -410,11 +421,13 @@ mg_status mg_lagrange_pattern(const mg_lagrange* lg, int32_t* h_b_rowptr, int32_
    entry outside K's pattern).  Any pointer may be NULL. */
 mg_status mg_lagrange_export_maps(const mg_lagrange* lg, int32_t* h_b_src_ptr, int32_t* h_b_src,
                                   int32_t* h_s_src);
-/* With MG_SADDLE_MTM: B^T B entry m sums B[k1] B[k2] over the pairs
-   h_pairs[h_pair_ptr[m] .. h_pair_ptr[m+1]) (int32 pairs (k1, k2), ascending
-   multiplier row) and adds into saddle entry h_slot[m].  Sizes: nnz_mtm + 1,
-   2 n_mtm_products, nnz_mtm.  Any pointer may be NULL. */
-mg_status mg_lagrange_export_mtm(const mg_lagrange* lg, int32_t* h_pair_ptr, int32_t* h_pairs, int32_t* h_slot);
+/* The product blocks, which = MG_SADDLE_MTM (B^T B) or MG_SADDLE_MMT (B B^T):
+   entry m sums B[k1] B[k2] over the pairs h_pairs[h_pair_ptr[m] ..
+   h_pair_ptr[m+1]) (int32 pairs (k1, k2); ascending multiplier row for B^T B,
+   ascending field column for B B^T) and adds into saddle entry h_slot[m].
+   Sizes: nnz + 1, 2 x products, nnz.  Any pointer may be NULL. */
+mg_status mg_lagrange_export_products(const mg_lagrange* lg, int32_t which, int32_t* h_pair_ptr, int32_t* h_pairs,
+                                      int32_t* h_slot);
 
 /* Values of B (nnz_b doubles, device) with the face card quad (MG_FACE_QUAD_*):
    one thread per face computes its nt x nb block, then one thread per entry of
@@ -425,13 +438,14 @@ mg_status mg_lagrange_assemble(mg_lagrange* lg, int32_t quad, double* d_b_values
    what buildEpetraCrs hands to Epetra for localMatrixLA3d.  Synchronous. */
 mg_status mg_lagrange_assemble_host(mg_lagrange* lg, int32_t quad, double* h_b_values);
 /* Saddle values (nnz_saddle doubles, device) from K's values (the plan's CSR)
-   and B's: [K + eye_field I + mtm_scale B^T B, B^T; B, eye_lam I].  eye_lam
-   must be 0 unless the pattern has the multiplier diagonal
-   (MG_SADDLE_LAM_DIAG), mtm_scale 0 unless it has B^T B (MG_SADDLE_MTM; one
-   thread per entry of B^T B sums its products in ascending multiplier row and
-   adds them to its own saddle entry: deterministic, no atomics). */
+   and B's: [K + eye_field I + mtm B^T B, B^T; B, eye_lam I + mmt B B^T], the
+   scales from `scales` (NULL = all 0).  eye_lam must be 0 unless the pattern
+   has the multiplier diagonal (MG_SADDLE_LAM_DIAG), mtm / mmt 0 unless it has
+   the product (MG_SADDLE_MTM / MG_SADDLE_MMT).  One thread per product entry
+   sums its products in a fixed order and adds the sum to its own saddle entry:
+   deterministic, no atomics. */
 mg_status mg_saddle_assemble(mg_lagrange* lg, const double* d_k_values, const double* d_b_values,
-                             double eye_field, double eye_lam, double mtm_scale, double* d_values, void* stream);
+                             const mg_saddle_scales* scales, double* d_values, void* stream);
 /* y = S x on the saddle matrix (ndof + n_multipliers doubles each). */
 mg_status mg_saddle_spmv(mg_lagrange* lg, const double* d_values, const double* d_x, double* d_y,
                          void* stream);

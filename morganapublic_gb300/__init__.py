@@ -74,7 +74,13 @@ _I32, _I64, _D = ctypes.c_int32, ctypes.c_int64, ctypes.c_double
 # name -> argtypes; every function returns mg_status (int) unless listed in _RESTYPES
 class LagrangeInfo(ctypes.Structure):
     _fields_ = [("n_faces", _I64), ("n_multipliers", _I64), ("ndof", _I64), ("nnz_b", _I64),
-                ("nnz_saddle", _I64), ("nnz_mtm", _I64), ("n_mtm_products", _I64), ("n_edge_multipliers", _I64)]
+                ("nnz_saddle", _I64), ("nnz_mtm", _I64), ("n_mtm_products", _I64), ("n_edge_multipliers", _I64),
+                ("nnz_mmt", _I64), ("n_mmt_products", _I64)]
+
+
+class SaddleScales(ctypes.Structure):
+    _fields_ = [("eye_field", ctypes.c_double), ("eye_lam", ctypes.c_double), ("mtm", ctypes.c_double),
+                ("mmt", ctypes.c_double)]
 
 
 SIGNATURES = {
@@ -113,8 +119,8 @@ SIGNATURES = {
     "mg_lagrange_export_maps": [_P, _P, _P, _P],
     "mg_lagrange_assemble": [_P, _I32, _P, _P],
     "mg_lagrange_assemble_host": [_P, _I32, _P],
-    "mg_saddle_assemble": [_P, _P, _P, _D, _D, _D, _P, _P],
-    "mg_lagrange_export_mtm": [_P, _P, _P, _P],
+    "mg_saddle_assemble": [_P, _P, _P, ctypes.POINTER(SaddleScales), _P, _P],
+    "mg_lagrange_export_products": [_P, _I32, _P, _P, _P],
     "mg_lagrange_export_edges": [_P, _P],
     "mg_saddle_spmv": [_P, _P, _P, _P, _P],
     "mg_lagrange_apply": [_P, _P, _P, _P, _P],
@@ -432,17 +438,18 @@ class LagrangeBuilder:
     MatrixBuilder, whose plan must outlive it."""
 
     def __init__(self, builder: MatrixBuilder, tris=None, lam_diag: bool = False, test_order: int = 1,
-                 mtm: bool = False):
+                 mtm: bool = False, mmt: bool = False):
         """tris: (k, 3) node ids of the boundary triangles that carry multipliers
         (the test field's geoId filter); None = every boundary face.
         test_order: 1 = P1 multipliers (one per boundary node), 0 = P0 (one per
         triangle, in the order of tris), 2 = P2 (the P1 ones, then one per
         boundary edge in (min node, max node) order).  lam_diag: store the multiplier block's
-        diagonal; mtm: merge B^T B into the field block (setMTM)."""
+        diagonal; mtm: merge B^T B into the field block (setMTM); mmt: merge
+        B B^T into the multiplier block (setMMT)."""
         self.builder = builder
         self.test_order = test_order
         t = None if tris is None else np.ascontiguousarray(tris, dtype=np.int32).reshape(-1, 3)
-        flags = (1 if lam_diag else 0) | (2 if mtm else 0)
+        flags = (1 if lam_diag else 0) | (2 if mtm else 0) | (4 if mmt else 0)
         h = _P()
         _check(lib().mg_lagrange_build(builder._h, int(test_order), 0 if t is None else t.shape[0], _ptr(t),
                                        flags, ctypes.byref(h)), "mg_lagrange_build")
@@ -453,6 +460,7 @@ class LagrangeBuilder:
         self.ndof, self.nnz_b, self.nnz_saddle = info.ndof, info.nnz_b, info.nnz_saddle
         self.nnz_mtm, self.n_mtm_products = info.nnz_mtm, info.n_mtm_products
         self.n_edge_multipliers = info.n_edge_multipliers
+        self.nnz_mmt, self.n_mmt_products = info.nnz_mmt, info.n_mmt_products
 
     def multipliers(self):
         """(node (P1) or face index (P0) of each multiplier, face element, face local index)."""
@@ -513,17 +521,20 @@ class LagrangeBuilder:
         _check(lib().mg_lagrange_export_edges(self._h, _ptr(out)), "mg_lagrange_export_edges")
         return out
 
-    def export_mtm(self):
-        """(pair_ptr, pairs (n, 2), slot) of the B^T B block (built with mtm=True)."""
-        pp = np.empty(self.nnz_mtm + 1, dtype=np.int32)
-        pr = np.empty((self.n_mtm_products, 2), dtype=np.int32)
-        sl = np.empty(self.nnz_mtm, dtype=np.int32)
-        _check(lib().mg_lagrange_export_mtm(self._h, _ptr(pp), _ptr(pr), _ptr(sl)), "mg_lagrange_export_mtm")
+    def export_products(self, which: str = "mtm"):
+        """(pair_ptr, pairs (n, 2), slot) of the B^T B ("mtm") or B B^T ("mmt") block."""
+        nnz, n = (self.nnz_mtm, self.n_mtm_products) if which == "mtm" else (self.nnz_mmt, self.n_mmt_products)
+        pp = np.empty(nnz + 1, dtype=np.int32)
+        pr = np.empty((n, 2), dtype=np.int32)
+        sl = np.empty(nnz, dtype=np.int32)
+        _check(lib().mg_lagrange_export_products(self._h, 2 if which == "mtm" else 4, _ptr(pp), _ptr(pr), _ptr(sl)),
+               "mg_lagrange_export_products")
         return pp, pr, sl
 
     def saddle(self, k_values, b_values, eye_field: float = 0.0, eye_lam: float = 0.0, mtm_scale: float = 0.0,
-               out=None, stream=None):
-        """Values of [K + eye_field I + mtm_scale B^T B, B^T; B, eye_lam I] (torch float64, nnz_saddle)."""
+               mmt_scale: float = 0.0, out=None, stream=None):
+        """Values of [K + eye_field I + mtm_scale B^T B, B^T; B, eye_lam I + mmt_scale B B^T]
+        (torch float64, nnz_saddle)."""
         torch = _torch()
         self._need(k_values, self.builder.nnz, "K values")
         if self.nnz_b:
@@ -532,8 +543,9 @@ class LagrangeBuilder:
             self._need(out, self.nnz_saddle, "out")
         if out is None:
             out = torch.empty(self.nnz_saddle, dtype=torch.float64, device="cuda")
-        _check(lib().mg_saddle_assemble(self._h, _ptr(k_values), _ptr(b_values), float(eye_field), float(eye_lam),
-                                        float(mtm_scale), _ptr(out), _stream_ptr(stream)), "mg_saddle_assemble")
+        scales = SaddleScales(float(eye_field), float(eye_lam), float(mtm_scale), float(mmt_scale))
+        _check(lib().mg_saddle_assemble(self._h, _ptr(k_values), _ptr(b_values), ctypes.byref(scales), _ptr(out),
+                                        _stream_ptr(stream)), "mg_saddle_assemble")
         return out
 
     def saddle_apply(self, values, x, out=None, stream=None):

@@ -206,6 +206,7 @@ struct mg_plan {
 };
 
 // Saddle entry sources other than K and B entries (see mg_lagrange::s_src).
+// kSrcZero: a B^T B or B B^T entry outside the K / multiplier-diagonal pattern.
 constexpr int32_t kSrcLamDiag = INT32_MIN;
 constexpr int32_t kSrcZero = INT32_MIN + 1;
 
@@ -236,6 +237,12 @@ struct mg_lagrange {
   int64_t nnz_m = 0;
   std::vector<int32_t> m_pair_ptr, m_slot;
   std::vector<int2> m_pairs;
+  // B B^T (setMMT), the same way over the multiplier block: entry (l1, l2) sums
+  // B[k1] B[k2] over the columns the rows share, ascending column
+  bool mmt = false;
+  int64_t nnz_p = 0;
+  std::vector<int32_t> p_pair_ptr, p_slot;
+  std::vector<int2> p_pairs;
   // device copies (uploaded on first GPU use)
   int2* d_faces = nullptr;  // (element, local face)
   int32_t *d_b_rowptr = nullptr, *d_b_colind = nullptr, *d_b_src_ptr = nullptr, *d_b_src = nullptr;
@@ -244,6 +251,8 @@ struct mg_lagrange {
   int32_t* d_s_diag = nullptr;
   int32_t *d_m_pair_ptr = nullptr, *d_m_slot = nullptr;
   int2* d_m_pairs = nullptr;
+  int32_t *d_p_pair_ptr = nullptr, *d_p_slot = nullptr;
+  int2* d_p_pairs = nullptr;
   bool on_device = false;
 };
 

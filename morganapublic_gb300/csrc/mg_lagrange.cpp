@@ -308,11 +308,73 @@ mg_status build_mtm(mg_lagrange* lg, std::vector<int32_t>* m_rowptr, std::vector
   return MG_OK;
 }
 
+// B B^T (setMMT): every pair of entries (k1, k2) of a field column c couples
+// multiplier rows (l1, l2); entry (l1, l2) sums B[k1] B[k2] over its columns c
+// in ascending order.  Structural pattern: zeros kept.  Returns its CSR
+// (n_multipliers rows, columns = multiplier indices).
+mg_status build_mmt(mg_lagrange* lg, std::vector<int32_t>* p_rowptr, std::vector<int32_t>* p_colind)
+{
+  const int64_t nl = lg->nl, nd = lg->ndof, nzb = lg->nnz_b;
+  // B's entries by column, rows ascending within a column (a counting transpose)
+  std::vector<int64_t> cstart(nd + 1, 0);
+  for (int64_t k = 0; k < nzb; ++k) cstart[lg->b_colind[k] + 1]++;
+  for (int64_t c = 0; c < nd; ++c) cstart[c + 1] += cstart[c];
+  std::vector<int32_t> by_col(nzb), row_of(nzb);
+  {
+    std::vector<int64_t> fill(cstart.begin(), cstart.end() - 1);
+    for (int64_t l = 0; l < nl; ++l)
+      for (int32_t k = lg->b_rowptr[l]; k < lg->b_rowptr[l + 1]; ++k) {
+        by_col[fill[lg->b_colind[k]]++] = k;
+        row_of[k] = (int32_t)l;
+      }
+  }
+  struct Prod {
+    uint64_t key;  // l1 << 32 | l2
+    int32_t c, k1, k2;
+    bool operator<(const Prod& o) const { return key != o.key ? key < o.key : c < o.c; }
+  };
+  std::vector<int64_t> off(nd + 1, 0);
+  for (int64_t c = 0; c < nd; ++c) {
+    const int64_t len = cstart[c + 1] - cstart[c];
+    off[c + 1] = off[c] + len * len;
+  }
+  if (off[nd] > kInt32Max) return set_error(MG_ERR_SIZE, "mg_lagrange_build: B B^T has more than 2^31 - 1 products");
+  std::vector<Prod> prods(off[nd]);
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int64_t c = 0; c < nd; ++c) {
+    int64_t o = off[c];
+    for (int64_t a = cstart[c]; a < cstart[c + 1]; ++a)
+      for (int64_t b = cstart[c]; b < cstart[c + 1]; ++b) {
+        const int32_t k1 = by_col[a], k2 = by_col[b];
+        prods[o++] = Prod{(uint64_t)(uint32_t)row_of[k1] << 32 | (uint32_t)row_of[k2], (int32_t)c, k1, k2};
+      }
+  }
+  __gnu_parallel::sort(prods.begin(), prods.end());
+  p_rowptr->assign(nl + 1, 0);
+  p_colind->clear();
+  lg->p_pair_ptr.clear();
+  lg->p_pairs.resize(prods.size());
+  for (size_t k = 0; k < prods.size(); ++k) {
+    if (k == 0 || prods[k].key != prods[k - 1].key) {
+      lg->p_pair_ptr.push_back((int32_t)k);
+      p_colind->push_back((int32_t)(prods[k].key & 0xffffffffu));
+      (*p_rowptr)[(prods[k].key >> 32) + 1]++;
+    }
+    lg->p_pairs[k] = make_int2(prods[k].k1, prods[k].k2);
+  }
+  lg->p_pair_ptr.push_back((int32_t)prods.size());
+  for (int64_t l = 0; l < nl; ++l) (*p_rowptr)[l + 1] += (*p_rowptr)[l];
+  lg->nnz_p = (int64_t)p_colind->size();
+  return MG_OK;
+}
+
 // Saddle: rows r < nd hold the union of K's and (setMTM) B^T B's columns, then
 // B^T's (columns nd + l, ascending l); rows nd + l hold B's row l (columns <
-// nd), then the diagonal if requested.  Fills s_rowptr / s_colind, the source
-// map s_src, each field row's diagonal entry s_diag and the B^T B slots m_slot.
-mg_status build_saddle(mg_lagrange* lg, const std::vector<int32_t>& m_rowptr, const std::vector<int32_t>& m_colind)
+// nd), then the union of the diagonal (if requested) and (setMMT) B B^T's
+// columns (nd + l2).  Fills s_rowptr / s_colind, the source map s_src, each
+// field row's diagonal entry s_diag and the B^T B / B B^T slots m_slot, p_slot.
+mg_status build_saddle(mg_lagrange* lg, const std::vector<int32_t>& m_rowptr, const std::vector<int32_t>& m_colind,
+                       const std::vector<int32_t>& p_rowptr, const std::vector<int32_t>& p_colind)
 {
   const mg_plan* p = lg->plan;
   const int64_t nd = lg->ndof, nl = lg->nl;
@@ -334,6 +396,26 @@ mg_status build_saddle(mg_lagrange* lg, const std::vector<int32_t>& m_rowptr, co
       }
     }
   };
+  // multiplier row l's trailing part: the diagonal (lam_diag) merged with B B^T
+  // row l: calls g(multiplier column, is diagonal, B B^T entry or -1)
+  auto merge_lam = [&](int64_t l, auto&& g) {
+    int32_t b = lg->mmt ? p_rowptr[l] : 0;
+    const int32_t b1 = lg->mmt ? p_rowptr[l + 1] : 0;
+    bool diag = lg->lam_diag;
+    while (diag || b < b1) {
+      if (diag && (b >= b1 || (int64_t)p_colind[b] > l)) {
+        g((int32_t)l, true, -1);
+        diag = false;
+      } else if (diag && (int64_t)p_colind[b] == l) {
+        g((int32_t)l, true, b);
+        diag = false;
+        ++b;
+      } else {
+        g(p_colind[b], false, b);
+        ++b;
+      }
+    }
+  };
   std::vector<int32_t> tcnt(nd + 1, 0);
   for (int64_t k = 0; k < lg->nnz_b; ++k) tcnt[lg->b_colind[k] + 1]++;
   for (int64_t r = 0; r < nd; ++r) tcnt[r + 1] += tcnt[r];
@@ -345,8 +427,11 @@ mg_status build_saddle(mg_lagrange* lg, const std::vector<int32_t>& m_rowptr, co
     srp[r + 1] = n + (tcnt[r + 1] - tcnt[r]);
   }
   for (int64_t r = 0; r < nd; ++r) srp[r + 1] += srp[r];
-  for (int64_t l = 0; l < nl; ++l)
-    srp[nd + l + 1] = srp[nd + l] + (lg->b_rowptr[l + 1] - lg->b_rowptr[l]) + (lg->lam_diag ? 1 : 0);
+  for (int64_t l = 0; l < nl; ++l) {
+    int64_t n = 0;
+    merge_lam(l, [&n](int32_t, bool, int32_t) { ++n; });
+    srp[nd + l + 1] = srp[nd + l] + (lg->b_rowptr[l + 1] - lg->b_rowptr[l]) + n;
+  }
   const int64_t ns = srp[nd + nl];
   if (ns > kInt32Max || nd + nl > kInt32Max)
     return set_error(MG_ERR_SIZE, "mg_lagrange_build: the saddle matrix has more than 2^31 - 1 entries");
@@ -356,6 +441,7 @@ mg_status build_saddle(mg_lagrange* lg, const std::vector<int32_t>& m_rowptr, co
   lg->s_src.resize(ns);
   lg->s_diag.assign(nd, -1);
   lg->m_slot.assign(lg->nnz_m, 0);
+  lg->p_slot.assign(lg->nnz_p, 0);
   std::vector<int32_t> tfill(nd);
 #pragma omp parallel for schedule(static)
   for (int64_t r = 0; r < nd; ++r) {  // K and B^T B part
@@ -376,16 +462,18 @@ mg_status build_saddle(mg_lagrange* lg, const std::vector<int32_t>& m_rowptr, co
       lg->s_src[s] = -(k + 1);
     }
 #pragma omp parallel for schedule(static)
-  for (int64_t l = 0; l < nl; ++l) {  // B part (+ diagonal)
+  for (int64_t l = 0; l < nl; ++l) {  // B part, then the diagonal and B B^T
     int32_t s = lg->s_rowptr[nd + l];
     for (int32_t k = lg->b_rowptr[l]; k < lg->b_rowptr[l + 1]; ++k, ++s) {
       lg->s_colind[s] = lg->b_colind[k];
       lg->s_src[s] = -(k + 1);
     }
-    if (lg->lam_diag) {
-      lg->s_colind[s] = (int32_t)(nd + l);
-      lg->s_src[s] = kSrcLamDiag;  // filled with eye_lam
-    }
+    merge_lam(l, [&](int32_t col, bool diag, int32_t pb) {
+      lg->s_colind[s] = (int32_t)(nd + col);
+      lg->s_src[s] = diag ? kSrcLamDiag : kSrcZero;  // the diagonal starts at eye_lam
+      if (pb >= 0) lg->p_slot[pb] = s;
+      ++s;
+    });
   }
   return MG_OK;
 }
@@ -393,7 +481,7 @@ mg_status build_saddle(mg_lagrange* lg, const std::vector<int32_t>& m_rowptr, co
 }  // namespace
 
 static mg_status build_lagrange(mg_lagrange* lg, int test_order, int64_t n_tris, const int32_t* h_tris,
-                                bool lam_diag, bool mtm)
+                                bool lam_diag, bool mtm, bool mmt)
 {
   const mg_mesh* m = lg->plan->mesh;
   lg->order = m->order;
@@ -403,6 +491,7 @@ static mg_status build_lagrange(mg_lagrange* lg, int test_order, int64_t n_tris,
   lg->nt = test_order == 2 ? 6 : (test_order == 1 ? 3 : 1);
   lg->lam_diag = lam_diag;
   lg->mtm = mtm;
+  lg->mmt = mmt;
   if (test_order == 2 && m->edge_rule != MG_EDGES_LEX)
     return set_error(MG_ERR_UNSUPPORTED,
                      "mg_lagrange_build: P2 multipliers follow the boundary edges' LEX numbering (MG_EDGES_LEX meshes)");
@@ -425,9 +514,10 @@ static mg_status build_lagrange(mg_lagrange* lg, int test_order, int64_t n_tris,
   std::vector<uint64_t> edge_keys;
   number_multipliers(lg, m, rank, &lam_of, &edge_keys);
   build_b(lg, m, rank, lam_of, edge_keys);
-  std::vector<int32_t> m_rowptr, m_colind;
+  std::vector<int32_t> m_rowptr, m_colind, p_rowptr, p_colind;
   if (mtm) MG_TRY(build_mtm(lg, &m_rowptr, &m_colind));
-  return build_saddle(lg, m_rowptr, m_colind);
+  if (mmt) MG_TRY(build_mmt(lg, &p_rowptr, &p_colind));
+  return build_saddle(lg, m_rowptr, m_colind, p_rowptr, p_colind);
 }
 
 template <typename T>
@@ -456,6 +546,11 @@ static void free_device(mg_lagrange* lg)
   cudaFree(lg->d_m_slot);
   lg->d_m_pair_ptr = lg->d_m_slot = nullptr;
   lg->d_m_pairs = nullptr;
+  cudaFree(lg->d_p_pair_ptr);
+  cudaFree(lg->d_p_pairs);
+  cudaFree(lg->d_p_slot);
+  lg->d_p_pair_ptr = lg->d_p_slot = nullptr;
+  lg->d_p_pairs = nullptr;
   lg->d_faces = nullptr;
   lg->d_b_rowptr = lg->d_b_colind = lg->d_b_src_ptr = lg->d_b_src = nullptr;
   lg->d_s_rowptr = lg->d_s_colind = lg->d_s_src = nullptr;
@@ -481,6 +576,9 @@ mg_status lagrange_device(mg_lagrange* lg)
   if (s == MG_OK && lg->mtm) s = upload(&lg->d_m_pair_ptr, lg->m_pair_ptr);
   if (s == MG_OK && lg->mtm) s = upload(&lg->d_m_pairs, lg->m_pairs);
   if (s == MG_OK && lg->mtm) s = upload(&lg->d_m_slot, lg->m_slot);
+  if (s == MG_OK && lg->mmt) s = upload(&lg->d_p_pair_ptr, lg->p_pair_ptr);
+  if (s == MG_OK && lg->mmt) s = upload(&lg->d_p_pairs, lg->p_pairs);
+  if (s == MG_OK && lg->mmt) s = upload(&lg->d_p_slot, lg->p_slot);
   if (s == MG_OK) {
     const cudaError_t e =
         cudaMalloc(&lg->d_face_mat, sizeof(double) * std::max<int64_t>(lg->n_faces * lg->nt * lg->nb, 1));
@@ -507,7 +605,8 @@ mg_status mg_lagrange_build(mg_plan* plan, int32_t test_order, int64_t n_tris, c
   if (!plan || !out) return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_build: null argument");
   if (test_order < 0 || test_order > 2)
     return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_build: multipliers are P0 (0), P1 (1) or P2 (2)");
-  if (flags & ~(MG_SADDLE_LAM_DIAG | MG_SADDLE_MTM)) return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_build: bad flags");
+  if (flags & ~(MG_SADDLE_LAM_DIAG | MG_SADDLE_MTM | MG_SADDLE_MMT))
+    return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_build: bad flags");
   if (n_tris < 0 || (n_tris > 0 && !h_tris)) return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_build: bad triangle list");
   *out = nullptr;
   mg_lagrange* lg = new (std::nothrow) mg_lagrange();
@@ -515,7 +614,8 @@ mg_status mg_lagrange_build(mg_plan* plan, int32_t test_order, int64_t n_tris, c
   lg->plan = plan;
   mg_status s;
   try {
-    s = build_lagrange(lg, test_order, n_tris, h_tris, (flags & MG_SADDLE_LAM_DIAG) != 0, (flags & MG_SADDLE_MTM) != 0);
+    s = build_lagrange(lg, test_order, n_tris, h_tris, (flags & MG_SADDLE_LAM_DIAG) != 0,
+                       (flags & MG_SADDLE_MTM) != 0, (flags & MG_SADDLE_MMT) != 0);
   } catch (const std::bad_alloc&) {
     s = set_error(MG_ERR_ALLOC, "mg_lagrange_build: out of host memory");
   }
@@ -545,6 +645,8 @@ mg_status mg_lagrange_get_info(const mg_lagrange* lg, mg_lagrange_info* info)
   info->nnz_saddle = lg->nnz_s;
   info->nnz_mtm = lg->nnz_m;
   info->n_edge_multipliers = (int64_t)lg->lam_edge.size() / 2;
+  info->nnz_mmt = lg->nnz_p;
+  info->n_mmt_products = (int64_t)lg->p_pairs.size();
   info->n_mtm_products = (int64_t)lg->m_pairs.size();
   return MG_OK;
 }
@@ -586,13 +688,20 @@ mg_status mg_lagrange_export_edges(const mg_lagrange* lg, int32_t* h_edge_nodes)
   return MG_OK;
 }
 
-mg_status mg_lagrange_export_mtm(const mg_lagrange* lg, int32_t* h_pair_ptr, int32_t* h_pairs, int32_t* h_slot)
+mg_status mg_lagrange_export_products(const mg_lagrange* lg, int32_t which, int32_t* h_pair_ptr, int32_t* h_pairs,
+                                      int32_t* h_slot)
 {
-  if (!lg) return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_export_mtm: null handle");
-  if (!lg->mtm) return MG_OK;
-  if (h_pair_ptr) std::memcpy(h_pair_ptr, lg->m_pair_ptr.data(), sizeof(int32_t) * lg->m_pair_ptr.size());
-  if (h_pairs && !lg->m_pairs.empty()) std::memcpy(h_pairs, lg->m_pairs.data(), sizeof(int2) * lg->m_pairs.size());
-  if (h_slot && lg->nnz_m) std::memcpy(h_slot, lg->m_slot.data(), sizeof(int32_t) * lg->nnz_m);
+  if (!lg) return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_export_products: null handle");
+  if (which != MG_SADDLE_MTM && which != MG_SADDLE_MMT)
+    return set_error(MG_ERR_INVALID_ARG, "mg_lagrange_export_products: which is MG_SADDLE_MTM or MG_SADDLE_MMT");
+  const bool mt = which == MG_SADDLE_MTM;
+  if (!(mt ? lg->mtm : lg->mmt)) return MG_OK;
+  const std::vector<int32_t>& ptr = mt ? lg->m_pair_ptr : lg->p_pair_ptr;
+  const std::vector<int2>& pairs = mt ? lg->m_pairs : lg->p_pairs;
+  const std::vector<int32_t>& slot = mt ? lg->m_slot : lg->p_slot;
+  if (h_pair_ptr) std::memcpy(h_pair_ptr, ptr.data(), sizeof(int32_t) * ptr.size());
+  if (h_pairs && !pairs.empty()) std::memcpy(h_pairs, pairs.data(), sizeof(int2) * pairs.size());
+  if (h_slot && !slot.empty()) std::memcpy(h_slot, slot.data(), sizeof(int32_t) * slot.size());
   return MG_OK;
 }
 

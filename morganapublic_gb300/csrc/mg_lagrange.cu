@@ -10,8 +10,9 @@
 // No atomics, so every run gives the same bits.  The work is O(boundary faces)
 // (n^2 against the volume operator's n^3) and runs in native FP64.
 // The saddle values are a gather from K's and B's values through a per-entry
-// source map (plus, for setMTM, one thread per entry of B^T B summing its
-// products); the products use the CSR SpMV kernel of mg_solve.cu.
+// source map (plus, for setMTM / setMMT, one thread per entry of B^T B or
+// B B^T summing its products); the products with the matrices use the CSR SpMV
+// kernel of mg_solve.cu.
 #include <algorithm>
 #include <climits>
 
@@ -83,9 +84,10 @@ __global__ void __launch_bounds__(kFaceThreads) k_saddle_fill(int64_t n, const i
   }
 }
 
-// B^T B entry m: scale * sum of bv[k1] bv[k2] over its pairs (ascending
-// multiplier row), added to its saddle entry (one entry per m: no atomics)
-__global__ void __launch_bounds__(kFaceThreads) k_saddle_mtm(int64_t n, const int32_t* __restrict__ pair_ptr,
+// Product entry m (B^T B or B B^T): scale * sum of bv[k1] bv[k2] over its
+// pairs (in their fixed order), added to its saddle entry (one entry per m: no
+// atomics)
+__global__ void __launch_bounds__(kFaceThreads) k_saddle_products(int64_t n, const int32_t* __restrict__ pair_ptr,
                                                          const int2* __restrict__ pairs,
                                                          const int32_t* __restrict__ slot,
                                                          const double* __restrict__ bv, double scale,
@@ -173,15 +175,19 @@ mg_status mg_lagrange_assemble_host(mg_lagrange* lg, int32_t quad, double* h_b_v
   return s;
 }
 
-mg_status mg_saddle_assemble(mg_lagrange* lg, const double* d_k_values, const double* d_b_values, double eye_field,
-                             double eye_lam, double mtm_scale, double* d_values, void* stream)
+mg_status mg_saddle_assemble(mg_lagrange* lg, const double* d_k_values, const double* d_b_values,
+                             const mg_saddle_scales* scales, double* d_values, void* stream)
 {
   NvtxRange nvtx_range("mg_saddle_assemble");
   if (!lg) return set_error(MG_ERR_INVALID_ARG, "mg_saddle_assemble: null handle");
+  const mg_saddle_scales sc = scales ? *scales : mg_saddle_scales{0.0, 0.0, 0.0, 0.0};
+  const double eye_field = sc.eye_field, eye_lam = sc.eye_lam, mtm_scale = sc.mtm, mmt_scale = sc.mmt;
   if (eye_lam != 0.0 && !lg->lam_diag)
     return set_error(MG_ERR_INVALID_ARG, "mg_saddle_assemble: eye_lam needs a pattern built with MG_SADDLE_LAM_DIAG");
   if (mtm_scale != 0.0 && !lg->mtm)
-    return set_error(MG_ERR_INVALID_ARG, "mg_saddle_assemble: mtm_scale needs a pattern built with MG_SADDLE_MTM");
+    return set_error(MG_ERR_INVALID_ARG, "mg_saddle_assemble: mtm needs a pattern built with MG_SADDLE_MTM");
+  if (mmt_scale != 0.0 && !lg->mmt)
+    return set_error(MG_ERR_INVALID_ARG, "mg_saddle_assemble: mmt needs a pattern built with MG_SADDLE_MMT");
   if (lg->nnz_s == 0) return MG_OK;
   if (!d_values || (lg->plan->nnz && !d_k_values) || (lg->nnz_b && !d_b_values))
     return set_error(MG_ERR_INVALID_ARG, "mg_saddle_assemble: null argument");
@@ -195,8 +201,13 @@ mg_status mg_saddle_assemble(mg_lagrange* lg, const double* d_k_values, const do
     MG_CUDA(cudaGetLastError());
   }
   if (mtm_scale != 0.0 && lg->nnz_m > 0) {
-    k_saddle_mtm<<<grid_for(lg->nnz_m), kFaceThreads, 0, st>>>(lg->nnz_m, lg->d_m_pair_ptr, lg->d_m_pairs,
-                                                               lg->d_m_slot, d_b_values, mtm_scale, d_values);
+    k_saddle_products<<<grid_for(lg->nnz_m), kFaceThreads, 0, st>>>(lg->nnz_m, lg->d_m_pair_ptr, lg->d_m_pairs,
+                                                                    lg->d_m_slot, d_b_values, mtm_scale, d_values);
+    MG_CUDA(cudaGetLastError());
+  }
+  if (mmt_scale != 0.0 && lg->nnz_p > 0) {
+    k_saddle_products<<<grid_for(lg->nnz_p), kFaceThreads, 0, st>>>(lg->nnz_p, lg->d_p_pair_ptr, lg->d_p_pairs,
+                                                                    lg->d_p_slot, d_b_values, mmt_scale, d_values);
     MG_CUDA(cudaGetLastError());
   }
   return MG_OK;

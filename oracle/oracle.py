@@ -321,15 +321,47 @@ def mtm(b_rowptr, b_colind, b_vals, ndof):
     return np.cumsum(rowptr).astype(np.int32), (ukey % ndof).astype(np.int32), vals
 
 
+def mmt(b_rowptr, b_colind, b_vals, ndof):
+    """M M^T of a CSR M (here B, n_multipliers rows): the structural product
+    pattern (every pair of entries of a column couples, zeros kept; setMMT) with
+    values summed over the columns in ascending order."""
+    nl = b_rowptr.shape[0] - 1
+    brow = np.repeat(np.arange(nl), np.diff(b_rowptr))
+    order = np.lexsort((brow, b_colind))  # entries by column, then row
+    t_ptr = np.concatenate([[0], np.cumsum(np.bincount(b_colind, minlength=ndof))])
+    I, J, V = [], [], []
+    for c in range(ndof):
+        ks = order[t_ptr[c]:t_ptr[c + 1]]
+        if len(ks) == 0:
+            continue
+        r = brow[ks].astype(np.int64)
+        v = b_vals[ks]
+        I.append(np.repeat(r, len(r)))
+        J.append(np.tile(r, len(r)))
+        V.append(np.outer(v, v).reshape(-1))
+    if not I:
+        return np.zeros(nl + 1, np.int32), np.zeros(0, np.int32), np.zeros(0)
+    I, J, V = np.concatenate(I), np.concatenate(J), np.concatenate(V)
+    key = I * max(nl, 1) + J
+    ukey, pos = np.unique(key, return_inverse=True)
+    vals = np.zeros(len(ukey))
+    np.add.at(vals, pos.reshape(-1), V)  # sequential: ascending column
+    rowptr = np.zeros(nl + 1, dtype=np.int64)
+    np.add.at(rowptr, ukey // max(nl, 1) + 1, 1)
+    return np.cumsum(rowptr).astype(np.int32), (ukey % max(nl, 1)).astype(np.int32), vals
+
+
 def saddle(k_rowptr, k_colind, k_vals, b_rowptr, b_colind, b_vals, ndof, lam_diag=False, eye_field=0.0,
-           eye_lam=0.0, with_mtm=False, mtm_scale=0.0):
-    """[K + eye_field I + mtm_scale B^T B, B^T; B, eye_lam I] over (ndof +
-    n_multipliers) rows, the layout of epetraSaddleAssembler::setDiagMatrix(K,
-    field block) plus setSymmMatrix(B, multiplier block, field block), setMTM(B,
-    field block, scale) and setEye on the blocks (epetraSaddleAssembler.cpp).
-    The field rows hold the union of K's and (with_mtm) B^T B's columns; the
-    multiplier diagonal is stored only with lam_diag.  Returns (rowptr, colind,
-    values)."""
+           eye_lam=0.0, with_mtm=False, mtm_scale=0.0, with_mmt=False, mmt_scale=0.0):
+    """[K + eye_field I + mtm_scale B^T B, B^T; B, eye_lam I + mmt_scale B B^T]
+    over (ndof + n_multipliers) rows, the layout of
+    epetraSaddleAssembler::setDiagMatrix(K, field block) plus setSymmMatrix(B,
+    multiplier block, field block), setMTM(B, field block, scale), setMMT(B,
+    multiplier block, scale) and setEye on the blocks
+    (epetraSaddleAssembler.cpp).  The field rows hold the union of K's and
+    (with_mtm) B^T B's columns; the multiplier rows B's columns, then the union
+    of the diagonal (lam_diag) and (with_mmt) B B^T's columns.  Returns
+    (rowptr, colind, values)."""
     nl = b_rowptr.shape[0] - 1
     brow = np.repeat(np.arange(nl), np.diff(b_rowptr))
     order = np.lexsort((brow, b_colind))  # B^T rows: by field column, then multiplier
@@ -351,14 +383,20 @@ def saddle(k_rowptr, k_colind, k_vals, b_rowptr, b_colind, b_vals, ndof, lam_dia
         cols = sorted(acc)
         rows_c.append(np.concatenate([np.array(cols, dtype=np.int64), t_col[t_ptr[r]:t_ptr[r + 1]]]))
         rows_v.append(np.concatenate([np.array([acc[c] for c in cols]), t_val[t_ptr[r]:t_ptr[r + 1]]]))
+    if with_mmt:
+        p_rp, p_ci, p_v = mmt(b_rowptr, b_colind, b_vals, ndof)
     for l in range(nl):
         c = b_colind[b_rowptr[l]:b_rowptr[l + 1]].astype(np.int64)
         v = np.asarray(b_vals[b_rowptr[l]:b_rowptr[l + 1]], dtype=np.float64)
+        acc = {}
         if lam_diag:
-            c = np.append(c, ndof + l)
-            v = np.append(v, eye_lam)
-        rows_c.append(c)
-        rows_v.append(v)
+            acc[l] = eye_lam
+        if with_mmt:
+            for cc, vv in zip(p_ci[p_rp[l]:p_rp[l + 1]], p_v[p_rp[l]:p_rp[l + 1]]):
+                acc[int(cc)] = acc.get(int(cc), 0.0) + mmt_scale * vv
+        lc = sorted(acc)
+        rows_c.append(np.concatenate([c, ndof + np.array(lc, dtype=np.int64)]))
+        rows_v.append(np.concatenate([v, np.array([acc[x] for x in lc], dtype=np.float64)]))
     lens = [len(c) for c in rows_c]
     rowptr = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
     colind = np.concatenate(rows_c).astype(np.int32) if rows_c else np.zeros(0, np.int32)

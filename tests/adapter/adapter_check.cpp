@@ -99,7 +99,7 @@ static int run_lagrange(FILE* f, mg_plan* plan, int64_t ndof, int64_t nnz, int64
   mg_epetra::check(mg_assemble(plan, MG_OP_STIFF_KAPPA, dkappa, 1.0, MG_QUAD_4, MG_F64, dk, nullptr));
   mg_epetra::check(mg_plan_status(plan));
   mg_epetra::check(mg_lagrange_assemble(lg, MG_FACE_QUAD_1, db, nullptr));
-  mg_epetra::check(mg_saddle_assemble(lg, dk, db, 0.0, 0.0, 0.0, ds, nullptr));
+  mg_epetra::check(mg_saddle_assemble(lg, dk, db, nullptr, ds, nullptr));
   Epetra_Map map((int)n, 0, comm);
   Epetra_MultiVector X(map, 2), Y(map, 2);
   for (int64_t i = 0; i < n; ++i) {

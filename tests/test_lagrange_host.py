@@ -169,12 +169,13 @@ def _tris_on_plane(m, axis, value):
     return fn[on][:, ::-1].copy()  # any vertex order
 
 
-@pytest.mark.parametrize("mtm", [False, True])
+@pytest.mark.parametrize("products", ["", "mtm", "mmt", "mtm+mmt"])
 @pytest.mark.parametrize("test_order", [1, 0, 2])
 @pytest.mark.parametrize("order", [1, 2])
 @pytest.mark.parametrize("select", [None, "x0", "x0z1"])
 @pytest.mark.parametrize("lam_diag", [False, True])
-def test_patterns_match_oracle(order, select, lam_diag, test_order, mtm):
+def test_patterns_match_oracle(order, select, lam_diag, test_order, products):
+    mtm, mmt = "mtm" in products, "mmt" in products
     m, mesh, b = _mesh(4 if order == 1 else 3, order, seed=11)
     tris = None
     if select == "x0":
@@ -182,7 +183,7 @@ def test_patterns_match_oracle(order, select, lam_diag, test_order, mtm):
     elif select == "x0z1":  # in an order unrelated to the faces': P0 multipliers follow it
         tris = np.concatenate([_tris_on_plane(m, 2, 1.0), _tris_on_plane(m, 0, 0.0)])
         tris = tris[np.random.default_rng(3).permutation(len(tris))]
-    lg = mg.LagrangeBuilder(b, tris=tris, lam_diag=lam_diag, test_order=test_order, mtm=mtm)
+    lg = mg.LagrangeBuilder(b, tris=tris, lam_diag=lam_diag, test_order=test_order, mtm=mtm, mmt=mmt)
     lam, fe, fl = lg.multipliers()
     (brp, bci), (srp, sci) = lg.pattern()
     dofs = mesh.elem_dofs()
@@ -191,6 +192,9 @@ def test_patterns_match_oracle(order, select, lam_diag, test_order, mtm):
     if mtm:
         mrp, mci, _ = orc.mtm(obrp, obci, obv, b.ndof)
         assert lg.nnz_mtm == len(mci)
+    if mmt:
+        prp, pci, _ = orc.mmt(obrp, obci, obv, b.ndof)
+        assert lg.nnz_mmt == len(pci)
     assert np.array_equal(fe, ofe) and np.array_equal(fl, ofl)
     assert np.array_equal(lam, olam)
     if test_order == 2:  # edge multipliers: the selected faces' edges in (min, max) order
@@ -199,21 +203,23 @@ def test_patterns_match_oracle(order, select, lam_diag, test_order, mtm):
         assert np.array_equal(lg.edge_multipliers(), ends)
     assert np.array_equal(brp, obrp) and np.array_equal(bci, obci)
     rp, ci = b.pattern()
-    orp, oci, _ = orc.saddle(rp, ci, np.zeros(len(ci)), obrp, obci, obv, b.ndof, lam_diag=lam_diag, with_mtm=mtm)
+    orp, oci, _ = orc.saddle(rp, ci, np.zeros(len(ci)), obrp, obci, obv, b.ndof, lam_diag=lam_diag, with_mtm=mtm,
+                             with_mmt=mmt)
     assert np.array_equal(srp, orp) and np.array_equal(sci, oci)
     if select is not None:
         assert lg.n_faces == len(tris)
 
 
-@pytest.mark.parametrize("mtm", [False, True])
+@pytest.mark.parametrize("products", ["", "mtm", "mmt", "mtm+mmt"])
 @pytest.mark.parametrize("test_order", [1, 0, 2])
 @pytest.mark.parametrize("order", [1, 2])
 @pytest.mark.parametrize("quad", [1, 6])
-def test_kernel_data_flow_matches_oracle(face_lib, order, quad, test_order, mtm):
+def test_kernel_data_flow_matches_oracle(face_lib, order, quad, test_order, products):
     """The two kernels' data flow on the host: face matrices (the kernel's own
     arithmetic), the per-entry gather lists of B, the saddle source map."""
     m, mesh, b = _mesh(4 if order == 1 else 3, order, seed=13)
-    lg = mg.LagrangeBuilder(b, lam_diag=True, test_order=test_order, mtm=mtm)
+    mtm, mmt = "mtm" in products, "mmt" in products
+    lg = mg.LagrangeBuilder(b, lam_diag=True, test_order=test_order, mtm=mtm, mmt=mmt)
     lam, fe, fl = lg.multipliers()
     (brp, bci), (srp, sci) = lg.pattern()
     bptr, bsrc, ssrc = lg.export_maps()
@@ -238,15 +244,17 @@ def test_kernel_data_flow_matches_oracle(face_lib, order, quad, test_order, mtm)
         hit = np.nonzero(sci[srp[r]:srp[r + 1]] == r)[0]
         if len(hit):
             sv[srp[r] + hit[0]] += 0.5
-    # k_saddle_mtm
-    if mtm:
-        pp, pairs, slot = lg.export_mtm()
-        for mm in range(lg.nnz_mtm):
+    # k_saddle_products, B^T B then B B^T
+    for which, on, scale in (("mtm", mtm, 2.0), ("mmt", mmt, -1.5)):
+        if not on:
+            continue
+        pp, pairs, slot = lg.export_products(which)
+        for mm in range(len(slot)):
             pr = pairs[pp[mm]:pp[mm + 1]]
-            sv[slot[mm]] += 2.0 * np.sum(bv[pr[:, 0]] * bv[pr[:, 1]])
-        assert len(np.unique(slot)) == lg.nnz_mtm  # one saddle entry per B^T B entry
+            sv[slot[mm]] += scale * np.sum(bv[pr[:, 0]] * bv[pr[:, 1]])
+        assert len(np.unique(slot)) == len(slot)  # one saddle entry per product entry
     orp_s, oci_s, osv = orc.saddle(rp, ci, kv, brp, bci, bv, nd, lam_diag=True, eye_field=0.5, eye_lam=-0.25,
-                                   with_mtm=mtm, mtm_scale=2.0)
+                                   with_mtm=mtm, mtm_scale=2.0, with_mmt=mmt, mmt_scale=-1.5)
     assert np.array_equal(srp, orp_s) and np.array_equal(sci, oci_s)
     assert row_scaled_err(orp_s, osv, sv) <= 1e-14
 

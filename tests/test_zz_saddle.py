@@ -264,3 +264,20 @@ def test_reference_mesh_mignon3dB_geo_id_2(tmp_path):
     xyz, conn = mesh.geometry()
     lam, rp, ci, ref, _, _ = orc.lagrange(1, 3, xyz, conn, mesh.elem_dofs(), b.ndof, tris=sel, test_order=0)
     assert lg.n_multipliers == 4 and row_scaled_err(rp, ref, got) <= 1e-12
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_saddle_with_mtm_and_mmt_matches_oracle(order):
+    """setMTM and setMMT together: K + eI + a B^T B and eI + b B B^T."""
+    m, mesh, b, _, _ = _setup(4 if order == 1 else 3, order, 30)
+    lg = mg.LagrangeBuilder(b, lam_diag=True, mtm=True, mmt=True)
+    K = b.assemble("stiff_const", quad=4)
+    B = lg.assemble(quad=3)
+    S = lg.saddle(K, B, eye_field=0.5, eye_lam=-0.25, mtm_scale=3.0, mmt_scale=-2.0)
+    dofs, rp, ci, kref = orc.full_operator("stiff_const", order, 4, m.xyz, m.conn)
+    _, brp, bci, bref, _, _ = orc.lagrange(order, 3, m.xyz, m.conn, dofs, b.ndof)
+    srp, sci, sref = orc.saddle(rp, ci, kref, brp, bci, bref, b.ndof, lam_diag=True, eye_field=0.5, eye_lam=-0.25,
+                                with_mtm=True, mtm_scale=3.0, with_mmt=True, mmt_scale=-2.0)
+    (_, _), (gsrp, gsci) = lg.pattern()
+    assert np.array_equal(gsrp, srp) and np.array_equal(gsci, sci)
+    assert row_scaled_err(srp, sref, S.cpu().numpy()) <= 1e-12
