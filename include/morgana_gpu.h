@@ -325,7 +325,7 @@ mg_status mg_adjoint_grad(mg_plan* plan, const double* d_u, const double* d_lamb
 
 /* ------------------------------------------- boundary multipliers -- */
 
-/* Dirichlet data the reference way: P1 or P0 Lagrange multipliers on boundary
+/* Dirichlet data the reference way: P0, P1 or P2 Lagrange multipliers on boundary
    triangles, coupled to the field by opLA3dA (u . q over each boundary face),
    and the saddle system [K B^T; B 0].  FP64 throughout: the boundary work is
    O(n^2) against the O(n^3) of the volume operator. */
@@ -418,7 +418,7 @@ mg_status mg_lagrange_pattern(const mg_lagrange* lg, int32_t* h_b_rowptr, int32_
    (face * nt + test basis) * nb + field basis, in that order; h_s_src (nnz_saddle):
    saddle entry k copies K entry h_s_src[k] (>= 0), B entry -(h_s_src[k] + 1),
    the multiplier diagonal (INT32_MIN) or starts at zero (INT32_MIN + 1: a B^T B
-   entry outside K's pattern).  Any pointer may be NULL. */
+   or B B^T entry outside the K / diagonal pattern).  Any pointer may be NULL. */
 mg_status mg_lagrange_export_maps(const mg_lagrange* lg, int32_t* h_b_src_ptr, int32_t* h_b_src,
                                   int32_t* h_s_src);
 /* The product blocks, which = MG_SADDLE_MTM (B^T B) or MG_SADDLE_MMT (B B^T):
