@@ -369,3 +369,27 @@ def test_reference_mesh_mignon3dB_multipliers_on_geo_id_2(face_lib, tmp_path, te
     fm = kernel_face_matrices(face_lib, 1, 3, xyz, conn, gfe, gfl, test_order).reshape(-1)
     bv = np.array([np.sum(fm[bsrc[bptr[k]:bptr[k + 1]]]) for k in range(lg.nnz_b)])
     assert row_scaled_err(rp, ref, bv) <= 1e-13
+
+
+@pytest.mark.parametrize("test_order", [0, 1, 2])
+@pytest.mark.parametrize("order", [1, 2])
+def test_edge_meshes_with_every_option(order, test_order):
+    """No tets (every row of K empty) and a single tet beside an unreferenced
+    node: patterns against the oracle with the diagonal, B^T B and B B^T."""
+    xyz = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1], [5, 5, 5]], dtype=np.float64)
+    for conn in (np.zeros((0, 4), np.int32), np.array([[0, 1, 2, 3]], np.int32)):
+        mesh = mg.Mesh(xyz, conn, order=order)
+        b = mg.MatrixBuilder(mesh)
+        lg = mg.LagrangeBuilder(b, test_order=test_order, lam_diag=True, mtm=True, mmt=True)
+        (brp, bci), (srp, sci) = lg.pattern()
+        if len(conn) == 0:
+            assert lg.n_faces == 0 and lg.n_multipliers == 0 and lg.nnz_b == 0 and lg.nnz_saddle == 0
+            continue
+        dofs = mesh.elem_dofs()
+        lam, rp_o, ci_o, v_o, fe, fl = orc.lagrange(order, 1, xyz, conn, dofs, b.ndof, test_order=test_order)
+        assert np.array_equal(lg.multipliers()[0], lam) and 4 not in lam  # the unreferenced node carries none
+        assert np.array_equal(brp, rp_o) and np.array_equal(bci, ci_o)
+        rp, ci = b.pattern()
+        orp, oci, _ = orc.saddle(rp, ci, np.zeros(len(ci)), rp_o, ci_o, v_o, b.ndof, lam_diag=True, with_mtm=True,
+                                 with_mmt=True)
+        assert np.array_equal(srp, orp) and np.array_equal(sci, oci)
