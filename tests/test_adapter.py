@@ -1,6 +1,7 @@
 """The Epetra and Tpetra drop-in adapters (include/morgana_gpu_epetra.hpp,
 include/morgana_gpu_tpetra.hpp) compiled against test doubles of the Trilinos
-classes they touch (tests/adapter/mock_trilinos): on CPU that they compile; on
+classes they touch (tests/adapter/mock_trilinos): on CPU that they compile and
+that the multiplier builders hand every row of B over; on
 the GPU that the operator they hand to the Trilinos side (rows inserted into the
 Epetra_FECrsMatrix, the same rows into the Tpetra::CrsMatrix, Apply through the
 Epetra_Operator seam) is the oracle's."""
@@ -21,6 +22,29 @@ FLAGS = ["-std=c++17", "-O1", "-I" + os.path.join(ROOT, "include"),
 
 def test_adapter_compiles(tmp_path):
     subprocess.run(["g++", *FLAGS, "-Wall", "-Werror", "-c", SRC, "-o", str(tmp_path / "a.o")], check=True)
+
+
+@pytest.mark.parametrize("test_order", [0, 1, 2])
+@pytest.mark.parametrize("order", [1, 2])
+def test_lagrange_rows_reach_epetra_and_tpetra(tmp_path, order, test_order):
+    """buildEpetraLagrange / buildTpetraLagrange on the host: every row of B, with
+    the maps the reference's builder gives it (domain = field, range =
+    multipliers).  Values come from a host definition of
+    mg_lagrange_assemble_host in the check itself, so no device is needed."""
+    from morganapublic_gb300 import meshgen
+    lib = mgbuild.build()
+    src = os.path.join(ROOT, "tests", "adapter", "lagrange_rows_check.cpp")
+    exe = str(tmp_path / "lagrange_rows_check")
+    subprocess.run(["g++", *FLAGS, "-Wall", "-Werror", src, "-o", exe, lib,
+                    "-L" + os.path.join(mgbuild.CUDA_HOME, "lib64"), "-lcudart", "-Wl,-rpath," + os.path.dirname(lib),
+                    "-Wl,-rpath," + os.path.join(mgbuild.CUDA_HOME, "lib64")], check=True)
+    m = meshgen.kuhn_cube(3, jitter=0.2, seed=33, permute=True)
+    with open(tmp_path / "in.bin", "wb") as f:
+        np.array([len(m.xyz), len(m.conn), order], dtype=np.int64).tofile(f)
+        m.xyz.astype(np.float64).tofile(f)
+        m.conn.astype(np.int32).tofile(f)
+    r = subprocess.run([exe, str(tmp_path / "in.bin"), str(test_order)], timeout=120)
+    assert r.returncode == 0, r.returncode
 
 
 @pytest.mark.gpu
