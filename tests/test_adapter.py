@@ -1,7 +1,7 @@
 """The Epetra and Tpetra drop-in adapters (include/morgana_gpu_epetra.hpp,
 include/morgana_gpu_tpetra.hpp) compiled against test doubles of the Trilinos
 classes they touch (tests/adapter/mock_trilinos): on CPU that they compile and
-that the multiplier builders hand every row of B over; on
+that the builders hand every row of K and B over; on
 the GPU that the operator they hand to the Trilinos side (rows inserted into the
 Epetra_FECrsMatrix, the same rows into the Tpetra::CrsMatrix, Apply through the
 Epetra_Operator seam) is the oracle's."""
@@ -26,15 +26,16 @@ def test_adapter_compiles(tmp_path):
 
 @pytest.mark.parametrize("test_order", [0, 1, 2])
 @pytest.mark.parametrize("order", [1, 2])
-def test_lagrange_rows_reach_epetra_and_tpetra(tmp_path, order, test_order):
-    """buildEpetraLagrange / buildTpetraLagrange on the host: every row of B, with
-    the maps the reference's builder gives it (domain = field, range =
-    multipliers).  Values come from a host definition of
-    mg_lagrange_assemble_host in the check itself, so no device is needed."""
+def test_rows_reach_epetra_and_tpetra(tmp_path, order, test_order):
+    """buildEpetraCrs / buildTpetraCrs (K) and buildEpetraLagrange /
+    buildTpetraLagrange (B) on the host: every row, with the maps the
+    reference's builder gives B (domain = field, range = multipliers).  Values
+    come from host definitions of mg_assemble_host and mg_lagrange_assemble_host
+    in the check itself, so no device is needed."""
     from morganapublic_gb300 import meshgen
     lib = mgbuild.build()
-    src = os.path.join(ROOT, "tests", "adapter", "lagrange_rows_check.cpp")
-    exe = str(tmp_path / "lagrange_rows_check")
+    src = os.path.join(ROOT, "tests", "adapter", "rows_check.cpp")
+    exe = str(tmp_path / "rows_check")
     subprocess.run(["g++", *FLAGS, "-Wall", "-Werror", src, "-o", exe, lib,
                     "-L" + os.path.join(mgbuild.CUDA_HOME, "lib64"), "-lcudart", "-Wl,-rpath," + os.path.dirname(lib),
                     "-Wl,-rpath," + os.path.join(mgbuild.CUDA_HOME, "lib64")], check=True)
