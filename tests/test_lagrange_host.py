@@ -393,3 +393,20 @@ def test_edge_meshes_with_every_option(order, test_order):
         orp, oci, _ = orc.saddle(rp, ci, np.zeros(len(ci)), rp_o, ci_o, v_o, b.ndof, lam_diag=True, with_mtm=True,
                                  with_mmt=True)
         assert np.array_equal(srp, orp) and np.array_equal(sci, oci)
+
+
+def test_argument_errors_before_any_device_work():
+    """Bad options are refused with MG_ERR_INVALID_ARG (or MG_ERR_UNSUPPORTED)
+    before anything touches a device."""
+    m, mesh, b = _mesh(2, 1)
+    L = mg.lib()
+    h = ctypes.c_void_p()
+    for test_order, flags in ((3, 0), (-1, 0), (1, 8), (1, -1)):
+        assert L.mg_lagrange_build(b._h, test_order, 0, None, flags, ctypes.byref(h)) == mg.MG_ERR_INVALID_ARG
+    lg = mg.LagrangeBuilder(b)  # no diagonal, no products in the pattern
+    assert L.mg_lagrange_assemble(lg._h, 2, None, None) == mg.MG_ERR_INVALID_ARG  # no 2-point card
+    for scales in (mg.SaddleScales(0, 1.0, 0, 0), mg.SaddleScales(0, 0, 1.0, 0), mg.SaddleScales(0, 0, 0, 1.0)):
+        assert L.mg_saddle_assemble(lg._h, None, None, ctypes.byref(scales), None, None) == mg.MG_ERR_INVALID_ARG
+    assert L.mg_lagrange_export_products(lg._h, 1, None, None, None) == mg.MG_ERR_INVALID_ARG
+    assert L.mg_lagrange_build(None, 1, 0, None, 0, ctypes.byref(h)) == mg.MG_ERR_INVALID_ARG
+    assert L.mg_lagrange_build(b._h, 1, 3, None, 0, ctypes.byref(h)) == mg.MG_ERR_INVALID_ARG  # count without list
