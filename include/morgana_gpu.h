@@ -432,7 +432,9 @@ mg_status mg_lagrange_export_products(const mg_lagrange* lg, int32_t which, int3
 /* Values of B (nnz_b doubles, device) with the face card quad (MG_FACE_QUAD_*):
    one thread per face computes its nt x nb block, then one thread per entry of
    B sums its blocks' contributions in the reference's insertion order
-   (deterministic, no atomics). */
+   (deterministic, no atomics).  The first device call on a handle (this one,
+   mg_saddle_assemble, mg_saddle_spmv or mg_lagrange_apply) uploads its tables
+   and waits for the copies: make it before capturing a CUDA graph. */
 mg_status mg_lagrange_assemble(mg_lagrange* lg, int32_t quad, double* d_b_values, void* stream);
 /* mg_lagrange_assemble with the values copied to host memory (nnz_b doubles):
    what buildEpetraCrs hands to Epetra for localMatrixLA3d.  Synchronous. */
