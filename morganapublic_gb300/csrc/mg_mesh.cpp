@@ -318,10 +318,15 @@ static mg_status finish_mesh(mg_mesh* m)
           return set_error(MG_ERR_BAD_MESH, "element " + std::to_string(e) + " repeats a node");
     }
   }
+  // finite coordinates (a NaN would also slip through the minimum below)
+  for (int64_t i = 0; i < 3 * N; ++i)
+    if (!std::isfinite(m->xyz[i]))
+      return set_error(MG_ERR_BAD_MESH, "node " + std::to_string(i / 3) + " has a non-finite coordinate");
   // Jacobian check: the map is affine, so detJ is the same at every vertex.
   double mn = INFINITY;
   int64_t bad = -1;
-#pragma omp parallel for reduction(min : mn)
+  int any_bad = 0;
+#pragma omp parallel for reduction(min : mn) reduction(max : any_bad)
   for (int64_t e = 0; e < E; ++e) {
     const int32_t* c = &m->conn[4 * e];
     double J[3][3];
@@ -331,9 +336,10 @@ static mg_status finish_mesh(mg_mesh* m)
                J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
                J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
     if (d < mn) mn = d;
+    if (!(d > 0.0)) any_bad = 1;
   }
   m->min_det = E > 0 ? mn : 0.0;
-  if (E > 0 && !(mn > 0.0)) {
+  if (E > 0 && (any_bad || !(mn > 0.0))) {
     for (int64_t e = 0; e < E && bad < 0; ++e) {
       const int32_t* c = &m->conn[4 * e];
       double J[3][3];

@@ -152,6 +152,13 @@ def test_bad_meshes_are_rejected():
     with pytest.raises(mg.MorganaError) as e:
         mg.Mesh.load_gmsh("/nonexistent/file.msh")
     assert e.value.status == mg.MG_ERR_IO
+    for bad in (np.nan, np.inf, -np.inf):  # non-finite coordinates, referenced or not
+        for node in (3, 4):
+            x = np.vstack([xyz, [[2.0, 2.0, 2.0]]])
+            x[node, 2] = bad
+            with pytest.raises(mg.MorganaError) as e:
+                mg.Mesh(x, np.array([[0, 1, 2, 3]], dtype=np.int32))
+            assert e.value.status == mg.MG_ERR_BAD_MESH
 
 
 def test_empty_and_single_tet():
