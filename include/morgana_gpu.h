@@ -377,9 +377,12 @@ typedef struct {
      the boundary elements keep: src/morganaGeometry/meshInit3d.hpp:400-430),
      or the face order when h_tris is NULL;
    - test_order 2 (fePr2d<2>): the P1 ones, then one per edge of the selected
-     triangles in (min node, max node) order, the boundary grid's edge
-     numbering under pMapItem (src/morganaGeometry/connect2d.hpp:336-451);
-     MG_ERR_UNSUPPORTED on MG_EDGES_FIRST meshes.
+     triangles in the boundary grid's edge order
+     (src/morganaGeometry/connect2d.hpp:336-451): MG_EDGES_LEX meshes (min
+     node, max node) order; MG_EDGES_FIRST meshes the order of first
+     appearance over every boundary face (element then local-face order) and
+     its edges (0,1), (1,2), (2,0) in faceToPoint vertex order, the order in
+     which connect3d stores a face.
    B (n_multipliers x ndof): each face inserts its full nt x nb block (nt = 3
    for P1, 1 for P0, 6 for P2), explicit zeros included, as
    traitsMatrixBuilder::buildEpetraCrs does for localMatrixLA3d

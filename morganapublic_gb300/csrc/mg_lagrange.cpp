@@ -125,8 +125,9 @@ uint64_t face_edge_key(const mg_mesh* m, int32_t e, int lf, int j)
 // with a triangle list, only those faces, and rank[f] = the list position of
 // face f (the boundary grid's element order, which numbers P0 multipliers),
 // else rank[f] = f.
+// all_ids receives every boundary face (the boundary grid, whatever is selected).
 mg_status select_faces(const mg_mesh* m, int64_t n_tris, const int32_t* h_tris, std::vector<int32_t>* ids,
-                       std::vector<int64_t>* rank)
+                       std::vector<int64_t>* rank, std::vector<int32_t>* all_ids)
 {
   const int64_t E = m->n_elem, N = m->n_nodes;
   std::vector<uint8_t> flag;
@@ -134,6 +135,7 @@ mg_status select_faces(const mg_mesh* m, int64_t n_tris, const int32_t* h_tris, 
   ids->clear();
   for (int64_t k = 0; k < 4 * E; ++k)
     if (flag[k]) ids->push_back((int32_t)k);
+  *all_ids = *ids;
   rank->clear();
   if (!h_tris) {
     rank->resize(ids->size());
@@ -170,16 +172,22 @@ mg_status select_faces(const mg_mesh* m, int64_t n_tris, const int32_t* h_tris, 
 }
 
 // Multipliers: P1 the nodes of the selected faces, ascending (lam_of[node] =
-// its multiplier); P2 those, then the faces' edges in (min, max) order
-// (edge_keys); P0 one per face, in the order of `rank`.
+// its multiplier); P2 those, then the faces' edges in the boundary grid's edge
+// order -- MG_EDGES_LEX: (min, max) order; MG_EDGES_FIRST: first appearance over
+// every boundary face (all_ids, element then local-face order) and its local
+// edges (0,1), (1,2), (2,0) in face-vertex order, as connect2d numbers the edges
+// of the boundary grid whose triangles connect3d stores in faceToPoint order.
+// edge_index = (key, multiplier offset among the edges), sorted by key.  P0: one
+// per face, in the order of `rank`.
 void number_multipliers(mg_lagrange* lg, const mg_mesh* m, const std::vector<int64_t>& rank,
-                        std::vector<int32_t>* lam_of, std::vector<uint64_t>* edge_keys)
+                        const std::vector<int32_t>& all_ids, std::vector<int32_t>* lam_of,
+                        std::vector<std::pair<uint64_t, int64_t>>* edge_index)
 {
   const int64_t N = m->n_nodes, nf = lg->n_faces;
   lg->lam_node.clear();
   lg->lam_edge.clear();
   lam_of->clear();
-  edge_keys->clear();
+  edge_index->clear();
   if (lg->test_order == 0) {
     lg->lam_node.resize(nf);
     for (int64_t f = 0; f < nf; ++f) lg->lam_node[rank[f]] = (int32_t)f;
@@ -198,16 +206,32 @@ void number_multipliers(mg_lagrange* lg, const mg_mesh* m, const std::vector<int
     }
   lg->n_vertex_lam = (int64_t)lg->lam_node.size();
   if (lg->test_order == 2) {
-    edge_keys->reserve(3 * nf);
+    std::vector<uint64_t> keys;  // the selected faces' edges
+    keys.reserve(3 * nf);
     for (int64_t f = 0; f < nf; ++f)
-      for (int j = 0; j < 3; ++j) edge_keys->push_back(face_edge_key(m, lg->face_elem[f], lg->face_local[f], j));
-    std::sort(edge_keys->begin(), edge_keys->end());
-    edge_keys->erase(std::unique(edge_keys->begin(), edge_keys->end()), edge_keys->end());
-    for (const uint64_t k : *edge_keys) {
-      lg->lam_node.push_back(-1);
-      lg->lam_edge.push_back((int32_t)(k >> 32));
-      lg->lam_edge.push_back((int32_t)(k & 0xffffffffu));
+      for (int j = 0; j < 3; ++j) keys.push_back(face_edge_key(m, lg->face_elem[f], lg->face_local[f], j));
+    std::sort(keys.begin(), keys.end());
+    keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+    if (m->edge_rule == MG_EDGES_FIRST) {
+      // rank of first appearance over the whole boundary grid
+      std::vector<std::pair<uint64_t, int64_t>> first;  // (key, first position)
+      first.reserve(3 * all_ids.size());
+      for (size_t q = 0; q < all_ids.size(); ++q)
+        for (int j = 0; j < 3; ++j)
+          first.push_back({face_edge_key(m, all_ids[q] / 4, all_ids[q] % 4, j), (int64_t)(3 * q + j)});
+      std::sort(first.begin(), first.end());  // by key, then position: the first of each key leads
+      auto pos_of = [&first](uint64_t k) {
+        return std::lower_bound(first.begin(), first.end(), std::make_pair(k, (int64_t)-1))->second;
+      };
+      std::sort(keys.begin(), keys.end(), [&](uint64_t x, uint64_t y) { return pos_of(x) < pos_of(y); });
     }
+    for (size_t i = 0; i < keys.size(); ++i) {
+      lg->lam_node.push_back(-1);
+      lg->lam_edge.push_back((int32_t)(keys[i] >> 32));
+      lg->lam_edge.push_back((int32_t)(keys[i] & 0xffffffffu));
+      edge_index->push_back({keys[i], (int64_t)i});
+    }
+    std::sort(edge_index->begin(), edge_index->end());
   }
   lg->nl = (int64_t)lg->lam_node.size();
 }
@@ -215,7 +239,7 @@ void number_multipliers(mg_lagrange* lg, const mg_mesh* m, const std::vector<int
 // B: (row, column) of every face-matrix entry, sorted by (row, column, source);
 // sources are generated ascending, so each entry's list is in insertion order.
 void build_b(mg_lagrange* lg, const mg_mesh* m, const std::vector<int64_t>& rank, const std::vector<int32_t>& lam_of,
-             const std::vector<uint64_t>& edge_keys)
+             const std::vector<std::pair<uint64_t, int64_t>>& edge_index)
 {
   const int nb = lg->nb, nt = lg->nt;
   const int64_t nf = lg->n_faces, nl = lg->nl;
@@ -238,7 +262,8 @@ void build_b(mg_lagrange* lg, const mg_mesh* m, const std::vector<int64_t>& rank
       } else {  // P2 edge function of face edge a - 3
         const uint64_t key = face_edge_key(m, (int32_t)e, lg->face_local[f], a - 3);
         row = (uint64_t)(lg->n_vertex_lam +
-                         (std::lower_bound(edge_keys.begin(), edge_keys.end(), key) - edge_keys.begin()));
+                         std::lower_bound(edge_index.begin(), edge_index.end(), std::make_pair(key, (int64_t)-1))
+                             ->second);
       }
       for (int i = 0; i < nb; ++i) {
         const int64_t s = (f * nt + a) * nb + i;
@@ -492,14 +517,11 @@ static mg_status build_lagrange(mg_lagrange* lg, int test_order, int64_t n_tris,
   lg->lam_diag = lam_diag;
   lg->mtm = mtm;
   lg->mmt = mmt;
-  if (test_order == 2 && m->edge_rule != MG_EDGES_LEX)
-    return set_error(MG_ERR_UNSUPPORTED,
-                     "mg_lagrange_build: P2 multipliers follow the boundary edges' LEX numbering (MG_EDGES_LEX meshes)");
   if (4 * m->n_elem > kInt32Max) return set_error(MG_ERR_SIZE, "mg_lagrange_build: more than 2^29 tets");
 
-  std::vector<int32_t> ids;
+  std::vector<int32_t> ids, all_ids;
   std::vector<int64_t> rank;
-  MG_TRY(select_faces(m, n_tris, h_tris, &ids, &rank));
+  MG_TRY(select_faces(m, n_tris, h_tris, &ids, &rank, &all_ids));
   const int64_t nf = (int64_t)ids.size();
   if (nf * lg->nt * lg->nb > kInt32Max) return set_error(MG_ERR_SIZE, "mg_lagrange_build: too many boundary faces");
   lg->n_faces = nf;
@@ -511,9 +533,9 @@ static mg_status build_lagrange(mg_lagrange* lg, int test_order, int64_t n_tris,
   }
 
   std::vector<int32_t> lam_of;
-  std::vector<uint64_t> edge_keys;
-  number_multipliers(lg, m, rank, &lam_of, &edge_keys);
-  build_b(lg, m, rank, lam_of, edge_keys);
+  std::vector<std::pair<uint64_t, int64_t>> edge_index;
+  number_multipliers(lg, m, rank, all_ids, &lam_of, &edge_index);
+  build_b(lg, m, rank, lam_of, edge_index);
   std::vector<int32_t> m_rowptr, m_colind, p_rowptr, p_colind;
   if (mtm) MG_TRY(build_mtm(lg, &m_rowptr, &m_colind));
   if (mmt) MG_TRY(build_mmt(lg, &p_rowptr, &p_colind));

@@ -231,7 +231,7 @@ def boundary_faces(conn, tris=None):
     return (idx // 4).astype(np.int32), (idx % 4).astype(np.int32)
 
 
-def lagrange(order, quad, xyz, conn, dofs, ndof, tris=None, faces=None, test_order=1):
+def lagrange(order, quad, xyz, conn, dofs, ndof, tris=None, faces=None, test_order=1, edge_rule="lex"):
     """B of opLA3dA with P1 (test_order 1), P0 (0) or P2 (2) multipliers on the
     boundary triangles.
 
@@ -242,9 +242,13 @@ def lagrange(order, quad, xyz, conn, dofs, ndof, tris=None, faces=None, test_ord
     the boundary grid's element order -- the order of `tris` when given (the
     Gmsh triangles' order, whose ids the boundary elements keep,
     meshInit3d.hpp:400-430), else the face order.  P2 multipliers: the P1 ones,
-    then one per edge of the selected faces in (min node, max node) order (the
-    boundary grid's edges numbered under pMapItem, connect2d.hpp:336-451, kept
-    in that order by dofMapStatic2d.hpp:1166-1380).  Rows = multipliers, columns =
+    then one per edge of the selected faces in the boundary grid's edge order
+    (connect2d.hpp:336-451, kept by dofMapStatic2d.hpp:1166-1380): under
+    pMapItem ("lex") (min node, max node) order; under pMapItemShare on one rank
+    ("first") the order of first appearance over every boundary triangle, in the
+    grid's element order (the faces' own, element then local face) and local
+    edges (1,2), (2,3), (3,1) of the triangle's nodes, stored as connect3d.hpp
+    stores the face (faceToPoint order, connect3dTest2.log).  Rows = multipliers, columns =
     field dofs; every face contributes its full local block, zeros included
     (traitsMatrixBuilder.hpp:363-441 inserts the whole block), summed in
     element, local-face, test-basis, field-basis order.  `faces` = (face_elem,
@@ -271,7 +275,17 @@ def lagrange(order, quad, xyz, conn, dofs, ndof, tris=None, faces=None, test_ord
             ends = np.sort(fnodes[:, TRI_EDGES], axis=2).astype(np.int64)  # nf x 3 x 2
             ekey = ends[:, :, 0] * xyz.shape[0] + ends[:, :, 1]
             uedge = np.unique(ekey)
-            face_rows = np.concatenate([face_rows, len(lam_node) + np.searchsorted(uedge, ekey)], axis=1)
+            if edge_rule == "first":  # first appearance over every boundary triangle
+                ae, al = boundary_faces(conn)
+                an = conn[ae[:, None], FACE_PTS[al]]
+                aends = np.sort(an[:, TRI_EDGES], axis=2).astype(np.int64)
+                akey = (aends[:, :, 0] * xyz.shape[0] + aends[:, :, 1]).reshape(-1)
+                _, first = np.unique(akey, return_index=True)
+                rank_of = dict(zip(akey[np.sort(first)].tolist(), range(len(first))))
+                uedge = np.array(sorted(uedge.tolist(), key=lambda k: rank_of[k]), dtype=np.int64)
+            pos = {k: i for i, k in enumerate(uedge.tolist())}
+            erow = np.array([pos[k] for k in ekey.reshape(-1).tolist()], dtype=np.int64).reshape(ekey.shape)
+            face_rows = np.concatenate([face_rows, len(lam_node) + erow], axis=1)
             lam_node = np.concatenate([lam_node, np.full(len(uedge), -1, dtype=np.int32)])
     else:
         if tris is None:

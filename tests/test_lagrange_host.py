@@ -290,13 +290,42 @@ def test_selected_triangles_errors():
     assert empty.nnz_saddle == len(ci)
 
 
-def test_p2_multipliers_need_lex_edges():
-    m = meshgen.kuhn_cube(2, jitter=0.2, seed=3, permute=True)
-    b = mg.MatrixBuilder(mg.Mesh(m.xyz, m.conn, order=2, edge_rule="first"))
-    with pytest.raises(mg.MorganaError) as e:
-        mg.LagrangeBuilder(b, test_order=2)
-    assert e.value.status == mg.MG_ERR_UNSUPPORTED
-    assert mg.LagrangeBuilder(b, test_order=1).n_multipliers > 0
+@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("select", [None, "x0z1"])
+def test_p2_multipliers_on_first_numbered_meshes(face_lib, order, select):
+    """Under the FIRST rule the edge multipliers follow first appearance over the
+    whole boundary grid, also when only some triangles carry multipliers."""
+    m = meshgen.kuhn_cube(3, jitter=0.2, seed=17, permute=True)
+    mesh = mg.Mesh(m.xyz, m.conn, order=order, edge_rule="first")
+    b = mg.MatrixBuilder(mesh)
+    tris = None
+    if select:
+        tris = np.concatenate([_tris_on_plane(m, 2, 1.0), _tris_on_plane(m, 0, 0.0)])
+    lg = mg.LagrangeBuilder(b, tris=tris, test_order=2)
+    dofs = mesh.elem_dofs()
+    lam, rp, ci, v, fe, fl = orc.lagrange(order, 6, m.xyz, m.conn, dofs, b.ndof, tris=tris, test_order=2,
+                                          edge_rule="first")
+    lex = orc.lagrange(order, 6, m.xyz, m.conn, dofs, b.ndof, tris=tris, test_order=2)
+    assert not np.array_equal(ci, lex[2]) or not np.array_equal(rp, lex[1])  # the rule changes the numbering
+    (brp, bci), _ = lg.pattern()
+    assert np.array_equal(lg.multipliers()[0], lam) and np.array_equal(brp, rp) and np.array_equal(bci, ci)
+    # the edge table in multiplier order: first appearance over every boundary face
+    ae, al = orc.boundary_faces(m.conn)
+    an = m.conn[ae[:, None], orc.FACE_PTS[al]]
+    seen, order_all = set(), []
+    for t in an.tolist():
+        for j in range(3):
+            k = tuple(sorted((t[j], t[(j + 1) % 3])))
+            if k not in seen:
+                seen.add(k)
+                order_all.append(k)
+    fn = m.conn[fe[:, None], orc.FACE_PTS[fl]]
+    mine = {tuple(sorted((t[j], t[(j + 1) % 3]))) for t in fn.tolist() for j in range(3)}
+    assert [tuple(e) for e in lg.edge_multipliers().tolist()] == [k for k in order_all if k in mine]
+    bptr, bsrc, _ = lg.export_maps()
+    fm = kernel_face_matrices(face_lib, order, 6, m.xyz, m.conn, fe, fl, 2).reshape(-1)
+    bv = np.array([np.sum(fm[bsrc[bptr[k]:bptr[k + 1]]]) for k in range(lg.nnz_b)])
+    assert row_scaled_err(rp, v, bv) <= 1e-13
 
 
 def test_face_in_three_tets_is_rejected():

@@ -281,3 +281,16 @@ def test_saddle_with_mtm_and_mmt_matches_oracle(order):
     (_, _), (gsrp, gsci) = lg.pattern()
     assert np.array_equal(gsrp, srp) and np.array_equal(gsci, sci)
     assert row_scaled_err(srp, sref, S.cpu().numpy()) <= 1e-12
+
+
+def test_p2_multipliers_on_first_numbered_mesh():
+    m = meshgen.kuhn_cube(3, jitter=0.2, seed=31, permute=True)
+    mesh = mg.Mesh(m.xyz, m.conn, order=2, edge_rule="first")
+    b = mg.MatrixBuilder(mesh)
+    lg = mg.LagrangeBuilder(b, test_order=2)
+    got = lg.assemble(quad=6).cpu().numpy()
+    lam, rp, ci, ref, _, _ = orc.lagrange(2, 6, m.xyz, m.conn, mesh.elem_dofs(), b.ndof, test_order=2,
+                                          edge_rule="first")
+    (brp, bci), _ = lg.pattern()
+    assert np.array_equal(brp, rp) and np.array_equal(bci, ci)
+    assert row_scaled_err(rp, ref, got) <= 1e-12
