@@ -1,21 +1,25 @@
 """Benchmark of the FE operator hot path on GB300.
 
 Workload (default): P1 variable-coefficient diffusion operator div(kappa grad u)
-on a 64^3-cell Kuhn cube (1,572,864 tets, 274,625 nodes, 4,018,753 CSR
-entries), interior nodes jittered by +-0.2h, elements randomly permuted (seed 1),
-kappa lognormal (sigma 1), 4-point quadrature.  One step = FP64 assembly of the
-operator from device-resident inputs + 100 FP64 CSR SpMVs on a random vector in
-[-1, 1].  `value` = tets pushed through that step per second (tets / step time),
-summed over replicas.  L2 is flushed (a 256 MB write) before every step.
+on a 128^3-cell Kuhn cube (12,582,912 tets, 2,146,689 nodes, 31,802,497 CSR
+entries), interior nodes jittered by +-0.25h, elements randomly permuted and
+kappa lognormal with sigma 1.5 (seed 3), 4-point quadrature.  One step = FP64
+assembly of the operator from device-resident inputs + 100 FP64 CSR SpMVs on a
+random vector in [-1, 1].  `value` = tets pushed through that step per second
+(tets / step time), summed over replicas.  L2 is flushed (a 256 MB write)
+before every step; the SpMV working set (425 MB) is larger than L2 as well.
 
-Also reported (measured after the timed steps, same data): FP32 assembly and
-SpMV, each kernel's achieved GB/s against the measured HBM peak, the FP64-PCG
-vs FP32-refined-CG time to a 1e-10 relative residual on the same operator with
-Dirichlet u = 0 and f = 1, the end-to-end number through the C ABI with host
-buffers, and the oracle (a restatement of the reference algorithm) timed on one
-host core as the CPU baseline.
+Also reported (measured after the timed steps, same data): FP32 and native-FP64
+assembly, FP32 SpMV, the load vector and the adjoint gradient, each kernel's
+achieved GB/s against the measured HBM peak; FP64-PCG vs FP32-refined CG to a
+1e-10 relative residual on a system whose exact discrete solution is known
+(rhs = A u*), with each solution's error; the end-to-end number through the C
+ABI with host buffers (warm: plan resident; cold: from host arrays, mesh and
+plan built inside the timed region); the P2 48^3 case (Keast 11-point rule,
+mixed vs FP64 CG) as a sub-record; and the oracle (a restatement of the
+reference algorithm) timed on one host core as the CPU baseline.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--n 64]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--config 2|3|5]
 """
 from __future__ import annotations
 
@@ -25,6 +29,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -32,30 +37,39 @@ sys.path.insert(0, ROOT)
 
 METRIC = "tets assembled/s + SpMV GB/s vs HBM peak; FP32-refined vs FP64 CG time to 1e-10"
 N_SPMV = 100
+# the P1 workloads: 2 = 64^3 (jitter 0.2h, sigma 1, seed 1), 5 = 128^3 (jitter 0.25h, sigma 1.5, seed 3)
+P1_CONFIGS = {2: {"n": 64, "jitter": 0.2, "seed": 1, "sigma": 1.0},
+              5: {"n": 128, "jitter": 0.25, "seed": 3, "sigma": 1.5}}
 
 
-def parse():
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--n", type=int, default=64, help="cells per cube edge")
-    ap.add_argument("--jitter", type=float, default=0.2)
-    ap.add_argument("--sigma", type=float, default=1.0)
-    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--config", type=int, default=5, choices=[2, 3, 5],
+                    help="5: P1 128^3 (default); 2: P1 64^3; 3: P2 48^3 mixed-precision vs FP64 CG only")
+    ap.add_argument("--n", type=int, default=None, help="cells per cube edge (default: the config's)")
+    ap.add_argument("--jitter", type=float, default=None)
+    ap.add_argument("--sigma", type=float, default=None)
+    ap.add_argument("--seed", type=int, default=None)
     ap.add_argument("--no-cg", action="store_true")
-    ap.add_argument("--eager", action="store_true", help="time the step as stream launches instead of a CUDA graph")
+    ap.add_argument("--no-p2", action="store_true", help="skip the P2 48^3 sub-record")
+    ap.add_argument("--no-cold", action="store_true", help="skip the cold end-to-end sub-record")
+    ap.add_argument("--graph", action="store_true", help="time the step as one CUDA graph replay")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--config", type=int, default=2, choices=[2, 3, 5],
-                    help="2: the headline step (default); 3: P2 48^3 mixed-precision vs FP64 CG; "
-                         "5: P1 128^3 kernels as fractions of the HBM roofline")
     ap.add_argument("--order", type=int, default=1, choices=[1, 2], help="element order of the --only modes")
     ap.add_argument("--only", default=None,
                     choices=["asm64", "asm32", "spmv64", "spmv32", "cg64", "cg32", "adj", "rhs", "suite", "setup",
                              "lagrange"],
                     help="run warmup + steps launches of one kernel only (for profilers) and print its timing")
-    return ap.parse_args()
+    a = ap.parse_args(argv)
+    base = P1_CONFIGS.get(a.config, P1_CONFIGS[5])
+    for k, v in base.items():
+        if getattr(a, k) is None:
+            setattr(a, k, v)
+    return a
 
 
 def peaks():
@@ -68,23 +82,30 @@ def peaks():
 
 def workload_config(a, E, N, nnz):
     return {"workload": f"P1 kappa-diffusion operator, {a.n}^3 cells x 6 tets ({E} tets, {N} nodes, {nnz} CSR entries), "
-                        f"jitter +-{a.jitter}h, element permutation seed {a.seed}, lognormal kappa sigma {a.sigma}, "
+                        f"jitter +-{a.jitter}h, element permutation and lognormal kappa sigma {a.sigma} (seed {a.seed}), "
                         f"4-point rule; step = FP64 assembly + {N_SPMV} FP64 SpMV",
             "n_cells": a.n, "tets": E, "nodes": N, "nnz": nnz, "quadrature": 4,
-            "l2": "flushed before every step (256 MB write)", "parallelism": f"replicas x{a.gpus}"}
+            "l2": "flushed before every step (256 MB write); the SpMV working set is larger than L2 at 128^3",
+            "parallelism": f"replicas x{a.gpus}"}
 
 
-def profiled_traffic(kernel):
-    """DRAM bytes per launch of `kernel` inside the step, from the committed ncu summary of the step"""
-    p = os.path.join(ROOT, "profiles", "launches_step_p1_64cube.md")
+def profiled_traffic(kernel, n):
+    """DRAM bytes per launch of `kernel` at n^3 cells, from the committed ncu summary
+    (a line `traffic_bytes_per_launch <kernel> <n> <bytes>`), or None."""
+    pdir = os.path.join(ROOT, "profiles")
     try:
-        for line in open(p):
-            f = line.split()
-            if len(f) == 3 and f[0] == "traffic_bytes_per_launch" and f[1] == kernel:
-                return float(f[2]), "profiles/launches_step_p1_64cube.md (ncu --cache-control none, mean over the step's launches)"
+        names = sorted(os.listdir(pdir))
     except OSError:
-        pass
-    return None, "no committed ncu capture for this kernel"
+        return None, "no profiles directory"
+    for name in names:
+        try:
+            for line in open(os.path.join(pdir, name)):
+                f = line.split()
+                if len(f) == 4 and f[0] == "traffic_bytes_per_launch" and f[1] == kernel and f[2] == str(n):
+                    return float(f[3]), f"profiles/{name} (ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch)"
+        except OSError:
+            continue
+    return None, f"no committed ncu capture of {kernel} at {n}^3"
 
 
 def asm_bytes(E, nv, nnz, sv, nb=4):
@@ -123,7 +144,7 @@ class ClockSampler:
 
     def __enter__(self):
         try:
-            self.out = open(os.path.join("/tmp", f"mg_clocks_{os.getpid()}.csv"), "w+")
+            self.out = tempfile.TemporaryFile("w+")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
                                           "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=self.out, stderr=subprocess.DEVNULL)
@@ -165,62 +186,77 @@ class ClockSampler:
 # --------------------------------------------------------------- reference --
 def _ref_worker(args):
     """One host process = one 'MPI rank' of the reference algorithm: assembles
-    its slab of elements into CSR (pattern + values, insertion order sums) and
+    its slab of elements into CSR (pattern + values, insertion-order sums) and
     applies the result 100 times.  Runs the oracle (CPU restatement)."""
-    n, jitter, seed, sigma, rank, nranks, steps = args
+    path, rank, nranks, steps, seed = args
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import numpy as np
     import oracle as orc
-    from morganapublic_gb300 import meshgen
-    m = meshgen.kuhn_cube(n, jitter=jitter, seed=seed, permute=True)
-    kappa = meshgen.lognormal(len(m.conn), sigma, seed)
-    E = len(m.conn)
+    d = np.load(path, mmap_mode="r")
+    E = d["conn"].shape[0]
     lo, hi = rank * E // nranks, (rank + 1) * E // nranks
-    conn = np.ascontiguousarray(m.conn[lo:hi])
-    kap = np.ascontiguousarray(kappa[lo:hi])
-    x = np.random.default_rng(seed).uniform(-1, 1, len(m.xyz))
+    xyz = np.ascontiguousarray(d["xyz"])
+    conn = np.ascontiguousarray(d["conn"][lo:hi])
+    kap = np.ascontiguousarray(d["kappa"][lo:hi])
+    x = np.random.default_rng(seed).uniform(-1, 1, len(xyz))
     times = []
     for _ in range(steps):
         t0 = time.perf_counter()
-        dofs = orc.elem_dofs(1, len(m.xyz), conn)
-        rp, ci = orc.pattern(1, len(m.xyz), dofs)
-        vals = orc.assemble("stiff_kappa", 1, 4, m.xyz, conn, dofs, rp, ci, kap)
+        dofs = orc.elem_dofs(1, len(xyz), conn)
+        rp, ci = orc.pattern(1, len(xyz), dofs)
+        vals = orc.assemble("stiff_kappa", 1, 4, xyz, conn, dofs, rp, ci, kap)
         for _ in range(N_SPMV):
-            y = orc.spmv(rp, ci, vals, x)
+            orc.spmv(rp, ci, vals, x)
         times.append(time.perf_counter() - t0)
     return times, hi - lo
 
 
 def run_reference(a):
+    """The reference algorithm (the oracle, a C restatement; the reference binary
+    needs MPI, Boost and Trilinos and does not build here) on all host cores, on
+    the same workload as the GPU arm: the elements split over one process per
+    core, each assembling its slab (pattern + values) and applying it 100 times."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
     import multiprocessing as mp
+    import numpy as np
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as orc
+    from morganapublic_gb300 import meshgen
     orc.build()
     nproc = os.cpu_count() or 1
+    m = meshgen.kuhn_cube(a.n, jitter=a.jitter, seed=a.seed, permute=True)
+    kappa = meshgen.lognormal(len(m.conn), a.sigma, a.seed)
+    E, N = len(m.conn), len(m.xyz)
+    # edges of the Kuhn cube (axis, face-diagonal and body-diagonal ones): nnz = N + 2 n_edges
+    n_edges = 3 * a.n * (a.n + 1) ** 2 + 3 * a.n ** 2 * (a.n + 1) + a.n ** 3
     # bounded sample: the full mesh split over all host cores, at most 1 warm-up
-    # and 5 timed steps (each step takes about a second on the host)
+    # and 5 timed steps (a 128^3 step takes a few seconds on the host)
     warm, timed = min(a.warmup, 1), max(1, min(a.steps, 5))
     steps = warm + timed
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(nproc) as pool:
-        res = pool.map(_ref_worker, [(a.n, a.jitter, a.seed, a.sigma, r, nproc, steps) for r in range(nproc)])
+    with tempfile.TemporaryDirectory() as td:
+        path = os.path.join(td, "mesh.npz")
+        np.savez(path, xyz=m.xyz, conn=m.conn, kappa=kappa)
+        del m
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(nproc) as pool:
+            res = pool.map(_ref_worker, [(path, r, nproc, steps, a.seed) for r in range(nproc)])
     per_step = [max(r[0][s] for r in res) for s in range(warm, steps)]
-    E = sum(r[1] for r in res)
+    assert sum(r[1] for r in res) == E
     t = statistics.mean(per_step)
     val = E / t
     line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "tets/s", "n_gpus": a.gpus,
             "steps": timed, "warmup": warm, "ms_per_step": t * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"P1 kappa-diffusion operator, {a.n}^3 cells x 6 tets, step = FP64 assembly "
-                                   f"(pattern + values) + {N_SPMV} SpMV, elements split over {nproc} host processes",
-                       "n_cells": a.n, "tets": E},
+            "config": {**workload_config(a, E, N, N + 2 * n_edges),
+                       "l2": "host run (no L2 flush)",
+                       "parallelism": f"elements split over {nproc} host processes (one per core)"},
             "cpu_baseline": {"value": val, "unit": "tets/s", "cores": nproc, "kind": "port",
-                             "sample": f"full {a.n}^3 mesh, {timed} timed steps, {nproc} processes x 1 thread, "
-                                       "CPU restatement of the reference algorithm (reference binary not buildable: "
-                                       "needs MPI, Boost, Trilinos)"},
+                             "sample": f"full {a.n}^3 mesh, {timed} timed steps (of the {a.steps} asked: a step "
+                                       f"takes seconds on the host), {nproc} processes x 1 thread, CPU restatement "
+                                       "of the reference algorithm (reference binary not buildable: needs MPI, "
+                                       "Boost, Trilinos)"},
             "e2e": {"value": val, "unit": "tets/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -444,7 +480,20 @@ def _timed_cuda(torch, stream, fn, reps, flush=None):
     return statistics.median(ts)
 
 
-def run_config3(a):
+def _rec(peak, bytes_, ms, units=None):
+    gbs = bytes_ / (ms * 1e-3) / 1e9
+    d = {"ms": ms, "gbs": gbs, "frac_of_hbm": gbs / peak, "algorithmic_bytes": bytes_}
+    if units:
+        d["tets_per_s"] = units / (ms * 1e-3)
+    return d
+
+
+def _sin_field(X):
+    import numpy as np
+    return np.sin(np.pi * X[:, 0]) * np.sin(np.pi * X[:, 1]) * np.sin(np.pi * X[:, 2])
+
+
+def p2_record(seed=1):
     """P2 (10-node) kappa-stiffness on 48^3 cells x 6 tets, Keast 11-point rule, kappa lognormal sigma 0.5.
     The right-hand side is A u_I for the P2 interpolant u_I of sin(pi x) sin(pi y) sin(pi z) (zero on the
     boundary, Dirichlet rows eliminated), so u_I is the exact discrete solution and each solver's error
@@ -458,7 +507,7 @@ def run_config3(a):
     stream = torch.cuda.Stream()
     peak, peak_kind = peaks()
     m = meshgen.kuhn_cube(n)
-    kappa_h = meshgen.lognormal(len(m.conn), 0.5, a.seed)
+    kappa_h = meshgen.lognormal(len(m.conn), 0.5, seed)
     setup = {}
     t0 = time.perf_counter()
     mesh = mg.Mesh(m.xyz, m.conn, order=2)
@@ -475,11 +524,12 @@ def run_config3(a):
     setup["identical"] = bool(np.array_equal(mesh.elem_dofs(), mesh_d.elem_dofs()) and
                               all(np.array_equal(u, w) for u, w in zip(b.pattern(), b_d.pattern())))
     b_d.close()
+    mesh_d.close()
     E, ndof, nnz = len(m.conn), b.ndof, b.nnz
     en, _ = mesh.edges()
     X = np.concatenate([m.xyz, 0.5 * (m.xyz[en[:, 0]] + m.xyz[en[:, 1]])])
     bmask = meshgen.p2_boundary(m.boundary, en)
-    uI = np.sin(np.pi * X[:, 0]) * np.sin(np.pi * X[:, 1]) * np.sin(np.pi * X[:, 2])
+    uI = _sin_field(X)
     uI[bmask] = 0.0
     kappa = torch.from_numpy(kappa_h).cuda()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -499,11 +549,15 @@ def run_config3(a):
     t64n = _timed_cuda(torch, stream, lambda: b.assemble("stiff_kappa", coeff=kappa, quad=q, prec="f64_native",
                                                          out=A64, stream=stream), 20, flush)
     with torch.cuda.stream(stream):
+        b.assemble("stiff_kappa", coeff=kappa, quad=q, prec="f64", out=A64, stream=stream)
         b.apply_dirichlet(A64, mask, stream=stream)
         b.apply_dirichlet(A32, mask, stream=stream)
     y = torch.empty_like(rhs)
     ts64 = _timed_cuda(torch, stream, lambda: b.apply(A64, uI_d, out=y, stream=stream), 20, flush)
-    res = {}
+    A32c = A32.clone()
+    x32 = uI_d.float()
+    y32 = torch.empty_like(x32)
+    ts32 = _timed_cuda(torch, stream, lambda: b.apply(A32c, x32, out=y32, stream=stream), 20, flush)
     for rep in range(2):
         with torch.cuda.stream(stream):
             xs, i64 = b.cg(A64, rhs, rtol=1e-10, maxit=50000, stream=stream)
@@ -517,119 +571,32 @@ def run_config3(a):
     tadj = _timed_cuda(torch, stream, lambda: b.adjoint_grad(xs, xr, quad=q, out=g, stream=stream), 20, flush)
     trhs = _timed_cuda(torch, stream, lambda: b.build_vector(field=uI_d, elem_scale=kappa, quad=q, out=yb,
                                                              stream=stream), 20, flush)
-    B64, B32 = asm_bytes(E, len(m.xyz), nnz, 8, nb=10), asm_bytes(E, len(m.xyz), nnz, 4, nb=10)
-    S64 = spmv_bytes(ndof, nnz, 8)
-    line = {"config": {"workload": f"P2 kappa-stiffness, {n}^3 cells x 6 tets ({E} tets, {ndof} dofs, {nnz} CSR entries), "
-                                   "Keast 11-point rule, lognormal kappa sigma 0.5, rhs = A u_I (u_I = P2 interpolant "
-                                   "of sin(pi x) sin(pi y) sin(pi z)), Dirichlet u = 0",
-                       "tets": E, "dofs": ndof, "nnz": nnz, "setup": setup},
-            "assembly_f64": {"ms": t64, "tets_per_s": E / (t64 * 1e-3), "gbs": B64 / (t64 * 1e-3) / 1e9,
-                             "frac_of_hbm": B64 / (t64 * 1e-3) / 1e9 / peak},
-            "assembly_f32": {"ms": t32, "tets_per_s": E / (t32 * 1e-3), "gbs": B32 / (t32 * 1e-3) / 1e9,
-                             "frac_of_hbm": B32 / (t32 * 1e-3) / 1e9 / peak},
-            "assembly_f64_native": {"ms": t64n, "tets_per_s": E / (t64n * 1e-3),
-                                    "note": "native FP64 element arithmetic (MG_F64_NATIVE), for comparison"},
-            "spmv_f64_cold": {"ms": ts64, "gbs": S64 / (ts64 * 1e-3) / 1e9, "frac_of_hbm": S64 / (ts64 * 1e-3) / 1e9 / peak},
-            "adjoint_grad": {"ms": tadj, "tets_per_s": E / (tadj * 1e-3),
-                             "gbs": adj_bytes(E, len(m.xyz), ndof, 10) / (tadj * 1e-3) / 1e9},
-            "load_vector": {"ms": trhs, "tets_per_s": E / (trhs * 1e-3),
-                            "gbs": rhs_bytes(E, len(m.xyz), ndof, 10) / (trhs * 1e-3) / 1e9},
-            "cg": {"fp64_pcg": i64.as_dict(), "fp32_refined": imx.as_dict(),
-                   "speedup_refined_vs_fp64": i64.seconds / imx.seconds if imx.seconds > 0 else None,
-                   "fp64_error_vs_exact_discrete": err64, "refined_error_vs_exact_discrete": errmx,
-                   "refined_vs_fp64_rel_diff": diff, "precond": "jacobi", "rtol": 1e-10, "inner_rtol": 1e-2},
-            "peak_gbs": peak, "peak_kind": peak_kind}
-    print(json.dumps(line))
-    return 0
+    nv = len(m.xyz)
+    rec = {"config": {"workload": f"P2 kappa-stiffness, {n}^3 cells x 6 tets ({E} tets, {ndof} dofs, {nnz} CSR "
+                                  "entries), Keast 11-point rule, lognormal kappa sigma 0.5, rhs = A u_I (u_I = P2 "
+                                  "interpolant of sin(pi x) sin(pi y) sin(pi z)), Dirichlet u = 0; L2 flushed "
+                                  "before each kernel timing",
+                      "tets": E, "dofs": ndof, "nnz": nnz, "setup": setup},
+           "assembly_f64": _rec(peak, asm_bytes(E, nv, nnz, 8, nb=10), t64, E),
+           "assembly_f32": _rec(peak, asm_bytes(E, nv, nnz, 4, nb=10), t32, E),
+           "assembly_f64_native": {**_rec(peak, asm_bytes(E, nv, nnz, 8, nb=10), t64n, E),
+                                   "note": "native FP64 element arithmetic (MG_F64_NATIVE), for comparison"},
+           "spmv_f64": _rec(peak, spmv_bytes(ndof, nnz, 8), ts64),
+           "spmv_f32": _rec(peak, spmv_bytes(ndof, nnz, 4), ts32),
+           "adjoint_grad": _rec(peak, adj_bytes(E, nv, ndof, 10), tadj, E),
+           "load_vector": _rec(peak, rhs_bytes(E, nv, ndof, 10), trhs, E),
+           "cg": {"fp64_pcg": i64.as_dict(), "fp32_refined": imx.as_dict(),
+                  "speedup_refined_vs_fp64": i64.seconds / imx.seconds if imx.seconds > 0 else None,
+                  "fp64_error_vs_exact_discrete": err64, "refined_error_vs_exact_discrete": errmx,
+                  "refined_vs_fp64_rel_diff": diff, "precond": "jacobi", "rtol": 1e-10, "inner_rtol": 1e-2},
+           "peak_gbs": peak, "peak_kind": peak_kind}
+    b.close()
+    mesh.close()
+    return rec
 
 
-def run_config5(a):
-    """P1 128^3 x 6 tets, jitter +-0.25h, element permutation, kappa lognormal sigma 1.5 (seed 3): FP64 and
-    FP32 assembly, FP64 and FP32 SpMV (L2 flushed before each), FP64 CG and FP32-refined CG to 1e-10 with
-    Dirichlet u = 0 and f = 1, and the adjoint gradient kernel; each kernel against the measured HBM peak."""
-    import numpy as np
-    import torch
-    import morganapublic_gb300 as mg
-    from morganapublic_gb300 import meshgen
-    n = 128
-    stream = torch.cuda.Stream()
-    peak, peak_kind = peaks()
-    m = meshgen.kuhn_cube(n, jitter=0.25, seed=3, permute=True)
-    kappa_h = meshgen.lognormal(len(m.conn), 1.5, 3)
-    t0 = time.perf_counter()
-    mesh = mg.Mesh(m.xyz, m.conn, order=1)
-    t_mesh = time.perf_counter() - t0
-    b = mg.MatrixBuilder(mesh)
-    t_plan = time.perf_counter() - t0 - t_mesh  # CSR pattern + assembly schedule (host)
-    E, N, ndof, nnz = len(m.conn), len(m.xyz), b.ndof, b.nnz
-    kappa = torch.from_numpy(kappa_h).cuda()
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    v64 = torch.empty(nnz, dtype=torch.float64, device="cuda")
-    v32 = torch.empty(nnz, dtype=torch.float32, device="cuda")
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    b.assemble("stiff_kappa", coeff=kappa, quad=4, prec="f64", out=v64)  # first use: chunk records + upload
-    torch.cuda.synchronize()
-    t_upload = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    bd = mg.MatrixBuilder(mesh, pattern_on_device=True)  # the same plan, CSR pattern built on the GPU
-    t_plan_dev = time.perf_counter() - t0
-    same_pattern = all(np.array_equal(u, w) for u, w in zip(b.pattern(), bd.pattern()))
-    bd.close()
-    x = torch.from_numpy(np.random.default_rng(3).uniform(-1, 1, ndof)).cuda()
-    x32 = x.float()
-    y, y32 = torch.empty_like(x), torch.empty_like(x32)
-    ta64 = _timed_cuda(torch, stream, lambda: b.assemble("stiff_kappa", coeff=kappa, quad=4, prec="f64", out=v64,
-                                                         stream=stream), 20, flush)
-    ta32 = _timed_cuda(torch, stream, lambda: b.assemble("stiff_kappa", coeff=kappa, quad=4, prec="f32", out=v32,
-                                                         stream=stream), 20, flush)
-    ta64n = _timed_cuda(torch, stream, lambda: b.assemble("stiff_kappa", coeff=kappa, quad=4, prec="f64_native",
-                                                          out=v64, stream=stream), 20, flush)
-    ts64 = _timed_cuda(torch, stream, lambda: b.apply(v64, x, out=y, stream=stream), 20, flush)
-    ts32 = _timed_cuda(torch, stream, lambda: b.apply(v32, x32, out=y32, stream=stream), 20, flush)
-    with torch.cuda.stream(stream):
-        rhs = b.build_vector(quad=4, stream=stream)
-        mask = torch.from_numpy(m.boundary)
-        b.apply_dirichlet(v64, mask, rhs, stream=stream)
-        b.apply_dirichlet(v32, mask, stream=stream)
-    torch.cuda.synchronize()
-    with torch.cuda.stream(stream):
-        xs, i64 = b.cg(v64, rhs, rtol=1e-10, maxit=50000, stream=stream)
-        xr, imx = b.cg_refined(v64, v32, rhs, rtol=1e-10, inner_rtol=1e-2, stream=stream)
-    torch.cuda.synchronize()
-    diff = float(torch.linalg.norm(xr - xs) / torch.linalg.norm(xs))
-    lam = torch.from_numpy(np.random.default_rng(4).uniform(-1, 1, ndof)).cuda()
-    g = torch.empty(E, dtype=torch.float64, device="cuda")
-    tg = _timed_cuda(torch, stream, lambda: b.adjoint_grad(xs, lam, quad=4, out=g, stream=stream), 20, flush)
-    yb = torch.empty_like(xs)
-    tb = _timed_cuda(torch, stream, lambda: b.build_vector(field=xs, elem_scale=kappa, quad=4, out=yb,
-                                                           stream=stream), 20, flush)
-
-    def rec(bytes_, ms, units=None):
-        gbs = bytes_ / (ms * 1e-3) / 1e9
-        d = {"ms": ms, "gbs": gbs, "frac_of_hbm": gbs / peak, "algorithmic_bytes": bytes_}
-        if units:
-            d["tets_per_s"] = units / (ms * 1e-3)
-        return d
-
-    line = {"config": {"workload": f"P1 kappa-diffusion, {n}^3 cells x 6 tets ({E} tets, {N} nodes, {nnz} CSR entries), "
-                                   "jitter +-0.25h, element permutation and lognormal kappa sigma 1.5 (seed 3), "
-                                   "4-point rule; L2 flushed before each kernel timing",
-                       "tets": E, "nodes": N, "nnz": nnz, "mesh_tables_seconds": t_mesh, "host_plan_seconds": t_plan,
-                       "first_use_seconds": t_upload, "plan_seconds_pattern_on_device": t_plan_dev,
-                       "device_pattern_identical": same_pattern},
-            "assembly_f64": rec(asm_bytes(E, N, nnz, 8), ta64, E),
-            "assembly_f32": rec(asm_bytes(E, N, nnz, 4), ta32, E),
-            "assembly_f64_native": rec(asm_bytes(E, N, nnz, 8), ta64n, E),
-            "spmv_f64": rec(spmv_bytes(ndof, nnz, 8), ts64),
-            "spmv_f32": rec(spmv_bytes(ndof, nnz, 4), ts32),
-            "adjoint_grad": rec(adj_bytes(E, N, ndof), tg, E),
-            "load_vector": rec(rhs_bytes(E, N, ndof), tb, E),
-            "cg": {"fp64_pcg": i64.as_dict(), "fp32_refined": imx.as_dict(),
-                   "speedup_refined_vs_fp64": i64.seconds / imx.seconds if imx.seconds > 0 else None,
-                   "refined_vs_fp64_rel_diff": diff, "precond": "jacobi", "rtol": 1e-10},
-            "peak_gbs": peak, "peak_kind": peak_kind}
-    print(json.dumps(line))
+def run_config3(a):
+    print(json.dumps(p2_record(a.seed)))
     return 0
 
 
@@ -644,8 +611,6 @@ def main():
         return run_only(a)
     if a.config == 3:
         return run_config3(a)
-    if a.config == 5:
-        return run_config5(a)
     cpu_base = None
     if rank == 0 and not a.no_cpu_baseline:
         cpu_base = cpu_baseline_port(a)  # before any CUDA work
@@ -664,8 +629,13 @@ def main():
     m = meshgen.kuhn_cube(a.n, jitter=a.jitter, seed=a.seed, permute=True)
     kappa_h = meshgen.lognormal(len(m.conn), a.sigma, a.seed)
     E, N = len(m.conn), len(m.xyz)
+    setup = {}
+    t0 = time.perf_counter()
     mesh = mg.Mesh(m.xyz, m.conn, order=1)
+    setup["mesh_tables_s"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
     b = mg.MatrixBuilder(mesh)
+    setup["plan_host_s"] = time.perf_counter() - t0
     nnz, ndof = b.nnz, b.ndof
     sched = b.schedule_info()
     kappa = torch.from_numpy(kappa_h).cuda()
@@ -676,6 +646,12 @@ def main():
     y = torch.empty(ndof, dtype=torch.float64, device="cuda")
     y32 = torch.empty(ndof, dtype=torch.float32, device="cuda")
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b.assemble("stiff_kappa", coeff=kappa, quad=4, prec="f64", out=v64)  # first use: upload of the plan
+    torch.cuda.synchronize()
+    setup["first_use_s"] = time.perf_counter() - t0
+    b.status()
 
     def step(ev=None):
         if ev:
@@ -688,15 +664,16 @@ def main():
         if ev:
             ev[2].record(stream)
 
-    # the step runs as a CUDA graph (captured once after warm-up: the same kernels
-    # with their launch overhead removed); --eager times the stream launches
+    # the step as stream launches (each launch is long against its launch cost at
+    # this size); events on the launching stream split it into the assembly and
+    # the SpMVs.  --graph replays it as one CUDA graph instead.
     graph = None
     with torch.cuda.stream(stream):
         for _ in range(a.warmup):
             flush.fill_(1.0)
             step()
         torch.cuda.synchronize()
-        if not a.eager:
+        if a.graph:
             graph = torch.cuda.CUDAGraph()
             with torch.cuda.graph(graph, stream=stream):
                 step()
@@ -724,104 +701,96 @@ def main():
         if world > 1:
             dist.barrier()
         torch.cuda.synchronize()
+    b.status()
     t_step = [e[0].elapsed_time(e[2]) for e in evs]
     if graph is None:
         t_asm = [e[0].elapsed_time(e[1]) for e in evs]
         t_spmv = [e[1].elapsed_time(e[2]) / N_SPMV for e in evs]
     else:
-        # split of the graph's time: the same step eagerly, with events between its parts
-        with torch.cuda.stream(stream):
-            evs2 = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(3)]
-            for s in range(3):
-                flush.fill_(float(s))
-                step(evs2[s])
-            torch.cuda.synchronize()
-        t_asm = [e[0].elapsed_time(e[1]) for e in evs2]
-        t_spmv = [e[1].elapsed_time(e[2]) / N_SPMV for e in evs2]
-        t_step_eager = [e[0].elapsed_time(e[2]) for e in evs2]
+        t_asm, t_spmv = [], []
     ms_step, value = replica_throughput(statistics.mean(t_step), E, world, "cuda")
 
-    # ---------------------------------------------------------- extra metrics (untimed above)
-    extras = {}
+    extras, line = {}, None
     if rank == 0:
-        def timed(fn, reps=20, flush_each=True):
-            ts = []
-            with torch.cuda.stream(stream):
-                for r in range(reps + 2):
-                    if flush_each:
-                        flush.fill_(float(r))
-                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                    e0.record(stream)
-                    fn()
-                    e1.record(stream)
-                    torch.cuda.synchronize()
-                    if r >= 2:
-                        ts.append(e0.elapsed_time(e1))
-            return statistics.median(ts)
-
-        B64 = asm_bytes(E, N, nnz, 8)
-        B32 = asm_bytes(E, N, nnz, 4)
+        B64, B32 = asm_bytes(E, N, nnz, 8), asm_bytes(E, N, nnz, 4)
         S64, S32 = spmv_bytes(ndof, nnz, 8), spmv_bytes(ndof, nnz, 4)
+        fl = dict(flush=flush)
+        if not t_asm:
+            t_asm = [_timed_cuda(torch, stream, lambda: b.assemble("stiff_kappa", coeff=kappa, quad=4, prec="f64",
+                                                                   out=v64, stream=stream), 20, **fl)]
+            t_spmv = [(ms_step - t_asm[0]) / N_SPMV]
         ta64 = statistics.median(t_asm)
-        ta32 = timed(lambda: b.assemble("stiff_kappa", coeff=kappa, quad=4, prec="f32", out=v32, stream=stream))
-        ts64_cold = timed(lambda: b.apply(v64, x, out=y, stream=stream))
-        ts32_cold = timed(lambda: b.apply(v32, x32, out=y32, stream=stream))
-        ts64_warm = statistics.median(t_spmv)
-
-        def rec(bytes_, ms, units=None):
-            gbs = bytes_ / (ms * 1e-3) / 1e9
-            d = {"ms": ms, "gbs": gbs, "frac_of_hbm": gbs / peak, "algorithmic_bytes": bytes_}
-            if units:
-                d["tets_per_s"] = units / (ms * 1e-3)
-            return d
-
-        extras["assembly_f64"] = rec(B64, ta64, E)
-        extras["assembly_f32"] = rec(B32, ta32, E)
-        extras["spmv_f64_cold"] = rec(S64, ts64_cold)
-        extras["spmv_f64_stream_launches"] = rec(S64, ts64_warm)
-        extras["spmv_f64_stream_launches"]["note"] = (f"{N_SPMV} back-to-back SpMVs as stream launches; the "
-                                                      f"{S64/1e6:.0f} MB working set stays in the 129 MB L2")
-        if graph is not None:
-            extras["step_graph_ms"] = ms_step
-            extras["step_eager_ms"] = statistics.mean(t_step_eager)
-            ts64_warm = (ms_step - ta64) / N_SPMV
-        extras["spmv_f64_in_step"] = rec(S64, ts64_warm)
-        extras["spmv_f64_in_step"]["note"] = ("per-SpMV time inside the timed step: (step - assembly) / "
-                                              f"{N_SPMV}; the working set stays in L2")
-        extras["spmv_f32_cold"] = rec(S32, ts32_cold)
+        ts64 = statistics.median(t_spmv)
+        ta32 = _timed_cuda(torch, stream, lambda: b.assemble("stiff_kappa", coeff=kappa, quad=4, prec="f32",
+                                                             out=v32, stream=stream), 20, **fl)
+        ta64n = _timed_cuda(torch, stream, lambda: b.assemble("stiff_kappa", coeff=kappa, quad=4, prec="f64_native",
+                                                              out=v64, stream=stream), 20, **fl)
+        ts64c = _timed_cuda(torch, stream, lambda: b.apply(v64, x, out=y, stream=stream), 20, **fl)
+        ts32 = _timed_cuda(torch, stream, lambda: b.apply(v32, x32, out=y32, stream=stream), 20, **fl)
+        lam = torch.from_numpy(np.random.default_rng(a.seed + 1).uniform(-1, 1, ndof)).cuda()
+        g = torch.empty(E, dtype=torch.float64, device="cuda")
+        yb = torch.empty_like(x)
+        b.adjoint_grad(x, lam, quad=4, out=g)  # first call builds the element-geometry cache
+        b.build_vector(field=x, elem_scale=kappa, quad=4, out=yb)  # and the load-vector map
+        tg = _timed_cuda(torch, stream, lambda: b.adjoint_grad(x, lam, quad=4, out=g, stream=stream), 20, **fl)
+        tb = _timed_cuda(torch, stream, lambda: b.build_vector(field=x, elem_scale=kappa, quad=4, out=yb,
+                                                               stream=stream), 20, **fl)
+        extras["assembly_f64"] = {**_rec(peak, B64, ta64, E),
+                                  "note": "in the timed step; double-word FP32 arithmetic, FP64-accurate values"}
+        extras["assembly_f32"] = _rec(peak, B32, ta32, E)
+        extras["assembly_f64_native"] = {**_rec(peak, B64, ta64n, E),
+                                         "note": "native FP64 element arithmetic (MG_F64_NATIVE), for comparison"}
+        extras["spmv_f64_in_step"] = {**_rec(peak, S64, ts64),
+                                      "note": f"per-SpMV time inside the timed step ({N_SPMV} back to back)"}
+        extras["spmv_f64_cold"] = {**_rec(peak, S64, ts64c), "note": "one launch, L2 flushed before it"}
+        extras["spmv_f32"] = {**_rec(peak, S32, ts32), "note": "one launch, L2 flushed before it"}
+        extras["adjoint_grad"] = _rec(peak, adj_bytes(E, N, ndof), tg, E)
+        extras["load_vector"] = _rec(peak, rhs_bytes(E, N, ndof), tb, E)
         extras["schedule"] = {"blocks": sched.nblocks, "items": sched.n_items, "recompute_factor": sched.n_items / E,
                               "entries": sched.n_entries, "padding_factor": sched.n_entries / max(1, sched.n_contrib)}
+        extras["setup"] = setup
+        if graph is not None:
+            extras["step_graph_ms"] = ms_step
 
-        # CG: FP64 PCG vs FP32-refined, Dirichlet u = 0, f = 1, to 1e-10
+        # CG: FP64 PCG vs FP32-refined, Dirichlet u = 0, rhs = A u* (u* = sin sin sin at the
+        # nodes, zero on the boundary), so u* is the exact discrete solution of the operator
+        # the parity tests check against the oracle; each solve's error against it
         if not a.no_cg:
+            us = _sin_field(m.xyz)
+            us[m.boundary] = 0.0
+            us_d = torch.from_numpy(us).cuda()
+            mask = torch.from_numpy(m.boundary)
             with torch.cuda.stream(stream):
-                rhs = b.build_vector(quad=4, stream=stream)
-                mask = torch.from_numpy(m.boundary)
                 A64 = b.assemble("stiff_kappa", coeff=kappa, quad=4, prec="f64", stream=stream)
                 A32 = b.assemble("stiff_kappa", coeff=kappa, quad=4, prec="f32", stream=stream)
-                b.apply_dirichlet(A64, mask, rhs, stream=stream)
+                b.apply_dirichlet(A64, mask, stream=stream)
                 b.apply_dirichlet(A32, mask, stream=stream)
+                rhs = b.apply(A64, us_d, stream=stream)
+            torch.cuda.synchronize()
+            for _ in range(2):  # the second solve of each is reported
+                with torch.cuda.stream(stream):
+                    xs, i64 = b.cg(A64, rhs, rtol=1e-10, maxit=50000, stream=stream)
+                    xr, imx = b.cg_refined(A64, A32, rhs, rtol=1e-10, inner_rtol=1e-2, stream=stream)
                 torch.cuda.synchronize()
-                xs, i64 = b.cg(A64, rhs, rtol=1e-10, maxit=20000, stream=stream)
-                xr, imx = b.cg_refined(A64, A32, rhs, rtol=1e-10, inner_rtol=1e-2, stream=stream)
-                torch.cuda.synchronize()
-                xs, i64 = b.cg(A64, rhs, rtol=1e-10, maxit=20000, stream=stream)
-                xr, imx = b.cg_refined(A64, A32, rhs, rtol=1e-10, inner_rtol=1e-2, stream=stream)
-                torch.cuda.synchronize()
-            diff = float(torch.linalg.norm(xr - xs) / torch.linalg.norm(xs))
+            nus = torch.linalg.norm(us_d)
             extras["cg"] = {"fp64_pcg": i64.as_dict(), "fp32_refined": imx.as_dict(),
                             "speedup_refined_vs_fp64": i64.seconds / imx.seconds if imx.seconds > 0 else None,
-                            "refined_vs_fp64_solution_rel_diff": diff, "precond": "jacobi", "rtol": 1e-10}
+                            "fp64_error_vs_exact_discrete": float(torch.linalg.norm(xs - us_d) / nus),
+                            "refined_error_vs_exact_discrete": float(torch.linalg.norm(xr - us_d) / nus),
+                            "refined_vs_fp64_solution_rel_diff": float(torch.linalg.norm(xr - xs) /
+                                                                       torch.linalg.norm(xs)),
+                            "precond": "jacobi", "rtol": 1e-10, "inner_rtol": 1e-2,
+                            "rhs": "A u*, u* = sin(pi x) sin(pi y) sin(pi z) at the nodes (zero on the boundary): "
+                                   "u* is the exact discrete solution"}
+            del A64, A32
 
-        # e2e through the C ABI with host buffers: kappa in, CSR values out, x in, y out
-        import ctypes
+        # e2e through the public API with host buffers: kappa in, CSR values out, x in, y out
         kap_pin = torch.from_numpy(kappa_h).pin_memory()
         x_pin = x.cpu().pin_memory()
         v_pin = torch.empty(nnz, dtype=torch.float64).pin_memory()
         y_pin = torch.empty(ndof, dtype=torch.float64).pin_memory()
         kap_d = torch.empty_like(kappa)
         x_d = torch.empty_like(x)
-
         # copies on a second stream overlap the kernels that do not need them: x
         # arrives during the assembly, the CSR values leave during the SpMVs
         cstream = torch.cuda.Stream()
@@ -845,36 +814,72 @@ def main():
             y_pin.copy_(y, non_blocking=True)
             stream.wait_event(ev_v)
 
-        te2e = timed(e2e_step, reps=max(3, min(a.steps, 10)))
-        h2d = 8 * E + 8 * ndof
-        d2h = 8 * nnz + 8 * ndof
-        del ctypes
+        te2e = _timed_cuda(torch, stream, e2e_step, max(3, min(a.steps, 10)), flush)
+        h2d, d2h = 8 * E + 8 * ndof, 8 * nnz + 8 * ndof
         e2e = {"value": world * E / (te2e * 1e-3), "unit": "tets/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "ms_per_step": te2e,
                "note": "kappa and x copied in from pinned host memory, CSR values and y copied out, per step; the x "
                        "upload overlaps the assembly and the values download overlaps the SpMVs (second stream)"}
 
-        dom = "assembly_f64" if statistics.median(t_asm) >= N_SPMV * ts64_warm else "spmv_f64_in_step"
-        rl = extras[dom]
-        kname = "k_assemble<1,kDW>" if dom == "assembly_f64" else "k_spmv<double,1>"
-        traffic, tnote = profiled_traffic(kname)
+        # cold e2e: the work the reference arm's step does, from host arrays -- mesh
+        # tables, CSR pattern (on the GPU) and assembly schedule, first assembly and
+        # 100 SpMVs, values and y back in host memory; wall clock
+        e2e_cold = None
+        if not a.no_cold:
+            ts = []
+            for _ in range(2):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                mc = mg.Mesh(m.xyz, m.conn, order=1)
+                bc = mg.MatrixBuilder(mc, pattern_on_device=True)
+                vc = bc.assemble("stiff_kappa", coeff=kap_pin, quad=4, prec="f64")
+                xc = x_pin.cuda()
+                yc = torch.empty_like(xc)
+                for _ in range(N_SPMV):
+                    bc.apply(vc, xc, out=yc)
+                vh, yh = vc.cpu(), yc.cpu()
+                torch.cuda.synchronize()
+                ts.append(time.perf_counter() - t0)
+                del vc, xc, yc, vh, yh
+                bc.close()
+                mc.close()
+            tc = statistics.mean(ts)
+            e2e_cold = {"value": world * E / tc, "unit": "tets/s", "ms_per_step": tc * 1e3,
+                        "runs_s": ts, "h2d_bytes_per_step": 24 * N + 16 * E + 8 * E + 8 * ndof,
+                        "d2h_bytes_per_step": d2h,
+                        "note": "from host arrays: mg_mesh_create + mg_pattern_build_device (CSR pattern on the GPU, "
+                                "assembly schedule on the host) + first mg_assemble (plan upload) + "
+                                f"{N_SPMV} SpMV, values and y copied back; wall clock, mean of 2 -- the work one "
+                                "step of the reference arm does"}
+
+        if not a.no_p2:
+            extras["config3_p2_48"] = p2_record()
+
+        rl = extras["spmv_f64_in_step"] if N_SPMV * ts64 >= ta64 else extras["assembly_f64"]
+        kname = "k_spmv<double,1>" if rl is extras["spmv_f64_in_step"] else "k_assemble<1,kDW>"
+        traffic, tnote = profiled_traffic(kname, a.n)
         roofline = {"bound": "hbm", "kernel": kname,
                     "achieved": rl["gbs"], "peak": peak, "unit": "GB/s", "frac": rl["gbs"] / peak,
                     "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
                     "traffic": traffic, "traffic_note": tnote,
-                    "note": "achieved = algorithmic bytes per launch / CUDA-event time per launch in the step; "
-                            "the step's SpMVs are served from L2 (traffic = DRAM bytes per launch)"}
+                    "note": "achieved = algorithmic bytes per launch (4-byte column indices counted) / CUDA-event "
+                            "time per launch inside the timed step"}
         clocks = clk.summary()
         line = {"metric": METRIC, "value": value, "unit": "tets/s", "n_gpus": world, "steps": a.steps,
                 "warmup": a.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Kuhn cube, lognormal kappa)",
+                "vs_baseline": None, "dtype": "f64",
+                "dtype_note": "FP64 values (IEEE doubles in and out, within 1e-12 row-scaled of the FP64 oracle); the "
+                              "assembly computes them in double-word FP32 arithmetic (two floats per number), the "
+                              "SpMV in native FP64; assembly_f64_native gives the native-FP64 assembly",
+                "data": "synthetic (seeded Kuhn cube, jitter, element permutation, lognormal kappa)",
                 "config": workload_config(a, E, N, nnz), "roofline": roofline, "cpu_baseline": cpu_base,
-                "e2e": e2e, "gpu_launches": a.steps * (1 + N_SPMV),
+                "e2e": e2e, "e2e_cold": e2e_cold, "gpu_launches": a.steps * (1 + N_SPMV),
                 "clocks": clocks, "wall_s_timed": t_wall, "kernels": extras}
-        print(json.dumps(line))
     if world > 1:
         dist.barrier()
         dist.destroy_process_group()
+    if line is not None:
+        print(json.dumps(line))
     return 0
 
 

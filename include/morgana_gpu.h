@@ -14,8 +14,11 @@
  *  - "d_" arguments are device pointers on the handle's device; "h_" arguments
  *    are host pointers, copied in or out inside the call.
  *  - stream: a cudaStream_t passed as void* (NULL = legacy default stream).
- *  - Handles own their device memory.  One handle per host thread; a handle may
- *    be shared between threads only under external locking.
+ *  - Handles own their device memory, on the device that was current at their
+ *    first GPU use; calls on a handle with another device current fail with
+ *    MG_ERR_INVALID_ARG.  One handle per host thread; a handle may be shared
+ *    between threads only under external locking (the first-use uploads are
+ *    locked, the calls themselves are not).
  *  - There is no CPU fallback: a call that cannot run on the GPU fails.
  */
 #ifndef MORGANA_GPU_H
@@ -94,7 +97,8 @@ typedef struct {
   int32_t outer_iterations;  /* refinement steps (0 for plain CG) */
   int32_t converged;
   int32_t reserved;
-  double rel_residual;       /* ||b - A x||_2 / ||b||_2 at exit, FP64 operator */
+  double rel_residual;       /* ||b - A x||_2 / ||b||_2 at exit, FP64 operator
+                                (b = 0: the absolute residual ||A x||_2) */
   double seconds;            /* device time of the solve (CUDA events) */
 } mg_cg_info;
 
@@ -304,7 +308,8 @@ mg_status mg_cg_refined(mg_plan* plan, const double* d_values64, const float* d_
    (larger plans get MG_ERR_SIZE).  The plan must already be resident on the
    device (any earlier GPU call on it, e.g. mg_assemble), else MG_ERR_INVALID_ARG.
    The first call on a device looks up the array's device address; make that
-   first call before any stream capture.  All calls share the one array: calls
+   first call before any stream capture.  The plan's device must be the
+   current device (else MG_ERR_INVALID_ARG).  All calls share the one array: calls
    that overlap on the GPU (other streams, other host threads) race and must be
    serialised by the caller.  Each call re-initialises what it reads. */
 #define MG_CG_NOALLOC_MAX_NDOF 400000
@@ -382,7 +387,10 @@ typedef struct {
      node, max node) order; MG_EDGES_FIRST meshes the order of first
      appearance over every boundary face (element then local-face order) and
      its edges (0,1), (1,2), (2,0) in faceToPoint vertex order, the order in
-     which connect3d stores a face.
+     which connect3d stores a face.  This takes the boundary grid to be the
+     whole boundary: the reference numbers the edges over the triangles its
+     Gmsh file lists (src/morganaGeometry/meshInit3d.hpp:411-428), which is the
+     same order when those triangles cover the boundary, as Gmsh writes them.
    B (n_multipliers x ndof): each face inserts its full nt x nb block (nt = 3
    for P1, 1 for P0, 6 for P2), explicit zeros included, as
    traitsMatrixBuilder::buildEpetraCrs does for localMatrixLA3d
@@ -437,7 +445,10 @@ mg_status mg_lagrange_export_products(const mg_lagrange* lg, int32_t which, int3
    B sums its blocks' contributions in the reference's insertion order
    (deterministic, no atomics).  The first device call on a handle (this one,
    mg_saddle_assemble, mg_saddle_spmv or mg_lagrange_apply) uploads its tables
-   and waits for the copies: make it before capturing a CUDA graph. */
+   and waits for the copies: make it before capturing a CUDA graph.  The face
+   blocks go through one staging buffer of the handle, so calls of this
+   function on one handle that overlap on the GPU (other streams or host
+   threads) race: serialise them. */
 mg_status mg_lagrange_assemble(mg_lagrange* lg, int32_t quad, double* d_b_values, void* stream);
 /* mg_lagrange_assemble with the values copied to host memory (nnz_b doubles):
    what buildEpetraCrs hands to Epetra for localMatrixLA3d.  Synchronous. */

@@ -1,7 +1,9 @@
 // Internal structures of libmorgana_gpu.so (not part of the C ABI).
 #pragma once
 
+#include <atomic>
 #include <cstdint>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -152,7 +154,10 @@ struct mg_mesh {
   float* d_lo_z = nullptr;
   int4* d_conn = nullptr;        // vertex node ids
   int32_t* d_dofs = nullptr;     // n_elem * nb
-  bool on_device = false;
+  // set once the device copies exist (first GPU use, under upload_mu); `device`
+  // is the device they live on
+  std::atomic<bool> on_device{false};
+  std::mutex upload_mu;
 };
 
 struct mg_plan {
@@ -202,7 +207,8 @@ struct mg_plan {
   double* d_tmp_coeff = nullptr;
   size_t tmp_coeff_bytes = 0;
   mg::HostSchedule* host_schedule = nullptr;  // until uploaded
-  bool on_device = false;
+  std::atomic<bool> on_device{false};  // set once uploaded (under upload_mu), on the mesh's device
+  std::mutex upload_mu;
 };
 
 // Saddle entry sources other than K and B entries (see mg_lagrange::s_src).
@@ -253,7 +259,8 @@ struct mg_lagrange {
   int2* d_m_pairs = nullptr;
   int32_t *d_p_pair_ptr = nullptr, *d_p_slot = nullptr;
   int2* d_p_pairs = nullptr;
-  bool on_device = false;
+  std::atomic<bool> on_device{false};  // set once uploaded (under upload_mu), on the plan's device
+  std::mutex upload_mu;
 };
 
 namespace mg {
@@ -273,6 +280,10 @@ struct HostSchedule {
   std::vector<int32_t> elem_order;   // all elements along a Morton curve of their centroids
   int32_t max_chunk_nodes = 0;
 };
+// MG_OK when `want` is the calling thread's current device, else
+// MG_ERR_INVALID_ARG naming both: a handle's device arrays are only valid on
+// the device they were uploaded to
+mg_status check_device(int want, const char* what);
 mg_status mesh_device(mg_mesh* m);  // uploads the mesh on first GPU use
 mg_status plan_device(mg_plan* p);  // uploads mesh + plan on first GPU use
 mg_status plan_tables(mg_plan* p, int quad, const RefTables** t, const double** d_tab);

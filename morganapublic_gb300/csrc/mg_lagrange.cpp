@@ -582,7 +582,9 @@ static void free_device(mg_lagrange* lg)
 
 mg_status lagrange_device(mg_lagrange* lg)
 {
-  if (lg->on_device) return MG_OK;
+  if (lg->on_device) return check_device(lg->plan->mesh->device, "the multiplier handle");
+  std::lock_guard<std::mutex> lock(lg->upload_mu);
+  if (lg->on_device) return check_device(lg->plan->mesh->device, "the multiplier handle");
   MG_TRY(plan_device(lg->plan));
   std::vector<int2> faces(lg->n_faces);
   for (int64_t f = 0; f < lg->n_faces; ++f) faces[f] = make_int2(lg->face_elem[f], lg->face_local[f]);

@@ -256,9 +256,21 @@ mg_status ensure_edges(mg_mesh* m)
   return MG_OK;
 }
 
+mg_status check_device(int want, const char* what)
+{
+  int dev = -1;
+  MG_CUDA(cudaGetDevice(&dev));
+  if (dev != want)
+    return set_error(MG_ERR_INVALID_ARG, std::string(what) + " was uploaded to device " + std::to_string(want) +
+                                             ", but device " + std::to_string(dev) + " is current");
+  return MG_OK;
+}
+
 mg_status mesh_device(mg_mesh* m)
 {
-  if (m->on_device) return MG_OK;
+  if (m->on_device) return check_device(m->device, "the mesh");
+  std::lock_guard<std::mutex> lock(m->upload_mu);
+  if (m->on_device) return check_device(m->device, "the mesh");
   MG_CUDA(cudaGetDevice(&m->device));
   const int64_t N = m->n_nodes, E = m->n_elem;
   std::vector<double4_32a> x64(N);

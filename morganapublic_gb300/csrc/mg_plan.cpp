@@ -561,7 +561,9 @@ static mg_status upload(T** dst, const std::vector<T>& src)
 
 mg_status plan_device(mg_plan* p)
 {
-  if (p->on_device) return MG_OK;
+  if (p->on_device) return check_device(p->mesh->device, "the plan");
+  std::lock_guard<std::mutex> lock(p->upload_mu);
+  if (p->on_device) return check_device(p->mesh->device, "the plan");
   MG_TRY(mesh_device(p->mesh));
   const HostSchedule& hs = *p->host_schedule;
   MG_TRY(upload(&p->d_rowptr, p->rowptr));

@@ -771,6 +771,14 @@ static mg_status cg_start(mg_plan* p, const V* vals, const V* b, const V* x, int
   return MG_OK;
 }
 
+// ||r|| / ||b|| from the squared norms; with b = 0 the absolute residual ||r||
+// (0 when r = 0 as well), never NaN
+static double rel_residual(double rr, double bb)
+{
+  if (rr == 0.0) return 0.0;
+  return bb > 0.0 ? std::sqrt(rr / bb) : std::sqrt(rr);
+}
+
 // ------------------------------------------------- CG without allocation --
 // Work space of mg_cg_solve_noalloc: a file-scope device array (16 MiB, 256-byte
 // aligned), enough for the CG vectors of MG_CG_NOALLOC_MAX_NDOF dofs.  Host code
@@ -823,6 +831,8 @@ mg_status mg_cg_solve_noalloc(mg_plan* p, const double* d_values, const double* 
                      "on it first, e.g. mg_assemble)");
   if (cg_work_bytes<double>(p->ndof) > kNoAllocScratchBytes)
     return set_error(MG_ERR_SIZE, "mg_cg_solve_noalloc: work space above the fixed array");
+  // the scratch address below is the current device's; the plan's arrays must be there too
+  MG_TRY(check_device(p->mesh->device, "mg_cg_solve_noalloc: the plan"));
   void* base = nullptr;
   MG_TRY(noalloc_scratch(&base));
   cudaStream_t st = (cudaStream_t)stream;
@@ -861,7 +871,7 @@ mg_status mg_cg_solve_noalloc(mg_plan* p, const double* d_values, const double* 
     info->iterations = hs.iter;
     info->outer_iterations = 0;
     info->converged = hs.done == 1;
-    info->rel_residual = std::sqrt(hs.rr / hs.bb);
+    info->rel_residual = rel_residual(hs.rr, hs.bb);
     info->seconds = secs;
   }
   if (hs.done == 2) return set_error(MG_ERR_NOT_CONVERGED, "CG breakdown: p.Ap <= 0");
@@ -907,7 +917,7 @@ mg_status mg_cg_solve(mg_plan* p, const double* d_values, const double* d_b, dou
     info->iterations = hs->iter;
     info->outer_iterations = 0;
     info->converged = hs->done == 1;
-    info->rel_residual = std::sqrt(hs->rr / hs->bb);
+    info->rel_residual = rel_residual(hs->rr, hs->bb);
     info->seconds = ms * 1e-3;
   }
   if (hs->done == 2) return set_error(MG_ERR_NOT_CONVERGED, "CG breakdown: p.Ap <= 0");
@@ -957,7 +967,7 @@ mg_status mg_cg_refined(mg_plan* p, const double* d_values64, const float* d_val
     MG_CUDA(cudaMemcpyAsync(hs, s64, sizeof(CgScalars), cudaMemcpyDeviceToHost, st));
     MG_CUDA(cudaStreamSynchronize(st));
     bb64 = hs->bb;
-    relres = std::sqrt(hs->rr / hs->bb);
+    relres = rel_residual(hs->rr, hs->bb);
     return MG_OK;
   };
   s = residual64();
