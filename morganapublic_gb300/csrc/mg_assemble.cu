@@ -276,6 +276,40 @@ __device__ __forceinline__ float hi_of<float>(const float& v) { return v; }
 template <>
 __device__ __forceinline__ float hi_of<ff>(const ff& v) { return v.hi; }
 
+template <>
+__device__ __forceinline__ float hi_of<double>(const double& v) { return (float)v; }
+
+// P1 stiffness needs the gradient of every vertex: the cofactor columns C_1..C_3
+// of J (gradients of vertices 1..3 times det) come from the edge vectors at
+// vertex 0, and vertex 0's follows from C_0 = -(C_1 + C_2 + C_3) -- the zero row
+// sums of the element matrix.  When |C_0| is small against the largest column
+// that sum cancels: its error is eps |C_max|, and the entries of vertex 0 (whose
+// row scale is |C_0| |C_max|) carry eps |C_max|^2.  On a Kuhn cube jittered by
+// 0.25 h the ratio |C_max| / |C_0| reaches 21 (12.6 M tets), which put the
+// double-word values 2.8e-12 row-scaled from the FP64 oracle.  Elements with
+// |C_max| > 3 |C_0| (under 1 % of such a mesh) take C_0 from the coordinates,
+// (x3 - x1) x (x2 - x1), and form the entries of vertex 0 as dot products.
+constexpr float kGradRatio2 = 9.0f;
+
+template <typename T>
+__device__ __forceinline__ bool c0_cancels(const Cof<T>& f)
+{
+  float n0 = 0.0f, nmax = 0.0f;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    float na = 0.0f;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) na = fmaf(hi_of(f.c[r][a]), hi_of(f.c[r][a]), na);
+    nmax = fmaxf(nmax, na);
+  }
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    const float s = hi_of(f.c[r][0]) + hi_of(f.c[r][1]) + hi_of(f.c[r][2]);
+    n0 = fmaf(s, s, n0);
+  }
+  return nmax > kGradRatio2 * n0;
+}
+
 // |det| small against its expansion terms
 template <typename T>
 __device__ __forceinline__ bool det_cancels(const T J[3][3], const Cof<T>& f)
@@ -454,6 +488,105 @@ __device__ __forceinline__ void p1_stiff_unique<ff>(const Cof<ff>& f, ff s, ff K
   K[2] = -(d[0][1] + d[1][1] + d[2][1]);
   K[3] = -(d[0][2] + d[1][2] + d[2][2]);
   K[0] = -(K[1] + K[2] + K[3]);
+}
+
+// C_0 = (x3 - x1) x (x2 - x1) (= -(C_1 + C_2 + C_3)) from the staged vertices,
+// accurate to its own magnitude: the edge vectors of the face opposite vertex 0
+// as differences of the chunk-relative coordinates, then their cross product.
+__device__ __forceinline__ void staged_c0(const float4* va, const float2* vb, ushort4 lc, float C0[3])
+{
+  const float4 a1 = va[lc.y], a2 = va[lc.z], a3 = va[lc.w];
+  const float2 b1 = vb[lc.y], b2 = vb[lc.z], b3 = vb[lc.w];
+  float f2[3], f3[3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    f2[r] = (vhi(a2, r) - vhi(a1, r)) + (vlo(a2, b2, r) - vlo(a1, b1, r));
+    f3[r] = (vhi(a3, r) - vhi(a1, r)) + (vlo(a3, b3, r) - vlo(a1, b1, r));
+  }
+  C0[0] = f3[1] * f2[2] - f3[2] * f2[1];
+  C0[1] = f3[2] * f2[0] - f3[0] * f2[2];
+  C0[2] = f3[0] * f2[1] - f3[1] * f2[0];
+}
+__device__ __forceinline__ void staged_c0(const float4* va, const float2* vb, ushort4 lc, ff C0[3])
+{
+  const float4 a1 = va[lc.y], a2 = va[lc.z], a3 = va[lc.w];
+  const float2 b1 = vb[lc.y], b2 = vb[lc.z], b3 = vb[lc.w];
+  ff f2[3], f3[3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    f2[r] = dw_diff2(vhi(a2, r), vhi(a1, r), vlo(a2, b2, r), vlo(a1, b1, r));
+    f3[r] = dw_diff2(vhi(a3, r), vhi(a1, r), vlo(a3, b3, r), vlo(a1, b1, r));
+  }
+  C0[0] = ff_cross(f3[1], f2[2], f3[2], f2[1]);
+  C0[1] = ff_cross(f3[2], f2[0], f3[0], f2[2]);
+  C0[2] = ff_cross(f3[0], f2[1], f3[1], f2[0]);
+}
+__device__ __forceinline__ void staged_c0(const float4* va, const float2* vb, ushort4 lc, double C0[3])
+{
+  Fetch<kF64> D;
+  fetch_staged<kF64>(va, vb, lc, D);
+  double f2[3], f3[3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    f2[r] = comp(D.x[2], r) - comp(D.x[1], r);
+    f3[r] = comp(D.x[3], r) - comp(D.x[1], r);
+  }
+  C0[0] = f3[1] * f2[2] - f3[2] * f2[1];
+  C0[1] = f3[2] * f2[0] - f3[0] * f2[2];
+  C0[2] = f3[0] * f2[1] - f3[1] * f2[0];
+}
+
+// P1 stiffness with every vertex gradient explicit: C_0 given, the entries of
+// vertex 0 as s (C_0 . C_j); the others as in p1_stiff_unique.
+template <typename T>
+__device__ __forceinline__ void p1_stiff_direct(const Cof<T>& f, const T C0[3], T s, T K[10])
+{
+  T d[3][3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = a; b < 3; ++b) {
+      d[a][b] = s * (f.c[0][a] * f.c[0][b] + f.c[1][a] * f.c[1][b] + f.c[2][a] * f.c[2][b]);
+      d[b][a] = d[a][b];
+    }
+  K[0] = s * (C0[0] * C0[0] + C0[1] * C0[1] + C0[2] * C0[2]);
+#pragma unroll
+  for (int b = 0; b < 3; ++b) K[1 + b] = s * (C0[0] * f.c[0][b] + C0[1] * f.c[1][b] + C0[2] * f.c[2][b]);
+  K[4] = d[0][0];
+  K[5] = d[0][1];
+  K[6] = d[0][2];
+  K[7] = d[1][1];
+  K[8] = d[1][2];
+  K[9] = d[2][2];
+}
+template <>
+__device__ __forceinline__ void p1_stiff_direct<ff>(const Cof<ff>& f, const ff C0[3], ff s, ff K[10])
+{
+  ff col[3][3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int r = 0; r < 3; ++r) col[a][r] = f.c[r][a];
+  K[0] = ff_mul(s, ff_dot3(C0, C0));
+#pragma unroll
+  for (int b = 0; b < 3; ++b) K[1 + b] = ff_mul(s, ff_dot3(C0, col[b]));
+  K[4] = ff_mul(s, ff_dot3(col[0], col[0]));
+  K[5] = ff_mul(s, ff_dot3(col[0], col[1]));
+  K[6] = ff_mul(s, ff_dot3(col[0], col[2]));
+  K[7] = ff_mul(s, ff_dot3(col[1], col[1]));
+  K[8] = ff_mul(s, ff_dot3(col[1], col[2]));
+  K[9] = ff_mul(s, ff_dot3(col[2], col[2]));
+}
+
+// The rare path above, out of line (like the FP64 geometry fallback), so that
+// its registers do not weigh on every other element.
+template <typename T>
+static __device__ __noinline__ void p1_stiff_direct_staged(const float4* va, const float2* vb, ushort4 lc,
+                                                           const Cof<T>& f, T s, T K[10])
+{
+  T C0[3];
+  staged_c0(va, vb, lc, C0);
+  p1_stiff_direct<T>(f, C0, s, K);
 }
 
 // The six scaled metric coefficients s (C_a . C_b), ab = 00,11,22,01,02,12.
@@ -840,7 +973,20 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
             T K[10];
             if (a.stiff) {
               const T sc = coef * wsum / f.det;
-              p1_stiff_unique<T>(f, sc, K);
+              // vertex 0's gradient from the coordinates where C_0 = -sum C_k
+              // cancels (rare; entered only when a lane of the warp needs it)
+              const bool direct = c0_cancels<T>(f);
+              if (__any_sync(__activemask(), direct)) {
+                if (direct) {
+                  const unsigned char* rb = stage_of(qq);
+                  const int n4 = (min(CI, d.item_count - c * CI) + 3) & ~3, nn = desc_of(qq)->n_nodes;
+                  const ushort4 lc = reinterpret_cast<const ushort4*>(rb + sizeof(ChunkDesc) + 4 * n4)[local];
+                  const float4* va = reinterpret_cast<const float4*>(rb + sizeof(ChunkDesc) + 12 * n4);
+                  const float2* vb = reinterpret_cast<const float2*>(rb + sizeof(ChunkDesc) + 12 * n4 + 16 * nn);
+                  p1_stiff_direct_staged<T>(va, vb, lc, f, sc, K);
+                }
+              }
+              if (!direct) p1_stiff_unique<T>(f, sc, K);
               check_scale(sc, K[4]);
             } else {
               const T sc = coef * f.det;

@@ -1,6 +1,6 @@
 """Generates the golden fixtures in this directory from the reference's own
-test data, read as text from a morganaPublic checkout (default
-/root/reference; pass another path as the first argument).
+test data, read as text from a morganaPublic checkout (its path is the
+required first argument).
 
   mignon3dC.json         tests/morganaMeshes/mignon3dC.msh: 7 nodes, 8 tets
                          (file order, node ids as written, geoId = 2nd tag)
@@ -15,14 +15,16 @@ test data, read as text from a morganaPublic checkout (default
                          the largest global dof id printed for P1 / P0 / P2 on
                          mignon3dC, i.e. the global dof counts
 
-Run: python tests/golden/make_golden.py [reference_root]
+Run: python tests/golden/make_golden.py <morganaPublic checkout>
 """
 import json
 import os
 import re
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    sys.exit("usage: make_golden.py <morganaPublic checkout>")
+REF = sys.argv[1]
 OUT = os.path.dirname(os.path.abspath(__file__))
 
 

@@ -567,3 +567,94 @@ def test_invalid_arguments_fail_loudly():
     assert e.value.status == mg.MG_ERR_INVALID_ARG
     with pytest.raises(mg.MorganaError):
         b.assemble("mass", quad=7)
+
+
+# ---------------------------------------------------------------------------
+# Against the reference's own code (tests/golden/ref_elements.npz: element
+# matrices computed by the reference's compiled quadrature cards, basis
+# polynomials, affine map and tensor3d inverse; the 8 tets of its mignon3dC test
+# mesh with kappa 12, and 8 jittered tets).  The tets are given disjoint nodes,
+# so each element matrix is its own block of the assembled CSR matrix.
+REF_QUAD = {1: 1, 2: 4, 3: 15, 4: 64}
+
+
+def _ref_disjoint():
+    import os
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_elements.npz"))
+    xyz = d["xyz"].reshape(-1, 3).copy()
+    conn = np.arange(len(xyz), dtype=np.int32).reshape(-1, 4)
+    return d, xyz, conn
+
+
+@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("op", ["stiff_kappa", "stiff_const", "mass", "mass_coeff"])
+def test_values_against_reference_code(op, order):
+    d, xyz, conn = _ref_disjoint()
+    kappa, c = d["kappa"], float(d["c"])
+    mesh = mg.Mesh(xyz, conn, order=order)
+    b = mg.MatrixBuilder(mesh)
+    dofs = mesh.elem_dofs()
+    rp, ci = b.pattern()
+    nb = dofs.shape[1]
+    for prec, quad in REF_QUAD.items():
+        ref_mats = d[f"m_{op}_{order}_{prec}"]
+        # the CSR matrix the reference's buildEpetraCrs makes of these element blocks
+        ref = np.zeros(b.nnz)
+        for e in range(len(conn)):
+            for i in range(nb):
+                for j in range(nb):
+                    r, col = dofs[e, j], dofs[e, i]
+                    k = rp[r] + np.searchsorted(ci[rp[r]:rp[r + 1]], col)
+                    ref[k] += ref_mats[e, i, j]
+        v64 = b.assemble(op, coeff=kappa, c=c, quad=quad, prec="f64").cpu().numpy()
+        assert row_scaled_err(rp, ref, v64) <= F64_TOL, (prec, row_scaled_err(rp, ref, v64))
+        v32 = b.assemble(op, coeff=kappa, c=c, quad=quad, prec="f32").cpu().numpy()
+        assert row_scaled_err(rp, ref, v32) <= (F32_TOL if order == 1 else 2 * F32_TOL), prec
+
+
+def test_adjoint_against_reference_code():
+    """dJ/dkappa_e = -lambda_e^T Khat_e u_e with Khat_e the reference's kappa-free
+    stiffness (opEL3dF with c = 1), P1 and P2, the 4-point card."""
+    d, xyz, conn = _ref_disjoint()
+    assert float(d["c"]) == 1.0
+    rng = np.random.default_rng(3)
+    for order in (1, 2):
+        mesh = mg.Mesh(xyz, conn, order=order)
+        b = mg.MatrixBuilder(mesh)
+        dofs = mesh.elem_dofs()
+        u, lam = rng.uniform(-1, 1, b.ndof), rng.uniform(-1, 1, b.ndof)
+        khat = d[f"m_stiff_const_{order}_2"]  # [field i, test j]
+        g_ref = np.array([-(lam[dofs[e]] @ khat[e].T @ u[dofs[e]]) for e in range(len(conn))])
+        g = b.adjoint_grad(torch.from_numpy(u).cuda(), torch.from_numpy(lam).cuda(), quad=4).cpu().numpy()
+        assert np.max(np.abs(g - g_ref)) <= 1e-12 * np.abs(g_ref).max(), order
+
+
+@pytest.mark.parametrize("jitter,seed", [(0.3, 11), (0.35, 12)])
+def test_strongly_jittered_mesh_all_entries(jitter, seed):
+    """Elements whose vertex-0 gradient is small against the others (|C_max| / |C_0|
+    up to ~60 here): the kernel takes that gradient from the coordinates instead of
+    the zero row sums, which would cancel; every entry against the oracle."""
+    m, kappa = _case(32, jitter, seed, True, 1.5)
+    b = mg.MatrixBuilder(mg.Mesh(m.xyz, m.conn, order=1))
+    _, rp, ci, ref = orc.full_operator("stiff_kappa", 1, 4, m.xyz, m.conn, coeff=kappa)
+    v64 = b.assemble("stiff_kappa", coeff=kappa, quad=4, prec="f64").cpu().numpy()
+    b.status()
+    assert row_scaled_err(rp, ref, v64) <= F64_TOL
+    v32 = b.assemble("stiff_kappa", coeff=kappa, quad=4, prec="f32").cpu().numpy()
+    assert row_scaled_err(rp, ref, v32) <= F32_TOL
+
+
+@pytest.mark.parametrize("jitter,seed", [(0.25, 13), (0.3, 14)])
+def test_strongly_jittered_mesh_p2(jitter, seed):
+    """P2 on jittered Kuhn cubes: every entry against the oracle (15-point card on
+    both sides)."""
+    m, kappa = _case(12, jitter, seed, True, 1.0)
+    b = mg.MatrixBuilder(mg.Mesh(m.xyz, m.conn, order=2))
+    _, rp, ci, ref = orc.full_operator("stiff_kappa", 2, 15, m.xyz, m.conn, coeff=kappa)
+    v64 = b.assemble("stiff_kappa", coeff=kappa, quad=15, prec="f64").cpu().numpy()
+    b.status()
+    e64 = row_scaled_err(rp, ref, v64)
+    v32 = b.assemble("stiff_kappa", coeff=kappa, quad=15, prec="f32").cpu().numpy()
+    e32 = row_scaled_err(rp, ref, v32)
+    print(f"P2 12^3 jitter {jitter}: FP64 {e64:.2e}, FP32 {e32:.2e}")
+    assert e64 <= F64_TOL and e32 <= 2 * F32_TOL

@@ -147,3 +147,39 @@ def test_cg_oracle_converges():
     assert rc == 0 and rr <= 1e-12
     r = b - orc.spmv(rp, ci, K, x)
     assert np.linalg.norm(r) <= 1e-11 * np.linalg.norm(b)
+
+
+# ---------------------------------------------------------------------------
+# The oracle against the reference's own code: tests/golden/ref_elements.npz
+# holds quadrature cards and element matrices computed by the reference's
+# compiled sources (intStaticCards, polyCards via the feStatic iterators,
+# geoMapInterface, tensor3d), driven through the opEL3dA/F/G/M integrands and the
+# integratorOEL3d_STD loop (oracle/ref, made by tests/golden/make_ref_elements.py).
+REF_OPS = ["stiff_kappa", "stiff_const", "mass", "mass_coeff"]
+QUAD_OF_PREC = {1: 1, 2: 4, 3: 15, 4: 64}
+
+
+def _ref_fixture():
+    return np.load(os.path.join(GOLDEN, "ref_elements.npz"))
+
+
+@pytest.mark.parametrize("prec", [1, 2, 3, 4])
+def test_quadrature_cards_equal_reference_code(prec):
+    d = _ref_fixture()
+    Y, W = orc.quad_rule(QUAD_OF_PREC[prec])
+    assert np.array_equal(Y, d[f"card{prec}_Y"]) and np.array_equal(W, d[f"card{prec}_W"])
+
+
+@pytest.mark.parametrize("op", REF_OPS)
+@pytest.mark.parametrize("order", [1, 2])
+def test_element_matrices_equal_reference_code(op, order):
+    """Bit for bit: the oracle restates the reference's arithmetic in the same
+    order (built without FP contraction, as the reference code was)."""
+    d = _ref_fixture()
+    xyz, kappa, c = d["xyz"], d["kappa"], float(d["c"])
+    nodes = np.arange(4, dtype=np.int32)
+    for prec in (1, 2, 3, 4):
+        ref = d[f"m_{op}_{order}_{prec}"]
+        for t in range(len(xyz)):
+            got = orc.local_matrix(op, order, QUAD_OF_PREC[prec], np.ascontiguousarray(xyz[t]), nodes, kappa[t], c)
+            assert np.array_equal(got, ref[t]), (op, order, prec, t, np.max(np.abs(got - ref[t])))
