@@ -747,7 +747,9 @@ def main():
         extras["adjoint_grad"] = _rec(peak, adj_bytes(E, N, ndof), tg, E)
         extras["load_vector"] = _rec(peak, rhs_bytes(E, N, ndof), tb, E)
         extras["schedule"] = {"blocks": sched.nblocks, "items": sched.n_items, "recompute_factor": sched.n_items / E,
-                              "entries": sched.n_entries, "padding_factor": sched.n_entries / max(1, sched.n_contrib)}
+                              "words": sched.n_entries,
+                              "word_bytes_per_contribution": 4 * sched.n_entries / max(1, sched.n_contrib),
+                              "padding_factor": 2 * sched.n_entries / max(1, sched.n_contrib)}  # P1: 4 per 2 words
         extras["setup"] = setup
         if graph is not None:
             extras["step_graph_ms"] = ms_step

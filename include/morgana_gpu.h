@@ -191,7 +191,7 @@ typedef struct {
   int32_t host_copy;   /* 1 while mg_plan_export_schedule is available */
   int64_t n_items;     /* element recomputations summed over blocks */
   int64_t n_chunks;
-  int64_t n_entries;   /* contribution-list entries, padding included */
+  int64_t n_entries;   /* contribution-list 32-bit words (two per 8-byte piece), padding included */
   int64_t n_contrib;   /* element-matrix entries scattered (= n_elements * nb^2) */
   int64_t n_item_slots;      /* length of the exported item array (padding included) */
   int64_t max_chunk_entries; /* words of the largest chunk (its shared-memory staging buffer) */
@@ -203,12 +203,16 @@ typedef struct {
 mg_status mg_plan_schedule_info(const mg_plan* plan, mg_schedule_info* info);
 
 /* h_blocks: nblocks x 8 int32 {item_begin, item_count, chunk_begin, nchunks,
-   row_begin, row_count, acc_used, 0}; h_items: element ids (each block's list
-   padded to a multiple of 4 with -1); h_chunk_ptr: n_chunks x (warps + 1)
-   offsets into h_entries; h_entries: n_entries words source | slot << 13 |
-   end-of-segment << 31, the source indexing the chunk's symmetric element
-   matrices stored entry-major (u * chunk_items + item, u the upper-triangle
-   index of (field, test)); h_rows / h_row_acc: ndof owned rows per block and
+   row_begin, row_count, acc_used, word_begin / 32}; h_items: element ids (each
+   block's list padded to a multiple of 4 with -1); h_chunk_ptr: n_chunks x
+   (warps + 1) offsets into h_entries; h_entries: n_entries 32-bit words, read
+   in pairs as 8-byte pieces laid out [piece][lane] per warp, each piece the
+   contributions of one accumulator slot: P1 four 12-bit sources at bits 0, 12,
+   24, 36 and the slot (14 bits) at bit 48; P2 two words source (13 bits) |
+   slot << 13.  A source indexes the chunk's symmetric element matrices stored
+   entry-major (u * chunk_items + item, u the upper-triangle index of (field,
+   test)); nu * chunk_items is the zero source of padding, and padding pieces
+   target the slot acc_max.  h_rows / h_row_acc: ndof owned rows per block and
    their accumulator base. */
 mg_status mg_plan_export_schedule(const mg_plan* plan, int32_t* h_blocks, int32_t* h_items,
                                   int64_t* h_chunk_ptr, uint32_t* h_entries, int32_t* h_rows,

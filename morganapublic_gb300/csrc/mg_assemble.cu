@@ -184,25 +184,28 @@ struct GeoPtrs {
 };
 
 // The coordinates an element needs.  The assembly kernel reads them from the
-// chunk record staged in shared memory (local vertex indices): coordinates
-// relative to the chunk's first vertex, split r = hi + lo (two floats).  The
-// adjoint kernel reads the mesh's absolute coordinates (x = hi + mid + lo) from
-// global memory.
-template <int MODE> struct Fetch;
-template <> struct Fetch<kF32> {
-  float4 a[4];  // hi.xyz, lo.x
-  float2 b[4];  // lo.y, lo.z
+// chunk record staged in shared memory: per distinct vertex of the chunk, its
+// coordinates relative to the chunk's first vertex split exactly into three
+// floats r = hi + mid + lo, in the layout of the mesh's absolute records
+// (a = hi.xyz mid.x, b = mid.yz lo.xy, c = lo.z).  An edge vector r_k - r_0 is
+// then the exact difference of the mesh's FP64 coordinates -- the reference's J,
+// which geoMapInterface::getGradient forms as x_k - x_0 -- up to the rounding of
+// the arithmetic that forms it.  (A two-float split kept 2^-48 of the chunk's
+// extent, several edges; a cancelling cofactor amplified that past 1e-12 on
+// strongly jittered 128^3 meshes.)  The adjoint kernel reads the mesh's absolute
+// records from global memory.
+struct StagedVerts {
+  const float4* a;  // hi.xyz, mid.x
+  const float4* b;  // mid.y, mid.z, lo.x, lo.y
+  const float* c;   // lo.z
 };
-template <> struct Fetch<kDW> {
-  float4 a[4];
-  float2 b[4];
-};
-template <> struct Fetch<kF64> {
-  double4_32a x[4];
-};
-struct FetchAbs {  // absolute coordinates (adjoint kernel)
+struct FetchAbs {  // four vertices in the three-float form (staged or absolute)
   float4 a[4], b[4];
   float lz[4];
+};
+template <int MODE> struct Fetch;
+template <> struct Fetch<kF64> {
+  double4_32a x[4];
 };
 
 __device__ __forceinline__ void fetch(const GeoPtrs& g, int4 n, FetchAbs& F)
@@ -216,37 +219,29 @@ __device__ __forceinline__ void fetch(const GeoPtrs& g, int4 n, FetchAbs& F)
   }
 }
 
-// from a staged chunk record: va = (hi.xyz, lo.x), vb = (lo.y, lo.z) per vertex
-template <int MODE>
-__device__ __forceinline__ void fetch_staged(const float4* va, const float2* vb, ushort4 lc, Fetch<MODE>& F)
+// the four vertices of an item from a staged record (LO: the third floats too;
+// the FP32 arithmetic needs hi + mid only)
+template <bool LO>
+__device__ __forceinline__ void fetch_staged(const StagedVerts& v, ushort4 lc, FetchAbs& F)
 {
   const int id[4] = {lc.x, lc.y, lc.z, lc.w};
 #pragma unroll
   for (int s = 0; s < 4; ++s) {
-    F.a[s] = va[id[s]];
-    F.b[s] = vb[id[s]];
-  }
-}
-// hi + lo summed in FP64 (to 2^-48 of the relative coordinate)
-template <>
-__device__ __forceinline__ void fetch_staged<kF64>(const float4* va, const float2* vb, ushort4 lc, Fetch<kF64>& F)
-{
-  const int id[4] = {lc.x, lc.y, lc.z, lc.w};
-#pragma unroll
-  for (int s = 0; s < 4; ++s) {
-    const float4 u = va[id[s]];
-    const float2 v = vb[id[s]];
-    F.x[s] = make_double4_32a((double)u.x + (double)u.w, (double)u.y + (double)v.x, (double)u.z + (double)v.y, 0.0);
+    F.a[s] = v.a[id[s]];
+    F.b[s] = v.b[id[s]];
+    F.lz[s] = LO ? v.c[id[s]] : 0.0f;
   }
 }
 
-// components of a staged vertex: hi, lo
-__device__ __forceinline__ float vhi(const float4& a, int r) { return r == 0 ? a.x : (r == 1 ? a.y : a.z); }
-__device__ __forceinline__ float vlo(const float4& a, const float2& b, int r) { return r == 0 ? a.w : (r == 1 ? b.x : b.y); }
-// components of an absolute mesh record: hi, mid, lo
+// components of a three-float record: hi, mid, lo
 __device__ __forceinline__ float rec_hi(const float4& a, int r) { return r == 0 ? a.x : (r == 1 ? a.y : a.z); }
 __device__ __forceinline__ float rec_mid(const float4& a, const float4& b, int r) { return r == 0 ? a.w : (r == 1 ? b.x : b.y); }
 __device__ __forceinline__ float rec_lo(const float4& b, float lz, int r) { return r == 0 ? b.z : (r == 1 ? b.w : lz); }
+// the coordinate as a double: hi + mid + lo, every partial sum exact
+__device__ __forceinline__ double rec_x(const float4& a, const float4& b, float lz, int r)
+{
+  return ((double)rec_hi(a, r) + (double)rec_mid(a, b, r)) + (double)rec_lo(b, lz, r);
+}
 
 __device__ __forceinline__ double comp(const double4_32a& v, int r) { return r == 0 ? v.x : (r == 1 ? v.y : v.z); }
 
@@ -279,35 +274,43 @@ __device__ __forceinline__ float hi_of<ff>(const ff& v) { return v.hi; }
 template <>
 __device__ __forceinline__ float hi_of<double>(const double& v) { return (float)v; }
 
-// P1 stiffness needs the gradient of every vertex: the cofactor columns C_1..C_3
-// of J (gradients of vertices 1..3 times det) come from the edge vectors at
-// vertex 0, and vertex 0's follows from C_0 = -(C_1 + C_2 + C_3) -- the zero row
-// sums of the element matrix.  When |C_0| is small against the largest column
-// that sum cancels: its error is eps |C_max|, and the entries of vertex 0 (whose
-// row scale is |C_0| |C_max|) carry eps |C_max|^2.  On a Kuhn cube jittered by
-// 0.25 h the ratio |C_max| / |C_0| reaches 21 (12.6 M tets), which put the
-// double-word values 2.8e-12 row-scaled from the FP64 oracle.  Elements with
-// |C_max| > 3 |C_0| (under 1 % of such a mesh) take C_0 from the coordinates,
-// (x3 - x1) x (x2 - x1), and form the entries of vertex 0 as dot products.
-constexpr float kGradRatio2 = 9.0f;
+// P1 stiffness needs the gradient of every vertex: the columns C_0..C_3 of the
+// cofactor matrix (gradients times det).  The common path takes C_1..C_3 from
+// the edge vectors at vertex 0 and C_0 = -(C_1 + C_2 + C_3) from the zero row
+// sums.  Two kinds of element take a rare path (p1_stiff_special):
+//  - |C_max| > 3 |C_0|: that sum cancels -- its error is eps |C_max|, which the
+//    entries of vertex 0 carry at a row scale of |C_0| |C_max| -- so C_0 is
+//    formed from the coordinates as (x3 - x1) x (x2 - x1), in the mode's
+//    arithmetic, and the entries of vertex 0 as dot products;
+//  - |C_max| > 8 |C_min| over all four: a cofactor is a 2x2 minor whose terms
+//    cancel by about that ratio, and the double-word (or FP32) rounding of its
+//    terms grows with it; the geometry is computed in FP64, as the reference's.
+// On a Kuhn cube jittered by 0.25 h (12.6 M tets, gradient ratios up to 21) the
+// first kind is ~1 % of the elements and the second ~0.01 %.
+enum { kP1Common = 0, kP1DirectC0 = 1, kP1Fp64 = 2 };
 
 template <typename T>
-__device__ __forceinline__ bool c0_cancels(const Cof<T>& f)
+__device__ __forceinline__ int p1_class(const Cof<T>& f)
 {
-  float n0 = 0.0f, nmax = 0.0f;
+  float n[4];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     float na = 0.0f;
 #pragma unroll
     for (int r = 0; r < 3; ++r) na = fmaf(hi_of(f.c[r][a]), hi_of(f.c[r][a]), na);
-    nmax = fmaxf(nmax, na);
+    n[a + 1] = na;
   }
+  n[0] = 0.0f;
 #pragma unroll
   for (int r = 0; r < 3; ++r) {
     const float s = hi_of(f.c[r][0]) + hi_of(f.c[r][1]) + hi_of(f.c[r][2]);
-    n0 = fmaf(s, s, n0);
+    n[0] = fmaf(s, s, n[0]);
   }
-  return nmax > kGradRatio2 * n0;
+  const float nmax = fmaxf(fmaxf(n[0], n[1]), fmaxf(n[2], n[3]));
+  const float nmin = fminf(fminf(n[0], n[1]), fminf(n[2], n[3]));
+  if (nmax > 64.0f * nmin) return kP1Fp64;
+  if (nmax > 9.0f * n[0]) return kP1DirectC0;
+  return kP1Common;
 }
 
 // |det| small against its expansion terms
@@ -319,16 +322,6 @@ __device__ __forceinline__ bool det_cancels(const T J[3][3], const Cof<T>& f)
   return t > kCancelTol * fabsf(hi_of(f.det));
 }
 
-// FP64 geometry from staged hi + lo coordinates (exact as doubles)
-__device__ __forceinline__ void geometry_fp64_staged(const float4* a, const float2* b, Cof<double>& d)
-{
-  Fetch<kF64> D;
-#pragma unroll
-  for (int s = 0; s < 4; ++s)
-    D.x[s] = make_double4_32a((double)a[s].x + (double)a[s].w, (double)a[s].y + (double)b[s].x,
-                              (double)a[s].z + (double)b[s].y, 0.0);
-  geometry(D, d);
-}
 __device__ __forceinline__ void store_geometry(const Cof<double>& d, Cof<float>& f)
 {
 #pragma unroll
@@ -345,20 +338,12 @@ __device__ __forceinline__ void store_geometry(const Cof<double>& d, Cof<ff>& f)
     for (int k = 0; k < 3; ++k) f.c[r][k] = ff_from_double_bits(d.c[r][k]);
   f.det = ff_from_double_bits(d.det);
 }
-// FP32: edge vectors (hi_k - hi_0) + (lo_k - lo_0) of the chunk-relative
-// coordinates, accurate to a few float ulps of the edge itself.
-// Returns whether the element needs the FP64 geometry (det_cancels).
-__device__ __forceinline__ bool geometry(const Fetch<kF32>& F, Cof<float>& f)
-{
-  float J[3][3];
-#pragma unroll
-  for (int r = 0; r < 3; ++r)
-#pragma unroll
-    for (int k = 0; k < 3; ++k)
-      J[r][k] = (vhi(F.a[k + 1], r) - vhi(F.a[0], r)) + (vlo(F.a[k + 1], F.b[k + 1], r) - vlo(F.a[0], F.b[0], r));
-  cofactors<float>(J, f);
-  return det_cancels<float>(J, f);
-}
+__device__ __forceinline__ void store_geometry(const Cof<double>& d, Cof<double>& f) { f = d; }
+
+template <typename T> __device__ __forceinline__ T from_double(double x);
+template <> __device__ __forceinline__ float from_double<float>(double x) { return (float)x; }
+template <> __device__ __forceinline__ ff from_double<ff>(double x) { return ff_from_double_bits(x); }
+template <> __device__ __forceinline__ double from_double<double>(double x) { return x; }
 
 // Double-word cofactors and determinant from double-word edge vectors.
 __device__ __forceinline__ void dw_cofactors(const ff J[3][3], Cof<ff>& f)
@@ -375,30 +360,9 @@ __device__ __forceinline__ void dw_cofactors(const ff J[3][3], Cof<ff>& f)
   f.det = ff_dot3(J[0], f.c[0]);
 }
 
-// Double-word, chunk-relative coordinates r = hi + lo (|r - hi - lo| <= 2^-48 |r|,
-// |r| a few edge lengths): r_k - r_0 = (hi_k - hi_0) + (lo_k - lo_0), the
-// leading difference error-free (two_sum) -- relative error ~2^-46 of the edge.
-__device__ __forceinline__ ff dw_diff2(float hb, float ha, float lb, float la)
-{
-  const ff s1 = two_sum(hb, -ha);
-  return two_sum(s1.hi, __fadd_rn(s1.lo, __fsub_rn(lb, la)));
-}
-
-__device__ __forceinline__ bool geometry(const Fetch<kDW>& F, Cof<ff>& f)
-{
-  ff J[3][3];
-#pragma unroll
-  for (int r = 0; r < 3; ++r)
-#pragma unroll
-    for (int k = 0; k < 3; ++k)
-      J[r][k] = dw_diff2(vhi(F.a[k + 1], r), vhi(F.a[0], r), vlo(F.a[k + 1], F.b[k + 1], r), vlo(F.a[0], F.b[0], r));
-  dw_cofactors(J, f);
-  return det_cancels<ff>(J, f);
-}
-
-// Double-word, absolute coordinates x = hi + mid + lo exactly (the adjoint
-// kernel):  x_k - x_0 = (hi_k - hi_0) + (mid_k - mid_0) + (lo_k - lo_0) with
-// the two leading differences error-free -- relative error ~2^-47 of the edge.
+// Double-word difference of two three-float numbers x = hi + mid + lo:
+// x_b - x_a = (hi_b - hi_a) + (mid_b - mid_a) + (lo_b - lo_a) with the two
+// leading differences error-free -- relative error ~2^-47 of the difference.
 __device__ __forceinline__ ff dw_diff3(float hb, float ha, float mb, float ma, float lb, float la)
 {
   const ff s1 = two_sum(hb, -ha);
@@ -406,6 +370,103 @@ __device__ __forceinline__ ff dw_diff3(float hb, float ha, float mb, float ma, f
   const ff s = two_sum(s1.hi, s2.hi);
   const float t = __fadd_rn(__fadd_rn(__fadd_rn(s.lo, s1.lo), s2.lo), __fsub_rn(lb, la));
   return two_sum(s.hi, t);
+}
+// component r of the edge from vertex j to vertex k, double-word and FP32
+__device__ __forceinline__ ff dw_edge(const FetchAbs& F, int k, int j, int r)
+{
+  return dw_diff3(rec_hi(F.a[k], r), rec_hi(F.a[j], r), rec_mid(F.a[k], F.b[k], r), rec_mid(F.a[j], F.b[j], r),
+                  rec_lo(F.b[k], F.lz[k], r), rec_lo(F.b[j], F.lz[j], r));
+}
+__device__ __forceinline__ float f32_edge(const FetchAbs& F, int k, int j, int r)
+{
+  return (rec_hi(F.a[k], r) - rec_hi(F.a[j], r)) + (rec_mid(F.a[k], F.b[k], r) - rec_mid(F.a[j], F.b[j], r));
+}
+
+// FP64 geometry from three-float coordinates (exact as doubles)
+__device__ __forceinline__ void geometry_fp64(const FetchAbs& F, Cof<double>& d)
+{
+  Fetch<kF64> D;
+#pragma unroll
+  for (int s = 0; s < 4; ++s)
+    D.x[s] = make_double4_32a(rec_x(F.a[s], F.b[s], F.lz[s], 0), rec_x(F.a[s], F.b[s], F.lz[s], 1),
+                              rec_x(F.a[s], F.b[s], F.lz[s], 2), 0.0);
+  geometry(D, d);
+}
+
+// The common path: geometry of a staged item in the mode's arithmetic, reading
+// vertex 0 and then one vertex per edge column (fewer live registers than all
+// four at once); returns whether the element needs the FP64 geometry
+// (det_cancels).  FP32: edge vectors (hi_k - hi_0) + (mid_k - mid_0), to a float
+// ulp of the edge; double-word: dw_diff3 of the three floats.
+template <int MODE>
+__device__ __forceinline__ bool geometry_staged_lazy(const StagedVerts& v, ushort4 lc, Cof<typename Arith<MODE>::T>& f)
+{
+  using T = typename Arith<MODE>::T;
+  constexpr bool LO = MODE != kF32;
+  FetchAbs F;  // slots 0 (vertex 0) and 1 (the current column's vertex) only
+  F.a[0] = v.a[lc.x];
+  F.b[0] = v.b[lc.x];
+  F.lz[0] = LO ? v.c[lc.x] : 0.0f;
+  T J[3][3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const int id = k == 0 ? lc.y : (k == 1 ? lc.z : lc.w);
+    F.a[1] = v.a[id];
+    F.b[1] = v.b[id];
+    F.lz[1] = LO ? v.c[id] : 0.0f;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      if constexpr (MODE == kF32) J[r][k] = f32_edge(F, 1, 0, r);
+      else if constexpr (MODE == kDW) J[r][k] = dw_edge(F, 1, 0, r);
+      else J[r][k] = rec_x(F.a[1], F.b[1], F.lz[1], r) - rec_x(F.a[0], F.b[0], F.lz[0], r);
+    }
+  }
+  if constexpr (MODE == kDW) dw_cofactors(J, f);
+  else cofactors<T>(J, f);
+  if constexpr (MODE == kF64) return false;
+  else return det_cancels<T>(J, f);
+}
+
+// Near-degenerate elements: the FP64 geometry of a staged item, out of line and
+// returned by value (no register of the caller is passed by address).
+template <typename T>
+static __device__ __noinline__ Cof<T> staged_geometry_fp64(StagedVerts v, ushort4 lc)
+{
+  FetchAbs D;
+  fetch_staged<true>(v, lc, D);
+  Cof<double> g;
+  geometry_fp64(D, g);
+  Cof<T> f;
+  store_geometry(g, f);
+  return f;
+}
+
+// Geometry of a staged item in the mode's arithmetic from four fetched vertices
+// (the rare paths); returns whether the element needs the FP64 geometry.
+__device__ __forceinline__ bool geometry_staged(const FetchAbs& F, Cof<float>& f)
+{
+  float J[3][3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) J[r][k] = f32_edge(F, k + 1, 0, r);
+  cofactors<float>(J, f);
+  return det_cancels<float>(J, f);
+}
+__device__ __forceinline__ bool geometry_staged(const FetchAbs& F, Cof<ff>& f)
+{
+  ff J[3][3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) J[r][k] = dw_edge(F, k + 1, 0, r);
+  dw_cofactors(J, f);
+  return det_cancels<ff>(J, f);
+}
+__device__ __forceinline__ bool geometry_staged(const FetchAbs& F, Cof<double>& f)
+{
+  geometry_fp64(F, f);
+  return false;
 }
 
 // near-degenerate elements: FP64 geometry from the mesh's FP64 coordinates
@@ -490,46 +551,41 @@ __device__ __forceinline__ void p1_stiff_unique<ff>(const Cof<ff>& f, ff s, ff K
   K[0] = -(K[1] + K[2] + K[3]);
 }
 
-// C_0 = (x3 - x1) x (x2 - x1) (= -(C_1 + C_2 + C_3)) from the staged vertices,
-// accurate to its own magnitude: the edge vectors of the face opposite vertex 0
-// as differences of the chunk-relative coordinates, then their cross product.
-__device__ __forceinline__ void staged_c0(const float4* va, const float2* vb, ushort4 lc, float C0[3])
+// C_0 = (x3 - x1) x (x2 - x1) (= -(C_1 + C_2 + C_3)) from the staged vertices in
+// the mode's arithmetic: the edges of the face opposite vertex 0, then their
+// cross product, accurate to its own magnitude.
+__device__ __forceinline__ void staged_c0(const FetchAbs& F, float C0[3])
 {
-  const float4 a1 = va[lc.y], a2 = va[lc.z], a3 = va[lc.w];
-  const float2 b1 = vb[lc.y], b2 = vb[lc.z], b3 = vb[lc.w];
   float f2[3], f3[3];
 #pragma unroll
   for (int r = 0; r < 3; ++r) {
-    f2[r] = (vhi(a2, r) - vhi(a1, r)) + (vlo(a2, b2, r) - vlo(a1, b1, r));
-    f3[r] = (vhi(a3, r) - vhi(a1, r)) + (vlo(a3, b3, r) - vlo(a1, b1, r));
+    f2[r] = f32_edge(F, 2, 1, r);
+    f3[r] = f32_edge(F, 3, 1, r);
   }
   C0[0] = f3[1] * f2[2] - f3[2] * f2[1];
   C0[1] = f3[2] * f2[0] - f3[0] * f2[2];
   C0[2] = f3[0] * f2[1] - f3[1] * f2[0];
 }
-__device__ __forceinline__ void staged_c0(const float4* va, const float2* vb, ushort4 lc, ff C0[3])
+__device__ __forceinline__ void staged_c0(const FetchAbs& F, ff C0[3])
 {
-  const float4 a1 = va[lc.y], a2 = va[lc.z], a3 = va[lc.w];
-  const float2 b1 = vb[lc.y], b2 = vb[lc.z], b3 = vb[lc.w];
   ff f2[3], f3[3];
 #pragma unroll
   for (int r = 0; r < 3; ++r) {
-    f2[r] = dw_diff2(vhi(a2, r), vhi(a1, r), vlo(a2, b2, r), vlo(a1, b1, r));
-    f3[r] = dw_diff2(vhi(a3, r), vhi(a1, r), vlo(a3, b3, r), vlo(a1, b1, r));
+    f2[r] = dw_edge(F, 2, 1, r);
+    f3[r] = dw_edge(F, 3, 1, r);
   }
   C0[0] = ff_cross(f3[1], f2[2], f3[2], f2[1]);
   C0[1] = ff_cross(f3[2], f2[0], f3[0], f2[2]);
   C0[2] = ff_cross(f3[0], f2[1], f3[1], f2[0]);
 }
-__device__ __forceinline__ void staged_c0(const float4* va, const float2* vb, ushort4 lc, double C0[3])
+__device__ __forceinline__ void staged_c0(const FetchAbs& F, double C0[3])
 {
-  Fetch<kF64> D;
-  fetch_staged<kF64>(va, vb, lc, D);
   double f2[3], f3[3];
 #pragma unroll
   for (int r = 0; r < 3; ++r) {
-    f2[r] = comp(D.x[2], r) - comp(D.x[1], r);
-    f3[r] = comp(D.x[3], r) - comp(D.x[1], r);
+    const double x1 = rec_x(F.a[1], F.b[1], F.lz[1], r);
+    f2[r] = rec_x(F.a[2], F.b[2], F.lz[2], r) - x1;
+    f3[r] = rec_x(F.a[3], F.b[3], F.lz[3], r) - x1;
   }
   C0[0] = f3[1] * f2[2] - f3[2] * f2[1];
   C0[1] = f3[2] * f2[0] - f3[0] * f2[2];
@@ -578,15 +634,46 @@ __device__ __forceinline__ void p1_stiff_direct<ff>(const Cof<ff>& f, const ff C
   K[9] = ff_mul(s, ff_dot3(col[2], col[2]));
 }
 
-// The rare path above, out of line (like the FP64 geometry fallback), so that
-// its registers do not weigh on every other element.
-template <typename T>
-static __device__ __noinline__ void p1_stiff_direct_staged(const float4* va, const float2* vb, ushort4 lc,
-                                                           const Cof<T>& f, T s, T K[10])
+// The rare path of the P1 stiffness (p1_class != kP1Common), out of line: it
+// re-reads the item's vertices from the staged record, recomputes the element
+// and writes its 10 unique entries (out[u * stride]) itself, so that no register
+// of the common path is passed by address.  coef is the element's coefficient
+// and wsum the card's weight sum, as doubles.  Records an out-of-range
+// double-word scale in *flags, as the common path does.
+template <int MODE>
+static __device__ __noinline__ void p1_stiff_special(StagedVerts v, ushort4 lc, int cls, double coef, double wsum,
+                                                     typename Arith<MODE>::T* out, int stride, uint32_t* flags)
 {
-  T C0[3];
-  staged_c0(va, vb, lc, C0);
+  using A = Arith<MODE>;
+  using T = typename A::T;
+  FetchAbs F;
+  fetch_staged<true>(v, lc, F);
+  Cof<T> f;
+  T C0[3], s;
+  if (MODE == kF64 || cls == kP1Fp64) {
+    Cof<double> d;
+    geometry_fp64(F, d);
+    double c0[3];
+    staged_c0(F, c0);
+    store_geometry(d, f);
+#pragma unroll
+    for (int r = 0; r < 3; ++r) C0[r] = from_double<T>(c0[r]);
+    s = from_double<T>(coef * wsum / d.det);
+  } else {
+    if (geometry_staged(F, f)) {  // a cancelling determinant as well
+      Cof<double> d;
+      geometry_fp64(F, d);
+      store_geometry(d, f);
+    }
+    staged_c0(F, C0);
+    s = A::from(coef) * A::from(wsum) / f.det;
+  }
+  T K[10];
   p1_stiff_direct<T>(f, C0, s, K);
+  if constexpr (MODE == kDW)
+    if (!dw_scale_ok(s) || !dw_scale_ok(K[4])) atomicOr(flags, 2u);
+#pragma unroll
+  for (int u = 0; u < 10; ++u) out[u * stride] = K[u];
 }
 
 // The six scaled metric coefficients s (C_a . C_b), ab = 00,11,22,01,02,12.
@@ -656,9 +743,9 @@ constexpr size_t align16(size_t n) { return (n + 15) / 16 * 16; }
 enum {
   kBarRecFull = 0,                        // [kRecStages] chunk-record stages
   kBarRecEmpty = kBarRecFull + kRecStages,  // [kRecStages]
-  kBarEntFull = kBarRecEmpty + kRecStages,  // [2] contribution-word buffers (one per group)
-  kBarEntEmpty = kBarEntFull + 2,           // [2]
-  kBarMetaFull = kBarEntEmpty + 2,          // row metadata of a block
+  kBarEntFull = kBarRecEmpty + kRecStages,  // [kWordStages] contribution-word stages
+  kBarEntEmpty = kBarEntFull + kWordStages,  // [kWordStages]
+  kBarMetaFull = kBarEntEmpty + kWordStages, // row metadata of a block
   kBarMetaEmpty = kBarMetaFull + 1,
   kBarBlkFull = kBarMetaEmpty + 1,          // [2] block descriptors
   kBarBlkEmpty = kBarBlkFull + 2,           // [2]
@@ -702,7 +789,7 @@ struct AsmLayout {
   __host__ __device__ static size_t off_words(int stage_cap) { return off_stage + kRecStages * stage_bytes(stage_cap); }
   __host__ __device__ static size_t total(int ent_cap, int stage_cap)
   {
-    return off_words(stage_cap) + 2 * words_bytes(ent_cap);
+    return off_words(stage_cap) + kWordStages * words_bytes(ent_cap);
   }
 };
 
@@ -765,7 +852,7 @@ __device__ __forceinline__ bool group_sync_or(int g, bool pred)
 // the producer stops issuing and lets its copies in flight land, and the CTA
 // records the failure.
 template <int ORDER, int MODE>
-__global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
+__global__ void __maxnreg__(112) k_assemble(AsmArgs a)
 {
   using A = Arith<MODE>;
   using T = typename A::T;
@@ -780,7 +867,7 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + L::off_bars);
   unsigned char* stage = smem + L::off_stage;  // [NS][sbytes]
   const int sbytes = (int)L::stage_bytes(a.stage_cap);
-  uint32_t* sent = reinterpret_cast<uint32_t*>(smem + L::off_words(a.stage_cap));  // [2][went]
+  uint32_t* sent = reinterpret_cast<uint32_t*>(smem + L::off_words(a.stage_cap));  // [kWordStages][went]
   const int went = (int)(L::words_bytes(a.ent_cap) / 4);
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -804,8 +891,14 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
   if (warp == kConsumers / 32) {
     // ------------------------------------------------------------ producer
     if (lane == 0) {
-      int last_rec[NS], last_ent[2] = {-1, -1}, last_meta = -1;
+      constexpr int NW = kWordStages;
+      // record stages are refilled kRefillLag chunks behind the word copies, so
+      // that the producer does not wait for the consumers' phase 1 of the chunk
+      // whose words it has just issued before it moves on to the next chunk
+      constexpr int kRefillLag = NS - 1;
+      int last_rec[NS], last_ent[NW], last_meta = -1;
       for (int s = 0; s < NS; ++s) last_rec[s] = -1;
+      for (int s = 0; s < NW; ++s) last_ent[s] = -1;
       auto wait = [&](int k, int parity) {
         if (!failed && !mbar_wait(&bars[k], (uint32_t)parity)) failed = true;
         return !failed;
@@ -839,21 +932,25 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
           const int qq = q + c;
           if (!wait(kBarRecFull + qq % NS, (qq / NS) & 1)) break;
           const ChunkDesc* cd = desc_of(qq);
-          if (qq >= 2 && !wait(kBarEntEmpty + (qq & 1), ((qq >> 1) - 1) & 1)) break;
+          if (qq >= NW && !wait(kBarEntEmpty + qq % NW, (qq / NW - 1) & 1)) break;
           const uint32_t bytes = (uint32_t)cd->warp_off[kWarps] * 4u;
           fence_proxy_async();
-          mbar_expect_tx(&bars[kBarEntFull + (qq & 1)], bytes);
-          if (bytes) bulk_g2s(sent + (qq & 1) * went, a.entries + cd->word_begin, bytes, &bars[kBarEntFull + (qq & 1)]);
-          last_ent[qq & 1] = qq;
-          // record c + NS goes into record c's stage once the consumers release
-          // it; its place is in record c, which nothing has overwritten yet
-          if (c + NS < n) {
-            if (!wait(kBarRecEmpty + qq % NS, (qq / NS) & 1)) break;
-            const int off16 = cd->next_off16, nb = cd->next_bytes;
+          mbar_expect_tx(&bars[kBarEntFull + qq % NW], bytes);
+          if (bytes) bulk_g2s(sent + (qq % NW) * went, a.entries + cd->word_begin, bytes, &bars[kBarEntFull + qq % NW]);
+          last_ent[qq % NW] = qq;
+          // record cr + NS goes into record cr's stage (cr = c - kRefillLag) once
+          // the consumers release it; its place is in record cr, which nothing has
+          // overwritten yet.  Every cr < n - NS comes up, as kRefillLag < NS.
+          const int cr = c - kRefillLag;
+          if (cr >= 0 && cr + NS < n) {
+            const int qr = q + cr;
+            if (!wait(kBarRecEmpty + qr % NS, (qr / NS) & 1)) break;
+            const ChunkDesc* crd = desc_of(qr);
+            const int off16 = crd->next_off16, nb = crd->next_bytes;
             fence_proxy_async();
-            mbar_expect_tx(&bars[kBarRecFull + qq % NS], (uint32_t)nb);
-            bulk_g2s(stage_of(qq), a.chunk_data + (int64_t)off16 * 16, (uint32_t)nb, &bars[kBarRecFull + qq % NS]);
-            last_rec[qq % NS] = qq + NS;
+            mbar_expect_tx(&bars[kBarRecFull + qr % NS], (uint32_t)nb);
+            bulk_g2s(stage_of(qr), a.chunk_data + (int64_t)off16 * 16, (uint32_t)nb, &bars[kBarRecFull + qr % NS]);
+            last_rec[qr % NS] = qr + NS;
           }
         }
         if (failed) break;
@@ -871,8 +968,8 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
         // let the copies in flight land before the CTA's shared memory goes away
         for (int s = 0; s < NS; ++s)
           if (last_rec[s] >= 0) mbar_wait(&bars[kBarRecFull + s], (uint32_t)((last_rec[s] / NS) & 1));
-        for (int s = 0; s < 2; ++s)
-          if (last_ent[s] >= 0) mbar_wait(&bars[kBarEntFull + s], (uint32_t)((last_ent[s] >> 1) & 1));
+        for (int s = 0; s < NW; ++s)
+          if (last_ent[s] >= 0) mbar_wait(&bars[kBarEntFull + s], (uint32_t)((last_ent[s] / NW) & 1));
         if (last_meta >= 0) mbar_wait(&bars[kBarMetaFull], (uint32_t)(last_meta & 1));
       }
     }
@@ -910,38 +1007,41 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
           w_beg = desc_of(qq)->warp_off[gwarp];
           w_end = desc_of(qq)->warp_off[gwarp + 1];
         }
-        // geometry and coefficient of item `it` of chunk c (from the staged record)
-        auto item_geometry = [&](int it, Cof<T>& f, T& coef) {
+        // the staged vertices of chunk c and the local vertex indices of item `it`
+        auto staged_verts = [&]() {
           const unsigned char* rb = stage_of(qq);
           const int n4 = (min(CI, d.item_count - c * CI) + 3) & ~3, nn = desc_of(qq)->n_nodes;
+          const unsigned char* v0 = rb + sizeof(ChunkDesc) + 12 * n4;
+          return StagedVerts{reinterpret_cast<const float4*>(v0), reinterpret_cast<const float4*>(v0 + 16 * nn),
+                             reinterpret_cast<const float*>(v0 + 32 * nn)};
+        };
+        auto item_lconn = [&](int it) {
+          const unsigned char* rb = stage_of(qq);
+          const int n4 = (min(CI, d.item_count - c * CI) + 3) & ~3;
+          return reinterpret_cast<const ushort4*>(rb + sizeof(ChunkDesc) + 4 * n4)[it];
+        };
+        // geometry and coefficient of item `it` of chunk c (from the staged
+        // record).  A near-degenerate element (det_cancels) gets its geometry in
+        // FP64 here unless `defer` is set (the P1 stiffness sends it down its own
+        // rare path); returns whether it is one.
+        auto item_geometry = [&](int it, Cof<T>& f, T& coef, double& coef_d, bool defer) {
+          const unsigned char* rb = stage_of(qq);
           const int e = reinterpret_cast<const int32_t*>(rb + sizeof(ChunkDesc))[it];
-          const double coef_d = a.coeff ? __ldg(a.coeff + e) : a.cconst;  // latency covered by the geometry
-          const ushort4 lc = reinterpret_cast<const ushort4*>(rb + sizeof(ChunkDesc) + 4 * n4)[it];
-          const float4* va = reinterpret_cast<const float4*>(rb + sizeof(ChunkDesc) + 12 * n4);
-          const float2* vb = reinterpret_cast<const float2*>(rb + sizeof(ChunkDesc) + 12 * n4 + 16 * nn);
-          Fetch<MODE> F;
-          fetch_staged<MODE>(va, vb, lc, F);
-          if constexpr (MODE == kF64) {
-            geometry(F, f);
-          } else {
-            const bool need = geometry(F, f);
-            // near-degenerate elements: FP64 geometry from the staged coordinates
-            // (re-read from shared memory, so the coordinates need not stay live),
+          coef_d = a.coeff ? __ldg(a.coeff + e) : a.cconst;  // latency covered by the geometry
+          const ushort4 lc = item_lconn(it);
+          const StagedVerts sv = staged_verts();
+          const bool need = geometry_staged_lazy<MODE>(sv, lc, f);
+          if constexpr (MODE != kF64) {
             // entered only when a lane of the warp needs it
-            if (__any_sync(__activemask(), need)) {
-              if (need) {
-                Fetch<kF64> D;
-                fetch_staged<kF64>(va, vb, lc, D);
-                Cof<double> d;
-                geometry(D, d);
-                store_geometry(d, f);
-              }
+            if (!defer && __any_sync(__activemask(), need)) {
+              if (need) f = staged_geometry_fp64<T>(sv, lc);
             }
           }
           coef = A::from(coef_d);
           // NaN / Inf coefficient: recorded for mg_plan_status (checked after the
           // geometry, where the load has long landed)
           if (((__double_as_longlong(coef_d) >> 52) & 0x7ff) == 0x7ff) atomicOr(&a.counters[4], 1u);
+          return need;
         };
         // double-word range of an element's scale factors, recorded for mg_plan_status
         auto check_scale = [&](const T& x, const T& y) {
@@ -955,7 +1055,8 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
           if (!failed && c * CI + local < d.item_count) {
             Cof<T> f;
             T coef;
-            item_geometry(local, f, coef);
+            double coef_d;
+            item_geometry(local, f, coef, coef_d, false);
             if (a.stiff) {
               T gm[6];
               metric<T>(f, coef / f.det, gm);
@@ -969,33 +1070,36 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
           if (!failed && c * CI + local < d.item_count) {
             Cof<T> f;
             T coef;
-            item_geometry(local, f, coef);
+            double coef_d;
+            const bool degenerate = item_geometry(local, f, coef, coef_d, a.stiff != 0);
             T K[10];
+            bool special = false;
             if (a.stiff) {
-              const T sc = coef * wsum / f.det;
-              // vertex 0's gradient from the coordinates where C_0 = -sum C_k
-              // cancels (rare; entered only when a lane of the warp needs it)
-              const bool direct = c0_cancels<T>(f);
-              if (__any_sync(__activemask(), direct)) {
-                if (direct) {
-                  const unsigned char* rb = stage_of(qq);
-                  const int n4 = (min(CI, d.item_count - c * CI) + 3) & ~3, nn = desc_of(qq)->n_nodes;
-                  const ushort4 lc = reinterpret_cast<const ushort4*>(rb + sizeof(ChunkDesc) + 4 * n4)[local];
-                  const float4* va = reinterpret_cast<const float4*>(rb + sizeof(ChunkDesc) + 12 * n4);
-                  const float2* vb = reinterpret_cast<const float2*>(rb + sizeof(ChunkDesc) + 12 * n4 + 16 * nn);
-                  p1_stiff_direct_staged<T>(va, vb, lc, f, sc, K);
-                }
+              // the rare elements (p1_class, or a cancelling determinant) go out of
+              // line, entered only when a lane of the warp has one; that path
+              // writes its entries itself
+              const int cls = degenerate ? (int)kP1Fp64 : p1_class<T>(f);
+              special = cls != kP1Common;
+              if (__any_sync(__activemask(), special)) {
+                if (special)
+                  p1_stiff_special<MODE>(staged_verts(), item_lconn(local), cls, coef_d, a.wsum, buf + local, CI,
+                                         &a.counters[4]);
               }
-              if (!direct) p1_stiff_unique<T>(f, sc, K);
-              check_scale(sc, K[4]);
+              if (!special) {
+                const T sc = coef * wsum / f.det;
+                p1_stiff_unique<T>(f, sc, K);
+                check_scale(sc, K[4]);
+              }
             } else {
               const T sc = coef * f.det;
               check_scale(sc, sc);
 #pragma unroll
               for (int u = 0; u < 10; ++u) K[u] = sc * tab[6 * NU + u];
             }
+            if (!special) {
 #pragma unroll
-            for (int u = 0; u < 10; ++u) buf[u * CI + local] = K[u];
+              for (int u = 0; u < 10; ++u) buf[u * CI + local] = K[u];
+            }
           }
         } else {
           // P2: the first warp of the group computes each item's scale factors
@@ -1004,7 +1108,8 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
           if (!failed && gwarp == 0 && c * CI + lane < d.item_count) {
             Cof<T> f;
             T coef;
-            item_geometry(lane, f, coef);
+            double coef_d;
+            item_geometry(lane, f, coef, coef_d, false);
             if (a.stiff) {
               T gm[6];
               const T sc = coef / f.det;
@@ -1037,29 +1142,32 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
         // one slot are summed in registers and update the slot once; within a
         // chunk every slot belongs to one thread, and the token orders the
         // chunks.
-        if (!failed && !mbar_wait(&bars[kBarEntFull + (qq & 1)], (uint32_t)((qq >> 1) & 1))) failed = true;
+        if (!failed && !mbar_wait(&bars[kBarEntFull + qq % kWordStages], (uint32_t)((qq / kWordStages) & 1)))
+          failed = true;
         if (c >= 1) {
           if (!failed && !mbar_wait(&bars[kBarToken + g], (uint32_t)(ntok & 1))) failed = true;
           ++ntok;
         }
         if (!failed) {
-          constexpr int PW = piece_words(ORDER);
-          const int K = (w_end - w_beg) / (32 * PW);
-          const uint32_t* ew = sent + (qq & 1) * went + w_beg + lane * PW;
+          // 8-byte pieces, [piece][lane] per warp (layout at piece_srcs)
+          const int K = (w_end - w_beg) / 64;
+          const uint2* ew = reinterpret_cast<const uint2*>(sent + (qq % kWordStages) * went + w_beg) + lane;
 #pragma unroll 2
           for (int k = 0; k < K; ++k) {
-            uint32_t w[PW];
-            if constexpr (PW == 4) {
-              const uint4 v = *reinterpret_cast<const uint4*>(ew + k * 32 * PW);
-              w[0] = v.x; w[1] = v.y; w[2] = v.z; w[3] = v.w;
+            const uint2 pc = ew[k * 32];
+            uint32_t slot;
+            T v;
+            if constexpr (ORDER == 1) {
+              slot = (pc.y >> (kP1SlotShift - 32)) & kSlotMask;
+              v = buf[pc.x & kP1SrcMask];
+              A::sum_into(v, buf[(pc.x >> kP1SrcBits) & kP1SrcMask]);
+              A::sum_into(v, buf[((pc.x >> (2 * kP1SrcBits)) | (pc.y << (32 - 2 * kP1SrcBits))) & kP1SrcMask]);
+              A::sum_into(v, buf[(pc.y >> (3 * kP1SrcBits - 32)) & kP1SrcMask]);
             } else {
-              const uint2 v = *reinterpret_cast<const uint2*>(ew + k * 32 * PW);
-              w[0] = v.x; w[1] = v.y;
+              slot = (pc.x >> kSrcBits) & kSlotMask;
+              v = buf[pc.x & kSrcMask];
+              A::sum_into(v, buf[pc.y & kSrcMask]);
             }
-            const uint32_t slot = (w[0] >> kSrcBits) & kSlotMask;
-            T v = buf[w[0] & kSrcMask];
-#pragma unroll
-            for (int p = 1; p < PW; ++p) A::sum_into(v, buf[w[p] & kSrcMask]);
             T a = acc[slot];
             A::sum_into(a, v);
             acc[slot] = a;
@@ -1067,7 +1175,7 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
         }
         if (c + 1 < n) mbar_arrive(&bars[kBarToken + (g ^ 1)]);  // release: the updates above precede
         failed = group_sync_or(g, failed);
-        if (gtid == 0) mbar_arrive(&bars[kBarEntEmpty + (qq & 1)]);
+        if (gtid == 0) mbar_arrive(&bars[kBarEntEmpty + qq % kWordStages]);
       }
       q += n;
       if (!failed && !mbar_wait(&bars[kBarMetaFull], (uint32_t)(j & 1))) failed = true;

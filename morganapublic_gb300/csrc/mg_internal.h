@@ -55,17 +55,22 @@ constexpr int kRecStages = 4;
 constexpr int kChunkP1 = 256;
 constexpr int kChunkP2 = 32;
 constexpr int kP2ThreadsPerItem = kThreads / kChunkP2;
-// Contribution-list word: source (13 bits) | accumulator slot (14 bits) << 13 |
-// end-of-segment flag << 31.  The source indexes the chunk's element matrices,
-// stored symmetric (nb (nb + 1) / 2 unique entries) and entry-major.  Padding
-// words carry the zero source; padding pieces the dummy slot kAccMax.
+// Contributions are applied in pieces: all contributions of a piece belong to one
+// accumulator slot; the kernel sums a piece in registers and updates the slot
+// once.  A piece is 8 bytes (two 32-bit words, the lower one first) and carries
+// piece_srcs(order) sources, each indexing the chunk's element matrices (stored
+// symmetric, nb (nb + 1) / 2 unique entries, entry-major):
+//   P1  4 sources of 12 bits at bits 0, 12, 24, 36 and the slot (14 bits) at bit 48
+//   P2  2 words, each source (13 bits) | slot (14 bits) << 13 (the slot in both)
+// Padding sources are the zero source (the entry past the chunk's matrices);
+// padding pieces target the dummy slot kAccMax.
 constexpr uint32_t kSrcBits = 13, kSlotBits = 14;
 constexpr uint32_t kSrcMask = (1u << kSrcBits) - 1, kSlotMask = (1u << kSlotBits) - 1;
-constexpr uint32_t kEndFlag = 1u << 31;
-// Contributions are applied in pieces of piece_words(order) words: all words of a
-// piece belong to one accumulator slot (carried by the piece's first word); the
-// kernel sums a piece in registers and updates the slot once.
-inline __host__ __device__ constexpr int piece_words(int order) { return order == 1 ? 4 : 2; }
+constexpr uint32_t kP1SrcBits = 12, kP1SrcMask = (1u << kP1SrcBits) - 1, kP1SlotShift = 48;
+inline __host__ __device__ constexpr int piece_srcs(int order) { return order == 1 ? 4 : 2; }
+// Stages of contribution words in shared memory: the words of chunk q go to
+// stage q % kWordStages, so copies run up to that many chunks ahead.
+constexpr int kWordStages = 4;
 
 // Values of precision `prec` are doubles (MG_F64, MG_F64_NATIVE) or floats (MG_F32).
 inline bool prec_valid(int prec) { return prec == MG_F64 || prec == MG_F32 || prec == MG_F64_NATIVE; }
@@ -97,8 +102,9 @@ struct BlockDesc {
 // Head of a chunk record.  The plan lays out, per chunk, one contiguous record
 // the kernel stages into shared memory with a single bulk copy:
 //   ChunkDesc (64 B) | element ids (4 B x n4) | local vertex indices (4 x 2 B x n4)
-//   | vertex coordinates relative to the chunk's first vertex, split r = hi + lo:
-//     float4 (hi.xyz, lo.x) x nn | float2 (lo.y, lo.z) x nn
+//   | vertex coordinates relative to the chunk's first vertex, split exactly
+//     r = hi + mid + lo: float4 (hi.xyz, mid.x) x nn | float4 (mid.yz, lo.xy) x nn
+//     | float lo.z x nn
 // n4 = the chunk's items rounded up to 4, nn = n_nodes (a multiple of 4), so
 // every part starts on a 16-byte boundary.  Element matrices depend on edge
 // vectors only, so the origin is not needed.
@@ -289,6 +295,7 @@ mg_status plan_device(mg_plan* p);  // uploads mesh + plan on first GPU use
 mg_status plan_tables(mg_plan* p, int quad, const RefTables** t, const double** d_tab);
 mg_status plan_work(mg_plan* p, size_t bytes, void** ptr);
 mg_status plan_rhs_map(mg_plan* p);  // the load-vector slot map (once per plan)
+int64_t schedule_block_count(int64_t wtot, int64_t wmax, int64_t sms);  // blocks of the schedule (mg_plan.cpp)
 mg_status build_pattern_device(mg_plan* p, cudaStream_t st);  // CSR pattern on the GPU (mg_pattern.cu)
 mg_status build_edges_device(mg_mesh* m, cudaStream_t st);    // edges on the GPU (mg_pattern.cu)
 mg_status ensure_edges(mg_mesh* m);

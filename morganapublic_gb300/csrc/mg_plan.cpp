@@ -126,6 +126,18 @@ static int64_t sm_count_hint()
   return 152;
 }
 
+// Block count of the schedule: the smallest nbk with W / nbk + wmax <= kAccMax
+// (W the total row weight, wmax the largest), raised to a multiple of `sms` when
+// it is above half of it.
+int64_t schedule_block_count(int64_t wtot, int64_t wmax, int64_t sms)
+{
+  if (wtot <= 0) return 1;
+  const int64_t room = std::max<int64_t>(1, kAccMax - wmax);
+  int64_t nbk = std::max<int64_t>(1, (wtot + room - 1) / room);
+  if (nbk > sms / 2) nbk = (nbk + sms - 1) / sms * sms;
+  return nbk;
+}
+
 static mg_status build_schedule(mg_plan* p, HostSchedule* hs)
 {
   mg_mesh* m = p->mesh;
@@ -166,38 +178,33 @@ static mg_status build_schedule(mg_plan* p, HostSchedule* hs)
 #pragma omp parallel for
     for (int64_t d = 0; d < nd; ++d) order[d] = kv[d].second;
   }
-  // greedy blocks of at most `cap` accumulator slots and kRowsMax rows.  The
-  // kernel runs one persistent CTA per SM, so the cap is lowered until the
-  // number of blocks is a multiple of the SM count (no partial last wave).
+  // blocks: contiguous runs of the Morton order, cut by prefix sums.  Row t has
+  // weight w_t = max(len_t, 4) (so a block of weight <= kAccMax holds at most
+  // kRowsMax rows); with W_t the exclusive prefix and W the total, row t goes to
+  // block floor(W_t nbk / W), and every block weighs at most W / nbk + max w <=
+  // kAccMax.  nbk is the smallest count that guarantees this, raised to a multiple
+  // of the SM count (the kernel runs one persistent CTA per SM: no partial last
+  // wave); blocks left empty by a heavy row are dropped.  The rule needs only a
+  // scan, so the GPU build computes the same blocks.
   std::vector<int32_t> block_of(nd);
   std::vector<int64_t> bstart;  // into order
-  auto cut = [&](int64_t cap) {
-    bstart.clear();
-    int64_t used = cap + 1, nrows = 0;
-    for (int64_t t = 0; t < nd; ++t) {
-      const int32_t r = order[t];
-      const int64_t l = p->rowptr[r + 1] - p->rowptr[r];
-      if (used + l > cap || nrows == kRowsMax) {
-        bstart.push_back(t);
-        used = 0;
-        nrows = 0;
-      }
-      used += l;
-      ++nrows;
-    }
-    return (int64_t)bstart.size();
-  };
   {
-    const int64_t n0 = cut(kAccMax), sms = sm_count_hint();
-    const int64_t target = (n0 + sms - 1) / sms * sms;
-    if (n0 > sms / 2 && target > n0) {
-      int64_t cap = std::max<int64_t>(1, (p->nnz + target - 1) / target);
-      while (cap < kAccMax && cut(cap) > target) cap += 8;
-      if (cap >= kAccMax) cut(kAccMax);
+    int64_t wtot = 0, wmax = 0;
+    for (int64_t t = 0; t < nd; ++t) {
+      const int64_t l = p->rowptr[order[t] + 1] - p->rowptr[order[t]];
+      wtot += std::max<int64_t>(l, 4);
+      wmax = std::max<int64_t>(wmax, std::max<int64_t>(l, 4));
     }
-    for (size_t b = 0; b < bstart.size(); ++b) {
-      const int64_t t1 = b + 1 < bstart.size() ? bstart[b + 1] : nd;
-      for (int64_t t = bstart[b]; t < t1; ++t) block_of[order[t]] = (int32_t)b;
+    const int64_t nbk = schedule_block_count(wtot, wmax, sm_count_hint());
+    int64_t wex = 0, prev = -1;
+    for (int64_t t = 0; t < nd; ++t) {
+      const int64_t b = wex * nbk / wtot;
+      if (b != prev) {
+        bstart.push_back(t);
+        prev = b;
+      }
+      block_of[order[t]] = (int32_t)bstart.size() - 1;
+      wex += std::max<int64_t>(p->rowptr[order[t] + 1] - p->rowptr[order[t]], 4);
     }
   }
   bstart.push_back(nd);
@@ -386,7 +393,7 @@ static mg_status build_schedule(mg_plan* p, HostSchedule* hs)
     for (int32_t b = 0; b < nbk; ++b)
       for (int32_t c = 0; c < hs->blocks[b].nchunks; ++c) {
         const int64_t n4 = (std::min(CI, hs->blocks[b].item_count - c * CI) + 3) & ~3;
-        maxb = std::max(maxb, (int64_t)sizeof(ChunkDesc) + 12 * n4 + 24 * (int64_t)hs->chunk_n_nodes[hs->blocks[b].chunk_begin + c]);
+        maxb = std::max(maxb, (int64_t)sizeof(ChunkDesc) + 12 * n4 + 36 * (int64_t)hs->chunk_n_nodes[hs->blocks[b].chunk_begin + c]);
       }
     if (maxb >= INT32_MAX) return set_error(MG_ERR_SIZE, "chunk record above 2 GiB");
     p->max_rec_bytes = (int32_t)maxb;
@@ -394,22 +401,34 @@ static mg_status build_schedule(mg_plan* p, HostSchedule* hs)
   // contribution lists, per block in parallel, then concatenated
   const int nu = nunique(m->order);
   const uint32_t zero_src = (uint32_t)(nu * CI);
-  if (zero_src > kSrcMask) return set_error(MG_ERR_SIZE, "chunk buffer above the 13-bit source index");
+  if (zero_src > (m->order == 1 ? kP1SrcMask : kSrcMask))
+    return set_error(MG_ERR_SIZE, "chunk buffer above the source index width");
   if (kAccMax + 1 > (int)kSlotMask + 1) return set_error(MG_ERR_SIZE, "accumulator above the 14-bit slot index");
-  const uint32_t pad_word = zero_src | ((uint32_t)kAccMax << kSrcBits);
-  const int PW = piece_words(m->order);
+  const int PW = piece_srcs(m->order);
+  // one 8-byte piece: PW sources of one slot (layout at piece_srcs)
+  auto make_piece = [&](uint32_t slot, const uint32_t* src) -> uint64_t {
+    if (PW == 4)
+      return (uint64_t)src[0] | (uint64_t)src[1] << kP1SrcBits | (uint64_t)src[2] << (2 * kP1SrcBits) |
+             (uint64_t)src[3] << (3 * kP1SrcBits) | (uint64_t)slot << kP1SlotShift;
+    const uint64_t w0 = src[0] | slot << kSrcBits, w1 = src[1] | slot << kSrcBits;
+    return w0 | w1 << 32;
+  };
+  uint64_t pad_piece;
+  {
+    const uint32_t z[4] = {zero_src, zero_src, zero_src, zero_src};
+    pad_piece = make_piece((uint32_t)kAccMax, z);
+  }
   std::vector<std::vector<uint32_t>> ent(nbk);
   std::vector<std::vector<int64_t>> cptr(nbk);
   std::vector<int64_t> contrib(nbk, 0), maxc(nbk, 0);
 #pragma omp parallel
   {
     struct Seg { int32_t slot, begin, len; };
-    std::vector<std::vector<uint32_t>> per(kThreads);
+    std::vector<std::vector<uint64_t>> per(kThreads);
     std::vector<std::vector<int32_t>> tseg(kThreads);
     std::vector<std::pair<int32_t, uint32_t>> list, tmp;  // (slot, src) in item order
     std::vector<Seg> segs, segs_by_len;
     std::vector<uint32_t> srcs;
-    std::vector<int64_t> heap;
     std::vector<int32_t> cnt;
 #pragma omp for schedule(dynamic, 1)
     for (int32_t b = 0; b < nbk; ++b) {
@@ -467,49 +486,40 @@ static mg_status build_schedule(mg_plan* p, HostSchedule* hs)
           for (const Seg& sg : segs) segs_by_len[cnt[maxlen - sg.len]++] = sg;
           segs.swap(segs_by_len);
         }
+        // dealt in snake order of that ranking: rank q goes to thread q mod T
+        // on even rounds (q / T) and T - 1 - q mod T on odd ones, which gives
+        // each thread nearly the same load and each warp lanes of similar loads
         for (auto& v : tseg) v.clear();
-        // min-heap of (load, thread): pops the least-loaded, lowest-numbered thread
-        heap.clear();
-        for (int t = 0; t < kThreads; ++t) heap.push_back(((int64_t)0 << 32) | t);
-        std::make_heap(heap.begin(), heap.end(), std::greater<int64_t>());
         for (size_t q = 0; q < segs.size(); ++q) {
-          const Seg& sg = segs[q];
-          std::pop_heap(heap.begin(), heap.end(), std::greater<int64_t>());
-          const int64_t top = heap.back();
-          const int best = (int)(top & 0xffffffff);
-          heap.back() = (((top >> 32) + (sg.len + PW - 1) / PW) << 32) | best;
-          std::push_heap(heap.begin(), heap.end(), std::greater<int64_t>());
-          tseg[best].push_back((int32_t)q);
+          const int r = (int)(q / kThreads), o = (int)(q % kThreads);
+          tseg[(r & 1) ? kThreads - 1 - o : o].push_back((int32_t)q);
         }
-        // each thread's segments cut into pieces of PW words (the last piece of
-        // a segment padded with zero-source words); pieces keep element order
+        // each thread's segments cut into pieces of PW sources (the last piece
+        // of a segment padded with the zero source); pieces keep element order
         for (int t = 0; t < kThreads; ++t) {
           auto& v = per[t];
           v.clear();
           for (int32_t q : tseg[t]) {
             const Seg& sg = segs[q];
-            for (int k0 = 0; k0 < sg.len; k0 += PW)
-              for (int k = k0; k < k0 + PW; ++k) {
-                const uint32_t slot_bits = (uint32_t)sg.slot << kSrcBits;
-                uint32_t w = k < sg.len ? (srcs[sg.begin + k] | slot_bits) : (zero_src | slot_bits);
-                if (k == sg.len - 1) w |= kEndFlag;
-                v.push_back(w);
-              }
+            for (int k0 = 0; k0 < sg.len; k0 += PW) {
+              uint32_t src[4];
+              for (int k = 0; k < PW; ++k) src[k] = k0 + k < sg.len ? srcs[sg.begin + k0 + k] : zero_src;
+              v.push_back(make_piece((uint32_t)sg.slot, src));
+            }
           }
         }
         const int64_t base = (int64_t)ent[b].size();
         for (int w = 0; w < kWarps; ++w) {
           cptr[b].push_back((int64_t)ent[b].size());
           size_t K = 0;  // pieces
-          for (int l = 0; l < 32; ++l) K = std::max(K, per[32 * w + l].size() / PW);
-          // layout [piece][lane][PW]: one PW*4-byte load per lane and piece
+          for (int l = 0; l < 32; ++l) K = std::max(K, per[32 * w + l].size());
+          // layout [piece][lane]: one 8-byte load per lane and piece (two words, lower first)
           for (size_t k = 0; k < K; ++k)
             for (int l = 0; l < 32; ++l) {
               const auto& v = per[32 * w + l];
-              for (int q = 0; q < PW; ++q) {
-                const size_t i = k * PW + q;
-                ent[b].push_back(i < v.size() ? v[i] : pad_word);
-              }
+              const uint64_t pc = k < v.size() ? v[k] : pad_piece;
+              ent[b].push_back((uint32_t)pc);
+              ent[b].push_back((uint32_t)(pc >> 32));
             }
         }
         cptr[b].push_back((int64_t)ent[b].size());
@@ -627,7 +637,7 @@ mg_status plan_device(mg_plan* p)
     int64_t maxb = 0;
     for (int64_t ck = 0; ck < nc; ++ck) {
       const int64_t n4 = (n_items(ck) + 3) & ~3, nn = hs.chunk_n_nodes[ck];
-      const int64_t bytes = (int64_t)sizeof(ChunkDesc) + 12 * n4 + 24 * nn;
+      const int64_t bytes = (int64_t)sizeof(ChunkDesc) + 12 * n4 + 36 * nn;
       off[ck + 1] = off[ck] + bytes;
       maxb = std::max(maxb, bytes);
     }
@@ -656,19 +666,24 @@ mg_status plan_device(mg_plan* p)
       std::memcpy(r + 64, &hs.items[first], 4 * n4);
       std::memcpy(r + 64 + 4 * n4, &hs.item_lconn[4 * first], 8 * n4);
       float4* va = reinterpret_cast<float4*>(r + 64 + 12 * n4);
-      float2* vb = reinterpret_cast<float2*>(r + 64 + 12 * n4 + 16 * nn);
+      float4* vb = reinterpret_cast<float4*>(r + 64 + 12 * n4 + 16 * nn);
+      float* vc = reinterpret_cast<float*>(r + 64 + 12 * n4 + 32 * nn);
       const int64_t n0 = hs.chunk_nodes[hs.chunk_node_begin[ck]];  // origin: the chunk's first vertex
       for (int64_t i = 0; i < nn; ++i) {
-        // r = x - origin (FP64), then r = hi + lo: hi = fl(r), lo = fl(r - hi)
+        // r = x - origin (FP64), then r = hi + mid + lo exactly: hi = fl(r),
+        // mid = fl(r - hi), lo = r - hi - mid (each remainder exact in FP64)
         const int64_t nd = hs.chunk_nodes[hs.chunk_node_begin[ck] + i];
-        float h[3], l[3];
+        float h[3], md[3], l[3];
         for (int k = 0; k < 3; ++k) {
           const double rr = xyz[3 * nd + k] - xyz[3 * n0 + k];
           h[k] = (float)rr;
-          l[k] = (float)(rr - (double)h[k]);
+          const double r1 = rr - (double)h[k];
+          md[k] = (float)r1;
+          l[k] = (float)(r1 - (double)md[k]);
         }
-        va[i] = make_float4(h[0], h[1], h[2], l[0]);
-        vb[i] = make_float2(l[1], l[2]);
+        va[i] = make_float4(h[0], h[1], h[2], md[0]);
+        vb[i] = make_float4(md[1], md[2], l[0], l[1]);
+        vc[i] = l[2];
       }
     }
     MG_TRY(upload(&p->d_chunk_data, data));

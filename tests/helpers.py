@@ -23,6 +23,23 @@ def sym_index(i, j, nb):
     return i * nb - i * (i - 1) // 2 + (j - i)
 
 
+def decode_pieces(words, order):
+    """The 8-byte contribution pieces of one warp's word range ([piece][lane], two
+    32-bit words each, the lower first) as (slot, sources) arrays of shape
+    (pieces, 32) and (pieces, 32, srcs): P1 four 12-bit sources at bits 0, 12,
+    24, 36 and the slot at bit 48; P2 two words source (13 bits) | slot << 13."""
+    w = np.asarray(words, dtype=np.uint64).reshape(-1, 32, 2)
+    pc = w[:, :, 0] | (w[:, :, 1] << np.uint64(32))
+    if order == 1:
+        srcs = np.stack([(pc >> np.uint64(12 * k)) & np.uint64(0xfff) for k in range(4)], axis=-1)
+        slot = (pc >> np.uint64(48)) & np.uint64(0x3fff)
+    else:
+        srcs = np.stack([w[:, :, 0] & np.uint64(0x1fff), w[:, :, 1] & np.uint64(0x1fff)], axis=-1)
+        slot = (w[:, :, 0] >> np.uint64(13)) & np.uint64(0x3fff)
+        assert np.array_equal(slot, (w[:, :, 1] >> np.uint64(13)) & np.uint64(0x3fff))
+    return slot.astype(np.int64), srcs.astype(np.int64)
+
+
 def emulate_schedule(sched, order, local_mats, nnz, rowptr):
     """Runs the assembly kernel's two phases on the host with given element
     matrices (local_mats[e] = [field i, test j]) -- checks the schedule only."""
@@ -46,15 +63,14 @@ def emulate_schedule(sched, order, local_mats, nnz, rowptr):
                     buf[u * CI + t] = local_mats[e][i, j]
             base = (cb + c) * (W + 1)
             for w in range(W):
-                # [piece][lane][PW]: a piece's words go to the slot of its first word
-                PW = 4 if order == 1 else 2
-                seg = ent[cptr[base + w]:cptr[base + w + 1]].reshape(-1, 32, PW)
+                # [piece][lane]: a piece's sources go to its slot
+                slots, srcs = decode_pieces(ent[cptr[base + w]:cptr[base + w + 1]], order)
                 for lane in range(32):
-                    for piece in seg[:, lane, :]:
-                        v = buf[int(piece[0]) & 0x1fff]
-                        for word in piece[1:]:
-                            v += buf[int(word) & 0x1fff]
-                        acc[(int(piece[0]) >> 13) & 0x3fff] += v
+                    for slot, src in zip(slots[:, lane], srcs[:, lane]):
+                        v = buf[src[0]]
+                        for x in src[1:]:
+                            v += buf[x]
+                        acc[slot] += v
         for r in range(rc):
             row, a0 = rows[rb + r], racc[rb + r]
             ln = rowptr[row + 1] - rowptr[row]

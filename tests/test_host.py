@@ -11,7 +11,7 @@ import pytest
 import morganapublic_gb300 as mg
 import oracle as orc
 from morganapublic_gb300 import meshgen
-from helpers import emulate_schedule, row_scaled_err
+from helpers import decode_pieces, emulate_schedule, row_scaled_err
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = os.path.join(ROOT, "tests", "golden")
@@ -200,12 +200,12 @@ def test_schedule_slots_have_one_writer_per_chunk(order):
             owner = {}
             PW = 4 if order == 1 else 2
             for w in range(info.warps):
-                seg = s["entries"][cp[w]:cp[w + 1]].reshape(-1, 32, PW)
+                slots, srcl = decode_pieces(s["entries"][cp[w]:cp[w + 1]], order)
+                assert srcl.shape[2] == PW
                 for lane in range(32):
                     t = 32 * w + lane
-                    for piece in seg[:, lane, :]:
-                        slot = (int(piece[0]) >> 13) & 0x3fff
-                        srcs = [int(x) & 0x1fff for x in piece]
+                    for slot, srcs in zip(slots[:, lane], srcl[:, lane]):
+                        slot, srcs = int(slot), [int(x) for x in srcs]
                         if slot == info.acc_max:
                             assert all(x == zero for x in srcs)
                             continue
