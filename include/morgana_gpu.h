@@ -161,11 +161,13 @@ mg_status mg_mesh_export_geometry(const mg_mesh* mesh, double* h_xyz, int32_t* h
    Replaces: the pattern half of traitsMatrixBuilder::buildEpetraCrs / numEntPerRow
    (src/morganaFiniteElements/traitsMatrixBuilder.hpp:363-544). */
 mg_status mg_pattern_build(mg_mesh* mesh, mg_plan** out);
-/* The same plan with the CSR pattern computed on the GPU (element couplings
-   as 64-bit keys, radix-sorted and de-duplicated on the device; identical
-   rowptr / colind), the assembly schedule then built on the host.  Needs a
-   device; waits for its own work on `stream`.  Up to 2^31 element couplings
-   (E nb^2), else MG_ERR_SIZE.
+/* The same plan built on the GPU: the CSR pattern (element couplings as
+   64-bit keys, radix-sorted and de-duplicated on the device) and the assembly
+   schedule (Morton orders by radix sort, blocks by a prefix sum, per chunk its
+   vertices, contribution list and words by one CTA), identical to the host
+   build's arrays.  The plan is device-resident on return.  Needs a device;
+   waits for its own work on `stream`.  Up to 2^31 element couplings (E nb^2),
+   else MG_ERR_SIZE.
    Replaces: the same pattern half of buildEpetraCrs. */
 mg_status mg_pattern_build_device(mg_mesh* mesh, mg_plan** out, void* stream);
 mg_status mg_plan_destroy(mg_plan* plan);
@@ -180,8 +182,9 @@ mg_status mg_pattern_device(const mg_plan* plan, const int32_t** d_rowptr, const
 /* Assembly schedule of a plan (no reference counterpart: the reference inserts
    element blocks into Epetra one by one).  The dofs are cut into blocks of at
    most acc_max CSR entries; one CTA of `threads` threads owns a block and
-   recomputes every element ("item") touching it.  For host-side checks the
-   schedule can be exported until the plan is first used on the GPU. */
+   recomputes every element ("item") touching it.  For checks the schedule can
+   be exported: from the host copy until a host-built plan is first used on the
+   GPU, from the device arrays for a plan built by mg_pattern_build_device. */
 typedef struct {
   int32_t nblocks;
   int32_t threads;

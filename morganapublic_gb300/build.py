@@ -23,7 +23,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["mg_assemble.cu", "mg_solve.cu", "mg_pattern.cu", "mg_lagrange.cu"]
+CU_SOURCES = ["mg_assemble.cu", "mg_solve.cu", "mg_pattern.cu", "mg_lagrange.cu", "mg_schedule.cu"]
 CPP_SOURCES = ["mg_mesh.cpp", "mg_plan.cpp", "mg_lagrange.cpp"]
 
 

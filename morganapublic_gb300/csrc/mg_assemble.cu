@@ -852,7 +852,7 @@ __device__ __forceinline__ bool group_sync_or(int g, bool pred)
 // the producer stops issuing and lets its copies in flight land, and the CTA
 // records the failure.
 template <int ORDER, int MODE>
-__global__ void __maxnreg__(112) k_assemble(AsmArgs a)
+__global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
 {
   using A = Arith<MODE>;
   using T = typename A::T;
@@ -1256,7 +1256,7 @@ static mg_status launch_assemble_t(AsmArgs a, cudaStream_t st)
     sms = cache.sms[dev];
   }
   MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_assemble<ORDER, MODE>, kAsmThreads, smem));
-  if (per_sm < 1) return set_error(MG_ERR_SIZE, "assembly CTA does not fit on an SM (shared memory)");
+  if (per_sm < 1) return set_error(MG_ERR_SIZE, "assembly CTA does not fit on an SM (shared memory or registers)");
   const int grid = std::max(1, std::min(a.nblocks, per_sm * sms));
   if (a.nblocks > 0) k_assemble<ORDER, MODE><<<grid, kAsmThreads, smem, st>>>(a);
   MG_CUDA(cudaGetLastError());

@@ -183,6 +183,7 @@ struct mg_plan {
   int32_t max_rec_bytes = 0;
   int32_t max_chunk_nodes = 0;
   int2* d_row_meta = nullptr;  // owned rows, schedule order: (accumulator base, CSR start - base)
+  int32_t* d_sched_rows = nullptr;  // device-built schedules: the owned rows (for the schedule export)
   int32_t* d_elem_order = nullptr;  // elements along a Morton curve of their centroids
   int32_t* d_dofs_morton = nullptr; // their dofs (nb each) in that order
   uint32_t* d_entries = nullptr;   // contribution words
@@ -296,7 +297,12 @@ mg_status plan_tables(mg_plan* p, int quad, const RefTables** t, const double** 
 mg_status plan_work(mg_plan* p, size_t bytes, void** ptr);
 mg_status plan_rhs_map(mg_plan* p);  // the load-vector slot map (once per plan)
 int64_t schedule_block_count(int64_t wtot, int64_t wmax, int64_t sms);  // blocks of the schedule (mg_plan.cpp)
-mg_status build_pattern_device(mg_plan* p, cudaStream_t st);  // CSR pattern on the GPU (mg_pattern.cu)
+// CSR pattern on the GPU (mg_pattern.cu); keep_device: its device arrays become
+// the plan's d_rowptr / d_colind
+mg_status build_pattern_device(mg_plan* p, cudaStream_t st, bool keep_device);
+// the assembly schedule on the GPU from the plan's device pattern (mg_schedule.cu):
+// the same arrays as the host build, uploaded state included (on_device)
+mg_status build_schedule_device(mg_plan* p, cudaStream_t st);
 mg_status build_edges_device(mg_mesh* m, cudaStream_t st);    // edges on the GPU (mg_pattern.cu)
 mg_status ensure_edges(mg_mesh* m);
 mg_status launch_assemble(mg_plan* p, int op, const double* d_coeff, double c, int quad, int prec,

@@ -15,7 +15,8 @@
 //   1. one 64-bit key row << 32 | col per element coupling (E nb^2 keys),
 //   2. a radix sort of the keys and removal of duplicates (CUB),
 //   3. row starts by binary search over the sorted unique keys.
-// The assembly schedule is then built on the host from the downloaded pattern.
+// The pattern is copied to the host (the export calls and the boundary-multiplier
+// build read it there) and, for the device schedule build, kept on the device.
 #include <algorithm>
 #include <vector>
 
@@ -222,7 +223,7 @@ mg_status build_edges_device(mg_mesh* m, cudaStream_t st)
   return MG_OK;
 }
 
-mg_status build_pattern_device(mg_plan* p, cudaStream_t st)
+mg_status build_pattern_device(mg_plan* p, cudaStream_t st, bool keep_device)
 {
   mg_mesh* m = p->mesh;
   const int nb = m->nb;
@@ -267,6 +268,12 @@ mg_status build_pattern_device(mg_plan* p, cudaStream_t st)
   p->nnz = nnz;
   for (int64_t r = 0; r < nd; ++r)
     if (p->rowptr[r + 1] - p->rowptr[r] > kAccMax) return set_error(MG_ERR_SIZE, "a CSR row has more than 8192 entries");
+  if (keep_device) {  // the device copies become the plan's (the schedule is built from them)
+    p->d_rowptr = d.rowptr;
+    p->d_colind = d.colind;
+    d.rowptr = nullptr;
+    d.colind = nullptr;
+  }
   return MG_OK;
 }
 

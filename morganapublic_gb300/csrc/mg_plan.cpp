@@ -710,6 +710,7 @@ static void free_plan(mg_plan* p)
   cudaFree(p->d_chunk_data);
   cudaFree(p->d_chunk_rec);
   cudaFree(p->d_row_meta);
+  cudaFree(p->d_sched_rows);
   cudaFree(p->d_elem_order);
   cudaFree(p->d_dofs_morton);
   cudaFree(p->d_rhs_ptr);
@@ -829,6 +830,44 @@ mg_status plan_work(mg_plan* p, size_t bytes, void** ptr)
 
 using namespace mg;
 
+// The schedule of a plan built on the GPU, in the export format, read back from
+// the device arrays (blocks, chunk records, words, row metadata).
+static mg_status export_device_schedule(const mg_plan* p, int32_t* h_blocks, int32_t* h_items, int64_t* h_chunk_ptr,
+                                        uint32_t* h_entries, int32_t* h_rows, int32_t* h_row_acc)
+{
+  const int CI = chunk_items(p->mesh->order);
+  std::vector<BlockDesc> blocks(p->nblocks);
+  if (p->nblocks) MG_CUDA(cudaMemcpy(blocks.data(), p->d_blocks, sizeof(BlockDesc) * p->nblocks, cudaMemcpyDeviceToHost));
+  if (h_blocks) std::memcpy(h_blocks, blocks.data(), sizeof(BlockDesc) * blocks.size());
+  if (h_entries && p->n_entries)
+    MG_CUDA(cudaMemcpy(h_entries, p->d_entries, sizeof(uint32_t) * p->n_entries, cudaMemcpyDeviceToHost));
+  if (h_rows && p->ndof) MG_CUDA(cudaMemcpy(h_rows, p->d_sched_rows, sizeof(int32_t) * p->ndof, cudaMemcpyDeviceToHost));
+  if (h_row_acc && p->ndof) {
+    std::vector<int2> meta(p->ndof);
+    MG_CUDA(cudaMemcpy(meta.data(), p->d_row_meta, sizeof(int2) * p->ndof, cudaMemcpyDeviceToHost));
+    for (int64_t k = 0; k < p->ndof; ++k) h_row_acc[k] = meta[k].x;
+  }
+  if (h_items || h_chunk_ptr) {
+    std::vector<int2> rec(p->n_chunks);
+    if (p->n_chunks) MG_CUDA(cudaMemcpy(rec.data(), p->d_chunk_rec, sizeof(int2) * p->n_chunks, cudaMemcpyDeviceToHost));
+    const int64_t bytes = p->n_chunks ? (int64_t)rec.back().x * 16 + rec.back().y : 0;
+    std::vector<unsigned char> data(std::max<int64_t>(bytes, 1));
+    if (bytes) MG_CUDA(cudaMemcpy(data.data(), p->d_chunk_data, bytes, cudaMemcpyDeviceToHost));
+    for (const BlockDesc& d : blocks)
+      for (int32_t c = 0; c < d.nchunks; ++c) {
+        const int64_t ck = d.chunk_begin + c;
+        const unsigned char* r = data.data() + (int64_t)rec[ck].x * 16;
+        ChunkDesc cd;
+        std::memcpy(&cd, r, sizeof cd);
+        if (h_chunk_ptr)
+          for (int w = 0; w <= kWarps; ++w) h_chunk_ptr[ck * (kWarps + 1) + w] = cd.word_begin + cd.warp_off[w];
+        const int n4 = (std::min(CI, d.item_count - c * CI) + 3) & ~3;
+        if (h_items) std::memcpy(h_items + d.item_begin + (int64_t)c * CI, r + sizeof(ChunkDesc), 4 * (size_t)n4);
+      }
+  }
+  return MG_OK;
+}
+
 extern "C" {
 
 mg_status mg_pattern_build(mg_mesh* mesh, mg_plan** out)
@@ -856,9 +895,8 @@ mg_status mg_pattern_build_device(mg_mesh* mesh, mg_plan** out, void* stream)
   *out = nullptr;
   mg_plan* p = new mg_plan();
   p->mesh = mesh;
-  p->host_schedule = new HostSchedule();
-  mg_status s = build_pattern_device(p, (cudaStream_t)stream);
-  if (s == MG_OK) s = build_schedule(p, p->host_schedule);
+  mg_status s = build_pattern_device(p, (cudaStream_t)stream, true);
+  if (s == MG_OK) s = build_schedule_device(p, (cudaStream_t)stream);
   if (s != MG_OK) {
     free_plan(p);
     return s;
@@ -907,7 +945,7 @@ mg_status mg_plan_schedule_info(const mg_plan* p, mg_schedule_info* info)
   info->warps = kWarps;
   info->acc_max = kAccMax;
   info->chunk_items = chunk_items(p->mesh->order);
-  info->host_copy = p->host_schedule != nullptr;
+  info->host_copy = p->host_schedule != nullptr || p->d_sched_rows != nullptr;
   info->n_items = p->n_items;
   info->n_chunks = p->n_chunks;
   info->n_entries = p->n_entries;
@@ -925,10 +963,11 @@ mg_status mg_plan_export_schedule(const mg_plan* p, int32_t* h_blocks, int32_t* 
 {
   if (!p) return set_error(MG_ERR_INVALID_ARG, "mg_plan_export_schedule: null plan");
   const HostSchedule* hs = p->host_schedule;
+  static_assert(sizeof(BlockDesc) == 8 * sizeof(int32_t), "BlockDesc layout");
+  if (!hs && p->d_sched_rows) return export_device_schedule(p, h_blocks, h_items, h_chunk_ptr, h_entries, h_rows, h_row_acc);
   if (!hs)
     return set_error(MG_ERR_UNSUPPORTED,
                      "the host copy of the schedule is released once the plan is used on the GPU");
-  static_assert(sizeof(BlockDesc) == 8 * sizeof(int32_t), "BlockDesc layout");
   if (h_blocks) std::memcpy(h_blocks, hs->blocks.data(), sizeof(BlockDesc) * hs->blocks.size());
   if (h_items) std::memcpy(h_items, hs->items.data(), sizeof(int32_t) * hs->items.size());
   if (h_chunk_ptr) std::memcpy(h_chunk_ptr, hs->chunk_ptr.data(), sizeof(int64_t) * hs->chunk_ptr.size());

@@ -260,16 +260,21 @@ def test_unreferenced_nodes_give_empty_rows():
     assert np.max(np.abs(r - r_ref)) <= 1e-13 * np.abs(r_ref).max()
 
 
-@pytest.mark.parametrize("case", ["p1", "p2_lex", "p2_first", "extra_nodes", "single", "no_elements"])
+@pytest.mark.parametrize("case", ["p1", "p2_lex", "p2_first", "extra_nodes", "single", "no_elements", "p1_big",
+                                  "p2_big"])
 def test_device_pattern_build_matches_host(case):
-    """mg_pattern_build_device (CSR pattern from sorted element-coupling keys on
-    the GPU) gives the host build's rowptr / colind bit for bit, hence the same
-    assembly schedule and values."""
+    """mg_pattern_build_device (CSR pattern from sorted element-coupling keys, then
+    the assembly schedule -- blocks, items, chunk records, contribution words --
+    all on the GPU) gives the host build's arrays bit for bit, hence the same
+    values."""
     xyz1 = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], dtype=np.float64)
     if case == "single":
         xyz, conn, order, rule = xyz1, np.array([[0, 1, 2, 3]], dtype=np.int32), 1, "lex"
     elif case == "no_elements":
         xyz, conn, order, rule = xyz1, np.zeros((0, 4), dtype=np.int32), 1, "lex"
+    elif case.endswith("big"):
+        m = meshgen.kuhn_cube(32 if case == "p1_big" else 12, jitter=0.25, seed=19, permute=True)
+        xyz, conn, order, rule = m.xyz, m.conn, 1 if case == "p1_big" else 2, "lex"
     else:
         m = meshgen.kuhn_cube(6 if case.startswith("p1") or case == "extra_nodes" else 4, jitter=0.2, seed=17,
                               permute=True)
@@ -286,6 +291,9 @@ def test_device_pattern_build_matches_host(case):
     rp_d, ci_d = dev.pattern()
     assert np.array_equal(rp_h, rp_d) and np.array_equal(ci_h, ci_d)
     sh, sd = host.export_schedule(), dev.export_schedule()
+    for f in ("nblocks", "n_items", "n_chunks", "n_entries", "n_contrib", "n_item_slots", "max_chunk_entries",
+              "max_chunk_vertices", "max_chunk_record_bytes"):
+        assert getattr(sh["info"], f) == getattr(sd["info"], f), f
     for k in sh:
         if k != "info":
             assert np.array_equal(np.asarray(sh[k]), np.asarray(sd[k])), k
