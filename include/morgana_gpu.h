@@ -243,6 +243,16 @@ mg_status mg_assemble(mg_plan* plan, int32_t op, const double* d_coeff, double c
    coefficient by a power of two).  Clears the record.  No reference counterpart (the reference asserts). */
 mg_status mg_plan_status(mg_plan* plan);
 
+/* Diagnostic: the number of polls after which a wait of this plan's assembly
+   pipeline (a bulk copy landing, a buffer released, the other consumer group's
+   token) gives up; the default is 2^22 (seconds, far beyond any real wait).  A
+   wait that gives up makes the kernel leave early -- its last copies in flight
+   still land before a CTA exits -- and mg_plan_status report MG_ERR_CUDA; 0
+   makes every wait give up at once, which is how the failure path is tested.
+   No reference counterpart. */
+#define MG_WAIT_LIMIT_DEFAULT 4194304u
+mg_status mg_plan_set_wait_limit(mg_plan* plan, uint32_t polls);
+
 /* Host-buffer form of mg_assemble, the call an Epetra/Tpetra adapter makes:
    copies h_coeff in, assembles, copies the nnz values out to h_values. */
 mg_status mg_assemble_host(mg_plan* plan, int32_t op, const double* h_coeff, double c, int32_t quad,

@@ -104,6 +104,7 @@ SIGNATURES = {
     "mg_assemble": [_P, _I32, _P, _D, _I32, _I32, _P, _P],
     "mg_assemble_host": [_P, _I32, _P, _D, _I32, _I32, _P, _P],
     "mg_plan_status": [_P],
+    "mg_plan_set_wait_limit": [_P, ctypes.c_uint32],
     "mg_assemble_rhs": [_P, _P, _P, _I32, _P, _P],
     "mg_apply_dirichlet": [_P, _P, _I32, _P, _P, _P],
     "mg_spmv": [_P, _I32, _P, _P, _P, _P],
@@ -367,6 +368,10 @@ class MatrixBuilder:
     def status(self):
         """Synchronises and raises if an earlier asynchronous assembly recorded a device-side failure."""
         _check(lib().mg_plan_status(self._h), "mg_plan_status")
+
+    def set_wait_limit(self, polls: int = 4194304):
+        """Diagnostic: polls before an assembly pipeline wait gives up (mg_plan_set_wait_limit)."""
+        _check(lib().mg_plan_set_wait_limit(self._h, polls), "mg_plan_set_wait_limit")
 
     def apply_dirichlet(self, values, mask, b=None, stream=None):
         torch = _torch()

@@ -143,12 +143,15 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
                : "memory");
 }
 
-// Bounded wait: gives up after kWaitLimit polls (each poll may suspend the
-// thread for a short, hardware-chosen time) and returns false.
-constexpr uint32_t kWaitLimit = 1u << 22;
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
+// Bounded wait: gives up after `limit` polls (each poll may suspend the thread
+// for a short, hardware-chosen time) and returns false.  The pipeline waits take
+// the plan's limit (kWaitLimit unless a diagnostic lowered it); the producer's
+// final waits for its own copies in flight always take kWaitLimit, so that no
+// bulk copy is still writing shared memory when the CTA exits.
+constexpr uint32_t kWaitLimit = MG_WAIT_LIMIT_DEFAULT;
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit)
 {
-  for (uint32_t i = 0; i < kWaitLimit; ++i)
+  for (uint32_t i = 0; i < limit; ++i)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
@@ -731,6 +734,7 @@ struct AsmArgs {
   int stiff;
   int ent_cap;           // words of one shared-memory contribution buffer
   int stage_cap;         // bytes of one chunk-record stage (the largest record)
+  uint32_t wait_limit;   // polls of a pipeline wait before it gives up (mbar_wait)
 };
 
 constexpr size_t align16(size_t n) { return (n + 15) / 16 * 16; }
@@ -900,7 +904,7 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
       for (int s = 0; s < NS; ++s) last_rec[s] = -1;
       for (int s = 0; s < NW; ++s) last_ent[s] = -1;
       auto wait = [&](int k, int parity) {
-        if (!failed && !mbar_wait(&bars[k], (uint32_t)parity)) failed = true;
+        if (!failed && !mbar_wait(&bars[k], (uint32_t)parity, a.wait_limit)) failed = true;
         return !failed;
       };
       auto put_rec = [&](int q, int off16, int bytes) {  // record fill q
@@ -967,10 +971,10 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
       if (failed) {
         // let the copies in flight land before the CTA's shared memory goes away
         for (int s = 0; s < NS; ++s)
-          if (last_rec[s] >= 0) mbar_wait(&bars[kBarRecFull + s], (uint32_t)((last_rec[s] / NS) & 1));
+          if (last_rec[s] >= 0) mbar_wait(&bars[kBarRecFull + s], (uint32_t)((last_rec[s] / NS) & 1), kWaitLimit);
         for (int s = 0; s < NW; ++s)
-          if (last_ent[s] >= 0) mbar_wait(&bars[kBarEntFull + s], (uint32_t)((last_ent[s] / NW) & 1));
-        if (last_meta >= 0) mbar_wait(&bars[kBarMetaFull], (uint32_t)(last_meta & 1));
+          if (last_ent[s] >= 0) mbar_wait(&bars[kBarEntFull + s], (uint32_t)((last_ent[s] / NW) & 1), kWaitLimit);
+        if (last_meta >= 0) mbar_wait(&bars[kBarMetaFull], (uint32_t)(last_meta & 1), kWaitLimit);
       }
     }
     __syncwarp();
@@ -989,7 +993,7 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
     const T wsum = A::from(a.wsum);
     int q = 0, ntok = 0;  // chunks before this block; token waits so far
     for (int j = 0;; ++j) {
-      if (!mbar_wait(&bars[kBarBlkFull + (j & 1)], (uint32_t)((j >> 1) & 1))) failed = true;
+      if (!mbar_wait(&bars[kBarBlkFull + (j & 1)], (uint32_t)((j >> 1) & 1), a.wait_limit)) failed = true;
       if (named_sync_or<1, kConsumers>(failed)) { failed = true; break; }
       const BlockDesc d = sblk[j & 1];
       mbar_arrive(&bars[kBarBlkEmpty + (j & 1)]);
@@ -1001,7 +1005,7 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
       for (int c = (g - q) & 1; c < n; c += kGroups) {
         const int qq = q + c;
         // ---- phase 1: element matrices of chunk c from its staged record
-        if (!failed && !mbar_wait(&bars[kBarRecFull + qq % NS], (uint32_t)((qq / NS) & 1))) failed = true;
+        if (!failed && !mbar_wait(&bars[kBarRecFull + qq % NS], (uint32_t)((qq / NS) & 1), a.wait_limit)) failed = true;
         int w_beg = 0, w_end = 0;  // this warp's contribution words (read before the record is released)
         if (!failed) {
           w_beg = desc_of(qq)->warp_off[gwarp];
@@ -1142,10 +1146,11 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
         // one slot are summed in registers and update the slot once; within a
         // chunk every slot belongs to one thread, and the token orders the
         // chunks.
-        if (!failed && !mbar_wait(&bars[kBarEntFull + qq % kWordStages], (uint32_t)((qq / kWordStages) & 1)))
+        if (!failed &&
+            !mbar_wait(&bars[kBarEntFull + qq % kWordStages], (uint32_t)((qq / kWordStages) & 1), a.wait_limit))
           failed = true;
         if (c >= 1) {
-          if (!failed && !mbar_wait(&bars[kBarToken + g], (uint32_t)(ntok & 1))) failed = true;
+          if (!failed && !mbar_wait(&bars[kBarToken + g], (uint32_t)(ntok & 1), a.wait_limit)) failed = true;
           ++ntok;
         }
         if (!failed) {
@@ -1178,7 +1183,7 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
         if (gtid == 0) mbar_arrive(&bars[kBarEntEmpty + qq % kWordStages]);
       }
       q += n;
-      if (!failed && !mbar_wait(&bars[kBarMetaFull], (uint32_t)(j & 1))) failed = true;
+      if (!failed && !mbar_wait(&bars[kBarMetaFull], (uint32_t)(j & 1), a.wait_limit)) failed = true;
       if (named_sync_or<1, kConsumers>(failed)) { failed = true; break; }
       // ---- write the owned rows, one row per thread: the stores of a pass go
       // to 32 rows at once, the accumulator reads (consecutive rows) spread
@@ -1295,6 +1300,7 @@ mg_status launch_assemble(mg_plan* p, int op, const double* d_coeff, double c, i
   a.stiff = (op == MG_OP_STIFF_KAPPA || op == MG_OP_STIFF_CONST);
   a.ent_cap = (int)((p->max_chunk_entries + 3) / 4 * 4);
   a.stage_cap = std::max(p->max_rec_bytes, 64);
+  a.wait_limit = p->wait_limit;
   if (m->order == 1) {
     if (prec == MG_F32) return launch_assemble_t<1, kF32>(a, st);
     return prec == MG_F64_NATIVE ? launch_assemble_t<1, kF64>(a, st) : launch_assemble_t<1, kDW>(a, st);
@@ -1620,6 +1626,13 @@ mg_status mg_plan_status(mg_plan* p)
     return set_error(MG_ERR_UNSUPPORTED,
                      "assembly: element-matrix scales outside 2^-96 .. 2^112, where the double-word MG_F64 "
                      "assembly keeps 1e-12 accuracy; use MG_F64_NATIVE or rescale the coefficient by a power of two");
+  return MG_OK;
+}
+
+mg_status mg_plan_set_wait_limit(mg_plan* p, uint32_t polls)
+{
+  if (!p) return set_error(MG_ERR_INVALID_ARG, "mg_plan_set_wait_limit: null plan");
+  p->wait_limit = polls;
   return MG_OK;
 }
 

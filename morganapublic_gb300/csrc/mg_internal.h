@@ -214,6 +214,7 @@ struct mg_plan {
   double* d_tmp_coeff = nullptr;
   size_t tmp_coeff_bytes = 0;
   mg::HostSchedule* host_schedule = nullptr;  // until uploaded
+  uint32_t wait_limit = MG_WAIT_LIMIT_DEFAULT;  // polls of an assembly pipeline wait (mg_plan_set_wait_limit)
   std::atomic<bool> on_device{false};  // set once uploaded (under upload_mu), on the mesh's device
   std::mutex upload_mu;
 };

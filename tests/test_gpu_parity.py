@@ -666,3 +666,29 @@ def test_strongly_jittered_mesh_p2(jitter, seed):
     e32 = row_scaled_err(rp, ref, v32)
     print(f"P2 12^3 jitter {jitter}: FP64 {e64:.2e}, FP32 {e32:.2e}")
     assert e64 <= F64_TOL and e32 <= 2 * F32_TOL
+
+
+@pytest.mark.parametrize("order,prec", [(1, "f64"), (1, "f32"), (2, "f64")])
+def test_bounded_wait_gives_up_and_the_plan_recovers(order, prec):
+    """The assembly pipeline's waits are bounded: with the limit lowered to 0
+    every wait gives up at once, the kernel returns (its last bulk copies land
+    first), mg_plan_status reports MG_ERR_CUDA, and with the default limit back
+    the same plan assembles the oracle's values again (the context stays usable)."""
+    m, kappa = _case(8 if order == 1 else 4, 0.2, 1, True, 1.0)
+    mesh = mg.Mesh(m.xyz, m.conn, order=order)
+    b = mg.MatrixBuilder(mesh)
+    quad = 4 if order == 1 else 15
+    _, rp, ci, ref = orc.full_operator("stiff_kappa", order, quad, m.xyz, m.conn, coeff=kappa)
+    v = b.assemble("stiff_kappa", coeff=kappa, quad=quad, prec=prec)
+    b.status()
+    b.set_wait_limit(0)
+    b.assemble("stiff_kappa", coeff=kappa, quad=quad, prec=prec, out=v)
+    with pytest.raises(mg.MorganaError) as err:
+        b.status()
+    assert err.value.status == mg.MG_ERR_CUDA
+    b.set_wait_limit()
+    b.status()  # the record was cleared
+    b.assemble("stiff_kappa", coeff=kappa, quad=quad, prec=prec, out=v)
+    b.status()
+    tol = F64_TOL if prec == "f64" else 2 * F32_TOL
+    assert row_scaled_err(rp, ref, v.cpu().numpy()) <= tol
