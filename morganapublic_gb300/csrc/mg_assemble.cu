@@ -380,6 +380,14 @@ __device__ __forceinline__ ff dw_edge(const FetchAbs& F, int k, int j, int r)
   return dw_diff3(rec_hi(F.a[k], r), rec_hi(F.a[j], r), rec_mid(F.a[k], F.b[k], r), rec_mid(F.a[j], F.b[j], r),
                   rec_lo(F.b[k], F.lz[k], r), rec_lo(F.b[j], F.lz[j], r));
 }
+// the same from hi + mid only (48 bits of the chunk-relative coordinate): the
+// common path, whose elements (gradient ratios <= 3, p1_class) do not amplify
+// that truncation past ~1e-13
+__device__ __forceinline__ ff dw_edge2(const FetchAbs& F, int k, int j, int r)
+{
+  const ff s1 = two_sum(rec_hi(F.a[k], r), -rec_hi(F.a[j], r));
+  return two_sum(s1.hi, __fadd_rn(s1.lo, __fsub_rn(rec_mid(F.a[k], F.b[k], r), rec_mid(F.a[j], F.b[j], r))));
+}
 __device__ __forceinline__ float f32_edge(const FetchAbs& F, int k, int j, int r)
 {
   return (rec_hi(F.a[k], r) - rec_hi(F.a[j], r)) + (rec_mid(F.a[k], F.b[k], r) - rec_mid(F.a[j], F.b[j], r));
@@ -405,7 +413,7 @@ template <int MODE>
 __device__ __forceinline__ bool geometry_staged_lazy(const StagedVerts& v, ushort4 lc, Cof<typename Arith<MODE>::T>& f)
 {
   using T = typename Arith<MODE>::T;
-  constexpr bool LO = MODE != kF32;
+  constexpr bool LO = MODE == kF64;
   FetchAbs F;  // slots 0 (vertex 0) and 1 (the current column's vertex) only
   F.a[0] = v.a[lc.x];
   F.b[0] = v.b[lc.x];
@@ -420,7 +428,7 @@ __device__ __forceinline__ bool geometry_staged_lazy(const StagedVerts& v, ushor
 #pragma unroll
     for (int r = 0; r < 3; ++r) {
       if constexpr (MODE == kF32) J[r][k] = f32_edge(F, 1, 0, r);
-      else if constexpr (MODE == kDW) J[r][k] = dw_edge(F, 1, 0, r);
+      else if constexpr (MODE == kDW) J[r][k] = dw_edge2(F, 1, 0, r);
       else J[r][k] = rec_x(F.a[1], F.b[1], F.lz[1], r) - rec_x(F.a[0], F.b[0], F.lz[0], r);
     }
   }
@@ -778,8 +786,9 @@ struct AsmLayout {
   static constexpr size_t blk_bytes = 2 * sizeof(BlockDesc);
   static constexpr size_t off_buf = acc_bytes;
   static constexpr size_t off_tab = off_buf + kGroups * buf_bytes;
-  // P2: per group, the 6 scale factors of each item of a chunk (computed once per item)
-  static constexpr size_t geo_bytes = ORDER == 2 ? align16(sizeof(T) * CI * 6) : 0;
+  // per group: P2 the 6 scale factors of each item of a chunk (computed once per
+  // item); P1 the chunk's rare stiffness items (a count, then item | class << 12)
+  static constexpr size_t geo_bytes = ORDER == 2 ? align16(sizeof(T) * CI * 6) : align16(4 + 2 * CI);
   static constexpr size_t off_geo = off_tab + tab_bytes;
   static constexpr size_t off_meta = off_geo + kGroups * geo_bytes;
   static constexpr size_t off_blk = off_meta + meta_bytes;
@@ -877,8 +886,10 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int i = tid; i < 7 * NU; i += blockDim.x) tab[i] = A::from(a.tables[i]);
   if (tid == 0) {
-    for (int g = 0; g < kGroups; ++g)
+    for (int g = 0; g < kGroups; ++g) {
       reinterpret_cast<T*>(smem + L::off_buf + g * L::buf_bytes)[NU * CI] = A::zero();
+      if (ORDER == 1) *reinterpret_cast<int*>(smem + L::off_geo + g * L::geo_bytes) = 0;
+    }
     for (int k = 0; k < kNumBars; ++k) {
       uint32_t count = 1;
       if (k == kBarBlkEmpty || k == kBarBlkEmpty + 1) count = kConsumers;
@@ -1084,12 +1095,10 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
               // writes its entries itself
               const int cls = degenerate ? (int)kP1Fp64 : p1_class<T>(f);
               special = cls != kP1Common;
-              if (__any_sync(__activemask(), special)) {
-                if (special)
-                  p1_stiff_special<MODE>(staged_verts(), item_lconn(local), cls, coef_d, a.wsum, buf + local, CI,
-                                         &a.counters[4]);
-              }
-              if (!special) {
+              if (special) {  // queued for the pass below
+                int* cnt = reinterpret_cast<int*>(sgeo);
+                reinterpret_cast<uint16_t*>(cnt + 1)[atomicAdd(cnt, 1)] = (uint16_t)(local | cls << 12);
+              } else {
                 const T sc = coef * wsum / f.det;
                 p1_stiff_unique<T>(f, sc, K);
                 check_scale(sc, K[4]);
@@ -1104,6 +1113,22 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
 #pragma unroll
               for (int u = 0; u < 10; ++u) buf[u * CI + local] = K[u];
             }
+          }
+          if (a.stiff) {
+            // the chunk's rare stiffness elements (p1_class: ~1 % on a 0.25 h jittered
+            // cube), one per thread after a group barrier, so that no warp runs the
+            // long path for one lane; each writes its own entries
+            failed = group_sync_or(g, failed);
+            const int* cnt = reinterpret_cast<const int*>(sgeo);
+            const int ns = *cnt;
+            if (!failed)
+              for (int k = gtid; k < ns; k += kThreads) {
+                const int v = reinterpret_cast<const uint16_t*>(cnt + 1)[k], it = v & 0xfff;
+                const int e = reinterpret_cast<const int32_t*>(stage_of(qq) + sizeof(ChunkDesc))[it];
+                const double coef_d = a.coeff ? __ldg(a.coeff + e) : a.cconst;
+                p1_stiff_special<MODE>(staged_verts(), item_lconn(it), v >> 12, coef_d, a.wsum, buf + it, CI,
+                                       &a.counters[4]);
+              }
           }
         } else {
           // P2: the first warp of the group computes each item's scale factors
@@ -1141,7 +1166,10 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
           }
         }
         failed = group_sync_or(g, failed);
-        if (gtid == 0) mbar_arrive(&bars[kBarRecEmpty + qq % NS]);
+        if (gtid == 0) {
+          mbar_arrive(&bars[kBarRecEmpty + qq % NS]);
+          if (ORDER == 1) *reinterpret_cast<int*>(sgeo) = 0;  // read by everyone before the barrier
+        }
         // ---- phase 2: segmented sums into owned slots.  Pieces of PW words of
         // one slot are summed in registers and update the slot once; within a
         // chunk every slot belongs to one thread, and the token orders the

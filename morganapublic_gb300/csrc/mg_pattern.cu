@@ -235,7 +235,15 @@ mg_status build_pattern_device(mg_plan* p, cudaStream_t st, bool keep_device)
   p->rowptr.assign(nd + 1, 0);
   p->colind.clear();
   p->nnz = 0;
-  if (n == 0) return MG_OK;
+  if (n == 0) {  // no elements: every row empty
+    if (keep_device) {
+      MG_CUDA(cudaMalloc(&p->d_rowptr, sizeof(int32_t) * (nd + 1)));
+      MG_CUDA(cudaMalloc(&p->d_colind, sizeof(int32_t)));
+      MG_CUDA(cudaMemsetAsync(p->d_rowptr, 0, sizeof(int32_t) * (nd + 1), st));
+      MG_CUDA(cudaStreamSynchronize(st));
+    }
+    return MG_OK;
+  }
   PatternBuffers d;
   MG_CUDA(cudaMalloc(&d.a, sizeof(unsigned long long) * n));
   MG_CUDA(cudaMalloc(&d.b, sizeof(unsigned long long) * n));

@@ -521,18 +521,23 @@ def test_gmsh_loaded_mesh_assembles(tmp_path):
 
 
 @pytest.mark.parametrize("order,rule", [(1, "lex"), (2, "lex"), (2, "first")])
-def test_reference_fixture_mignon3dC(order, rule):
-    """The reference's own unit-test cases on its mignon3dC.msh fixture (7 nodes,
+def test_reference_fixture_mignon3dC(order, rule, tmp_path):
+    """The reference's own unit-test cases on its mignon3dC.msh mesh (7 nodes,
     8 tets; tests/morganaIntegrator/integratorOEL3d_STDTest1.cpp: opEL3dA with
-    kappa = 12, tests/morganaFiniteElements/localMatrixEL3dTest1.cpp: kappa = 1),
-    loaded through the Gmsh reader and assembled on the GPU with every quadrature
-    card and operator, against the oracle."""
+    kappa = 12, tests/morganaFiniteElements/localMatrixEL3dTest1.cpp: kappa = 1):
+    the mesh from its fixture (tests/golden/mignon3dC.json) written back as a Gmsh 2
+    file, loaded through the Gmsh reader and assembled on the GPU with every
+    quadrature card and operator, against the oracle."""
     import json
     import os
     g = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "mignon3dC.json")))
     xyz = np.array(g["nodes"], dtype=np.float64)
     conn = np.array(g["tets_1based"], dtype=np.int32) - 1
-    mesh = mg.Mesh(xyz, conn, order=order, edge_rule=rule)
+    path = str(tmp_path / "mignon3dC.msh")
+    meshgen.write_gmsh(path, xyz, conn)
+    mesh = mg.Mesh.load_gmsh(path, order=order, edge_rule=rule)
+    gx, gc = mesh.geometry()
+    assert np.array_equal(gx, xyz) and np.array_equal(gc, conn)
     b = mg.MatrixBuilder(mesh)
     for op, coef in (("stiff_kappa", 12.0), ("stiff_kappa", 1.0), ("stiff_const", 12.0), ("mass", 1.0),
                      ("mass_coeff", 12.0)):
