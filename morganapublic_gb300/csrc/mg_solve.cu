@@ -122,6 +122,12 @@ static int row_group(const mg_plan* p)
   return row_group<V>(p->ndof, p->nnz);
 }
 
+// CTAs covering every row once (G lanes per row), for the standalone SpMV.
+static int spmv_full_grid(int64_t rows, int G)
+{
+  return (int)std::max<int64_t>(1, std::min<int64_t>((rows * G + kSolveThreads - 1) / kSolveThreads, INT32_MAX));
+}
+
 // CTAs of a row kernel with G lanes per row, at most `per_sm` per SM.
 static int row_blocks(int64_t rows, int G, int per_sm)
 {
@@ -621,7 +627,9 @@ mg_status launch_spmv(mg_plan* p, int prec, const void* vals, const void* x, voi
   if (!vals || !x || !y) return set_error(MG_ERR_INVALID_ARG, "mg_spmv: null argument");
   MG_TRY(plan_device(p));
   if (prec_is_f64(prec)) {
-    const int G = row_group<double>(p), nb = row_blocks<double>(p, G);
+    // FP64: a CTA for every 256 / G rows, no grid-stride loop (measured on GB300 at
+    // P1 128^3: 84.7 us against 88.7 us with 8 CTAs per SM and a grid-stride loop)
+    const int G = row_group<double>(p), nb = spmv_full_grid(p->ndof, G);
     if (p->d_coloff) {
       MG_DISPATCH_G(G, (launch_pdl(k_spmv<double, g, int16_t>, nb, kSolveThreads, st, p->ndof,
                                    (const int32_t*)p->d_rowptr, (const int16_t*)p->d_coloff, (const double*)vals,
