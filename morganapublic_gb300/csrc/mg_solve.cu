@@ -101,6 +101,10 @@ static int sm_count()
 }
 
 template <typename V> constexpr int kEntriesPerLane = sizeof(V) == 8 ? 16 : 8;
+// entries per lane and pass of the standalone SpMV: FP64 one lane per row 15 (the
+// interior rows of a P1 Kuhn mesh have 15 entries: one pass, no FMA wasted on an
+// empty 16th; measured at P1 128^3: 80.5 us against 84.6 us with 16)
+template <typename V, int G> constexpr int kSpmvEntries = (sizeof(V) == 8 && G == 1) ? 15 : kEntriesPerLane<V>;
 
 // Lanes per row of the standalone SpMV (measured on GB300 at P1 128^3 and P2
 // 48^3): FP64 one lane per row up to 16 entries on average (P1), two above
@@ -349,7 +353,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_spmv(int64_t n, const int32_t
   pdl_trigger();
   const int64_t groups = (int64_t)gridDim.x * (kSolveThreads / G);
   for (int64_t row = (blockIdx.x * (int64_t)kSolveThreads + threadIdx.x) / G; row < n; row += groups) {
-    const V s = row_dot<V, G, kEntriesPerLane<V>, I>(row, rp, ci, val, x);
+    const V s = row_dot<V, G, kSpmvEntries<V, G>, I>(row, rp, ci, val, x);
     if ((threadIdx.x & (G - 1)) == 0) y[row] = s;
   }
 }
