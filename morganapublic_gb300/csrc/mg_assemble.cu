@@ -278,18 +278,19 @@ template <>
 __device__ __forceinline__ float hi_of<double>(const double& v) { return (float)v; }
 
 // P1 stiffness needs the gradient of every vertex: the columns C_0..C_3 of the
-// cofactor matrix (gradients times det).  The common path takes C_1..C_3 from
-// the edge vectors at vertex 0 and C_0 = -(C_1 + C_2 + C_3) from the zero row
-// sums.  Two kinds of element take a rare path (p1_stiff_special):
-//  - |C_max| > 3 |C_0|: that sum cancels -- its error is eps |C_max|, which the
-//    entries of vertex 0 carry at a row scale of |C_0| |C_max| -- so C_0 is
-//    formed from the coordinates as (x3 - x1) x (x2 - x1), in the mode's
-//    arithmetic, and the entries of vertex 0 as dot products;
-//  - |C_max| > 8 |C_min| over all four: a cofactor is a 2x2 minor whose terms
-//    cancel by about that ratio, and the double-word (or FP32) rounding of its
-//    terms grows with it; the geometry is computed in FP64, as the reference's.
-// On a Kuhn cube jittered by 0.25 h (12.6 M tets, gradient ratios up to 21) the
-// first kind is ~1 % of the elements and the second ~0.01 %.
+// cofactor matrix (gradients times det).  C_1..C_3 come from the edge vectors at
+// vertex 0.  C_0:
+//  - FP32: formed for every element from the face opposite vertex 0,
+//    (x3 - x1) x (x2 - x1), accurate to its own magnitude -- cheap in FP32, and
+//    the zero-row-sum form C_0 = -(C_1 + C_2 + C_3) would cost eps |C_max| / |C_0|
+//    relative on the entries of vertex 0, too much at FP32's eps;
+//  - double-word: the zero-row-sum form (eps 2^-47).
+// Elements whose gradients differ by more than 8x (|C_max| > 8 |C_min| over all
+// four, or a cancelling determinant) take the rare path p1_stiff_special: a
+// cofactor is a 2x2 minor whose terms then cancel by about that ratio, and so does
+// the zero-row sum; the rare path computes the geometry in FP64 from the exact
+// coordinates, as the reference does.  On a Kuhn cube jittered by 0.25 h (12.6 M
+// tets, ratios up to 21) ~0.01 % of the elements are rare.
 enum { kP1Common = 0, kP1DirectC0 = 1, kP1Fp64 = 2 };
 
 template <typename T>
@@ -311,9 +312,7 @@ __device__ __forceinline__ int p1_class(const Cof<T>& f)
   }
   const float nmax = fmaxf(fmaxf(n[0], n[1]), fmaxf(n[2], n[3]));
   const float nmin = fminf(fminf(n[0], n[1]), fminf(n[2], n[3]));
-  if (nmax > 64.0f * nmin) return kP1Fp64;
-  if (nmax > 9.0f * n[0]) return kP1DirectC0;
-  return kP1Common;
+  return nmax > 64.0f * nmin ? kP1Fp64 : kP1Common;
 }
 
 // |det| small against its expansion terms
@@ -730,6 +729,7 @@ struct AsmArgs {
   const BlockDesc* blocks;
   const unsigned char* chunk_data;  // chunk records (layout at ChunkDesc)
   const int2* chunk_rec;            // (offset / 16, bytes) per chunk
+  const int64_t* chunk_wb;          // first contribution word of each chunk (n_chunks + 1; contiguous)
   const uint32_t* entries;
   const int2* row_meta;             // (accumulator base, CSR start - base) per owned row
   const double* coeff;   // per element, or null
@@ -905,12 +905,13 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
 
   if (warp == kConsumers / 32) {
     // ------------------------------------------------------------ producer
-    if (lane == 0) {
+    // Two lanes with independent waits: lane 0 takes the blocks and streams the
+    // contribution words and row metadata, lane 1 the chunk records.  Each runs
+    // up to NS (NW) chunks ahead of the consumers, across block boundaries, and
+    // waits only on the barrier of its own next copy; the word ranges and record
+    // places come from global tables, loaded ahead of those waits.
+    if (lane < 2) {
       constexpr int NW = kWordStages;
-      // record stages are refilled kRefillLag chunks behind the word copies, so
-      // that the producer does not wait for the consumers' phase 1 of the chunk
-      // whose words it has just issued before it moves on to the next chunk
-      constexpr int kRefillLag = NS - 1;
       int last_rec[NS], last_ent[NW], last_meta = -1;
       for (int s = 0; s < NS; ++s) last_rec[s] = -1;
       for (int s = 0; s < NW; ++s) last_ent[s] = -1;
@@ -918,17 +919,11 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
         if (!failed && !mbar_wait(&bars[k], (uint32_t)parity, a.wait_limit)) failed = true;
         return !failed;
       };
-      auto put_rec = [&](int q, int off16, int bytes) {  // record fill q
-        if (q >= NS && !wait(kBarRecEmpty + q % NS, (q / NS - 1) & 1)) return;
-        fence_proxy_async();
-        mbar_expect_tx(&bars[kBarRecFull + q % NS], (uint32_t)bytes);
-        bulk_g2s(stage_of(q), a.chunk_data + (int64_t)off16 * 16, (uint32_t)bytes, &bars[kBarRecFull + q % NS]);
-        last_rec[q % NS] = q;
-      };
       int q = 0;
       for (int j = 0;; ++j) {
-        const int b = (int)atomicAdd(&a.counters[0], 1u);
-        if (j >= 2 && !wait(kBarBlkEmpty + (j & 1), ((j >> 1) - 1) & 1)) break;
+        int b = 0;
+        if (lane == 0) b = (int)atomicAdd(&a.counters[0], 1u);
+        b = __shfl_sync(0x3u, b, 0);
         BlockDesc d;
         if (b < a.nblocks) {
           d = a.blocks[b];
@@ -936,51 +931,57 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
           d = BlockDesc{};
           d.nchunks = -1;  // no more blocks
         }
-        sblk[j & 1] = d;
-        mbar_arrive(&bars[kBarBlkFull + (j & 1)]);
-        if (d.nchunks < 0) break;
-        const int n = d.nchunks;
-        int2 r0[NS];
-        for (int c = 0; c < n && c < NS; ++c) r0[c] = a.chunk_rec[d.chunk_begin + c];
-        for (int c = 0; c < n && c < NS; ++c) put_rec(q + c, r0[c].x, r0[c].y);
-        for (int c = 0; c < n && !failed; ++c) {
-          const int qq = q + c;
-          if (!wait(kBarRecFull + qq % NS, (qq / NS) & 1)) break;
-          const ChunkDesc* cd = desc_of(qq);
-          if (qq >= NW && !wait(kBarEntEmpty + qq % NW, (qq / NW - 1) & 1)) break;
-          const uint32_t bytes = (uint32_t)cd->warp_off[kWarps] * 4u;
-          fence_proxy_async();
-          mbar_expect_tx(&bars[kBarEntFull + qq % NW], bytes);
-          if (bytes) bulk_g2s(sent + (qq % NW) * went, a.entries + cd->word_begin, bytes, &bars[kBarEntFull + qq % NW]);
-          last_ent[qq % NW] = qq;
-          // record cr + NS goes into record cr's stage (cr = c - kRefillLag) once
-          // the consumers release it; its place is in record cr, which nothing has
-          // overwritten yet.  Every cr < n - NS comes up, as kRefillLag < NS.
-          const int cr = c - kRefillLag;
-          if (cr >= 0 && cr + NS < n) {
-            const int qr = q + cr;
-            if (!wait(kBarRecEmpty + qr % NS, (qr / NS) & 1)) break;
-            const ChunkDesc* crd = desc_of(qr);
-            const int off16 = crd->next_off16, nb = crd->next_bytes;
-            fence_proxy_async();
-            mbar_expect_tx(&bars[kBarRecFull + qr % NS], (uint32_t)nb);
-            bulk_g2s(stage_of(qr), a.chunk_data + (int64_t)off16 * 16, (uint32_t)nb, &bars[kBarRecFull + qr % NS]);
-            last_rec[qr % NS] = qr + NS;
+        if (lane == 0) {
+          if (j >= 2 && !wait(kBarBlkEmpty + (j & 1), ((j >> 1) - 1) & 1)) d.nchunks = -1;
+          if (!failed) {
+            sblk[j & 1] = d;
+            mbar_arrive(&bars[kBarBlkFull + (j & 1)]);
           }
         }
+        if (__any_sync(0x3u, failed) || d.nchunks < 0) {
+          failed = __any_sync(0x3u, failed);
+          break;
+        }
+        const int n = d.nchunks;
+        if (lane == 1) {
+          // records: chunk c into stage (q + c) % NS once chunk q + c - NS is released
+          for (int c = 0; c < n; ++c) {
+            const int qq = q + c;
+            const int2 r = a.chunk_rec[d.chunk_begin + c];  // lands during the wait
+            if (qq >= NS && !wait(kBarRecEmpty + qq % NS, (qq / NS - 1) & 1)) break;
+            fence_proxy_async();
+            mbar_expect_tx(&bars[kBarRecFull + qq % NS], (uint32_t)r.y);
+            bulk_g2s(stage_of(qq), a.chunk_data + (int64_t)r.x * 16, (uint32_t)r.y, &bars[kBarRecFull + qq % NS]);
+            last_rec[qq % NS] = qq;
+          }
+        } else {
+          // words: chunk c into stage (q + c) % NW once chunk q + c - NW is released
+          for (int c = 0; c < n; ++c) {
+            const int qq = q + c;
+            const int64_t w0 = a.chunk_wb[d.chunk_begin + c], w1 = a.chunk_wb[d.chunk_begin + c + 1];
+            if (qq >= NW && !wait(kBarEntEmpty + qq % NW, (qq / NW - 1) & 1)) break;
+            const uint32_t bytes = (uint32_t)(w1 - w0) * 4u;
+            fence_proxy_async();
+            mbar_expect_tx(&bars[kBarEntFull + qq % NW], bytes);
+            if (bytes) bulk_g2s(sent + (qq % NW) * went, a.entries + w0, bytes, &bars[kBarEntFull + qq % NW]);
+            last_ent[qq % NW] = qq;
+          }
+          // the block's row metadata: rows row_begin .. row_begin + row_count and
+          // the row after, 16-byte aligned
+          if (!failed && (j == 0 || wait(kBarMetaEmpty, (j - 1) & 1))) {
+            const int i0 = d.row_begin & ~1, i1 = (d.row_begin + d.row_count + 2) & ~1;
+            fence_proxy_async();
+            mbar_expect_tx(&bars[kBarMetaFull], (uint32_t)(i1 - i0) * 8u);
+            bulk_g2s(smeta, a.row_meta + i0, (uint32_t)(i1 - i0) * 8u, &bars[kBarMetaFull]);
+            last_meta = j;
+          }
+        }
+        failed = __any_sync(0x3u, failed);
         if (failed) break;
         q += n;
-        // the block's row metadata: rows row_begin .. row_begin + row_count and
-        // the row after, 16-byte aligned
-        if (j >= 1 && !wait(kBarMetaEmpty, (j - 1) & 1)) break;
-        const int i0 = d.row_begin & ~1, i1 = (d.row_begin + d.row_count + 2) & ~1;
-        fence_proxy_async();
-        mbar_expect_tx(&bars[kBarMetaFull], (uint32_t)(i1 - i0) * 8u);
-        bulk_g2s(smeta, a.row_meta + i0, (uint32_t)(i1 - i0) * 8u, &bars[kBarMetaFull]);
-        last_meta = j;
       }
       if (failed) {
-        // let the copies in flight land before the CTA's shared memory goes away
+        // let this lane's copies in flight land before the CTA's shared memory goes away
         for (int s = 0; s < NS; ++s)
           if (last_rec[s] >= 0) mbar_wait(&bars[kBarRecFull + s], (uint32_t)((last_rec[s] / NS) & 1), kWaitLimit);
         for (int s = 0; s < NW; ++s)
@@ -1098,6 +1099,13 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
               if (special) {  // queued for the pass below
                 int* cnt = reinterpret_cast<int*>(sgeo);
                 reinterpret_cast<uint16_t*>(cnt + 1)[atomicAdd(cnt, 1)] = (uint16_t)(local | cls << 12);
+              } else if constexpr (MODE == kF32) {
+                // FP32: C_0 from the edges of the face opposite vertex 0, every element
+                FetchAbs F;
+                fetch_staged<false>(staged_verts(), item_lconn(local), F);
+                T C0[3];
+                staged_c0(F, C0);
+                p1_stiff_direct<T>(f, C0, coef * wsum / f.det, K);
               } else {
                 const T sc = coef * wsum / f.det;
                 p1_stiff_unique<T>(f, sc, K);
@@ -1316,6 +1324,7 @@ mg_status launch_assemble(mg_plan* p, int op, const double* d_coeff, double c, i
   a.blocks = p->d_blocks;
   a.chunk_data = p->d_chunk_data;
   a.chunk_rec = p->d_chunk_rec;
+  a.chunk_wb = p->d_chunk_wb;
   a.entries = p->d_entries;
   a.row_meta = p->d_row_meta;
   a.coeff = needs_coeff ? d_coeff : nullptr;

@@ -113,7 +113,8 @@ struct ChunkDesc {
   int32_t warp_off[kWarps + 1];  // per-warp offsets relative to word_begin; [kWarps] = chunk size
   int32_t n_nodes;            // distinct vertices of the chunk's elements (multiple of 4)
   int32_t next_off16;         // record of chunk + kRecStages of the same block: offset / 16
-  int32_t next_bytes;         //   and size (0 when the block has no such chunk)
+  int32_t next_bytes;         //   and size (0 when the block has no such chunk); the
+                              //   kernel takes record places from the chunk table
   int32_t pad[2];
 };
 static_assert(sizeof(ChunkDesc) == 64, "ChunkDesc must stay 64 bytes");
@@ -180,6 +181,7 @@ struct mg_plan {
   mg::BlockDesc* d_blocks = nullptr;
   unsigned char* d_chunk_data = nullptr;  // chunk records (see ChunkDesc), 16-byte aligned
   int2* d_chunk_rec = nullptr;            // (offset / 16, bytes) of each chunk record
+  int64_t* d_chunk_wb = nullptr;          // first contribution word of each chunk (n_chunks + 1)
   int32_t max_rec_bytes = 0;
   int32_t max_chunk_nodes = 0;
   int2* d_row_meta = nullptr;  // owned rows, schedule order: (accumulator base, CSR start - base)

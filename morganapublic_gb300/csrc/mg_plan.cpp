@@ -688,6 +688,11 @@ mg_status plan_device(mg_plan* p)
     }
     MG_TRY(upload(&p->d_chunk_data, data));
     MG_TRY(upload(&p->d_chunk_rec, rec));
+    // first word of each chunk (chunks are contiguous in the word array)
+    std::vector<int64_t> wb(nc + 1, 0);
+    for (int64_t ck = 0; ck < nc; ++ck) wb[ck] = hs.chunk_ptr[ck * (kWarps + 1)];
+    wb[nc] = (int64_t)hs.entries.size();
+    MG_TRY(upload(&p->d_chunk_wb, wb));
     if (maxb != p->max_rec_bytes) return set_error(MG_ERR_SIZE, "chunk record size mismatch");
   }
   MG_TRY(upload(&p->d_counters, std::vector<uint32_t>(8, 0u)));
@@ -709,6 +714,7 @@ static void free_plan(mg_plan* p)
   cudaFree(p->d_blocks);
   cudaFree(p->d_chunk_data);
   cudaFree(p->d_chunk_rec);
+  cudaFree(p->d_chunk_wb);
   cudaFree(p->d_row_meta);
   cudaFree(p->d_sched_rows);
   cudaFree(p->d_elem_order);

@@ -904,10 +904,11 @@ mg_status build_schedule_device(mg_plan* p, cudaStream_t st)
   p->d_row_meta = d_meta;
   p->d_chunk_data = d_records;
   p->d_chunk_rec = d_rec;
+  p->d_chunk_wb = d_word_begin;
   p->d_counters = d_counters;
   p->d_sched_rows = rows;
   for (void* q : {(void*)rows, (void*)d_diag, (void*)d_blocks, (void*)d_entries, (void*)d_elem_order, (void*)d_dm, (void*)d_meta,
-                  (void*)d_records, (void*)d_rec, (void*)d_counters})
+                  (void*)d_records, (void*)d_rec, (void*)d_word_begin, (void*)d_counters})
     B.keep(q);
   if (p->d_coloff) B.keep(d_coloff);
   p->nblocks = nbk;
