@@ -286,7 +286,7 @@ __device__ __forceinline__ float hi_of<double>(const double& v) { return (float)
 //    relative on the entries of vertex 0, too much at FP32's eps;
 //  - double-word: the zero-row-sum form (eps 2^-47).
 // Elements whose gradients differ by more than 8x (|C_max| > 8 |C_min| over all
-// four, or a cancelling determinant) take the rare path p1_stiff_special: a
+// four, or a cancelling determinant) take the rare path staged_rare_geometry: a
 // cofactor is a 2x2 minor whose terms then cancel by about that ratio, and so does
 // the zero-row sum; the rare path computes the geometry in FP64 from the exact
 // coordinates, as the reference does.  On a Kuhn cube jittered by 0.25 h (12.6 M
@@ -644,46 +644,37 @@ __device__ __forceinline__ void p1_stiff_direct<ff>(const Cof<ff>& f, const ff C
   K[9] = ff_mul(s, ff_dot3(col[2], col[2]));
 }
 
-// The rare path of the P1 stiffness (p1_class != kP1Common), out of line: it
-// re-reads the item's vertices from the staged record, recomputes the element
-// and writes its 10 unique entries (out[u * stride]) itself, so that no register
-// of the common path is passed by address.  coef is the element's coefficient
-// and wsum the card's weight sum, as doubles.  Records an out-of-range
-// double-word scale in *flags, as the common path does.
+// The rare P1 stiffness elements (p1_class): their geometry in FP64 from the exact
+// staged coordinates, C_0 from its own face, returned by value (out of line, and
+// no register of the caller is passed by address, so the common path keeps its
+// registers).
+template <typename T>
+struct RareK {
+  T K[10];
+};
 template <int MODE>
-static __device__ __noinline__ void p1_stiff_special(StagedVerts v, ushort4 lc, int cls, double coef, double wsum,
-                                                     typename Arith<MODE>::T* out, int stride, uint32_t* flags)
+static __device__ __noinline__ RareK<typename Arith<MODE>::T> staged_rare_stiffness(StagedVerts v, ushort4 lc,
+                                                                                   double coef, double wsum,
+                                                                                   uint32_t* flags)
 {
-  using A = Arith<MODE>;
-  using T = typename A::T;
+  using T = typename Arith<MODE>::T;
   FetchAbs F;
   fetch_staged<true>(v, lc, F);
+  Cof<double> d;
+  geometry_fp64(F, d);
+  double c0[3];
+  staged_c0(F, c0);
   Cof<T> f;
-  T C0[3], s;
-  if (MODE == kF64 || cls == kP1Fp64) {
-    Cof<double> d;
-    geometry_fp64(F, d);
-    double c0[3];
-    staged_c0(F, c0);
-    store_geometry(d, f);
+  store_geometry(d, f);
+  T C0[3];
 #pragma unroll
-    for (int r = 0; r < 3; ++r) C0[r] = from_double<T>(c0[r]);
-    s = from_double<T>(coef * wsum / d.det);
-  } else {
-    if (geometry_staged(F, f)) {  // a cancelling determinant as well
-      Cof<double> d;
-      geometry_fp64(F, d);
-      store_geometry(d, f);
-    }
-    staged_c0(F, C0);
-    s = A::from(coef) * A::from(wsum) / f.det;
-  }
-  T K[10];
-  p1_stiff_direct<T>(f, C0, s, K);
+  for (int k = 0; k < 3; ++k) C0[k] = from_double<T>(c0[k]);
+  const T s = Arith<MODE>::from(coef) * Arith<MODE>::from(wsum) / f.det;
+  RareK<T> r;
+  p1_stiff_direct<T>(f, C0, s, r.K);
   if constexpr (MODE == kDW)
-    if (!dw_scale_ok(s) || !dw_scale_ok(K[4])) atomicOr(flags, 2u);
-#pragma unroll
-  for (int u = 0; u < 10; ++u) out[u * stride] = K[u];
+    if (!dw_scale_ok(s) || !dw_scale_ok(r.K[4])) atomicOr(flags, 2u);
+  return r;
 }
 
 // The six scaled metric coefficients s (C_a . C_b), ab = 00,11,22,01,02,12.
@@ -786,9 +777,8 @@ struct AsmLayout {
   static constexpr size_t blk_bytes = 2 * sizeof(BlockDesc);
   static constexpr size_t off_buf = acc_bytes;
   static constexpr size_t off_tab = off_buf + kGroups * buf_bytes;
-  // per group: P2 the 6 scale factors of each item of a chunk (computed once per
-  // item); P1 the chunk's rare stiffness items (a count, then item | class << 12)
-  static constexpr size_t geo_bytes = ORDER == 2 ? align16(sizeof(T) * CI * 6) : align16(4 + 2 * CI);
+  // P2: per group, the 6 scale factors of each item of a chunk (computed once per item)
+  static constexpr size_t geo_bytes = ORDER == 2 ? align16(sizeof(T) * CI * 6) : 0;
   static constexpr size_t off_geo = off_tab + tab_bytes;
   static constexpr size_t off_meta = off_geo + kGroups * geo_bytes;
   static constexpr size_t off_blk = off_meta + meta_bytes;
@@ -888,7 +878,6 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
   if (tid == 0) {
     for (int g = 0; g < kGroups; ++g) {
       reinterpret_cast<T*>(smem + L::off_buf + g * L::buf_bytes)[NU * CI] = A::zero();
-      if (ORDER == 1) *reinterpret_cast<int*>(smem + L::off_geo + g * L::geo_bytes) = 0;
     }
     for (int k = 0; k < kNumBars; ++k) {
       uint32_t count = 1;
@@ -1094,11 +1083,17 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
               // the rare elements (p1_class, or a cancelling determinant) go out of
               // line, entered only when a lane of the warp has one; that path
               // writes its entries itself
-              const int cls = degenerate ? (int)kP1Fp64 : p1_class<T>(f);
-              special = cls != kP1Common;
-              if (special) {  // queued for the pass below
-                int* cnt = reinterpret_cast<int*>(sgeo);
-                reinterpret_cast<uint16_t*>(cnt + 1)[atomicAdd(cnt, 1)] = (uint16_t)(local | cls << 12);
+              const bool rare = degenerate || p1_class<T>(f) != kP1Common;
+              // entered only when a lane of the warp has one (~0.01 % of the elements)
+              if (__any_sync(__activemask(), rare)) {
+                if (rare) {
+                  const RareK<T> rk =
+                      staged_rare_stiffness<MODE>(staged_verts(), item_lconn(local), coef_d, a.wsum, &a.counters[4]);
+#pragma unroll
+                  for (int u = 0; u < 10; ++u) K[u] = rk.K[u];
+                }
+              }
+              if (rare) {
               } else if constexpr (MODE == kF32) {
                 // FP32: C_0 from the edges of the face opposite vertex 0, every element
                 FetchAbs F;
@@ -1121,22 +1116,6 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
 #pragma unroll
               for (int u = 0; u < 10; ++u) buf[u * CI + local] = K[u];
             }
-          }
-          if (a.stiff) {
-            // the chunk's rare stiffness elements (p1_class: ~1 % on a 0.25 h jittered
-            // cube), one per thread after a group barrier, so that no warp runs the
-            // long path for one lane; each writes its own entries
-            failed = group_sync_or(g, failed);
-            const int* cnt = reinterpret_cast<const int*>(sgeo);
-            const int ns = *cnt;
-            if (!failed)
-              for (int k = gtid; k < ns; k += kThreads) {
-                const int v = reinterpret_cast<const uint16_t*>(cnt + 1)[k], it = v & 0xfff;
-                const int e = reinterpret_cast<const int32_t*>(stage_of(qq) + sizeof(ChunkDesc))[it];
-                const double coef_d = a.coeff ? __ldg(a.coeff + e) : a.cconst;
-                p1_stiff_special<MODE>(staged_verts(), item_lconn(it), v >> 12, coef_d, a.wsum, buf + it, CI,
-                                       &a.counters[4]);
-              }
           }
         } else {
           // P2: the first warp of the group computes each item's scale factors
@@ -1174,10 +1153,7 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
           }
         }
         failed = group_sync_or(g, failed);
-        if (gtid == 0) {
-          mbar_arrive(&bars[kBarRecEmpty + qq % NS]);
-          if (ORDER == 1) *reinterpret_cast<int*>(sgeo) = 0;  // read by everyone before the barrier
-        }
+        if (gtid == 0) mbar_arrive(&bars[kBarRecEmpty + qq % NS]);
         // ---- phase 2: segmented sums into owned slots.  Pieces of PW words of
         // one slot are summed in registers and update the slot once; within a
         // chunk every slot belongs to one thread, and the token orders the
