@@ -199,7 +199,7 @@ typedef struct {
   int64_t n_item_slots;      /* length of the exported item array (padding included) */
   int64_t max_chunk_entries; /* words of the largest chunk (its shared-memory staging buffer) */
   int64_t max_chunk_vertices;     /* distinct vertices of the largest chunk (padded to 4) */
-  int64_t max_chunk_record_bytes; /* largest chunk record: element ids, local vertex indices,
+  int64_t max_chunk_record_bytes; /* largest chunk record: element ranks, local vertex indices,
                                      vertex coordinates (its shared-memory stage) */
 } mg_schedule_info;
 
@@ -227,7 +227,10 @@ mg_status mg_plan_export_schedule(const mg_plan* plan, int32_t* h_blocks, int32_
    double for MG_F64 or float for MG_F32).  coeff: per-element kappa (device,
    n_elements doubles) for MG_OP_STIFF_KAPPA / MG_OP_MASS_COEFF, else ignored;
    c: the constant of MG_OP_STIFF_CONST.  Deterministic: the same inputs give
-   the same bits on every call.
+   the same bits on every call.  Two assemblies on one plan must not overlap on
+   the GPU (other streams): the plan holds the kernel's work counter and a copy
+   of the coefficient in its element order (allocated by the first call that
+   takes a coefficient -- make that call before any stream capture).
    Replaces: the value half of matrixBuilder<localMatrixEL3d<...>>::buildEpetraCrs
    (traitsMatrixBuilder.hpp:363-441) with integratorOEL3d_STD::integration
    (src/morganaIntegrator/integratorOEL3d_STD.hpp:106-137). */

@@ -5,7 +5,7 @@
 // k_assemble is a persistent kernel: each CTA repeatedly takes the next block of
 // rows (an integer work counter) and, for every chunk of the block's elements,
 //   stage    a bulk copy (cp.async.bulk, completion on an mbarrier) brings the
-//            chunk's element nodes and element ids into shared memory while the
+//            chunk's element nodes and element ranks into shared memory while the
 //            previous chunk is reduced, and the chunk's contribution words while
 //            its element matrices are computed;
 //   phase 1  one thread per P1 element (eight per P2 element) computes the
@@ -723,7 +723,7 @@ struct AsmArgs {
   const int64_t* chunk_wb;          // first contribution word of each chunk (n_chunks + 1; contiguous)
   const uint32_t* entries;
   const int2* row_meta;             // (accumulator base, CSR start - base) per owned row
-  const double* coeff;   // per element, or null
+  const double* coeff;   // per element in Morton order (indexed by the records' ranks), or null
   double cconst;         // used when coeff is null
   const double* tables;  // unique-entry tables: stiff[6][nu] then mass[nu]
   double wsum;
@@ -1031,8 +1031,8 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
         // rare path); returns whether it is one.
         auto item_geometry = [&](int it, Cof<T>& f, T& coef, double& coef_d, bool defer) {
           const unsigned char* rb = stage_of(qq);
-          const int e = reinterpret_cast<const int32_t*>(rb + sizeof(ChunkDesc))[it];
-          coef_d = a.coeff ? __ldg(a.coeff + e) : a.cconst;  // latency covered by the geometry
+          const int rk = reinterpret_cast<const int32_t*>(rb + sizeof(ChunkDesc))[it];
+          coef_d = a.coeff ? __ldg(a.coeff + rk) : a.cconst;  // latency covered by the geometry
           const ushort4 lc = item_lconn(it);
           const StagedVerts sv = staged_verts();
           const bool need = geometry_staged_lazy<MODE>(sv, lc, f);
@@ -1280,6 +1280,16 @@ static mg_status launch_assemble_t(AsmArgs a, cudaStream_t st)
   return MG_OK;
 }
 
+// The coefficient in the plan's Morton element order: a chunk's items are
+// consecutive ranks of one block, so the assembly reads it in runs (its elements
+// are neighbours; the caller's element order may be arbitrary).
+__global__ void __launch_bounds__(256) k_coeff_morton(int64_t n_elem, const int32_t* __restrict__ elem_order,
+                                                      const double* __restrict__ coeff, double* __restrict__ out)
+{
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r < n_elem) out[r] = __ldg(coeff + elem_order[r]);
+}
+
 mg_status launch_assemble(mg_plan* p, int op, const double* d_coeff, double c, int quad, int prec,
                           void* d_values, cudaStream_t st)
 {
@@ -1303,7 +1313,17 @@ mg_status launch_assemble(mg_plan* p, int op, const double* d_coeff, double c, i
   a.chunk_wb = p->d_chunk_wb;
   a.entries = p->d_entries;
   a.row_meta = p->d_row_meta;
-  a.coeff = needs_coeff ? d_coeff : nullptr;
+  a.coeff = nullptr;
+  if (needs_coeff) {
+    {
+      std::lock_guard<std::mutex> lock(p->upload_mu);
+      if (!p->d_coeff_m) MG_CUDA(cudaMalloc(&p->d_coeff_m, sizeof(double) * m->n_elem));
+    }
+    k_coeff_morton<<<(unsigned)((m->n_elem + 255) / 256), 256, 0, st>>>(m->n_elem, p->d_elem_order, d_coeff,
+                                                                        p->d_coeff_m);
+    MG_CUDA(cudaGetLastError());
+    a.coeff = p->d_coeff_m;
+  }
   a.cconst = op == MG_OP_STIFF_CONST ? c : 1.0;
   a.tables = d_tab;
   a.wsum = t->wsum;

@@ -101,7 +101,9 @@ struct BlockDesc {
 
 // Head of a chunk record.  The plan lays out, per chunk, one contiguous record
 // the kernel stages into shared memory with a single bulk copy:
-//   ChunkDesc (64 B) | element ids (4 B x n4) | local vertex indices (4 x 2 B x n4)
+//   ChunkDesc (64 B) | the items' element Morton ranks (4 B x n4; the kernel
+//   reads each element's coefficient from a copy in that order)
+//   | local vertex indices (4 x 2 B x n4)
 //   | vertex coordinates relative to the chunk's first vertex, split exactly
 //     r = hi + mid + lo: float4 (hi.xyz, mid.x) x nn | float4 (mid.yz, lo.xy) x nn
 //     | float lo.z x nn
@@ -187,6 +189,7 @@ struct mg_plan {
   int2* d_row_meta = nullptr;  // owned rows, schedule order: (accumulator base, CSR start - base)
   int32_t* d_sched_rows = nullptr;  // device-built schedules: the owned rows (for the schedule export)
   int32_t* d_elem_order = nullptr;  // elements along a Morton curve of their centroids
+  double* d_coeff_m = nullptr;      // the coefficient of the current assembly in that order (n_elem)
   int32_t* d_dofs_morton = nullptr; // their dofs (nb each) in that order
   uint32_t* d_entries = nullptr;   // contribution words
   uint32_t* d_counters = nullptr;   // [0] work counter, [1] exit counter, [2] device error, [3] detail

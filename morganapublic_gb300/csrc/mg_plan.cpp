@@ -546,10 +546,10 @@ static mg_status build_schedule(mg_plan* p, HostSchedule* hs)
     for (size_t k = 0; k < cptr[b].size(); ++k) hs->chunk_ptr[ck * (kWarps + 1) + k] = cptr[b][k] + boff[b];
     std::vector<uint32_t>().swap(ent[b]);
   }
-  // blocks taken largest first (the work counter hands them out in array
-  // order), so the last ones to start are the shortest
-  std::stable_sort(hs->blocks.begin(), hs->blocks.end(),
-                   [](const BlockDesc& x, const BlockDesc& y) { return x.nchunks > y.nchunks; });
+  // blocks stay in Morton order of their rows (the work counter hands them out
+  // in array order): the blocks in flight at one time are neighbours, so the
+  // coefficients of the elements they share are read from L2; the cut by
+  // weight makes them nearly equal, so no longest-first order is needed
   p->nblocks = nbk;
   p->n_items = 0;
   for (int32_t b = 0; b < nbk; ++b) p->n_items += hs->blocks[b].item_count;
@@ -646,6 +646,8 @@ mg_status plan_device(mg_plan* p)
     for (int64_t ck = 0; ck < nc; ++ck) rec[ck] = make_int2((int32_t)(off[ck] / 16), (int32_t)(off[ck + 1] - off[ck]));
     std::vector<unsigned char> data(std::max<int64_t>(off[nc], 16), 0);
     const std::vector<double>& xyz = p->mesh->xyz;
+    std::vector<int32_t> rank_of(hs.elem_order.size());
+    for (size_t i = 0; i < hs.elem_order.size(); ++i) rank_of[hs.elem_order[i]] = (int32_t)i;
 #pragma omp parallel for schedule(dynamic, 16)
     for (int64_t ck = 0; ck < nc; ++ck) {
       unsigned char* r = data.data() + off[ck];
@@ -663,7 +665,12 @@ mg_status plan_device(mg_plan* p)
       }
       std::memcpy(r, &cd, sizeof cd);
       const int64_t first = (int64_t)d.item_begin + (int64_t)c * CI;
-      std::memcpy(r + 64, &hs.items[first], 4 * n4);
+      // the items' Morton ranks (the kernel reads the coefficient in that order)
+      int32_t* ranks = reinterpret_cast<int32_t*>(r + 64);
+      for (int64_t i = 0; i < n4; ++i) {
+        const int32_t e = hs.items[first + i];
+        ranks[i] = e >= 0 ? rank_of[e] : -1;
+      }
       std::memcpy(r + 64 + 4 * n4, &hs.item_lconn[4 * first], 8 * n4);
       float4* va = reinterpret_cast<float4*>(r + 64 + 12 * n4);
       float4* vb = reinterpret_cast<float4*>(r + 64 + 12 * n4 + 16 * nn);
@@ -718,6 +725,7 @@ static void free_plan(mg_plan* p)
   cudaFree(p->d_row_meta);
   cudaFree(p->d_sched_rows);
   cudaFree(p->d_elem_order);
+  cudaFree(p->d_coeff_m);
   cudaFree(p->d_dofs_morton);
   cudaFree(p->d_rhs_ptr);
   cudaFree(p->d_rhs_slot);
@@ -868,7 +876,12 @@ static mg_status export_device_schedule(const mg_plan* p, int32_t* h_blocks, int
         if (h_chunk_ptr)
           for (int w = 0; w <= kWarps; ++w) h_chunk_ptr[ck * (kWarps + 1) + w] = cd.word_begin + cd.warp_off[w];
         const int n4 = (std::min(CI, d.item_count - c * CI) + 3) & ~3;
-        if (h_items) std::memcpy(h_items + d.item_begin + (int64_t)c * CI, r + sizeof(ChunkDesc), 4 * (size_t)n4);
+        if (h_items) {
+          // the records hold Morton ranks: back to element ids
+          const int32_t* rk = reinterpret_cast<const int32_t*>(r + sizeof(ChunkDesc));
+          int32_t* out = h_items + d.item_begin + (int64_t)c * CI;
+          for (int64_t i = 0; i < n4; ++i) out[i] = rk[i] >= 0 ? p->h_elem_order[rk[i]] : -1;
+        }
       }
   }
   return MG_OK;

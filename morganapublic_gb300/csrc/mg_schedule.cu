@@ -285,6 +285,7 @@ __device__ int cta_scan(int* a, int n, int* tmp /* blockDim.x + 1 */)
 struct ChunkArgs {
   int order, nb, CI, nu;
   const int32_t* items;        // padded per-block item lists
+  const int32_t* rank;         // Morton rank of each element
   const int32_t* item_begin;   // per block
   const int32_t* item_count;   // per block
   const int32_t* nchunks;      // per block
@@ -486,7 +487,7 @@ __global__ void __launch_bounds__(kSchedThreads) k_chunk(ChunkArgs A)
     }
     int32_t* ids = reinterpret_cast<int32_t*>(rec + sizeof(ChunkDesc));
     uint16_t* lc = reinterpret_cast<uint16_t*>(rec + sizeof(ChunkDesc) + 4 * n4);
-    for (int i = t; i < n4; i += T) ids[i] = it_ids[i];  // the padded lists hold -1 past the items
+    for (int i = t; i < n4; i += T) ids[i] = it_ids[i] >= 0 ? A.rank[it_ids[i]] : -1;  // -1 past the items
     for (int p = t; p < 4 * n4; p += T) lc[p] = p < 4 * n_items ? S.local_of[p] : (uint16_t)0;
     float4* va = reinterpret_cast<float4*>(rec + sizeof(ChunkDesc) + 12 * n4);
     float4* vb = reinterpret_cast<float4*>(rec + sizeof(ChunkDesc) + 12 * n4 + 16 * nn);
@@ -791,7 +792,7 @@ mg_status build_schedule_device(mg_plan* p, cudaStream_t st)
   // ---- 5. per chunk: pass 1 (counts), host scans, pass 2 (records and words)
   ChunkArgs A{};
   A.order = order, A.nb = nb, A.CI = CI, A.nu = nu;
-  A.items = d_items, A.item_begin = d_item_begin, A.item_count = bcount, A.nchunks = d_nchunks;
+  A.items = d_items, A.rank = rank, A.item_begin = d_item_begin, A.item_count = bcount, A.nchunks = d_nchunks;
   A.cblk = cblk, A.cpos = cpos;
   A.conn = m->d_conn, A.dofs = m->d_dofs, A.block_of = block_of, A.row_acc_of = row_acc_of;
   A.rowptr = p->d_rowptr, A.colind = p->d_colind, A.xyz = m->d_xyz;
@@ -846,7 +847,7 @@ mg_status build_schedule_device(mg_plan* p, cudaStream_t st)
     h_rec[ck] = make_int2((int32_t)(rec_off[ck] / 16), (int32_t)(rec_off[ck + 1] - rec_off[ck]));
   int2* d_rec;
   MG_TRY(upload_to(B, &d_rec, h_rec, st));
-  // ---- blocks, largest first (stable), on the host
+  // ---- block descriptors, in Morton order of their rows (as the host builder)
   std::vector<BlockDesc> blocks(nbk);
   {
     std::vector<int32_t> h_accex;
@@ -864,8 +865,6 @@ mg_status build_schedule_device(mg_plan* p, cudaStream_t st)
       d.acc_used = h_accex[r1] - h_accex[h_bstart[b]];
       d.word_begin32 = (int32_t)(word_begin[h_chunk_begin[b]] / 32);
     }
-    std::stable_sort(blocks.begin(), blocks.end(),
-                     [](const BlockDesc& x, const BlockDesc& y) { return x.nchunks > y.nchunks; });
   }
   BlockDesc* d_blocks;
   MG_TRY(upload_to(B, &d_blocks, blocks, st));
