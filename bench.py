@@ -849,8 +849,8 @@ def main():
             e2e_cold = {"value": world * E / tc, "unit": "tets/s", "ms_per_step": tc * 1e3,
                         "runs_s": ts, "h2d_bytes_per_step": 24 * N + 16 * E + 8 * E + 8 * ndof,
                         "d2h_bytes_per_step": d2h,
-                        "note": "from host arrays: mg_mesh_create + mg_pattern_build_device (CSR pattern on the GPU, "
-                                "assembly schedule on the host) + first mg_assemble (plan upload) + "
+                        "note": "from host arrays: mg_mesh_create + mg_pattern_build_device (CSR pattern and assembly "
+                                "schedule built on the GPU) + first mg_assemble + "
                                 f"{N_SPMV} SpMV, values and y copied back; wall clock, mean of 2 -- the work one "
                                 "step of the reference arm does"}
 
@@ -875,7 +875,7 @@ def main():
                               "SpMV in native FP64; assembly_f64_native gives the native-FP64 assembly",
                 "data": "synthetic (seeded Kuhn cube, jitter, element permutation, lognormal kappa)",
                 "config": workload_config(a, E, N, nnz), "roofline": roofline, "cpu_baseline": cpu_base,
-                "e2e": e2e, "e2e_cold": e2e_cold, "gpu_launches": a.steps * (1 + N_SPMV),
+                "e2e": e2e, "e2e_cold": e2e_cold, "gpu_launches": a.steps * (2 + N_SPMV),  # coefficient gather + assembly + SpMVs
                 "clocks": clocks, "wall_s_timed": t_wall, "kernels": extras}
     if world > 1:
         dist.barrier()

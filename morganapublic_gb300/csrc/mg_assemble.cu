@@ -72,7 +72,13 @@ template <> struct Arith<kF32> {
   using T = float;
   __device__ static void sum_into(T& s, T x) { s += x; }
   using Out = float;
-  __device__ static T from(double x) { return (float)x; }
+  // double -> float by integer operations (the conversion instruction runs on
+  // the FP64 pipe): hi + lo of the double-word split, rounded once
+  __device__ static T from(double x)
+  {
+    const ff t = ff_from_double_bits(x);
+    return __fadd_rn(t.hi, t.lo);
+  }
   __device__ static T zero() { return 0.0f; }
   __device__ static Out out(T v) { return v; }
 };
@@ -286,12 +292,12 @@ __device__ __forceinline__ float hi_of<double>(const double& v) { return (float)
 //    relative on the entries of vertex 0, too much at FP32's eps;
 //  - double-word: the zero-row-sum form (eps 2^-47).
 // Elements whose gradients differ by more than 8x (|C_max| > 8 |C_min| over all
-// four, or a cancelling determinant) take the rare path staged_rare_geometry: a
+// four, or a cancelling determinant) take the rare path staged_rare_stiffness: a
 // cofactor is a 2x2 minor whose terms then cancel by about that ratio, and so does
 // the zero-row sum; the rare path computes the geometry in FP64 from the exact
 // coordinates, as the reference does.  On a Kuhn cube jittered by 0.25 h (12.6 M
 // tets, ratios up to 21) ~0.01 % of the elements are rare.
-enum { kP1Common = 0, kP1DirectC0 = 1, kP1Fp64 = 2 };
+enum { kP1Common = 0, kP1Fp64 = 1 };
 
 template <typename T>
 __device__ __forceinline__ int p1_class(const Cof<T>& f)
@@ -373,15 +379,10 @@ __device__ __forceinline__ ff dw_diff3(float hb, float ha, float mb, float ma, f
   const float t = __fadd_rn(__fadd_rn(__fadd_rn(s.lo, s1.lo), s2.lo), __fsub_rn(lb, la));
   return two_sum(s.hi, t);
 }
-// component r of the edge from vertex j to vertex k, double-word and FP32
-__device__ __forceinline__ ff dw_edge(const FetchAbs& F, int k, int j, int r)
-{
-  return dw_diff3(rec_hi(F.a[k], r), rec_hi(F.a[j], r), rec_mid(F.a[k], F.b[k], r), rec_mid(F.a[j], F.b[j], r),
-                  rec_lo(F.b[k], F.lz[k], r), rec_lo(F.b[j], F.lz[j], r));
-}
-// the same from hi + mid only (48 bits of the chunk-relative coordinate): the
-// common path, whose elements (gradient ratios <= 3, p1_class) do not amplify
-// that truncation past ~1e-13
+// component r of the edge from vertex j to vertex k, double-word and FP32, from
+// hi + mid only (48 bits of the chunk-relative coordinate): the common path,
+// whose elements (gradient ratios <= 8, p1_class) do not amplify that
+// truncation past ~1e-13
 __device__ __forceinline__ ff dw_edge2(const FetchAbs& F, int k, int j, int r)
 {
   const ff s1 = two_sum(rec_hi(F.a[k], r), -rec_hi(F.a[j], r));
@@ -407,9 +408,13 @@ __device__ __forceinline__ void geometry_fp64(const FetchAbs& F, Cof<double>& d)
 // vertex 0 and then one vertex per edge column (fewer live registers than all
 // four at once); returns whether the element needs the FP64 geometry
 // (det_cancels).  FP32: edge vectors (hi_k - hi_0) + (mid_k - mid_0), to a float
-// ulp of the edge; double-word: dw_diff3 of the three floats.
+// ulp of the edge; double-word: dw_edge2 of hi + mid.  With c0 (FP32 P1
+// stiffness) also C_0 = (x3 - x1) x (x2 - x1) from the edge columns,
+// x_k - x_1 = J_k - J_1: on the common path (gradient ratios <= 8, p1_class) the
+// face edges are within a few float ulps, and no vertex is read twice.
 template <int MODE>
-__device__ __forceinline__ bool geometry_staged_lazy(const StagedVerts& v, ushort4 lc, Cof<typename Arith<MODE>::T>& f)
+__device__ __forceinline__ bool geometry_staged_lazy(const StagedVerts& v, ushort4 lc, Cof<typename Arith<MODE>::T>& f,
+                                                     float* c0 = nullptr)
 {
   using T = typename Arith<MODE>::T;
   constexpr bool LO = MODE == kF64;
@@ -433,6 +438,19 @@ __device__ __forceinline__ bool geometry_staged_lazy(const StagedVerts& v, ushor
   }
   if constexpr (MODE == kDW) dw_cofactors(J, f);
   else cofactors<T>(J, f);
+  if constexpr (MODE == kF32) {
+    if (c0) {
+      float f2[3], f3[3];
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        f2[r] = J[r][1] - J[r][0];
+        f3[r] = J[r][2] - J[r][0];
+      }
+      c0[0] = f3[1] * f2[2] - f3[2] * f2[1];
+      c0[1] = f3[2] * f2[0] - f3[0] * f2[2];
+      c0[2] = f3[0] * f2[1] - f3[1] * f2[0];
+    }
+  }
   if constexpr (MODE == kF64) return false;
   else return det_cancels<T>(J, f);
 }
@@ -449,34 +467,6 @@ static __device__ __noinline__ Cof<T> staged_geometry_fp64(StagedVerts v, ushort
   Cof<T> f;
   store_geometry(g, f);
   return f;
-}
-
-// Geometry of a staged item in the mode's arithmetic from four fetched vertices
-// (the rare paths); returns whether the element needs the FP64 geometry.
-__device__ __forceinline__ bool geometry_staged(const FetchAbs& F, Cof<float>& f)
-{
-  float J[3][3];
-#pragma unroll
-  for (int r = 0; r < 3; ++r)
-#pragma unroll
-    for (int k = 0; k < 3; ++k) J[r][k] = f32_edge(F, k + 1, 0, r);
-  cofactors<float>(J, f);
-  return det_cancels<float>(J, f);
-}
-__device__ __forceinline__ bool geometry_staged(const FetchAbs& F, Cof<ff>& f)
-{
-  ff J[3][3];
-#pragma unroll
-  for (int r = 0; r < 3; ++r)
-#pragma unroll
-    for (int k = 0; k < 3; ++k) J[r][k] = dw_edge(F, k + 1, 0, r);
-  dw_cofactors(J, f);
-  return det_cancels<ff>(J, f);
-}
-__device__ __forceinline__ bool geometry_staged(const FetchAbs& F, Cof<double>& f)
-{
-  geometry_fp64(F, f);
-  return false;
 }
 
 // near-degenerate elements: FP64 geometry from the mesh's FP64 coordinates
@@ -561,33 +551,9 @@ __device__ __forceinline__ void p1_stiff_unique<ff>(const Cof<ff>& f, ff s, ff K
   K[0] = -(K[1] + K[2] + K[3]);
 }
 
-// C_0 = (x3 - x1) x (x2 - x1) (= -(C_1 + C_2 + C_3)) from the staged vertices in
-// the mode's arithmetic: the edges of the face opposite vertex 0, then their
-// cross product, accurate to its own magnitude.
-__device__ __forceinline__ void staged_c0(const FetchAbs& F, float C0[3])
-{
-  float f2[3], f3[3];
-#pragma unroll
-  for (int r = 0; r < 3; ++r) {
-    f2[r] = f32_edge(F, 2, 1, r);
-    f3[r] = f32_edge(F, 3, 1, r);
-  }
-  C0[0] = f3[1] * f2[2] - f3[2] * f2[1];
-  C0[1] = f3[2] * f2[0] - f3[0] * f2[2];
-  C0[2] = f3[0] * f2[1] - f3[1] * f2[0];
-}
-__device__ __forceinline__ void staged_c0(const FetchAbs& F, ff C0[3])
-{
-  ff f2[3], f3[3];
-#pragma unroll
-  for (int r = 0; r < 3; ++r) {
-    f2[r] = dw_edge(F, 2, 1, r);
-    f3[r] = dw_edge(F, 3, 1, r);
-  }
-  C0[0] = ff_cross(f3[1], f2[2], f3[2], f2[1]);
-  C0[1] = ff_cross(f3[2], f2[0], f3[0], f2[2]);
-  C0[2] = ff_cross(f3[0], f2[1], f3[1], f2[0]);
-}
+// C_0 = (x3 - x1) x (x2 - x1) (= -(C_1 + C_2 + C_3)) in FP64 from the exact
+// staged coordinates (the rare path): the edges of the face opposite vertex 0,
+// then their cross product, accurate to its own magnitude.
 __device__ __forceinline__ void staged_c0(const FetchAbs& F, double C0[3])
 {
   double f2[3], f3[3];
@@ -1029,13 +995,13 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
         // record).  A near-degenerate element (det_cancels) gets its geometry in
         // FP64 here unless `defer` is set (the P1 stiffness sends it down its own
         // rare path); returns whether it is one.
-        auto item_geometry = [&](int it, Cof<T>& f, T& coef, double& coef_d, bool defer) {
+        auto item_geometry = [&](int it, Cof<T>& f, T& coef, double& coef_d, bool defer, float* c0 = nullptr) {
           const unsigned char* rb = stage_of(qq);
           const int rk = reinterpret_cast<const int32_t*>(rb + sizeof(ChunkDesc))[it];
           coef_d = a.coeff ? __ldg(a.coeff + rk) : a.cconst;  // latency covered by the geometry
           const ushort4 lc = item_lconn(it);
           const StagedVerts sv = staged_verts();
-          const bool need = geometry_staged_lazy<MODE>(sv, lc, f);
+          const bool need = geometry_staged_lazy<MODE>(sv, lc, f, c0);
           if constexpr (MODE != kF64) {
             // entered only when a lane of the warp needs it
             if (!defer && __any_sync(__activemask(), need)) {
@@ -1076,9 +1042,10 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
             Cof<T> f;
             T coef;
             double coef_d;
-            const bool degenerate = item_geometry(local, f, coef, coef_d, a.stiff != 0);
+            float c0[3];  // FP32 stiffness: C_0 from the edge columns (geometry_staged_lazy)
+            const bool degenerate =
+                item_geometry(local, f, coef, coef_d, a.stiff != 0, MODE == kF32 && a.stiff ? c0 : nullptr);
             T K[10];
-            bool special = false;
             if (a.stiff) {
               // the rare elements (p1_class, or a cancelling determinant) go out of
               // line, entered only when a lane of the warp has one; that path
@@ -1095,12 +1062,8 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
               }
               if (rare) {
               } else if constexpr (MODE == kF32) {
-                // FP32: C_0 from the edges of the face opposite vertex 0, every element
-                FetchAbs F;
-                fetch_staged<false>(staged_verts(), item_lconn(local), F);
-                T C0[3];
-                staged_c0(F, C0);
-                p1_stiff_direct<T>(f, C0, coef * wsum / f.det, K);
+                // FP32: C_0 from the face opposite vertex 0, every element
+                p1_stiff_direct<T>(f, c0, coef * wsum / f.det, K);
               } else {
                 const T sc = coef * wsum / f.det;
                 p1_stiff_unique<T>(f, sc, K);
@@ -1112,10 +1075,8 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
 #pragma unroll
               for (int u = 0; u < 10; ++u) K[u] = sc * tab[6 * NU + u];
             }
-            if (!special) {
 #pragma unroll
-              for (int u = 0; u < 10; ++u) buf[u * CI + local] = K[u];
-            }
+            for (int u = 0; u < 10; ++u) buf[u * CI + local] = K[u];
           }
         } else {
           // P2: the first warp of the group computes each item's scale factors

@@ -73,6 +73,10 @@ __device__ __forceinline__ ff ff_add_s(ff a, ff b)
 
 // a.b of two 3-vectors: error-free products of the high parts chained with
 // two_sum, every low-order term collected in one float, one renormalisation.
+// The renormalisation is fast_two_sum although the dot may cancel below its low
+// part (|hi| < |lo|): the result is then still within ~2^-48 of the terms'
+// magnitudes, which is the accuracy every caller needs (entries are compared
+// row-scaled; a cancelling determinant is caught by det_cancels).
 __device__ __forceinline__ ff ff_dot3(const ff* a, const ff* b)
 {
   ff p = two_prod(a[0].hi, b[0].hi);
@@ -85,10 +89,11 @@ __device__ __forceinline__ ff ff_dot3(const ff* a, const ff* b)
     hi = s.hi;
     lo = __fadd_rn(lo, __fadd_rn(s.lo, __fmaf_rn(a[k].hi, b[k].lo, __fmaf_rn(a[k].lo, b[k].hi, q.lo))));
   }
-  return two_sum(hi, lo);  // the dot may cancel below its low part
+  return fast_two_sum(hi, lo);
 }
 
-// a * b - c * d in the same style (the cofactor pattern).
+// a * b - c * d in the same style (the cofactor pattern), absolute error
+// ~2^-48 (|a b| + |c d|) also when the difference cancels (see ff_dot3).
 __device__ __forceinline__ ff ff_cross(ff a, ff b, ff c, ff d)
 {
   const ff p = two_prod(a.hi, b.hi), q = two_prod(-c.hi, d.hi);
@@ -96,7 +101,7 @@ __device__ __forceinline__ ff ff_cross(ff a, ff b, ff c, ff d)
   float lo = __fadd_rn(s.lo, __fadd_rn(p.lo, q.lo));
   lo = __fadd_rn(lo, __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, 0.0f)));
   lo = __fsub_rn(lo, __fmaf_rn(c.hi, d.lo, __fmaf_rn(c.lo, d.hi, 0.0f)));
-  return two_sum(s.hi, lo);
+  return fast_two_sum(s.hi, lo);
 }
 
 __device__ __forceinline__ ff ff_neg(ff a) { return ff{-a.hi, -a.lo}; }
