@@ -706,9 +706,9 @@ constexpr size_t align16(size_t n) { return (n + 15) / 16 * 16; }
 
 // Barriers of k_assemble (mbarriers in shared memory).  "full" barriers complete
 // when a bulk copy has landed (producer arrival + transaction bytes); "empty"
-// barriers when the consumers have finished with a buffer; the two token
-// barriers hand the right to update the accumulators from one consumer group
-// to the other.
+// barriers when the consumers have finished with a buffer; the token barriers
+// hand the right to update the accumulators from one consumer group to the
+// next.
 enum {
   kBarRecFull = 0,                        // [kRecStages] chunk-record stages
   kBarRecEmpty = kBarRecFull + kRecStages,  // [kRecStages]
@@ -718,13 +718,24 @@ enum {
   kBarMetaEmpty = kBarMetaFull + 1,
   kBarBlkFull = kBarMetaEmpty + 1,          // [2] block descriptors
   kBarBlkEmpty = kBarBlkFull + 2,           // [2]
-  kBarToken = kBarBlkEmpty + 2,             // [2] group g may run phase 2
-  kNumBars = kBarToken + 2
+  kBarToken = kBarBlkEmpty + 2,             // [kMaxGroups] group g may run phase 2
+  kMaxGroups = 3,
+  kNumBars = kBarToken + kMaxGroups
 };
 
-constexpr int kGroups = 2;                          // consumer groups of kThreads threads
-constexpr int kConsumers = kGroups * kThreads;
-constexpr int kAsmThreads = kConsumers + 32;        // + the producer warp
+// Consumer groups of kThreads threads per CTA, plus one producer warp.  Two
+// groups (17 warps: at most 5 on one SM sub-partition, 5 x 32 x 96 of its 16 K
+// registers) in every mode.  The kernel takes up to kMaxGroups; three FP32
+// groups (25 warps, which caps a thread at 72 registers) were measured slower
+// on GB300 at P1 128^3 (0.906 against 0.859 ms; the P1 FP32 element math
+// spills at 72 registers) and at P2 48^3 (0.496 against 0.484 ms).
+template <int MODE> struct AsmShape {
+  static constexpr int groups = 2;
+  static constexpr int consumers = groups * kThreads;
+  static constexpr int threads = consumers + 32;
+  static constexpr int max_regs = 96;
+};
+static_assert(AsmShape<kF32>::groups <= kMaxGroups && AsmShape<kDW>::groups <= kMaxGroups, "token barriers");
 
 // Shared-memory layout of k_assemble.  Every region starts on a 16-byte
 // boundary: the bulk copies (chunk records, contribution words, row metadata)
@@ -742,11 +753,12 @@ struct AsmLayout {
   static constexpr size_t meta_bytes = align16(8 * (kRowsMax + 4));
   static constexpr size_t blk_bytes = 2 * sizeof(BlockDesc);
   static constexpr size_t off_buf = acc_bytes;
-  static constexpr size_t off_tab = off_buf + kGroups * buf_bytes;
+  static constexpr int G = AsmShape<MODE>::groups;
+  static constexpr size_t off_tab = off_buf + G * buf_bytes;
   // P2: per group, the 6 scale factors of each item of a chunk (computed once per item)
   static constexpr size_t geo_bytes = ORDER == 2 ? align16(sizeof(T) * CI * 6) : 0;
   static constexpr size_t off_geo = off_tab + tab_bytes;
-  static constexpr size_t off_meta = off_geo + kGroups * geo_bytes;
+  static constexpr size_t off_meta = off_geo + G * geo_bytes;
   static constexpr size_t off_blk = off_meta + meta_bytes;
   static constexpr size_t off_bars = off_blk + blk_bytes;
   static constexpr size_t off_stage = off_bars + align16(8 * kNumBars);
@@ -793,11 +805,13 @@ __device__ __forceinline__ bool named_sync_or(bool pred)
 }
 __device__ __forceinline__ bool group_sync_or(int g, bool pred)
 {
-  return g == 0 ? named_sync_or<2, kThreads>(pred) : named_sync_or<3, kThreads>(pred);
+  if (g == 0) return named_sync_or<2, kThreads>(pred);
+  if (g == 1) return named_sync_or<3, kThreads>(pred);
+  return named_sync_or<4, kThreads>(pred);
 }
 
 // k_assemble: a persistent, warp-specialised kernel; per CTA one producer warp
-// and two consumer groups of kThreads threads.
+// and G consumer groups of kThreads threads (AsmShape).
 //
 // The producer (one thread) takes blocks from the work counter and streams, for
 // chunk q of the CTA (counted across its blocks), the chunk record into stage
@@ -805,15 +819,15 @@ __device__ __forceinline__ bool group_sync_or(int g, bool pred)
 // block's row metadata; it waits on an "empty" barrier before reusing a buffer
 // and runs several chunks (and across block boundaries) ahead.
 //
-// Consumer group g takes the chunks q with q % 2 == g:
+// Consumer group g takes the chunks q with q % G == g:
 //   phase 1    wait record q; gather the element coefficients; element
 //              matrices from the staged vertices -> the group's buf
 //   barrier    (group) release record q
-//   phase 2    wait words q and the token (the other group finished phase 2 of
-//              chunk q - 1); add the contributions to the owned slots; pass
-//              the token on
+//   phase 2    wait words q and the token (the previous group finished phase 2
+//              of chunk q - 1); add the contributions to the owned slots; pass
+//              the token on to the next group
 //   barrier    (group) release words q
-// so one group's phase 1 runs beside the other's phase 2, while the
+// so the groups' phase 1 runs beside another group's phase 2, while the
 // accumulator updates stay in chunk order (the sums are bitwise reproducible).
 // Per block both groups zero the accumulators first and write the owned rows
 // last.  Every wait is bounded; after a wait gives up the consumers keep their
@@ -821,11 +835,13 @@ __device__ __forceinline__ bool group_sync_or(int g, bool pred)
 // the producer stops issuing and lets its copies in flight land, and the CTA
 // records the failure.
 template <int ORDER, int MODE>
-__global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
+__global__ void __launch_bounds__(AsmShape<MODE>::threads, 1) __maxnreg__(AsmShape<MODE>::max_regs)
+    k_assemble(AsmArgs a)
 {
   using A = Arith<MODE>;
   using T = typename A::T;
   using L = AsmLayout<ORDER, MODE>;
+  constexpr int kGroups = AsmShape<MODE>::groups, kConsumers = AsmShape<MODE>::consumers;
   constexpr int NU = L::NU, CI = L::CI, NS = kRecStages;
   constexpr int TPI = ORDER == 1 ? 1 : kP2ThreadsPerItem;  // threads per item
   extern __shared__ __align__(16) unsigned char smem[];
@@ -848,7 +864,7 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
     for (int k = 0; k < kNumBars; ++k) {
       uint32_t count = 1;
       if (k == kBarBlkEmpty || k == kBarBlkEmpty + 1) count = kConsumers;
-      if (k == kBarToken || k == kBarToken + 1) count = kThreads;
+      if (k >= kBarToken && k < kBarToken + kMaxGroups) count = kThreads;
       mbar_init(&bars[k], count);
     }
     mbar_fence_init();
@@ -969,7 +985,7 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
       for (int i = tid; i < kAccMax; i += kConsumers) acc[i] = A::zero();
       named_sync<1, kConsumers>();  // zeroed before any phase 2
 
-      for (int c = (g - q) & 1; c < n; c += kGroups) {
+      for (int c = ((g - q) % kGroups + kGroups) % kGroups; c < n; c += kGroups) {
         const int qq = q + c;
         // ---- phase 1: element matrices of chunk c from its staged record
         if (!failed && !mbar_wait(&bars[kBarRecFull + qq % NS], (uint32_t)((qq / NS) & 1), a.wait_limit)) failed = true;
@@ -1151,7 +1167,7 @@ __global__ void __launch_bounds__(kAsmThreads, 1) k_assemble(AsmArgs a)
             acc[slot] = a;
           }
         }
-        if (c + 1 < n) mbar_arrive(&bars[kBarToken + (g ^ 1)]);  // release: the updates above precede
+        if (c + 1 < n) mbar_arrive(&bars[kBarToken + (g + 1) % kGroups]);  // release: the updates above precede
         failed = group_sync_or(g, failed);
         if (gtid == 0) mbar_arrive(&bars[kBarEntEmpty + qq % kWordStages]);
       }
@@ -1233,10 +1249,11 @@ static mg_status launch_assemble_t(AsmArgs a, cudaStream_t st)
     }
     sms = cache.sms[dev];
   }
-  MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_assemble<ORDER, MODE>, kAsmThreads, smem));
+  constexpr int threads = AsmShape<MODE>::threads;
+  MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_assemble<ORDER, MODE>, threads, smem));
   if (per_sm < 1) return set_error(MG_ERR_SIZE, "assembly CTA does not fit on an SM (shared memory or registers)");
   const int grid = std::max(1, std::min(a.nblocks, per_sm * sms));
-  if (a.nblocks > 0) k_assemble<ORDER, MODE><<<grid, kAsmThreads, smem, st>>>(a);
+  if (a.nblocks > 0) k_assemble<ORDER, MODE><<<grid, threads, smem, st>>>(a);
   MG_CUDA(cudaGetLastError());
   return MG_OK;
 }
