@@ -828,13 +828,18 @@ def main():
         # 100 SpMVs, values and y back in host memory; wall clock
         e2e_cold = None
         if not a.no_cold:
-            ts = []
+            ts, stages = [], []
             for _ in range(2):
                 torch.cuda.synchronize()
                 t0 = time.perf_counter()
                 mc = mg.Mesh(m.xyz, m.conn, order=1)
+                t1 = time.perf_counter()
                 bc = mg.MatrixBuilder(mc, pattern_on_device=True)
+                torch.cuda.synchronize()
+                t2 = time.perf_counter()
                 vc = bc.assemble("stiff_kappa", coeff=kap_pin, quad=4, prec="f64")
+                torch.cuda.synchronize()
+                t3 = time.perf_counter()
                 xc = x_pin.cuda()
                 yc = torch.empty_like(xc)
                 for _ in range(N_SPMV):
@@ -842,12 +847,16 @@ def main():
                 vh, yh = vc.cpu(), yc.cpu()
                 torch.cuda.synchronize()
                 ts.append(time.perf_counter() - t0)
+                stages.append((t1 - t0, t2 - t1, t3 - t2, ts[-1] - (t3 - t0)))
                 del vc, xc, yc, vh, yh
                 bc.close()
                 mc.close()
             tc = statistics.mean(ts)
             e2e_cold = {"value": world * E / tc, "unit": "tets/s", "ms_per_step": tc * 1e3,
-                        "runs_s": ts, "h2d_bytes_per_step": 24 * N + 16 * E + 8 * E + 8 * ndof,
+                        "runs_s": ts,
+                        "stages_s": {k: statistics.mean(s[i] for s in stages) for i, k in enumerate(
+                            ("mesh_create", "plan_build_device", "first_assembly_with_coefficient_upload",
+                             "spmvs_and_copies"))}, "h2d_bytes_per_step": 24 * N + 16 * E + 8 * E + 8 * ndof,
                         "d2h_bytes_per_step": d2h,
                         "note": "from host arrays: mg_mesh_create + mg_pattern_build_device (CSR pattern and assembly "
                                 "schedule built on the GPU) + first mg_assemble + "
