@@ -278,8 +278,8 @@ class MatrixBuilder:
     the reference's matrixBuilder / vectorBuilder and of the operator Belos uses."""
 
     def __init__(self, mesh: Mesh, pattern_on_device: bool = False, stream=None):
-        """pattern_on_device: compute the CSR pattern on the GPU (mg_pattern_build_device)
-        instead of the host; the result is identical."""
+        """pattern_on_device: build the CSR pattern and the assembly schedule on the GPU
+        (mg_pattern_build_device) instead of the host; the arrays are identical."""
         self.mesh = mesh
         h = _P()
         if pattern_on_device:
