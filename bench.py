@@ -637,7 +637,7 @@ def main():
     b = mg.MatrixBuilder(mesh)
     setup["plan_host_s"] = time.perf_counter() - t0
     nnz, ndof = b.nnz, b.ndof
-    sched = b.schedule_info()
+    smi = b.slot_map_info()
     kappa = torch.from_numpy(kappa_h).cuda()
     x = torch.from_numpy(np.random.default_rng(a.seed).uniform(-1, 1, ndof)).cuda()
     x32 = x.float()
@@ -746,10 +746,12 @@ def main():
         extras["spmv_f32"] = {**_rec(peak, S32, ts32), "note": "one launch, L2 flushed before it"}
         extras["adjoint_grad"] = _rec(peak, adj_bytes(E, N, ndof), tg, E)
         extras["load_vector"] = _rec(peak, rhs_bytes(E, N, ndof), tb, E)
-        extras["schedule"] = {"blocks": sched.nblocks, "items": sched.n_items, "recompute_factor": sched.n_items / E,
-                              "words": sched.n_entries,
-                              "word_bytes_per_contribution": 4 * sched.n_entries / max(1, sched.n_contrib),
-                              "padding_factor": 2 * sched.n_entries / max(1, sched.n_contrib)}  # P1: 4 per 2 words
+        extras["slot_map"] = {"upper_entries": smi.n_upper, "sources": smi.n_contrib,
+                              "sources_per_upper_entry": smi.n_contrib / max(1, smi.n_upper),
+                              "index_bytes": 4 * smi.n_contrib + 12 * smi.n_upper,
+                              "element_matrix_bytes_f64": 8 * smi.nunique * smi.n_elem,
+                              "note": "each element's matrix computed once (k_elem_mat), then one gather thread per "
+                                      "diagonal or upper CSR entry (k_slot_gather) writing the entry and its mirror"}
         extras["setup"] = setup
         if graph is not None:
             extras["step_graph_ms"] = ms_step
@@ -824,7 +826,7 @@ def main():
                        "upload overlaps the assembly and the values download overlaps the SpMVs (second stream)"}
 
         # cold e2e: the work the reference arm's step does, from host arrays -- mesh
-        # tables, CSR pattern (on the GPU) and assembly schedule, first assembly and
+        # tables, CSR pattern, element order and slot map (on the GPU), first assembly and
         # 100 SpMVs, values and y back in host memory; wall clock
         e2e_cold = None
         if not a.no_cold:
@@ -858,8 +860,8 @@ def main():
                             ("mesh_create", "plan_build_device", "first_assembly_with_coefficient_upload",
                              "spmvs_and_copies"))}, "h2d_bytes_per_step": 24 * N + 16 * E + 8 * E + 8 * ndof,
                         "d2h_bytes_per_step": d2h,
-                        "note": "from host arrays: mg_mesh_create + mg_pattern_build_device (CSR pattern and assembly "
-                                "schedule built on the GPU) + first mg_assemble + "
+                        "note": "from host arrays: mg_mesh_create + mg_pattern_build_device (CSR pattern, element "
+                                "order and slot map built on the GPU) + first mg_assemble + "
                                 f"{N_SPMV} SpMV, values and y copied back; wall clock, mean of 2 -- the work one "
                                 "step of the reference arm does"}
 
@@ -867,7 +869,7 @@ def main():
             extras["config3_p2_48"] = p2_record()
 
         rl = extras["spmv_f64_in_step"] if N_SPMV * ts64 >= ta64 else extras["assembly_f64"]
-        kname = "k_spmv<double,1>" if rl is extras["spmv_f64_in_step"] else "k_assemble<1,kDW>"
+        kname = "k_spmv<double,1>" if rl is extras["spmv_f64_in_step"] else "k_elem_mat<1,kDW> + k_slot_gather<kDW>"
         traffic, tnote = profiled_traffic(kname, a.n)
         roofline = {"bound": "hbm", "kernel": kname,
                     "achieved": rl["gbs"], "peak": peak, "unit": "GB/s", "frac": rl["gbs"] / peak,

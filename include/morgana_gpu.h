@@ -157,17 +157,18 @@ mg_status mg_mesh_export_geometry(const mg_mesh* mesh, double* h_xyz, int32_t* h
 /* --------------------------------------------------------------- pattern -- */
 
 /* Builds the CSR sparsity pattern (union of element couplings, explicit zeros
-   kept, sorted columns) and the GPU assembly schedule of the mesh.
+   kept, sorted columns) and the element order of the GPU assembly (a Morton
+   curve of the element centroids).  The first GPU use of the plan uploads it
+   and builds the assembly's slot map on the device.
    Replaces: the pattern half of traitsMatrixBuilder::buildEpetraCrs / numEntPerRow
    (src/morganaFiniteElements/traitsMatrixBuilder.hpp:363-544). */
 mg_status mg_pattern_build(mg_mesh* mesh, mg_plan** out);
 /* The same plan built on the GPU: the CSR pattern (element couplings as
-   64-bit keys, radix-sorted and de-duplicated on the device) and the assembly
-   schedule (Morton orders by radix sort, blocks by a prefix sum, per chunk its
-   vertices, contribution list and words by one CTA), identical to the host
-   build's arrays.  The plan is device-resident on return.  Needs a device;
-   waits for its own work on `stream`.  Up to 2^31 element couplings (E nb^2),
-   else MG_ERR_SIZE.
+   64-bit keys, radix-sorted and de-duplicated on the device), the element order
+   (Morton keys radix-sorted) and the slot map, identical to the host build's
+   arrays.  The plan is device-resident on return.  Needs a device; waits for
+   its own work on `stream`.  Up to 2^31 element couplings (E nb^2), else
+   MG_ERR_SIZE.
    Replaces: the same pattern half of buildEpetraCrs. */
 mg_status mg_pattern_build_device(mg_mesh* mesh, mg_plan** out, void* stream);
 mg_status mg_plan_destroy(mg_plan* plan);
@@ -179,47 +180,31 @@ mg_status mg_pattern_export(const mg_plan* plan, int32_t* h_rowptr, int32_t* h_c
 /* Device copies owned by the plan (valid until mg_plan_destroy). */
 mg_status mg_pattern_device(const mg_plan* plan, const int32_t** d_rowptr, const int32_t** d_colind);
 
-/* Assembly schedule of a plan (no reference counterpart: the reference inserts
-   element blocks into Epetra one by one).  The dofs are cut into blocks of at
-   most acc_max CSR entries; one CTA of `threads` threads owns a block and
-   recomputes every element ("item") touching it.  For checks the schedule can
-   be exported: from the host copy until a host-built plan is first used on the
-   GPU, from the device arrays for a plan built by mg_pattern_build_device. */
+/* Slot map of the GPU assembly (no reference counterpart: the reference inserts
+   element blocks into Epetra one by one).  The operators are symmetric, so the
+   assembly sums each diagonal and upper CSR entry t once and writes it to the
+   entry h_uslot[t] and to its mirror h_umirror[t] (the same entry on the
+   diagonal); its sources are h_src[h_useg[t] .. h_useg[t+1]), the element-matrix
+   entries of every element holding both dofs, in ascending Morton position p of
+   the element (h_elem_order[p] = element id).  A source is p * nunique + u
+   (elem_major = 1, P1) or u * n_elem + p (P2), u the upper-triangle index of the
+   element's local pair (i <= j, row-major).  Both calls make the plan
+   device-resident (they need a device). */
 typedef struct {
-  int32_t nblocks;
-  int32_t threads;
-  int32_t warps;
-  int32_t acc_max;
-  int32_t chunk_items;
-  int32_t host_copy;   /* 1 while mg_plan_export_schedule is available */
-  int64_t n_items;     /* element recomputations summed over blocks */
-  int64_t n_chunks;
-  int64_t n_entries;   /* contribution-list 32-bit words (two per 8-byte piece), padding included */
-  int64_t n_contrib;   /* element-matrix entries scattered (= n_elements * nb^2) */
-  int64_t n_item_slots;      /* length of the exported item array (padding included) */
-  int64_t max_chunk_entries; /* words of the largest chunk (its shared-memory staging buffer) */
-  int64_t max_chunk_vertices;     /* distinct vertices of the largest chunk (padded to 4) */
-  int64_t max_chunk_record_bytes; /* largest chunk record: element ranks, local vertex indices,
-                                     vertex coordinates (its shared-memory stage) */
-} mg_schedule_info;
+  int64_t n_upper;    /* diagonal and upper CSR entries */
+  int64_t n_contrib;  /* sources summed over them */
+  int64_t n_elem;
+  int32_t nunique;    /* unique entries of an element matrix: 10 (P1), 55 (P2) */
+  int32_t elem_major; /* element-matrix layout of the sources (see above) */
+} mg_slot_map_info;
 
-mg_status mg_plan_schedule_info(const mg_plan* plan, mg_schedule_info* info);
-
-/* h_blocks: nblocks x 8 int32 {item_begin, item_count, chunk_begin, nchunks,
-   row_begin, row_count, acc_used, word_begin / 32}; h_items: element ids (each
-   block's list padded to a multiple of 4 with -1); h_chunk_ptr: n_chunks x
-   (warps + 1) offsets into h_entries; h_entries: n_entries 32-bit words, read
-   in pairs as 8-byte pieces laid out [piece][lane] per warp, each piece the
-   contributions of one accumulator slot: P1 four 12-bit sources at bits 0, 12,
-   24, 36 and the slot (14 bits) at bit 48; P2 two words source (13 bits) |
-   slot << 13.  A source indexes the chunk's symmetric element matrices stored
-   entry-major (u * chunk_items + item, u the upper-triangle index of (field,
-   test)); nu * chunk_items is the zero source of padding, and padding pieces
-   target the slot acc_max.  h_rows / h_row_acc: ndof owned rows per block and
-   their accumulator base. */
-mg_status mg_plan_export_schedule(const mg_plan* plan, int32_t* h_blocks, int32_t* h_items,
-                                  int64_t* h_chunk_ptr, uint32_t* h_entries, int32_t* h_rows,
-                                  int32_t* h_row_acc);
+mg_status mg_plan_slot_map_info(mg_plan* plan, mg_slot_map_info* info);
+/* h_elem_order: n_elem; h_useg: n_upper + 1; h_uslot, h_umirror: n_upper;
+   h_src: n_contrib (any may be NULL). */
+mg_status mg_plan_export_slot_map(mg_plan* plan, int32_t* h_elem_order, int32_t* h_useg, int32_t* h_uslot,
+                                  int32_t* h_umirror, uint32_t* h_src);
+/* The Morton element order alone (host copy; no device needed). */
+mg_status mg_plan_export_elem_order(const mg_plan* plan, int32_t* h_elem_order);
 
 /* ------------------------------------------------------------- assembly -- */
 
@@ -228,9 +213,9 @@ mg_status mg_plan_export_schedule(const mg_plan* plan, int32_t* h_blocks, int32_
    n_elements doubles) for MG_OP_STIFF_KAPPA / MG_OP_MASS_COEFF, else ignored;
    c: the constant of MG_OP_STIFF_CONST.  Deterministic: the same inputs give
    the same bits on every call.  Two assemblies on one plan must not overlap on
-   the GPU (other streams): the plan holds the kernel's work counter and a copy
-   of the coefficient in its element order (allocated by the first call that
-   takes a coefficient -- make that call before any stream capture).
+   the GPU (other streams): they share the plan's element-matrix array
+   (nunique x n_elem entries of 8 bytes, allocated by the first assembly -- make
+   that call before any stream capture).
    Replaces: the value half of matrixBuilder<localMatrixEL3d<...>>::buildEpetraCrs
    (traitsMatrixBuilder.hpp:363-441) with integratorOEL3d_STD::integration
    (src/morganaIntegrator/integratorOEL3d_STD.hpp:106-137). */
@@ -238,23 +223,12 @@ mg_status mg_assemble(mg_plan* plan, int32_t op, const double* d_coeff, double c
                       int32_t prec, void* d_values, void* stream);
 
 /* Synchronises the device and reports a failure recorded by an earlier
-   asynchronous assembly on this plan: MG_ERR_CUDA when a bounded wait inside
-   the kernel gave up (the values of that call are incomplete),
-   MG_ERR_INVALID_ARG when the coefficient array held NaN or Inf,
+   asynchronous assembly on this plan: MG_ERR_INVALID_ARG when the coefficient
+   array held NaN or Inf,
    MG_ERR_UNSUPPORTED when an MG_F64 assembly met element-matrix scales outside
    its double-word range (assemble with MG_F64_NATIVE, or rescale the
    coefficient by a power of two).  Clears the record.  No reference counterpart (the reference asserts). */
 mg_status mg_plan_status(mg_plan* plan);
-
-/* Diagnostic: the number of polls after which a wait of this plan's assembly
-   pipeline (a bulk copy landing, a buffer released, the other consumer group's
-   token) gives up; the default is 2^22 (seconds, far beyond any real wait).  A
-   wait that gives up makes the kernel leave early -- its last copies in flight
-   still land before a CTA exits -- and mg_plan_status report MG_ERR_CUDA; 0
-   makes every wait give up at once, which is how the failure path is tested.
-   No reference counterpart. */
-#define MG_WAIT_LIMIT_DEFAULT 4194304u
-mg_status mg_plan_set_wait_limit(mg_plan* plan, uint32_t polls);
 
 /* Host-buffer form of mg_assemble, the call an Epetra/Tpetra adapter makes:
    copies h_coeff in, assembles, copies the nnz values out to h_values. */

@@ -60,13 +60,9 @@ class CgInfo(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
 
 
-class ScheduleInfo(ctypes.Structure):
-    _fields_ = [("nblocks", ctypes.c_int32), ("threads", ctypes.c_int32), ("warps", ctypes.c_int32),
-                ("acc_max", ctypes.c_int32), ("chunk_items", ctypes.c_int32), ("host_copy", ctypes.c_int32),
-                ("n_items", ctypes.c_int64), ("n_chunks", ctypes.c_int64), ("n_entries", ctypes.c_int64),
-                ("n_contrib", ctypes.c_int64), ("n_item_slots", ctypes.c_int64),
-                ("max_chunk_entries", ctypes.c_int64), ("max_chunk_vertices", ctypes.c_int64),
-                ("max_chunk_record_bytes", ctypes.c_int64)]
+class SlotMapInfo(ctypes.Structure):
+    _fields_ = [("n_upper", ctypes.c_int64), ("n_contrib", ctypes.c_int64), ("n_elem", ctypes.c_int64),
+                ("nunique", ctypes.c_int32), ("elem_major", ctypes.c_int32)]
 
 
 _P = ctypes.c_void_p
@@ -99,12 +95,12 @@ SIGNATURES = {
     "mg_pattern_info": [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64)],
     "mg_pattern_export": [_P, _P, _P],
     "mg_pattern_device": [_P, ctypes.POINTER(_P), ctypes.POINTER(_P)],
-    "mg_plan_schedule_info": [_P, ctypes.POINTER(ScheduleInfo)],
-    "mg_plan_export_schedule": [_P, _P, _P, _P, _P, _P, _P],
+    "mg_plan_slot_map_info": [_P, ctypes.POINTER(SlotMapInfo)],
+    "mg_plan_export_slot_map": [_P, _P, _P, _P, _P, _P],
+    "mg_plan_export_elem_order": [_P, _P],
     "mg_assemble": [_P, _I32, _P, _D, _I32, _I32, _P, _P],
     "mg_assemble_host": [_P, _I32, _P, _D, _I32, _I32, _P, _P],
     "mg_plan_status": [_P],
-    "mg_plan_set_wait_limit": [_P, ctypes.c_uint32],
     "mg_assemble_rhs": [_P, _P, _P, _I32, _P, _P],
     "mg_apply_dirichlet": [_P, _P, _I32, _P, _P, _P],
     "mg_spmv": [_P, _I32, _P, _P, _P, _P],
@@ -274,12 +270,12 @@ class Csr:
 
 
 class MatrixBuilder:
-    """CSR pattern + GPU assembly schedule of a mesh (mg_plan); the counterpart of
+    """CSR pattern + GPU assembly plan of a mesh (mg_plan); the counterpart of
     the reference's matrixBuilder / vectorBuilder and of the operator Belos uses."""
 
     def __init__(self, mesh: Mesh, pattern_on_device: bool = False, stream=None):
-        """pattern_on_device: build the CSR pattern and the assembly schedule on the GPU
-        (mg_pattern_build_device) instead of the host; the arrays are identical."""
+        """pattern_on_device: build the CSR pattern, the element order and the slot map on
+        the GPU (mg_pattern_build_device) instead of the host; the arrays are identical."""
         self.mesh = mesh
         h = _P()
         if pattern_on_device:
@@ -300,24 +296,28 @@ class MatrixBuilder:
         _check(lib().mg_pattern_export(self._h, _ptr(rp), _ptr(ci)), "mg_pattern_export")
         return rp, ci
 
-    def schedule_info(self) -> ScheduleInfo:
-        info = ScheduleInfo()
-        _check(lib().mg_plan_schedule_info(self._h, ctypes.byref(info)), "mg_plan_schedule_info")
+    def elem_order(self) -> np.ndarray:
+        """The assembly's element order (a Morton curve of the centroids): element ids."""
+        out = np.empty(self.mesh.n_elements, dtype=np.int32)
+        _check(lib().mg_plan_export_elem_order(self._h, _ptr(out)), "mg_plan_export_elem_order")
+        return out
+
+    def slot_map_info(self) -> SlotMapInfo:
+        info = SlotMapInfo()
+        _check(lib().mg_plan_slot_map_info(self._h, ctypes.byref(info)), "mg_plan_slot_map_info")
         return info
 
-    def export_schedule(self) -> dict:
-        info = self.schedule_info()
-        out = {
-            "blocks": np.empty((info.nblocks, 8), dtype=np.int32),
-            "items": np.empty(info.n_item_slots, dtype=np.int32),
-            "chunk_ptr": np.empty(info.n_chunks * (info.warps + 1), dtype=np.int64),
-            "entries": np.empty(info.n_entries, dtype=np.uint32),
-            "rows": np.empty(self.ndof, dtype=np.int32),
-            "row_acc": np.empty(self.ndof, dtype=np.int32),
-        }
-        _check(lib().mg_plan_export_schedule(self._h, *[_ptr(out[k]) for k in
-                                                        ("blocks", "items", "chunk_ptr", "entries", "rows",
-                                                         "row_acc")]), "mg_plan_export_schedule")
+    def export_slot_map(self) -> dict:
+        """The assembly's slot map (mg_plan_export_slot_map); makes the plan device-resident."""
+        info = self.slot_map_info()
+        out = {"elem_order": np.empty(info.n_elem, dtype=np.int32),
+               "useg": np.empty(info.n_upper + 1, dtype=np.int32),
+               "uslot": np.empty(info.n_upper, dtype=np.int32),
+               "umirror": np.empty(info.n_upper, dtype=np.int32),
+               "src": np.empty(info.n_contrib, dtype=np.uint32)}
+        _check(lib().mg_plan_export_slot_map(self._h, *[_ptr(out[k]) for k in
+                                                        ("elem_order", "useg", "uslot", "umirror", "src")]),
+               "mg_plan_export_slot_map")
         out["info"] = info
         return out
 
@@ -368,10 +368,6 @@ class MatrixBuilder:
     def status(self):
         """Synchronises and raises if an earlier asynchronous assembly recorded a device-side failure."""
         _check(lib().mg_plan_status(self._h), "mg_plan_status")
-
-    def set_wait_limit(self, polls: int = 4194304):
-        """Diagnostic: polls before an assembly pipeline wait gives up (mg_plan_set_wait_limit)."""
-        _check(lib().mg_plan_set_wait_limit(self._h, polls), "mg_plan_set_wait_limit")
 
     def apply_dirichlet(self, values, mask, b=None, stream=None):
         torch = _torch()

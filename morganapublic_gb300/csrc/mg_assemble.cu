@@ -1,21 +1,17 @@
 // Assembly kernels for sm_103a: element matrices of the P1/P2 bilinear forms
-// reduced straight into CSR values, plus the Dirichlet elimination, the
-// adjoint-gradient kernel and the load vector.
+// reduced into CSR values, plus the Dirichlet elimination, the adjoint-gradient
+// kernel and the load vector.
 //
-// k_assemble is a persistent kernel: each CTA repeatedly takes the next block of
-// rows (an integer work counter) and, for every chunk of the block's elements,
-//   stage    a bulk copy (cp.async.bulk, completion on an mbarrier) brings the
-//            chunk's element nodes and element ranks into shared memory while the
-//            previous chunk is reduced, and the chunk's contribution words while
-//            its element matrices are computed;
-//   phase 1  one thread per P1 element (eight per P2 element) computes the
-//            symmetric element matrix into shared memory, entry-major;
-//   phase 2  every thread walks its own slot-sorted segments of contribution
-//            words and adds each contribution to its accumulator slot -- within
-//            a chunk a slot belongs to exactly one thread.
-// The owned rows are then written to their contiguous CSR ranges.  No atomics
-// touch values; the per-slot summation order is fixed by the plan, so the
-// results are bitwise reproducible.
+// The assembly takes two passes, each element computed once:
+//   k_elem_mat     one thread per element along the plan's Morton element order:
+//                  the unique entries of its (symmetric) element matrix into the
+//                  plan's element-matrix array;
+//   k_slot_gather  one thread per diagonal or upper CSR entry: the sum of the
+//                  element-matrix entries of every element holding both of its
+//                  dofs, in ascending Morton position (the plan's slot map),
+//                  written to the entry and to its mirror.
+// No atomics touch values; the per-entry summation order is fixed by the plan,
+// so the results are bitwise reproducible.
 //
 // Element math (reference: src/morganaIntegrator/integratorOEL3d_STD.hpp:106-137,
 // src/morganaOperators/opEL3dA.hpp:129-165, opEL3dF.hpp:102-133, opEL3dG.hpp:83-108,
@@ -104,66 +100,6 @@ template <> struct Arith<kF64> {
   __device__ static Out out(T v) { return v; }
 };
 
-// ------------------------------------------------------------ PTX helpers --
-__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
-{
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
-{
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
-               : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
-{
-  uint32_t ok;
-  asm volatile(
-      "{\n"
-      " .reg .pred p;\n"
-      " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-      " selp.u32 %0, 1, 0, p;\n"
-      "}\n"
-      : "=r"(ok)
-      : "r"(smem_addr(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// Orders this thread's earlier generic-proxy shared-memory accesses before
-// later async-proxy (bulk copy) writes to the same buffers.
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-
-// Bulk copy global -> shared (16-byte aligned addresses, size a multiple of 16),
-// completion signalled on `bar` as transaction bytes.
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
-{
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                   smem_addr(dst)),
-               "l"(src), "r"(bytes), "r"(smem_addr(bar))
-               : "memory");
-}
-
-// Bounded wait: gives up after `limit` polls (each poll may suspend the thread
-// for a short, hardware-chosen time) and returns false.  The pipeline waits take
-// the plan's limit (kWaitLimit unless a diagnostic lowered it); the producer's
-// final waits for its own copies in flight always take kWaitLimit, so that no
-// bulk copy is still writing shared memory when the CTA exits.
-constexpr uint32_t kWaitLimit = MG_WAIT_LIMIT_DEFAULT;
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit)
-{
-  for (uint32_t i = 0; i < limit; ++i)
-    if (mbar_try_wait(bar, parity)) return true;
-  return false;
-}
-
-enum { kDevErrTimeout = 1 };
-
 // ---------------------------------------------------------------- geometry --
 template <typename T>
 struct Cof {
@@ -192,22 +128,6 @@ struct GeoPtrs {
   const float* loz;        // lz
 };
 
-// The coordinates an element needs.  The assembly kernel reads them from the
-// chunk record staged in shared memory: per distinct vertex of the chunk, its
-// coordinates relative to the chunk's first vertex split exactly into three
-// floats r = hi + mid + lo, in the layout of the mesh's absolute records
-// (a = hi.xyz mid.x, b = mid.yz lo.xy, c = lo.z).  An edge vector r_k - r_0 is
-// then the exact difference of the mesh's FP64 coordinates -- the reference's J,
-// which geoMapInterface::getGradient forms as x_k - x_0 -- up to the rounding of
-// the arithmetic that forms it.  (A two-float split kept 2^-48 of the chunk's
-// extent, several edges; a cancelling cofactor amplified that past 1e-12 on
-// strongly jittered 128^3 meshes.)  The adjoint kernel reads the mesh's absolute
-// records from global memory.
-struct StagedVerts {
-  const float4* a;  // hi.xyz, mid.x
-  const float4* b;  // mid.y, mid.z, lo.x, lo.y
-  const float* c;   // lo.z
-};
 struct FetchAbs {  // four vertices in the three-float form (staged or absolute)
   float4 a[4], b[4];
   float lz[4];
@@ -225,20 +145,6 @@ __device__ __forceinline__ void fetch(const GeoPtrs& g, int4 n, FetchAbs& F)
     F.a[s] = g.rec[2 * (int64_t)id[s]];
     F.b[s] = g.rec[2 * (int64_t)id[s] + 1];
     F.lz[s] = g.loz[id[s]];
-  }
-}
-
-// the four vertices of an item from a staged record (LO: the third floats too;
-// the FP32 arithmetic needs hi + mid only)
-template <bool LO>
-__device__ __forceinline__ void fetch_staged(const StagedVerts& v, ushort4 lc, FetchAbs& F)
-{
-  const int id[4] = {lc.x, lc.y, lc.z, lc.w};
-#pragma unroll
-  for (int s = 0; s < 4; ++s) {
-    F.a[s] = v.a[id[s]];
-    F.b[s] = v.b[id[s]];
-    F.lz[s] = LO ? v.c[id[s]] : 0.0f;
   }
 }
 
@@ -379,20 +285,6 @@ __device__ __forceinline__ ff dw_diff3(float hb, float ha, float mb, float ma, f
   const float t = __fadd_rn(__fadd_rn(__fadd_rn(s.lo, s1.lo), s2.lo), __fsub_rn(lb, la));
   return two_sum(s.hi, t);
 }
-// component r of the edge from vertex j to vertex k, double-word and FP32, from
-// hi + mid only (48 bits of the chunk-relative coordinate): the common path,
-// whose elements (gradient ratios <= 8, p1_class) do not amplify that
-// truncation past ~1e-13
-__device__ __forceinline__ ff dw_edge2(const FetchAbs& F, int k, int j, int r)
-{
-  const ff s1 = two_sum(rec_hi(F.a[k], r), -rec_hi(F.a[j], r));
-  return two_sum(s1.hi, __fadd_rn(s1.lo, __fsub_rn(rec_mid(F.a[k], F.b[k], r), rec_mid(F.a[j], F.b[j], r))));
-}
-__device__ __forceinline__ float f32_edge(const FetchAbs& F, int k, int j, int r)
-{
-  return (rec_hi(F.a[k], r) - rec_hi(F.a[j], r)) + (rec_mid(F.a[k], F.b[k], r) - rec_mid(F.a[j], F.b[j], r));
-}
-
 // FP64 geometry from three-float coordinates (exact as doubles)
 __device__ __forceinline__ void geometry_fp64(const FetchAbs& F, Cof<double>& d)
 {
@@ -402,71 +294,6 @@ __device__ __forceinline__ void geometry_fp64(const FetchAbs& F, Cof<double>& d)
     D.x[s] = make_double4_32a(rec_x(F.a[s], F.b[s], F.lz[s], 0), rec_x(F.a[s], F.b[s], F.lz[s], 1),
                               rec_x(F.a[s], F.b[s], F.lz[s], 2), 0.0);
   geometry(D, d);
-}
-
-// The common path: geometry of a staged item in the mode's arithmetic, reading
-// vertex 0 and then one vertex per edge column (fewer live registers than all
-// four at once); returns whether the element needs the FP64 geometry
-// (det_cancels).  FP32: edge vectors (hi_k - hi_0) + (mid_k - mid_0), to a float
-// ulp of the edge; double-word: dw_edge2 of hi + mid.  With c0 (FP32 P1
-// stiffness) also C_0 = (x3 - x1) x (x2 - x1) from the edge columns,
-// x_k - x_1 = J_k - J_1: on the common path (gradient ratios <= 8, p1_class) the
-// face edges are within a few float ulps, and no vertex is read twice.
-template <int MODE>
-__device__ __forceinline__ bool geometry_staged_lazy(const StagedVerts& v, ushort4 lc, Cof<typename Arith<MODE>::T>& f,
-                                                     float* c0 = nullptr)
-{
-  using T = typename Arith<MODE>::T;
-  constexpr bool LO = MODE == kF64;
-  FetchAbs F;  // slots 0 (vertex 0) and 1 (the current column's vertex) only
-  F.a[0] = v.a[lc.x];
-  F.b[0] = v.b[lc.x];
-  F.lz[0] = LO ? v.c[lc.x] : 0.0f;
-  T J[3][3];
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    const int id = k == 0 ? lc.y : (k == 1 ? lc.z : lc.w);
-    F.a[1] = v.a[id];
-    F.b[1] = v.b[id];
-    F.lz[1] = LO ? v.c[id] : 0.0f;
-#pragma unroll
-    for (int r = 0; r < 3; ++r) {
-      if constexpr (MODE == kF32) J[r][k] = f32_edge(F, 1, 0, r);
-      else if constexpr (MODE == kDW) J[r][k] = dw_edge2(F, 1, 0, r);
-      else J[r][k] = rec_x(F.a[1], F.b[1], F.lz[1], r) - rec_x(F.a[0], F.b[0], F.lz[0], r);
-    }
-  }
-  if constexpr (MODE == kDW) dw_cofactors(J, f);
-  else cofactors<T>(J, f);
-  if constexpr (MODE == kF32) {
-    if (c0) {
-      float f2[3], f3[3];
-#pragma unroll
-      for (int r = 0; r < 3; ++r) {
-        f2[r] = J[r][1] - J[r][0];
-        f3[r] = J[r][2] - J[r][0];
-      }
-      c0[0] = f3[1] * f2[2] - f3[2] * f2[1];
-      c0[1] = f3[2] * f2[0] - f3[0] * f2[2];
-      c0[2] = f3[0] * f2[1] - f3[1] * f2[0];
-    }
-  }
-  if constexpr (MODE == kF64) return false;
-  else return det_cancels<T>(J, f);
-}
-
-// Near-degenerate elements: the FP64 geometry of a staged item, out of line and
-// returned by value (no register of the caller is passed by address).
-template <typename T>
-static __device__ __noinline__ Cof<T> staged_geometry_fp64(StagedVerts v, ushort4 lc)
-{
-  FetchAbs D;
-  fetch_staged<true>(v, lc, D);
-  Cof<double> g;
-  geometry_fp64(D, g);
-  Cof<T> f;
-  store_geometry(g, f);
-  return f;
 }
 
 // near-degenerate elements: FP64 geometry from the mesh's FP64 coordinates
@@ -551,23 +378,6 @@ __device__ __forceinline__ void p1_stiff_unique<ff>(const Cof<ff>& f, ff s, ff K
   K[0] = -(K[1] + K[2] + K[3]);
 }
 
-// C_0 = (x3 - x1) x (x2 - x1) (= -(C_1 + C_2 + C_3)) in FP64 from the exact
-// staged coordinates (the rare path): the edges of the face opposite vertex 0,
-// then their cross product, accurate to its own magnitude.
-__device__ __forceinline__ void staged_c0(const FetchAbs& F, double C0[3])
-{
-  double f2[3], f3[3];
-#pragma unroll
-  for (int r = 0; r < 3; ++r) {
-    const double x1 = rec_x(F.a[1], F.b[1], F.lz[1], r);
-    f2[r] = rec_x(F.a[2], F.b[2], F.lz[2], r) - x1;
-    f3[r] = rec_x(F.a[3], F.b[3], F.lz[3], r) - x1;
-  }
-  C0[0] = f3[1] * f2[2] - f3[2] * f2[1];
-  C0[1] = f3[2] * f2[0] - f3[0] * f2[2];
-  C0[2] = f3[0] * f2[1] - f3[1] * f2[0];
-}
-
 // P1 stiffness with every vertex gradient explicit: C_0 given, the entries of
 // vertex 0 as s (C_0 . C_j); the others as in p1_stiff_unique.
 template <typename T>
@@ -610,38 +420,12 @@ __device__ __forceinline__ void p1_stiff_direct<ff>(const Cof<ff>& f, const ff C
   K[9] = ff_mul(s, ff_dot3(col[2], col[2]));
 }
 
-// The rare P1 stiffness elements (p1_class): their geometry in FP64 from the exact
-// staged coordinates, C_0 from its own face, returned by value (out of line, and
-// no register of the caller is passed by address, so the common path keeps its
-// registers).
+// A P1 element matrix returned by value (the out-of-line rare paths: no register
+// of the caller is passed by address, so the common path keeps its registers).
 template <typename T>
 struct RareK {
   T K[10];
 };
-template <int MODE>
-static __device__ __noinline__ RareK<typename Arith<MODE>::T> staged_rare_stiffness(StagedVerts v, ushort4 lc,
-                                                                                   double coef, double wsum,
-                                                                                   uint32_t* flags)
-{
-  using T = typename Arith<MODE>::T;
-  FetchAbs F;
-  fetch_staged<true>(v, lc, F);
-  Cof<double> d;
-  geometry_fp64(F, d);
-  double c0[3];
-  staged_c0(F, c0);
-  Cof<T> f;
-  store_geometry(d, f);
-  T C0[3];
-#pragma unroll
-  for (int k = 0; k < 3; ++k) C0[k] = from_double<T>(c0[k]);
-  const T s = Arith<MODE>::from(coef) * Arith<MODE>::from(wsum) / f.det;
-  RareK<T> r;
-  p1_stiff_direct<T>(f, C0, s, r.K);
-  if constexpr (MODE == kDW)
-    if (!dw_scale_ok(s) || !dw_scale_ok(r.K[4])) atomicOr(flags, 2u);
-  return r;
-}
 
 // The six scaled metric coefficients s (C_a . C_b), ab = 00,11,22,01,02,12.
 template <typename T>
@@ -682,590 +466,365 @@ __device__ __forceinline__ ff metric_dot<ff>(const ff g[6], const ff* tab, int N
   return two_sum(hi, lo);
 }
 
-struct AsmArgs {
-  const BlockDesc* blocks;
-  const unsigned char* chunk_data;  // chunk records (layout at ChunkDesc)
-  const int2* chunk_rec;            // (offset / 16, bytes) per chunk
-  const int64_t* chunk_wb;          // first contribution word of each chunk (n_chunks + 1; contiguous)
-  const uint32_t* entries;
-  const int2* row_meta;             // (accumulator base, CSR start - base) per owned row
-  const double* coeff;   // per element in Morton order (indexed by the records' ranks), or null
-  double cconst;         // used when coeff is null
-  const double* tables;  // unique-entry tables: stiff[6][nu] then mass[nu]
-  double wsum;
-  void* values;
-  uint32_t* counters;
-  int nblocks;
-  int stiff;
-  int ent_cap;           // words of one shared-memory contribution buffer
-  int stage_cap;         // bytes of one chunk-record stage (the largest record)
-  uint32_t wait_limit;   // polls of a pipeline wait before it gives up (mbar_wait)
-};
+// ------------------------------------------------------- gather assembly --
+// Two passes, each element computed once:
+//   k_elem_mat     one thread per element, along the plan's Morton order p: the
+//                  unique entries u of its (symmetric) element matrix into the
+//                  plan's element-matrix array em;
+//   k_slot_gather  one thread per diagonal or upper CSR entry: the sum of the em
+//                  entries of every element holding both of its dofs, in
+//                  ascending p (the slot map, build_slot_map), written to the
+//                  entry and to its mirror -- a fixed order, so the values are
+//                  bitwise reproducible, with no atomics.
 
-constexpr size_t align16(size_t n) { return (n + 15) / 16 * 16; }
-
-// Barriers of k_assemble (mbarriers in shared memory).  "full" barriers complete
-// when a bulk copy has landed (producer arrival + transaction bytes); "empty"
-// barriers when the consumers have finished with a buffer; the token barriers
-// hand the right to update the accumulators from one consumer group to the
-// next.
-enum {
-  kBarRecFull = 0,                        // [kRecStages] chunk-record stages
-  kBarRecEmpty = kBarRecFull + kRecStages,  // [kRecStages]
-  kBarEntFull = kBarRecEmpty + kRecStages,  // [kWordStages] contribution-word stages
-  kBarEntEmpty = kBarEntFull + kWordStages,  // [kWordStages]
-  kBarMetaFull = kBarEntEmpty + kWordStages, // row metadata of a block
-  kBarMetaEmpty = kBarMetaFull + 1,
-  kBarBlkFull = kBarMetaEmpty + 1,          // [2] block descriptors
-  kBarBlkEmpty = kBarBlkFull + 2,           // [2]
-  kBarToken = kBarBlkEmpty + 2,             // [kMaxGroups] group g may run phase 2
-  kMaxGroups = 3,
-  kNumBars = kBarToken + kMaxGroups
-};
-
-// Consumer groups of kThreads threads per CTA, plus one producer warp.  Two
-// groups (17 warps: at most 5 on one SM sub-partition, 5 x 32 x 96 of its 16 K
-// registers) in every mode.  The kernel takes up to kMaxGroups; three FP32
-// groups (25 warps, which caps a thread at 72 registers) were measured slower
-// on GB300 at P1 128^3 (0.906 against 0.859 ms; the P1 FP32 element math
-// spills at 72 registers) and at P2 48^3 (0.496 against 0.484 ms).
-template <int MODE> struct AsmShape {
-  static constexpr int groups = 2;
-  static constexpr int consumers = groups * kThreads;
-  static constexpr int threads = consumers + 32;
-  static constexpr int max_regs = 96;
-};
-static_assert(AsmShape<kF32>::groups <= kMaxGroups && AsmShape<kDW>::groups <= kMaxGroups, "token barriers");
-
-// Shared-memory layout of k_assemble.  Every region starts on a 16-byte
-// boundary: the bulk copies (chunk records, contribution words, row metadata)
-// require 16-byte aligned destinations, the mbarriers 8-byte.
-template <int ORDER, int MODE>
-struct AsmLayout {
+// Geometry of an element from the mesh's absolute node records, in the mode's
+// arithmetic; returns whether the determinant cancels (det_cancels).
+//  FP32          edges (hi_k - hi_0) + (mid_k - mid_0), to a float ulp of the
+//                edge; with c0 (P1 stiffness) also C_0 = (x3 - x1) x (x2 - x1)
+//                from the edge columns;
+//  double-word   edges dw_diff3 of the three floats: the exact FP64 difference
+//                of the mesh coordinates (the reference's x_k - x_0) to ~2^-47;
+//  FP64          from the FP64 coordinates.
+template <int MODE>
+__device__ __forceinline__ bool geometry_abs_lazy(const GeoPtrs& g, int4 n, Cof<typename Arith<MODE>::T>& f,
+                                                  float* c0)
+{
   using T = typename Arith<MODE>::T;
-  static constexpr int NB = ORDER == 1 ? 4 : 10;
-  static constexpr int NU = ORDER == 1 ? 10 : 55;
-  static constexpr int CI = ORDER == 1 ? kChunkP1 : kChunkP2;
-  static constexpr size_t acc_bytes = align16(sizeof(T) * (kAccMax + 1));  // + the padding words' dummy slot
-  static constexpr size_t buf_bytes = align16(sizeof(T) * (NU * CI + 1));  // per group, + the zero source
-  static constexpr size_t tab_bytes = align16(sizeof(T) * 7 * NU);
-  // an aligned copy of a block's rows (and the row after) spans at most kRowsMax + 3 entries
-  static constexpr size_t meta_bytes = align16(8 * (kRowsMax + 4));
-  static constexpr size_t blk_bytes = 2 * sizeof(BlockDesc);
-  static constexpr size_t off_buf = acc_bytes;
-  static constexpr int G = AsmShape<MODE>::groups;
-  static constexpr size_t off_tab = off_buf + G * buf_bytes;
-  // P2: per group, the 6 scale factors of each item of a chunk (computed once per item)
-  static constexpr size_t geo_bytes = ORDER == 2 ? align16(sizeof(T) * CI * 6) : 0;
-  static constexpr size_t off_geo = off_tab + tab_bytes;
-  static constexpr size_t off_meta = off_geo + G * geo_bytes;
-  static constexpr size_t off_blk = off_meta + meta_bytes;
-  static constexpr size_t off_bars = off_blk + blk_bytes;
-  static constexpr size_t off_stage = off_bars + align16(8 * kNumBars);
-  static_assert(off_buf % 16 == 0 && off_tab % 16 == 0 && off_geo % 16 == 0 && off_meta % 16 == 0 && off_blk % 16 == 0 &&
-                    off_bars % 16 == 0 && off_stage % 16 == 0 && buf_bytes % 16 == 0,
-                "shared-memory regions must start on 16-byte boundaries");
-  __host__ __device__ static size_t stage_bytes(int stage_cap) { return ((size_t)stage_cap + 15) / 16 * 16; }
-  __host__ __device__ static size_t words_bytes(int ent_cap) { return ((size_t)ent_cap * 4 + 15) / 16 * 16; }
-  __host__ __device__ static size_t off_words(int stage_cap) { return off_stage + kRecStages * stage_bytes(stage_cap); }
-  __host__ __device__ static size_t total(int ent_cap, int stage_cap)
-  {
-    return off_words(stage_cap) + kWordStages * words_bytes(ent_cap);
+  T J[3][3];
+  if constexpr (MODE == kF64) {
+    const double4_32a x0 = g.xyz[n.x];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const double4_32a xk = g.xyz[k == 0 ? n.y : (k == 1 ? n.z : n.w)];
+#pragma unroll
+      for (int r = 0; r < 3; ++r) J[r][k] = comp(xk, r) - comp(x0, r);
+    }
+    cofactors<double>(J, f);
+    return false;
+  } else {
+    const float4 a0 = g.rec[2 * (int64_t)n.x], b0 = g.rec[2 * (int64_t)n.x + 1];
+    const float lz0 = MODE == kDW ? g.loz[n.x] : 0.0f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const int64_t id = k == 0 ? n.y : (k == 1 ? n.z : n.w);
+      const float4 ak = g.rec[2 * id], bk = g.rec[2 * id + 1];
+      const float lzk = MODE == kDW ? g.loz[id] : 0.0f;
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        if constexpr (MODE == kF32)
+          J[r][k] = (rec_hi(ak, r) - rec_hi(a0, r)) + (rec_mid(ak, bk, r) - rec_mid(a0, b0, r));
+        else
+          J[r][k] = dw_diff3(rec_hi(ak, r), rec_hi(a0, r), rec_mid(ak, bk, r), rec_mid(a0, b0, r), rec_lo(bk, lzk, r),
+                             rec_lo(b0, lz0, r));
+      }
+    }
+    if constexpr (MODE == kDW) dw_cofactors(J, f);
+    else cofactors<T>(J, f);
+    if constexpr (MODE == kF32) {
+      if (c0) {
+        float f2[3], f3[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+          f2[r] = J[r][1] - J[r][0];
+          f3[r] = J[r][2] - J[r][0];
+        }
+        c0[0] = f3[1] * f2[2] - f3[2] * f2[1];
+        c0[1] = f3[2] * f2[0] - f3[0] * f2[2];
+        c0[2] = f3[0] * f2[1] - f3[1] * f2[0];
+      }
+    }
+    return det_cancels<T>(J, f);
   }
+}
+
+// Near-degenerate elements: the FP64 geometry from the mesh's FP64 coordinates,
+// out of line and returned by value.
+template <typename T>
+static __device__ __noinline__ Cof<T> abs_geometry_fp64(const double4_32a* xyz, int4 n)
+{
+  Fetch<kF64> D;
+  D.x[0] = xyz[n.x];
+  D.x[1] = xyz[n.y];
+  D.x[2] = xyz[n.z];
+  D.x[3] = xyz[n.w];
+  Cof<double> g;
+  geometry(D, g);
+  Cof<T> f;
+  store_geometry(g, f);
+  return f;
+}
+
+// The rare P1 stiffness elements (p1_class, or a cancelling determinant): the
+// geometry in FP64 from the mesh's FP64 coordinates and C_0 from the face
+// opposite vertex 0, returned by value (out of line).
+template <int MODE>
+static __device__ __noinline__ RareK<typename Arith<MODE>::T> abs_rare_stiffness(const double4_32a* xyz, int4 n,
+                                                                                 double coef, double wsum,
+                                                                                 uint32_t* flags)
+{
+  using T = typename Arith<MODE>::T;
+  Fetch<kF64> D;
+  D.x[0] = xyz[n.x];
+  D.x[1] = xyz[n.y];
+  D.x[2] = xyz[n.z];
+  D.x[3] = xyz[n.w];
+  Cof<double> d;
+  geometry(D, d);
+  double f2[3], f3[3], c0[3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    f2[r] = comp(D.x[2], r) - comp(D.x[1], r);
+    f3[r] = comp(D.x[3], r) - comp(D.x[1], r);
+  }
+  c0[0] = f3[1] * f2[2] - f3[2] * f2[1];
+  c0[1] = f3[2] * f2[0] - f3[0] * f2[2];
+  c0[2] = f3[0] * f2[1] - f3[1] * f2[0];
+  Cof<T> f;
+  store_geometry(d, f);
+  T C0[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) C0[k] = from_double<T>(c0[k]);
+  const T s = Arith<MODE>::from(coef) * Arith<MODE>::from(wsum) / f.det;
+  RareK<T> r;
+  p1_stiff_direct<T>(f, C0, s, r.K);
+  if constexpr (MODE == kDW)
+    if (!dw_scale_ok(s) || !dw_scale_ok(r.K[4])) atomicOr(flags, 2u);
+  return r;
+}
+
+__device__ __forceinline__ void em_put(void* em, int64_t i, float v) { static_cast<float*>(em)[i] = v; }
+__device__ __forceinline__ void em_put(void* em, int64_t i, ff v)
+{
+  static_cast<float2*>(em)[i] = make_float2(v.hi, v.lo);
+}
+__device__ __forceinline__ void em_put(void* em, int64_t i, double v) { static_cast<double*>(em)[i] = v; }
+template <typename T> __device__ __forceinline__ T em_get(const void* em, uint32_t i);
+template <> __device__ __forceinline__ float em_get<float>(const void* em, uint32_t i)
+{
+  return __ldg(static_cast<const float*>(em) + i);
+}
+template <> __device__ __forceinline__ ff em_get<ff>(const void* em, uint32_t i)
+{
+  const float2 v = __ldg(static_cast<const float2*>(em) + i);
+  return ff{v.x, v.y};
+}
+template <> __device__ __forceinline__ double em_get<double>(const void* em, uint32_t i)
+{
+  return __ldg(static_cast<const double*>(em) + i);
+}
+
+struct ElemArgs {
+  int64_t n_elem;
+  const int32_t* elem_order;  // Morton position -> element (the caller's numbering)
+  const int32_t* dofs_m;      // dofs in Morton order (nb each; the first four are the vertices)
+  GeoPtrs geo;
+  const double* coeff;        // per element in the caller's order, or null
+  double cconst;              // used when coeff is null
+  const double* tables;       // unique-entry tables: stiff[6][nu] then mass[nu]
+  double wsum;
+  int stiff;
+  void* em;                   // out: nu x n_elem entries
+  uint32_t* flags;            // bit 0: NaN / Inf coefficient; bit 1: outside the double-word range
 };
 
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar)
-{
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
-}
-
-// Named barriers among consumer threads (the producer warp never takes part):
-// id 1 = all consumers, id 2 + g = consumer group g.  The _or forms return the
-// OR of `pred` over the participants.
-template <int ID, int COUNT>
-__device__ __forceinline__ void named_sync()
-{
-  asm volatile("bar.sync %0, %1;" ::"n"(ID), "n"(COUNT) : "memory");
-}
-template <int ID, int COUNT>
-__device__ __forceinline__ bool named_sync_or(bool pred)
-{
-  uint32_t r;
-  asm volatile(
-      "{\n"
-      " .reg .pred p, q;\n"
-      " setp.ne.u32 p, %1, 0;\n"
-      " bar.red.or.pred q, %2, %3, p;\n"
-      " selp.u32 %0, 1, 0, q;\n"
-      "}\n"
-      : "=r"(r)
-      : "r"((uint32_t)pred), "n"(ID), "n"(COUNT)
-      : "memory");
-  return r != 0;
-}
-__device__ __forceinline__ bool group_sync_or(int g, bool pred)
-{
-  if (g == 0) return named_sync_or<2, kThreads>(pred);
-  if (g == 1) return named_sync_or<3, kThreads>(pred);
-  return named_sync_or<4, kThreads>(pred);
-}
-
-// k_assemble: a persistent, warp-specialised kernel; per CTA one producer warp
-// and G consumer groups of kThreads threads (AsmShape).
-//
-// The producer (one thread) takes blocks from the work counter and streams, for
-// chunk q of the CTA (counted across its blocks), the chunk record into stage
-// q % kRecStages and the contribution words into buffer q % 2, then each
-// block's row metadata; it waits on an "empty" barrier before reusing a buffer
-// and runs several chunks (and across block boundaries) ahead.
-//
-// Consumer group g takes the chunks q with q % G == g:
-//   phase 1    wait record q; gather the element coefficients; element
-//              matrices from the staged vertices -> the group's buf
-//   barrier    (group) release record q
-//   phase 2    wait words q and the token (the previous group finished phase 2
-//              of chunk q - 1); add the contributions to the owned slots; pass
-//              the token on to the next group
-//   barrier    (group) release words q
-// so the groups' phase 1 runs beside another group's phase 2, while the
-// accumulator updates stay in chunk order (the sums are bitwise reproducible).
-// Per block both groups zero the accumulators first and write the owned rows
-// last.  Every wait is bounded; after a wait gives up the consumers keep their
-// barrier sequence but skip the work, leave together at the end of the block,
-// the producer stops issuing and lets its copies in flight land, and the CTA
-// records the failure.
-template <int ORDER, int MODE>
-__global__ void __launch_bounds__(AsmShape<MODE>::threads, 1) __maxnreg__(AsmShape<MODE>::max_regs)
-    k_assemble(AsmArgs a)
+// The P1 element matrix (10 unique entries) of Morton element p.
+template <int MODE>
+__device__ __forceinline__ void p1_element(const ElemArgs& a, const typename Arith<MODE>::T* tab, int64_t p,
+                                           typename Arith<MODE>::T K[10])
 {
   using A = Arith<MODE>;
   using T = typename A::T;
-  using L = AsmLayout<ORDER, MODE>;
-  constexpr int kGroups = AsmShape<MODE>::groups, kConsumers = AsmShape<MODE>::consumers;
-  constexpr int NU = L::NU, CI = L::CI, NS = kRecStages;
-  constexpr int TPI = ORDER == 1 ? 1 : kP2ThreadsPerItem;  // threads per item
-  extern __shared__ __align__(16) unsigned char smem[];
-  T* acc = reinterpret_cast<T*>(smem);
-  T* tab = reinterpret_cast<T*>(smem + L::off_tab);
-  int2* smeta = reinterpret_cast<int2*>(smem + L::off_meta);
-  BlockDesc* sblk = reinterpret_cast<BlockDesc*>(smem + L::off_blk);
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + L::off_bars);
-  unsigned char* stage = smem + L::off_stage;  // [NS][sbytes]
-  const int sbytes = (int)L::stage_bytes(a.stage_cap);
-  uint32_t* sent = reinterpret_cast<uint32_t*>(smem + L::off_words(a.stage_cap));  // [kWordStages][went]
-  const int went = (int)(L::words_bytes(a.ent_cap) / 4);
-
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  for (int i = tid; i < 7 * NU; i += blockDim.x) tab[i] = A::from(a.tables[i]);
-  if (tid == 0) {
-    for (int g = 0; g < kGroups; ++g) {
-      reinterpret_cast<T*>(smem + L::off_buf + g * L::buf_bytes)[NU * CI] = A::zero();
-    }
-    for (int k = 0; k < kNumBars; ++k) {
-      uint32_t count = 1;
-      if (k == kBarBlkEmpty || k == kBarBlkEmpty + 1) count = kConsumers;
-      if (k >= kBarToken && k < kBarToken + kMaxGroups) count = kThreads;
-      mbar_init(&bars[k], count);
-    }
-    mbar_fence_init();
-  }
-  __syncthreads();
-  auto stage_of = [&](int q) { return stage + (q % NS) * sbytes; };
-  auto desc_of = [&](int q) { return reinterpret_cast<const ChunkDesc*>(stage_of(q)); };
-  bool failed = false;
-
-  if (warp == kConsumers / 32) {
-    // ------------------------------------------------------------ producer
-    // Two lanes with independent waits: lane 0 takes the blocks and streams the
-    // contribution words and row metadata, lane 1 the chunk records.  Each runs
-    // up to NS (NW) chunks ahead of the consumers, across block boundaries, and
-    // waits only on the barrier of its own next copy; the word ranges and record
-    // places come from global tables, loaded ahead of those waits.
-    if (lane < 2) {
-      constexpr int NW = kWordStages;
-      int last_rec[NS], last_ent[NW], last_meta = -1;
-      for (int s = 0; s < NS; ++s) last_rec[s] = -1;
-      for (int s = 0; s < NW; ++s) last_ent[s] = -1;
-      auto wait = [&](int k, int parity) {
-        if (!failed && !mbar_wait(&bars[k], (uint32_t)parity, a.wait_limit)) failed = true;
-        return !failed;
-      };
-      int q = 0;
-      for (int j = 0;; ++j) {
-        int b = 0;
-        if (lane == 0) b = (int)atomicAdd(&a.counters[0], 1u);
-        b = __shfl_sync(0x3u, b, 0);
-        BlockDesc d;
-        if (b < a.nblocks) {
-          d = a.blocks[b];
-        } else {
-          d = BlockDesc{};
-          d.nchunks = -1;  // no more blocks
-        }
-        if (lane == 0) {
-          if (j >= 2 && !wait(kBarBlkEmpty + (j & 1), ((j >> 1) - 1) & 1)) d.nchunks = -1;
-          if (!failed) {
-            sblk[j & 1] = d;
-            mbar_arrive(&bars[kBarBlkFull + (j & 1)]);
-          }
-        }
-        if (__any_sync(0x3u, failed) || d.nchunks < 0) {
-          failed = __any_sync(0x3u, failed);
-          break;
-        }
-        const int n = d.nchunks;
-        if (lane == 1) {
-          // records: chunk c into stage (q + c) % NS once chunk q + c - NS is released
-          for (int c = 0; c < n; ++c) {
-            const int qq = q + c;
-            const int2 r = a.chunk_rec[d.chunk_begin + c];  // lands during the wait
-            if (qq >= NS && !wait(kBarRecEmpty + qq % NS, (qq / NS - 1) & 1)) break;
-            fence_proxy_async();
-            mbar_expect_tx(&bars[kBarRecFull + qq % NS], (uint32_t)r.y);
-            bulk_g2s(stage_of(qq), a.chunk_data + (int64_t)r.x * 16, (uint32_t)r.y, &bars[kBarRecFull + qq % NS]);
-            last_rec[qq % NS] = qq;
-          }
-        } else {
-          // words: chunk c into stage (q + c) % NW once chunk q + c - NW is released
-          for (int c = 0; c < n; ++c) {
-            const int qq = q + c;
-            const int64_t w0 = a.chunk_wb[d.chunk_begin + c], w1 = a.chunk_wb[d.chunk_begin + c + 1];
-            if (qq >= NW && !wait(kBarEntEmpty + qq % NW, (qq / NW - 1) & 1)) break;
-            const uint32_t bytes = (uint32_t)(w1 - w0) * 4u;
-            fence_proxy_async();
-            mbar_expect_tx(&bars[kBarEntFull + qq % NW], bytes);
-            if (bytes) bulk_g2s(sent + (qq % NW) * went, a.entries + w0, bytes, &bars[kBarEntFull + qq % NW]);
-            last_ent[qq % NW] = qq;
-          }
-          // the block's row metadata: rows row_begin .. row_begin + row_count and
-          // the row after, 16-byte aligned
-          if (!failed && (j == 0 || wait(kBarMetaEmpty, (j - 1) & 1))) {
-            const int i0 = d.row_begin & ~1, i1 = (d.row_begin + d.row_count + 2) & ~1;
-            fence_proxy_async();
-            mbar_expect_tx(&bars[kBarMetaFull], (uint32_t)(i1 - i0) * 8u);
-            bulk_g2s(smeta, a.row_meta + i0, (uint32_t)(i1 - i0) * 8u, &bars[kBarMetaFull]);
-            last_meta = j;
-          }
-        }
-        failed = __any_sync(0x3u, failed);
-        if (failed) break;
-        q += n;
-      }
-      if (failed) {
-        // let this lane's copies in flight land before the CTA's shared memory goes away
-        for (int s = 0; s < NS; ++s)
-          if (last_rec[s] >= 0) mbar_wait(&bars[kBarRecFull + s], (uint32_t)((last_rec[s] / NS) & 1), kWaitLimit);
-        for (int s = 0; s < NW; ++s)
-          if (last_ent[s] >= 0) mbar_wait(&bars[kBarEntFull + s], (uint32_t)((last_ent[s] / NW) & 1), kWaitLimit);
-        if (last_meta >= 0) mbar_wait(&bars[kBarMetaFull], (uint32_t)(last_meta & 1), kWaitLimit);
+  constexpr int NU = 10;
+  const double coef_d = a.coeff ? __ldg(a.coeff + a.elem_order[p]) : a.cconst;
+  const int4 n = reinterpret_cast<const int4*>(a.dofs_m)[p];
+  Cof<T> f;
+  float c0[3];
+  const bool degenerate = geometry_abs_lazy<MODE>(a.geo, n, f, MODE == kF32 && a.stiff ? c0 : nullptr);
+  // NaN / Inf coefficient: recorded for mg_plan_status (checked after the
+  // geometry, where the load has long landed)
+  if (((__double_as_longlong(coef_d) >> 52) & 0x7ff) == 0x7ff) atomicOr(a.flags, 1u);
+  const T coef = A::from(coef_d);
+  if (a.stiff) {
+    // the rare elements (p1_class, or a cancelling determinant) go out of line,
+    // entered only when a lane of the warp has one (~0.01 % of the elements)
+    const bool rare = degenerate || p1_class<T>(f) != kP1Common;
+    if (__any_sync(__activemask(), rare)) {
+      if (rare) {
+        const RareK<T> rk = abs_rare_stiffness<MODE>(a.geo.xyz, n, coef_d, a.wsum, a.flags);
+#pragma unroll
+        for (int u = 0; u < 10; ++u) K[u] = rk.K[u];
       }
     }
-    __syncwarp();
+    if (!rare) {
+      const T sc = coef * A::from(a.wsum) / f.det;
+      if constexpr (MODE == kF32) {
+        p1_stiff_direct<T>(f, c0, sc, K);  // C_0 from the face opposite vertex 0
+      } else {
+        p1_stiff_unique<T>(f, sc, K);
+        if constexpr (MODE == kDW)
+          if (!dw_scale_ok(sc) || !dw_scale_ok(K[4])) atomicOr(a.flags, 2u);
+      }
+    }
   } else {
-    // ----------------------------------------------------------- consumers
-    const int g = tid / kThreads;           // group
-    const int gtid = tid - g * kThreads;    // thread within the group
-    const int gwarp = gtid >> 5;
-    // item of the chunk and share of its entries: for P2 the lanes of a warp take
-    // the 32 items and the warps the entries (u = warp + 8k), so the entry-major
-    // stores buf[u * CI + item] of a warp hit consecutive words (the other way
-    // round, 8-way bank conflicts)
-    const int local = gtid % CI, sub = gtid / CI;
-    T* buf = reinterpret_cast<T*>(smem + L::off_buf + g * L::buf_bytes);
-    T* sgeo = reinterpret_cast<T*>(smem + L::off_geo + g * L::geo_bytes);  // P2: [6][CI]
-    const T wsum = A::from(a.wsum);
-    int q = 0, ntok = 0;  // chunks before this block; token waits so far
-    for (int j = 0;; ++j) {
-      if (!mbar_wait(&bars[kBarBlkFull + (j & 1)], (uint32_t)((j >> 1) & 1), a.wait_limit)) failed = true;
-      if (named_sync_or<1, kConsumers>(failed)) { failed = true; break; }
-      const BlockDesc d = sblk[j & 1];
-      mbar_arrive(&bars[kBarBlkEmpty + (j & 1)]);
-      if (d.nchunks < 0) break;
-      const int n = d.nchunks;
-      for (int i = tid; i < kAccMax; i += kConsumers) acc[i] = A::zero();
-      named_sync<1, kConsumers>();  // zeroed before any phase 2
-
-      for (int c = ((g - q) % kGroups + kGroups) % kGroups; c < n; c += kGroups) {
-        const int qq = q + c;
-        // ---- phase 1: element matrices of chunk c from its staged record
-        if (!failed && !mbar_wait(&bars[kBarRecFull + qq % NS], (uint32_t)((qq / NS) & 1), a.wait_limit)) failed = true;
-        int w_beg = 0, w_end = 0;  // this warp's contribution words (read before the record is released)
-        if (!failed) {
-          w_beg = desc_of(qq)->warp_off[gwarp];
-          w_end = desc_of(qq)->warp_off[gwarp + 1];
-        }
-        // the staged vertices of chunk c and the local vertex indices of item `it`
-        auto staged_verts = [&]() {
-          const unsigned char* rb = stage_of(qq);
-          const int n4 = (min(CI, d.item_count - c * CI) + 3) & ~3, nn = desc_of(qq)->n_nodes;
-          const unsigned char* v0 = rb + sizeof(ChunkDesc) + 12 * n4;
-          return StagedVerts{reinterpret_cast<const float4*>(v0), reinterpret_cast<const float4*>(v0 + 16 * nn),
-                             reinterpret_cast<const float*>(v0 + 32 * nn)};
-        };
-        auto item_lconn = [&](int it) {
-          const unsigned char* rb = stage_of(qq);
-          const int n4 = (min(CI, d.item_count - c * CI) + 3) & ~3;
-          return reinterpret_cast<const ushort4*>(rb + sizeof(ChunkDesc) + 4 * n4)[it];
-        };
-        // geometry and coefficient of item `it` of chunk c (from the staged
-        // record).  A near-degenerate element (det_cancels) gets its geometry in
-        // FP64 here unless `defer` is set (the P1 stiffness sends it down its own
-        // rare path); returns whether it is one.
-        auto item_geometry = [&](int it, Cof<T>& f, T& coef, double& coef_d, bool defer, float* c0 = nullptr) {
-          const unsigned char* rb = stage_of(qq);
-          const int rk = reinterpret_cast<const int32_t*>(rb + sizeof(ChunkDesc))[it];
-          coef_d = a.coeff ? __ldg(a.coeff + rk) : a.cconst;  // latency covered by the geometry
-          const ushort4 lc = item_lconn(it);
-          const StagedVerts sv = staged_verts();
-          const bool need = geometry_staged_lazy<MODE>(sv, lc, f, c0);
-          if constexpr (MODE != kF64) {
-            // entered only when a lane of the warp needs it
-            if (!defer && __any_sync(__activemask(), need)) {
-              if (need) f = staged_geometry_fp64<T>(sv, lc);
-            }
-          }
-          coef = A::from(coef_d);
-          // NaN / Inf coefficient: recorded for mg_plan_status (checked after the
-          // geometry, where the load has long landed)
-          if (((__double_as_longlong(coef_d) >> 52) & 0x7ff) == 0x7ff) atomicOr(&a.counters[4], 1u);
-          return need;
-        };
-        // double-word range of an element's scale factors, recorded for mg_plan_status
-        auto check_scale = [&](const T& x, const T& y) {
-          if constexpr (MODE == kDW)
-            if (!dw_scale_ok(x) || !dw_scale_ok(y)) atomicOr(&a.counters[4], 2u);
-        };
-        // P2 in the FP64 modes: the double-word geometry is worth computing once per
-        // item; FP32 recomputes it in each of the item's threads (no extra barrier)
-        constexpr bool kGeoOnce = ORDER == 2 && MODE != kF32;
-        if (ORDER == 2 && !kGeoOnce) {
-          if (!failed && c * CI + local < d.item_count) {
-            Cof<T> f;
-            T coef;
-            double coef_d;
-            item_geometry(local, f, coef, coef_d, false);
-            if (a.stiff) {
-              T gm[6];
-              metric<T>(f, coef / f.det, gm);
-              for (int u = sub; u < NU; u += TPI) buf[u * CI + local] = metric_dot<T>(gm, tab, NU, u);
-            } else {
-              const T sc = coef * f.det;
-              for (int u = sub; u < NU; u += TPI) buf[u * CI + local] = sc * tab[6 * NU + u];
-            }
-          }
-        } else if (ORDER == 1) {
-          if (!failed && c * CI + local < d.item_count) {
-            Cof<T> f;
-            T coef;
-            double coef_d;
-            float c0[3];  // FP32 stiffness: C_0 from the edge columns (geometry_staged_lazy)
-            const bool degenerate =
-                item_geometry(local, f, coef, coef_d, a.stiff != 0, MODE == kF32 && a.stiff ? c0 : nullptr);
-            T K[10];
-            if (a.stiff) {
-              // the rare elements (p1_class, or a cancelling determinant) go out of
-              // line, entered only when a lane of the warp has one; that path
-              // writes its entries itself
-              const bool rare = degenerate || p1_class<T>(f) != kP1Common;
-              // entered only when a lane of the warp has one (~0.01 % of the elements)
-              if (__any_sync(__activemask(), rare)) {
-                if (rare) {
-                  const RareK<T> rk =
-                      staged_rare_stiffness<MODE>(staged_verts(), item_lconn(local), coef_d, a.wsum, &a.counters[4]);
-#pragma unroll
-                  for (int u = 0; u < 10; ++u) K[u] = rk.K[u];
-                }
-              }
-              if (rare) {
-              } else if constexpr (MODE == kF32) {
-                // FP32: C_0 from the face opposite vertex 0, every element
-                p1_stiff_direct<T>(f, c0, coef * wsum / f.det, K);
-              } else {
-                const T sc = coef * wsum / f.det;
-                p1_stiff_unique<T>(f, sc, K);
-                check_scale(sc, K[4]);
-              }
-            } else {
-              const T sc = coef * f.det;
-              check_scale(sc, sc);
-#pragma unroll
-              for (int u = 0; u < 10; ++u) K[u] = sc * tab[6 * NU + u];
-            }
-#pragma unroll
-            for (int u = 0; u < 10; ++u) buf[u * CI + local] = K[u];
-          }
-        } else {
-          // P2: the first warp of the group computes each item's scale factors
-          // once (6 metric coefficients, or coef * det for the mass); then every
-          // thread forms its share of the item's 55 entries
-          if (!failed && gwarp == 0 && c * CI + lane < d.item_count) {
-            Cof<T> f;
-            T coef;
-            double coef_d;
-            item_geometry(lane, f, coef, coef_d, false);
-            if (a.stiff) {
-              T gm[6];
-              const T sc = coef / f.det;
-              metric<T>(f, sc, gm);
-              check_scale(sc, gm[0]);
-#pragma unroll
-              for (int k = 0; k < 6; ++k) sgeo[k * CI + lane] = gm[k];
-            } else {
-              const T sc = coef * f.det;
-              check_scale(sc, sc);
-              sgeo[lane] = sc;
-            }
-          }
-          failed = group_sync_or(g, failed);
-          if (!failed && c * CI + local < d.item_count) {
-            if (a.stiff) {
-              T gm[6];
-#pragma unroll
-              for (int k = 0; k < 6; ++k) gm[k] = sgeo[k * CI + local];
-              for (int u = sub; u < NU; u += TPI) buf[u * CI + local] = metric_dot<T>(gm, tab, NU, u);
-            } else {
-              const T sc = sgeo[local];
-              for (int u = sub; u < NU; u += TPI) buf[u * CI + local] = sc * tab[6 * NU + u];
-            }
-          }
-        }
-        failed = group_sync_or(g, failed);
-        if (gtid == 0) mbar_arrive(&bars[kBarRecEmpty + qq % NS]);
-        // ---- phase 2: segmented sums into owned slots.  Pieces of PW words of
-        // one slot are summed in registers and update the slot once; within a
-        // chunk every slot belongs to one thread, and the token orders the
-        // chunks.
-        if (!failed &&
-            !mbar_wait(&bars[kBarEntFull + qq % kWordStages], (uint32_t)((qq / kWordStages) & 1), a.wait_limit))
-          failed = true;
-        if (c >= 1) {
-          if (!failed && !mbar_wait(&bars[kBarToken + g], (uint32_t)(ntok & 1), a.wait_limit)) failed = true;
-          ++ntok;
-        }
-        if (!failed) {
-          // 8-byte pieces, [piece][lane] per warp (layout at piece_srcs)
-          const int K = (w_end - w_beg) / 64;
-          const uint2* ew = reinterpret_cast<const uint2*>(sent + (qq % kWordStages) * went + w_beg) + lane;
-#pragma unroll 2
-          for (int k = 0; k < K; ++k) {
-            const uint2 pc = ew[k * 32];
-            uint32_t slot;
-            T v;
-            if constexpr (ORDER == 1) {
-              slot = (pc.y >> (kP1SlotShift - 32)) & kSlotMask;
-              v = buf[pc.x & kP1SrcMask];
-              A::sum_into(v, buf[(pc.x >> kP1SrcBits) & kP1SrcMask]);
-              A::sum_into(v, buf[((pc.x >> (2 * kP1SrcBits)) | (pc.y << (32 - 2 * kP1SrcBits))) & kP1SrcMask]);
-              A::sum_into(v, buf[(pc.y >> (3 * kP1SrcBits - 32)) & kP1SrcMask]);
-            } else {
-              slot = (pc.x >> kSrcBits) & kSlotMask;
-              v = buf[pc.x & kSrcMask];
-              A::sum_into(v, buf[pc.y & kSrcMask]);
-            }
-            T a = acc[slot];
-            A::sum_into(a, v);
-            acc[slot] = a;
-          }
-        }
-        if (c + 1 < n) mbar_arrive(&bars[kBarToken + (g + 1) % kGroups]);  // release: the updates above precede
-        failed = group_sync_or(g, failed);
-        if (gtid == 0) mbar_arrive(&bars[kBarEntEmpty + qq % kWordStages]);
+    if constexpr (MODE != kF64) {
+      if (__any_sync(__activemask(), degenerate)) {
+        if (degenerate) f = abs_geometry_fp64<T>(a.geo.xyz, n);
       }
-      q += n;
-      if (!failed && !mbar_wait(&bars[kBarMetaFull], (uint32_t)(j & 1), a.wait_limit)) failed = true;
-      if (named_sync_or<1, kConsumers>(failed)) { failed = true; break; }
-      // ---- write the owned rows, one row per thread: the stores of a pass go
-      // to 32 rows at once, the accumulator reads (consecutive rows) spread
-      // over the banks
-      using Out = typename A::Out;
-      Out* out = reinterpret_cast<Out*>(a.values);
-      const int2* sm = smeta + (d.row_begin & 1);  // sm[i]: row i of the block
-      for (int r = tid; r - tid < d.row_count; r += kConsumers) {
-        int base = 0, len = 0, off = 0;
-        if (r < d.row_count) {
-          const int2 m = sm[r];
-          base = m.x;
-          off = m.y;
-          len = ((r + 1 < d.row_count) ? sm[r + 1].x : d.acc_used) - base;
-        }
-        const int maxlen = __reduce_max_sync(0xffffffffu, len);
-        Out* o = out + base + off;
-        const T* s0 = acc + base;
-#pragma unroll 4
-        for (int k = 0; k < maxlen; ++k)
-          if (k < len) o[k] = A::out(s0[k]);
-      }
-      named_sync<1, kConsumers>();
-      if (tid == 0) mbar_arrive(&bars[kBarMetaEmpty]);
     }
+    const T sc = coef * f.det;
+    if constexpr (MODE == kDW)
+      if (!dw_scale_ok(sc)) atomicOr(a.flags, 2u);
+#pragma unroll
+    for (int u = 0; u < 10; ++u) K[u] = sc * tab[6 * NU + u];
   }
-  if (failed && (tid == 0 || tid == kConsumers)) {
-    atomicExch(&a.counters[2], (uint32_t)kDevErrTimeout);
-    atomicExch(&a.counters[3], (uint32_t)blockIdx.x);
-  }
+}
+
+// One thread per element along the plan's Morton order p.  P1: the 10 entries of
+// each element staged in shared memory, then the CTA's contiguous range
+// em[p0 * 10 ..] written with coalesced stores (element-major).  P2: the 55
+// entries to em[u * E + p] (entry-major: the stores of one u coalesce across the
+// warp), the metric contraction reading the tables from shared memory.
+template <int ORDER, int MODE>
+__global__ void __launch_bounds__(256, ORDER == 1 ? 4 : 1) k_elem_mat(ElemArgs a)
+{
+  using A = Arith<MODE>;
+  using T = typename A::T;
+  constexpr int NU = ORDER == 1 ? 10 : 55;
+  __shared__ T tab[7 * NU];
+  for (int i = threadIdx.x; i < 7 * NU; i += blockDim.x) tab[i] = A::from(a.tables[i]);
   __syncthreads();
-  if (tid == 0) {
-    __threadfence();
-    if (atomicAdd(&a.counters[1], 1u) == gridDim.x - 1) {
-      a.counters[0] = 0;
-      a.counters[1] = 0;
-      __threadfence();
+  const int64_t E = a.n_elem;
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if constexpr (ORDER == 1) {
+    __shared__ T stage[256 * 10];
+    T K[10];
+    if (p < E) p1_element<MODE>(a, tab, p, K);
+#pragma unroll
+    for (int u = 0; u < 10; ++u) stage[threadIdx.x * 10 + u] = K[u];
+    __syncthreads();
+    const int64_t p0 = (int64_t)blockIdx.x * blockDim.x;
+    const int nvals = (int)min((int64_t)blockDim.x, E - p0) * 10;
+    for (int i = threadIdx.x; i < nvals; i += blockDim.x) em_put(a.em, p0 * 10 + i, stage[i]);
+  } else {
+    if (p >= E) return;
+    const double coef_d = a.coeff ? __ldg(a.coeff + a.elem_order[p]) : a.cconst;
+    const int32_t* dp = a.dofs_m + p * 10;
+    const int4 n = make_int4(dp[0], dp[1], dp[2], dp[3]);
+    Cof<T> f;
+    const bool degenerate = geometry_abs_lazy<MODE>(a.geo, n, f, nullptr);
+    if (((__double_as_longlong(coef_d) >> 52) & 0x7ff) == 0x7ff) atomicOr(a.flags, 1u);
+    const T coef = A::from(coef_d);
+    if constexpr (MODE != kF64) {
+      if (__any_sync(__activemask(), degenerate)) {
+        if (degenerate) f = abs_geometry_fp64<T>(a.geo.xyz, n);
+      }
+    }
+    if (a.stiff) {
+      T g[6];
+      const T sc = coef / f.det;
+      metric<T>(f, sc, g);
+      if constexpr (MODE == kDW)
+        if (!dw_scale_ok(sc) || !dw_scale_ok(g[0])) atomicOr(a.flags, 2u);
+#pragma unroll 5
+      for (int u = 0; u < NU; ++u) em_put(a.em, u * E + p, metric_dot<T>(g, tab, NU, u));
+    } else {
+      const T sc = coef * f.det;
+      if constexpr (MODE == kDW)
+        if (!dw_scale_ok(sc)) atomicOr(a.flags, 2u);
+#pragma unroll 5
+      for (int u = 0; u < NU; ++u) em_put(a.em, u * E + p, sc * tab[6 * NU + u]);
     }
   }
 }
 
-// Per kernel instantiation and device: SM count, opt-in shared-memory limit and
-// the dynamic shared-memory size the kernel attribute has been raised to
-// (only ever raised, so plans of different sizes and threads can share it).
-struct KernelLaunchCache {
-  static constexpr int kMaxDevices = 64;
-  std::mutex mu;
-  int sms[kMaxDevices] = {};
-  int max_smem[kMaxDevices] = {};
-  size_t attr_smem[kMaxDevices] = {};
-};
+// Sums the sources of the diagonal and upper CSR entries t, K loads in flight
+// (their indices, then their values), in the slot map's order, and writes each
+// sum to the entry and to its mirror (the operators are symmetric).
+template <int MODE, int K>
+__global__ void __launch_bounds__(256) k_slot_gather(int64_t n_upper, const int32_t* __restrict__ useg,
+                                                     const int32_t* __restrict__ uslot,
+                                                     const int32_t* __restrict__ umirror,
+                                                     const uint32_t* __restrict__ src, const void* __restrict__ em,
+                                                     typename Arith<MODE>::Out* __restrict__ values)
+{
+  using A = Arith<MODE>;
+  using T = typename A::T;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= n_upper) return;
+  int32_t k = useg[t];
+  const int32_t k1 = useg[t + 1];
+  T v = A::zero();
+  for (; k < k1; k += K) {
+    uint32_t idx[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) idx[j] = k + j < k1 ? __ldg(src + k + j) : 0u;
+    T x[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) x[j] = k + j < k1 ? em_get<T>(em, idx[j]) : A::zero();
+#pragma unroll
+    for (int j = 0; j < K; ++j)
+      if (k + j < k1) A::sum_into(v, x[j]);
+  }
+  const typename A::Out o = A::out(v);
+  const int32_t s = uslot[t], m = umirror[t];
+  values[s] = o;
+  if (m != s) values[m] = o;
+}
+
+// The element-matrix array of a plan (allocated by its first assembly).
+static mg_status plan_gather(mg_plan* p)
+{
+  std::lock_guard<std::mutex> lock(p->upload_mu);
+  if (!p->d_em) {
+    const int64_t n = (int64_t)nunique(p->mesh->order) * p->mesh->n_elem;
+    MG_CUDA(cudaMalloc(&p->d_em, sizeof(double) * (size_t)std::max<int64_t>(n, 1)));
+  }
+  return MG_OK;
+}
 
 template <int ORDER, int MODE>
-static mg_status launch_assemble_t(AsmArgs a, cudaStream_t st)
+static mg_status launch_gather_t(mg_plan* p, const ElemArgs& a, void* d_values, cudaStream_t st)
 {
-  using L = AsmLayout<ORDER, MODE>;
-  const size_t smem = L::total(a.ent_cap, a.stage_cap);
-  static KernelLaunchCache cache;
-  int dev = 0, sms = 0, per_sm = 0;
-  MG_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= KernelLaunchCache::kMaxDevices) return set_error(MG_ERR_UNSUPPORTED, "device index above 63");
-  {
-    std::lock_guard<std::mutex> lock(cache.mu);
-    if (!cache.sms[dev]) {
-      MG_CUDA(cudaDeviceGetAttribute(&cache.sms[dev], cudaDevAttrMultiProcessorCount, dev));
-      MG_CUDA(cudaDeviceGetAttribute(&cache.max_smem[dev], cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    }
-    if (smem > (size_t)cache.max_smem[dev])
-      return set_error(MG_ERR_SIZE, "assembly CTA needs " + std::to_string(smem) + " bytes of shared memory, above " +
-                                        std::to_string(cache.max_smem[dev]) + " (chunks touch too many vertices)");
-    if (cache.attr_smem[dev] < smem) {
-      MG_CUDA(cudaFuncSetAttribute(k_assemble<ORDER, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      cache.attr_smem[dev] = smem;
-    }
-    sms = cache.sms[dev];
-  }
-  constexpr int threads = AsmShape<MODE>::threads;
-  MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_assemble<ORDER, MODE>, threads, smem));
-  if (per_sm < 1) return set_error(MG_ERR_SIZE, "assembly CTA does not fit on an SM (shared memory or registers)");
-  const int grid = std::max(1, std::min(a.nblocks, per_sm * sms));
-  if (a.nblocks > 0) k_assemble<ORDER, MODE><<<grid, threads, smem, st>>>(a);
+  const int64_t E = a.n_elem;
+  if (E > 0) k_elem_mat<ORDER, MODE><<<(unsigned)((E + 255) / 256), 256, 0, st>>>(a);
+  MG_CUDA(cudaGetLastError());
+  using Out = typename Arith<MODE>::Out;
+  const unsigned g = (unsigned)((p->n_upper + 255) / 256);
+  Out* o = static_cast<Out*>(d_values);
+  // 8 sources in flight per thread (measured on GB300 at P1 128^3 and P2 48^3
+  // against 4 and 16)
+  if (p->n_upper > 0)
+    k_slot_gather<MODE, 8><<<g, 256, 0, st>>>(p->n_upper, p->d_useg, p->d_uslot, p->d_umirror, p->d_src, p->d_em, o);
   MG_CUDA(cudaGetLastError());
   return MG_OK;
 }
 
-// The coefficient in the plan's Morton element order: a chunk's items are
-// consecutive ranks of one block, so the assembly reads it in runs (its elements
-// are neighbours; the caller's element order may be arbitrary).
-__global__ void __launch_bounds__(256) k_coeff_morton(int64_t n_elem, const int32_t* __restrict__ elem_order,
-                                                      const double* __restrict__ coeff, double* __restrict__ out)
+static mg_status launch_assemble_gather(mg_plan* p, int op, const double* d_coeff, double c, const RefTables* t,
+                                        const double* d_tab, int prec, void* d_values, cudaStream_t st)
 {
-  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (r < n_elem) out[r] = __ldg(coeff + elem_order[r]);
+  MG_TRY(plan_gather(p));
+  mg_mesh* m = p->mesh;
+  const bool needs_coeff = (op == MG_OP_STIFF_KAPPA || op == MG_OP_MASS_COEFF);
+  ElemArgs a;
+  a.n_elem = m->n_elem;
+  a.elem_order = p->d_elem_order;
+  a.dofs_m = p->d_dofs_morton;
+  a.geo = GeoPtrs{m->d_xyz, m->d_node_rec, m->d_lo_z};
+  a.coeff = needs_coeff ? d_coeff : nullptr;
+  a.cconst = op == MG_OP_STIFF_CONST ? c : 1.0;
+  a.tables = d_tab;
+  a.wsum = t->wsum;
+  a.stiff = (op == MG_OP_STIFF_KAPPA || op == MG_OP_STIFF_CONST);
+  a.em = p->d_em;
+  a.flags = p->d_counters + 4;
+  if (m->order == 1) {
+    if (prec == MG_F32) return launch_gather_t<1, kF32>(p, a, d_values, st);
+    return prec == MG_F64_NATIVE ? launch_gather_t<1, kF64>(p, a, d_values, st)
+                                 : launch_gather_t<1, kDW>(p, a, d_values, st);
+  }
+  if (prec == MG_F32) return launch_gather_t<2, kF32>(p, a, d_values, st);
+  return prec == MG_F64_NATIVE ? launch_gather_t<2, kF64>(p, a, d_values, st)
+                               : launch_gather_t<2, kDW>(p, a, d_values, st);
 }
 
 mg_status launch_assemble(mg_plan* p, int op, const double* d_coeff, double c, int quad, int prec,
@@ -1283,41 +842,7 @@ mg_status launch_assemble(mg_plan* p, int op, const double* d_coeff, double c, i
   if (p->nnz == 0) return MG_OK;  // empty mesh: nothing to write
   if (!d_values) return set_error(MG_ERR_INVALID_ARG, "mg_assemble: null values");
   MG_TRY(plan_device(p));
-  mg_mesh* m = p->mesh;
-  AsmArgs a;
-  a.blocks = p->d_blocks;
-  a.chunk_data = p->d_chunk_data;
-  a.chunk_rec = p->d_chunk_rec;
-  a.chunk_wb = p->d_chunk_wb;
-  a.entries = p->d_entries;
-  a.row_meta = p->d_row_meta;
-  a.coeff = nullptr;
-  if (needs_coeff) {
-    {
-      std::lock_guard<std::mutex> lock(p->upload_mu);
-      if (!p->d_coeff_m) MG_CUDA(cudaMalloc(&p->d_coeff_m, sizeof(double) * m->n_elem));
-    }
-    k_coeff_morton<<<(unsigned)((m->n_elem + 255) / 256), 256, 0, st>>>(m->n_elem, p->d_elem_order, d_coeff,
-                                                                        p->d_coeff_m);
-    MG_CUDA(cudaGetLastError());
-    a.coeff = p->d_coeff_m;
-  }
-  a.cconst = op == MG_OP_STIFF_CONST ? c : 1.0;
-  a.tables = d_tab;
-  a.wsum = t->wsum;
-  a.values = d_values;
-  a.counters = p->d_counters;
-  a.nblocks = p->nblocks;
-  a.stiff = (op == MG_OP_STIFF_KAPPA || op == MG_OP_STIFF_CONST);
-  a.ent_cap = (int)((p->max_chunk_entries + 3) / 4 * 4);
-  a.stage_cap = std::max(p->max_rec_bytes, 64);
-  a.wait_limit = p->wait_limit;
-  if (m->order == 1) {
-    if (prec == MG_F32) return launch_assemble_t<1, kF32>(a, st);
-    return prec == MG_F64_NATIVE ? launch_assemble_t<1, kF64>(a, st) : launch_assemble_t<1, kDW>(a, st);
-  }
-  if (prec == MG_F32) return launch_assemble_t<2, kF32>(a, st);
-  return prec == MG_F64_NATIVE ? launch_assemble_t<2, kF64>(a, st) : launch_assemble_t<2, kDW>(a, st);
+  return launch_assemble_gather(p, op, d_coeff, c, t, d_tab, prec, d_values, st);
 }
 
 // --------------------------------------------------------------- Dirichlet --
@@ -1622,28 +1147,18 @@ mg_status mg_plan_status(mg_plan* p)
   if (!p) return set_error(MG_ERR_INVALID_ARG, "mg_plan_status: null plan");
   if (!p->on_device) return MG_OK;
   MG_CUDA(cudaDeviceSynchronize());
-  uint32_t c[5];
-  MG_CUDA(cudaMemcpy(c, p->d_counters, sizeof(c), cudaMemcpyDeviceToHost));
-  if (c[2] || c[4]) {
-    const uint32_t zero[3] = {0u, 0u, 0u};
-    MG_CUDA(cudaMemcpy(p->d_counters + 2, zero, sizeof(zero), cudaMemcpyHostToDevice));
+  uint32_t flags = 0;
+  MG_CUDA(cudaMemcpy(&flags, p->d_counters + 4, sizeof(flags), cudaMemcpyDeviceToHost));
+  if (flags) {
+    const uint32_t zero = 0u;
+    MG_CUDA(cudaMemcpy(p->d_counters + 4, &zero, sizeof(zero), cudaMemcpyHostToDevice));
   }
-  if (c[2])
-    return set_error(MG_ERR_CUDA, "assembly kernel: a bulk-copy wait timed out in CTA " + std::to_string(c[3]) +
-                                      "; the values of that call are incomplete");
-  if (c[4] & 1u)
+  if (flags & 1u)
     return set_error(MG_ERR_INVALID_ARG, "assembly: the coefficient array holds NaN or Inf (the values are not usable)");
-  if (c[4] & 2u)
+  if (flags & 2u)
     return set_error(MG_ERR_UNSUPPORTED,
                      "assembly: element-matrix scales outside 2^-96 .. 2^112, where the double-word MG_F64 "
                      "assembly keeps 1e-12 accuracy; use MG_F64_NATIVE or rescale the coefficient by a power of two");
-  return MG_OK;
-}
-
-mg_status mg_plan_set_wait_limit(mg_plan* p, uint32_t polls)
-{
-  if (!p) return set_error(MG_ERR_INVALID_ARG, "mg_plan_set_wait_limit: null plan");
-  p->wait_limit = polls;
   return MG_OK;
 }
 

@@ -274,9 +274,7 @@ mg_status build_pattern_device(mg_plan* p, cudaStream_t st, bool keep_device)
     MG_CUDA(cudaMemcpyAsync(p->colind.data(), d.colind, sizeof(int32_t) * nnz, cudaMemcpyDeviceToHost, st));
   MG_CUDA(cudaStreamSynchronize(st));
   p->nnz = nnz;
-  for (int64_t r = 0; r < nd; ++r)
-    if (p->rowptr[r + 1] - p->rowptr[r] > kAccMax) return set_error(MG_ERR_SIZE, "a CSR row has more than 8192 entries");
-  if (keep_device) {  // the device copies become the plan's (the schedule is built from them)
+  if (keep_device) {  // the device copies become the plan's (the plan's device state is built from them)
     p->d_rowptr = d.rowptr;
     p->d_colind = d.colind;
     d.rowptr = nullptr;

@@ -23,56 +23,78 @@ def sym_index(i, j, nb):
     return i * nb - i * (i - 1) // 2 + (j - i)
 
 
-def decode_pieces(words, order):
-    """The 8-byte contribution pieces of one warp's word range ([piece][lane], two
-    32-bit words each, the lower first) as (slot, sources) arrays of shape
-    (pieces, 32) and (pieces, 32, srcs): P1 four 12-bit sources at bits 0, 12,
-    24, 36 and the slot at bit 48; P2 two words source (13 bits) | slot << 13."""
-    w = np.asarray(words, dtype=np.uint64).reshape(-1, 32, 2)
-    pc = w[:, :, 0] | (w[:, :, 1] << np.uint64(32))
-    if order == 1:
-        srcs = np.stack([(pc >> np.uint64(12 * k)) & np.uint64(0xfff) for k in range(4)], axis=-1)
-        slot = (pc >> np.uint64(48)) & np.uint64(0x3fff)
-    else:
-        srcs = np.stack([w[:, :, 0] & np.uint64(0x1fff), w[:, :, 1] & np.uint64(0x1fff)], axis=-1)
-        slot = (w[:, :, 0] >> np.uint64(13)) & np.uint64(0x3fff)
-        assert np.array_equal(slot, (w[:, :, 1] >> np.uint64(13)) & np.uint64(0x3fff))
-    return slot.astype(np.int64), srcs.astype(np.int64)
+def morton_elem_order(xyz, conn):
+    """The assembly's element order restated: Morton keys (21 bits per axis over the
+    nodes' bounding box) of the centroids 0.25 x_v summed over v in order, sorted by
+    key, ties by element id."""
+    xyz = np.asarray(xyz, dtype=np.float64)
+    conn = np.asarray(conn, dtype=np.int64)
+    if len(conn) == 0:
+        return np.zeros(0, dtype=np.int32)
+    lo, hi = xyz.min(axis=0), xyz.max(axis=0)
+    c = np.zeros((len(conn), 3))
+    for v in range(4):
+        c = c + 0.25 * xyz[conn[:, v]]
+    key = np.zeros(len(conn), dtype=np.uint64)
+    for k in range(3):
+        t = (c[:, k] - lo[k]) / (hi[k] - lo[k]) if hi[k] > lo[k] else np.zeros(len(conn))
+        q = np.minimum(2097151.0, np.maximum(0.0, t * 2097151.0)).astype(np.uint64)
+        spread = np.zeros(len(conn), dtype=np.uint64)
+        for bit in range(21):
+            spread |= ((q >> np.uint64(bit)) & np.uint64(1)) << np.uint64(3 * bit)
+        key |= spread << np.uint64(k)
+    return np.lexsort((np.arange(len(conn)), key)).astype(np.int32)
 
 
-def emulate_schedule(sched, order, local_mats, nnz, rowptr):
-    """Runs the assembly kernel's two phases on the host with given element
-    matrices (local_mats[e] = [field i, test j]) -- checks the schedule only."""
-    info = sched["info"]
+def expected_slot_map(order, elem_order, dofs, rowptr, colind):
+    """The slot map of the gather assembly restated: for every diagonal or upper CSR
+    entry (r, c) in CSR order, its mirror (c, r) and the element-matrix entries of
+    every element holding both dofs, in ascending Morton position p, each
+    p * nu + u (P1, element-major) or u * E + p (P2), u = sym_index of the pair."""
     nb = 4 if order == 1 else 10
     nu = nb * (nb + 1) // 2
+    E = len(elem_order)
+    dm = np.asarray(dofs)[np.asarray(elem_order)]
+    contrib = {}
+    for p in range(E):
+        for i in range(nb):
+            for j in range(nb):
+                r, c = int(dm[p, i]), int(dm[p, j])
+                if c >= r:
+                    u = sym_index(i, j, nb)
+                    contrib.setdefault((r, c), []).append(p * nu + u if order == 1 else u * E + p)
+    useg, uslot, umirror, src = [0], [], [], []
+    for r in range(len(rowptr) - 1):
+        for k in range(rowptr[r], rowptr[r + 1]):
+            c = int(colind[k])
+            if c < r:
+                continue
+            uslot.append(k)
+            m0 = rowptr[c]
+            umirror.append(m0 + int(np.searchsorted(colind[m0:rowptr[c + 1]], r)))
+            src.extend(contrib.get((r, c), []))
+            useg.append(len(src))
+    return {"useg": np.array(useg, dtype=np.int32), "uslot": np.array(uslot, dtype=np.int32),
+            "umirror": np.array(umirror, dtype=np.int32), "src": np.array(src, dtype=np.uint32)}
+
+
+def emulate_slot_map(sm, order, elem_order, local_mats, nnz):
+    """The gather assembly run on the host with given element matrices
+    (local_mats[e] = [field i, test j]) through a slot map -- checks the map only."""
+    nb = 4 if order == 1 else 10
+    nu = nb * (nb + 1) // 2
+    E = len(elem_order)
+    em = np.zeros((E, nu))
     pairs = [(i, j) for i in range(nb) for j in range(i, nb)]
-    assert [sym_index(i, j, nb) for i, j in pairs] == list(range(nu))
-    CI, W = info.chunk_items, info.warps
-    out = np.zeros(nnz)
-    blocks, items, cptr, ent = sched["blocks"], sched["items"], sched["chunk_ptr"], sched["entries"]
-    rows, racc = sched["rows"], sched["row_acc"]
-    for b in range(info.nblocks):
-        ib, ic, cb, nc, rb, rc = (int(v) for v in blocks[b, :6])
-        acc = np.zeros(info.acc_max + 1)  # + the padding words' dummy slot
-        for c in range(nc):
-            buf = np.zeros(nu * CI + 1)
-            for t in range(min(CI, ic - c * CI)):
-                e = items[ib + c * CI + t]
-                for u, (i, j) in enumerate(pairs):
-                    buf[u * CI + t] = local_mats[e][i, j]
-            base = (cb + c) * (W + 1)
-            for w in range(W):
-                # [piece][lane]: a piece's sources go to its slot
-                slots, srcs = decode_pieces(ent[cptr[base + w]:cptr[base + w + 1]], order)
-                for lane in range(32):
-                    for slot, src in zip(slots[:, lane], srcs[:, lane]):
-                        v = buf[src[0]]
-                        for x in src[1:]:
-                            v += buf[x]
-                        acc[slot] += v
-        for r in range(rc):
-            row, a0 = rows[rb + r], racc[rb + r]
-            ln = rowptr[row + 1] - rowptr[row]
-            out[rowptr[row]:rowptr[row + 1]] = acc[a0:a0 + ln]
+    for p, e in enumerate(elem_order):
+        for u, (i, j) in enumerate(pairs):
+            em[p, u] = local_mats[e][i, j]
+    flat = em.reshape(-1) if order == 1 else em.T.reshape(-1)
+    out = np.full(nnz, np.nan)
+    for t in range(len(sm["uslot"])):
+        v = 0.0
+        for s in sm["src"][sm["useg"][t]:sm["useg"][t + 1]]:
+            v += flat[s]
+        out[sm["uslot"][t]] = v
+        out[sm["umirror"][t]] = v
     return out

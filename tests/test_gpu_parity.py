@@ -9,7 +9,7 @@ import pytest
 import morganapublic_gb300 as mg
 import oracle as orc
 from morganapublic_gb300 import meshgen
-from helpers import row_scaled_err
+from helpers import emulate_slot_map, expected_slot_map, row_scaled_err
 
 pytestmark = pytest.mark.gpu
 
@@ -263,10 +263,9 @@ def test_unreferenced_nodes_give_empty_rows():
 @pytest.mark.parametrize("case", ["p1", "p2_lex", "p2_first", "extra_nodes", "single", "no_elements", "p1_big",
                                   "p2_big"])
 def test_device_pattern_build_matches_host(case):
-    """mg_pattern_build_device (CSR pattern from sorted element-coupling keys, then
-    the assembly schedule -- blocks, items, chunk records, contribution words --
-    all on the GPU) gives the host build's arrays bit for bit, hence the same
-    values."""
+    """mg_pattern_build_device (CSR pattern from sorted element-coupling keys, the
+    Morton element order and the slot map, all on the GPU) gives the host build's
+    arrays bit for bit, hence the same values."""
     xyz1 = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], dtype=np.float64)
     if case == "single":
         xyz, conn, order, rule = xyz1, np.array([[0, 1, 2, 3]], dtype=np.int32), 1, "lex"
@@ -290,9 +289,8 @@ def test_device_pattern_build_matches_host(case):
     rp_h, ci_h = host.pattern()
     rp_d, ci_d = dev.pattern()
     assert np.array_equal(rp_h, rp_d) and np.array_equal(ci_h, ci_d)
-    sh, sd = host.export_schedule(), dev.export_schedule()
-    for f in ("nblocks", "n_items", "n_chunks", "n_entries", "n_contrib", "n_item_slots", "max_chunk_entries",
-              "max_chunk_vertices", "max_chunk_record_bytes"):
+    sh, sd = host.export_slot_map(), dev.export_slot_map()
+    for f in ("n_upper", "n_contrib", "n_elem", "nunique", "elem_major"):
         assert getattr(sh["info"], f) == getattr(sd["info"], f), f
     for k in sh:
         if k != "info":
@@ -673,27 +671,25 @@ def test_strongly_jittered_mesh_p2(jitter, seed):
     assert e64 <= F64_TOL and e32 <= 2 * F32_TOL
 
 
-@pytest.mark.parametrize("order,prec", [(1, "f64"), (1, "f32"), (2, "f64")])
-def test_bounded_wait_gives_up_and_the_plan_recovers(order, prec):
-    """The assembly pipeline's waits are bounded: with the limit lowered to 0
-    every wait gives up at once, the kernel returns (its last bulk copies land
-    first), mg_plan_status reports MG_ERR_CUDA, and with the default limit back
-    the same plan assembles the oracle's values again (the context stays usable)."""
-    m, kappa = _case(8 if order == 1 else 4, 0.2, 1, True, 1.0)
-    mesh = mg.Mesh(m.xyz, m.conn, order=order)
+@pytest.mark.parametrize("order,rule", [(1, "lex"), (2, "lex"), (2, "first")])
+@pytest.mark.parametrize("n,jitter", [(3, 0.2), (4, 0.0)])
+def test_slot_map_matches_restatement_and_oracle(order, rule, n, jitter):
+    """The device-built slot map equals its numpy restatement bit for bit (entries,
+    mirrors, sources in ascending Morton position), and summing the oracle's element
+    matrices through it gives the oracle's CSR values."""
+    m = meshgen.kuhn_cube(n, jitter=jitter, seed=8, permute=True)
+    kappa = meshgen.lognormal(len(m.conn), 1.0, 6)
+    mesh = mg.Mesh(m.xyz, m.conn, order=order, edge_rule=rule)
     b = mg.MatrixBuilder(mesh)
+    sm = b.export_slot_map()
+    rp, ci = b.pattern()
+    exp = expected_slot_map(order, sm["elem_order"], mesh.elem_dofs(), rp, ci)
+    for k in ("useg", "uslot", "umirror", "src"):
+        assert np.array_equal(sm[k], exp[k]), k
+    assert sm["info"].n_contrib == len(exp["src"]) and sm["info"].elem_major == (order == 1)
     quad = 4 if order == 1 else 15
-    _, rp, ci, ref = orc.full_operator("stiff_kappa", order, quad, m.xyz, m.conn, coeff=kappa)
-    v = b.assemble("stiff_kappa", coeff=kappa, quad=quad, prec=prec)
-    b.status()
-    b.set_wait_limit(0)
-    b.assemble("stiff_kappa", coeff=kappa, quad=quad, prec=prec, out=v)
-    with pytest.raises(mg.MorganaError) as err:
-        b.status()
-    assert err.value.status == mg.MG_ERR_CUDA
-    b.set_wait_limit()
-    b.status()  # the record was cleared
-    b.assemble("stiff_kappa", coeff=kappa, quad=quad, prec=prec, out=v)
-    b.status()
-    tol = F64_TOL if prec == "f64" else 2 * F32_TOL
-    assert row_scaled_err(rp, ref, v.cpu().numpy()) <= tol
+    dofs, rpo, cio, ref = orc.full_operator("stiff_kappa", order, quad, m.xyz, m.conn, coeff=kappa, edge_rule=rule)
+    mats = [orc.local_matrix("stiff_kappa", order, quad, m.xyz, m.conn[e], kappa=kappa[e]) for e in range(len(m.conn))]
+    got = emulate_slot_map(sm, order, sm["elem_order"], mats, b.nnz)
+    assert not np.isnan(got).any()
+    assert row_scaled_err(rp, ref, got) <= 1e-14

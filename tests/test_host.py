@@ -1,6 +1,6 @@
 """CPU tests of the product library's host side (no GPU calls): exported
 symbols, mesh ingest, edge/dof numbering and CSR pattern against the oracle,
-error paths, and the assembly schedule emulated on the host."""
+error paths, and the assembly's element order against its restatement."""
 import json
 import os
 import re
@@ -11,7 +11,7 @@ import pytest
 import morganapublic_gb300 as mg
 import oracle as orc
 from morganapublic_gb300 import meshgen
-from helpers import decode_pieces, emulate_schedule, row_scaled_err
+from helpers import morton_elem_order
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = os.path.join(ROOT, "tests", "golden")
@@ -66,37 +66,16 @@ def test_pattern_sizes_of_survey_formulas():
     assert b2.nnz == 230 * n ** 3 + 138 * n ** 2 + 24 * n + 1
 
 
-@pytest.mark.parametrize("order,op,quad", [(1, "stiff_kappa", 4), (1, "mass", 4), (2, "stiff_kappa", 15),
-                                           (2, "mass_coeff", 15)])
-def test_schedule_emulation_matches_oracle(order, op, quad):
-    """The exported schedule, run on the host with the oracle's element matrices,
-    reproduces the oracle's CSR values (same terms; the per-slot association of
-    the sum differs, so to a few ulps of the row)."""
-    m = meshgen.kuhn_cube(3, jitter=0.2, seed=4, permute=True)
-    kappa = meshgen.lognormal(len(m.conn), 1.0, 9)
-    mesh = mg.Mesh(m.xyz, m.conn, order=order)
-    builder = mg.MatrixBuilder(mesh)
-    sched = builder.export_schedule()
-    info = sched["info"]
-    nb = 4 if order == 1 else 10
-    assert info.n_contrib == len(m.conn) * nb * nb
-    assert info.n_items >= len(m.conn)
-    dofs, rp, ci, vals = orc.full_operator(op, order, quad, m.xyz, m.conn, coeff=kappa)
-    mats = np.stack([orc.local_matrix(op, order, quad, m.xyz, m.conn[e], kappa=kappa[e]) for e in range(len(m.conn))])
-    got = emulate_schedule(sched, order, mats, builder.nnz, rp)
-    assert row_scaled_err(rp, vals, got) <= 1e-14
-
-
-def test_schedule_covers_every_row_once():
-    m = meshgen.kuhn_cube(4, permute=True, seed=3)
-    builder = mg.MatrixBuilder(mg.Mesh(m.xyz, m.conn, order=2))
-    s = builder.export_schedule()
-    assert np.array_equal(np.sort(s["rows"]), np.arange(builder.ndof))
-    rp, _ = builder.pattern()
-    for b in range(s["info"].nblocks):
-        rb, rc, used = s["blocks"][b, 4], s["blocks"][b, 5], s["blocks"][b, 6]
-        rows = s["rows"][rb:rb + rc]
-        assert used == int(np.sum(rp[rows + 1] - rp[rows])) <= s["info"].acc_max
+@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("n,jitter,permute", [(3, 0.0, False), (5, 0.25, True)])
+def test_elem_order_matches_restatement(order, n, jitter, permute):
+    """The host plan's element order (a Morton curve of the centroids, ties by id)
+    equals its numpy restatement, and is a permutation of the elements."""
+    m = meshgen.kuhn_cube(n, jitter=jitter, seed=3, permute=permute)
+    b = mg.MatrixBuilder(mg.Mesh(m.xyz, m.conn, order=order))
+    eo = b.elem_order()
+    assert np.array_equal(np.sort(eo), np.arange(len(m.conn)))
+    assert np.array_equal(eo, morton_elem_order(m.xyz, m.conn))
 
 
 def test_gmsh_roundtrip(tmp_path):
@@ -170,50 +149,7 @@ def test_empty_and_single_tet():
     assert one.ndof == 10 and one.nnz == 100
 
 
-def test_export_schedule_info_fields():
-    m = meshgen.kuhn_cube(2)
-    b = mg.MatrixBuilder(mg.Mesh(m.xyz, m.conn))
-    info = b.schedule_info()
-    assert info.threads == 256 and info.warps == 8 and info.acc_max == 8192 and info.host_copy == 1
-    assert info.n_entries >= info.n_contrib
-    s = b.export_schedule()
-    # every block's item list is padded to a multiple of 4 with -1
-    assert len(s["items"]) % 4 == 0 and (s["items"] >= -1).all()
-
-
-@pytest.mark.parametrize("order", [1, 2])
-def test_schedule_slots_have_one_writer_per_chunk(order):
-    """Within a chunk each accumulator slot is written by exactly one thread (the
-    kernel's race freedom); a piece's first word carries its slot and a real
-    source; padding pieces target only the dummy slot with zero sources; real
-    slots lie inside the block."""
-    m = meshgen.kuhn_cube(4, jitter=0.2, seed=2, permute=True)
-    b = mg.MatrixBuilder(mg.Mesh(m.xyz, m.conn, order=order))
-    s = b.export_schedule()
-    info = s["info"]
-    nu = 10 if order == 1 else 55
-    zero = nu * info.chunk_items
-    for bk in range(info.nblocks):
-        cb, nc, used = s["blocks"][bk, 2], s["blocks"][bk, 3], s["blocks"][bk, 6]
-        for c in range(cb, cb + nc):
-            cp = s["chunk_ptr"][c * (info.warps + 1):(c + 1) * (info.warps + 1)]
-            owner = {}
-            PW = 4 if order == 1 else 2
-            for w in range(info.warps):
-                slots, srcl = decode_pieces(s["entries"][cp[w]:cp[w + 1]], order)
-                assert srcl.shape[2] == PW
-                for lane in range(32):
-                    t = 32 * w + lane
-                    for slot, srcs in zip(slots[:, lane], srcl[:, lane]):
-                        slot, srcs = int(slot), [int(x) for x in srcs]
-                        if slot == info.acc_max:
-                            assert all(x == zero for x in srcs)
-                            continue
-                        assert slot < used and all(x <= zero for x in srcs) and srcs[0] < zero
-                        assert owner.setdefault(slot, t) == t
-
-
-_SCHEDULE_DUMP = r"""
+_PLAN_DUMP = r"""
 import sys, pickle
 import numpy as np
 sys.path.insert(0, sys.argv[1])
@@ -224,28 +160,25 @@ for n, order in ((12, 1), (5, 2)):
     m = meshgen.kuhn_cube(n, jitter=0.25, seed=3, permute=True)
     b = mg.MatrixBuilder(mg.Mesh(m.xyz, m.conn, order=order))
     rp, ci = b.pattern()
-    sched = b.export_schedule()
-    out[(n, order)] = (rp, ci, {k: np.asarray(v) for k, v in sched.items() if k != "info"})
+    out[(n, order)] = (rp, ci, b.elem_order())
 pickle.dump(out, open(sys.argv[2], "wb"))
 """
 
 
 def test_plan_independent_of_thread_count(tmp_path):
-    """The host plan (pattern and assembly schedule) is built with OpenMP; its
+    """The host plan (pattern and element order) is built with OpenMP; its
     per-thread counts and fills must give the same arrays for any thread count."""
     import pickle
     import subprocess
     import sys
     script = tmp_path / "dump.py"
-    script.write_text(_SCHEDULE_DUMP)
+    script.write_text(_PLAN_DUMP)
     res = {}
     for nth in (1, 4):
         env = dict(os.environ, OMP_NUM_THREADS=str(nth))
         out = tmp_path / f"s{nth}.pkl"
         subprocess.run([sys.executable, str(script), ROOT, str(out)], env=env, check=True, timeout=300)
         res[nth] = pickle.load(open(out, "rb"))
-    for key, (rp, ci, sched) in res[1].items():
-        rp4, ci4, sched4 = res[4][key]
-        assert np.array_equal(rp, rp4) and np.array_equal(ci, ci4)
-        for name, arr in sched.items():
-            assert np.array_equal(arr, sched4[name]), (key, name)
+    for key, (rp, ci, eo) in res[1].items():
+        rp4, ci4, eo4 = res[4][key]
+        assert np.array_equal(rp, rp4) and np.array_equal(ci, ci4) and np.array_equal(eo, eo4)
