@@ -748,10 +748,12 @@ def main():
         extras["load_vector"] = _rec(peak, rhs_bytes(E, N, ndof), tb, E)
         extras["slot_map"] = {"upper_entries": smi.n_upper, "sources": smi.n_contrib,
                               "sources_per_upper_entry": smi.n_contrib / max(1, smi.n_upper),
-                              "index_bytes": 4 * smi.n_contrib + 12 * smi.n_upper,
+                              "padding_factor": smi.n_src / max(1, smi.n_contrib),
+                              "index_bytes": 4 * smi.n_src + 8 * smi.n_upper + 4 * smi.n_groups,
                               "element_matrix_bytes_f64": 8 * smi.nunique * smi.n_elem,
                               "note": "each element's matrix computed once (k_elem_mat), then one gather thread per "
-                                      "diagonal or upper CSR entry (k_slot_gather) writing the entry and its mirror"}
+                                      "diagonal or upper CSR entry (k_slot_gather, a warp per group of 32) writing the "
+                                      "entry and its mirror"}
         extras["setup"] = setup
         if graph is not None:
             extras["step_graph_ms"] = ms_step

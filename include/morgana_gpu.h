@@ -182,26 +182,35 @@ mg_status mg_pattern_device(const mg_plan* plan, const int32_t** d_rowptr, const
 
 /* Slot map of the GPU assembly (no reference counterpart: the reference inserts
    element blocks into Epetra one by one).  The operators are symmetric, so the
-   assembly sums each diagonal and upper CSR entry t once and writes it to the
-   entry h_uslot[t] and to its mirror h_umirror[t] (the same entry on the
-   diagonal); its sources are h_src[h_useg[t] .. h_useg[t+1]), the element-matrix
-   entries of every element holding both dofs, in ascending Morton position p of
-   the element (h_elem_order[p] = element id).  A source is p * nunique + u
-   (elem_major = 1, P1) or u * n_elem + p (P2), u the upper-triangle index of the
-   element's local pair (i <= j, row-major).  Both calls make the plan
-   device-resident (they need a device). */
+   assembly sums each diagonal and upper CSR entry once and writes it to the entry
+   and to its mirror.  These entries are laid out in groups of 32 (one per warp of
+   the gather) in the order of (row / rows_per_block, off-diagonal, CSR position):
+   per block of rows its diagonal entries, then its other upper entries; entry t
+   is written to h_uslot[t] and h_umirror[t] (the same on the diagonal).  Group g holds L = (h_goff[g+1] - h_goff[g]) / 32 rows of sources:
+   lane l's j-th source is h_src[h_goff[g] + 32 j + l], 0xffffffff past the end
+   of its list.  An entry's sources are the element-matrix entries of every
+   element holding both dofs, in ascending Morton position p of the element
+   (h_elem_order[p] = element id); a source is p * nunique + u (elem_major = 1,
+   P1) or u * n_elem + p (P2), u the upper-triangle index of the element's local
+   pair (i <= j, row-major).  Both calls make the plan device-resident (they need
+   a device). */
 typedef struct {
   int64_t n_upper;    /* diagonal and upper CSR entries */
-  int64_t n_contrib;  /* sources summed over them */
+  int64_t n_groups;   /* groups of 32 of them */
+  int64_t n_diag;     /* diagonal entries (the first groups) */
+  int64_t n_contrib;  /* sources summed, padding excluded */
+  int64_t n_src;      /* length of the source array, padding included */
   int64_t n_elem;
   int32_t nunique;    /* unique entries of an element matrix: 10 (P1), 55 (P2) */
   int32_t elem_major; /* element-matrix layout of the sources (see above) */
+  int32_t rows_per_block;
+  int32_t reserved;
 } mg_slot_map_info;
 
 mg_status mg_plan_slot_map_info(mg_plan* plan, mg_slot_map_info* info);
-/* h_elem_order: n_elem; h_useg: n_upper + 1; h_uslot, h_umirror: n_upper;
-   h_src: n_contrib (any may be NULL). */
-mg_status mg_plan_export_slot_map(mg_plan* plan, int32_t* h_elem_order, int32_t* h_useg, int32_t* h_uslot,
+/* h_elem_order: n_elem; h_goff: n_groups + 1; h_uslot, h_umirror: n_upper;
+   h_src: n_src (any may be NULL). */
+mg_status mg_plan_export_slot_map(mg_plan* plan, int32_t* h_elem_order, int32_t* h_goff, int32_t* h_uslot,
                                   int32_t* h_umirror, uint32_t* h_src);
 /* The Morton element order alone (host copy; no device needed). */
 mg_status mg_plan_export_elem_order(const mg_plan* plan, int32_t* h_elem_order);

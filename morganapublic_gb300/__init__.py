@@ -61,8 +61,10 @@ class CgInfo(ctypes.Structure):
 
 
 class SlotMapInfo(ctypes.Structure):
-    _fields_ = [("n_upper", ctypes.c_int64), ("n_contrib", ctypes.c_int64), ("n_elem", ctypes.c_int64),
-                ("nunique", ctypes.c_int32), ("elem_major", ctypes.c_int32)]
+    _fields_ = [("n_upper", ctypes.c_int64), ("n_groups", ctypes.c_int64), ("n_diag", ctypes.c_int64),
+                ("n_contrib", ctypes.c_int64), ("n_src", ctypes.c_int64), ("n_elem", ctypes.c_int64),
+                ("nunique", ctypes.c_int32), ("elem_major", ctypes.c_int32), ("rows_per_block", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
 
 
 _P = ctypes.c_void_p
@@ -311,12 +313,12 @@ class MatrixBuilder:
         """The assembly's slot map (mg_plan_export_slot_map); makes the plan device-resident."""
         info = self.slot_map_info()
         out = {"elem_order": np.empty(info.n_elem, dtype=np.int32),
-               "useg": np.empty(info.n_upper + 1, dtype=np.int32),
+               "goff": np.empty(info.n_groups + 1, dtype=np.int32),
                "uslot": np.empty(info.n_upper, dtype=np.int32),
                "umirror": np.empty(info.n_upper, dtype=np.int32),
-               "src": np.empty(info.n_contrib, dtype=np.uint32)}
+               "src": np.empty(info.n_src, dtype=np.uint32)}
         _check(lib().mg_plan_export_slot_map(self._h, *[_ptr(out[k]) for k in
-                                                        ("elem_order", "useg", "uslot", "umirror", "src")]),
+                                                        ("elem_order", "goff", "uslot", "umirror", "src")]),
                "mg_plan_export_slot_map")
         out["info"] = info
         return out

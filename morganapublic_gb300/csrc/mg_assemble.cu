@@ -737,38 +737,45 @@ __global__ void __launch_bounds__(256, ORDER == 1 ? 4 : 1) k_elem_mat(ElemArgs a
   }
 }
 
-// Sums the sources of the diagonal and upper CSR entries t, K loads in flight
-// (their indices, then their values), in the slot map's order, and writes each
-// sum to the entry and to its mirror (the operators are symmetric).
+// One warp per group of 32 diagonal or upper CSR entries (the slot map's
+// layout): lane l sums the sources src[o + 32 j + l] of its entry, j < L, K
+// loads in flight (a coalesced line of indices per j, then the element-matrix
+// values), in the slot map's order, and writes the sum to the entry and to its
+// mirror (the operators are symmetric).  Padding sources (kPadSource) read the
+// zero entry `zero` past the element matrices.
 template <int MODE, int K>
-__global__ void __launch_bounds__(256) k_slot_gather(int64_t n_upper, const int32_t* __restrict__ useg,
+__global__ void __launch_bounds__(256) k_slot_gather(int64_t n_groups, int64_t n_upper, const int32_t* __restrict__ goff,
                                                      const int32_t* __restrict__ uslot,
                                                      const int32_t* __restrict__ umirror,
                                                      const uint32_t* __restrict__ src, const void* __restrict__ em,
-                                                     typename Arith<MODE>::Out* __restrict__ values)
+                                                     uint32_t zero, typename Arith<MODE>::Out* __restrict__ values)
 {
   using A = Arith<MODE>;
   using T = typename A::T;
-  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= n_upper) return;
-  int32_t k = useg[t];
-  const int32_t k1 = useg[t + 1];
+  const int64_t g = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  if (g >= n_groups) return;
+  const int lane = threadIdx.x & 31;
+  const int32_t o = goff[g], L = (goff[g + 1] - o) >> 5;
+  const uint32_t* s = src + o + lane;
   T v = A::zero();
-  for (; k < k1; k += K) {
+  for (int32_t j = 0; j < L; j += K) {
     uint32_t idx[K];
 #pragma unroll
-    for (int j = 0; j < K; ++j) idx[j] = k + j < k1 ? __ldg(src + k + j) : 0u;
+    for (int i = 0; i < K; ++i) idx[i] = j + i < L ? min(__ldg(s + 32 * (j + i)), zero) : zero;
     T x[K];
 #pragma unroll
-    for (int j = 0; j < K; ++j) x[j] = k + j < k1 ? em_get<T>(em, idx[j]) : A::zero();
+    for (int i = 0; i < K; ++i) x[i] = j + i < L ? em_get<T>(em, idx[i]) : A::zero();
 #pragma unroll
-    for (int j = 0; j < K; ++j)
-      if (k + j < k1) A::sum_into(v, x[j]);
+    for (int i = 0; i < K; ++i)
+      if (j + i < L) A::sum_into(v, x[i]);
   }
-  const typename A::Out o = A::out(v);
-  const int32_t s = uslot[t], m = umirror[t];
-  values[s] = o;
-  if (m != s) values[m] = o;
+  const int64_t t = 32 * g + lane;
+  if (t < n_upper) {
+    const typename A::Out out = A::out(v);
+    const int32_t a = uslot[t], m = umirror[t];
+    values[a] = out;
+    if (m != a) values[m] = out;
+  }
 }
 
 // The element-matrix array of a plan (allocated by its first assembly).
@@ -776,8 +783,11 @@ static mg_status plan_gather(mg_plan* p)
 {
   std::lock_guard<std::mutex> lock(p->upload_mu);
   if (!p->d_em) {
+    // nunique x n_elem entries of up to 8 bytes, then one zero entry (8 bytes:
+    // the FP32 gather reads its first float) for the padding sources
     const int64_t n = (int64_t)nunique(p->mesh->order) * p->mesh->n_elem;
-    MG_CUDA(cudaMalloc(&p->d_em, sizeof(double) * (size_t)std::max<int64_t>(n, 1)));
+    MG_CUDA(cudaMalloc(&p->d_em, sizeof(double) * (size_t)(n + 1)));
+    MG_CUDA(cudaMemset(static_cast<double*>(p->d_em) + n, 0, sizeof(double)));
   }
   return MG_OK;
 }
@@ -789,12 +799,14 @@ static mg_status launch_gather_t(mg_plan* p, const ElemArgs& a, void* d_values, 
   if (E > 0) k_elem_mat<ORDER, MODE><<<(unsigned)((E + 255) / 256), 256, 0, st>>>(a);
   MG_CUDA(cudaGetLastError());
   using Out = typename Arith<MODE>::Out;
-  const unsigned g = (unsigned)((p->n_upper + 255) / 256);
-  Out* o = static_cast<Out*>(d_values);
+  const unsigned blocks = (unsigned)((p->n_groups + 7) / 8);  // 8 warps (groups) per CTA
+  // the zero entry: index nunique * n_elem of the 8-byte entries, 2 * that of floats
+  const uint32_t zero = (uint32_t)((MODE == kF32 ? 2 : 1) * (int64_t)nunique(ORDER) * E);
   // 8 sources in flight per thread (measured on GB300 at P1 128^3 and P2 48^3
   // against 4 and 16)
-  if (p->n_upper > 0)
-    k_slot_gather<MODE, 8><<<g, 256, 0, st>>>(p->n_upper, p->d_useg, p->d_uslot, p->d_umirror, p->d_src, p->d_em, o);
+  if (p->n_groups > 0)
+    k_slot_gather<MODE, 8><<<blocks, 256, 0, st>>>(p->n_groups, p->n_upper, p->d_goff, p->d_uslot, p->d_umirror,
+                                                   p->d_src, p->d_em, zero, static_cast<Out*>(d_values));
   MG_CUDA(cudaGetLastError());
   return MG_OK;
 }

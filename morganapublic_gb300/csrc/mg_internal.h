@@ -107,14 +107,17 @@ struct mg_plan {
   int32_t* d_elem_order = nullptr;  // elements along a Morton curve of their centroids
   int32_t* d_dofs_morton = nullptr; // their dofs (nb each) in that order
   uint32_t* d_counters = nullptr;   // [4]: assembly flags (bit 0 NaN / Inf coefficient, bit 1 double-word range)
-  // slot map of the gather assembly (built with the plan's device state; see build_slot_map):
-  // per diagonal or upper CSR entry t, its sources src[useg[t] .. useg[t+1]), the
-  // entry uslot[t] and its mirror umirror[t]
-  int32_t* d_useg = nullptr;        // n_upper + 1
+  // slot map of the gather assembly (built with the plan's device state; see
+  // build_slot_map): the diagonal and upper CSR entries in groups of 32 (one per
+  // warp; per block of kGatherRowBlock rows the diagonal entries first), entry t
+  // written to uslot[t] and umirror[t];
+  // group g's sources src[goff[g] + 32 j + lane], j < (goff[g+1] - goff[g]) / 32,
+  // padded with kPadSource
+  int32_t* d_goff = nullptr;        // n_groups + 1
   int32_t* d_uslot = nullptr;       // n_upper
   int32_t* d_umirror = nullptr;     // n_upper
-  uint32_t* d_src = nullptr;        // n_slot_contrib
-  int64_t n_upper = 0, n_slot_contrib = 0;
+  uint32_t* d_src = nullptr;        // n_src
+  int64_t n_upper = 0, n_groups = 0, n_diag = 0, n_slot_contrib = 0, n_src = 0;
   void* d_em = nullptr;             // element matrices, nunique x n_elem entries (up to 8 bytes each)
   // load vector (built on the first mg_assemble_rhs): per dof, the slots p * nb + l
   // (p = Morton position of an element touching it, l = the dof's local index)
@@ -216,6 +219,12 @@ mg_status build_schedule_device(mg_plan* p, cudaStream_t st);
 // dofs (mg_schedule.cu); once per plan
 mg_status build_slot_map(mg_plan* p, cudaStream_t st);
 bool slot_map_aos(int order);  // element-matrix layout: element-major (true) or entry-major
+// padding source of the gather layout; the kernel maps it to the zero entry past
+// the element matrices
+constexpr uint32_t kPadSource = 0xffffffffu;
+// rows per block of the gather's order: a block's diagonal entries, then its
+// other upper entries (its element matrices stay in L2 across both)
+constexpr int kGatherRowBlock = 256;
 mg_status build_edges_device(mg_mesh* m, cudaStream_t st);    // edges on the GPU (mg_pattern.cu)
 mg_status ensure_edges(mg_mesh* m);
 mg_status launch_assemble(mg_plan* p, int op, const double* d_coeff, double c, int quad, int prec,

@@ -199,7 +199,7 @@ static void free_plan(mg_plan* p)
   cudaFree(p->d_coloff);
   cudaFree(p->d_elem_order);
   cudaFree(p->d_dofs_morton);
-  cudaFree(p->d_useg);
+  cudaFree(p->d_goff);
   cudaFree(p->d_uslot);
   cudaFree(p->d_umirror);
   cudaFree(p->d_src);
@@ -392,24 +392,29 @@ mg_status mg_plan_slot_map_info(mg_plan* p, mg_slot_map_info* info)
   if (!p || !info) return set_error(MG_ERR_INVALID_ARG, "mg_plan_slot_map_info: null argument");
   MG_TRY(plan_device(p));
   info->n_upper = p->n_upper;
+  info->n_groups = p->n_groups;
+  info->n_diag = p->n_diag;
   info->n_contrib = p->n_slot_contrib;
+  info->n_src = p->n_src;
   info->n_elem = p->mesh->n_elem;
   info->nunique = nunique(p->mesh->order);
   info->elem_major = slot_map_aos(p->mesh->order) ? 1 : 0;
+  info->rows_per_block = kGatherRowBlock;
+  info->reserved = 0;
   return MG_OK;
 }
 
-mg_status mg_plan_export_slot_map(mg_plan* p, int32_t* h_elem_order, int32_t* h_useg, int32_t* h_uslot,
+mg_status mg_plan_export_slot_map(mg_plan* p, int32_t* h_elem_order, int32_t* h_goff, int32_t* h_uslot,
                                   int32_t* h_umirror, uint32_t* h_src)
 {
   if (!p) return set_error(MG_ERR_INVALID_ARG, "mg_plan_export_slot_map: null plan");
   MG_TRY(plan_device(p));
-  const int64_t E = p->mesh->n_elem, U = p->n_upper, C = p->n_slot_contrib;
+  const int64_t E = p->mesh->n_elem, U = p->n_upper, G = p->n_groups, S = p->n_src;
   if (h_elem_order && E) std::memcpy(h_elem_order, p->h_elem_order.data(), sizeof(int32_t) * E);
-  if (h_useg) MG_CUDA(cudaMemcpy(h_useg, p->d_useg, sizeof(int32_t) * (U + 1), cudaMemcpyDeviceToHost));
+  if (h_goff) MG_CUDA(cudaMemcpy(h_goff, p->d_goff, sizeof(int32_t) * (G + 1), cudaMemcpyDeviceToHost));
   if (h_uslot && U) MG_CUDA(cudaMemcpy(h_uslot, p->d_uslot, sizeof(int32_t) * U, cudaMemcpyDeviceToHost));
   if (h_umirror && U) MG_CUDA(cudaMemcpy(h_umirror, p->d_umirror, sizeof(int32_t) * U, cudaMemcpyDeviceToHost));
-  if (h_src && C) MG_CUDA(cudaMemcpy(h_src, p->d_src, sizeof(uint32_t) * C, cudaMemcpyDeviceToHost));
+  if (h_src && S) MG_CUDA(cudaMemcpy(h_src, p->d_src, sizeof(uint32_t) * S, cudaMemcpyDeviceToHost));
   return MG_OK;
 }
 

@@ -207,7 +207,8 @@ __global__ void __launch_bounds__(256) k_slot_map(int64_t nd, int nb, int64_t E,
                                                   const int32_t* __restrict__ rowptr, const int32_t* __restrict__ colind,
                                                   const int32_t* __restrict__ up_first,
                                                   const int32_t* __restrict__ src_first, int32_t* cur, int32_t* useg,
-                                                  int32_t* uslot, int32_t* umirror, uint32_t* src, int* bad)
+                                                  int32_t* uslot, int32_t* umirror, int32_t* urow, uint32_t* src,
+                                                  int* bad)
 {
   const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (r >= nd) return;
@@ -236,6 +237,7 @@ __global__ void __launch_bounds__(256) k_slot_map(int64_t nd, int nb, int64_t E,
     const int32_t t = u0 + (k - kd);
     useg[t] = pos;
     uslot[t] = r0 + k;
+    urow[t] = (int32_t)r;
     const int32_t col = cols[k];
     const int32_t m0 = rowptr[col], ml = rowptr[col + 1] - m0;
     const int km = find_col(colind + m0, ml, (int32_t)r);
@@ -261,6 +263,64 @@ __global__ void __launch_bounds__(256) k_slot_map(int64_t nd, int nb, int64_t E,
   }
 }
 
+
+// ---- the gather's layout: upper entries regrouped (diagonal entries first, each
+// class in CSR order) into groups of 32, one per warp; a group's sources stored
+// [j][lane], padded to its longest list with kPadSource
+// key of upper entry t in the gather's order: (row / kGatherRowBlock, off-diagonal)
+__global__ void k_group_keys(int64_t U, const int32_t* __restrict__ urow, const int32_t* __restrict__ uslot,
+                             const int32_t* __restrict__ umirror, uint32_t* __restrict__ key, uint32_t* __restrict__ id,
+                             int32_t* __restrict__ ndiag)
+{
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= U) return;
+  const bool dg = uslot[t] == umirror[t];
+  key[t] = ((uint32_t)(urow[t] / kGatherRowBlock) << 1) | (dg ? 0u : 1u);
+  id[t] = (uint32_t)t;
+  if (dg) atomicAdd(ndiag, 1);
+}
+
+__global__ void k_group_len(int64_t G, int64_t U, const uint32_t* __restrict__ perm, const int32_t* __restrict__ useg,
+                            int32_t* __restrict__ glen)
+{
+  const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (g > G) return;
+  int32_t L = 0;
+  if (g < G)
+    for (int64_t t = 32 * g; t < min(32 * g + 32, U); ++t) {
+      const uint32_t q = perm[t];
+      L = max(L, useg[q + 1] - useg[q]);
+    }
+  glen[g] = 32 * L;
+}
+
+__global__ void k_narrow(int64_t n, const int64_t* __restrict__ a, int32_t* __restrict__ b)
+{
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (int32_t)a[i];
+}
+
+__global__ void k_group_fill(int64_t G, int64_t U, const uint32_t* __restrict__ perm, const int32_t* __restrict__ useg,
+                             const uint32_t* __restrict__ src_in, const int32_t* __restrict__ uslot_in,
+                             const int32_t* __restrict__ umirror_in, const int32_t* __restrict__ goff,
+                             uint32_t* __restrict__ src, int32_t* __restrict__ uslot, int32_t* __restrict__ umirror)
+{
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= 32 * G) return;
+  const int64_t g = t >> 5;
+  const int lane = (int)(t & 31);
+  const int32_t o = goff[g], L = (goff[g + 1] - o) >> 5;
+  int32_t s0 = 0, len = 0;
+  if (t < U) {
+    const uint32_t q = perm[t];
+    s0 = useg[q];
+    len = useg[q + 1] - s0;
+    uslot[t] = uslot_in[q];
+    umirror[t] = umirror_in[q];
+  }
+  for (int32_t j = 0; j < L; ++j) src[o + 32 * j + lane] = j < len ? src_in[s0 + j] : kPadSource;
+}
+
 }  // namespace
 
 // --------------------------------------------------------------- slot map --
@@ -273,8 +333,8 @@ mg_status build_slot_map(mg_plan* p, cudaStream_t st)
   const int nb = m->nb;
   const int64_t E = m->n_elem, nd = p->ndof, nnz = p->nnz, n = E * nb;
   if (n * nb >= INT32_MAX) return set_error(MG_ERR_SIZE, "slot map above 2^31 contributions");
-  if ((int64_t)nunique(m->order) * E >= (int64_t)UINT32_MAX)
-    return set_error(MG_ERR_SIZE, "element matrices above 2^32 entries");
+  if ((int64_t)nunique(m->order) * E >= (int64_t)INT32_MAX)
+    return set_error(MG_ERR_SIZE, "element matrices above 2^31 entries");
   SchedBuffers B;
   int32_t *inc_ptr, *cur, *nup, *ncon, *up_first, *src_first;
   uint32_t *keys, *vin, *vout;
@@ -313,15 +373,16 @@ mg_status build_slot_map(mg_plan* p, cudaStream_t st)
   MG_CUDA(cudaMemcpyAsync(&tot[1], src_first + nd, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
   MG_CUDA(cudaStreamSynchronize(st));
   const int64_t U = tot[0], C = tot[1];
-  int32_t *useg, *uslot, *umirror;
+  int32_t *useg, *uslot, *umirror, *urow;
   uint32_t* src;
   MG_TRY(B.alloc(&useg, U + 1));
   MG_TRY(B.alloc(&uslot, U));
   MG_TRY(B.alloc(&umirror, U));
+  MG_TRY(B.alloc(&urow, U));
   MG_TRY(B.alloc(&src, C));
   k_slot_map<<<grid_of(nd), 256, 0, st>>>(nd, nb, E, slot_map_aos(m->order) ? 1 : 0, inc_ptr, vout,
                                            p->d_dofs_morton, p->d_rowptr, p->d_colind, up_first, src_first, cur, useg,
-                                           uslot, umirror, src, bad);
+                                           uslot, umirror, urow, src, bad);
   const int32_t last = (int32_t)C;
   MG_CUDA(cudaMemcpyAsync(useg + U, &last, sizeof(int32_t), cudaMemcpyHostToDevice, st));
   MG_CUDA(cudaGetLastError());
@@ -329,13 +390,58 @@ mg_status build_slot_map(mg_plan* p, cudaStream_t st)
   MG_CUDA(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
   MG_CUDA(cudaStreamSynchronize(st));
   if (hbad) return set_error(MG_ERR_INVALID_ARG, "slot map: an element coupling is missing from the plan's pattern");
-  p->d_useg = useg;
-  p->d_uslot = uslot;
-  p->d_umirror = umirror;
-  p->d_src = src;
+  // ---- regroup for the gather: entries stably sorted by (row block, off-diagonal)
+  const int64_t G = (U + 31) / 32;
+  int32_t *glen, *goff, *gslot, *gmirror, *d_ndiag;
+  uint32_t *gkey, *gkey2, *gid, *perm, *gsrc;
+  MG_TRY(B.alloc(&gkey, U));
+  MG_TRY(B.alloc(&gkey2, U));
+  MG_TRY(B.alloc(&gid, U));
+  MG_TRY(B.alloc(&perm, U));
+  MG_TRY(B.alloc(&glen, G + 1));
+  MG_TRY(B.alloc(&goff, G + 1));
+  MG_TRY(B.alloc(&gslot, U));
+  MG_TRY(B.alloc(&gmirror, U));
+  MG_TRY(B.alloc(&d_ndiag, 1));
+  MG_CUDA(cudaMemsetAsync(d_ndiag, 0, sizeof(int32_t), st));
+  int gbits = 1;
+  while ((1ll << gbits) <= 2 * (nd / kGatherRowBlock + 1)) ++gbits;
+  size_t tb3 = 0;
+  MG_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tb3, gkey, gkey2, gid, perm, (int)U, 0, gbits, st));
+  unsigned char* tmp3;
+  MG_TRY(B.alloc(&tmp3, (int64_t)std::max(tb3, (size_t)1)));
+  if (U > 0) k_group_keys<<<grid_of(U), 256, 0, st>>>(U, urow, uslot, umirror, gkey, gid, d_ndiag);
+  MG_CUDA(cub::DeviceRadixSort::SortPairs(tmp3, tb3, gkey, gkey2, gid, perm, (int)U, 0, gbits, st));
+  int32_t ndiag = 0;
+  MG_CUDA(cudaMemcpyAsync(&ndiag, d_ndiag, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  k_group_len<<<grid_of(G + 1), 256, 0, st>>>(G, U, perm, useg, glen);
+  // group offsets summed in 64 bits, checked against the 32-bit layout
+  int64_t* goff64;
+  MG_TRY(B.alloc(&goff64, G + 1));
+  size_t tb4 = 0;
+  MG_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tb4, glen, goff64, (int)(G + 1), st));
+  unsigned char* tmp4;
+  MG_TRY(B.alloc(&tmp4, (int64_t)std::max(tb4, (size_t)1)));
+  MG_CUDA(cub::DeviceScan::ExclusiveSum(tmp4, tb4, glen, goff64, (int)(G + 1), st));
+  int64_t S = 0;
+  MG_CUDA(cudaMemcpyAsync(&S, goff64 + G, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  MG_CUDA(cudaStreamSynchronize(st));
+  if (S >= INT32_MAX) return set_error(MG_ERR_SIZE, "slot map: padded sources above 2^31");
+  k_narrow<<<grid_of(G + 1), 256, 0, st>>>(G + 1, goff64, goff);
+  MG_TRY(B.alloc(&gsrc, S));
+  k_group_fill<<<grid_of(32 * G), 256, 0, st>>>(G, U, perm, useg, src, uslot, umirror, goff, gsrc, gslot, gmirror);
+  MG_CUDA(cudaGetLastError());
+  MG_CUDA(cudaStreamSynchronize(st));
+  p->d_goff = goff;
+  p->d_uslot = gslot;
+  p->d_umirror = gmirror;
+  p->d_src = gsrc;
   p->n_upper = U;
+  p->n_groups = G;
+  p->n_diag = ndiag;
   p->n_slot_contrib = C;
-  for (void* q : {(void*)useg, (void*)uslot, (void*)umirror, (void*)src}) B.keep(q);
+  p->n_src = S;
+  for (void* q : {(void*)goff, (void*)gslot, (void*)gmirror, (void*)gsrc}) B.keep(q);
   return MG_OK;
 }
 

@@ -46,11 +46,16 @@ def morton_elem_order(xyz, conn):
     return np.lexsort((np.arange(len(conn)), key)).astype(np.int32)
 
 
-def expected_slot_map(order, elem_order, dofs, rowptr, colind):
-    """The slot map of the gather assembly restated: for every diagonal or upper CSR
-    entry (r, c) in CSR order, its mirror (c, r) and the element-matrix entries of
-    every element holding both dofs, in ascending Morton position p, each
-    p * nu + u (P1, element-major) or u * E + p (P2), u = sym_index of the pair."""
+PAD_SOURCE = 0xFFFFFFFF
+
+
+def expected_slot_map(order, elem_order, dofs, rowptr, colind, rows_per_block=256):
+    """The slot map of the gather assembly restated.  For every diagonal or upper
+    CSR entry (r, c): its mirror (c, r) and the element-matrix entries of every
+    element holding both dofs, in ascending Morton position p, each p * nu + u
+    (P1, element-major) or u * E + p (P2), u = sym_index of the pair.  Entries in
+    groups of 32, ordered by (row // rows_per_block, off-diagonal, CSR position);
+    a group's sources [j][lane], padded to its longest list with PAD_SOURCE."""
     nb = 4 if order == 1 else 10
     nu = nb * (nb + 1) // 2
     E = len(elem_order)
@@ -63,19 +68,30 @@ def expected_slot_map(order, elem_order, dofs, rowptr, colind):
                 if c >= r:
                     u = sym_index(i, j, nb)
                     contrib.setdefault((r, c), []).append(p * nu + u if order == 1 else u * E + p)
-    useg, uslot, umirror, src = [0], [], [], []
+    keyed = []
     for r in range(len(rowptr) - 1):
         for k in range(rowptr[r], rowptr[r + 1]):
             c = int(colind[k])
             if c < r:
                 continue
-            uslot.append(k)
             m0 = rowptr[c]
-            umirror.append(m0 + int(np.searchsorted(colind[m0:rowptr[c + 1]], r)))
-            src.extend(contrib.get((r, c), []))
-            useg.append(len(src))
-    return {"useg": np.array(useg, dtype=np.int32), "uslot": np.array(uslot, dtype=np.int32),
-            "umirror": np.array(umirror, dtype=np.int32), "src": np.array(src, dtype=np.uint32)}
+            entry = (k, m0 + int(np.searchsorted(colind[m0:rowptr[c + 1]], r)), contrib.get((r, c), []))
+            keyed.append(((r // rows_per_block, c != r, k), entry))
+    keyed.sort(key=lambda x: x[0])
+    entries = [e for _, e in keyed]
+    n_diag = sum(1 for key, _ in keyed if not key[1])
+    goff, src = [0], []
+    for g in range(0, len(entries), 32):
+        grp = entries[g:g + 32]
+        L = max(len(e[2]) for e in grp)
+        block = np.full((L, 32), PAD_SOURCE, dtype=np.uint64)
+        for lane, e in enumerate(grp):
+            block[:len(e[2]), lane] = e[2]
+        src.extend(block.reshape(-1).tolist())
+        goff.append(len(src))
+    return {"goff": np.array(goff, dtype=np.int32), "uslot": np.array([e[0] for e in entries], dtype=np.int32),
+            "umirror": np.array([e[1] for e in entries], dtype=np.int32), "src": np.array(src, dtype=np.uint32),
+            "n_diag": n_diag}
 
 
 def emulate_slot_map(sm, order, elem_order, local_mats, nnz):
@@ -89,12 +105,18 @@ def emulate_slot_map(sm, order, elem_order, local_mats, nnz):
     for p, e in enumerate(elem_order):
         for u, (i, j) in enumerate(pairs):
             em[p, u] = local_mats[e][i, j]
-    flat = em.reshape(-1) if order == 1 else em.T.reshape(-1)
+    flat = np.append(em.reshape(-1) if order == 1 else em.T.reshape(-1), 0.0)
     out = np.full(nnz, np.nan)
-    for t in range(len(sm["uslot"])):
-        v = 0.0
-        for s in sm["src"][sm["useg"][t]:sm["useg"][t + 1]]:
-            v += flat[s]
-        out[sm["uslot"][t]] = v
-        out[sm["umirror"][t]] = v
+    U = len(sm["uslot"])
+    for g in range(len(sm["goff"]) - 1):
+        blk = sm["src"][sm["goff"][g]:sm["goff"][g + 1]].reshape(-1, 32)
+        for lane in range(32):
+            t = 32 * g + lane
+            if t >= U:
+                continue
+            v = 0.0
+            for s in blk[:, lane]:
+                v += flat[min(int(s), len(flat) - 1)]
+            out[sm["uslot"][t]] = v
+            out[sm["umirror"][t]] = v
     return out

@@ -290,7 +290,8 @@ def test_device_pattern_build_matches_host(case):
     rp_d, ci_d = dev.pattern()
     assert np.array_equal(rp_h, rp_d) and np.array_equal(ci_h, ci_d)
     sh, sd = host.export_slot_map(), dev.export_slot_map()
-    for f in ("n_upper", "n_contrib", "n_elem", "nunique", "elem_major"):
+    for f in ("n_upper", "n_groups", "n_diag", "n_contrib", "n_src", "n_elem", "nunique", "elem_major",
+              "rows_per_block"):
         assert getattr(sh["info"], f) == getattr(sd["info"], f), f
     for k in sh:
         if k != "info":
@@ -672,7 +673,7 @@ def test_strongly_jittered_mesh_p2(jitter, seed):
 
 
 @pytest.mark.parametrize("order,rule", [(1, "lex"), (2, "lex"), (2, "first")])
-@pytest.mark.parametrize("n,jitter", [(3, 0.2), (4, 0.0)])
+@pytest.mark.parametrize("n,jitter", [(3, 0.2), (4, 0.0), (7, 0.25)])
 def test_slot_map_matches_restatement_and_oracle(order, rule, n, jitter):
     """The device-built slot map equals its numpy restatement bit for bit (entries,
     mirrors, sources in ascending Morton position), and summing the oracle's element
@@ -683,10 +684,13 @@ def test_slot_map_matches_restatement_and_oracle(order, rule, n, jitter):
     b = mg.MatrixBuilder(mesh)
     sm = b.export_slot_map()
     rp, ci = b.pattern()
-    exp = expected_slot_map(order, sm["elem_order"], mesh.elem_dofs(), rp, ci)
-    for k in ("useg", "uslot", "umirror", "src"):
+    assert sm["info"].rows_per_block == 256
+    exp = expected_slot_map(order, sm["elem_order"], mesh.elem_dofs(), rp, ci, sm["info"].rows_per_block)
+    for k in ("goff", "uslot", "umirror", "src"):
         assert np.array_equal(sm[k], exp[k]), k
-    assert sm["info"].n_contrib == len(exp["src"]) and sm["info"].elem_major == (order == 1)
+    info = sm["info"]
+    assert info.n_diag == exp["n_diag"] == b.ndof and info.elem_major == (order == 1)
+    assert info.n_contrib == int(np.sum(exp["src"] != 0xFFFFFFFF)) and info.n_src == len(exp["src"])
     quad = 4 if order == 1 else 15
     dofs, rpo, cio, ref = orc.full_operator("stiff_kappa", order, quad, m.xyz, m.conn, coeff=kappa, edge_rule=rule)
     mats = [orc.local_matrix("stiff_kappa", order, quad, m.xyz, m.conn[e], kappa=kappa[e]) for e in range(len(m.conn))]
