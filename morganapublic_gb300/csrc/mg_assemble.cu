@@ -738,11 +738,12 @@ __global__ void __launch_bounds__(256, ORDER == 1 ? 4 : 1) k_elem_mat(ElemArgs a
 }
 
 // One warp per group of 32 diagonal or upper CSR entries (the slot map's
-// layout): lane l sums the sources src[o + 32 j + l] of its entry, j < L, K
-// loads in flight (a coalesced line of indices per j, then the element-matrix
-// values), in the slot map's order, and writes the sum to the entry and to its
-// mirror (the operators are symmetric).  Padding sources (kPadSource) read the
-// zero entry `zero` past the element matrices.
+// layout): lane l sums the sources src[o + 32 j + l] of its entry, j < L, in the
+// slot map's order, K at a time, and writes the sum to the entry and to its
+// mirror (the operators are symmetric).  Software-pipelined: the indices of the
+// next K sources (one coalesced line per j) and the output positions load while
+// the current element-matrix values are in flight.  Padding sources
+// (kPadSource) read the zero entry `zero` past the element matrices.
 template <int MODE, int K>
 __global__ void __launch_bounds__(256) k_slot_gather(int64_t n_groups, int64_t n_upper, const int32_t* __restrict__ goff,
                                                      const int32_t* __restrict__ uslot,
@@ -755,13 +756,21 @@ __global__ void __launch_bounds__(256) k_slot_gather(int64_t n_groups, int64_t n
   const int64_t g = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   if (g >= n_groups) return;
   const int lane = threadIdx.x & 31;
+  const int64_t t = 32 * g + lane;
+  const bool live = t < n_upper;
+  const int32_t out_a = live ? __ldg(uslot + t) : 0, out_m = live ? __ldg(umirror + t) : 0;
   const int32_t o = goff[g], L = (goff[g + 1] - o) >> 5;
   const uint32_t* s = src + o + lane;
+  uint32_t nxt[K];
+#pragma unroll
+  for (int i = 0; i < K; ++i) nxt[i] = i < L ? __ldg(s + 32 * i) : kPadSource;
   T v = A::zero();
   for (int32_t j = 0; j < L; j += K) {
     uint32_t idx[K];
 #pragma unroll
-    for (int i = 0; i < K; ++i) idx[i] = j + i < L ? min(__ldg(s + 32 * (j + i)), zero) : zero;
+    for (int i = 0; i < K; ++i) idx[i] = min(nxt[i], zero);
+#pragma unroll
+    for (int i = 0; i < K; ++i) nxt[i] = j + K + i < L ? __ldg(s + 32 * (j + K + i)) : kPadSource;
     T x[K];
 #pragma unroll
     for (int i = 0; i < K; ++i) x[i] = j + i < L ? em_get<T>(em, idx[i]) : A::zero();
@@ -769,12 +778,10 @@ __global__ void __launch_bounds__(256) k_slot_gather(int64_t n_groups, int64_t n
     for (int i = 0; i < K; ++i)
       if (j + i < L) A::sum_into(v, x[i]);
   }
-  const int64_t t = 32 * g + lane;
-  if (t < n_upper) {
-    const typename A::Out out = A::out(v);
-    const int32_t a = uslot[t], m = umirror[t];
-    values[a] = out;
-    if (m != a) values[m] = out;
+  if (live) {
+    const typename A::Out r = A::out(v);
+    values[out_a] = r;
+    if (out_m != out_a) values[out_m] = r;
   }
 }
 
