@@ -214,7 +214,7 @@ mg_status plan_rhs_map(mg_plan* p);  // the load-vector slot map (once per plan)
 mg_status build_pattern_device(mg_plan* p, cudaStream_t st, bool keep_device);
 // the plan's device state from its device pattern (mg_schedule.cu): the same
 // arrays plan_device makes for a host-built plan, slot map included (on_device)
-mg_status build_schedule_device(mg_plan* p, cudaStream_t st);
+mg_status build_plan_device(mg_plan* p, cudaStream_t st);
 // the slot map of the gather assembly from the plan's device pattern and Morton
 // dofs (mg_schedule.cu); once per plan
 mg_status build_slot_map(mg_plan* p, cudaStream_t st);

@@ -16,7 +16,7 @@
 //   2. a radix sort of the keys and removal of duplicates (CUB),
 //   3. row starts by binary search over the sorted unique keys.
 // The pattern is copied to the host (the export calls and the boundary-multiplier
-// build read it there) and, for the device schedule build, kept on the device.
+// build read it there) and, for the device plan build, kept on the device.
 #include <algorithm>
 #include <vector>
 

@@ -346,7 +346,7 @@ mg_status mg_pattern_build_device(mg_mesh* mesh, mg_plan** out, void* stream)
   mg_plan* p = new mg_plan();
   p->mesh = mesh;
   mg_status s = build_pattern_device(p, (cudaStream_t)stream, true);
-  if (s == MG_OK) s = build_schedule_device(p, (cudaStream_t)stream);
+  if (s == MG_OK) s = build_plan_device(p, (cudaStream_t)stream);
   if (s != MG_OK) {
     free_plan(p);
     return s;

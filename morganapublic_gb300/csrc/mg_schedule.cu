@@ -96,7 +96,7 @@ __global__ void k_diag_coloff(int64_t nd, const int32_t* __restrict__ rowptr, co
   }
 }
 
-// Device buffers of one schedule build, freed on every exit path unless handed
+// Device buffers of one plan build, freed on every exit path unless handed
 // to the plan.
 struct SchedBuffers {
   std::vector<void*> ptrs;
@@ -105,7 +105,7 @@ struct SchedBuffers {
   {
     void* q = nullptr;
     const cudaError_t e = cudaMalloc(&q, sizeof(T) * (size_t)std::max<int64_t>(n, 1));
-    if (e != cudaSuccess) return cuda_error(e, "device schedule buffer");
+    if (e != cudaSuccess) return cuda_error(e, "device plan buffer");
     ptrs.push_back(q);
     *p = static_cast<T*>(q);
     return MG_OK;
@@ -450,7 +450,7 @@ mg_status build_slot_map(mg_plan* p, cudaStream_t st)
 // the dofs in that order, the diagonal entries and 16-bit column offsets, the
 // status counters and the slot map -- the arrays plan_device makes for a
 // host-built plan, from the same rules.
-mg_status build_schedule_device(mg_plan* p, cudaStream_t st)
+mg_status build_plan_device(mg_plan* p, cudaStream_t st)
 {
   mg_mesh* m = p->mesh;
   const int nb = m->nb;
