@@ -637,7 +637,7 @@ def main():
     b = mg.MatrixBuilder(mesh)
     setup["plan_host_s"] = time.perf_counter() - t0
     nnz, ndof = b.nnz, b.ndof
-    smi = b.slot_map_info()
+    bmi = b.block_map_info()
     kappa = torch.from_numpy(kappa_h).cuda()
     x = torch.from_numpy(np.random.default_rng(a.seed).uniform(-1, 1, ndof)).cuda()
     x32 = x.float()
@@ -746,14 +746,18 @@ def main():
         extras["spmv_f32"] = {**_rec(peak, S32, ts32), "note": "one launch, L2 flushed before it"}
         extras["adjoint_grad"] = _rec(peak, adj_bytes(E, N, ndof), tg, E)
         extras["load_vector"] = _rec(peak, rhs_bytes(E, N, ndof), tb, E)
-        extras["slot_map"] = {"upper_entries": smi.n_upper, "sources": smi.n_contrib,
-                              "sources_per_upper_entry": smi.n_contrib / max(1, smi.n_upper),
-                              "padding_factor": smi.n_src / max(1, smi.n_contrib),
-                              "index_bytes": 4 * smi.n_src + 8 * smi.n_upper + 4 * smi.n_groups,
-                              "element_matrix_bytes_f64": 8 * smi.nunique * smi.n_elem,
-                              "note": "each element's matrix computed once (k_elem_mat), then one gather thread per "
-                                      "diagonal or upper CSR entry (k_slot_gather, a warp per group of 32) writing the "
-                                      "entry and its mirror"}
+        extras["block_map"] = {"upper_entries": bmi.n_upper, "sources": bmi.n_contrib, "blocks": bmi.n_blocks,
+                               "elems_per_block": bmi.elems_per_block, "runs": bmi.n_runs,
+                               "shared_entries": bmi.n_shared,
+                               "shared_fraction": bmi.n_shared / max(1, bmi.n_upper),
+                               "partial_slots": bmi.n_partial,
+                               "padding_factor": bmi.n_src / max(1, bmi.n_contrib),
+                               "map_bytes": 2 * bmi.n_src + 8 * 32 * bmi.n_groups + 4 * (bmi.n_groups + bmi.n_blocks)
+                               + 8 * 32 * bmi.n_shared_groups + 4 * bmi.n_shared_groups,
+                               "note": "one CTA per block of Morton-consecutive elements: element matrices in shared "
+                                       "memory, each diagonal / upper CSR entry summed there and written with its "
+                                       "mirror (k_block_asm); entries spanning blocks through per-block partial sums "
+                                       "added in block order (k_shared_sum)"}
         extras["setup"] = setup
         if graph is not None:
             extras["step_graph_ms"] = ms_step
@@ -828,12 +832,12 @@ def main():
                        "upload overlaps the assembly and the values download overlaps the SpMVs (second stream)"}
 
         # cold e2e: the work the reference arm's step does, from host arrays -- mesh
-        # tables, CSR pattern, element order and slot map (on the GPU), first assembly and
+        # tables, CSR pattern, element order and block map (on the GPU), first assembly and
         # 100 SpMVs, values and y back in host memory; wall clock
         e2e_cold = None
         if not a.no_cold:
             ts, stages = [], []
-            for _ in range(2):
+            for _ in range(3):
                 torch.cuda.synchronize()
                 t0 = time.perf_counter()
                 mc = mg.Mesh(m.xyz, m.conn, order=1)
@@ -855,23 +859,23 @@ def main():
                 del vc, xc, yc, vh, yh
                 bc.close()
                 mc.close()
-            tc = statistics.mean(ts)
+            tc = statistics.median(ts)
             e2e_cold = {"value": world * E / tc, "unit": "tets/s", "ms_per_step": tc * 1e3,
                         "runs_s": ts,
-                        "stages_s": {k: statistics.mean(s[i] for s in stages) for i, k in enumerate(
+                        "stages_s": {k: statistics.median(s[i] for s in stages) for i, k in enumerate(
                             ("mesh_create", "plan_build_device", "first_assembly_with_coefficient_upload",
                              "spmvs_and_copies"))}, "h2d_bytes_per_step": 24 * N + 16 * E + 8 * E + 8 * ndof,
                         "d2h_bytes_per_step": d2h,
                         "note": "from host arrays: mg_mesh_create + mg_pattern_build_device (CSR pattern, element "
-                                "order and slot map built on the GPU) + first mg_assemble + "
-                                f"{N_SPMV} SpMV, values and y copied back; wall clock, mean of 2 -- the work one "
+                                "order and block map built on the GPU) + first mg_assemble + "
+                                f"{N_SPMV} SpMV, values and y copied back; wall clock, median of 3 -- the work one "
                                 "step of the reference arm does"}
 
         if not a.no_p2:
             extras["config3_p2_48"] = p2_record()
 
         rl = extras["spmv_f64_in_step"] if N_SPMV * ts64 >= ta64 else extras["assembly_f64"]
-        kname = "k_spmv<double,1>" if rl is extras["spmv_f64_in_step"] else "k_elem_mat<1,kDW> + k_slot_gather<kDW>"
+        kname = "k_spmv<double,1>" if rl is extras["spmv_f64_in_step"] else "k_block_asm<kDW> + k_shared_sum<kDW>"
         traffic, tnote = profiled_traffic(kname, a.n)
         roofline = {"bound": "hbm", "kernel": kname,
                     "achieved": rl["gbs"], "peak": peak, "unit": "GB/s", "frac": rl["gbs"] / peak,

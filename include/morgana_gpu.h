@@ -180,8 +180,10 @@ mg_status mg_pattern_export(const mg_plan* plan, int32_t* h_rowptr, int32_t* h_c
 /* Device copies owned by the plan (valid until mg_plan_destroy). */
 mg_status mg_pattern_device(const mg_plan* plan, const int32_t** d_rowptr, const int32_t** d_colind);
 
-/* Slot map of the GPU assembly (no reference counterpart: the reference inserts
-   element blocks into Epetra one by one).  The operators are symmetric, so the
+/* Slot map of the two-pass GPU assembly of P2 plans (no reference counterpart:
+   the reference inserts element blocks into Epetra one by one; P1 plans use the
+   block map below, and these calls return MG_ERR_UNSUPPORTED for them).  The
+   operators are symmetric, so the
    assembly sums each diagonal and upper CSR entry once and writes it to the entry
    and to its mirror.  These entries are laid out in groups of 32 (one per warp of
    the gather) in the order of (row / rows_per_block, off-diagonal, CSR position):
@@ -212,6 +214,51 @@ mg_status mg_plan_slot_map_info(mg_plan* plan, mg_slot_map_info* info);
    h_src: n_src (any may be NULL). */
 mg_status mg_plan_export_slot_map(mg_plan* plan, int32_t* h_elem_order, int32_t* h_goff, int32_t* h_uslot,
                                   int32_t* h_umirror, uint32_t* h_src);
+/* Block map of the one-pass GPU assembly of P1 plans (no reference counterpart;
+   P2 plans use the slot map above, and these calls return MG_ERR_UNSUPPORTED for
+   them).  The elements, in Morton order p, form blocks of elems_per_block
+   consecutive positions, one CTA each: the CTA computes its elements' matrices
+   into shared memory, then sums its block's part of every diagonal and upper CSR
+   entry.  An upper entry's sources are the element-matrix entries (p, u) of every
+   element holding both of its dofs, ascending p; a run is a maximal stretch of
+   them in one block.  An entry with one run is complete and written by its
+   block; the others are shared, their runs j = 0, 1, .. in ascending block each
+   written to a partial-sum slot, and summed in that order by a second kernel.
+   Block b's runs form the groups h_bgrp[b] .. h_bgrp[b+1] of 32 lanes, the
+   longest runs first (lengths of 63 and more tied; equal lengths in CSR order).
+   Group g
+   holds L = (h_goff[g+1] - h_goff[g]) / 32 rows of local sources: lane l's j-th
+   source is h_src[h_goff[g] + 32 j + l] = (p - b elems_per_block) nunique + u,
+   elems_per_block nunique past the end of its run.  Its output (two int32 per
+   lane, h_out[2 (32 g + l)] and [+1]) is (CSR entry, mirror entry) for a complete
+   entry, (-1 - q, 0) for partial-sum slot q, (INT32_MIN, 0) for an empty lane.
+   The shared entries, sorted by their number of runs (most first; 63 and more
+   tied; then CSR order), form groups of 32: group g's slots are
+   h_sgoff[g] + 32 j + l, j < (h_sgoff[g+1] - h_sgoff[g]) / 32 (run j of lane l's
+   entry; slots past its last run stay zero), and lane l writes its sum to
+   h_sout[2 (32 g + l)] and [+1] (INT32_MIN for an empty lane).  Both calls make
+   the plan device-resident (they need a device). */
+typedef struct {
+  int64_t n_upper;          /* diagonal and upper CSR entries */
+  int64_t n_contrib;        /* sources summed */
+  int64_t n_blocks;         /* element blocks (CTAs) */
+  int64_t n_groups;         /* groups of 32 runs */
+  int64_t n_src;            /* length of the local-source array, padding included */
+  int64_t n_runs;
+  int64_t n_shared;         /* entries with sources in more than one block */
+  int64_t n_shared_groups;  /* groups of 32 of them */
+  int64_t n_partial;        /* partial-sum slots, padding included */
+  int64_t n_elem;
+  int32_t nunique;          /* unique entries of an element matrix: 10 */
+  int32_t elems_per_block;
+} mg_block_map_info;
+
+mg_status mg_plan_block_map_info(mg_plan* plan, mg_block_map_info* info);
+/* h_elem_order: n_elem; h_bgrp: n_blocks + 1; h_goff: n_groups + 1; h_src: n_src;
+   h_out: 64 n_groups; h_sgoff: n_shared_groups + 1; h_sout: 64 n_shared_groups
+   (any may be NULL). */
+mg_status mg_plan_export_block_map(mg_plan* plan, int32_t* h_elem_order, int32_t* h_bgrp, int32_t* h_goff,
+                                   uint16_t* h_src, int32_t* h_out, int32_t* h_sgoff, int32_t* h_sout);
 /* The Morton element order alone (host copy; no device needed). */
 mg_status mg_plan_export_elem_order(const mg_plan* plan, int32_t* h_elem_order);
 
@@ -222,9 +269,10 @@ mg_status mg_plan_export_elem_order(const mg_plan* plan, int32_t* h_elem_order);
    n_elements doubles) for MG_OP_STIFF_KAPPA / MG_OP_MASS_COEFF, else ignored;
    c: the constant of MG_OP_STIFF_CONST.  Deterministic: the same inputs give
    the same bits on every call.  Two assemblies on one plan must not overlap on
-   the GPU (other streams): they share the plan's element-matrix array
-   (nunique x n_elem entries of 8 bytes, allocated by the first assembly -- make
-   that call before any stream capture).
+   the GPU (other streams): they share the plan's work arrays -- P1: the partial
+   sums of the block map (8 bytes per slot, allocated with the plan's device
+   state); P2: the element-matrix array (55 x n_elem entries of 8 bytes,
+   allocated by the first assembly -- make that call before any stream capture).
    Replaces: the value half of matrixBuilder<localMatrixEL3d<...>>::buildEpetraCrs
    (traitsMatrixBuilder.hpp:363-441) with integratorOEL3d_STD::integration
    (src/morganaIntegrator/integratorOEL3d_STD.hpp:106-137). */

@@ -67,6 +67,13 @@ class SlotMapInfo(ctypes.Structure):
                 ("reserved", ctypes.c_int32)]
 
 
+class BlockMapInfo(ctypes.Structure):
+    _fields_ = [("n_upper", ctypes.c_int64), ("n_contrib", ctypes.c_int64), ("n_blocks", ctypes.c_int64),
+                ("n_groups", ctypes.c_int64), ("n_src", ctypes.c_int64), ("n_runs", ctypes.c_int64),
+                ("n_shared", ctypes.c_int64), ("n_shared_groups", ctypes.c_int64), ("n_partial", ctypes.c_int64),
+                ("n_elem", ctypes.c_int64), ("nunique", ctypes.c_int32), ("elems_per_block", ctypes.c_int32)]
+
+
 _P = ctypes.c_void_p
 _I32, _I64, _D = ctypes.c_int32, ctypes.c_int64, ctypes.c_double
 # name -> argtypes; every function returns mg_status (int) unless listed in _RESTYPES
@@ -99,6 +106,8 @@ SIGNATURES = {
     "mg_pattern_device": [_P, ctypes.POINTER(_P), ctypes.POINTER(_P)],
     "mg_plan_slot_map_info": [_P, ctypes.POINTER(SlotMapInfo)],
     "mg_plan_export_slot_map": [_P, _P, _P, _P, _P, _P],
+    "mg_plan_block_map_info": [_P, ctypes.POINTER(BlockMapInfo)],
+    "mg_plan_export_block_map": [_P, _P, _P, _P, _P, _P, _P, _P],
     "mg_plan_export_elem_order": [_P, _P],
     "mg_assemble": [_P, _I32, _P, _D, _I32, _I32, _P, _P],
     "mg_assemble_host": [_P, _I32, _P, _D, _I32, _I32, _P, _P],
@@ -302,6 +311,29 @@ class MatrixBuilder:
         """The assembly's element order (a Morton curve of the centroids): element ids."""
         out = np.empty(self.mesh.n_elements, dtype=np.int32)
         _check(lib().mg_plan_export_elem_order(self._h, _ptr(out)), "mg_plan_export_elem_order")
+        return out
+
+    def block_map_info(self) -> BlockMapInfo:
+        """Sizes of the one-pass P1 assembly's block map (mg_plan_block_map_info)."""
+        info = BlockMapInfo()
+        _check(lib().mg_plan_block_map_info(self._h, ctypes.byref(info)), "mg_plan_block_map_info")
+        return info
+
+    def export_block_map(self) -> dict:
+        """The P1 assembly's block map (mg_plan_export_block_map); makes the plan device-resident."""
+        info = self.block_map_info()
+        out = {"elem_order": np.empty(info.n_elem, dtype=np.int32),
+               "bgrp": np.empty(info.n_blocks + 1, dtype=np.int32),
+               "goff": np.empty(info.n_groups + 1, dtype=np.int32),
+               "src": np.empty(info.n_src, dtype=np.uint16),
+               "out": np.empty((32 * info.n_groups, 2), dtype=np.int32),
+               "sgoff": np.empty(info.n_shared_groups + 1, dtype=np.int32),
+               "sout": np.empty((32 * info.n_shared_groups, 2), dtype=np.int32)}
+        _check(lib().mg_plan_export_block_map(self._h, *[_ptr(out[k]) for k in
+                                                         ("elem_order", "bgrp", "goff", "src", "out", "sgoff",
+                                                          "sout")]),
+               "mg_plan_export_block_map")
+        out["info"] = info
         return out
 
     def slot_map_info(self) -> SlotMapInfo:

@@ -2,14 +2,16 @@
 // reduced into CSR values, plus the Dirichlet elimination, the adjoint-gradient
 // kernel and the load vector.
 //
-// The assembly takes two passes, each element computed once:
-//   k_elem_mat     one thread per element along the plan's Morton element order:
-//                  the unique entries of its (symmetric) element matrix into the
-//                  plan's element-matrix array;
-//   k_slot_gather  one thread per diagonal or upper CSR entry: the sum of the
-//                  element-matrix entries of every element holding both of its
-//                  dofs, in ascending Morton position (the plan's slot map),
-//                  written to the entry and to its mirror.
+// Every element matrix is computed once, along the plan's Morton element order:
+//   P1 (one pass)  k_block_asm: one CTA per block of consecutive elements, their
+//                  matrices in shared memory, every diagonal or upper CSR entry
+//                  summed there (the plan's block map) and written to the entry
+//                  and its mirror; entries whose elements span blocks get a
+//                  partial sum per block, added in block order by k_shared_sum;
+//   P2 (two passes) k_elem_mat: one thread per element, its 55 unique entries to
+//                  the plan's element-matrix array; k_slot_gather: one thread
+//                  per diagonal or upper CSR entry, the sum of its entries in
+//                  ascending Morton position (the plan's slot map).
 // No atomics touch values; the per-entry summation order is fixed by the plan,
 // so the results are bitwise reproducible.
 //
@@ -466,8 +468,9 @@ __device__ __forceinline__ ff metric_dot<ff>(const ff g[6], const ff* tab, int N
   return two_sum(hi, lo);
 }
 
-// ------------------------------------------------------- gather assembly --
-// Two passes, each element computed once:
+// ------------------------------------------------------------ assembly --
+// P1: the one-pass block assembly (k_block_asm, k_shared_sum, below).
+// P2, two passes, each element computed once:
 //   k_elem_mat     one thread per element, along the plan's Morton order p: the
 //                  unique entries u of its (symmetric) element matrix into the
 //                  plan's element-matrix array em;
@@ -627,16 +630,25 @@ struct ElemArgs {
   uint32_t* flags;            // bit 0: NaN / Inf coefficient; bit 1: outside the double-word range
 };
 
-// The P1 element matrix (10 unique entries) of Morton element p.
+// The coefficient and the vertex dofs of Morton element p.
+__device__ __forceinline__ double elem_coef(const ElemArgs& a, int64_t p)
+{
+  return a.coeff ? __ldg(a.coeff + a.elem_order[p]) : a.cconst;
+}
+__device__ __forceinline__ int4 elem_nodes(const ElemArgs& a, int64_t p)
+{
+  return __ldg(reinterpret_cast<const int4*>(a.dofs_m) + p);
+}
+
+// The P1 element matrix from the element's vertex dofs n and coefficient coef_d
+// (loaded by the caller, elem_nodes / elem_coef).
 template <int MODE>
-__device__ __forceinline__ void p1_element(const ElemArgs& a, const typename Arith<MODE>::T* tab, int64_t p,
-                                           typename Arith<MODE>::T K[10])
+__device__ __forceinline__ void p1_element(const ElemArgs& a, const typename Arith<MODE>::T* tab, int4 n,
+                                           double coef_d, typename Arith<MODE>::T K[10])
 {
   using A = Arith<MODE>;
   using T = typename A::T;
   constexpr int NU = 10;
-  const double coef_d = a.coeff ? __ldg(a.coeff + a.elem_order[p]) : a.cconst;
-  const int4 n = reinterpret_cast<const int4*>(a.dofs_m)[p];
   Cof<T> f;
   float c0[3];
   const bool degenerate = geometry_abs_lazy<MODE>(a.geo, n, f, MODE == kF32 && a.stiff ? c0 : nullptr);
@@ -679,33 +691,22 @@ __device__ __forceinline__ void p1_element(const ElemArgs& a, const typename Ari
   }
 }
 
-// One thread per element along the plan's Morton order p.  P1: the 10 entries of
-// each element staged in shared memory, then the CTA's contiguous range
-// em[p0 * 10 ..] written with coalesced stores (element-major).  P2: the 55
-// entries to em[u * E + p] (entry-major: the stores of one u coalesce across the
-// warp), the metric contraction reading the tables from shared memory.
-template <int ORDER, int MODE>
-__global__ void __launch_bounds__(256, ORDER == 1 ? 4 : 1) k_elem_mat(ElemArgs a)
+// The element pass of the two-pass P2 assembly: one thread per element along
+// the plan's Morton order p, its 55 entries to em[u * E + p] (entry-major: the
+// stores of one u coalesce across the warp), the metric contraction reading the
+// tables from shared memory.
+template <int MODE>
+__global__ void __launch_bounds__(256, 1) k_elem_mat(ElemArgs a)
 {
   using A = Arith<MODE>;
   using T = typename A::T;
-  constexpr int NU = ORDER == 1 ? 10 : 55;
+  constexpr int NU = 55;
   __shared__ T tab[7 * NU];
   for (int i = threadIdx.x; i < 7 * NU; i += blockDim.x) tab[i] = A::from(a.tables[i]);
   __syncthreads();
   const int64_t E = a.n_elem;
   const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if constexpr (ORDER == 1) {
-    __shared__ T stage[256 * 10];
-    T K[10];
-    if (p < E) p1_element<MODE>(a, tab, p, K);
-#pragma unroll
-    for (int u = 0; u < 10; ++u) stage[threadIdx.x * 10 + u] = K[u];
-    __syncthreads();
-    const int64_t p0 = (int64_t)blockIdx.x * blockDim.x;
-    const int nvals = (int)min((int64_t)blockDim.x, E - p0) * 10;
-    for (int i = threadIdx.x; i < nvals; i += blockDim.x) em_put(a.em, p0 * 10 + i, stage[i]);
-  } else {
+  {
     if (p >= E) return;
     const double coef_d = a.coeff ? __ldg(a.coeff + a.elem_order[p]) : a.cconst;
     const int32_t* dp = a.dofs_m + p * 10;
@@ -785,6 +786,209 @@ __global__ void __launch_bounds__(256) k_slot_gather(int64_t n_groups, int64_t n
   }
 }
 
+// ---------------------------------------------------- one-pass assembly (P1) --
+// k_block_asm: one CTA per block of kElemBlock consecutive Morton positions.
+//   1. each thread computes the element matrices of one or two elements into
+//      shared memory (10 unique entries each);
+//   2. each warp takes groups of 32 of the block's local entries (the block map):
+//      lane l sums its entry's local sources in ascending p, and writes the sum
+//      to the CSR entry and its mirror when every source of the entry lies in
+//      this block, else to the entry's partial-sum slot.
+// k_shared_sum: one warp per group of 32 shared entries: the partial sums in
+//   ascending block (coalesced [j][lane]), written to the entry and its mirror.
+// Each entry's summation order is fixed by the plan, so the values are bitwise
+// reproducible; no atomics, no element matrix leaves the SM.
+struct BlockArgs {
+  const int32_t* bgrp;
+  const int32_t* bsrc0;
+  const int32_t* bgoff;
+  const uint16_t* bsrc;
+  const int2* bout;
+  void* partial;  // 8-byte slots: float2 (double-word), double, or a float in the low half
+};
+
+__device__ __forceinline__ void partial_put(void* pp, int32_t q, float v) { static_cast<float2*>(pp)[q].x = v; }
+__device__ __forceinline__ void partial_put(void* pp, int32_t q, ff v)
+{
+  static_cast<float2*>(pp)[q] = make_float2(v.hi, v.lo);
+}
+__device__ __forceinline__ void partial_put(void* pp, int32_t q, double v) { static_cast<double*>(pp)[q] = v; }
+template <typename T> __device__ __forceinline__ T partial_get(const void* pp, int32_t q);
+template <> __device__ __forceinline__ float partial_get<float>(const void* pp, int32_t q)
+{
+  return __ldg(static_cast<const float2*>(pp) + q).x;
+}
+template <> __device__ __forceinline__ ff partial_get<ff>(const void* pp, int32_t q)
+{
+  const float2 v = __ldg(static_cast<const float2*>(pp) + q);
+  return ff{v.x, v.y};
+}
+template <> __device__ __forceinline__ double partial_get<double>(const void* pp, int32_t q)
+{
+  return __ldg(static_cast<const double*>(pp) + q);
+}
+
+// Block-map staging in shared memory: the block's local sources (up to
+// kStageSrc, the first groups' rows) and group offsets (up to kStageGroups + 1),
+// copied with cp.async while the element matrices are computed.
+constexpr int kStageSrc = 6144;
+constexpr int kStageGroups = 96;
+template <typename T>
+constexpr size_t block_smem_bytes()
+{
+  return ((sizeof(T) * (kElemBlock * 10 + 1) + 15) / 16) * 16 + 2 * kStageSrc + 4 * (kStageGroups + 1);
+}
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem)
+{
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
+               "l"(gmem));
+}
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem)
+{
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
+               "l"(gmem));
+}
+
+// THREADS per CTA: 512 (one element each, two CTAs per SM) for the double-word
+// and FP64 arithmetic, 256 (two elements each, four CTAs per SM) for FP32 --
+// measured on GB300 at P1 128^3 (the double-word loop over two elements spills).
+template <int MODE, int THREADS>
+__global__ void __launch_bounds__(THREADS, 2048 / THREADS / 2) k_block_asm(ElemArgs a, BlockArgs bm,
+                                                                         typename Arith<MODE>::Out* __restrict__ values)
+{
+  using A = Arith<MODE>;
+  using T = typename A::T;
+  constexpr int NU = 10;
+  extern __shared__ __align__(16) unsigned char smem[];
+  T* em = reinterpret_cast<T*>(smem);  // the block's element matrices, then a zero (padding source)
+  uint16_t* s_src = reinterpret_cast<uint16_t*>(smem + ((sizeof(T) * (kElemBlock * NU + 1) + 15) / 16) * 16);
+  int32_t* s_goff = reinterpret_cast<int32_t*>(s_src + kStageSrc);
+  __shared__ T tab[7 * NU];
+  const int32_t g0 = bm.bgrp[blockIdx.x], g1 = bm.bgrp[blockIdx.x + 1];
+  const int32_t src0 = bm.bsrc0[blockIdx.x], src1 = bm.bsrc0[blockIdx.x + 1];
+  // the staged part: whole 16-byte chunks (group offsets are multiples of 32
+  // sources, so the range is 64-byte aligned)
+  const int32_t n_src = min(src1 - src0, kStageSrc), n_goff = min(g1 - g0, kStageGroups) + 1;
+  for (int i = threadIdx.x; i < n_src / 8; i += THREADS) cp_async16(s_src + 8 * i, bm.bsrc + src0 + 8 * i);
+  for (int i = threadIdx.x; i < n_goff; i += THREADS) cp_async4(s_goff + i, bm.bgoff + g0 + i);
+  asm volatile("cp.async.commit_group;\n" ::);
+  const int64_t p0 = (int64_t)blockIdx.x * kElemBlock;
+  const int64_t E = a.n_elem;
+  for (int i = threadIdx.x; i < 7 * NU; i += THREADS) tab[i] = A::from(a.tables[i]);
+  if (threadIdx.x == 0) em[kElemBlock * NU] = A::zero();
+  __syncthreads();
+#pragma unroll 1
+  for (int i = 0; i < kElemBlock / THREADS; ++i) {
+    const int lp = i * THREADS + threadIdx.x;
+    if (p0 + lp < E) {
+      T K[NU];
+      p1_element<MODE>(a, tab, elem_nodes(a, p0 + lp), elem_coef(a, p0 + lp), K);
+#pragma unroll
+      for (int u = 0; u < NU; ++u) em[lp * NU + u] = K[u];
+    }
+  }
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  for (int32_t g = g0 + (threadIdx.x >> 5); g < g1; g += THREADS / 32) {
+    const int2 out = bm.bout[32 * g + lane];  // used after the sum: its latency overlaps it
+    const int32_t gi = g - g0;
+    const int32_t o = gi < kStageGroups ? s_goff[gi] : bm.bgoff[g];
+    const int32_t o1 = gi + 1 <= kStageGroups ? s_goff[gi + 1] : bm.bgoff[g + 1];
+    const int32_t L = (o1 - o) >> 5;
+    T v = A::zero();
+    if (o1 - src0 <= kStageSrc) {
+      const uint16_t* s = s_src + (o - src0) + lane;
+      int32_t j = 0;
+      for (; j + 4 <= L; j += 4) {
+        const uint32_t i0 = s[32 * j], i1 = s[32 * j + 32], i2 = s[32 * j + 64], i3 = s[32 * j + 96];
+        const T x0 = em[i0], x1 = em[i1], x2 = em[i2], x3 = em[i3];
+        A::sum_into(v, x0);
+        A::sum_into(v, x1);
+        A::sum_into(v, x2);
+        A::sum_into(v, x3);
+      }
+      for (; j < L; ++j) A::sum_into(v, em[s[32 * j]]);
+    } else {
+      // past the stage (rare): the rows from global memory, 4 in flight
+      const uint16_t* s = bm.bsrc + o + lane;
+      int32_t j = 0;
+      for (; j + 4 <= L; j += 4) {
+        const uint32_t i0 = __ldg(s + 32 * j), i1 = __ldg(s + 32 * j + 32), i2 = __ldg(s + 32 * j + 64),
+                       i3 = __ldg(s + 32 * j + 96);
+        A::sum_into(v, em[i0]);
+        A::sum_into(v, em[i1]);
+        A::sum_into(v, em[i2]);
+        A::sum_into(v, em[i3]);
+      }
+      for (; j < L; ++j) A::sum_into(v, em[__ldg(s + 32 * j)]);
+    }
+    if (out.x >= 0) {
+      const typename A::Out r = A::out(v);
+      values[out.x] = r;
+      if (out.y != out.x) values[out.y] = r;
+    } else if (out.x != kNoOutput) {
+      partial_put(bm.partial, -1 - out.x, v);
+    }
+  }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(256) k_shared_sum(int64_t n_groups, const int32_t* __restrict__ sgoff,
+                                                    const int2* __restrict__ sout, const void* __restrict__ partial,
+                                                    typename Arith<MODE>::Out* __restrict__ values)
+{
+  using A = Arith<MODE>;
+  using T = typename A::T;
+  const int64_t g = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  if (g >= n_groups) return;
+  const int lane = threadIdx.x & 31;
+  const int2 out = sout[32 * g + lane];
+  const int32_t o = sgoff[g], L = (sgoff[g + 1] - o) >> 5;
+  T v = A::zero();
+  // 8 partials in flight, summed in ascending j
+  for (int32_t j = 0; j < L; j += 8) {
+    T x[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) x[i] = j + i < L ? partial_get<T>(partial, o + 32 * (j + i) + lane) : A::zero();
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+      if (j + i < L) A::sum_into(v, x[i]);
+  }
+  if (out.x >= 0) {
+    const typename A::Out r = A::out(v);
+    values[out.x] = r;
+    if (out.y != out.x) values[out.y] = r;
+  }
+}
+
+template <int MODE>
+static mg_status launch_block_t(mg_plan* p, const ElemArgs& a, void* d_values, cudaStream_t st)
+{
+  using Out = typename Arith<MODE>::Out;
+  const BlockArgs bm{p->d_bgrp, p->d_bsrc0, p->d_bgoff, p->d_bsrc, p->d_bout, p->d_partial};
+  constexpr size_t smem = block_smem_bytes<typename Arith<MODE>::T>();
+  constexpr int threads = MODE == kF32 ? 256 : 512;
+  static std::once_flag attr_once[64];
+  int dev = 0;
+  MG_CUDA(cudaGetDevice(&dev));
+  cudaError_t attr_err = cudaSuccess;
+  std::call_once(attr_once[dev & 63], [&] {
+    attr_err =
+        cudaFuncSetAttribute(k_block_asm<MODE, threads>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  });
+  MG_CUDA(attr_err);
+  if (a.n_elem > 0)
+    k_block_asm<MODE, threads><<<(unsigned)p->n_blocks, threads, smem, st>>>(a, bm, static_cast<Out*>(d_values));
+  MG_CUDA(cudaGetLastError());
+  if (p->n_sgroups > 0)
+    k_shared_sum<MODE><<<(unsigned)((p->n_sgroups + 7) / 8), 256, 0, st>>>(p->n_sgroups, p->d_sgoff, p->d_sout,
+                                                                         p->d_partial, static_cast<Out*>(d_values));
+  MG_CUDA(cudaGetLastError());
+  return MG_OK;
+}
+
 // The element-matrix array of a plan (allocated by its first assembly).
 static mg_status plan_gather(mg_plan* p)
 {
@@ -799,11 +1003,12 @@ static mg_status plan_gather(mg_plan* p)
   return MG_OK;
 }
 
-template <int ORDER, int MODE>
+template <int MODE>
 static mg_status launch_gather_t(mg_plan* p, const ElemArgs& a, void* d_values, cudaStream_t st)
 {
+  constexpr int ORDER = 2;
   const int64_t E = a.n_elem;
-  if (E > 0) k_elem_mat<ORDER, MODE><<<(unsigned)((E + 255) / 256), 256, 0, st>>>(a);
+  if (E > 0) k_elem_mat<MODE><<<(unsigned)((E + 255) / 256), 256, 0, st>>>(a);
   MG_CUDA(cudaGetLastError());
   using Out = typename Arith<MODE>::Out;
   const unsigned blocks = (unsigned)((p->n_groups + 7) / 8);  // 8 warps (groups) per CTA
@@ -821,8 +1026,8 @@ static mg_status launch_gather_t(mg_plan* p, const ElemArgs& a, void* d_values, 
 static mg_status launch_assemble_gather(mg_plan* p, int op, const double* d_coeff, double c, const RefTables* t,
                                         const double* d_tab, int prec, void* d_values, cudaStream_t st)
 {
-  MG_TRY(plan_gather(p));
   mg_mesh* m = p->mesh;
+  if (!uses_block_map(m->order)) MG_TRY(plan_gather(p));
   const bool needs_coeff = (op == MG_OP_STIFF_KAPPA || op == MG_OP_MASS_COEFF);
   ElemArgs a;
   a.n_elem = m->n_elem;
@@ -837,13 +1042,11 @@ static mg_status launch_assemble_gather(mg_plan* p, int op, const double* d_coef
   a.em = p->d_em;
   a.flags = p->d_counters + 4;
   if (m->order == 1) {
-    if (prec == MG_F32) return launch_gather_t<1, kF32>(p, a, d_values, st);
-    return prec == MG_F64_NATIVE ? launch_gather_t<1, kF64>(p, a, d_values, st)
-                                 : launch_gather_t<1, kDW>(p, a, d_values, st);
+    if (prec == MG_F32) return launch_block_t<kF32>(p, a, d_values, st);
+    return prec == MG_F64_NATIVE ? launch_block_t<kF64>(p, a, d_values, st) : launch_block_t<kDW>(p, a, d_values, st);
   }
-  if (prec == MG_F32) return launch_gather_t<2, kF32>(p, a, d_values, st);
-  return prec == MG_F64_NATIVE ? launch_gather_t<2, kF64>(p, a, d_values, st)
-                               : launch_gather_t<2, kDW>(p, a, d_values, st);
+  if (prec == MG_F32) return launch_gather_t<kF32>(p, a, d_values, st);
+  return prec == MG_F64_NATIVE ? launch_gather_t<kF64>(p, a, d_values, st) : launch_gather_t<kDW>(p, a, d_values, st);
 }
 
 mg_status launch_assemble(mg_plan* p, int op, const double* d_coeff, double c, int quad, int prec,

@@ -119,6 +119,25 @@ struct mg_plan {
   uint32_t* d_src = nullptr;        // n_src
   int64_t n_upper = 0, n_groups = 0, n_diag = 0, n_slot_contrib = 0, n_src = 0;
   void* d_em = nullptr;             // element matrices, nunique x n_elem entries (up to 8 bytes each)
+  // block map of the one-pass P1 assembly (build_block_map): elements in blocks
+  // of kElemBlock consecutive Morton positions, one CTA each.  Block b's local
+  // entries (the runs of an upper entry's sources that fall in the block, longest
+  // first) are the groups bgrp[b] .. bgrp[b+1] of 32 lanes; group g's local sources
+  // bsrc[bgoff[g] + 32 j + lane] (16-bit (p - b kElemBlock) nu + u, padded with
+  // kElemBlock nu), its outputs bout[32 g + lane]: (CSR entry, mirror) of a
+  // complete entry, (-1 - q, 0) for partial sum q of a shared entry, kNoOutput
+  // for an empty lane.  Shared entries (sources in several blocks) in groups of
+  // 32: partials partial[sgoff[g] + 32 j + lane], j < (sgoff[g+1] - sgoff[g]) / 32
+  // in ascending block (zero past a lane's count), written to sout[32 g + lane]
+  int32_t* d_bgrp = nullptr;        // n_blocks + 1
+  int32_t* d_bsrc0 = nullptr;       // n_blocks + 1: bgoff[bgrp[b]] (block b's first local source)
+  int32_t* d_bgoff = nullptr;       // n_bgroups + 1
+  uint16_t* d_bsrc = nullptr;       // n_bsrc
+  int2* d_bout = nullptr;           // 32 n_bgroups
+  int32_t* d_sgoff = nullptr;       // n_sgroups + 1
+  int2* d_sout = nullptr;           // 32 n_sgroups
+  void* d_partial = nullptr;        // n_partial slots of 8 bytes (zero at padding)
+  int64_t n_blocks = 0, n_bgroups = 0, n_bsrc = 0, n_runs = 0, n_shared = 0, n_sgroups = 0, n_partial = 0;
   // load vector (built on the first mg_assemble_rhs): per dof, the slots p * nb + l
   // (p = Morton position of an element touching it, l = the dof's local index)
   // of the element vectors it sums, ascending; and the element-vector buffer
@@ -225,6 +244,17 @@ constexpr uint32_t kPadSource = 0xffffffffu;
 // rows per block of the gather's order: a block's diagonal entries, then its
 // other upper entries (its element matrices stay in L2 across both)
 constexpr int kGatherRowBlock = 256;
+// the one-pass P1 assembly: elements per block (one CTA) and the empty-lane
+// output of its block map
+constexpr int kElemBlock = 512;
+constexpr int32_t kNoOutput = INT32_MIN;
+// the assembly of an element order runs through the block map (one pass, P1)
+// or the slot map and the element-matrix array (two passes, P2)
+inline bool uses_block_map(int order) { return order == 1; }
+// the block map from the per-entry source lists of the slot map (P1 layout,
+// p nu + u, ascending p): see mg_plan::d_bgrp
+mg_status build_block_map(mg_plan* p, int64_t U, const int32_t* useg, const int32_t* uslot, const int32_t* umirror,
+                          const uint32_t* src, cudaStream_t st);
 mg_status build_edges_device(mg_mesh* m, cudaStream_t st);    // edges on the GPU (mg_pattern.cu)
 mg_status ensure_edges(mg_mesh* m);
 mg_status launch_assemble(mg_plan* p, int op, const double* d_coeff, double c, int quad, int prec,

@@ -204,6 +204,14 @@ static void free_plan(mg_plan* p)
   cudaFree(p->d_umirror);
   cudaFree(p->d_src);
   cudaFree(p->d_em);
+  cudaFree(p->d_bgrp);
+  cudaFree(p->d_bsrc0);
+  cudaFree(p->d_bgoff);
+  cudaFree(p->d_bsrc);
+  cudaFree(p->d_bout);
+  cudaFree(p->d_sgoff);
+  cudaFree(p->d_sout);
+  cudaFree(p->d_partial);
   cudaFree(p->d_rhs_ptr);
   cudaFree(p->d_rhs_slot);
   cudaFree(p->d_rhs_y);
@@ -390,6 +398,8 @@ mg_status mg_pattern_device(const mg_plan* pc, const int32_t** d_rowptr, const i
 mg_status mg_plan_slot_map_info(mg_plan* p, mg_slot_map_info* info)
 {
   if (!p || !info) return set_error(MG_ERR_INVALID_ARG, "mg_plan_slot_map_info: null argument");
+  if (uses_block_map(p->mesh->order))
+    return set_error(MG_ERR_UNSUPPORTED, "P1 plans assemble through the block map (mg_plan_block_map_info)");
   MG_TRY(plan_device(p));
   info->n_upper = p->n_upper;
   info->n_groups = p->n_groups;
@@ -408,6 +418,8 @@ mg_status mg_plan_export_slot_map(mg_plan* p, int32_t* h_elem_order, int32_t* h_
                                   int32_t* h_umirror, uint32_t* h_src)
 {
   if (!p) return set_error(MG_ERR_INVALID_ARG, "mg_plan_export_slot_map: null plan");
+  if (uses_block_map(p->mesh->order))
+    return set_error(MG_ERR_UNSUPPORTED, "P1 plans assemble through the block map (mg_plan_export_block_map)");
   MG_TRY(plan_device(p));
   const int64_t E = p->mesh->n_elem, U = p->n_upper, G = p->n_groups, S = p->n_src;
   if (h_elem_order && E) std::memcpy(h_elem_order, p->h_elem_order.data(), sizeof(int32_t) * E);
@@ -415,6 +427,46 @@ mg_status mg_plan_export_slot_map(mg_plan* p, int32_t* h_elem_order, int32_t* h_
   if (h_uslot && U) MG_CUDA(cudaMemcpy(h_uslot, p->d_uslot, sizeof(int32_t) * U, cudaMemcpyDeviceToHost));
   if (h_umirror && U) MG_CUDA(cudaMemcpy(h_umirror, p->d_umirror, sizeof(int32_t) * U, cudaMemcpyDeviceToHost));
   if (h_src && S) MG_CUDA(cudaMemcpy(h_src, p->d_src, sizeof(uint32_t) * S, cudaMemcpyDeviceToHost));
+  return MG_OK;
+}
+
+mg_status mg_plan_block_map_info(mg_plan* p, mg_block_map_info* info)
+{
+  if (!p || !info) return set_error(MG_ERR_INVALID_ARG, "mg_plan_block_map_info: null argument");
+  if (!uses_block_map(p->mesh->order))
+    return set_error(MG_ERR_UNSUPPORTED, "P2 plans assemble through the slot map (mg_plan_slot_map_info)");
+  MG_TRY(plan_device(p));
+  info->n_upper = p->n_upper;
+  info->n_contrib = p->n_slot_contrib;
+  info->n_blocks = p->n_blocks;
+  info->n_groups = p->n_bgroups;
+  info->n_src = p->n_bsrc;
+  info->n_runs = p->n_runs;
+  info->n_shared = p->n_shared;
+  info->n_shared_groups = p->n_sgroups;
+  info->n_partial = p->n_partial;
+  info->n_elem = p->mesh->n_elem;
+  info->nunique = nunique(p->mesh->order);
+  info->elems_per_block = kElemBlock;
+  return MG_OK;
+}
+
+mg_status mg_plan_export_block_map(mg_plan* p, int32_t* h_elem_order, int32_t* h_bgrp, int32_t* h_goff,
+                                   uint16_t* h_src, int32_t* h_out, int32_t* h_sgoff, int32_t* h_sout)
+{
+  if (!p) return set_error(MG_ERR_INVALID_ARG, "mg_plan_export_block_map: null plan");
+  if (!uses_block_map(p->mesh->order))
+    return set_error(MG_ERR_UNSUPPORTED, "P2 plans assemble through the slot map (mg_plan_export_slot_map)");
+  MG_TRY(plan_device(p));
+  const int64_t E = p->mesh->n_elem, G = p->n_bgroups, G3 = p->n_sgroups;
+  if (h_elem_order && E) std::memcpy(h_elem_order, p->h_elem_order.data(), sizeof(int32_t) * E);
+  if (h_bgrp) MG_CUDA(cudaMemcpy(h_bgrp, p->d_bgrp, sizeof(int32_t) * (p->n_blocks + 1), cudaMemcpyDeviceToHost));
+  if (h_goff) MG_CUDA(cudaMemcpy(h_goff, p->d_bgoff, sizeof(int32_t) * (G + 1), cudaMemcpyDeviceToHost));
+  if (h_src && p->n_bsrc)
+    MG_CUDA(cudaMemcpy(h_src, p->d_bsrc, sizeof(uint16_t) * p->n_bsrc, cudaMemcpyDeviceToHost));
+  if (h_out && G) MG_CUDA(cudaMemcpy(h_out, p->d_bout, sizeof(int2) * 32 * G, cudaMemcpyDeviceToHost));
+  if (h_sgoff) MG_CUDA(cudaMemcpy(h_sgoff, p->d_sgoff, sizeof(int32_t) * (G3 + 1), cudaMemcpyDeviceToHost));
+  if (h_sout && G3) MG_CUDA(cudaMemcpy(h_sout, p->d_sout, sizeof(int2) * 32 * G3, cudaMemcpyDeviceToHost));
   return MG_OK;
 }
 

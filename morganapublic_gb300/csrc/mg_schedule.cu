@@ -4,7 +4,9 @@
 //      radix-sorted with the element id (ties by id) -- the host build
 //      (mg_plan.cpp) computes the same keys and order;
 //   2. the slot map (build_slot_map): for every diagonal or upper CSR entry the
-//      element-matrix entries summed into it, in ascending Morton position.
+//      element-matrix entries summed into it, in ascending Morton position;
+//      laid out for the two-pass gather (P2) or turned into the block map of
+//      the one-pass assembly (P1, build_block_map).
 // Setup-only library calls: CUB radix sorts and scans.
 #include <algorithm>
 #include <vector>
@@ -159,13 +161,13 @@ __global__ void k_iota32(int64_t n, uint32_t* v)
   if (i < n) v[i] = (uint32_t)i;
 }
 
-// ptr[d] = first t with key[t] >= d, d = 0 .. nkeys (keys sorted ascending)
-__global__ void k_run_starts(int64_t n, const uint32_t* key, int64_t nkeys, int32_t* ptr)
+// ptr[d] = first t with (key[t] >> shift) >= d, d = 0 .. nkeys (keys sorted ascending)
+__global__ void k_run_starts(int64_t n, const uint32_t* key, int64_t nkeys, int32_t* ptr, int shift = 0)
 {
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t > n) return;
-  const int64_t lo = t == 0 ? 0 : (int64_t)key[t - 1] + 1;
-  const int64_t hi = t == n ? nkeys : (int64_t)key[t];
+  const int64_t lo = t == 0 ? 0 : (int64_t)(key[t - 1] >> shift) + 1;
+  const int64_t hi = t == n ? nkeys : (int64_t)(key[t] >> shift);
   for (int64_t d = lo; d <= hi; ++d) ptr[d] = (int32_t)t;
 }
 
@@ -321,6 +323,225 @@ __global__ void k_group_fill(int64_t G, int64_t U, const uint32_t* __restrict__ 
   for (int32_t j = 0; j < L; ++j) src[o + 32 * j + lane] = j < len ? src_in[s0 + j] : kPadSource;
 }
 
+
+// ---- the block map of the one-pass P1 assembly (see mg_plan::d_bgrp).  A run
+// is a maximal stretch of an upper entry's sources (ascending p) in one element
+// block; an entry with one run is complete, else shared, its runs numbered j in
+// ascending block.  An entry without sources (not produced by a mesh's pattern)
+// counts as one empty run of block 0, so that its value is written (zero).
+__device__ __forceinline__ int32_t block_of(uint32_t s, int nu) { return (int32_t)(s / (uint32_t)nu / kElemBlock); }
+
+__global__ void k_run_count(int64_t U, int nu, const int32_t* __restrict__ useg, const uint32_t* __restrict__ src,
+                            int32_t* __restrict__ nrun, int32_t* __restrict__ shared)
+{
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t > U) return;
+  if (t == U) {  // the exclusive scans' last entry
+    nrun[U] = 0;
+    shared[U] = 0;
+    return;
+  }
+  int32_t n = 0, prev = -1;
+  for (int32_t k = useg[t]; k < useg[t + 1]; ++k) {
+    const int32_t b = block_of(src[k], nu);
+    if (b != prev) ++n, prev = b;
+  }
+  n = max(n, 1);
+  nrun[t] = n;
+  shared[t] = n > 1 ? 1 : 0;
+}
+
+// per run: sort key 64 b + 63 - min(length, 63) (per block the longest runs
+// first, so that a group's lanes have similar lengths), its entry, rank, first
+// source, length
+__device__ __forceinline__ uint32_t run_key(int32_t b, int32_t len)
+{
+  return 64u * (uint32_t)b + 63u - (uint32_t)min(len, 63);
+}
+
+__global__ void k_run_emit(int64_t U, int nu, const int32_t* __restrict__ useg, const uint32_t* __restrict__ src,
+                           const int32_t* __restrict__ rfirst, uint32_t* __restrict__ rkey, uint32_t* __restrict__ rid,
+                           int32_t* __restrict__ rt, int32_t* __restrict__ rj, int32_t* __restrict__ rstart,
+                           int32_t* __restrict__ rlen)
+{
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= U) return;
+  const int32_t k0 = useg[t], k1 = useg[t + 1];
+  int32_t ri = rfirst[t], j = 0;
+  if (k0 == k1) {
+    rkey[ri] = run_key(0, 0), rid[ri] = (uint32_t)ri, rt[ri] = (int32_t)t, rj[ri] = 0, rstart[ri] = k0, rlen[ri] = 0;
+    return;
+  }
+  for (int32_t k = k0; k < k1;) {
+    const int32_t b = block_of(src[k], nu);
+    int32_t e = k + 1;
+    while (e < k1 && block_of(src[e], nu) == b) ++e;
+    rkey[ri] = run_key(b, e - k);
+    rid[ri] = (uint32_t)ri;
+    rt[ri] = (int32_t)t;
+    rj[ri] = j++;
+    rstart[ri] = k;
+    rlen[ri] = e - k;
+    ++ri;
+    k = e;
+  }
+}
+
+// groups of 32 runs per block: their count, then each group's first sorted run
+// and lane count
+__global__ void k_seg_groups(int64_t nseg, const int32_t* __restrict__ seg_ptr, int32_t* __restrict__ ng)
+{
+  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s < nseg) ng[s] = (seg_ptr[s + 1] - seg_ptr[s] + 31) / 32;
+  else if (s == nseg) ng[s] = 0;
+}
+
+__global__ void k_seg_fill(int64_t nseg, const int32_t* __restrict__ seg_ptr, const int32_t* __restrict__ seg_g,
+                           int32_t* __restrict__ grun0, int32_t* __restrict__ gcnt)
+{
+  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= nseg) return;
+  const int32_t r0 = seg_ptr[s], r1 = seg_ptr[s + 1];
+  for (int32_t g = seg_g[s], r = r0; r < r1; ++g, r += 32) {
+    grun0[g] = r;
+    gcnt[g] = min(32, r1 - r);
+  }
+}
+
+// 32 x the longest run of each group (the [j][lane] rows of its sources)
+__global__ void k_bgroup_len(int64_t G, const int32_t* __restrict__ grun0, const int32_t* __restrict__ gcnt,
+                             const uint32_t* __restrict__ perm, const int32_t* __restrict__ rlen, int32_t* __restrict__ glen)
+{
+  const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (g > G) return;
+  int32_t L = 0;
+  if (g < G)
+    for (int32_t l = 0; l < gcnt[g]; ++l) L = max(L, rlen[perm[grun0[g] + l]]);
+  glen[g] = 32 * L;
+}
+
+// the shared entries in CSR order, and 32 x the most runs of each group of 32
+__global__ void k_shared_list(int64_t U, const int32_t* __restrict__ shared, const int32_t* __restrict__ sidx,
+                              int32_t* __restrict__ sh_t)
+{
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t < U && shared[t]) sh_t[sidx[t]] = (int32_t)t;
+}
+
+// shared entry i (CSR order) keyed by its run count, most first; and the
+// inverse of the sorted order
+__global__ void k_shared_keys(int64_t S, const int32_t* __restrict__ sh_t, const int32_t* __restrict__ nrun,
+                              uint32_t* __restrict__ key)
+{
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < S) key[i] = 63u - (uint32_t)min(nrun[sh_t[i]], 63);
+}
+
+__global__ void k_shared_rank(int64_t S, const int32_t* __restrict__ sh_sorted, int32_t* __restrict__ srank)
+{
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < S) srank[sh_sorted[i]] = (int32_t)i;
+}
+
+__global__ void k_sgroup_len(int64_t G3, int64_t S, const int32_t* __restrict__ sh_t, const int32_t* __restrict__ nrun,
+                             int32_t* __restrict__ slen)
+{
+  const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (g > G3) return;
+  int32_t L = 0;
+  if (g < G3)
+    for (int64_t i = 32 * g; i < min(32 * g + 32, S); ++i) L = max(L, nrun[sh_t[i]]);
+  slen[g] = 32 * L;
+}
+
+__global__ void k_sgroup_out(int64_t G3, int64_t S, const int32_t* __restrict__ sh_t, const int32_t* __restrict__ uslot,
+                             const int32_t* __restrict__ umirror, int2* __restrict__ sout)
+{
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= 32 * G3) return;
+  sout[i] = i < S ? make_int2(uslot[sh_t[i]], umirror[sh_t[i]]) : make_int2(kNoOutput, kNoOutput);
+}
+
+// one thread per (group, lane): the run's local sources [j][lane] and its output
+__global__ void k_bfill(int64_t G, int nu, const int32_t* __restrict__ grun0, const int32_t* __restrict__ gcnt,
+                        const uint32_t* __restrict__ perm, const uint32_t* __restrict__ skey,
+                        const int32_t* __restrict__ rt, const int32_t* __restrict__ rj,
+                        const int32_t* __restrict__ rstart, const int32_t* __restrict__ rlen,
+                        const uint32_t* __restrict__ src, const int32_t* __restrict__ uslot,
+                        const int32_t* __restrict__ umirror, const int32_t* __restrict__ nrun,
+                        const int32_t* __restrict__ srank, const int32_t* __restrict__ sgoff,
+                        const int32_t* __restrict__ bgoff, uint16_t* __restrict__ bsrc, int2* __restrict__ bout)
+{
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= 32 * G) return;
+  const int64_t g = i >> 5;
+  const int lane = (int)(i & 31);
+  const int32_t o = bgoff[g], L = (bgoff[g + 1] - o) >> 5;
+  const uint16_t pad = (uint16_t)(kElemBlock * nu);
+  if (lane >= gcnt[g]) {
+    bout[i] = make_int2(kNoOutput, 0);
+    for (int32_t j = 0; j < L; ++j) bsrc[o + 32 * j + lane] = pad;
+    return;
+  }
+  const int32_t sr = grun0[g] + lane;
+  const uint32_t ri = perm[sr];
+  const uint32_t base = (skey[sr] >> 6) * (uint32_t)kElemBlock * (uint32_t)nu;
+  const int32_t t = rt[ri], k0 = rstart[ri], len = rlen[ri];
+  for (int32_t j = 0; j < L; ++j) bsrc[o + 32 * j + lane] = j < len ? (uint16_t)(src[k0 + j] - base) : pad;
+  if (nrun[t] == 1) {
+    bout[i] = make_int2(uslot[t], umirror[t]);
+  } else {
+    const int32_t s = srank[t];
+    const int32_t q = sgoff[s >> 5] + 32 * rj[ri] + (s & 31);
+    bout[i] = make_int2(-1 - q, 0);
+  }
+}
+
+// block b's first group and first local source
+__global__ void k_bgrp(int64_t nblk, const int32_t* __restrict__ seg_g, const int32_t* __restrict__ bgoff,
+                       int32_t* __restrict__ bgrp, int32_t* __restrict__ bsrc0)
+{
+  const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (b <= nblk) {
+    bgrp[b] = seg_g[b];
+    bsrc0[b] = bgoff[seg_g[b]];
+  }
+}
+
+template <typename In, typename Out>
+mg_status exclusive_scan(SchedBuffers& B, const In* in, Out* out, int64_t n, cudaStream_t st)
+{
+  size_t tb = 0;
+  MG_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tb, in, out, (int)n, st));
+  unsigned char* tmp;
+  MG_TRY(B.alloc(&tmp, (int64_t)std::max(tb, (size_t)1)));
+  MG_CUDA(cub::DeviceScan::ExclusiveSum(tmp, tb, in, out, (int)n, st));
+  return MG_OK;
+}
+
+template <typename T>
+mg_status read_back(T* h, const T* d, cudaStream_t st)
+{
+  MG_CUDA(cudaMemcpyAsync(h, d, sizeof(T), cudaMemcpyDeviceToHost, st));
+  MG_CUDA(cudaStreamSynchronize(st));
+  return MG_OK;
+}
+
+// 64-bit offsets narrowed to the plan's 32-bit layout, checked
+mg_status narrow_offsets(SchedBuffers& B, const int32_t* len, int64_t n, int32_t** out, int64_t* total,
+                         const char* what, cudaStream_t st)
+{
+  int64_t* off64;
+  MG_TRY(B.alloc(&off64, n + 1));
+  MG_TRY(exclusive_scan(B, len, off64, n + 1, st));
+  MG_TRY(read_back(total, off64 + n, st));
+  if (*total >= INT32_MAX) return set_error(MG_ERR_SIZE, std::string(what) + " above 2^31 entries");
+  MG_TRY(B.alloc(out, n + 1));
+  k_narrow<<<grid_of(n + 1), 256, 0, st>>>(n + 1, off64, *out);
+  MG_CUDA(cudaGetLastError());
+  return MG_OK;
+}
+
 }  // namespace
 
 // --------------------------------------------------------------- slot map --
@@ -390,6 +611,13 @@ mg_status build_slot_map(mg_plan* p, cudaStream_t st)
   MG_CUDA(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
   MG_CUDA(cudaStreamSynchronize(st));
   if (hbad) return set_error(MG_ERR_INVALID_ARG, "slot map: an element coupling is missing from the plan's pattern");
+  if (uses_block_map(m->order)) {
+    // one-pass assembly: the per-entry lists become the block map
+    MG_TRY(build_block_map(p, U, useg, uslot, umirror, src, st));
+    p->n_upper = U;
+    p->n_slot_contrib = C;
+    return MG_OK;
+  }
   // ---- regroup for the gather: entries stably sorted by (row block, off-diagonal)
   const int64_t G = (U + 31) / 32;
   int32_t *glen, *goff, *gslot, *gmirror, *d_ndiag;
@@ -445,6 +673,141 @@ mg_status build_slot_map(mg_plan* p, cudaStream_t st)
   return MG_OK;
 }
 
+
+// ------------------------------------------------------------- block map --
+// The one-pass P1 assembly's layout (see mg_plan::d_bgrp) from the slot map's
+// per-entry source lists (p nu + u, ascending p):
+//   1. runs per upper entry (block changes along its sources) and their prefix;
+//      the shared entries (more than one run) and their prefix;
+//   2. one record per run, radix-sorted (stable) by (block, longest first):
+//      runs of equal length (or 63 and more) in CSR order;
+//   3. groups of 32 runs per block, each sized by its longest run;
+//   4. the shared entries sorted (stable) by run count, most first, in groups
+//      of 32 sized by their most runs: the partial-sum slots, which fix each
+//      run's output;
+//   5. one thread per (group, lane): the local sources and the output.
+mg_status build_block_map(mg_plan* p, int64_t U, const int32_t* useg, const int32_t* uslot, const int32_t* umirror,
+                          const uint32_t* src, cudaStream_t st)
+{
+  const int nu = nunique(p->mesh->order);
+  const int64_t E = p->mesh->n_elem;
+  const int64_t nblk = std::max<int64_t>(1, (E + kElemBlock - 1) / kElemBlock);
+  const int64_t nseg = nblk;
+  if (64 * nblk >= UINT32_MAX / 2) return set_error(MG_ERR_SIZE, "block map: too many element blocks");
+  SchedBuffers B;
+  int32_t *nrun, *shared, *rfirst, *sidx;
+  MG_TRY(B.alloc(&nrun, U + 1));
+  MG_TRY(B.alloc(&shared, U + 1));
+  MG_TRY(B.alloc(&rfirst, U + 1));
+  MG_TRY(B.alloc(&sidx, U + 1));
+  k_run_count<<<grid_of(U + 1), 256, 0, st>>>(U, nu, useg, src, nrun, shared);
+  MG_CUDA(cudaGetLastError());
+  MG_TRY(exclusive_scan(B, nrun, rfirst, U + 1, st));
+  MG_TRY(exclusive_scan(B, shared, sidx, U + 1, st));
+  int32_t R = 0, S = 0;
+  MG_TRY(read_back(&R, rfirst + U, st));
+  MG_TRY(read_back(&S, sidx + U, st));
+  // ---- runs, sorted by (block, length); the sort is stable, so CSR order within
+  uint32_t *rkey, *skey, *rid, *perm;
+  int32_t *rt, *rj, *rstart, *rlen;
+  MG_TRY(B.alloc(&rkey, R));
+  MG_TRY(B.alloc(&skey, R));
+  MG_TRY(B.alloc(&rid, R));
+  MG_TRY(B.alloc(&perm, R));
+  MG_TRY(B.alloc(&rt, R));
+  MG_TRY(B.alloc(&rj, R));
+  MG_TRY(B.alloc(&rstart, R));
+  MG_TRY(B.alloc(&rlen, R));
+  if (U > 0)
+    k_run_emit<<<grid_of(U), 256, 0, st>>>(U, nu, useg, src, rfirst, rkey, rid, rt, rj, rstart, rlen);
+  int kbits = 1;
+  while ((1ll << kbits) <= 64 * nblk) ++kbits;
+  size_t tb = 0;
+  MG_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tb, rkey, skey, rid, perm, (int)R, 0, kbits, st));
+  unsigned char* tmp;
+  MG_TRY(B.alloc(&tmp, (int64_t)std::max(tb, (size_t)1)));
+  MG_CUDA(cub::DeviceRadixSort::SortPairs(tmp, tb, rkey, skey, rid, perm, (int)R, 0, kbits, st));
+  // ---- groups of 32 runs per block
+  int32_t *seg_ptr, *ng, *seg_g;
+  MG_TRY(B.alloc(&seg_ptr, nseg + 1));
+  MG_TRY(B.alloc(&ng, nseg + 1));
+  MG_TRY(B.alloc(&seg_g, nseg + 1));
+  k_run_starts<<<grid_of((int64_t)R + 1), 256, 0, st>>>(R, skey, nseg, seg_ptr, 6);
+  k_seg_groups<<<grid_of(nseg + 1), 256, 0, st>>>(nseg, seg_ptr, ng);
+  MG_CUDA(cudaGetLastError());
+  MG_TRY(exclusive_scan(B, ng, seg_g, nseg + 1, st));
+  int32_t G = 0;
+  MG_TRY(read_back(&G, seg_g + nseg, st));
+  int32_t *grun0, *gcnt, *glen, *bgoff;
+  MG_TRY(B.alloc(&grun0, G));
+  MG_TRY(B.alloc(&gcnt, G));
+  MG_TRY(B.alloc(&glen, (int64_t)G + 1));
+  k_seg_fill<<<grid_of(nseg), 256, 0, st>>>(nseg, seg_ptr, seg_g, grun0, gcnt);
+  k_bgroup_len<<<grid_of((int64_t)G + 1), 256, 0, st>>>(G, grun0, gcnt, perm, rlen, glen);
+  MG_CUDA(cudaGetLastError());
+  int64_t nsrc = 0;
+  MG_TRY(narrow_offsets(B, glen, G, &bgoff, &nsrc, "block map: padded sources", st));
+  // ---- shared entries (most runs first) and their partial-sum slots
+  const int64_t G3 = ((int64_t)S + 31) / 32;
+  int32_t *sh_csr, *sh_t, *srank, *slen, *sgoff;
+  uint32_t *shk, *shk2;
+  int2* sout;
+  MG_TRY(B.alloc(&sh_csr, S));
+  MG_TRY(B.alloc(&sh_t, S));
+  MG_TRY(B.alloc(&srank, U));
+  MG_TRY(B.alloc(&shk, S));
+  MG_TRY(B.alloc(&shk2, S));
+  MG_TRY(B.alloc(&slen, G3 + 1));
+  MG_TRY(B.alloc(&sout, 32 * G3));
+  if (U > 0) k_shared_list<<<grid_of(U), 256, 0, st>>>(U, shared, sidx, sh_csr);
+  if (S > 0) k_shared_keys<<<grid_of(S), 256, 0, st>>>(S, sh_csr, nrun, shk);
+  size_t tb5 = 0;
+  MG_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tb5, shk, shk2, sh_csr, sh_t, (int)S, 0, 6, st));
+  unsigned char* tmp5;
+  MG_TRY(B.alloc(&tmp5, (int64_t)std::max(tb5, (size_t)1)));
+  MG_CUDA(cub::DeviceRadixSort::SortPairs(tmp5, tb5, shk, shk2, sh_csr, sh_t, (int)S, 0, 6, st));
+  if (S > 0) k_shared_rank<<<grid_of(S), 256, 0, st>>>(S, sh_t, srank);
+  k_sgroup_len<<<grid_of(G3 + 1), 256, 0, st>>>(G3, S, sh_t, nrun, slen);
+  MG_CUDA(cudaGetLastError());
+  int64_t Q = 0;
+  MG_TRY(narrow_offsets(B, slen, G3, &sgoff, &Q, "block map: partial sums", st));
+  if (G3 > 0) k_sgroup_out<<<grid_of(32 * G3), 256, 0, st>>>(G3, S, sh_t, uslot, umirror, sout);
+  // ---- local sources and outputs
+  uint16_t* bsrc;
+  int2* bout;
+  int32_t *bgrp, *bsrc0;
+  void* partial;
+  MG_TRY(B.alloc(&bsrc, nsrc));
+  MG_TRY(B.alloc(&bout, 32 * (int64_t)G));
+  MG_TRY(B.alloc(&bgrp, nblk + 1));
+  MG_TRY(B.alloc(&bsrc0, nblk + 1));
+  MG_TRY(B.alloc(reinterpret_cast<double**>(&partial), Q));
+  MG_CUDA(cudaMemsetAsync(partial, 0, sizeof(double) * (size_t)std::max<int64_t>(Q, 1), st));
+  if (G > 0)
+    k_bfill<<<grid_of(32 * (int64_t)G), 256, 0, st>>>(G, nu, grun0, gcnt, perm, skey, rt, rj, rstart, rlen, src, uslot,
+                                                      umirror, nrun, srank, sgoff, bgoff, bsrc, bout);
+  k_bgrp<<<grid_of(nblk + 1), 256, 0, st>>>(nblk, seg_g, bgoff, bgrp, bsrc0);
+  MG_CUDA(cudaGetLastError());
+  MG_CUDA(cudaStreamSynchronize(st));
+  p->d_bgrp = bgrp;
+  p->d_bsrc0 = bsrc0;
+  p->d_bgoff = bgoff;
+  p->d_bsrc = bsrc;
+  p->d_bout = bout;
+  p->d_sgoff = sgoff;
+  p->d_sout = sout;
+  p->d_partial = partial;
+  p->n_blocks = nblk;
+  p->n_bgroups = G;
+  p->n_bsrc = nsrc;
+  p->n_runs = R;
+  p->n_shared = S;
+  p->n_sgroups = G3;
+  p->n_partial = Q;
+  for (void* q : {(void*)bgrp, (void*)bsrc0, (void*)bgoff, (void*)bsrc, (void*)bout, (void*)sgoff, (void*)sout, partial})
+    B.keep(q);
+  return MG_OK;
+}
 
 // The plan's device state from its device pattern: the Morton element order,
 // the dofs in that order, the diagonal entries and 16-bit column offsets, the

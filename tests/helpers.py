@@ -120,3 +120,132 @@ def emulate_slot_map(sm, order, elem_order, local_mats, nnz):
             out[sm["uslot"][t]] = v
             out[sm["umirror"][t]] = v
     return out
+
+
+NO_OUTPUT = -2**31
+
+
+def expected_block_map(elem_order, dofs, rowptr, colind, elems_per_block=512):
+    """The block map of the one-pass P1 assembly restated.  Upper entries (r, c),
+    c >= r, in CSR order; an entry's sources are p * 10 + u for every element p
+    (Morton position) holding both dofs, ascending p.  A run is a maximal stretch
+    of them in one block (p // elems_per_block); an entry with one run is complete,
+    else shared (an entry without sources is one empty run of block 0).  Runs
+    sorted stably by (block, longest first, lengths from 63 up tied) and cut
+    into groups of 32 per block; a group's local sources (p - b Be) * 10 + u stored [j][lane], padded
+    with Be * 10; outputs (slot, mirror) for a complete entry, (-1 - q, 0) for
+    partial slot q, (NO_OUTPUT, 0) for an empty lane.  Shared entries sorted
+    stably by run count (most first, 63 and more tied), groups of 32, run j of
+    lane l at slot sgoff[g] + 32 j + l."""
+    nb, nu, Be = 4, 10, elems_per_block
+    E = len(elem_order)
+    nblk = max(1, (E + Be - 1) // Be)
+    dm = np.asarray(dofs)[np.asarray(elem_order)]
+    contrib = {}
+    for p in range(E):
+        for i in range(nb):
+            for j in range(nb):
+                r, c = int(dm[p, i]), int(dm[p, j])
+                if c >= r:
+                    contrib.setdefault((r, c), []).append(p * nu + sym_index(i, j, nb))
+    entries = []  # (slot, mirror, sources)
+    for r in range(len(rowptr) - 1):
+        for k in range(rowptr[r], rowptr[r + 1]):
+            c = int(colind[k])
+            if c < r:
+                continue
+            m0 = rowptr[c]
+            mirror = m0 + int(np.searchsorted(colind[m0:rowptr[c + 1]], r))
+            entries.append((k, mirror, contrib.get((r, c), [])))
+    runs_of = []
+    for slot, mirror, srcs in entries:
+        runs = []
+        for s in srcs:
+            b = (s // nu) // Be
+            if runs and runs[-1][0] == b:
+                runs[-1][1].append(s)
+            else:
+                runs.append((b, [s]))
+        runs_of.append(runs if runs else [(0, [])])
+    shared = [t for t in range(len(entries)) if len(runs_of[t]) > 1]
+    shared.sort(key=lambda t: 63 - min(len(runs_of[t]), 63))  # stable: most runs first, then CSR order
+    sidx = {t: i for i, t in enumerate(shared)}
+    sgoff, sout = [0], []
+    for g in range(0, len(shared), 32):
+        grp = shared[g:g + 32]
+        sgoff.append(sgoff[-1] + 32 * max(len(runs_of[t]) for t in grp))
+        sout.extend([entries[t][0], entries[t][1]] for t in grp)
+        sout.extend([NO_OUTPUT, NO_OUTPUT] for _ in range(32 - len(grp)))
+    recs = []  # ((block, 63 - min(length, 63)), t, j, sources)
+    for t, runs in enumerate(runs_of):
+        for j, (b, srcs) in enumerate(runs):
+            recs.append(((b, 63 - min(len(srcs), 63)), t, j, srcs))
+    recs.sort(key=lambda x: x[0])  # stable: CSR order, then j, within a (block, length)
+    by_block = [[] for _ in range(nblk)]
+    for x in recs:
+        by_block[x[0][0]].append(x)
+    bgrp, goff, src, out = [], [0], [], []
+    for b in range(nblk):
+        bgrp.append(len(goff) - 1)
+        if True:
+            seg = by_block[b]
+            for g in range(0, len(seg), 32):
+                grp = seg[g:g + 32]
+                L = max(len(x[3]) for x in grp)
+                rows = np.full((L, 32), Be * nu, dtype=np.uint16)
+                for lane, (_, t, j, srcs) in enumerate(grp):
+                    rows[:len(srcs), lane] = [s - b * Be * nu for s in srcs]
+                    if len(runs_of[t]) == 1:
+                        out.append([entries[t][0], entries[t][1]])
+                    else:
+                        s_i = sidx[t]
+                        out.append([-1 - (sgoff[s_i // 32] + 32 * j + s_i % 32), 0])
+                out.extend([NO_OUTPUT, 0] for _ in range(32 - len(grp)))
+                src.extend(rows.reshape(-1).tolist())
+                goff.append(len(src))
+    bgrp.append(len(goff) - 1)
+    return {"bgrp": np.array(bgrp, dtype=np.int32), "goff": np.array(goff, dtype=np.int32),
+            "src": np.array(src, dtype=np.uint16), "out": np.array(out, dtype=np.int32).reshape(-1, 2),
+            "sgoff": np.array(sgoff, dtype=np.int32), "sout": np.array(sout, dtype=np.int32).reshape(-1, 2),
+            "n_shared": len(shared), "n_runs": len(recs), "n_upper": len(entries)}
+
+
+def emulate_block_map(bm, elem_order, local_mats, nnz, elems_per_block=None):
+    """The one-pass P1 assembly run on the host with given element matrices
+    (local_mats[e] = [field i, test j]) through a block map -- checks the map only:
+    per block its local sums (complete entries written, shared ones to their
+    partial slots), then the partial sums in slot order."""
+    nu = 10
+    Be = int(bm["info"].elems_per_block if elems_per_block is None else elems_per_block)
+    pairs = [(i, j) for i in range(4) for j in range(i, 4)]
+    E = len(elem_order)
+    em = np.zeros((max(1, (E + Be - 1) // Be) * Be, nu))
+    for p, e in enumerate(elem_order):
+        for u, (i, j) in enumerate(pairs):
+            em[p, u] = local_mats[e][i, j]
+    values = np.full(nnz, np.nan)
+    partial = np.zeros(max(1, int(bm["sgoff"][-1])))
+    for b in range(len(bm["bgrp"]) - 1):
+        local = np.append(em[b * Be:(b + 1) * Be].reshape(-1), 0.0)
+        for g in range(bm["bgrp"][b], bm["bgrp"][b + 1]):
+            rows = bm["src"][bm["goff"][g]:bm["goff"][g + 1]].reshape(-1, 32)
+            for lane in range(32):
+                v = 0.0
+                for s in rows[:, lane]:
+                    v += local[int(s)]
+                o = bm["out"][32 * g + lane]
+                if o[0] >= 0:
+                    values[o[0]] = v
+                    values[o[1]] = v
+                elif o[0] != NO_OUTPUT:
+                    partial[-1 - o[0]] = v
+    for g in range(len(bm["sgoff"]) - 1):
+        rows = partial[bm["sgoff"][g]:bm["sgoff"][g + 1]].reshape(-1, 32)
+        for lane in range(32):
+            o = bm["sout"][32 * g + lane]
+            if o[0] >= 0:
+                v = 0.0
+                for x in rows[:, lane]:
+                    v += x
+                values[o[0]] = values[o[1]] = v
+    return values

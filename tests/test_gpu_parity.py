@@ -9,7 +9,7 @@ import pytest
 import morganapublic_gb300 as mg
 import oracle as orc
 from morganapublic_gb300 import meshgen
-from helpers import emulate_slot_map, expected_slot_map, row_scaled_err
+from helpers import emulate_block_map, emulate_slot_map, expected_block_map, expected_slot_map, row_scaled_err
 
 pytestmark = pytest.mark.gpu
 
@@ -289,9 +289,15 @@ def test_device_pattern_build_matches_host(case):
     rp_h, ci_h = host.pattern()
     rp_d, ci_d = dev.pattern()
     assert np.array_equal(rp_h, rp_d) and np.array_equal(ci_h, ci_d)
-    sh, sd = host.export_slot_map(), dev.export_slot_map()
-    for f in ("n_upper", "n_groups", "n_diag", "n_contrib", "n_src", "n_elem", "nunique", "elem_major",
-              "rows_per_block"):
+    if order == 1:
+        sh, sd = host.export_block_map(), dev.export_block_map()
+        fields = ("n_upper", "n_contrib", "n_blocks", "n_groups", "n_src", "n_runs", "n_shared", "n_shared_groups",
+                  "n_partial", "n_elem", "nunique", "elems_per_block")
+    else:
+        sh, sd = host.export_slot_map(), dev.export_slot_map()
+        fields = ("n_upper", "n_groups", "n_diag", "n_contrib", "n_src", "n_elem", "nunique", "elem_major",
+                  "rows_per_block")
+    for f in fields:
         assert getattr(sh["info"], f) == getattr(sd["info"], f), f
     for k in sh:
         if k != "info":
@@ -672,7 +678,38 @@ def test_strongly_jittered_mesh_p2(jitter, seed):
     assert e64 <= F64_TOL and e32 <= 2 * F32_TOL
 
 
-@pytest.mark.parametrize("order,rule", [(1, "lex"), (2, "lex"), (2, "first")])
+@pytest.mark.parametrize("n,jitter", [(3, 0.2), (7, 0.25), (12, 0.3)])
+def test_block_map_matches_restatement_and_oracle(n, jitter):
+    """The device-built block map of a P1 plan equals its numpy restatement bit for
+    bit (runs per block, local sources, outputs, partial-sum slots of the shared
+    entries), and summing the oracle's element matrices through it gives the
+    oracle's CSR values.  12^3 spans 21 element blocks."""
+    m = meshgen.kuhn_cube(n, jitter=jitter, seed=8, permute=True)
+    kappa = meshgen.lognormal(len(m.conn), 1.0, 6)
+    mesh = mg.Mesh(m.xyz, m.conn, order=1)
+    b = mg.MatrixBuilder(mesh)
+    bm = b.export_block_map()
+    rp, ci = b.pattern()
+    info = bm["info"]
+    assert info.elems_per_block == 512 and info.nunique == 10
+    exp = expected_block_map(bm["elem_order"], mesh.elem_dofs(), rp, ci, info.elems_per_block)
+    for k in ("bgrp", "goff", "src", "out", "sgoff", "sout"):
+        assert np.array_equal(bm[k], exp[k]), k
+    assert (info.n_shared, info.n_runs, info.n_upper) == (exp["n_shared"], exp["n_runs"], exp["n_upper"])
+    assert info.n_blocks == (len(m.conn) + 511) // 512 and info.n_contrib == 10 * len(m.conn)
+    assert (info.n_shared > 0) == (info.n_blocks > 1)
+    with pytest.raises(mg.MorganaError):
+        b.export_slot_map()  # P1 plans have no two-pass slot map
+    dofs, rpo, cio, ref = orc.full_operator("stiff_kappa", 1, 4, m.xyz, m.conn, coeff=kappa)
+    mats = [orc.local_matrix("stiff_kappa", 1, 4, m.xyz, m.conn[e], kappa=kappa[e]) for e in range(len(m.conn))]
+    got = emulate_block_map(bm, bm["elem_order"], mats, b.nnz)
+    assert not np.isnan(got).any()
+    assert row_scaled_err(rp, ref, got) <= 1e-14
+    v = b.assemble("stiff_kappa", coeff=kappa, quad=4, prec="f64").cpu().numpy()
+    assert row_scaled_err(rp, ref, v) <= F64_TOL
+
+
+@pytest.mark.parametrize("order,rule", [(2, "lex"), (2, "first")])
 @pytest.mark.parametrize("n,jitter", [(3, 0.2), (4, 0.0), (7, 0.25)])
 def test_slot_map_matches_restatement_and_oracle(order, rule, n, jitter):
     """The device-built slot map equals its numpy restatement bit for bit (entries,

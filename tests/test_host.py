@@ -11,7 +11,7 @@ import pytest
 import morganapublic_gb300 as mg
 import oracle as orc
 from morganapublic_gb300 import meshgen
-from helpers import morton_elem_order
+from helpers import emulate_block_map, expected_block_map, morton_elem_order, row_scaled_err
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = os.path.join(ROOT, "tests", "golden")
@@ -182,3 +182,28 @@ def test_plan_independent_of_thread_count(tmp_path):
     for key, (rp, ci, eo) in res[1].items():
         rp4, ci4, eo4 = res[4][key]
         assert np.array_equal(rp, rp4) and np.array_equal(ci, ci4) and np.array_equal(eo, eo4)
+
+
+@pytest.mark.parametrize("elems_per_block", [16, 64, 512])
+def test_block_map_restatement_sums_to_oracle(elems_per_block):
+    """The block-map restatement (the layout the GPU build is checked against) is
+    self-consistent on CPU: with small blocks most entries span several blocks,
+    and summing the oracle's element matrices through its local sums and partial
+    slots gives the oracle's CSR values; every partial slot of a lane's runs is
+    written exactly once, padding slots never."""
+    m = meshgen.kuhn_cube(4, jitter=0.25, seed=4, permute=True)
+    kappa = meshgen.lognormal(len(m.conn), 1.0, 9)
+    b = mg.MatrixBuilder(mg.Mesh(m.xyz, m.conn, order=1))
+    rp, ci = b.pattern()
+    order = b.elem_order()
+    bm = expected_block_map(order, m.conn, rp, ci, elems_per_block)
+    nblk = (len(m.conn) + elems_per_block - 1) // elems_per_block
+    assert len(bm["bgrp"]) == nblk + 1 and (bm["n_shared"] > 0) == (nblk > 1)
+    q = -1 - bm["out"][:, 0][(bm["out"][:, 0] < 0) & (bm["out"][:, 0] != -2**31)]
+    assert len(q) == len(set(q.tolist())) == bm["n_runs"] - (bm["n_upper"] - bm["n_shared"])
+    assert np.all(q < bm["sgoff"][-1])
+    _, rpo, cio, ref = orc.full_operator("stiff_kappa", 1, 4, m.xyz, m.conn, coeff=kappa)
+    mats = [orc.local_matrix("stiff_kappa", 1, 4, m.xyz, m.conn[e], kappa=kappa[e]) for e in range(len(m.conn))]
+    got = emulate_block_map(bm, order, mats, b.nnz, elems_per_block)
+    assert not np.isnan(got).any()
+    assert row_scaled_err(rp, ref, got) <= 1e-14
