@@ -854,8 +854,8 @@ __device__ __forceinline__ void cp_async4(void* smem, const void* gmem)
 // and FP64 arithmetic, 256 (two elements each, four CTAs per SM) for FP32 --
 // measured on GB300 at P1 128^3 (the double-word loop over two elements spills).
 template <int MODE, int THREADS>
-__global__ void __launch_bounds__(THREADS, 2048 / THREADS / 2) k_block_asm(ElemArgs a, BlockArgs bm,
-                                                                         typename Arith<MODE>::Out* __restrict__ values)
+__global__ void __launch_bounds__(THREADS, 2048 / THREADS / 2)
+    k_block_asm(ElemArgs a, BlockArgs bm, typename Arith<MODE>::Out* __restrict__ values)
 {
   using A = Arith<MODE>;
   using T = typename A::T;

@@ -410,7 +410,8 @@ __global__ void k_seg_fill(int64_t nseg, const int32_t* __restrict__ seg_ptr, co
 
 // 32 x the longest run of each group (the [j][lane] rows of its sources)
 __global__ void k_bgroup_len(int64_t G, const int32_t* __restrict__ grun0, const int32_t* __restrict__ gcnt,
-                             const uint32_t* __restrict__ perm, const int32_t* __restrict__ rlen, int32_t* __restrict__ glen)
+                             const uint32_t* __restrict__ perm, const int32_t* __restrict__ rlen,
+                             int32_t* __restrict__ glen)
 {
   const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (g > G) return;
@@ -804,7 +805,8 @@ mg_status build_block_map(mg_plan* p, int64_t U, const int32_t* useg, const int3
   p->n_shared = S;
   p->n_sgroups = G3;
   p->n_partial = Q;
-  for (void* q : {(void*)bgrp, (void*)bsrc0, (void*)bgoff, (void*)bsrc, (void*)bout, (void*)sgoff, (void*)sout, partial})
+  for (void* q : {(void*)bgrp, (void*)bsrc0, (void*)bgoff, (void*)bsrc, (void*)bout, (void*)sgoff, (void*)sout,
+                  partial})
     B.keep(q);
   return MG_OK;
 }

@@ -101,15 +101,21 @@ static int sm_count()
 }
 
 template <typename V> constexpr int kEntriesPerLane = sizeof(V) == 8 ? 16 : 8;
-// entries per lane and pass of the standalone SpMV: FP64 one lane per row 15 (the
-// interior rows of a P1 Kuhn mesh have 15 entries: one pass, no FMA wasted on an
-// empty 16th; measured at P1 128^3: 80.5 us against 84.6 us with 16)
-template <typename V, int G> constexpr int kSpmvEntries = (sizeof(V) == 8 && G == 1) ? 15 : kEntriesPerLane<V>;
 
-// Lanes per row of the standalone SpMV (measured on GB300 at P1 128^3 and P2
-// 48^3): FP64 one lane per row up to 16 entries on average (P1), two above
-// (P2); FP32 the smallest group of at least 2 lanes whose pass covers the mean
-// row length.
+// FP64 row shape.  GB300 issues 2 FP64 FMA lanes per SM per clock, about as many
+// products as HBM delivers matrix entries, and a warp instruction occupies the
+// FP64 pipe whatever its active lanes: every lane of a warp issues the FMAs of
+// the passes its longest row needs.  The FP64 kernels therefore prefer one
+// thread per row (no shuffle-adds) with 15 entries per pass: interior P1 rows
+// have 15 entries, one pass; P2 rows (19, 27 and 65 entries) take 2, 2 and 5.
+// The standalone SpMV keeps two lanes of 16 entries for rows above 16 entries
+// on average: there the single-lane loads cost more L1 throughput than the FMAs
+// they save (measured on GB300 at P2 48^3: 101 us against 99 us).
+constexpr int kF64Entries = 15;
+
+// Lanes per row of the standalone SpMV: FP64 one up to 16 entries on average
+// (P1), two above (P2); FP32 the smallest group of at least 2 lanes whose pass
+// covers the mean row length (measured on GB300 at P1 128^3 and P2 48^3).
 template <typename V>
 static int row_group(int64_t rows, int64_t nnz)
 {
@@ -149,16 +155,19 @@ static int row_blocks(const mg_plan* p, int G)
   return row_blocks(p, G, 8);
 }
 
-// Shape of the CG kernels (measured on GB300 at 64^3 P1 and 32^3 / 48^3 P2):
-// rows by 2 lanes x 8 entries (more lanes for longer rows); FP64 at most 4
-// CTAs per SM (fewer partials for the last CTA to sum) and launched without
+// Shape of the CG kernels: FP64 one thread per row, 15 entries per pass (the
+// FP64 row shape above; measured on GB300 against two or four lanes of 8: 151
+// against 159 us per iteration at P1 128^3, 136 against 142 us at P2 48^3);
+// FP32 rows by 2 lanes x 8 entries (more lanes for longer rows).  FP64 at most
+// 4 CTAs per SM (fewer partials for the last CTA to sum) and launched without
 // programmatic dependent launch (it slowed the FP64 iteration); FP32 up to 8
 // CTAs per SM, with programmatic dependent launch.
 template <typename V> struct CgShape {
-  static constexpr int U = 8;
+  static constexpr int U = sizeof(V) == 8 ? kF64Entries : 8;
   static constexpr bool pdl = sizeof(V) == 4;
   static int group(const mg_plan* p)
   {
+    if (sizeof(V) == 8) return 1;
     const double mean = p->ndof > 0 ? (double)p->nnz / (double)p->ndof : 1.0;
     for (int g = 2; g < 32; g *= 2)
       if (mean <= g * U) return g;
@@ -344,7 +353,7 @@ __device__ __forceinline__ bool last_block(uint32_t* ticket)
   return last;
 }
 
-template <typename V, int G, typename I>
+template <typename V, int G, int U, typename I>
 __global__ void __launch_bounds__(kSolveThreads) k_spmv(int64_t n, const int32_t* __restrict__ rp,
                                                         const I* __restrict__ ci, const V* __restrict__ val,
                                                         const V* __restrict__ x, V* __restrict__ y)
@@ -353,7 +362,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_spmv(int64_t n, const int32_t
   pdl_trigger();
   const int64_t groups = (int64_t)gridDim.x * (kSolveThreads / G);
   for (int64_t row = (blockIdx.x * (int64_t)kSolveThreads + threadIdx.x) / G; row < n; row += groups) {
-    const V s = row_dot<V, G, kSpmvEntries<V, G>, I>(row, rp, ci, val, x);
+    const V s = row_dot<V, G, U, I>(row, rp, ci, val, x);
     if ((threadIdx.x & (G - 1)) == 0) y[row] = s;
   }
 }
@@ -631,26 +640,31 @@ mg_status launch_spmv(mg_plan* p, int prec, const void* vals, const void* x, voi
   if (!vals || !x || !y) return set_error(MG_ERR_INVALID_ARG, "mg_spmv: null argument");
   MG_TRY(plan_device(p));
   if (prec_is_f64(prec)) {
-    // FP64: a CTA for every 256 / G rows, no grid-stride loop (measured on GB300 at
-    // P1 128^3: 84.7 us against 88.7 us with 8 CTAs per SM and a grid-stride loop)
+    // FP64: one thread per row, a CTA for every 256 rows, no grid-stride loop
+    // (measured on GB300 at P1 128^3: 84.7 us against 88.7 us with 8 CTAs per SM
+    // and a grid-stride loop)
     const int G = row_group<double>(p), nb = spmv_full_grid(p->ndof, G);
+    const double *v = (const double*)vals, *xx = (const double*)x;
+    double* yy = (double*)y;
+    const int32_t* rp = p->d_rowptr;
+    const int64_t n = p->ndof;
     if (p->d_coloff) {
-      MG_DISPATCH_G(G, (launch_pdl(k_spmv<double, g, int16_t>, nb, kSolveThreads, st, p->ndof,
-                                   (const int32_t*)p->d_rowptr, (const int16_t*)p->d_coloff, (const double*)vals,
-                                   (const double*)x, (double*)y)));
+      const int16_t* c = p->d_coloff;
+      if (G == 1) launch_pdl(k_spmv<double, 1, kF64Entries, int16_t>, nb, kSolveThreads, st, n, rp, c, v, xx, yy);
+      else launch_pdl(k_spmv<double, 2, 16, int16_t>, nb, kSolveThreads, st, n, rp, c, v, xx, yy);
     } else {
-      MG_DISPATCH_G(G, (launch_pdl(k_spmv<double, g, int32_t>, nb, kSolveThreads, st, p->ndof,
-                                   (const int32_t*)p->d_rowptr, (const int32_t*)p->d_colind, (const double*)vals,
-                                   (const double*)x, (double*)y)));
+      const int32_t* c = p->d_colind;
+      if (G == 1) launch_pdl(k_spmv<double, 1, kF64Entries, int32_t>, nb, kSolveThreads, st, n, rp, c, v, xx, yy);
+      else launch_pdl(k_spmv<double, 2, 16, int32_t>, nb, kSolveThreads, st, n, rp, c, v, xx, yy);
     }
   } else {
     const int G = row_group<float>(p), nb = row_blocks<float>(p, G);
     if (p->d_coloff) {
-      MG_DISPATCH_G(G, (launch_pdl(k_spmv<float, g, int16_t>, nb, kSolveThreads, st, p->ndof,
+      MG_DISPATCH_G(G, (launch_pdl(k_spmv<float, g, kEntriesPerLane<float>, int16_t>, nb, kSolveThreads, st, p->ndof,
                                    (const int32_t*)p->d_rowptr, (const int16_t*)p->d_coloff, (const float*)vals,
                                    (const float*)x, (float*)y)));
     } else {
-      MG_DISPATCH_G(G, (launch_pdl(k_spmv<float, g, int32_t>, nb, kSolveThreads, st, p->ndof,
+      MG_DISPATCH_G(G, (launch_pdl(k_spmv<float, g, kEntriesPerLane<float>, int32_t>, nb, kSolveThreads, st, p->ndof,
                                    (const int32_t*)p->d_rowptr, (const int32_t*)p->d_colind, (const float*)vals,
                                    (const float*)x, (float*)y)));
     }
@@ -666,8 +680,10 @@ mg_status launch_spmv_csr(int64_t rows, int64_t nnz, const int32_t* rowptr, cons
 {
   if (rows == 0) return MG_OK;
   const int G = row_group<double>(rows, nnz), nb = row_blocks(rows, G, 8);
-  MG_DISPATCH_G(G, (launch_pdl(k_spmv<double, g, int32_t>, nb, kSolveThreads, st, rows, rowptr, colind, vals, x,
-                               y)));
+  if (G == 1)
+    launch_pdl(k_spmv<double, 1, kF64Entries, int32_t>, nb, kSolveThreads, st, rows, rowptr, colind, vals, x, y);
+  else
+    launch_pdl(k_spmv<double, 2, 16, int32_t>, nb, kSolveThreads, st, rows, rowptr, colind, vals, x, y);
   MG_CUDA(cudaGetLastError());
   return MG_OK;
 }
