@@ -159,13 +159,13 @@ mg_status mg_mesh_export_geometry(const mg_mesh* mesh, double* h_xyz, int32_t* h
 /* Builds the CSR sparsity pattern (union of element couplings, explicit zeros
    kept, sorted columns) and the element order of the GPU assembly (a Morton
    curve of the element centroids).  The first GPU use of the plan uploads it
-   and builds the assembly's slot map on the device.
+   and builds the assembly's block map (P1) or slot map (P2) on the device.
    Replaces: the pattern half of traitsMatrixBuilder::buildEpetraCrs / numEntPerRow
    (src/morganaFiniteElements/traitsMatrixBuilder.hpp:363-544). */
 mg_status mg_pattern_build(mg_mesh* mesh, mg_plan** out);
 /* The same plan built on the GPU: the CSR pattern (element couplings as
    64-bit keys, radix-sorted and de-duplicated on the device), the element order
-   (Morton keys radix-sorted) and the slot map, identical to the host build's
+   (Morton keys radix-sorted) and the block / slot map, identical to the host build's
    arrays.  The plan is device-resident on return.  Needs a device; waits for
    its own work on `stream`.  Up to 2^31 element couplings (E nb^2), else
    MG_ERR_SIZE.
