@@ -202,23 +202,22 @@ mg_status ensure_edges(mg_mesh* m)
       inc_hi[pos] = std::max(a, b);
       inc_idx[pos] = 6 * e + j;
     }
-  // per bucket: unique his (sorted) and the first incidence of each
+  // per bucket: unique his (sorted) and the first incidence of each; a bucket
+  // holds any number of edges (a vertex may start hundreds)
   std::vector<int32_t> nuniq(N + 1, 0);
   std::vector<int32_t> local_rank(M);  // rank of the incidence's edge within its bucket
-#pragma omp parallel for schedule(dynamic, 4096)
-  for (int64_t v = 0; v < N; ++v) {
-    int32_t his[256];
-    int n = 0;
-    for (int64_t t = start[v]; t < start[v + 1]; ++t) {
-      int32_t h = inc_hi[t];
-      bool seen = false;
-      for (int u = 0; u < n; ++u) seen |= (his[u] == h);
-      if (!seen && n < 256) his[n++] = h;
+#pragma omp parallel
+  {
+    std::vector<int32_t> his;
+#pragma omp for schedule(dynamic, 4096)
+    for (int64_t v = 0; v < N; ++v) {
+      his.assign(inc_hi.begin() + start[v], inc_hi.begin() + start[v + 1]);
+      std::sort(his.begin(), his.end());
+      his.erase(std::unique(his.begin(), his.end()), his.end());
+      nuniq[v + 1] = (int32_t)his.size();
+      for (int64_t t = start[v]; t < start[v + 1]; ++t)
+        local_rank[t] = (int32_t)(std::lower_bound(his.begin(), his.end(), inc_hi[t]) - his.begin());
     }
-    std::sort(his, his + n);
-    nuniq[v + 1] = n;
-    for (int64_t t = start[v]; t < start[v + 1]; ++t)
-      local_rank[t] = (int32_t)(std::lower_bound(his, his + n, inc_hi[t]) - his);
   }
   for (int64_t v = 0; v < N; ++v) nuniq[v + 1] += nuniq[v];
   const int64_t nE = nuniq[N];

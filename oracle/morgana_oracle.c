@@ -500,17 +500,18 @@ int or_pattern(int order, int64_t ndof, int64_t n_elem, const int32_t *dofs, int
   memcpy(pos, cnt, sizeof(int64_t) * (size_t)(ndof + 1));
   int64_t *inc = (int64_t *)malloc(sizeof(int64_t) * (size_t)(n_elem * nb > 0 ? n_elem * nb : 1));
   for (int64_t k = 0; k < n_elem * nb; ++k) inc[pos[dofs[k]]++] = k / nb;
-  int32_t *tmp = (int32_t *)malloc(sizeof(int32_t) * 4096);
+  /* the row buffer holds the couplings of the row with the most incidences */
+  int64_t max_inc = 1;
+  for (int64_t r = 0; r < ndof; ++r)
+    if (cnt[r + 1] - cnt[r] > max_inc) max_inc = cnt[r + 1] - cnt[r];
+  int32_t *tmp = (int32_t *)malloc(sizeof(int32_t) * (size_t)(max_inc * nb));
   int64_t nnz = 0;
   rowptr[0] = 0;
   for (int64_t r = 0; r < ndof; ++r) {
     int64_t n = 0;
     for (int64_t t = cnt[r]; t < cnt[r + 1]; ++t) {
       int64_t e = inc[t];
-      for (int i = 0; i < nb; ++i) {
-        if (n >= 4096) { free(cnt); free(pos); free(inc); free(tmp); return OR_ERR_ARG; }
-        tmp[n++] = dofs[nb * e + i];
-      }
+      for (int i = 0; i < nb; ++i) tmp[n++] = dofs[nb * e + i];
     }
     qsort(tmp, (size_t)n, sizeof(int32_t), cmp_i32);
     for (int64_t t = 0; t < n; ++t) {

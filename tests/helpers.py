@@ -249,3 +249,38 @@ def emulate_block_map(bm, elem_order, local_mats, nnz, elems_per_block=None):
                     v += x
                 values[o[0]] = values[o[1]] = v
     return values
+
+
+def _oriented(xyz, conn):
+    """conn with each tet's last two vertices swapped where its determinant is negative."""
+    conn = np.array(conn, dtype=np.int32)
+    e = xyz[conn[:, 1:]] - xyz[conn[:, :1]]
+    neg = np.linalg.det(e) < 0
+    conn[neg, 2], conn[neg, 3] = conn[neg, 3].copy(), conn[neg, 2].copy()
+    return conn
+
+
+def star_mesh(n_points=700, seed=0):
+    """Tetrahedra joining a centre node to the hull triangles of points on a sphere
+    (all of them on the hull: 2 n_points - 4 elements): every element holds node 0
+    (one node of very high valence)."""
+    from scipy.spatial import ConvexHull
+    k = np.arange(n_points) + 0.5
+    phi = np.arccos(1 - 2 * k / n_points)
+    th = np.pi * (1 + 5 ** 0.5) * k
+    pts = np.stack([np.cos(th) * np.sin(phi), np.sin(th) * np.sin(phi), np.cos(phi)], axis=1)
+    pts = pts @ np.linalg.qr(np.random.default_rng(seed).normal(size=(3, 3)))[0]  # a seeded rotation
+    xyz = np.vstack([np.zeros((1, 3)), pts])
+    tris = ConvexHull(pts).simplices + 1
+    conn = np.hstack([np.zeros((len(tris), 1), dtype=np.int64), tris])
+    return xyz, _oriented(xyz, conn)
+
+
+def disjoint_tets(n_tets=1500, seed=0):
+    """Tetrahedra sharing no node: every CSR entry has one source."""
+    rng = np.random.default_rng(seed)
+    base = rng.uniform(0, 10, (n_tets, 1, 3))
+    ref = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], dtype=np.float64)
+    xyz = (base + ref[None] + 0.1 * rng.uniform(-1, 1, (n_tets, 4, 3))).reshape(-1, 3)
+    conn = np.arange(4 * n_tets).reshape(n_tets, 4)
+    return xyz, _oriented(xyz, conn)

@@ -9,7 +9,8 @@ import pytest
 import morganapublic_gb300 as mg
 import oracle as orc
 from morganapublic_gb300 import meshgen
-from helpers import emulate_block_map, emulate_slot_map, expected_block_map, expected_slot_map, row_scaled_err
+from helpers import (disjoint_tets, emulate_block_map, emulate_slot_map, expected_block_map, expected_slot_map,
+                     row_scaled_err, star_mesh)
 
 pytestmark = pytest.mark.gpu
 
@@ -706,6 +707,61 @@ def test_block_map_matches_restatement_and_oracle(n, jitter):
     assert not np.isnan(got).any()
     assert row_scaled_err(rp, ref, got) <= 1e-14
     v = b.assemble("stiff_kappa", coeff=kappa, quad=4, prec="f64").cpu().numpy()
+    assert row_scaled_err(rp, ref, v) <= F64_TOL
+
+
+@pytest.mark.parametrize("case", ["star", "disjoint"])
+def test_block_map_beyond_the_shared_memory_stage(case):
+    """Blocks whose map does not fit the assembly's shared-memory stage read the rest
+    from global memory: a node held by every element (star: a 512-source run, so one
+    group pads to 16384 sources, above the 6144 staged) and elements sharing no node
+    (disjoint: 160 groups of single-source runs per block, above the 96 group
+    offsets staged).  The map equals its restatement and the FP64 / FP32 values the
+    oracle's."""
+    xyz, conn = star_mesh(700, seed=3) if case == "star" else disjoint_tets(1500, seed=4)
+    kappa = meshgen.lognormal(len(conn), 1.0, 21)
+    mesh = mg.Mesh(xyz, conn, order=1)
+    b = mg.MatrixBuilder(mesh)
+    bm = b.export_block_map()
+    rp, ci = b.pattern()
+    exp = expected_block_map(bm["elem_order"], mesh.elem_dofs(), rp, ci, bm["info"].elems_per_block)
+    for k in ("bgrp", "goff", "src", "out", "sgoff", "sout"):
+        assert np.array_equal(bm[k], exp[k]), k
+    per_block_src = bm["goff"][bm["bgrp"][1:]] - bm["goff"][bm["bgrp"][:-1]]
+    per_block_groups = np.diff(bm["bgrp"])
+    if case == "star":
+        assert per_block_src.max() > 6144
+    else:
+        assert per_block_groups.max() > 96 and bm["info"].n_shared == 0
+    _, rpo, cio, ref = orc.full_operator("stiff_kappa", 1, 4, xyz, conn, coeff=kappa)
+    assert np.array_equal(rp, rpo) and np.array_equal(ci, cio)
+    v64 = b.assemble("stiff_kappa", coeff=kappa, quad=4, prec="f64").cpu().numpy()
+    b.status()
+    assert row_scaled_err(rp, ref, v64) <= F64_TOL
+    v32 = b.assemble("stiff_kappa", coeff=kappa, quad=4, prec="f32").cpu().numpy()
+    assert row_scaled_err(rp, ref, v32) <= F32_TOL
+    _, _, _, mref = orc.full_operator("mass", 1, 4, xyz, conn)
+    vm = b.assemble("mass", quad=4, prec="f64").cpu().numpy()
+    assert row_scaled_err(rp, mref, vm) <= F64_TOL
+
+
+@pytest.mark.parametrize("rule", ["lex", "first"])
+def test_high_valence_node_p2(rule):
+    """P2 on a star mesh (one vertex starts 700 edges): the edges enumerated on the
+    GPU equal the host's, and the assembled P2 operator the oracle's."""
+    xyz, conn = star_mesh(700, seed=3)
+    kappa = meshgen.lognormal(len(conn), 0.5, 22)
+    host = mg.Mesh(xyz, conn, order=2, edge_rule=rule)
+    dev = mg.Mesh(xyz, conn, order=2, edge_rule=rule, edges_on_device=True)
+    for a, b in zip(host.edges(), dev.edges()):
+        assert np.array_equal(a, b)
+    assert np.array_equal(host.elem_dofs(), dev.elem_dofs())
+    b = mg.MatrixBuilder(dev, pattern_on_device=True)
+    _, rp, ci, ref = orc.full_operator("stiff_kappa", 2, 15, xyz, conn, coeff=kappa, edge_rule=rule)
+    rph, cih = b.pattern()
+    assert np.array_equal(rph, rp) and np.array_equal(cih, ci)
+    v = b.assemble("stiff_kappa", coeff=kappa, quad=15, prec="f64").cpu().numpy()
+    b.status()
     assert row_scaled_err(rp, ref, v) <= F64_TOL
 
 

@@ -11,7 +11,7 @@ import pytest
 import morganapublic_gb300 as mg
 import oracle as orc
 from morganapublic_gb300 import meshgen
-from helpers import emulate_block_map, expected_block_map, morton_elem_order, row_scaled_err
+from helpers import emulate_block_map, expected_block_map, morton_elem_order, row_scaled_err, star_mesh
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = os.path.join(ROOT, "tests", "golden")
@@ -54,6 +54,27 @@ def test_numbering_and_pattern_match_oracle(order, rule, n, jitter, permute):
     rp, ci = builder.pattern()
     assert np.array_equal(rp, rp_o) and np.array_equal(ci, ci_o)
     assert abs(mesh.min_det - m.min_det) <= 1e-15 * abs(m.min_det) + 1e-300
+
+
+@pytest.mark.parametrize("order,rule", [(1, "lex"), (2, "lex"), (2, "first")])
+def test_high_valence_node_numbering_and_pattern(order, rule):
+    """A node that starts 700 edges (every tet of a star mesh holds it): edge table,
+    dof map and CSR pattern equal the oracle's -- no per-vertex or per-row limit."""
+    xyz, conn = star_mesh(700, seed=3)
+    mesh = mg.Mesh(xyz, conn, order=order, edge_rule=rule)
+    ee = None
+    ndof = len(xyz)
+    if order == 2:
+        en_o, ee = orc.edges(len(xyz), conn, rule)
+        en, ee_p = mesh.edges()
+        assert np.array_equal(en, en_o) and np.array_equal(ee_p, ee)
+        ndof += len(en_o)
+    dofs_o = orc.elem_dofs(order, len(xyz), conn, ee)
+    assert mesh.ndof == ndof and np.array_equal(mesh.elem_dofs(), dofs_o)
+    rp_o, ci_o = orc.pattern(order, ndof, dofs_o)
+    rp, ci = mg.MatrixBuilder(mesh).pattern()
+    assert np.array_equal(rp, rp_o) and np.array_equal(ci, ci_o)
+    assert np.diff(rp).max() == ndof  # the centre couples with every dof
 
 
 def test_pattern_sizes_of_survey_formulas():
