@@ -833,10 +833,17 @@ template <> __device__ __forceinline__ double partial_get<double>(const void* pp
 // copied with cp.async while the element matrices are computed.
 constexpr int kStageSrc = 6144;
 constexpr int kStageGroups = 96;
-template <typename T>
-constexpr size_t block_smem_bytes()
+// dynamic shared memory of a block: its element matrices (BE x NU entries, then
+// the zero of the padding sources), the staged sources and group offsets
+template <typename T, int BE, int NU>
+__host__ __device__ constexpr size_t block_em_bytes()
 {
-  return ((sizeof(T) * (kElemBlock * 10 + 1) + 15) / 16) * 16 + 2 * kStageSrc + 4 * (kStageGroups + 1);
+  return ((sizeof(T) * (BE * NU + 1) + 15) / 16) * 16;
+}
+template <typename T, int BE, int NU>
+__host__ __device__ constexpr size_t block_smem_bytes()
+{
+  return block_em_bytes<T, BE, NU>() + 2 * kStageSrc + 4 * (kStageGroups + 1);
 }
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem)
@@ -850,46 +857,33 @@ __device__ __forceinline__ void cp_async4(void* smem, const void* gmem)
                "l"(gmem));
 }
 
-// THREADS per CTA: 512 (one element each, two CTAs per SM) for the double-word
-// and FP64 arithmetic, 256 (two elements each, four CTAs per SM) for FP32 --
-// measured on GB300 at P1 128^3 (the double-word loop over two elements spills).
-template <int MODE, int THREADS>
-__global__ void __launch_bounds__(THREADS, 2048 / THREADS / 2)
-    k_block_asm(ElemArgs a, BlockArgs bm, typename Arith<MODE>::Out* __restrict__ values)
+// The block's map rows into shared memory with cp.async (waited for by the
+// caller's cp.async.wait_all): whole 16-byte chunks of its local sources (group
+// offsets are multiples of 32 sources, so the range is 64-byte aligned) and its
+// group offsets, each up to the stage's size.
+template <int THREADS>
+__device__ __forceinline__ void stage_block_map(const BlockArgs& bm, int32_t g0, int32_t g1, int32_t src0,
+                                                int32_t src1, uint16_t* s_src, int32_t* s_goff)
 {
-  using A = Arith<MODE>;
-  using T = typename A::T;
-  constexpr int NU = 10;
-  extern __shared__ __align__(16) unsigned char smem[];
-  T* em = reinterpret_cast<T*>(smem);  // the block's element matrices, then a zero (padding source)
-  uint16_t* s_src = reinterpret_cast<uint16_t*>(smem + ((sizeof(T) * (kElemBlock * NU + 1) + 15) / 16) * 16);
-  int32_t* s_goff = reinterpret_cast<int32_t*>(s_src + kStageSrc);
-  __shared__ T tab[7 * NU];
-  const int32_t g0 = bm.bgrp[blockIdx.x], g1 = bm.bgrp[blockIdx.x + 1];
-  const int32_t src0 = bm.bsrc0[blockIdx.x], src1 = bm.bsrc0[blockIdx.x + 1];
-  // the staged part: whole 16-byte chunks (group offsets are multiples of 32
-  // sources, so the range is 64-byte aligned)
   const int32_t n_src = min(src1 - src0, kStageSrc), n_goff = min(g1 - g0, kStageGroups) + 1;
   for (int i = threadIdx.x; i < n_src / 8; i += THREADS) cp_async16(s_src + 8 * i, bm.bsrc + src0 + 8 * i);
   for (int i = threadIdx.x; i < n_goff; i += THREADS) cp_async4(s_goff + i, bm.bgoff + g0 + i);
   asm volatile("cp.async.commit_group;\n" ::);
-  const int64_t p0 = (int64_t)blockIdx.x * kElemBlock;
-  const int64_t E = a.n_elem;
-  for (int i = threadIdx.x; i < 7 * NU; i += THREADS) tab[i] = A::from(a.tables[i]);
-  if (threadIdx.x == 0) em[kElemBlock * NU] = A::zero();
-  __syncthreads();
-#pragma unroll 1
-  for (int i = 0; i < kElemBlock / THREADS; ++i) {
-    const int lp = i * THREADS + threadIdx.x;
-    if (p0 + lp < E) {
-      T K[NU];
-      p1_element<MODE>(a, tab, elem_nodes(a, p0 + lp), elem_coef(a, p0 + lp), K);
-#pragma unroll
-      for (int u = 0; u < NU; ++u) em[lp * NU + u] = K[u];
-    }
-  }
-  asm volatile("cp.async.wait_all;\n" ::: "memory");
-  __syncthreads();
+}
+
+// Phase 2 of the block assembly: each warp takes groups of 32 of the block's
+// runs; lane l sums its run's sources from the element matrices em in shared
+// memory (4 at a time, ascending p) and writes a complete entry to its CSR
+// position and mirror, a shared entry's partial to its slot.  Rows past the
+// stage come from global memory.
+template <int MODE, int THREADS>
+__device__ __forceinline__ void block_sums(const BlockArgs& bm, int32_t g0, int32_t g1, int32_t src0,
+                                           const uint16_t* s_src, const int32_t* s_goff,
+                                           const typename Arith<MODE>::T* em,
+                                           typename Arith<MODE>::Out* __restrict__ values)
+{
+  using A = Arith<MODE>;
+  using T = typename A::T;
   const int lane = threadIdx.x & 31;
   for (int32_t g = g0 + (threadIdx.x >> 5); g < g1; g += THREADS / 32) {
     const int2 out = bm.bout[32 * g + lane];  // used after the sum: its latency overlaps it
@@ -934,6 +928,45 @@ __global__ void __launch_bounds__(THREADS, 2048 / THREADS / 2)
   }
 }
 
+// P1: one CTA per block of kElemBlock elements.  THREADS per CTA: 512 (one
+// element each, two CTAs per SM) for the double-word and FP64 arithmetic, 256
+// (two elements each, four CTAs per SM) for FP32 -- measured on GB300 at P1
+// 128^3 (the double-word loop over two elements spills).
+template <int MODE, int THREADS>
+__global__ void __launch_bounds__(THREADS, 2048 / THREADS / 2)
+    k_block_asm(ElemArgs a, BlockArgs bm, typename Arith<MODE>::Out* __restrict__ values)
+{
+  using A = Arith<MODE>;
+  using T = typename A::T;
+  constexpr int NU = 10;
+  extern __shared__ __align__(16) unsigned char smem[];
+  T* em = reinterpret_cast<T*>(smem);  // the block's element matrices, then a zero (padding source)
+  uint16_t* s_src = reinterpret_cast<uint16_t*>(smem + block_em_bytes<T, kElemBlock, NU>());
+  int32_t* s_goff = reinterpret_cast<int32_t*>(s_src + kStageSrc);
+  __shared__ T tab[7 * NU];
+  const int32_t g0 = bm.bgrp[blockIdx.x], g1 = bm.bgrp[blockIdx.x + 1];
+  const int32_t src0 = bm.bsrc0[blockIdx.x], src1 = bm.bsrc0[blockIdx.x + 1];
+  stage_block_map<THREADS>(bm, g0, g1, src0, src1, s_src, s_goff);
+  const int64_t p0 = (int64_t)blockIdx.x * kElemBlock;
+  const int64_t E = a.n_elem;
+  for (int i = threadIdx.x; i < 7 * NU; i += THREADS) tab[i] = A::from(a.tables[i]);
+  if (threadIdx.x == 0) em[kElemBlock * NU] = A::zero();
+  __syncthreads();
+#pragma unroll 1
+  for (int i = 0; i < kElemBlock / THREADS; ++i) {
+    const int lp = i * THREADS + threadIdx.x;
+    if (p0 + lp < E) {
+      T K[NU];
+      p1_element<MODE>(a, tab, elem_nodes(a, p0 + lp), elem_coef(a, p0 + lp), K);
+#pragma unroll
+      for (int u = 0; u < NU; ++u) em[lp * NU + u] = K[u];
+    }
+  }
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+  __syncthreads();
+  block_sums<MODE, THREADS>(bm, g0, g1, src0, s_src, s_goff, em, values);
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(256) k_shared_sum(int64_t n_groups, const int32_t* __restrict__ sgoff,
                                                     const int2* __restrict__ sout, const void* __restrict__ partial,
@@ -963,24 +996,33 @@ __global__ void __launch_bounds__(256) k_shared_sum(int64_t n_groups, const int3
   }
 }
 
+// Sets the dynamic shared-memory limit of a kernel once per device (the first
+// assembly of each kind on a device).
+template <typename K>
+static mg_status allow_smem(K kernel, size_t bytes, std::once_flag (&once)[64])
+{
+  int dev = 0;
+  MG_CUDA(cudaGetDevice(&dev));
+  cudaError_t err = cudaSuccess;
+  std::call_once(once[dev & 63],
+                 [&] { err = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes); });
+  MG_CUDA(err);
+  return MG_OK;
+}
+
 template <int MODE>
 static mg_status launch_block_t(mg_plan* p, const ElemArgs& a, void* d_values, cudaStream_t st)
 {
   using Out = typename Arith<MODE>::Out;
+  using T = typename Arith<MODE>::T;
   const BlockArgs bm{p->d_bgrp, p->d_bsrc0, p->d_bgoff, p->d_bsrc, p->d_bout, p->d_partial};
-  constexpr size_t smem = block_smem_bytes<typename Arith<MODE>::T>();
-  constexpr int threads = MODE == kF32 ? 256 : 512;
-  static std::once_flag attr_once[64];
-  int dev = 0;
-  MG_CUDA(cudaGetDevice(&dev));
-  cudaError_t attr_err = cudaSuccess;
-  std::call_once(attr_once[dev & 63], [&] {
-    attr_err =
-        cudaFuncSetAttribute(k_block_asm<MODE, threads>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  });
-  MG_CUDA(attr_err);
-  if (a.n_elem > 0)
+  static std::once_flag once[64];
+  if (a.n_elem > 0) {
+    constexpr size_t smem = block_smem_bytes<T, kElemBlock, 10>();
+    constexpr int threads = MODE == kF32 ? 256 : 512;
+    MG_TRY(allow_smem(k_block_asm<MODE, threads>, smem, once));
     k_block_asm<MODE, threads><<<(unsigned)p->n_blocks, threads, smem, st>>>(a, bm, static_cast<Out*>(d_values));
+  }
   MG_CUDA(cudaGetLastError());
   if (p->n_sgroups > 0)
     k_shared_sum<MODE><<<(unsigned)((p->n_sgroups + 7) / 8), 256, 0, st>>>(p->n_sgroups, p->d_sgoff, p->d_sout,
@@ -1041,7 +1083,7 @@ static mg_status launch_assemble_gather(mg_plan* p, int op, const double* d_coef
   a.stiff = (op == MG_OP_STIFF_KAPPA || op == MG_OP_STIFF_CONST);
   a.em = p->d_em;
   a.flags = p->d_counters + 4;
-  if (m->order == 1) {
+  if (uses_block_map(m->order)) {
     if (prec == MG_F32) return launch_block_t<kF32>(p, a, d_values, st);
     return prec == MG_F64_NATIVE ? launch_block_t<kF64>(p, a, d_values, st) : launch_block_t<kDW>(p, a, d_values, st);
   }

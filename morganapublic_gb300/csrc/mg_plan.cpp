@@ -447,7 +447,7 @@ mg_status mg_plan_block_map_info(mg_plan* p, mg_block_map_info* info)
   info->n_partial = p->n_partial;
   info->n_elem = p->mesh->n_elem;
   info->nunique = nunique(p->mesh->order);
-  info->elems_per_block = kElemBlock;
+  info->elems_per_block = elems_per_block(p->mesh->order);
   return MG_OK;
 }
 

@@ -329,10 +329,10 @@ __global__ void k_group_fill(int64_t G, int64_t U, const uint32_t* __restrict__ 
 // block; an entry with one run is complete, else shared, its runs numbered j in
 // ascending block.  An entry without sources (not produced by a mesh's pattern)
 // counts as one empty run of block 0, so that its value is written (zero).
-__device__ __forceinline__ int32_t block_of(uint32_t s, int nu) { return (int32_t)(s / (uint32_t)nu / kElemBlock); }
+__device__ __forceinline__ int32_t block_of(uint32_t s, int nu, int be) { return (int32_t)(s / (uint32_t)nu / be); }
 
-__global__ void k_run_count(int64_t U, int nu, const int32_t* __restrict__ useg, const uint32_t* __restrict__ src,
-                            int32_t* __restrict__ nrun, int32_t* __restrict__ shared)
+__global__ void k_run_count(int64_t U, int nu, int be, const int32_t* __restrict__ useg,
+                            const uint32_t* __restrict__ src, int32_t* __restrict__ nrun, int32_t* __restrict__ shared)
 {
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t > U) return;
@@ -343,7 +343,7 @@ __global__ void k_run_count(int64_t U, int nu, const int32_t* __restrict__ useg,
   }
   int32_t n = 0, prev = -1;
   for (int32_t k = useg[t]; k < useg[t + 1]; ++k) {
-    const int32_t b = block_of(src[k], nu);
+    const int32_t b = block_of(src[k], nu, be);
     if (b != prev) ++n, prev = b;
   }
   n = max(n, 1);
@@ -359,7 +359,8 @@ __device__ __forceinline__ uint32_t run_key(int32_t b, int32_t len)
   return 64u * (uint32_t)b + 63u - (uint32_t)min(len, 63);
 }
 
-__global__ void k_run_emit(int64_t U, int nu, const int32_t* __restrict__ useg, const uint32_t* __restrict__ src,
+__global__ void k_run_emit(int64_t U, int nu, int be, const int32_t* __restrict__ useg,
+                           const uint32_t* __restrict__ src,
                            const int32_t* __restrict__ rfirst, uint32_t* __restrict__ rkey, uint32_t* __restrict__ rid,
                            int32_t* __restrict__ rt, int32_t* __restrict__ rj, int32_t* __restrict__ rstart,
                            int32_t* __restrict__ rlen)
@@ -373,9 +374,9 @@ __global__ void k_run_emit(int64_t U, int nu, const int32_t* __restrict__ useg, 
     return;
   }
   for (int32_t k = k0; k < k1;) {
-    const int32_t b = block_of(src[k], nu);
+    const int32_t b = block_of(src[k], nu, be);
     int32_t e = k + 1;
-    while (e < k1 && block_of(src[e], nu) == b) ++e;
+    while (e < k1 && block_of(src[e], nu, be) == b) ++e;
     rkey[ri] = run_key(b, e - k);
     rid[ri] = (uint32_t)ri;
     rt[ri] = (int32_t)t;
@@ -464,7 +465,7 @@ __global__ void k_sgroup_out(int64_t G3, int64_t S, const int32_t* __restrict__ 
 }
 
 // one thread per (group, lane): the run's local sources [j][lane] and its output
-__global__ void k_bfill(int64_t G, int nu, const int32_t* __restrict__ grun0, const int32_t* __restrict__ gcnt,
+__global__ void k_bfill(int64_t G, int nu, int be, const int32_t* __restrict__ grun0, const int32_t* __restrict__ gcnt,
                         const uint32_t* __restrict__ perm, const uint32_t* __restrict__ skey,
                         const int32_t* __restrict__ rt, const int32_t* __restrict__ rj,
                         const int32_t* __restrict__ rstart, const int32_t* __restrict__ rlen,
@@ -478,7 +479,7 @@ __global__ void k_bfill(int64_t G, int nu, const int32_t* __restrict__ grun0, co
   const int64_t g = i >> 5;
   const int lane = (int)(i & 31);
   const int32_t o = bgoff[g], L = (bgoff[g + 1] - o) >> 5;
-  const uint16_t pad = (uint16_t)(kElemBlock * nu);
+  const uint16_t pad = (uint16_t)(be * nu);
   if (lane >= gcnt[g]) {
     bout[i] = make_int2(kNoOutput, 0);
     for (int32_t j = 0; j < L; ++j) bsrc[o + 32 * j + lane] = pad;
@@ -486,7 +487,7 @@ __global__ void k_bfill(int64_t G, int nu, const int32_t* __restrict__ grun0, co
   }
   const int32_t sr = grun0[g] + lane;
   const uint32_t ri = perm[sr];
-  const uint32_t base = (skey[sr] >> 6) * (uint32_t)kElemBlock * (uint32_t)nu;
+  const uint32_t base = (skey[sr] >> 6) * (uint32_t)be * (uint32_t)nu;
   const int32_t t = rt[ri], k0 = rstart[ri], len = rlen[ri];
   for (int32_t j = 0; j < L; ++j) bsrc[o + 32 * j + lane] = j < len ? (uint16_t)(src[k0 + j] - base) : pad;
   if (nrun[t] == 1) {
@@ -690,9 +691,10 @@ mg_status build_slot_map(mg_plan* p, cudaStream_t st)
 mg_status build_block_map(mg_plan* p, int64_t U, const int32_t* useg, const int32_t* uslot, const int32_t* umirror,
                           const uint32_t* src, cudaStream_t st)
 {
-  const int nu = nunique(p->mesh->order);
+  const int nu = nunique(p->mesh->order), be = elems_per_block(p->mesh->order);
+  if (be * nu >= UINT16_MAX) return set_error(MG_ERR_SIZE, "block map: a block's entries above 16 bits");
   const int64_t E = p->mesh->n_elem;
-  const int64_t nblk = std::max<int64_t>(1, (E + kElemBlock - 1) / kElemBlock);
+  const int64_t nblk = std::max<int64_t>(1, (E + be - 1) / be);
   const int64_t nseg = nblk;
   if (64 * nblk >= UINT32_MAX / 2) return set_error(MG_ERR_SIZE, "block map: too many element blocks");
   SchedBuffers B;
@@ -701,7 +703,7 @@ mg_status build_block_map(mg_plan* p, int64_t U, const int32_t* useg, const int3
   MG_TRY(B.alloc(&shared, U + 1));
   MG_TRY(B.alloc(&rfirst, U + 1));
   MG_TRY(B.alloc(&sidx, U + 1));
-  k_run_count<<<grid_of(U + 1), 256, 0, st>>>(U, nu, useg, src, nrun, shared);
+  k_run_count<<<grid_of(U + 1), 256, 0, st>>>(U, nu, be, useg, src, nrun, shared);
   MG_CUDA(cudaGetLastError());
   MG_TRY(exclusive_scan(B, nrun, rfirst, U + 1, st));
   MG_TRY(exclusive_scan(B, shared, sidx, U + 1, st));
@@ -720,7 +722,7 @@ mg_status build_block_map(mg_plan* p, int64_t U, const int32_t* useg, const int3
   MG_TRY(B.alloc(&rstart, R));
   MG_TRY(B.alloc(&rlen, R));
   if (U > 0)
-    k_run_emit<<<grid_of(U), 256, 0, st>>>(U, nu, useg, src, rfirst, rkey, rid, rt, rj, rstart, rlen);
+    k_run_emit<<<grid_of(U), 256, 0, st>>>(U, nu, be, useg, src, rfirst, rkey, rid, rt, rj, rstart, rlen);
   int kbits = 1;
   while ((1ll << kbits) <= 64 * nblk) ++kbits;
   size_t tb = 0;
@@ -785,7 +787,7 @@ mg_status build_block_map(mg_plan* p, int64_t U, const int32_t* useg, const int3
   MG_TRY(B.alloc(reinterpret_cast<double**>(&partial), Q));
   MG_CUDA(cudaMemsetAsync(partial, 0, sizeof(double) * (size_t)std::max<int64_t>(Q, 1), st));
   if (G > 0)
-    k_bfill<<<grid_of(32 * (int64_t)G), 256, 0, st>>>(G, nu, grun0, gcnt, perm, skey, rt, rj, rstart, rlen, src, uslot,
+    k_bfill<<<grid_of(32 * (int64_t)G), 256, 0, st>>>(G, nu, be, grun0, gcnt, perm, skey, rt, rj, rstart, rlen, src, uslot,
                                                       umirror, nrun, srank, sgoff, bgoff, bsrc, bout);
   k_bgrp<<<grid_of(nblk + 1), 256, 0, st>>>(nblk, seg_g, bgoff, bgrp, bsrc0);
   MG_CUDA(cudaGetLastError());
