@@ -891,7 +891,7 @@ def main():
                               "SpMV in native FP64; assembly_f64_native gives the native-FP64 assembly",
                 "data": "synthetic (seeded Kuhn cube, jitter, element permutation, lognormal kappa)",
                 "config": workload_config(a, E, N, nnz), "roofline": roofline, "cpu_baseline": cpu_base,
-                "e2e": e2e, "e2e_cold": e2e_cold, "gpu_launches": a.steps * (2 + N_SPMV),  # coefficient gather + assembly + SpMVs
+                "e2e": e2e, "e2e_cold": e2e_cold, "gpu_launches": a.steps * (2 + N_SPMV),  # block assembly + shared sums + SpMVs
                 "clocks": clocks, "wall_s_timed": t_wall, "kernels": extras}
     if world > 1:
         dist.barrier()

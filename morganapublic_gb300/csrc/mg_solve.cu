@@ -108,10 +108,14 @@ template <typename V> constexpr int kEntriesPerLane = sizeof(V) == 8 ? 16 : 8;
 // the passes its longest row needs.  The FP64 kernels therefore prefer one
 // thread per row (no shuffle-adds) with 15 entries per pass: interior P1 rows
 // have 15 entries, one pass; P2 rows (19, 27 and 65 entries) take 2, 2 and 5.
-// The standalone SpMV keeps two lanes of 16 entries for rows above 16 entries
-// on average: there the single-lane loads cost more L1 throughput than the FMAs
-// they save (measured on GB300 at P2 48^3: 101 us against 99 us).
+// The standalone SpMV keeps two lanes per row for rows above 16 entries on
+// average: there single-lane loads cost more L1 throughput than the FMAs they
+// save (measured on GB300 at P2 48^3: 101 us against 99 us with two lanes of
+// 16).  Two lanes of 14 (28 entries per pass: P2 rows of 19 and 27 in one pass,
+// 65 in three; ~1.38 FMA slots per entry against ~1.56 with 16) measured 90.8
+// against 99.0 us there.
 constexpr int kF64Entries = 15;
+constexpr int kF64PairEntries = 14;
 
 // Lanes per row of the standalone SpMV: FP64 one up to 16 entries on average
 // (P1), two above (P2); FP32 the smallest group of at least 2 lanes whose pass
@@ -651,11 +655,11 @@ mg_status launch_spmv(mg_plan* p, int prec, const void* vals, const void* x, voi
     if (p->d_coloff) {
       const int16_t* c = p->d_coloff;
       if (G == 1) launch_pdl(k_spmv<double, 1, kF64Entries, int16_t>, nb, kSolveThreads, st, n, rp, c, v, xx, yy);
-      else launch_pdl(k_spmv<double, 2, 16, int16_t>, nb, kSolveThreads, st, n, rp, c, v, xx, yy);
+      else launch_pdl(k_spmv<double, 2, kF64PairEntries, int16_t>, nb, kSolveThreads, st, n, rp, c, v, xx, yy);
     } else {
       const int32_t* c = p->d_colind;
       if (G == 1) launch_pdl(k_spmv<double, 1, kF64Entries, int32_t>, nb, kSolveThreads, st, n, rp, c, v, xx, yy);
-      else launch_pdl(k_spmv<double, 2, 16, int32_t>, nb, kSolveThreads, st, n, rp, c, v, xx, yy);
+      else launch_pdl(k_spmv<double, 2, kF64PairEntries, int32_t>, nb, kSolveThreads, st, n, rp, c, v, xx, yy);
     }
   } else {
     const int G = row_group<float>(p), nb = row_blocks<float>(p, G);
@@ -683,7 +687,8 @@ mg_status launch_spmv_csr(int64_t rows, int64_t nnz, const int32_t* rowptr, cons
   if (G == 1)
     launch_pdl(k_spmv<double, 1, kF64Entries, int32_t>, nb, kSolveThreads, st, rows, rowptr, colind, vals, x, y);
   else
-    launch_pdl(k_spmv<double, 2, 16, int32_t>, nb, kSolveThreads, st, rows, rowptr, colind, vals, x, y);
+    launch_pdl(k_spmv<double, 2, kF64PairEntries, int32_t>, nb, kSolveThreads, st, rows, rowptr, colind, vals, x,
+               y);
   MG_CUDA(cudaGetLastError());
   return MG_OK;
 }
