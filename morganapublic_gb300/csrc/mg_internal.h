@@ -79,7 +79,7 @@ struct mg_mesh {
   std::vector<int32_t> conn;        // n_elem * 4
   std::vector<int32_t> elem_edge;   // n_elem * 6 (when built)
   std::vector<int32_t> edge_nodes;  // n_edges * 2 (when built)
-  std::vector<int32_t> dofs;        // n_elem * nb
+  std::vector<int32_t> dofs;        // n_elem * nb (P2; P1 reads conn: mesh_dofs)
   std::vector<int32_t> tri_nodes;   // Gmsh ingest: boundary triangles (3 node ids each), file order
   std::vector<int32_t> tri_geo;     //   and their geoIds (2nd tag)
   // device copies
@@ -219,6 +219,8 @@ struct mg_lagrange {
 };
 
 namespace mg {
+// The element -> dof table, n_elem x nb: the connectivity itself for P1.
+inline const int32_t* mesh_dofs(const mg_mesh* m) { return m->order == 1 ? m->conn.data() : m->dofs.data(); }
 // MG_OK when `want` is the calling thread's current device, else
 // MG_ERR_INVALID_ARG naming both: a handle's device arrays are only valid on
 // the device they were uploaded to

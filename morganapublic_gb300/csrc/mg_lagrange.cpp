@@ -267,7 +267,7 @@ void build_b(mg_lagrange* lg, const mg_mesh* m, const std::vector<int64_t>& rank
       }
       for (int i = 0; i < nb; ++i) {
         const int64_t s = (f * nt + a) * nb + i;
-        pairs[s] = Pair{row << 32 | (uint64_t)(uint32_t)m->dofs[e * nb + i], (int32_t)s};
+        pairs[s] = Pair{row << 32 | (uint64_t)(uint32_t)mesh_dofs(m)[e * nb + i], (int32_t)s};
       }
     }
   }

@@ -275,6 +275,7 @@ mg_status mesh_device(mg_mesh* m)
   std::vector<double4_32a> x64(N);
   std::vector<float4> rec(2 * N);
   std::vector<float> loz(N);
+#pragma omp parallel for
   for (int64_t i = 0; i < N; ++i) {
     double c[3] = {m->xyz[3 * i], m->xyz[3 * i + 1], m->xyz[3 * i + 2]};
     float h[3], md[3], l[3];
@@ -298,7 +299,10 @@ mg_status mesh_device(mg_mesh* m)
   MG_CUDA(cudaMemcpy(m->d_node_rec, rec.data(), 2 * sizeof(float4) * N, cudaMemcpyHostToDevice));
   MG_CUDA(cudaMemcpy(m->d_lo_z, loz.data(), sizeof(float) * N, cudaMemcpyHostToDevice));
   MG_CUDA(cudaMemcpy(m->d_conn, m->conn.data(), sizeof(int4) * E, cudaMemcpyHostToDevice));
-  MG_CUDA(cudaMemcpy(m->d_dofs, m->dofs.data(), sizeof(int32_t) * E * m->nb, cudaMemcpyHostToDevice));
+  if (m->order == 1)  // P1 dofs = the connectivity, already on the device
+    MG_CUDA(cudaMemcpy(m->d_dofs, m->d_conn, sizeof(int32_t) * E * 4, cudaMemcpyDeviceToDevice));
+  else
+    MG_CUDA(cudaMemcpy(m->d_dofs, m->dofs.data(), sizeof(int32_t) * E * m->nb, cudaMemcpyHostToDevice));
   m->on_device = true;
   return MG_OK;
 }
@@ -317,22 +321,42 @@ static void free_mesh(mg_mesh* m)
 static mg_status finish_mesh(mg_mesh* m)
 {
   const int64_t N = m->n_nodes, E = m->n_elem;
-  // node ids in range, distinct within a tet
-  for (int64_t e = 0; e < E; ++e) {
+  // node ids in range, distinct within a tet (checked in parallel; the first
+  // offending element is then found in order, for the message)
+  auto elem_ok = [&](int64_t e) {
     const int32_t* c = &m->conn[4 * e];
     for (int s = 0; s < 4; ++s) {
-      if (c[s] < 0 || c[s] >= N)
-        return set_error(MG_ERR_BAD_MESH, "element " + std::to_string(e) + " has node id " +
-                                              std::to_string(c[s]) + " outside [0, n_nodes)");
+      if (c[s] < 0 || c[s] >= N) return false;
       for (int t = 0; t < s; ++t)
-        if (c[s] == c[t])
-          return set_error(MG_ERR_BAD_MESH, "element " + std::to_string(e) + " repeats a node");
+        if (c[s] == c[t]) return false;
     }
-  }
+    return true;
+  };
+  int ids_bad = 0;
+#pragma omp parallel for reduction(max : ids_bad)
+  for (int64_t e = 0; e < E; ++e)
+    if (!elem_ok(e)) ids_bad = 1;
+  if (ids_bad)
+    for (int64_t e = 0; e < E; ++e) {
+      const int32_t* c = &m->conn[4 * e];
+      for (int s = 0; s < 4; ++s) {
+        if (c[s] < 0 || c[s] >= N)
+          return set_error(MG_ERR_BAD_MESH, "element " + std::to_string(e) + " has node id " +
+                                                std::to_string(c[s]) + " outside [0, n_nodes)");
+        for (int t = 0; t < s; ++t)
+          if (c[s] == c[t])
+            return set_error(MG_ERR_BAD_MESH, "element " + std::to_string(e) + " repeats a node");
+      }
+    }
   // finite coordinates (a NaN would also slip through the minimum below)
+  int nonfinite = 0;
+#pragma omp parallel for reduction(max : nonfinite)
   for (int64_t i = 0; i < 3 * N; ++i)
-    if (!std::isfinite(m->xyz[i]))
-      return set_error(MG_ERR_BAD_MESH, "node " + std::to_string(i / 3) + " has a non-finite coordinate");
+    if (!std::isfinite(m->xyz[i])) nonfinite = 1;
+  if (nonfinite)
+    for (int64_t i = 0; i < 3 * N; ++i)
+      if (!std::isfinite(m->xyz[i]))
+        return set_error(MG_ERR_BAD_MESH, "node " + std::to_string(i / 3) + " has a non-finite coordinate");
   // Jacobian check: the map is affine, so detJ is the same at every vertex.
   double mn = INFINITY;
   int64_t bad = -1;
@@ -369,11 +393,13 @@ static mg_status finish_mesh(mg_mesh* m)
   if (m->order == 2)
     MG_TRY(m->edges_on_device ? build_edges_device(m, (cudaStream_t)m->edge_stream) : ensure_edges(m));
   m->ndof = m->order == 1 ? N : N + m->n_edges;
-  m->dofs.resize(E * m->nb);
-  for (int64_t e = 0; e < E; ++e) {
-    for (int v = 0; v < 4; ++v) m->dofs[m->nb * e + v] = m->conn[4 * e + v];
-    if (m->order == 2)
+  if (m->order == 2) {  // P1: the dofs are the vertices (mesh_dofs reads conn)
+    m->dofs.resize(E * m->nb);
+#pragma omp parallel for
+    for (int64_t e = 0; e < E; ++e) {
+      for (int v = 0; v < 4; ++v) m->dofs[m->nb * e + v] = m->conn[4 * e + v];
       for (int j = 0; j < 6; ++j) m->dofs[m->nb * e + 4 + j] = (int32_t)(N + m->elem_edge[6 * e + j]);
+    }
   }
   if (m->ndof >= INT32_MAX) return set_error(MG_ERR_SIZE, "more than 2^31-1 dofs");
   return MG_OK;
@@ -382,6 +408,17 @@ static mg_status finish_mesh(mg_mesh* m)
 }  // namespace mg
 
 using namespace mg;
+
+// dst = src[0 .. n), copied in chunks over the host threads
+template <typename T>
+static void parallel_copy(std::vector<T>& dst, const T* src, int64_t n)
+{
+  dst.resize(n);
+  const int64_t chunk = 1 << 20;
+#pragma omp parallel for schedule(static)
+  for (int64_t c = 0; c < (n + chunk - 1) / chunk; ++c)
+    std::memcpy(dst.data() + c * chunk, src + c * chunk, sizeof(T) * (size_t)std::min(chunk, n - c * chunk));
+}
 
 extern "C" {
 
@@ -405,8 +442,8 @@ static mg_status create_mesh(mg_mesh** out, int64_t n_nodes, const double* h_xyz
   m->nb = nbasis(order);
   m->n_nodes = n_nodes;
   m->n_elem = n_elements;
-  m->xyz.assign(h_xyz, h_xyz + 3 * n_nodes);
-  m->conn.assign(h_conn, h_conn + 4 * n_elements);
+  parallel_copy(m->xyz, h_xyz, 3 * n_nodes);
+  parallel_copy(m->conn, h_conn, 4 * n_elements);
   mg_status s = finish_mesh(m);
   if (s != MG_OK) {
     free_mesh(m);
@@ -519,7 +556,7 @@ mg_status mg_mesh_get_info(const mg_mesh* m, mg_mesh_info* info)
 mg_status mg_mesh_export_dofs(const mg_mesh* m, int32_t* h_elem_dofs)
 {
   if (!m || !h_elem_dofs) return set_error(MG_ERR_INVALID_ARG, "mg_mesh_export_dofs: null argument");
-  std::memcpy(h_elem_dofs, m->dofs.data(), sizeof(int32_t) * m->dofs.size());
+  std::memcpy(h_elem_dofs, mesh_dofs(m), sizeof(int32_t) * (size_t)(m->n_elem * m->nb));
   return MG_OK;
 }
 

@@ -39,13 +39,14 @@ static mg_status build_pattern(mg_plan* p)
   mg_mesh* m = p->mesh;
   const int nb = m->nb;
   const int64_t E = m->n_elem, nd = m->ndof;
+  const int32_t* dofs = mesh_dofs(m);
   // dof -> incident elements (the order inside a row does not matter: the
   // row's columns are de-duplicated and sorted below)
   std::vector<int64_t> start(nd + 1, 0);
 #pragma omp parallel for
   for (int64_t k = 0; k < E * nb; ++k) {
 #pragma omp atomic
-    start[m->dofs[k] + 1]++;
+    start[dofs[k] + 1]++;
   }
   for (int64_t r = 0; r < nd; ++r) start[r + 1] += start[r];
   std::vector<int64_t> fill(start.begin(), start.end() - 1);
@@ -54,7 +55,7 @@ static mg_status build_pattern(mg_plan* p)
   for (int64_t k = 0; k < E * nb; ++k) {
     int64_t slot;
 #pragma omp atomic capture
-    slot = fill[m->dofs[k]]++;
+    slot = fill[dofs[k]]++;
     inc[slot] = (int32_t)(k / nb);
   }
   // one pass over the rows: the union of the incident elements' dofs,
@@ -76,7 +77,7 @@ static mg_status build_pattern(mg_plan* p)
       tmp.clear();
       for (int64_t k = start[r]; k < start[r + 1]; ++k)
         for (int i = 0; i < nb; ++i) {
-          const int32_t c = m->dofs[(int64_t)inc[k] * nb + i];
+          const int32_t c = dofs[(int64_t)inc[k] * nb + i];
           if (stamp[c] != (int32_t)r) {
             stamp[c] = (int32_t)r;
             tmp.push_back(c);
@@ -179,7 +180,7 @@ mg_status plan_device(mg_plan* p)
     std::vector<int32_t> dm((size_t)E * nb);
 #pragma omp parallel for
     for (int64_t i = 0; i < E; ++i)
-      for (int k = 0; k < nb; ++k) dm[i * nb + k] = p->mesh->dofs[(int64_t)p->h_elem_order[i] * nb + k];
+      for (int k = 0; k < nb; ++k) dm[i * nb + k] = mesh_dofs(p->mesh)[(int64_t)p->h_elem_order[i] * nb + k];
     MG_TRY(upload(&p->d_elem_order, p->h_elem_order));
     MG_TRY(upload(&p->d_dofs_morton, dm));
   }
@@ -268,7 +269,7 @@ mg_status plan_rhs_map(mg_plan* p)
   if (pairs >= INT32_MAX) return set_error(MG_ERR_SIZE, "load-vector map above 2^31 element-vector entries");
   if ((int64_t)p->h_elem_order.size() != E) return set_error(MG_ERR_INVALID_ARG, "plan without an element order");
   const int32_t* eo = p->h_elem_order.data();
-  const int32_t* dofs = m->dofs.data();
+  const int32_t* dofs = mesh_dofs(m);
   auto dof_of = [&](int64_t q) { return dofs[(int64_t)eo[q / nb] * nb + q % nb]; };
   std::vector<int32_t> ptr(nd + 1, 0), slot(std::max<int64_t>(pairs, 1));
 #pragma omp parallel for
