@@ -107,8 +107,8 @@ struct mg_plan {
   int32_t* d_elem_order = nullptr;  // elements along a Morton curve of their centroids
   int32_t* d_dofs_morton = nullptr; // their dofs (nb each) in that order
   uint32_t* d_counters = nullptr;   // [4]: assembly flags (bit 0 NaN / Inf coefficient, bit 1 double-word range)
-  // slot map of the gather assembly (built with the plan's device state; see
-  // build_slot_map): the diagonal and upper CSR entries in groups of 32 (one per
+  // slot map of the two-pass (P2) gather assembly (built with the plan's device
+  // state; see build_slot_map): the diagonal and upper CSR entries in groups of 32 (one per
   // warp; per block of kGatherRowBlock rows the diagonal entries first), entry t
   // written to uslot[t] and umirror[t];
   // group g's sources src[goff[g] + 32 j + lane], j < (goff[g+1] - goff[g]) / 32,
@@ -118,7 +118,7 @@ struct mg_plan {
   int32_t* d_umirror = nullptr;     // n_upper
   uint32_t* d_src = nullptr;        // n_src
   int64_t n_upper = 0, n_groups = 0, n_diag = 0, n_slot_contrib = 0, n_src = 0;
-  void* d_em = nullptr;             // element matrices, nunique x n_elem entries (up to 8 bytes each)
+  void* d_em = nullptr;             // P2 element matrices, nunique x n_elem entries (up to 8 bytes each)
   // block map of the one-pass P1 assembly (build_block_map): elements in blocks
   // of kElemBlock consecutive Morton positions, one CTA each.  Block b's local
   // entries (the runs of an upper entry's sources that fall in the block, longest
@@ -234,10 +234,12 @@ mg_status plan_rhs_map(mg_plan* p);  // the load-vector slot map (once per plan)
 // the plan's d_rowptr / d_colind
 mg_status build_pattern_device(mg_plan* p, cudaStream_t st, bool keep_device);
 // the plan's device state from its device pattern (mg_schedule.cu): the same
-// arrays plan_device makes for a host-built plan, slot map included (on_device)
+// arrays plan_device makes for a host-built plan, the assembly's map included
+// (on_device)
 mg_status build_plan_device(mg_plan* p, cudaStream_t st);
-// the slot map of the gather assembly from the plan's device pattern and Morton
-// dofs (mg_schedule.cu); once per plan
+// the assembly's map from the plan's device pattern and Morton dofs
+// (mg_schedule.cu), once per plan: the per-entry source lists, laid out as the
+// block map (P1) or the gather's slot map (P2)
 mg_status build_slot_map(mg_plan* p, cudaStream_t st);
 bool slot_map_aos(int order);  // element-matrix layout: element-major (true) or entry-major
 // padding source of the gather layout; the kernel maps it to the zero entry past

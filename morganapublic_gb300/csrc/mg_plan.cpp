@@ -6,10 +6,10 @@
 // (src/morganaFiniteElements/traitsMatrixBuilder.hpp:363-544 in morganaPublic).
 //
 // Element order: the assembly visits the elements along a Morton curve of their
-// centroids, so that neighbouring threads read neighbouring vertices and the
-// gather's element-matrix reads stay local.  The slot map of the gather (for
-// every diagonal or upper CSR entry, the element-matrix entries it sums) is
-// built on the GPU from the uploaded pattern (mg_schedule.cu).
+// centroids, so that neighbouring threads read neighbouring vertices and a block
+// of consecutive elements covers a compact region.  The assembly's map from
+// element-matrix entries to CSR entries -- the block map (P1) or the slot map
+// (P2) -- is built on the GPU from the uploaded pattern (mg_schedule.cu).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
