@@ -34,6 +34,8 @@
 // double-word float arithmetic on the FP32 pipes, written as IEEE doubles), kF64
 // (native FP64).  GB300 runs FP64 at ~1/60 of its FP32 rate, so MG_F64 uses kDW;
 // MG_F64_NATIVE selects kF64 (the full FP64 exponent range).
+#include <cfloat>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <mutex>
@@ -1300,7 +1302,7 @@ __global__ void __launch_bounds__(256) k_adjoint(int64_t n_elem, const int32_t* 
 template <int ORDER>
 __global__ void __launch_bounds__(256) k_rhs_elem(int64_t n_elem, const int32_t* elem_order, const int32_t* dofs_m,
                                                   const float2* gdet, const double* mass, const double* field,
-                                                  const double* scale, double* y)
+                                                  const double* scale, double* y, int two_valued)
 {
   constexpr int NB = ORDER == 1 ? 4 : 10, NU = ORDER == 1 ? 10 : 55;
   __shared__ ff tab[NU];
@@ -1342,12 +1344,24 @@ __global__ void __launch_bounds__(256) k_rhs_elem(int64_t n_elem, const int32_t*
     ff fr[NB];
 #pragma unroll
     for (int k = 0; k < NB; ++k) fr[k] = ff_rescaled(f[k], ef);
+    if (ORDER == 1 && two_valued) {
+      // M^_lk = o + (d - o) [l = k]: (M^ f)_l = o sum_k f_k + (d - o) f_l, with
+      // d = tab(0,0) and o = tab(0,1) from the table
+      const ff o = tab[1], dmo = tab[0] - tab[1];
+      ff sf = fr[0];
 #pragma unroll
-    for (int l = 0; l < NB; ++l) {
-      ff a = tab[sym_index(l, 0, NB)] * fr[0];
+      for (int k = 1; k < NB; ++k) sf = sf + fr[k];
+      const ff base = o * sf;
 #pragma unroll
-      for (int k = 1; k < NB; ++k) a = a + tab[sym_index(l, k, NB)] * fr[k];
-      v[l] = a * sdet;
+      for (int l = 0; l < NB; ++l) v[l] = (base + dmo * fr[l]) * sdet;
+    } else {
+#pragma unroll
+      for (int l = 0; l < NB; ++l) {
+        ff a = tab[sym_index(l, 0, NB)] * fr[0];
+#pragma unroll
+        for (int k = 1; k < NB; ++k) a = a + tab[sym_index(l, k, NB)] * fr[k];
+        v[l] = a * sdet;
+      }
     }
   } else {
 #pragma unroll
@@ -1556,13 +1570,27 @@ mg_status mg_assemble_rhs(mg_plan* p, const double* d_field, const double* d_ele
   const int nu = m->nb * (m->nb + 1) / 2;
   MG_TRY(plan_geometry(p, st));
   const int eblocks = (int)((m->n_elem + threads - 1) / threads);
+  // A P1 mass table with one diagonal and one off-diagonal value (to a few ulps:
+  // every symmetric card gives (1 + [i = j]) |T^| / 20) takes the two-value form
+  // of the mat-vec in the element pass.
+  int two_valued = 0;
+  if (m->order == 1) {
+    const double d = t->mass[0], o = t->mass[1];
+    double mx = 0.0, dev = 0.0;
+    for (int i = 0; i < 4; ++i)
+      for (int j = 0; j < 4; ++j) {
+        mx = std::max(mx, std::fabs(t->mass[4 * i + j]));
+        dev = std::max(dev, std::fabs(t->mass[4 * i + j] - (i == j ? d : o)));
+      }
+    two_valued = dev <= 8.0 * DBL_EPSILON * mx ? 1 : 0;
+  }
   if (eblocks > 0) {
     if (m->order == 1)
       k_rhs_elem<1><<<eblocks, threads, 0, st>>>(m->n_elem, p->d_elem_order, p->d_dofs_morton, p->d_geo_det,
-                                                 d_tab + 6 * nu, d_field, d_elem_scale, p->d_rhs_y);
+                                                 d_tab + 6 * nu, d_field, d_elem_scale, p->d_rhs_y, two_valued);
     else
       k_rhs_elem<2><<<eblocks, threads, 0, st>>>(m->n_elem, p->d_elem_order, p->d_dofs_morton, p->d_geo_det,
-                                                 d_tab + 6 * nu, d_field, d_elem_scale, p->d_rhs_y);
+                                                 d_tab + 6 * nu, d_field, d_elem_scale, p->d_rhs_y, 0);
     MG_CUDA(cudaGetLastError());
   }
   // two lanes per dof when dofs sum more than 16 entries on average (P1: ~24),
