@@ -228,3 +228,15 @@ def test_block_map_restatement_sums_to_oracle(elems_per_block):
     got = emulate_block_map(bm, order, mats, b.nnz, elems_per_block)
     assert not np.isnan(got).any()
     assert row_scaled_err(rp, ref, got) <= 1e-14
+
+
+def test_assembly_map_exports_refuse_the_other_order():
+    """P1 plans assemble through the block map, P2 plans through the slot map: each
+    export refuses the other kind with MG_ERR_UNSUPPORTED before any device work."""
+    m = meshgen.kuhn_cube(2)
+    b1 = mg.MatrixBuilder(mg.Mesh(m.xyz, m.conn, order=1))
+    b2 = mg.MatrixBuilder(mg.Mesh(m.xyz, m.conn, order=2))
+    for call in (b1.slot_map_info, b1.export_slot_map, b2.block_map_info, b2.export_block_map):
+        with pytest.raises(mg.MorganaError) as e:
+            call()
+        assert e.value.status == mg.MG_ERR_UNSUPPORTED
