@@ -708,6 +708,11 @@ def test_block_map_matches_restatement_and_oracle(n, jitter):
     assert row_scaled_err(rp, ref, got) <= 1e-14
     v = b.assemble("stiff_kappa", coeff=kappa, quad=4, prec="f64").cpu().numpy()
     assert row_scaled_err(rp, ref, v) <= F64_TOL
+    v = b.assemble("stiff_kappa", coeff=kappa, quad=4, prec="f64_native").cpu().numpy()
+    assert row_scaled_err(rp, ref, v) <= F64_TOL
+    v = b.assemble("stiff_kappa", coeff=kappa, quad=4, prec="f32").cpu().numpy()
+    assert row_scaled_err(rp, ref, v) <= F32_TOL
+    b.status()
 
 
 @pytest.mark.parametrize("case", ["star", "disjoint"])
@@ -740,6 +745,8 @@ def test_block_map_beyond_the_shared_memory_stage(case):
     assert row_scaled_err(rp, ref, v64) <= F64_TOL
     v32 = b.assemble("stiff_kappa", coeff=kappa, quad=4, prec="f32").cpu().numpy()
     assert row_scaled_err(rp, ref, v32) <= F32_TOL
+    vn = b.assemble("stiff_kappa", coeff=kappa, quad=4, prec="f64_native").cpu().numpy()
+    assert row_scaled_err(rp, ref, vn) <= F64_TOL
     _, _, _, mref = orc.full_operator("mass", 1, 4, xyz, conn)
     vm = b.assemble("mass", quad=4, prec="f64").cpu().numpy()
     assert row_scaled_err(rp, mref, vm) <= F64_TOL
