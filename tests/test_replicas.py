@@ -49,3 +49,17 @@ def test_reference_arm_nonzero_rank_exits_without_work():
     r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference"], env=env,
                        capture_output=True, text=True, timeout=120)
     assert r.returncode == 0 and r.stdout.strip() == ""
+
+
+def test_reference_arm_runs_the_steps_it_is_given():
+    """Rank 0 of the reference arm runs exactly the warm-up and timed steps asked,
+    each on the full mesh, and prints one JSON line in the GPU arm's metric."""
+    import json
+    env = dict(os.environ, RANK="0", WORLD_SIZE="1")
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--n", "6",
+                        "--steps", "3", "--warmup", "2"], env=env, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["steps"] == 3 and line["warmup"] == 2
+    assert line["unit"] == "tets/s" and line["value"] > 0 and line["config"]["tets"] == 6 * 6 ** 3
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["kind"] == "port"
